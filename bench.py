@@ -1,0 +1,340 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 drop-of-blood MAC fluid step.
+
+Workload (one "step" = one full fluid step of the scene, inputs resident in
+HBM): the 192x256x192 closed-box drop scene with three r=12 drops released
+at steps 0/40/80 and 393216 parcels, FP32 storage, 4 V-cycles of 2+2
+red-black sweeps on 4 grids per step (dropfluid.scenes.box192).  The
+mixed-precision variant of the same scene is measured beside it.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Multi-GPU: the step does not exchange data between replicas on this pool
+(one GPU per box): N ranks run N independent replicas ("scaling": "weak");
+rank 0 prints one JSON line with the whole-job throughput (sum over
+replicas, timed as the max over ranks).
+
+--impl reference runs the CPU restatement of the reference step (the
+oracle; the reference itself is TypeScript + WGSL for a browser's WebGPU
+and cannot run here) on the host cores, on the same scene, and prints the
+same JSON line with "impl": "reference".
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "drop-of-blood_gb300")
+ORACLE_DIR = os.path.join(ROOT, "oracle")
+for _p in (PKG, ORACLE_DIR):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "steps/s @192x256x192: mixed vs FP32 at div<1e-5; adjoint/forward step ratio"
+
+
+def rank_info():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+class Dist:
+    """Host-side barrier and max-reduction for replica timing (gloo, CPU)."""
+
+    def __init__(self, world):
+        self.world = world
+        self.pg = None
+        if world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.world > 1:
+            self.dist.barrier()
+
+    def max(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.dist.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.lines = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.t:
+            self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if parts[5 + k].lower() in ("active", "1", "yes"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs, burst copy)"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback 6.8 TB/s"
+
+
+def ncu_traffic():
+    """Per-launch DRAM bytes of the dominant kernel from the committed ncu
+    summary (profiles/roofline_traffic.json), scaled to this workload."""
+    p = os.path.join(ROOT, "profiles", "roofline_traffic.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return d
+    except (OSError, ValueError):
+        return None
+
+
+def run_scene_steps(scene, eng, start, n, timed):
+    """Advance n steps from `start`, releasing drops on schedule.  Returns
+    the device milliseconds of the step segments when `timed` (releases are
+    host calls between segments and are not timed)."""
+    total = 0.0
+    k = start
+    end = start + n
+    while k < end:
+        for d in scene.releases_at(k):
+            scene.release(eng, d)
+        nxt = end
+        for d in scene.drops:
+            if k < d.release_step < nxt:
+                nxt = d.release_step
+        seg = nxt - k
+        if timed:
+            total += eng.time_steps(seg)
+        else:
+            eng.step(seg)
+        k = nxt
+    return total
+
+
+def cpu_baseline(scene_fn, steps, threads):
+    import oracle
+    oracle.build()
+    oracle.set_threads(threads)
+    sc = scene_fn()
+    sim = oracle.OracleSim(sc.config)
+    for d in sc.releases_at(0):
+        sc.release(sim, d)
+    sim.step(1)  # warm-up
+    t0 = time.perf_counter()
+    sim.step(steps)
+    dt = time.perf_counter() - t0
+    return steps / dt, dt
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    from dropfluid import scenes
+    threads = os.cpu_count() or 1
+    steps = max(1, min(args.steps, 6))
+    t_start = time.perf_counter()
+    value, secs = cpu_baseline(scenes.box192, steps, threads)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world,
+        "steps": steps, "warmup": 1, "ms_per_step": 1000.0 / value, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "box192: 192x256x192 closed-box MAC step, 3 drops r=12, 393216 parcels, FP32, "
+                               "4 V-cycles of 2+2 RBGS on 4 grids (dropfluid.scenes.box192)",
+                   "grid": [192, 256, 192], "parallelism": "replicas"},
+        "cpu_baseline": {"value": value, "unit": "steps/s", "cores": threads, "kind": "port",
+                         "sample": f"{steps} steps of box192 after drop 0 released and 1 warm-up step "
+                                   f"({secs:.1f} s); the reference's own WGSL step needs a browser WebGPU "
+                                   f"stack, unavailable on this box"},
+        "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "wall_s": time.perf_counter() - t_start,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = rank_info()
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    if world > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    args.warmup = max(3, args.warmup)
+
+    from dropfluid import DropFluid, abi, build, scenes
+    build.build()
+    dist = Dist(world)
+
+    # ---- FP32 drop-in step (the headline) ----------------------------------------------------
+    sc = scenes.box192()
+    eng = DropFluid(sc.config)
+    run_scene_steps(sc, eng, 0, args.warmup, timed=False)
+    eng.sync()
+    clocks = ClockSampler()
+    clocks.start()
+    dist.barrier()
+    eng.sync()
+    ms = run_scene_steps(sc, eng, args.warmup, args.steps, timed=True)
+    eng.sync()
+    dist.barrier()
+    clk = clocks.stop()
+    ms_max = dist.max(ms)
+    value = world * args.steps / (ms_max / 1000.0)
+    st = eng.step(1, stats=True)
+    nstep = args.warmup + args.steps + 1
+    launches = eng.launches_per_step()
+    # per-stage device time (stage-by-stage launches with events)
+    tst = eng.step(2, timing=True)
+    stage_ms = {k: v / 2.0 for k, v in tst["stage_ms"].items() if v > 0}
+    # dominant kernel: the level-0 smoother pass, timed alone on the live state
+    k_ms, k_bytes = eng.bench_kernel(0, reps=20)
+    peak, peak_src = measured_peaks()
+    achieved = k_bytes / (k_ms * 1e-3) / 1e9
+    traffic = None
+    tr = ncu_traffic()
+    if tr and "bytes_per_cell" in tr:
+        traffic = tr["bytes_per_cell"] * sc.config.nx * sc.config.ny * sc.config.nz
+    h2d, d2h = eng.io_bytes()
+
+    # ---- end to end: public API, host uniform/params upload + stats readback every step --------
+    eng.sync()
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        eng.step(1, stats=True)
+    e2e_s = dist.max(time.perf_counter() - t0)
+    e2e_value = world * args.steps / e2e_s
+
+    # ---- mixed precision on the same scene -----------------------------------------------------
+    mixed = None
+    if not args.no_mixed:
+        eng.close()
+        scm = scenes.box192(abi.DOB_PREC_MIXED)
+        em = DropFluid(scm.config)
+        run_scene_steps(scm, em, 0, args.warmup, timed=False)
+        em.sync()
+        dist.barrier()
+        ms_m = dist.max(run_scene_steps(scm, em, args.warmup, args.steps, timed=True))
+        stm = em.step(1, stats=True)
+        mixed = {"value": world * args.steps / (ms_m / 1000.0), "unit": "steps/s",
+                 "speedup_vs_fp32": (world * args.steps / (ms_m / 1000.0)) / value,
+                 "max_div": stm["max_div"], "outer_iters": stm["outer_iters"],
+                 "rel_residual": stm["residual_l2"] / max(stm["rhs_l2"], 1e-300),
+                 "precision": "FP16 dye, BF16 correction levels, FP64 defect residual, FP32 compute"}
+        em.close()
+
+    # ---- CPU baseline (rank 0, N=1 only) ----------------------------------------------------------
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        cval, csecs = cpu_baseline(scenes.box192, 3, threads)
+        cpu = {"value": cval, "unit": "steps/s", "cores": threads, "kind": "port",
+               "sample": f"3 steps of box192 (FP32 oracle, OpenMP on {threads} threads) after drop 0 "
+                         f"and 1 warm-up step: {csecs:.1f} s"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "box192: 192x256x192 closed-box MAC step, 3 drops r=12 released at "
+                                   "steps 0/40/80, 393216 parcels, FP32 storage, 4 V-cycles of 2+2 RBGS on "
+                                   "4 grids, Casson tau_y=0.005 mu_p=1e-3, dx=1 dt=0.02",
+                       "grid": [192, 256, 192], "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "inputs larger than L2 (>=12 fields x 37.7 MB per step), no flush",
+                       "timed": "device time of K graph-replayed steps (CUDA events on the library stream); "
+                                "drop releases between segments untimed"},
+            "cell_updates_per_s": value * 192 * 256 * 192,
+            "max_div": st["max_div"], "residual_l2": st["residual_l2"], "rhs_l2": st["rhs_l2"],
+            "mixed": mixed,
+            "adjoint_forward_ratio": None,
+            "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "path": "DropFluid.step(1, stats=True) per step: params host->device, step graph, "
+                            "statistics device->host, synchronize"},
+            "gpu_launches": launches * args.steps,
+            "launches_per_step": launches,
+            "stage_ms": stage_ms,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "kernel": "level-0 RBGS smoother pass (red + black sweep of p), timed alone on the live "
+                                   "state with CUDA events, 20 launches",
+                         "algorithmic_bytes_per_launch": k_bytes, "avg_launch_ms": k_ms, "peak_source": peak_src},
+            "clocks": clk,
+            "cpu_baseline": cpu,
+            "steps_total": nstep,
+        }
+        print(json.dumps(line), flush=True)
+    dist.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

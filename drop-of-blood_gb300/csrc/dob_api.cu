@@ -1,0 +1,837 @@
+// dob_api.cu — the C ABI (include/dropfluid.h): context lifetime, device
+// memory, host<->device field I/O, step orchestration on one CUDA stream
+// with captured CUDA graphs, statistics and timing.
+//
+// A step is the reference's encodePhysicsStep (BloodDropEngine.ts:1855-2111)
+// minus the wave and lighting passes: advect -> centre -> [curl] -> Casson/
+// forces -> divergence -> V-cycles -> project -> centre -> clear splats ->
+// parcel emit -> parcel advect/splat -> dye predict -> dye resolve.  The
+// stage sequence is captured once into a CUDA graph per dye ping-pong parity
+// and replayed; the per-step parameters reach the device by one 600-byte
+// copy from a pinned ring before each replay.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <string>
+#include <vector>
+
+#include "dob_kernels.cuh"
+
+using namespace dob;
+
+namespace {
+
+constexpr int kParamRing = 16;
+constexpr int kSnapshots = 8;
+
+struct Snapshot {
+  std::vector<void*> bufs;
+  std::vector<size_t> sizes;
+  uint32_t high_water = 0;
+  int step_index = 0;
+  bool valid = false;
+};
+
+}  // namespace
+
+struct dob_ctx {
+  dob_config cfg;
+  DevState s;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  float U[128];
+  StepParams* host_params = nullptr;  // pinned ring
+  cudaEvent_t param_ev[kParamRing];
+  int param_slot = 0;
+  uint32_t high_water = 0;
+  int step_index = 0;
+  std::vector<void*> allocs;
+  uint64_t bytes = 0;
+  cudaGraphExec_t graph[4] = {nullptr, nullptr, nullptr, nullptr};
+  void* graph_conc[4] = {nullptr, nullptr, nullptr, nullptr};  // conc pointer each graph was captured with
+  int kernels_per_step = 0;
+  Snapshot snaps[kSnapshots];
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t stage_ev[DOB_STAGE_COUNT + 1];
+};
+
+static const char* g_static_err = "no error";
+
+#define CK(call)                                                               \
+  do {                                                                         \
+    cudaError_t e_ = (call);                                                   \
+    if (e_ != cudaSuccess) return fail(ctx, DOB_ECUDA, #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+static dob_status fail(dob_ctx* ctx, dob_status st, const char* what, const char* detail) {
+  if (ctx) {
+    ctx->err = std::string(what) + ": " + (detail ? detail : "");
+  } else {
+    static thread_local std::string msg;
+    msg = std::string(what) + ": " + (detail ? detail : "");
+    g_static_err = msg.c_str();
+  }
+  return st;
+}
+
+static size_t vs_bytes(int prec) { return prec == DOB_PREC_REFERENCE_FP16 ? 2 : 4; }
+static size_t ds_bytes(int prec) { return prec == DOB_PREC_FP32 ? 4 : 2; }
+
+static bool valid_config(const dob_config* c, std::string* why) {
+  auto no = [&](const char* m) { *why = m; return false; };
+  if (!c) return no("null config");
+  if (c->struct_size != sizeof(dob_config)) return no("struct_size mismatch");
+  if (c->nx < 4 || c->ny < 4 || c->nz < 4) return no("grid dims must be >= 4");
+  if (c->nx > 2048 || c->ny > 2048 || c->nz > 2048) return no("grid dims must be <= 2048");
+  if (c->nx % 2 || c->ny % 2 || c->nz % 2) return no("grid dims must be even");
+  if (c->dye_refine != 1 && c->dye_refine != 2) return no("dye_refine must be 1 or 2");
+  if (c->mg_levels < 1 || c->mg_levels > kMaxLevels) return no("mg_levels out of range");
+  const uint32_t m = 1u << (c->mg_levels - 1);
+  if (c->nx % m || c->ny % m || c->nz % m) return no("dims not divisible by 2^(mg_levels-1)");
+  if ((c->nx >> (c->mg_levels - 1)) < 2 || (c->ny >> (c->mg_levels - 1)) < 2 || (c->nz >> (c->mg_levels - 1)) < 2)
+    return no("coarsest grid smaller than 2");
+  if (c->bc_mode != DOB_BC_REFERENCE && c->bc_mode != DOB_BC_CLOSED_BOX) return no("bad bc_mode");
+  if (c->precision_mode < 0 || c->precision_mode > 2) return no("bad precision_mode");
+  if (c->mg_pre < 0 || c->mg_post < 0 || c->mg_coarse_sweeps < 0 || c->mg_cycles < 0) return no("negative sweeps");
+  if (c->precision_mode == DOB_PREC_MIXED && (c->mg_max_outer < 1 || c->mg_max_outer > 32)) return no("mg_max_outer must be 1..32");
+  if (c->parcel_capacity < 1 || c->parcel_capacity > (1u << 26)) return no("parcel_capacity out of range");
+  if (c->bc_mode == DOB_BC_CLOSED_BOX) {
+    if (!(c->dt > 0.0f) || !isfinite(c->dt)) return no("dt must be finite and > 0");
+    if (!(c->dx > 0.0f) || !isfinite(c->dx)) return no("dx must be finite and > 0");
+    for (int k = 0; k < 3; ++k)
+      if (!(c->domain_max[k] > c->domain_min[k])) return no("empty domain");
+  }
+  return true;
+}
+
+static void default_uniforms(float* U) {
+  memset(U, 0, 128 * sizeof(float));
+  U[36] = 1.0f; U[37] = 1.0f; U[38] = 1.0f / 60.0f;
+  U[40] = 0.30f; U[41] = 1.0f; U[43] = 1.0f;
+  U[44] = 1.02f; U[45] = 0.48f; U[46] = 0.9993f; U[47] = 0.995f;
+  U[48] = 1.0f; U[49] = 1.0f; U[50] = 1.0f;
+  U[52] = 0.48f; U[53] = -0.98f; U[54] = 0.30f; U[55] = 1.10f;
+  U[57] = 0.0032f; U[58] = 1.0f; U[59] = 0.088f;
+  U[60] = 0.032f; U[63] = 0.028f;
+}
+
+static dob_status dev_alloc(dob_ctx* ctx, void** p, size_t bytes) {
+  *p = nullptr;
+  if (bytes == 0) return DOB_OK;
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(ctx, DOB_ENOMEM, "cudaMalloc", cudaGetErrorString(e));
+  }
+  ctx->allocs.push_back(*p);
+  ctx->bytes += bytes;
+  return DOB_OK;
+}
+
+// Fill the step parameters for the next step (host) from the uniform block or
+// the closed-box configuration.
+static void fill_params(dob_ctx* ctx, StepParams* P, uint32_t spawn) {
+  const dob_config& c = ctx->cfg;
+  memcpy(P->U, ctx->U, sizeof(P->U));
+  if (c.bc_mode == DOB_BC_REFERENCE) {
+    const float dtr = ctx->U[38];
+    P->dt = dob_clampf(dtr, 0.0f, 0.025f);
+    P->dmin[0] = -ctx->U[52]; P->dmin[1] = ctx->U[53]; P->dmin[2] = -ctx->U[52];
+    P->dmax[0] = ctx->U[52]; P->dmax[1] = ctx->U[54]; P->dmax[2] = ctx->U[52];
+    P->damp = ctx->U[46];
+    P->sharp = ctx->U[47];
+  } else {
+    P->dt = c.dt;
+    for (int k = 0; k < 3; ++k) { P->dmin[k] = c.domain_min[k]; P->dmax[k] = c.domain_max[k]; }
+    P->damp = c.vel_damping;
+    P->sharp = c.dye_sharpness;
+  }
+  for (int k = 0; k < 3; ++k) P->dsize[k] = P->dmax[k] - P->dmin[k];
+  P->tau_y = c.casson_tau_y;
+  P->mu_p = c.casson_mu_p;
+  P->dx = c.dx;
+  P->spawn_count = spawn;
+  const float cur = ctx->U[61] > 0.0f ? ctx->U[61] : 0.0f;
+  P->cursor = (uint32_t)cur;
+  P->high_water = ctx->high_water;
+  const uint64_t hw = ((uint64_t)ctx->high_water + 255u) / 256u * 256u;
+  P->advect_count = (uint32_t)(hw < ctx->s.cap ? hw : ctx->s.cap);
+  P->step_index = ctx->step_index;
+}
+
+static uint32_t spawn_count(const dob_ctx* ctx) {
+  if (ctx->cfg.bc_mode != DOB_BC_REFERENCE) return 0u;
+  const float sc = ctx->U[62] > 0.0f ? ctx->U[62] : 0.0f;
+  uint32_t n = (uint32_t)sc;
+  if (n > 8192u) n = 8192u;  // the emit dispatch covers at most 8192 parcels (BloodDropEngine.ts:1835)
+  return n > ctx->s.cap ? ctx->s.cap : n;
+}
+
+// Copy the step parameters to the device (pinned ring slot + event guard).
+static dob_status upload_params(dob_ctx* ctx, uint32_t spawn) {
+  const int k = ctx->param_slot;
+  ctx->param_slot = (k + 1) % kParamRing;
+  CK(cudaEventSynchronize(ctx->param_ev[k]));
+  fill_params(ctx, &ctx->host_params[k], spawn);
+  CK(cudaMemcpyAsync(ctx->s.params, &ctx->host_params[k], sizeof(StepParams), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaEventRecord(ctx->param_ev[k], ctx->stream));
+  return DOB_OK;
+}
+
+static void swap_vel(DevState& s) {
+  std::swap(s.u, s.u2);
+  std::swap(s.v, s.v2);
+  std::swap(s.w, s.w2);
+}
+
+// Enqueue one stage on the context's stream, updating the ping-pong state.
+static void enqueue_stage(dob_ctx* ctx, DevState& s, int stage, cudaStream_t st) {
+  const size_t nc = s.gc.n();
+  switch (stage) {
+    case DOB_STAGE_ADVECT_MAC: launch_advect_mac(s, st); swap_vel(s); break;
+    case DOB_STAGE_MAC_TO_CENTER: launch_mac_to_center(s, st); break;
+    case DOB_STAGE_CURL: if (s.curl) launch_curl(s, st); break;
+    case DOB_STAGE_CASSON_FORCES: launch_casson(s, st); swap_vel(s); break;
+    case DOB_STAGE_MAC_RHS: launch_mac_rhs(s, st); break;
+    case DOB_STAGE_PRESSURE_SOLVE: launch_pressure_solve(s, st); break;
+    case DOB_STAGE_PROJECT: launch_project(s, st); break;
+    case DOB_STAGE_CLEAR_SPLATS:
+      cudaMemsetAsync(s.splatI, 0, nc * 4, st);
+      cudaMemsetAsync(s.splatL, 0, nc * 4, st);
+      break;
+    case DOB_STAGE_PARCEL_EMIT: launch_parcel_emit(s, st); break;
+    case DOB_STAGE_PARCEL_ADVECT: launch_parcel_advect(s, st); break;
+    case DOB_STAGE_CONC_PREDICT: launch_conc_predict(s, st); break;
+    case DOB_STAGE_CONC_RESOLVE: launch_conc_resolve(s, st); std::swap(s.conc, s.conc2); break;
+    default: break;
+  }
+  (void)ctx;
+}
+
+static const int kStepOrder[] = {
+    DOB_STAGE_ADVECT_MAC, DOB_STAGE_MAC_TO_CENTER, DOB_STAGE_CURL,          DOB_STAGE_CASSON_FORCES,
+    DOB_STAGE_MAC_RHS,    DOB_STAGE_PRESSURE_SOLVE, DOB_STAGE_PROJECT,      DOB_STAGE_MAC_TO_CENTER,
+    DOB_STAGE_CLEAR_SPLATS, DOB_STAGE_PARCEL_EMIT, DOB_STAGE_PARCEL_ADVECT, DOB_STAGE_CONC_PREDICT,
+    DOB_STAGE_CONC_RESOLVE};
+
+static void enqueue_step_body(dob_ctx* ctx, DevState& s, cudaStream_t st, float* stage_ms, bool stats_div) {
+  const int n = (int)(sizeof(kStepOrder) / sizeof(kStepOrder[0]));
+  for (int k = 0; k < n; ++k) {
+    const int stage = kStepOrder[k];
+    if (stage == DOB_STAGE_CURL && !(s.ref && (s.flags & DOB_PHYS_VORT_CONF))) continue;
+    if (stage_ms) cudaEventRecord(ctx->stage_ev[0], st);
+    enqueue_stage(ctx, s, stage, st);
+    if (stage_ms) {
+      cudaEventRecord(ctx->stage_ev[1], st);
+      cudaEventSynchronize(ctx->stage_ev[1]);
+      float ms = 0.0f;
+      cudaEventElapsedTime(&ms, ctx->stage_ev[0], ctx->stage_ev[1]);
+      stage_ms[stage] += ms;
+    }
+    if (stats_div && stage == DOB_STAGE_MAC_RHS) {
+      cudaMemsetAsync(s.red + RED_RHS_NORM2, 0, sizeof(double), st);
+      launch_sumsq(s.rhs, s.g.n(), s.red + RED_RHS_NORM2, s.num_sms, st);
+    }
+    if (stats_div && stage == DOB_STAGE_PRESSURE_SOLVE) {
+      launch_residual_norm(s, s.red + RED_RES_NORM2, st);
+    }
+    if (stats_div && stage == DOB_STAGE_PROJECT) {
+      const float scale = s.ref ? 1.0f : ctx->cfg.dt / ctx->cfg.dx;
+      cudaMemsetAsync(s.redu + REDU_MAXDIV, 0, sizeof(unsigned int), st);
+      launch_divergence(s, nullptr, scale, s.redu + REDU_MAXDIV, st);
+    }
+  }
+}
+
+// Graphs are cached per (dye ping-pong parity, statistics on/off).
+static dob_status get_graph(dob_ctx* ctx, bool stats, cudaGraphExec_t* out) {
+  const int base = stats ? 2 : 0;
+  for (int k = base; k < base + 2; ++k) {
+    if (ctx->graph[k] && ctx->graph_conc[k] == ctx->s.conc) {
+      *out = ctx->graph[k];
+      return DOB_OK;
+    }
+  }
+  const int slot = ctx->graph[base] ? base + 1 : base;
+  DevState s = ctx->s;
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  enqueue_step_body(ctx, s, ctx->stream, nullptr, stats);
+  cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+  if (e != cudaSuccess) return fail(ctx, DOB_ECUDA, "cudaStreamEndCapture", cudaGetErrorString(e));
+  size_t nn = 0;
+  cudaGraphGetNodes(g, nullptr, &nn);
+  std::vector<cudaGraphNode_t> nodes(nn);
+  if (nn) cudaGraphGetNodes(g, nodes.data(), &nn);
+  int kernels = 0;
+  for (size_t k = 0; k < nn; ++k) {
+    cudaGraphNodeType t;
+    if (cudaGraphNodeGetType(nodes[k], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++kernels;
+  }
+  if (!stats) ctx->kernels_per_step = kernels;
+  cudaGraphExec_t ex = nullptr;
+  e = cudaGraphInstantiate(&ex, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return fail(ctx, DOB_ECUDA, "cudaGraphInstantiate", cudaGetErrorString(e));
+  ctx->graph[slot] = ex;
+  ctx->graph_conc[slot] = ctx->s.conc;
+  *out = ex;
+  return DOB_OK;
+}
+
+static void drop_graphs(dob_ctx* ctx) {
+  for (int k = 0; k < 4; ++k) {
+    if (ctx->graph[k]) cudaGraphExecDestroy(ctx->graph[k]);
+    ctx->graph[k] = nullptr;
+    ctx->graph_conc[k] = nullptr;
+  }
+}
+
+static dob_status one_step(dob_ctx* ctx, uint32_t flags, float* stage_ms) {
+  const uint32_t spawn = spawn_count(ctx);
+  if (ctx->cfg.bc_mode == DOB_BC_REFERENCE) {  // BloodDropEngine.ts:1832-1840
+    const uint64_t hw = (uint64_t)ctx->high_water + spawn;
+    ctx->high_water = (uint32_t)(hw < ctx->s.cap ? hw : ctx->s.cap);
+  }
+  dob_status st = upload_params(ctx, spawn);
+  if (st != DOB_OK) return st;
+  const bool stats = (flags & DOB_STEP_STATS) != 0;
+  if (stage_ms || (flags & DOB_STEP_NO_GRAPH)) {
+    enqueue_step_body(ctx, ctx->s, ctx->stream, stage_ms, stats);
+  } else {
+    cudaGraphExec_t ex = nullptr;
+    st = get_graph(ctx, stats, &ex);
+    if (st != DOB_OK) return st;
+    CK(cudaGraphLaunch(ex, ctx->stream));
+    std::swap(ctx->s.conc, ctx->s.conc2);  // the graph's resolve wrote conc2
+  }
+  CK(cudaGetLastError());
+  ctx->step_index++;
+  return DOB_OK;
+}
+
+static dob_status finish_stats(dob_ctx* ctx, dob_step_stats* stats, int steps) {
+  if (!stats) return DOB_OK;
+  DevState& s = ctx->s;
+  double red[RED_COUNT];
+  unsigned int redu[REDU_COUNT];
+  launch_count_alive(s, s.redu + REDU_ALIVE, ctx->stream);
+  CK(cudaMemcpyAsync(red, s.red, sizeof(red), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(redu, s.redu, sizeof(redu), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  stats->struct_size = sizeof(dob_step_stats);
+  stats->steps_done = steps;
+  const int levels_cycles = ctx->cfg.mg_cycles;
+  if (ctx->cfg.precision_mode == DOB_PREC_MIXED) {
+    stats->outer_iters = (int)redu[REDU_ITERS];
+    stats->vcycles = (int)redu[REDU_ITERS] * levels_cycles;
+  } else {
+    stats->outer_iters = 0;
+    stats->vcycles = levels_cycles;
+  }
+  stats->residual_l2 = sqrt(red[RED_RES_NORM2]);
+  stats->rhs_l2 = sqrt(red[RED_RHS_NORM2]);
+  float md;
+  memcpy(&md, &redu[REDU_MAXDIV], 4);
+  stats->max_div = (double)md;
+  stats->parcels_alive = redu[REDU_ALIVE];
+  return DOB_OK;
+}
+
+extern "C" {
+
+int dob_abi_version(void) { return DOB_ABI_VERSION; }
+
+const char* dob_last_error(const dob_ctx* ctx) { return ctx ? ctx->err.c_str() : g_static_err; }
+
+dob_status dob_config_reference(dob_config* c) {
+  if (!c) return DOB_EINVAL;
+  memset(c, 0, sizeof(*c));
+  c->struct_size = sizeof(dob_config);
+  c->nx = 96; c->ny = 128; c->nz = 96;
+  c->dye_refine = 2;
+  c->dx = 0.01f;
+  c->dt = 1.0f / 60.0f;
+  c->domain_min[0] = -0.48f; c->domain_min[1] = -0.98f; c->domain_min[2] = -0.48f;
+  c->domain_max[0] = 0.48f; c->domain_max[1] = 0.30f; c->domain_max[2] = 0.48f;
+  c->bc_mode = DOB_BC_REFERENCE;
+  c->precision_mode = DOB_PREC_FP32;
+  c->mg_levels = 4; c->mg_pre = 2; c->mg_post = 2; c->mg_coarse_sweeps = 6; c->mg_cycles = 1;
+  c->mg_max_outer = 1; c->mg_rel_tol = 0.0;
+  c->physics_flags = DOB_PHYS_REFERENCE_ALL;
+  c->parcel_capacity = 393216;
+  c->reference_schedule = 1;
+  c->vel_damping = 1.0f;
+  c->dye_sharpness = 1.0f;
+  return DOB_OK;
+}
+
+dob_status dob_config_closed_box(dob_config* c, uint32_t nx, uint32_t ny, uint32_t nz) {
+  if (!c) return DOB_EINVAL;
+  memset(c, 0, sizeof(*c));
+  c->struct_size = sizeof(dob_config);
+  c->nx = nx; c->ny = ny; c->nz = nz;
+  c->dye_refine = 1;
+  c->dx = 1.0f;
+  c->dt = 0.02f;
+  c->domain_max[0] = (float)nx; c->domain_max[1] = (float)ny; c->domain_max[2] = (float)nz;
+  c->bc_mode = DOB_BC_CLOSED_BOX;
+  c->precision_mode = DOB_PREC_FP32;
+  c->mg_levels = 4; c->mg_pre = 2; c->mg_post = 2; c->mg_coarse_sweeps = 16; c->mg_cycles = 4;
+  c->mg_max_outer = 8; c->mg_rel_tol = 1e-8;
+  c->casson_tau_y = 0.005f; c->casson_mu_p = 1e-3f;
+  c->physics_flags = 0;
+  c->parcel_capacity = 8192;
+  c->reference_schedule = 0;
+  c->vel_damping = 1.0f;
+  c->dye_sharpness = 1.0f;
+  return DOB_OK;
+}
+
+dob_status dob_create(const dob_config* cfg, dob_ctx** out) {
+  if (!out) return fail(nullptr, DOB_EINVAL, "dob_create", "null out pointer");
+  *out = nullptr;
+  std::string why;
+  if (!valid_config(cfg, &why)) return fail(nullptr, DOB_EINVAL, "dob_create", why.c_str());
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return fail(nullptr, DOB_ECUDA, "dob_create", e != cudaSuccess ? cudaGetErrorString(e) : "no CUDA device");
+  }
+  dob_ctx* ctx = new dob_ctx();
+  ctx->cfg = *cfg;
+  default_uniforms(ctx->U);
+  DevState& s = ctx->s;
+  memset(&s, 0, sizeof(s));
+  CK(cudaGetDevice(&ctx->device));
+  CK(cudaDeviceGetAttribute(&s.num_sms, cudaDevAttrMultiProcessorCount, ctx->device));
+  CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+  CK(mg_prepare());
+  s.g = Grid{(int)cfg->nx, (int)cfg->ny, (int)cfg->nz};
+  s.gc = Grid{(int)(cfg->nx * cfg->dye_refine), (int)(cfg->ny * cfg->dye_refine), (int)(cfg->nz * cfg->dye_refine)};
+  s.prec = cfg->precision_mode;
+  s.ref = cfg->bc_mode == DOB_BC_REFERENCE;
+  s.flags = s.ref ? cfg->physics_flags : 0;
+  s.cap = cfg->parcel_capacity;
+  const size_t N = s.g.n(), Nc = s.gc.n();
+  const size_t vsb = vs_bytes(s.prec), dsb = ds_bytes(s.prec);
+  dob_status st = DOB_OK;
+  auto A = [&](void** p, size_t b) { if (st == DOB_OK) st = dev_alloc(ctx, p, b); };
+  A((void**)&s.params, sizeof(StepParams));
+  A(&s.u, N * vsb); A(&s.v, N * vsb); A(&s.w, N * vsb);
+  A(&s.u2, N * vsb); A(&s.v2, N * vsb); A(&s.w2, N * vsb);
+  A(&s.cen, N * 4 * vsb);
+  if (s.ref) A(&s.curl, N * 4 * vsb);
+  A((void**)&s.p, N * 4); A((void**)&s.rhs, N * 4);
+  const int nch = s.ref ? 4 : 1;
+  A(&s.conc, Nc * nch * dsb); A(&s.conc2, Nc * nch * dsb); A(&s.pred, Nc * dsb);
+  A((void**)&s.splatI, Nc * 4); A((void**)&s.splatL, Nc * 4);
+  A((void**)&s.wave, (size_t)kWaveN * kWaveN * 16);
+  A((void**)&s.parcels, (size_t)s.cap * 32);
+  A((void**)&s.red, RED_COUNT * sizeof(double));
+  A((void**)&s.redu, REDU_COUNT * sizeof(unsigned int));
+  s.nlev = cfg->mg_levels;
+  for (int l = 0; l < s.nlev; ++l) {
+    MgLevel& L = s.lv[l];
+    L.d = Grid{s.g.nx >> l, s.g.ny >> l, s.g.nz >> l};
+    const float sc = (float)s.g.nx / (float)L.d.nx;
+    L.h2 = sc * sc;
+    if (l == 0) { L.e = s.p; L.b = s.rhs; continue; }
+    if (s.prec == DOB_PREC_MIXED) {
+      A((void**)&L.eh, L.d.n() * 2); A((void**)&L.bh, L.d.n() * 2);
+    } else {
+      A((void**)&L.e, L.d.n() * 4); A((void**)&L.b, L.d.n() * 4);
+    }
+  }
+  if (s.prec == DOB_PREC_MIXED) {
+    A((void**)&s.e0h, N * 2); A((void**)&s.r0h, N * 2);
+    s.lv[0].eh = s.e0h; s.lv[0].bh = s.r0h;
+  }
+  s.pre0 = cfg->reference_schedule ? 1 : cfg->mg_pre;
+  s.post0 = cfg->reference_schedule ? 1 : cfg->mg_post;
+  s.pre = cfg->mg_pre; s.post = cfg->mg_post;
+  s.coarse_sweeps = cfg->mg_coarse_sweeps;
+  s.cycles = cfg->mg_cycles;
+  s.max_outer = cfg->mg_max_outer;
+  s.rel_tol = cfg->mg_rel_tol;
+  if (st != DOB_OK) {
+    *out = nullptr;
+    std::string keep = ctx->err;
+    dob_destroy(ctx);
+    return fail(nullptr, st, "dob_create", keep.c_str());
+  }
+  cudaError_t eh = cudaMallocHost((void**)&ctx->host_params, sizeof(StepParams) * kParamRing);
+  if (eh != cudaSuccess) {
+    dob_destroy(ctx);
+    return fail(nullptr, DOB_ENOMEM, "cudaMallocHost", cudaGetErrorString(eh));
+  }
+  for (int k = 0; k < kParamRing; ++k) CK(cudaEventCreateWithFlags(&ctx->param_ev[k], cudaEventDisableTiming));
+  CK(cudaEventCreate(&ctx->ev0));
+  CK(cudaEventCreate(&ctx->ev1));
+  for (int k = 0; k <= DOB_STAGE_COUNT; ++k) CK(cudaEventCreate(&ctx->stage_ev[k]));
+  CK(cudaMemsetAsync(s.wave, 0, (size_t)kWaveN * kWaveN * 16, ctx->stream));
+  dob_status r = dob_reset(ctx);
+  if (r != DOB_OK) {
+    std::string keep = ctx->err;
+    dob_destroy(ctx);
+    return fail(nullptr, r, "dob_create/reset", keep.c_str());
+  }
+  *out = ctx;
+  return DOB_OK;
+}
+
+void dob_destroy(dob_ctx* ctx) {
+  if (!ctx) return;
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  drop_graphs(ctx);
+  for (auto& sn : ctx->snaps)
+    for (void* p : sn.bufs) cudaFree(p);
+  for (void* p : ctx->allocs) cudaFree(p);
+  if (ctx->host_params) cudaFreeHost(ctx->host_params);
+  for (int k = 0; k < kParamRing; ++k)
+    if (ctx->param_ev[k]) cudaEventDestroy(ctx->param_ev[k]);
+  if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+  if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  for (int k = 0; k <= DOB_STAGE_COUNT; ++k)
+    if (ctx->stage_ev[k]) cudaEventDestroy(ctx->stage_ev[k]);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+dob_status dob_reset(dob_ctx* ctx) {
+  if (!ctx) return DOB_EINVAL;
+  DevState& s = ctx->s;
+  const size_t N = s.g.n(), Nc = s.gc.n();
+  const size_t vsb = vs_bytes(s.prec), dsb = ds_bytes(s.prec);
+  const int nch = s.ref ? 4 : 1;
+  ctx->high_water = 0;
+  ctx->step_index = 0;
+  dob_status st = upload_params(ctx, 0);
+  if (st != DOB_OK) return st;
+  for (void* p : {s.u, s.v, s.w, s.u2, s.v2, s.w2}) CK(cudaMemsetAsync(p, 0, N * vsb, ctx->stream));
+  CK(cudaMemsetAsync(s.cen, 0, N * 4 * vsb, ctx->stream));
+  if (s.curl) CK(cudaMemsetAsync(s.curl, 0, N * 4 * vsb, ctx->stream));
+  if (s.ref) launch_init_vel(s, ctx->stream);
+  CK(cudaMemsetAsync(s.p, 0, N * 4, ctx->stream));
+  CK(cudaMemsetAsync(s.rhs, 0, N * 4, ctx->stream));
+  for (int l = 1; l < s.nlev; ++l) {
+    const size_t n = s.lv[l].d.n();
+    if (s.lv[l].e) CK(cudaMemsetAsync(s.lv[l].e, 0, n * 4, ctx->stream));
+    if (s.lv[l].b) CK(cudaMemsetAsync(s.lv[l].b, 0, n * 4, ctx->stream));
+    if (s.lv[l].eh) CK(cudaMemsetAsync(s.lv[l].eh, 0, n * 2, ctx->stream));
+    if (s.lv[l].bh) CK(cudaMemsetAsync(s.lv[l].bh, 0, n * 2, ctx->stream));
+  }
+  if (s.e0h) CK(cudaMemsetAsync(s.e0h, 0, N * 2, ctx->stream));
+  if (s.r0h) CK(cudaMemsetAsync(s.r0h, 0, N * 2, ctx->stream));
+  CK(cudaMemsetAsync(s.conc, 0, Nc * nch * dsb, ctx->stream));
+  CK(cudaMemsetAsync(s.conc2, 0, Nc * nch * dsb, ctx->stream));
+  CK(cudaMemsetAsync(s.pred, 0, Nc * dsb, ctx->stream));
+  CK(cudaMemsetAsync(s.splatI, 0, Nc * 4, ctx->stream));
+  CK(cudaMemsetAsync(s.splatL, 0, Nc * 4, ctx->stream));
+  // PARTICLE_RESET (particles.ts:27-45): posAndMass = 0, stretchAndLysis = (0, -0.003, 0, 0)
+  std::vector<float> empty((size_t)s.cap * 8, 0.0f);
+  for (uint32_t k = 0; k < s.cap; ++k) empty[(size_t)k * 8 + 5] = -0.003f;
+  CK(cudaMemcpy(s.parcels, empty.data(), empty.size() * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemsetAsync(s.red, 0, RED_COUNT * sizeof(double), ctx->stream));
+  CK(cudaMemsetAsync(s.redu, 0, REDU_COUNT * sizeof(unsigned int), ctx->stream));
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  return DOB_OK;
+}
+
+dob_status dob_set_uniforms(dob_ctx* ctx, const float* u) {
+  if (!ctx || !u) return DOB_EINVAL;
+  for (int k = 0; k < 128; ++k)
+    if (!isfinite(u[k])) return fail(ctx, DOB_EINVAL, "dob_set_uniforms", "non-finite value in the uniform block");
+  memcpy(ctx->U, u, sizeof(ctx->U));
+  return DOB_OK;
+}
+
+dob_status dob_inject_sphere(dob_ctx* ctx, const float c[3], float r, float dye, const float vel[3], float sigma,
+                             uint64_t seed) {
+  if (!ctx || !c || !vel) return DOB_EINVAL;
+  if (ctx->cfg.bc_mode != DOB_BC_CLOSED_BOX)
+    return fail(ctx, DOB_ESTATE, "dob_inject_sphere", "sphere injection is a closed-box operation");
+  if (!(r > 0.0f) || !isfinite(r) || !isfinite(dye) || !isfinite(sigma))
+    return fail(ctx, DOB_EINVAL, "dob_inject_sphere", "bad radius/dye/sigma");
+  dob_status st = upload_params(ctx, 0);
+  if (st != DOB_OK) return st;
+  launch_inject_sphere(ctx->s, c, r, dye, vel, sigma, seed, ctx->stream);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  return DOB_OK;
+}
+
+dob_status dob_set_parcels(dob_ctx* ctx, const float* p, uint32_t n, uint32_t off) {
+  if (!ctx || (!p && n)) return DOB_EINVAL;
+  if ((uint64_t)off + n > ctx->s.cap) return fail(ctx, DOB_EINVAL, "dob_set_parcels", "range exceeds capacity");
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaMemcpy(ctx->s.parcels + (size_t)off * 8, p, (size_t)n * 32, cudaMemcpyHostToDevice));
+  if (off + n > ctx->high_water) ctx->high_water = off + n;
+  return DOB_OK;
+}
+
+dob_status dob_get_parcels(dob_ctx* ctx, float* p, uint32_t n, uint32_t off) {
+  if (!ctx || (!p && n)) return DOB_EINVAL;
+  if ((uint64_t)off + n > ctx->s.cap) return fail(ctx, DOB_EINVAL, "dob_get_parcels", "range exceeds capacity");
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaMemcpy(p, ctx->s.parcels + (size_t)off * 8, (size_t)n * 32, cudaMemcpyDeviceToHost));
+  return DOB_OK;
+}
+
+dob_status dob_set_high_water(dob_ctx* ctx, uint32_t hw) {
+  if (!ctx) return DOB_EINVAL;
+  ctx->high_water = hw < ctx->s.cap ? hw : ctx->s.cap;
+  return DOB_OK;
+}
+
+// ---- field I/O -----------------------------------------------------------------------
+namespace {
+struct FieldDesc {
+  void* dev;
+  size_t count;     // host elements
+  int kind;         // 0: VS, 1: DS, 2: f32, 3: u32
+};
+}  // namespace
+
+static bool field_desc(dob_ctx* ctx, int field, FieldDesc* f) {
+  DevState& s = ctx->s;
+  const size_t N = s.g.n(), Nc = s.gc.n();
+  switch (field) {
+    case DOB_FIELD_VEL_U: *f = {s.u, N, 0}; return true;
+    case DOB_FIELD_VEL_V: *f = {s.v, N, 0}; return true;
+    case DOB_FIELD_VEL_W: *f = {s.w, N, 0}; return true;
+    case DOB_FIELD_VEL_CENTER: *f = {s.cen, 4 * N, 0}; return true;
+    case DOB_FIELD_CURL: *f = {s.curl, 4 * N, 0}; return s.curl != nullptr;
+    case DOB_FIELD_PRESSURE: *f = {s.p, N, 2}; return true;
+    case DOB_FIELD_RHS: *f = {s.rhs, N, 2}; return true;
+    case DOB_FIELD_CONC: *f = {s.conc, (s.ref ? 4 : 1) * Nc, 1}; return true;
+    case DOB_FIELD_CONC_PRED: *f = {s.pred, Nc, 1}; return true;
+    case DOB_FIELD_SPLAT_INTACT: *f = {s.splatI, Nc, 3}; return true;
+    case DOB_FIELD_SPLAT_LYSED: *f = {s.splatL, Nc, 3}; return true;
+    case DOB_FIELD_WAVE: *f = {s.wave, (size_t)4 * kWaveN * kWaveN, 2}; return true;
+    default: return false;
+  }
+}
+
+dob_status dob_set_field(dob_ctx* ctx, int field, const void* host, size_t bytes) {
+  if (!ctx || !host) return DOB_EINVAL;
+  FieldDesc f;
+  if (!field_desc(ctx, field, &f)) return fail(ctx, DOB_EINVAL, "dob_set_field", "unknown or read-only field");
+  if (bytes != f.count * 4) return fail(ctx, DOB_EINVAL, "dob_set_field", "byte count does not match the field");
+  CK(cudaStreamSynchronize(ctx->stream));
+  const size_t eb = f.kind == 0 ? vs_bytes(ctx->s.prec) : f.kind == 1 ? ds_bytes(ctx->s.prec) : 4;
+  if (eb == 4) {
+    CK(cudaMemcpy(f.dev, host, bytes, cudaMemcpyHostToDevice));
+  } else {
+    std::vector<uint16_t> tmp(f.count);
+    const float* src = (const float*)host;
+    for (size_t i = 0; i < f.count; ++i) tmp[i] = dob_f32_to_f16_bits(src[i]);
+    CK(cudaMemcpy(f.dev, tmp.data(), f.count * 2, cudaMemcpyHostToDevice));
+  }
+  return DOB_OK;
+}
+
+dob_status dob_get_field(dob_ctx* ctx, int field, void* host, size_t bytes) {
+  if (!ctx || !host) return DOB_EINVAL;
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (field == DOB_FIELD_DIVERGENCE) {
+    const size_t N = ctx->s.g.n();
+    if (bytes != N * 4) return fail(ctx, DOB_EINVAL, "dob_get_field", "byte count does not match the field");
+    float* tmp = nullptr;
+    CK(cudaMalloc(&tmp, N * 4));
+    launch_divergence(ctx->s, tmp, 1.0f, nullptr, ctx->stream);
+    cudaError_t e = cudaMemcpyAsync(host, tmp, N * 4, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    cudaFree(tmp);
+    if (e != cudaSuccess) return fail(ctx, DOB_ECUDA, "dob_get_field(divergence)", cudaGetErrorString(e));
+    return DOB_OK;
+  }
+  FieldDesc f;
+  if (!field_desc(ctx, field, &f)) return fail(ctx, DOB_EINVAL, "dob_get_field", "unknown field");
+  if (bytes != f.count * 4) return fail(ctx, DOB_EINVAL, "dob_get_field", "byte count does not match the field");
+  const size_t eb = f.kind == 0 ? vs_bytes(ctx->s.prec) : f.kind == 1 ? ds_bytes(ctx->s.prec) : 4;
+  if (eb == 4) {
+    CK(cudaMemcpy(host, f.dev, bytes, cudaMemcpyDeviceToHost));
+  } else {
+    std::vector<uint16_t> tmp(f.count);
+    CK(cudaMemcpy(tmp.data(), f.dev, f.count * 2, cudaMemcpyDeviceToHost));
+    float* dst = (float*)host;
+    for (size_t i = 0; i < f.count; ++i) dst[i] = dob_f16_bits_to_f32(tmp[i]);
+  }
+  return DOB_OK;
+}
+
+// ---- stepping ----------------------------------------------------------------------------
+dob_status dob_step(dob_ctx* ctx, int nsteps, uint32_t flags, dob_step_stats* stats) {
+  if (!ctx || nsteps < 0) return DOB_EINVAL;
+  if (ctx->cfg.bc_mode == DOB_BC_REFERENCE && !isfinite(ctx->U[38]))
+    return fail(ctx, DOB_EINVAL, "dob_step", "non-finite dt");
+  float stage_ms[DOB_STAGE_COUNT] = {0};
+  const bool timing = (flags & DOB_STEP_TIMING) != 0;
+  for (int k = 0; k < nsteps; ++k) {
+    dob_status st = one_step(ctx, flags, timing ? stage_ms : nullptr);
+    if (st != DOB_OK) return st;
+  }
+  if (stats) {
+    memset(stats, 0, sizeof(*stats));
+    if (flags & DOB_STEP_STATS) {
+      dob_status st = finish_stats(ctx, stats, nsteps);
+      if (st != DOB_OK) return st;
+    } else {
+      CK(cudaStreamSynchronize(ctx->stream));
+      stats->struct_size = sizeof(dob_step_stats);
+      stats->steps_done = nsteps;
+    }
+    for (int k = 0; k < DOB_STAGE_COUNT; ++k) stats->stage_ms[k] = stage_ms[k];
+  }
+  return DOB_OK;
+}
+
+dob_status dob_step_uniforms(dob_ctx* ctx, const float* blocks, int nsteps, uint32_t flags, dob_step_stats* stats) {
+  if (!ctx || (!blocks && nsteps) || nsteps < 0) return DOB_EINVAL;
+  for (int k = 0; k < nsteps; ++k) {
+    dob_status st = dob_set_uniforms(ctx, blocks + (size_t)k * 128);
+    if (st != DOB_OK) return st;
+    st = dob_step(ctx, 1, flags, k == nsteps - 1 ? stats : nullptr);
+    if (st != DOB_OK) return st;
+  }
+  return DOB_OK;
+}
+
+dob_status dob_run_stage(dob_ctx* ctx, int stage) {
+  if (!ctx) return DOB_EINVAL;
+  if (stage < 0 || stage >= DOB_STAGE_COUNT) return fail(ctx, DOB_EINVAL, "dob_run_stage", "bad stage");
+  const uint32_t spawn = stage == DOB_STAGE_PARCEL_EMIT ? spawn_count(ctx) : 0u;
+  dob_status st = upload_params(ctx, spawn);
+  if (st != DOB_OK) return st;
+  if (stage == DOB_STAGE_CURL && !ctx->s.curl) return fail(ctx, DOB_ESTATE, "dob_run_stage", "no curl field in this mode");
+  enqueue_stage(ctx, ctx->s, stage, ctx->stream);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  return DOB_OK;
+}
+
+dob_status dob_sync(dob_ctx* ctx) {
+  if (!ctx) return DOB_EINVAL;
+  CK(cudaStreamSynchronize(ctx->stream));
+  return DOB_OK;
+}
+
+dob_status dob_launches_per_step(dob_ctx* ctx, int* n) {
+  if (!ctx || !n) return DOB_EINVAL;
+  if (!ctx->kernels_per_step) {
+    // capture the plain step graph once (no launch) to count its kernel nodes
+    cudaGraphExec_t ex = nullptr;
+    dob_status st = get_graph(ctx, false, &ex);
+    if (st != DOB_OK) return st;
+  }
+  *n = ctx->kernels_per_step;
+  return DOB_OK;
+}
+
+dob_status dob_io_bytes(const dob_ctx* ctx, uint64_t* h2d, uint64_t* d2h) {
+  if (!ctx || !h2d || !d2h) return DOB_EINVAL;
+  *h2d = sizeof(StepParams);
+  *d2h = sizeof(double) * RED_COUNT + sizeof(unsigned int) * REDU_COUNT;
+  return DOB_OK;
+}
+
+dob_status dob_memory_bytes(const dob_ctx* ctx, uint64_t* bytes) {
+  if (!ctx || !bytes) return DOB_EINVAL;
+  *bytes = ctx->bytes;
+  return DOB_OK;
+}
+
+dob_status dob_time_steps(dob_ctx* ctx, int nsteps, uint32_t flags, float* ms) {
+  if (!ctx || !ms || nsteps < 0) return DOB_EINVAL;
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  for (int k = 0; k < nsteps; ++k) {
+    dob_status st = one_step(ctx, flags & ~(uint32_t)(DOB_STEP_STATS | DOB_STEP_TIMING), nullptr);
+    if (st != DOB_OK) return st;
+  }
+  CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  CK(cudaEventSynchronize(ctx->ev1));
+  CK(cudaEventElapsedTime(ms, ctx->ev0, ctx->ev1));
+  return DOB_OK;
+}
+
+dob_status dob_bench_kernel(dob_ctx* ctx, int which, int reps, float* avg_ms, double* bytes_per_launch) {
+  if (!ctx || !avg_ms || reps < 1 || which != 0) return DOB_EINVAL;
+  CK(cudaStreamSynchronize(ctx->stream));
+  double total = 0.0, bytes = 0.0;
+  for (int r = 0; r < reps; ++r) {
+    CK(cudaEventRecord(ctx->ev0, ctx->stream));
+    bytes = smoother_pass(ctx->s, ctx->stream);
+    CK(cudaEventRecord(ctx->ev1, ctx->stream));
+    CK(cudaEventSynchronize(ctx->ev1));
+    float ms = 0.0f;
+    CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    total += ms;
+  }
+  *avg_ms = (float)(total / reps);
+  if (bytes_per_launch) *bytes_per_launch = bytes;
+  return DOB_OK;
+}
+
+dob_status dob_save_state(dob_ctx* ctx, int slot) {
+  if (!ctx || slot < 0 || slot >= kSnapshots) return DOB_EINVAL;
+  DevState& s = ctx->s;
+  const size_t N = s.g.n(), Nc = s.gc.n();
+  const size_t vsb = vs_bytes(s.prec), dsb = ds_bytes(s.prec);
+  const int nch = s.ref ? 4 : 1;
+  void* src[] = {s.u, s.v, s.w, s.cen, s.curl, s.p, s.conc, s.parcels};
+  const size_t sz[] = {N * vsb, N * vsb, N * vsb, N * 4 * vsb, s.curl ? N * 4 * vsb : 0, N * 4, Nc * nch * dsb,
+                       (size_t)s.cap * 32};
+  Snapshot& sn = ctx->snaps[slot];
+  if (!sn.valid) {
+    for (size_t k = 0; k < sizeof(sz) / sizeof(sz[0]); ++k) {
+      void* p = nullptr;
+      if (sz[k]) {
+        cudaError_t e = cudaMalloc(&p, sz[k]);
+        if (e != cudaSuccess) {
+          cudaGetLastError();
+          return fail(ctx, DOB_ENOMEM, "dob_save_state", cudaGetErrorString(e));
+        }
+      }
+      sn.bufs.push_back(p);
+      sn.sizes.push_back(sz[k]);
+    }
+    sn.valid = true;
+  }
+  for (size_t k = 0; k < sn.bufs.size(); ++k)
+    if (sn.sizes[k]) CK(cudaMemcpyAsync(sn.bufs[k], src[k], sn.sizes[k], cudaMemcpyDeviceToDevice, ctx->stream));
+  sn.high_water = ctx->high_water;
+  sn.step_index = ctx->step_index;
+  CK(cudaStreamSynchronize(ctx->stream));
+  return DOB_OK;
+}
+
+dob_status dob_load_state(dob_ctx* ctx, int slot) {
+  if (!ctx || slot < 0 || slot >= kSnapshots) return DOB_EINVAL;
+  Snapshot& sn = ctx->snaps[slot];
+  if (!sn.valid) return fail(ctx, DOB_ESTATE, "dob_load_state", "empty snapshot slot");
+  DevState& s = ctx->s;
+  void* dst[] = {s.u, s.v, s.w, s.cen, s.curl, s.p, s.conc, s.parcels};
+  for (size_t k = 0; k < sn.bufs.size(); ++k)
+    if (sn.sizes[k]) CK(cudaMemcpyAsync(dst[k], sn.bufs[k], sn.sizes[k], cudaMemcpyDeviceToDevice, ctx->stream));
+  ctx->high_water = sn.high_water;
+  ctx->step_index = sn.step_index;
+  CK(cudaStreamSynchronize(ctx->stream));
+  return DOB_OK;
+}
+
+dob_status dob_eval_math(int fn, const float* x, const float* y, float* out, uint32_t n) {
+  if (!x || !out || fn < 0 || fn > 8 || (fn == 4 || fn == 5) && !y) return DOB_EINVAL;
+  if (n == 0) return DOB_OK;
+  cudaError_t e = eval_math_device(fn, x, y, out, n);
+  if (e != cudaSuccess) return fail(nullptr, DOB_ECUDA, "dob_eval_math", cudaGetErrorString(e));
+  return DOB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,179 @@
+// dob_device.cuh — device-side data layout and shared helpers of the
+// GB300 fluid step.
+//
+// HBM layout (x fastest, index = (z*ny + y)*nx + x):
+//   MAC velocity   u, v, w       3 SoA arrays of VS (float | binary16)
+//   centre velocity              AoS 4 x VS (x, y, z, 0) — one 16 B (8 B) gather per tap
+//   curl                         AoS 4 x VS (wx, wy, wz, |w|)
+//   pressure p, rhs b            float; MG levels float (BF16 in the mixed inner solve)
+//   conc (reference mode)        AoS 4 x DS (intact, lysed, ox/shear, bed) on the dye grid
+//   dye  (closed box)            1 x DS on the dye grid
+//   predictor                    1 x DS (the .g channel CONC_PREDICT writes)
+//   splat accumulators           2 x u32 on the dye grid
+//   parcels                      AoS 8 x float (RbcParcel, 32 B)
+// VS/DS are the velocity/dye storage types; arithmetic is always FP32.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+#include "dob_math.h"
+
+namespace dob {
+
+constexpr int kMaxDrops = 8;
+constexpr int kWaveN = 512;
+constexpr float kSplatScale = 65536.0f;
+constexpr float kSplatInv = 1.52587891e-5f;  // (1/65536).toExponential(8), advect.ts:125
+constexpr float kParcelMass = 0.13400f;      // particles.ts:14, 177
+
+// Per-step parameters, resident in device memory and refreshed by one small
+// host->device copy before each step (so a captured step graph stays valid).
+struct StepParams {
+  float U[128];        // the reference's SimUniforms block (common.ts:31-43)
+  float dt;            // effective dt (reference: clamp(U[38], 0, 0.025))
+  float dmin[3];
+  float dmax[3];
+  float dsize[3];
+  float damp;          // advection damping
+  float sharp;         // MacCormack sharpness
+  float tau_y, mu_p, dx;
+  uint32_t spawn_count;
+  uint32_t cursor;
+  uint32_t high_water;
+  uint32_t advect_count;
+  int32_t step_index;
+};
+
+struct Grid {
+  int nx, ny, nz;
+  __host__ __device__ size_t n() const { return (size_t)nx * ny * nz; }
+  __host__ __device__ size_t at(int x, int y, int z) const { return ((size_t)z * ny + y) * nx + x; }
+};
+
+// ---- storage types -------------------------------------------------------------
+struct alignas(8) half4 {
+  __half x, y, z, w;
+};
+
+template <class S> struct Vec4Of;
+template <> struct Vec4Of<float> { using type = float4; };
+template <> struct Vec4Of<__half> { using type = half4; };
+
+__device__ __forceinline__ float ldf(const float* p) { return __ldg(p); }
+__device__ __forceinline__ float ldf(const __half* p) { return __half2float(__ldg(p)); }
+__device__ __forceinline__ float ldf(const __nv_bfloat16* p) { return __bfloat162float(__ldg(p)); }
+__device__ __forceinline__ float ldv(const float* p) { return *p; }
+__device__ __forceinline__ float ldv(const __half* p) { return __half2float(*p); }
+__device__ __forceinline__ float ldv(const __nv_bfloat16* p) { return __bfloat162float(*p); }
+__device__ __forceinline__ void stf(float* p, float v) { *p = v; }
+__device__ __forceinline__ void stf(__half* p, float v) { *p = __float2half_rn(v); }
+__device__ __forceinline__ void stf(__nv_bfloat16* p, float v) { *p = __float2bfloat16_rn(v); }
+
+__device__ __forceinline__ float4 ld4(const float4* p) { return __ldg(p); }
+__device__ __forceinline__ float4 ld4(const half4* p) {
+  const uint2 r = __ldg(reinterpret_cast<const uint2*>(p));
+  const __half2 a = *reinterpret_cast<const __half2*>(&r.x);
+  const __half2 b = *reinterpret_cast<const __half2*>(&r.y);
+  const float2 fa = __half22float2(a), fb = __half22float2(b);
+  return make_float4(fa.x, fa.y, fb.x, fb.y);
+}
+__device__ __forceinline__ void st4(float4* p, float4 v) { *p = v; }
+__device__ __forceinline__ void st4(half4* p, float4 v) {
+  const __half2 a = __floats2half2_rn(v.x, v.y);
+  const __half2 b = __floats2half2_rn(v.z, v.w);
+  uint2 r;
+  r.x = *reinterpret_cast<const uint32_t*>(&a);
+  r.y = *reinterpret_cast<const uint32_t*>(&b);
+  *reinterpret_cast<uint2*>(p) = r;
+}
+
+// ---- WebGPU linear / clamp-to-edge sampling (texel = uvw*dims - 0.5) ----------
+struct Taps {
+  size_t i[8];
+  float fx, fy, fz;
+};
+__device__ __forceinline__ Taps make_taps(const Grid& g, float u, float v, float w) {
+  Taps t;
+  const float cx = u * (float)g.nx - 0.5f, cy = v * (float)g.ny - 0.5f, cz = w * (float)g.nz - 0.5f;
+  const float bx = floorf(cx), by = floorf(cy), bz = floorf(cz);
+  t.fx = cx - bx; t.fy = cy - by; t.fz = cz - bz;
+  const int ix = (int)bx, iy = (int)by, iz = (int)bz;
+  const int x0 = dob_clampi(ix, 0, g.nx - 1), x1 = dob_clampi(ix + 1, 0, g.nx - 1);
+  const int y0 = dob_clampi(iy, 0, g.ny - 1), y1 = dob_clampi(iy + 1, 0, g.ny - 1);
+  const int z0 = dob_clampi(iz, 0, g.nz - 1), z1 = dob_clampi(iz + 1, 0, g.nz - 1);
+  t.i[0] = g.at(x0, y0, z0); t.i[1] = g.at(x1, y0, z0);
+  t.i[2] = g.at(x0, y1, z0); t.i[3] = g.at(x1, y1, z0);
+  t.i[4] = g.at(x0, y0, z1); t.i[5] = g.at(x1, y0, z1);
+  t.i[6] = g.at(x0, y1, z1); t.i[7] = g.at(x1, y1, z1);
+  return t;
+}
+template <class S> __device__ __forceinline__ float lerp8(const Taps& t, const S* a) {
+  const float x00 = dob_mix(ldf(a + t.i[0]), ldf(a + t.i[1]), t.fx);
+  const float x10 = dob_mix(ldf(a + t.i[2]), ldf(a + t.i[3]), t.fx);
+  const float x01 = dob_mix(ldf(a + t.i[4]), ldf(a + t.i[5]), t.fx);
+  const float x11 = dob_mix(ldf(a + t.i[6]), ldf(a + t.i[7]), t.fx);
+  const float y0 = dob_mix(x00, x10, t.fy);
+  const float y1 = dob_mix(x01, x11, t.fy);
+  return dob_mix(y0, y1, t.fz);
+}
+template <class V4> __device__ __forceinline__ float4 lerp8x4(const Taps& t, const V4* a) {
+  float4 c[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) c[k] = ld4(a + t.i[k]);
+  float4 r;
+  {
+    const float x00 = dob_mix(c[0].x, c[1].x, t.fx), x10 = dob_mix(c[2].x, c[3].x, t.fx);
+    const float x01 = dob_mix(c[4].x, c[5].x, t.fx), x11 = dob_mix(c[6].x, c[7].x, t.fx);
+    r.x = dob_mix(dob_mix(x00, x10, t.fy), dob_mix(x01, x11, t.fy), t.fz);
+  }
+  {
+    const float x00 = dob_mix(c[0].y, c[1].y, t.fx), x10 = dob_mix(c[2].y, c[3].y, t.fx);
+    const float x01 = dob_mix(c[4].y, c[5].y, t.fx), x11 = dob_mix(c[6].y, c[7].y, t.fx);
+    r.y = dob_mix(dob_mix(x00, x10, t.fy), dob_mix(x01, x11, t.fy), t.fz);
+  }
+  {
+    const float x00 = dob_mix(c[0].z, c[1].z, t.fx), x10 = dob_mix(c[2].z, c[3].z, t.fx);
+    const float x01 = dob_mix(c[4].z, c[5].z, t.fx), x11 = dob_mix(c[6].z, c[7].z, t.fx);
+    r.z = dob_mix(dob_mix(x00, x10, t.fy), dob_mix(x01, x11, t.fy), t.fz);
+  }
+  {
+    const float x00 = dob_mix(c[0].w, c[1].w, t.fx), x10 = dob_mix(c[2].w, c[3].w, t.fx);
+    const float x01 = dob_mix(c[4].w, c[5].w, t.fx), x11 = dob_mix(c[6].w, c[7].w, t.fx);
+    r.w = dob_mix(dob_mix(x00, x10, t.fy), dob_mix(x01, x11, t.fy), t.fz);
+  }
+  return r;
+}
+template <class V4> __device__ __forceinline__ dob_v3 sample_center(const Grid& g, const V4* cen, dob_v3 uvw) {
+  const Taps t = make_taps(g, uvw.x, uvw.y, uvw.z);
+  const float4 r = lerp8x4(t, cen);
+  return v3(r.x, r.y, r.z);
+}
+
+// 512x512 wave texture, bilinear clamp-to-edge, worldXZToWaveUV (common.ts:65-67).
+__device__ __forceinline__ float4 sample_wave(const float4* wave, float x, float z, float lo, float hi) {
+  const float su = dob_clampf((x + 1.60f) / 3.20f, lo, hi);
+  const float sv = dob_clampf((z + 1.60f) / 3.20f, lo, hi);
+  const float cx = su * (float)kWaveN - 0.5f, cy = sv * (float)kWaveN - 0.5f;
+  const float bx = floorf(cx), by = floorf(cy);
+  const float fx = cx - bx, fy = cy - by;
+  const int x0 = dob_clampi((int)bx, 0, kWaveN - 1), x1 = dob_clampi((int)bx + 1, 0, kWaveN - 1);
+  const int y0 = dob_clampi((int)by, 0, kWaveN - 1), y1 = dob_clampi((int)by + 1, 0, kWaveN - 1);
+  const float4 a00 = __ldg(wave + y0 * kWaveN + x0), a10 = __ldg(wave + y0 * kWaveN + x1);
+  const float4 a01 = __ldg(wave + y1 * kWaveN + x0), a11 = __ldg(wave + y1 * kWaveN + x1);
+  float4 r;
+  r.x = dob_mix(dob_mix(a00.x, a10.x, fx), dob_mix(a01.x, a11.x, fx), fy);
+  r.y = dob_mix(dob_mix(a00.y, a10.y, fx), dob_mix(a01.y, a11.y, fx), fy);
+  r.z = dob_mix(dob_mix(a00.z, a10.z, fx), dob_mix(a01.z, a11.z, fx), fy);
+  r.w = dob_mix(dob_mix(a00.w, a10.w, fx), dob_mix(a01.w, a11.w, fx), fy);
+  return r;
+}
+
+__device__ __forceinline__ dob_v3 dmin_of(const StepParams& P) { return v3(P.dmin[0], P.dmin[1], P.dmin[2]); }
+__device__ __forceinline__ dob_v3 dsize_of(const StepParams& P) { return v3(P.dsize[0], P.dsize[1], P.dsize[2]); }
+__device__ __forceinline__ dob_v3 to_world(const StepParams& P, dob_v3 uvw) { return dmin_of(P) + uvw * dsize_of(P); }
+__device__ __forceinline__ dob_v3 to_uvw(const StepParams& P, dob_v3 p) { return (p - dmin_of(P)) / dsize_of(P); }
+__device__ __forceinline__ float drop(const StepParams& P, int d, int k) { return P.U[64 + 8 * d + k]; }
+
+}  // namespace dob

@@ -1,0 +1,151 @@
+// dob_kernels.cuh — device state of one context and the launchers of every
+// kernel of the step (one .cu file per kernel family).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "../../include/dropfluid.h"
+#include "dob_device.cuh"
+
+namespace dob {
+
+constexpr int kMaxLevels = 10;
+
+// One grid of the multigrid hierarchy.  Level 0 reuses the pressure / rhs
+// arrays; every level owns a residual-free layout (residual + restriction are
+// fused, so no residual array exists).
+struct MgLevel {
+  Grid d;
+  float h2;
+  float* e;            // correction (levels >= 1), FP32
+  float* b;            // right-hand side (levels >= 1), FP32
+  __nv_bfloat16* eh;   // BF16 copies used by the mixed-precision inner solve
+  __nv_bfloat16* bh;
+};
+
+struct DevState {
+  Grid g;    // velocity / pressure grid
+  Grid gc;   // dye grid
+  int prec;  // DOB_PREC_*
+  int ref;   // reference boundary conditions
+  int flags; // DOB_PHYS_* (reference mode only)
+  int num_sms;
+  StepParams* params;            // device copy of this step's parameters
+  void *u, *v, *w, *u2, *v2, *w2;  // MAC faces (VS)
+  void *cen, *curl;              // 4 x VS AoS
+  float *p, *rhs;
+  void *conc, *conc2, *pred;     // dye (DS)
+  uint32_t *splatI, *splatL;
+  float4* wave;
+  float* parcels;
+  uint32_t cap;
+  double* red;                   // FP64 reduction slots
+  unsigned int* redu;            // u32 reduction slots / flags
+  int nlev;
+  MgLevel lv[kMaxLevels];
+  int pre0, post0, pre, post, coarse_sweeps, cycles;
+  // mixed-precision defect correction
+  __nv_bfloat16 *e0h, *r0h;      // level-0 correction and residual (BF16)
+  int max_outer;
+  double rel_tol;
+};
+
+// reduction slot indices in DevState::red / redu
+enum {
+  RED_RHS_SUM = 0,
+  RED_P_SUM = 1,
+  RED_RHS_NORM2 = 2,
+  RED_RES_NORM2 = 3,
+  RED_DEFECT_NORM2 = 4,   // base of per-outer-iteration defect norms
+  RED_COUNT = 4 + 32
+};
+enum {
+  REDU_MAXDIV = 0,
+  REDU_ALIVE = 1,
+  REDU_DONE = 2,          // defect loop converged (kernels of later iterations exit)
+  REDU_ITERS = 3,         // defect iterations executed
+  REDU_COUNT = 8
+};
+
+// ---- block reductions ---------------------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ float warp_maxf(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+// Sum `v` over the block and add it to *out with one FP64 atomic per block.
+__device__ __forceinline__ void block_sum_atomic(double v, double* out) {
+  __shared__ double part[32];
+  const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  const int nthreads = blockDim.x * blockDim.y * blockDim.z;
+  v = warp_sum(v);
+  if ((tid & 31) == 0) part[tid >> 5] = v;
+  __syncthreads();
+  if (tid < 32) {
+    double s = tid < (nthreads + 31) / 32 ? part[tid] : 0.0;
+    s = warp_sum(s);
+    if (tid == 0 && s != 0.0) atomicAdd(out, s);
+  }
+}
+// Max of non-negative floats via their bit patterns.
+__device__ __forceinline__ void block_max_atomic(float v, unsigned int* out) {
+  __shared__ float part[32];
+  const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  const int nthreads = blockDim.x * blockDim.y * blockDim.z;
+  v = warp_maxf(v);
+  if ((tid & 31) == 0) part[tid >> 5] = v;
+  __syncthreads();
+  if (tid < 32) {
+    float s = tid < (nthreads + 31) / 32 ? part[tid] : 0.0f;
+    s = warp_maxf(s);
+    if (tid == 0 && s > 0.0f) atomicMax(out, __float_as_uint(s));
+  }
+}
+
+// Instantiate a launch body for the storage types of a precision mode:
+//   VS = velocity storage, DS = dye storage.
+#define DOB_VEL_DISPATCH(prec, ...)                                                             \
+  do {                                                                                          \
+    if ((prec) == DOB_PREC_REFERENCE_FP16) { using VS = __half; using DS = __half; __VA_ARGS__; } \
+    else if ((prec) == DOB_PREC_MIXED) { using VS = float; using DS = __half; __VA_ARGS__; }      \
+    else { using VS = float; using DS = float; __VA_ARGS__; }                                     \
+  } while (0)
+
+// ---- launchers (k_fluid.cu) -----------------------------------------------------------
+void launch_init_vel(const DevState& s, cudaStream_t st);
+void launch_advect_mac(const DevState& s, cudaStream_t st);
+void launch_mac_to_center(const DevState& s, cudaStream_t st);
+void launch_curl(const DevState& s, cudaStream_t st);
+void launch_casson(const DevState& s, cudaStream_t st);
+void launch_mac_rhs(const DevState& s, cudaStream_t st);
+void launch_project(const DevState& s, cudaStream_t st);
+void launch_divergence(const DevState& s, float* out, float scale, unsigned int* maxbits, cudaStream_t st);
+void launch_conc_predict(const DevState& s, cudaStream_t st);
+void launch_conc_resolve(const DevState& s, cudaStream_t st);
+
+// ---- launchers (k_mg.cu) ---------------------------------------------------------------
+// Raise the dynamic shared-memory limit of the coarse-grid kernel (once per process).
+cudaError_t mg_prepare();
+void launch_pressure_solve(const DevState& s, cudaStream_t st);
+void launch_residual_norm(const DevState& s, double* out, cudaStream_t st);
+void launch_sum(const float* a, size_t n, double* out, int num_sms, cudaStream_t st);
+void launch_sub_mean(float* a, size_t n, const double* sum, int num_sms, cudaStream_t st);
+void launch_sumsq(const float* a, size_t n, double* out, int num_sms, cudaStream_t st);
+// One pass of the level-0 pressure smoother on the current state; returns the
+// pass's algorithmic HBM bytes (read p and b, write p once).
+double smoother_pass(const DevState& s, cudaStream_t st);
+
+// ---- launchers (k_exact.cu: FMA-free, bit-reproducible on the host) -------------------
+void launch_parcel_emit(const DevState& s, cudaStream_t st);
+void launch_parcel_advect(const DevState& s, cudaStream_t st);
+void launch_count_alive(const DevState& s, unsigned int* out, cudaStream_t st);
+void launch_inject_sphere(const DevState& s, const float c[3], float r, float dye, const float vel[3], float sigma,
+                          uint64_t seed, cudaStream_t st);
+cudaError_t eval_math_device(int fn, const float* x, const float* y, float* out, uint32_t n);
+
+}  // namespace dob

@@ -1,0 +1,754 @@
+// k_fluid.cu — velocity-grid kernels of the step: initial field, MAC
+// advection, MAC->centre, curl, Casson viscosity + forces, divergence,
+// projection, and the dye/conc transport kernels.
+//
+// Each kernel is one HBM-bound pass over the grid (one thread per cell,
+// x-fastest warps so every field access is a coalesced row segment; the
+// trilinear gathers of the centre field are 16 B AoS loads).
+#include "dob_kernels.cuh"
+
+namespace dob {
+
+// ---- evalTopDirichletPressure (fluid.ts:16-77) ------------------------------------
+__device__ float top_pressure(const Grid& g, const StepParams& P, const float4* wave, int ix, int iz) {
+  const float halfXZ = P.U[52];
+  const float fx = ((float)ix + 0.5f) / (float)g.nx;
+  const float fz = ((float)iz + 0.5f) / (float)g.nz;
+  const float wx = dob_mix(-halfXZ, halfXZ, fx), wz = dob_mix(-halfXZ, halfXZ, fz);
+  const float dtv = P.dt;
+  const float cellH = (2.0f * halfXZ) / (float)g.nx;
+  const float dtOverH = dtv / cellH;
+  const float4 ws = sample_wave(wave, wx, wz, 0.002f, 0.998f);
+  const float eta = ws.x, lap = ws.z;
+  const float capTerm = -18.4f * lap;
+  float pK = 2.45f * (0.155f * eta + 0.00095f * capTerm);
+  for (int d = 0; d < kMaxDrops; ++d) {
+    const float signedSeed = drop(P, d, 7), drain = drop(P, d, 6);
+    if (signedSeed > 0.0f && drain > 0.0005f) {
+      const float rx = wx - drop(P, d, 0), rz = wz - drop(P, d, 2);
+      const float r = length2f(rx, rz);
+      const float theta = dob_atan2(rz, rx);
+      const float seed = signedSeed;
+      const float azim = 1.0f + 0.022f * dob_cos(4.0f * theta + seed * 1.73f) +
+                         0.016f * dob_cos(6.0f * theta - seed * 2.31f) + 0.010f * dob_sin(8.0f * theta + seed * 0.89f);
+      const float slugPhase = dob_smoothstep(0.32f, 0.92f, drain);
+      const float rOrifice =
+          dob_clampf(drop(P, d, 3) * 1.12f + dob_mix(0.018f, 0.032f, slugPhase), 0.030f, 0.090f) * azim;
+      const float rNorm = r / dob_maxf(rOrifice, 1e-4f);
+      const float speedY = dob_clampf(-drop(P, d, 4), 0.08f, 0.65f);
+      const float neck = (0.28f + 1.05f * rNorm * rNorm) * dob_exp(-0.92f * rNorm * rNorm) * (1.0f - 0.38f * rNorm * rNorm);
+      pK = pK + drain * (0.014f + 0.048f * speedY) * neck;
+    }
+  }
+  const float wallTaper = 1.0f - dob_smoothstep(halfXZ * 0.72f, halfXZ * 0.96f, dob_maxf(fabsf(wx), fabsf(wz)));
+  return pK * dtOverH * wallTaper;
+}
+
+#define CELL_INDEX                                   \
+  const int x = blockIdx.x * blockDim.x + threadIdx.x; \
+  const int y = blockIdx.y * blockDim.y + threadIdx.y; \
+  const int z = blockIdx.z;                          \
+  if (x >= g.nx || y >= g.ny) return;                \
+  const size_t i = g.at(x, y, z);
+
+// ---- FLUID_INIT_VEL (fluid.ts:80-121) --------------------------------------------------
+template <class VS>
+__global__ void k_init_vel(Grid g, const StepParams* __restrict__ Pp, VS* u, VS* v, VS* w,
+                           typename Vec4Of<VS>::type* cen, typename Vec4Of<VS>::type* curl) {
+  CELL_INDEX
+  const StepParams& P = *Pp;
+  const dob_v3 dims = v3((float)g.nx, (float)g.ny, (float)g.nz);
+  const float seed = P.U[43], surfY = P.U[40], halfXZ = P.U[52];
+  const dob_v3 pX = to_world(P, v3((float)x + 1.0f, (float)y + 0.5f, (float)z + 0.5f) / dims);
+  const dob_v3 pY = to_world(P, v3((float)x + 0.5f, (float)y + 1.0f, (float)z + 0.5f) / dims);
+  const dob_v3 pZ = to_world(P, v3((float)x + 0.5f, (float)y + 0.5f, (float)z + 1.0f) / dims);
+  auto fade = [&](dob_v3 q) {
+    return (1.0f - dob_smoothstep(halfXZ * 0.55f, halfXZ * 0.96f, dob_maxf(fabsf(q.x), fabsf(q.z)))) *
+           (1.0f - dob_smoothstep(surfY - 0.12f, surfY, q.y)) * dob_smoothstep(0.06f, 0.24f, length2f(q.x, q.z));
+  };
+  float vx = 0.00045f * dob_sin(pX.x * 6.5f) * dob_cos(pX.z * 6.5f) * dob_sin(pX.y * 5.2f + seed * 1.3f) * fade(pX);
+  float vy = 0.00030f * dob_cos(pY.x * 6.5f) * dob_sin(pY.z * 6.5f) * dob_cos(pY.y * 5.2f + seed * 0.7f) * fade(pY);
+  float vz = -0.00045f * dob_cos(pZ.x * 6.5f) * dob_sin(pZ.z * 6.5f) * dob_sin(pZ.y * 5.2f + seed * 1.3f) * fade(pZ);
+  if (x >= g.nx - 1) vx = 0.0f;
+  if (z >= g.nz - 1) vz = 0.0f;
+  stf(u + i, vx); stf(v + i, vy); stf(w + i, vz);
+  st4(cen + i, make_float4(vx, vy, vz, 0.0f));
+  st4(curl + i, make_float4(vx, vy, vz, 0.0f));
+}
+
+// ---- FLUID_ADVECT_MAC (fluid.ts:144-329) ------------------------------------------------
+template <class VS>
+__device__ __forceinline__ float sample_mac(const Grid& g, const VS* a, dob_v3 uvw, int comp) {
+  if (comp == 0) uvw.x = uvw.x - 0.5f / (float)g.nx;
+  if (comp == 1) uvw.y = uvw.y - 0.5f / (float)g.ny;
+  if (comp == 2) uvw.z = uvw.z - 0.5f / (float)g.nz;
+  uvw = clamp3(uvw, 0.001f, 0.999f);
+  const Taps t = make_taps(g, uvw.x, uvw.y, uvw.z);
+  return lerp8(t, a);
+}
+template <class V4>
+__device__ __forceinline__ dob_v3 trace_back(const Grid& g, const V4* cen, dob_v3 uvwF, float dtv, dob_v3 dom) {
+  const dob_v3 v0 = sample_center(g, cen, clamp3(uvwF, 0.002f, 0.998f));
+  const dob_v3 uvwMid = clamp3(uvwF - (0.5f * (v0 * dtv)) / dom, 0.002f, 0.998f);
+  const dob_v3 vMid = sample_center(g, cen, uvwMid);
+  return clamp3(uvwF - (vMid * dtv) / dom, 0.002f, 0.998f);
+}
+__device__ __forceinline__ float azim_neck(float theta, float seed) {
+  return 1.0f + 0.036f * dob_cos(4.0f * theta + seed * 1.73f) + 0.026f * dob_cos(6.0f * theta - seed * 2.31f) +
+         0.018f * dob_sin(8.0f * theta + seed * 0.89f);
+}
+
+template <class VS>
+__global__ void __launch_bounds__(256) k_advect_mac(Grid g, const StepParams* __restrict__ Pp, int ref, int flags,
+                                                    const VS* __restrict__ u, const VS* __restrict__ v,
+                                                    const VS* __restrict__ w,
+                                                    const typename Vec4Of<VS>::type* __restrict__ cen,
+                                                    const float4* __restrict__ wave, VS* __restrict__ uo,
+                                                    VS* __restrict__ vo, VS* __restrict__ wo) {
+  CELL_INDEX
+  const StepParams& P = *Pp;
+  const dob_v3 dims = v3((float)g.nx, (float)g.ny, (float)g.nz);
+  const float dtv = P.dt;
+  const dob_v3 dom = dsize_of(P);
+  const float damp = P.damp;
+  const dob_v3 uvwX = v3((float)x + 1.0f, (float)y + 0.5f, (float)z + 0.5f) / dims;
+  const dob_v3 uvwY = v3((float)x + 0.5f, (float)y + 1.0f, (float)z + 0.5f) / dims;
+  const dob_v3 uvwZ = v3((float)x + 0.5f, (float)y + 0.5f, (float)z + 1.0f) / dims;
+  float vx = sample_mac(g, u, trace_back(g, cen, uvwX, dtv, dom), 0) * damp;
+  float vy = sample_mac(g, v, trace_back(g, cen, uvwY, dtv, dom), 1) * damp;
+  float vz = sample_mac(g, w, trace_back(g, cen, uvwZ, dtv, dom), 2) * damp;
+  if (ref) {
+    const float surfY = P.U[40];
+    const dob_v3 pCell = to_world(P, (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / dims);
+    const dob_v3 pFaceY = to_world(P, uvwY);
+    float activeNeckMask = 0.0f;
+    if (flags & DOB_PHYS_NECK) {
+      for (int d = 0; d < kMaxDrops; ++d) {
+        const float signedSeed = drop(P, d, 7), drain = drop(P, d, 6);
+        if (!(signedSeed > 0.0f && drain > 0.0005f)) continue;
+        const float dX = drop(P, d, 0), dZ = drop(P, d, 2);
+        const float relx = pFaceY.x - dX, relz = pFaceY.z - dZ;
+        const float r = length2f(relx, relz);
+        const float theta = dob_atan2(relz, relx);
+        const float seed = signedSeed;
+        const float azim = azim_neck(theta, seed);
+        const float sp = dob_smoothstep(0.14f, 0.76f, drain);
+        const float rNeckBase =
+            dob_clampf(drop(P, d, 3) * dob_mix(0.80f, 1.08f, sp) + dob_mix(0.012f, 0.030f, sp), 0.018f, 0.088f);
+        const float rNeck = rNeckBase * azim;
+        const float rRatio = r / dob_maxf(rNeck, 1e-4f);
+        const float slugRadial = (0.14f + 1.00f * dob_minf(rRatio * rRatio, 1.20f)) * (1.0f - dob_smoothstep(0.78f, 1.15f, rRatio));
+        const float stemRadial = (0.68f + 0.32f * dob_minf(rRatio * rRatio, 1.0f)) * (1.0f - dob_smoothstep(0.74f, 1.10f, rRatio));
+        const float radialProfile = dob_mix(stemRadial, slugRadial, sp);
+        const float vertMask = dob_smoothstep(surfY - 0.058f, surfY - 0.014f, pFaceY.y);
+        const float meniscusShear = dob_mix(1.0f, 0.36f, dob_smoothstep(surfY - 0.024f, surfY - 0.002f, pFaceY.y));
+        const float mask = radialProfile * vertMask;
+        activeNeckMask = dob_maxf(activeNeckMask, radialProfile);
+        if (mask > 0.001f) {
+          const float lobeMod = 1.0f + 0.036f * dob_cos(4.0f * theta + seed * 1.73f) + 0.026f * dob_cos(6.0f * theta - seed * 2.31f);
+          const float impactSpeed = dob_clampf(-drop(P, d, 4), 0.10f, 0.65f);
+          const float slugDrive = dob_clampf(dob_pow(dob_maxf(drain, 0.0f), 0.66f) * 0.84f, 0.0f, 1.24f);
+          const float stemDrive = dob_clampf(0.045f + drain * 0.22f, 0.0f, 0.20f) * dob_smoothstep(0.0f, 0.05f, drain);
+          const float fluxDrive = dob_mix(stemDrive, slugDrive, sp);
+          const float targetVy = -dob_clampf(0.14f + 0.64f * impactSpeed, 0.15f, 0.39f) * fluxDrive * lobeMod * meniscusShear;
+          const float blend = dob_clampf(dtv * dob_mix(14.0f, 22.0f, sp) * mask, 0.0f, 1.0f);
+          vy = dob_mix(vy, targetVy, blend);
+        }
+        const float vertMaskXZ = dob_smoothstep(surfY - 0.058f, surfY - 0.014f, pCell.y);
+        if (vertMaskXZ > 0.001f) {
+          const float flare = dob_mix(0.104f * (0.35f + 0.65f * sp), -0.020f, dob_smoothstep(surfY - 0.066f, surfY - 0.012f, pCell.y)) *
+                              dob_clampf(drain, 0.0f, 1.3f);
+          for (int comp = 0; comp < 2; ++comp) {
+            const dob_v3 fw = to_world(P, comp == 0 ? uvwX : uvwZ);
+            const float ax = fw.x - dX, az = fw.z - dZ;
+            const float rF = length2f(ax, az);
+            if (rF > 1e-4f && rF < rNeckBase * 1.34f) {
+              const float thF = dob_atan2(az, ax);
+              const float azF = azim_neck(thF, seed);
+              const float rR = rF / dob_maxf(rNeckBase * azF, 1e-4f);
+              if (rR < 1.22f) {
+                const float slugR = (0.14f + 1.00f * dob_minf(rR * rR, 1.20f)) * (1.0f - dob_smoothstep(0.78f, 1.15f, rR));
+                const float stemR = (0.68f + 0.32f * dob_minf(rR * rR, 1.0f)) * (1.0f - dob_smoothstep(0.74f, 1.10f, rR));
+                const float maskF = dob_mix(stemR, slugR, sp) * vertMaskXZ;
+                const float blendF = dob_clampf(dtv * dob_mix(14.0f, 22.0f, sp) * maskF, 0.0f, 1.0f);
+                if (comp == 0) vx = dob_mix(vx, (ax / rF) * flare, blendF * 0.65f);
+                else vz = dob_mix(vz, (az / rF) * flare, blendF * 0.65f);
+              }
+            }
+          }
+        }
+      }
+    }
+    if ((flags & DOB_PHYS_SURFACE) && y >= g.ny - 3) {
+      const float topFade = (float)(y - (g.ny - 3) + 1) / 3.0f;
+      const float epsW = 0.015f;
+      const float4 wc = sample_wave(wave, pCell.x, pCell.z, 0.002f, 0.998f);
+      const float wC = wc.w;
+      const float wXp = sample_wave(wave, pCell.x + epsW, pCell.z, 0.002f, 0.998f).w;
+      const float wXn = sample_wave(wave, pCell.x - epsW, pCell.z, 0.002f, 0.998f).w;
+      const float wZp = sample_wave(wave, pCell.x, pCell.z + epsW, 0.002f, 0.998f).w;
+      const float wZn = sample_wave(wave, pCell.x, pCell.z - epsW, 0.002f, 0.998f).w;
+      const float cmcWindow = 1.0f - dob_smoothstep(0.45f, 0.88f, wC);
+      const float gx = (wXp - wXn) / (2.0f * epsW), gz = (wZp - wZn) / (2.0f * epsW);
+      const float sc = -P.U[41] * 0.026f * cmcWindow;
+      vx = vx + (sc * gx * topFade) * dtv;
+      vz = vz + (sc * gz * topFade) * dtv;
+      if (y >= g.ny - 2 && activeNeckMask < 0.02f) {
+        const float calmGate = 1.0f - dob_smoothstep(0.020f, 0.14f, fabsf(wc.y));
+        const float layerWeight = (y == g.ny - 1) ? 0.72f : 0.26f;
+        vy = dob_mix(vy, dob_clampf(wc.y * 0.35f, -0.045f, 0.045f), calmGate * layerWeight);
+      }
+    }
+    if (flags & DOB_PHYS_SPONGE) {
+      const float halfXZ = P.U[52], yMin = P.U[53];
+      const float rCellXZ = length2f(pCell.x, pCell.z);
+      const float wallFade = (1.0f - dob_smoothstep(halfXZ * 0.68f, halfXZ * 0.94f, rCellXZ)) *
+                             dob_smoothstep(yMin + 0.004f, yMin + 0.052f, pCell.y);
+      const float spongeMul = dob_mix(0.84f, 1.0f, wallFade);
+      vx = vx * spongeMul; vy = vy * spongeMul; vz = vz * spongeMul;
+    }
+  }
+  if (x >= g.nx - 1) vx = 0.0f;
+  if (z >= g.nz - 1) vz = 0.0f;
+  if (!ref && y >= g.ny - 1) vy = 0.0f;
+  stf(uo + i, vx); stf(vo + i, vy); stf(wo + i, vz);
+}
+
+// ---- FLUID_MAC_TO_CENTER (fluid.ts:917-962) -----------------------------------------------
+template <class VS>
+__global__ void __launch_bounds__(256) k_mac_to_center(Grid g, const StepParams* __restrict__ Pp, int ref, int flags,
+                                                       const VS* __restrict__ u, const VS* __restrict__ v,
+                                                       const VS* __restrict__ w,
+                                                       typename Vec4Of<VS>::type* __restrict__ cen) {
+  CELL_INDEX
+  const float uR = x >= g.nx - 1 ? 0.0f : ldf(u + i);
+  const float uL = x == 0 ? 0.0f : ldf(u + i - 1);
+  const float vU = (!ref && y >= g.ny - 1) ? 0.0f : ldf(v + i);
+  const float vD = y == 0 ? 0.0f : ldf(v + i - g.nx);
+  const float wF = z >= g.nz - 1 ? 0.0f : ldf(w + i);
+  const float wB = z == 0 ? 0.0f : ldf(w + i - (size_t)g.nx * g.ny);
+  const float cx = 0.5f * (uL + uR), cz = 0.5f * (wB + wF);
+  float cy = 0.5f * (vD + vU);
+  if (ref && (flags & DOB_PHYS_SURFACE) && y >= g.ny - 2 && cy < 0.0f) {
+    const StepParams& P = *Pp;
+    const dob_v3 dims = v3((float)g.nx, (float)g.ny, (float)g.nz);
+    const dob_v3 pCell = to_world(P, (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / dims);
+    float activeNeck = 0.0f;
+    for (int d = 0; d < kMaxDrops; ++d) {
+      if (drop(P, d, 7) > 0.0f && drop(P, d, 6) > 0.008f) {
+        const float rActive = dob_clampf(drop(P, d, 3) * 1.15f + 0.032f, 0.046f, 0.092f);
+        const float rDist = length2f(pCell.x - drop(P, d, 0), pCell.z - drop(P, d, 2));
+        const float drainGate = dob_smoothstep(0.008f, 0.065f, drop(P, d, 6));
+        activeNeck = dob_maxf(activeNeck, (1.0f - dob_smoothstep(rActive * 0.78f, rActive * 1.20f, rDist)) * drainGate);
+      }
+    }
+    const float stagGate = dob_mix(0.45f, 1.0f, dob_smoothstep(0.002f, 0.018f, dob_maxf(0.0f, P.U[40] - pCell.y)));
+    cy = cy * dob_mix(stagGate, 1.0f, activeNeck);
+  }
+  st4(cen + i, make_float4(cx, cy, cz, 0.0f));
+}
+
+// ---- FLUID_CURL (fluid.ts:331-369) ----------------------------------------------------------
+template <class V4>
+__device__ __forceinline__ float4 ldc4(const Grid& g, const V4* a, int x, int y, int z) {
+  return ld4(a + g.at(dob_clampi(x, 0, g.nx - 1), dob_clampi(y, 0, g.ny - 1), dob_clampi(z, 0, g.nz - 1)));
+}
+template <class VS>
+__global__ void __launch_bounds__(256) k_curl(Grid g, const typename Vec4Of<VS>::type* __restrict__ cen,
+                                              typename Vec4Of<VS>::type* __restrict__ curl) {
+  CELL_INDEX
+  const float4 vR = ldc4(g, cen, x + 1, y, z), vL = ldc4(g, cen, x - 1, y, z);
+  const float4 vU = ldc4(g, cen, x, y + 1, z), vD = ldc4(g, cen, x, y - 1, z);
+  const float4 vF = ldc4(g, cen, x, y, z + 1), vB = ldc4(g, cen, x, y, z - 1);
+  const dob_v3 om = 0.5f * v3((vU.z - vD.z) - (vF.y - vB.y), (vF.x - vB.x) - (vR.z - vL.z), (vR.y - vL.y) - (vU.x - vD.x));
+  const float mag = length3(om);
+  st4(curl + i, make_float4(om.x, om.y, om.z, mag));
+}
+
+// ---- FLUID_CASSON_FORCES (fluid.ts:377-511) ------------------------------------------------
+template <class VS>
+__device__ __forceinline__ dob_v3 ldmac(const Grid& g, const VS* u, const VS* v, const VS* w, int x, int y, int z) {
+  const size_t j = g.at(dob_clampi(x, 0, g.nx - 1), dob_clampi(y, 0, g.ny - 1), dob_clampi(z, 0, g.nz - 1));
+  return v3(ldf(u + j), ldf(v + j), ldf(w + j));
+}
+template <class V4>
+__device__ __forceinline__ dob_v3 vort_conf(const Grid& g, const V4* curl, int ix, int iy, int iz, float vc) {
+  if (ix <= 1 || ix >= g.nx - 2 || iy <= 1 || iy >= g.ny - 3 || iz <= 1 || iz >= g.nz - 2) return v3(0.0f, 0.0f, 0.0f);
+  const float4 c = ld4(curl + g.at(ix, iy, iz));
+  const dob_v3 omega = v3(c.x, c.y, c.z);
+  const float omegaMag = c.w;
+  if (omegaMag <= 0.18f) return v3(0.0f, 0.0f, 0.0f);
+  const float ringGate = dob_smoothstep(0.18f, 0.95f, omegaMag) / (1.0f + 0.28f * omegaMag);
+  const dob_v3 eta = 0.5f * v3(ldc4(g, curl, ix + 1, iy, iz).w - ldc4(g, curl, ix - 1, iy, iz).w,
+                               ldc4(g, curl, ix, iy + 1, iz).w - ldc4(g, curl, ix, iy - 1, iz).w,
+                               ldc4(g, curl, ix, iy, iz + 1).w - ldc4(g, curl, ix, iy, iz - 1).w);
+  const float etaLen = length3(eta);
+  if (etaLen <= 1e-5f) return v3(0.0f, 0.0f, 0.0f);
+  return (vc * ringGate) * cross3(eta / etaLen, omega);
+}
+template <class DS>
+__device__ __forceinline__ dob_v3 sample_conc_rg(const Grid& gc, const typename Vec4Of<DS>::type* conc4, dob_v3 uvw) {
+  const Taps t = make_taps(gc, uvw.x, uvw.y, uvw.z);
+  const float4 r = lerp8x4(t, conc4);
+  return v3(r.x, r.y, 0.0f);
+}
+
+template <class VS, class DS>
+__global__ void __launch_bounds__(256) k_casson(Grid g, Grid gc, const StepParams* __restrict__ Pp, int ref, int flags,
+                                                const VS* __restrict__ u, const VS* __restrict__ v,
+                                                const VS* __restrict__ w,
+                                                const typename Vec4Of<VS>::type* __restrict__ curl,
+                                                const typename Vec4Of<DS>::type* __restrict__ conc4,
+                                                const DS* __restrict__ dye, VS* __restrict__ uo, VS* __restrict__ vo,
+                                                VS* __restrict__ wo) {
+  CELL_INDEX
+  const StepParams& P = *Pp;
+  const dob_v3 dims = v3((float)g.nx, (float)g.ny, (float)g.nz);
+  const float dtv = P.dt;
+  dob_v3 mac = v3(ldf(u + i), ldf(v + i), ldf(w + i));
+  const dob_v3 mXp = ldmac(g, u, v, w, x + 1, y, z), mXn = ldmac(g, u, v, w, x - 1, y, z);
+  const dob_v3 mYp = ldmac(g, u, v, w, x, y + 1, z), mYn = ldmac(g, u, v, w, x, y - 1, z);
+  const dob_v3 mZp = ldmac(g, u, v, w, x, y, z + 1), mZn = ldmac(g, u, v, w, x, y, z - 1);
+  const dob_v3 uvwCell = (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / dims;
+  const dob_v3 du = mXp - mXn, dv = mYp - mYn, dw = mZp - mZn;
+  const dob_v3 lapMac = (mXp + mXn + mYp + mYn + mZp + mZn) - 6.0f * mac;
+  if (ref) {
+    const dob_v3 concCell = sample_conc_rg<DS>(gc, conc4, uvwCell);
+    const float cRbc = dob_clampf(concCell.x, 0.0f, 1.5f);
+    const float shearRate = 50.0f * dob_sqrt(dot3(du, du) + dot3(dv, dv) + dot3(dw, dw) + 1e-6f);
+    const float cassonScale = P.U[58];
+    const float sqrtMuInf = dob_sqrt(0.00010f * (1.0f + 1.35f * cRbc));
+    const float tauYield = 0.0036f * cassonScale * cRbc * cRbc;
+    const float sqrtYieldTerm = dob_sqrt(tauYield / dob_maxf(shearRate + 0.40f, 0.40f));
+    const float alpha = dob_clampf((sqrtMuInf + sqrtYieldTerm) * (sqrtMuInf + sqrtYieldTerm), 0.00010f, 0.0044f);
+    mac = mac + alpha * lapMac;
+    if (flags & DOB_PHYS_VORT_CONF) {
+      const float vcs = P.U[44];
+      const dob_v3 vc0 = vort_conf(g, curl, x, y, z, vcs);
+      const float vcX = 0.5f * (vc0.x + vort_conf(g, curl, min(x + 1, g.nx - 1), y, z, vcs).x);
+      const float vcY = 0.5f * (vc0.y + vort_conf(g, curl, x, min(y + 1, g.ny - 1), z, vcs).y);
+      const float vcZ = 0.5f * (vc0.z + vort_conf(g, curl, x, y, min(z + 1, g.nz - 1), vcs).z);
+      mac = mac + v3(vcX, vcY, vcZ) * dtv;
+    }
+    if (flags & DOB_PHYS_BUOYANCY) {
+      const dob_v3 uvwFaceY = v3((float)x + 0.5f, (float)y + 1.0f, (float)z + 0.5f) / dims;
+      const dob_v3 cf = sample_conc_rg<DS>(gc, conc4, clamp3(uvwFaceY, 0.001f, 0.999f));
+      const float buoyDensity = 1.24f * cf.x + 0.26f * cf.y;
+      if (buoyDensity > 0.0008f) {
+        const dob_v3 pFaceY = to_world(P, uvwFaceY);
+        const float surfBuoyGate = dob_smoothstep(0.002f, 0.024f, dob_maxf(0.0f, P.U[40] - pFaceY.y));
+        const float effBuoyConc = 1.24f * dob_tanh(buoyDensity / 1.24f);
+        const float buoyAccel = -P.U[45] * 0.345f * effBuoyConc * surfBuoyGate;
+        mac.y = mac.y + buoyAccel * dtv;
+      }
+    }
+    if (flags & DOB_PHYS_SOLENOIDAL) {
+      const dob_v3 pc = to_world(P, uvwCell);
+      const float depthBelow = P.U[40] - pc.y;
+      const float unfurlGate = dob_smoothstep(0.11f, 0.36f, depthBelow) * dob_smoothstep(0.0008f, 0.015f, cRbc + 0.45f * concCell.y);
+      if (unfurlGate > 0.001f) {
+        const float tSwirl = P.U[35] * 0.36f + P.U[60] * 1.7f;
+        const float q1 = 6.4f * pc.x + 4.0f * pc.y + 5.2f * pc.z + tSwirl;
+        const float q2 = -5.6f * pc.x + 4.8f * pc.y + 7.2f * pc.z - tSwirl * 0.77f;
+        const float q3 = 9.0f * pc.x - 6.0f * pc.y - 6.4f * pc.z + tSwirl * 1.13f;
+        const float c1 = dob_cos(q1), c2 = dob_cos(q2), s3 = 0.42f * dob_sin(q3);
+        const dob_v3 sf = v3(-6.25f, 2.85f, 5.50f) * c1 + v3(-6.30f, -1.26f, -4.06f) * c2 + v3(6.40f, -0.96f, 9.90f) * s3;
+        const float vertMod = dob_smoothstep(0.16f, 0.42f, depthBelow);
+        mac = mac + v3(sf.x, sf.y * vertMod, sf.z) * (0.0028f * unfurlGate * dtv);
+      }
+    }
+    mac = clamp3(mac, -1.8f, 1.8f);
+  } else {
+    // Closed box: nu = (sqrt(mu_p) + sqrt(tau_y c^2 / (gdot + 0.4)))^2, explicit
+    // u += min(nu dt / dx^2, 1/8) lap u.
+    const float cval = gc.nx == g.nx ? ldf(dye + i) : lerp8(make_taps(gc, uvwCell.x, uvwCell.y, uvwCell.z), dye);
+    const float c = dob_clampf(cval, 0.0f, 1.5f);
+    const float dxv = P.dx;
+    const float gdot = dob_sqrt(dot3(du, du) + dot3(dv, dv) + dot3(dw, dw)) / (2.0f * dxv);
+    const float sqrtMu = dob_sqrt(P.mu_p);
+    const float sqrtYield = dob_sqrt(P.tau_y * c * c / (gdot + 0.4f));
+    const float nu = (sqrtMu + sqrtYield) * (sqrtMu + sqrtYield);
+    const float alpha = dob_minf(nu * dtv / (dxv * dxv), 0.125f);
+    mac = mac + alpha * lapMac;
+  }
+  if (x >= g.nx - 1) mac.x = 0.0f;
+  if (z >= g.nz - 1) mac.z = 0.0f;
+  if (!ref && y >= g.ny - 1) mac.y = 0.0f;
+  stf(uo + i, mac.x); stf(vo + i, mac.y); stf(wo + i, mac.z);
+}
+
+// ---- FLUID_MAC_RHS (fluid.ts:517-555) with the FP64 compatibility sum ---------------------
+template <class VS>
+__global__ void __launch_bounds__(256) k_mac_rhs(Grid g, const StepParams* __restrict__ Pp, int ref,
+                                                 const VS* __restrict__ u, const VS* __restrict__ v,
+                                                 const VS* __restrict__ w, const float4* __restrict__ wave,
+                                                 float* __restrict__ rhs, double* __restrict__ sum) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  double part = 0.0;
+  if (x < g.nx && y < g.ny) {
+    const size_t i = g.at(x, y, z);
+    const float uRight = x >= g.nx - 1 ? 0.0f : ldf(u + i);
+    const float uLeft = x == 0 ? 0.0f : ldf(u + i - 1);
+    const float vTop = (!ref && y >= g.ny - 1) ? 0.0f : ldf(v + i);
+    const float vBot = y == 0 ? 0.0f : ldf(v + i - g.nx);
+    const float wFront = z >= g.nz - 1 ? 0.0f : ldf(w + i);
+    const float wBack = z == 0 ? 0.0f : ldf(w + i - (size_t)g.nx * g.ny);
+    float r = (uRight - uLeft) + (vTop - vBot) + (wFront - wBack);
+    if (ref && y == g.ny - 1) r = r - top_pressure(g, *Pp, wave, x, z);
+    rhs[i] = r;
+    part = (double)r;
+  }
+  if (sum) block_sum_atomic(part, sum);
+}
+
+// ---- FLUID_MAC_PROJECT (fluid.ts:863-911), in place ----------------------------------------
+template <class VS>
+__global__ void __launch_bounds__(256) k_project(Grid g, const StepParams* __restrict__ Pp, int ref, VS* u, VS* v, VS* w,
+                                                 const float* __restrict__ p, const float4* __restrict__ wave) {
+  CELL_INDEX
+  float mx = ldv(u + i), my = ldv(v + i), mz = ldv(w + i);
+  const float pC = p[i];
+  if (x < g.nx - 1) mx = mx - (p[i + 1] - pC); else mx = 0.0f;
+  if (y < g.ny - 1) my = my - (p[i + g.nx] - pC);
+  else if (ref) my = my - (top_pressure(g, *Pp, wave, x, z) - pC);
+  else my = 0.0f;
+  if (z < g.nz - 1) mz = mz - (p[i + (size_t)g.nx * g.ny] - pC); else mz = 0.0f;
+  if (ref) {
+    mx = dob_clampf(mx, -2.0f, 2.0f); my = dob_clampf(my, -2.0f, 2.0f); mz = dob_clampf(mz, -2.0f, 2.0f);
+  }
+  stf(u + i, mx); stf(v + i, my); stf(w + i, mz);
+}
+
+// ---- divergence field and its max (statistics) -----------------------------------------
+template <class VS>
+__global__ void __launch_bounds__(256) k_divergence(Grid g, int ref, const VS* __restrict__ u, const VS* __restrict__ v,
+                                                    const VS* __restrict__ w, float* __restrict__ out,
+                                                    float scale, unsigned int* __restrict__ maxbits) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  float m = 0.0f;
+  if (x < g.nx && y < g.ny) {
+    const size_t i = g.at(x, y, z);
+    const float uRight = x >= g.nx - 1 ? 0.0f : ldf(u + i);
+    const float uLeft = x == 0 ? 0.0f : ldf(u + i - 1);
+    const float vTop = (!ref && y >= g.ny - 1) ? 0.0f : ldf(v + i);
+    const float vBot = y == 0 ? 0.0f : ldf(v + i - g.nx);
+    const float wFront = z >= g.nz - 1 ? 0.0f : ldf(w + i);
+    const float wBack = z == 0 ? 0.0f : ldf(w + i - (size_t)g.nx * g.ny);
+    const float d = (uRight - uLeft) + (vTop - vBot) + (wFront - wBack);
+    if (out) out[i] = d;
+    if (!(ref && y == g.ny - 1)) m = fabsf(d) * scale;
+  }
+  if (maxbits) block_max_atomic(m, maxbits);
+}
+
+// ---- CONC_PREDICT (advect.ts:28-72) -----------------------------------------------------------
+template <class VS, class DS>
+__global__ void __launch_bounds__(256) k_conc_predict(Grid gc, Grid g, const StepParams* __restrict__ Pp, int ref,
+                                                      const typename Vec4Of<VS>::type* __restrict__ cen,
+                                                      const typename Vec4Of<DS>::type* __restrict__ conc4,
+                                                      const DS* __restrict__ dye, DS* __restrict__ pred) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  if (x >= gc.nx || y >= gc.ny) return;
+  const size_t i = gc.at(x, y, z);
+  const StepParams& P = *Pp;
+  const dob_v3 dims = v3((float)gc.nx, (float)gc.ny, (float)gc.nz);
+  const float dtv = P.dt;
+  const dob_v3 dom = dsize_of(P);
+  const dob_v3 uvw = (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / dims;
+  if (ref) {
+    if (x == 0 || x >= gc.nx - 1 || z == 0 || z >= gc.nz - 1 || y >= gc.ny - 1) { stf(pred + i, 0.0f); return; }
+    const dob_v3 v0 = sample_center(g, cen, uvw);
+    const float speed2 = dot3(v0, v0);
+    if (speed2 < 2.5e-5f) { stf(pred + i, ld4(conc4 + i).y); return; }
+    dob_v3 back;
+    if (speed2 < 0.012f) {
+      back = clamp3(uvw - (v0 * dtv) / dom, 0.001f, 0.999f);
+    } else {
+      const dob_v3 mid = clamp3(uvw - (0.5f * (v0 * dtv)) / dom, 0.001f, 0.999f);
+      const dob_v3 vMid = sample_center(g, cen, mid);
+      back = clamp3(uvw - (vMid * dtv) / dom, 0.001f, 0.999f);
+    }
+    const Taps t = make_taps(gc, back.x, back.y, back.z);
+    stf(pred + i, lerp8x4(t, conc4).y);
+  } else {
+    const dob_v3 v0 = sample_center(g, cen, uvw);
+    const dob_v3 mid = clamp3(uvw - (0.5f * (v0 * dtv)) / dom, 0.001f, 0.999f);
+    const dob_v3 vMid = sample_center(g, cen, mid);
+    const dob_v3 back = clamp3(uvw - (vMid * dtv) / dom, 0.001f, 0.999f);
+    stf(pred + i, lerp8(make_taps(gc, back.x, back.y, back.z), dye));
+  }
+}
+
+// ---- CONC_RESOLVE (advect.ts:81-298) ------------------------------------------------------------
+template <class S>
+__device__ __forceinline__ float ldcs(const Grid& gc, const S* a, int x, int y, int z) {
+  return ldf(a + gc.at(dob_clampi(x, 0, gc.nx - 1), dob_clampi(y, 0, gc.ny - 1), dob_clampi(z, 0, gc.nz - 1)));
+}
+template <class V4>
+__device__ __forceinline__ float4 ldc4v(const Grid& gc, const V4* a, int x, int y, int z) {
+  return ld4(a + gc.at(dob_clampi(x, 0, gc.nx - 1), dob_clampi(y, 0, gc.ny - 1), dob_clampi(z, 0, gc.nz - 1)));
+}
+__device__ __forceinline__ float intact_raw(const Grid& gc, const uint32_t* s, int x, int y, int z) {
+  return (float)__ldg(s + gc.at(dob_clampi(x, 0, gc.nx - 1), dob_clampi(y, 0, gc.ny - 1), dob_clampi(z, 0, gc.nz - 1))) * kSplatInv;
+}
+
+template <class VS, class DS>
+__global__ void __launch_bounds__(256) k_conc_resolve_ref(Grid gc, Grid g, const StepParams* __restrict__ Pp,
+                                                          const typename Vec4Of<VS>::type* __restrict__ cen,
+                                                          const typename Vec4Of<DS>::type* __restrict__ conc,
+                                                          const DS* __restrict__ pred,
+                                                          const uint32_t* __restrict__ splatI,
+                                                          const uint32_t* __restrict__ splatL,
+                                                          typename Vec4Of<DS>::type* __restrict__ out) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  if (x >= gc.nx || y >= gc.ny) return;
+  const size_t i = gc.at(x, y, z);
+  if (x == 0 || x >= gc.nx - 1 || z == 0 || z >= gc.nz - 1 || y >= gc.ny - 1) {
+    st4(out + i, make_float4(0.f, 0.f, 0.f, 0.f));
+    return;
+  }
+  const StepParams& P = *Pp;
+  const dob_v3 dims = v3((float)gc.nx, (float)gc.ny, (float)gc.nz);
+  const uint32_t rawIntact = __ldg(splatI + i), rawLysed = __ldg(splatL + i);
+  const bool inFloorZone = y <= 7;
+  if (rawIntact == 0u && rawLysed == 0u) {
+    const dob_v3 g0 = v3((float)x, (float)y, (float)z) / dims;
+    const dob_v3 g1 = (v3((float)x, (float)y, (float)z) + v3(1.0f, 1.0f, 1.0f)) / dims;
+    const float oct0 = lerp8(make_taps(gc, g0.x, g0.y, g0.z), pred);
+    const float oct1 = lerp8(make_taps(gc, g1.x, g1.y, g1.z), pred);
+    float bedActive = 0.0f;
+    if (inFloorZone) {
+      const dob_v3 gh = (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / dims;
+      bedActive = lerp8x4(make_taps(gc, gh.x, gh.y, gh.z), conc).w;
+    }
+    if (oct0 + oct1 <= 1.0e-7f && bedActive <= 1.0e-6f) {
+      st4(out + i, make_float4(0.f, 0.f, 0.f, 0.f));
+      return;
+    }
+  }
+  const float gPred = ldf(pred + i);
+  const float lapNeighborsG = (ldcs(gc, pred, x + 1, y, z) + ldcs(gc, pred, x - 1, y, z) + ldcs(gc, pred, x, y + 1, z) +
+                               ldcs(gc, pred, x, y - 1, z) + ldcs(gc, pred, x, y, z + 1) + ldcs(gc, pred, x, y, z - 1)) *
+                              (1.0f / 6.0f);
+  if (!inFloorZone && rawIntact == 0u && rawLysed == 0u && gPred <= 1.2e-6f && lapNeighborsG <= 1.2e-6f) {
+    st4(out + i, make_float4(0.f, 0.f, 0.f, 0.f));
+    return;
+  }
+  float lapIntact = 0.0f;
+  if (rawIntact > 0u || gPred > 8.0e-5f || lapNeighborsG > 8.0e-5f)
+    lapIntact = (intact_raw(gc, splatI, x + 1, y, z) + intact_raw(gc, splatI, x - 1, y, z) + intact_raw(gc, splatI, x, y + 1, z) +
+                 intact_raw(gc, splatI, x, y - 1, z) + intact_raw(gc, splatI, x, y, z + 1) + intact_raw(gc, splatI, x, y, z - 1)) *
+                (1.0f / 6.0f);
+  const dob_v3 uvw = (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / dims;
+  const float dtv = P.dt;
+  const dob_v3 dom = dsize_of(P);
+  const dob_v3 pw = to_world(P, uvw);
+  const float halfXZ = P.U[52], yMin = P.U[53];
+  const dob_v3 v0 = sample_center(g, cen, uvw);
+  const dob_v3 uvwMid = clamp3(uvw - (0.5f * (v0 * dtv)) / dom, 0.001f, 0.999f);
+  const dob_v3 vMid = sample_center(g, cen, uvwMid);
+  const dob_v3 uvwBack = clamp3(uvw - (vMid * dtv) / dom, 0.001f, 0.999f);
+  const dob_v3 uvwFwd = clamp3(uvw + (v0 * dtv) / dom, 0.001f, 0.999f);
+  const float gBackEst = lerp8(make_taps(gc, uvwFwd.x, uvwFwd.y, uvwFwd.z), pred);
+  const float4 orig = ld4(conc + i);
+  const float gOrig = orig.y;
+  const float gCorr = gPred + (0.45f * P.U[47]) * (gOrig - gBackEst);
+  const dob_v3 tc = uvwBack * dims - v3(0.5f, 0.5f, 0.5f);
+  const int bx = (int)floorf(tc.x), by = (int)floorf(tc.y), bz = (int)floorf(tc.z);
+  const float s000 = ldc4v(gc, conc, bx, by, bz).y, s100 = ldc4v(gc, conc, bx + 1, by, bz).y;
+  const float s010 = ldc4v(gc, conc, bx, by + 1, bz).y, s110 = ldc4v(gc, conc, bx + 1, by + 1, bz).y;
+  const float s001 = ldc4v(gc, conc, bx, by, bz + 1).y, s101 = ldc4v(gc, conc, bx + 1, by, bz + 1).y;
+  const float s011 = ldc4v(gc, conc, bx, by + 1, bz + 1).y, s111 = ldc4v(gc, conc, bx + 1, by + 1, bz + 1).y;
+  const float minG = dob_minf(dob_minf(dob_minf(s000, s100), dob_minf(s010, s110)), dob_minf(dob_minf(s001, s101), dob_minf(s011, s111)));
+  const float maxG = dob_maxf(dob_maxf(dob_maxf(s000, s100), dob_maxf(s010, s110)), dob_maxf(dob_maxf(s001, s101), dob_maxf(s011, s111)));
+  float cLysed = dob_clampf(gCorr, minG, maxG);
+  const float diffBlend = dob_clampf(dtv * 5.60f, 0.0f, 0.105f);
+  cLysed = dob_mix(cLysed, lapNeighborsG, diffBlend);
+  const float upperDilute = dob_exp(-dtv * dob_mix(0.016f, 0.034f, dob_smoothstep(yMin + 0.045f, yMin + 0.26f, pw.y)));
+  cLysed = cLysed * upperDilute;
+  const float dmTransfer = (float)rawLysed * kSplatInv;
+  const float floorBedCapture = 1.0f - dob_smoothstep(yMin + 0.018f, yMin + 0.058f, pw.y);
+  cLysed = cLysed + dmTransfer * (1.0f - floorBedCapture * 0.72f);
+  if (cLysed < 2.5e-6f) cLysed = 0.0f;
+  const float rHoriz = length2f(pw.x, pw.z);
+  float cBed = 0.0f;
+  if (inFloorZone) {
+    const float bCenter = orig.w;
+    const float bHoriz = 0.25f * (ldc4v(gc, conc, x + 1, y, z).w + ldc4v(gc, conc, x - 1, y, z).w +
+                                  ldc4v(gc, conc, x, y, z + 1).w + ldc4v(gc, conc, x, y, z - 1).w);
+    const float bAbove = ldc4v(gc, conc, x, y + 1, z).w;
+    const float bBelow = ldc4v(gc, conc, x, max(0, y - 1), z).w;
+    const float spreadAlpha = dob_clampf(dtv * (3.20f + 6.50f * dob_minf(bCenter, 0.65f)), 0.0f, 0.165f);
+    const float vertDiffuse = dob_clampf(dtv * 0.75f, 0.0f, 0.026f);
+    const float settleAlpha = dob_clampf(dtv * 2.80f, 0.0f, 0.090f);
+    const float bedDecay = dob_exp(-dtv * dob_mix(0.095f, 0.28f, dob_smoothstep(halfXZ * 0.35f, halfXZ * 0.78f, rHoriz)));
+    const float drainedSelf = (y == 0 ? bCenter : bCenter * (1.0f - settleAlpha)) * bedDecay;
+    const float settledFromAbove = y >= 7 ? 0.0f : bAbove * settleAlpha;
+    const float advectedBed = drainedSelf + settledFromAbove;
+    const float smoothedBed = dob_mix(dob_mix(advectedBed, bHoriz, spreadAlpha), 0.5f * (bAbove + bBelow), vertDiffuse);
+    const float topBedFade = 1.0f - 0.38f * dob_smoothstep(3.5f, 7.0f, (float)y);
+    cBed = (smoothedBed + dmTransfer * floorBedCapture * 0.68f) * topBedFade;
+    if (cBed < 1.0e-6f) cBed = 0.0f;
+  }
+  const float wallSponge = 1.0f - dob_smoothstep(halfXZ * 0.68f, halfXZ * 0.94f, rHoriz);
+  const float floorRadialTaper = 1.0f - dob_smoothstep(halfXZ * 0.52f, halfXZ * 0.88f, rHoriz);
+  const float maxBedProfile = 0.54f * dob_exp(-0.56f * (float)y) * floorRadialTaper;
+  cBed = dob_minf(cBed * wallSponge, maxBedProfile);
+  const float cParcelRaw = (float)rawIntact * kSplatInv;
+  const float shoulderFeather = rawIntact > 0u ? 0.36f : 0.18f;
+  const float cParcelIntact = dob_mix(cParcelRaw, lapIntact, shoulderFeather) * wallSponge;
+  const float cIntact = cParcelIntact + cBed;
+  cLysed = cLysed * wallSponge;
+  const float cTotal = cIntact + cLysed;
+  float vOx = 0.0f;
+  if (cTotal > 1.0e-5f) {
+    const float fLysis = dob_clampf(cLysed / dob_maxf(cTotal, 1.0e-5f), 0.0f, 1.0f);
+    const float intactFrac = 1.0f - fLysis;
+    const float bedFrac = dob_smoothstep(0.0f, 0.85f, cBed / dob_maxf(cTotal, 1.0e-5f));
+    const float flowSpeed = length3(v0);
+    const float convShear = length3(v0 - vMid) / dob_maxf(0.5f * dtv, 1.0e-3f);
+    const float shearDispersion = dob_smoothstep(0.014f, 0.135f, flowSpeed + 0.38f * convShear);
+    const float thinIntactSheet = (1.0f - dob_smoothstep(0.024f, 0.24f, cIntact)) * dob_smoothstep(0.0006f, 0.0065f, cIntact);
+    const float activeSheet = thinIntactSheet * (0.38f + 0.62f * shearDispersion) * intactFrac;
+    const float rawOx = dob_clampf(0.08f + 0.62f * activeSheet + 0.36f * shearDispersion * intactFrac, 0.0f, 1.0f);
+    vOx = rawOx * (1.0f - 0.82f * bedFrac);
+  }
+  st4(out + i, make_float4(cIntact, cLysed, vOx, cBed));
+}
+
+// Closed box: MacCormack correction of the single dye, 8-tap min/max limiter.
+template <class VS, class DS>
+__global__ void __launch_bounds__(256) k_dye_resolve_box(Grid gc, Grid g, const StepParams* __restrict__ Pp,
+                                                         const typename Vec4Of<VS>::type* __restrict__ cen,
+                                                         const DS* __restrict__ dye, const DS* __restrict__ pred,
+                                                         DS* __restrict__ out) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  if (x >= gc.nx || y >= gc.ny) return;
+  const size_t i = gc.at(x, y, z);
+  const StepParams& P = *Pp;
+  const dob_v3 dims = v3((float)gc.nx, (float)gc.ny, (float)gc.nz);
+  const float dtv = P.dt;
+  const dob_v3 dom = dsize_of(P);
+  const dob_v3 uvw = (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / dims;
+  const dob_v3 v0 = sample_center(g, cen, uvw);
+  const dob_v3 uvwMid = clamp3(uvw - (0.5f * (v0 * dtv)) / dom, 0.001f, 0.999f);
+  const dob_v3 vMid = sample_center(g, cen, uvwMid);
+  const dob_v3 uvwBack = clamp3(uvw - (vMid * dtv) / dom, 0.001f, 0.999f);
+  const dob_v3 uvwFwd = clamp3(uvw + (v0 * dtv) / dom, 0.001f, 0.999f);
+  const float gBackEst = lerp8(make_taps(gc, uvwFwd.x, uvwFwd.y, uvwFwd.z), pred);
+  const float gOrig = ldf(dye + i);
+  const float gCorr = ldf(pred + i) + (0.45f * P.sharp) * (gOrig - gBackEst);
+  const dob_v3 tc = uvwBack * dims - v3(0.5f, 0.5f, 0.5f);
+  const int bx = (int)floorf(tc.x), by = (int)floorf(tc.y), bz = (int)floorf(tc.z);
+  const float s000 = ldcs(gc, dye, bx, by, bz), s100 = ldcs(gc, dye, bx + 1, by, bz);
+  const float s010 = ldcs(gc, dye, bx, by + 1, bz), s110 = ldcs(gc, dye, bx + 1, by + 1, bz);
+  const float s001 = ldcs(gc, dye, bx, by, bz + 1), s101 = ldcs(gc, dye, bx + 1, by, bz + 1);
+  const float s011 = ldcs(gc, dye, bx, by + 1, bz + 1), s111 = ldcs(gc, dye, bx + 1, by + 1, bz + 1);
+  const float minG = dob_minf(dob_minf(dob_minf(s000, s100), dob_minf(s010, s110)), dob_minf(dob_minf(s001, s101), dob_minf(s011, s111)));
+  const float maxG = dob_maxf(dob_maxf(dob_maxf(s000, s100), dob_maxf(s010, s110)), dob_maxf(dob_maxf(s001, s101), dob_maxf(s011, s111)));
+  stf(out + i, dob_clampf(gCorr, minG, maxG));
+}
+
+// ---- host launchers ------------------------------------------------------------------------------
+static inline dim3 cell_grid(const Grid& g) { return dim3((g.nx + 31) / 32, (g.ny + 7) / 8, g.nz); }
+static inline dim3 cell_block() { return dim3(32, 8, 1); }
+
+
+
+void launch_init_vel(const DevState& s, cudaStream_t st) {
+  DOB_VEL_DISPATCH(s.prec, {
+    k_init_vel<VS><<<cell_grid(s.g), cell_block(), 0, st>>>(s.g, s.params, (VS*)s.u, (VS*)s.v, (VS*)s.w,
+                                                            (typename Vec4Of<VS>::type*)s.cen,
+                                                            (typename Vec4Of<VS>::type*)s.curl);
+  });
+}
+
+void launch_advect_mac(const DevState& s, cudaStream_t st) {
+  DOB_VEL_DISPATCH(s.prec, {
+    k_advect_mac<VS><<<cell_grid(s.g), cell_block(), 0, st>>>(
+        s.g, s.params, s.ref, s.flags, (const VS*)s.u, (const VS*)s.v, (const VS*)s.w,
+        (const typename Vec4Of<VS>::type*)s.cen, s.wave, (VS*)s.u2, (VS*)s.v2, (VS*)s.w2);
+  });
+}
+
+void launch_mac_to_center(const DevState& s, cudaStream_t st) {
+  DOB_VEL_DISPATCH(s.prec, {
+    k_mac_to_center<VS><<<cell_grid(s.g), cell_block(), 0, st>>>(s.g, s.params, s.ref, s.flags, (const VS*)s.u,
+                                                                 (const VS*)s.v, (const VS*)s.w,
+                                                                 (typename Vec4Of<VS>::type*)s.cen);
+  });
+}
+
+void launch_curl(const DevState& s, cudaStream_t st) {
+  DOB_VEL_DISPATCH(s.prec, {
+    k_curl<VS><<<cell_grid(s.g), cell_block(), 0, st>>>(s.g, (const typename Vec4Of<VS>::type*)s.cen,
+                                                        (typename Vec4Of<VS>::type*)s.curl);
+  });
+}
+
+void launch_casson(const DevState& s, cudaStream_t st) {
+  DOB_VEL_DISPATCH(s.prec, {
+    k_casson<VS, DS><<<cell_grid(s.g), cell_block(), 0, st>>>(
+        s.g, s.gc, s.params, s.ref, s.flags, (const VS*)s.u, (const VS*)s.v, (const VS*)s.w,
+        (const typename Vec4Of<VS>::type*)s.curl, (const typename Vec4Of<DS>::type*)s.conc, (const DS*)s.conc,
+        (VS*)s.u2, (VS*)s.v2, (VS*)s.w2);
+  });
+}
+
+void launch_mac_rhs(const DevState& s, cudaStream_t st) {
+  if (!s.ref) cudaMemsetAsync(s.red + RED_RHS_SUM, 0, sizeof(double), st);
+  DOB_VEL_DISPATCH(s.prec, {
+    k_mac_rhs<VS><<<cell_grid(s.g), cell_block(), 0, st>>>(s.g, s.params, s.ref, (const VS*)s.u, (const VS*)s.v,
+                                                           (const VS*)s.w, s.wave, s.rhs,
+                                                           s.ref ? nullptr : s.red + RED_RHS_SUM);
+  });
+  if (!s.ref) launch_sub_mean(s.rhs, s.g.n(), s.red + RED_RHS_SUM, s.num_sms, st);
+}
+
+void launch_project(const DevState& s, cudaStream_t st) {
+  DOB_VEL_DISPATCH(s.prec, {
+    k_project<VS><<<cell_grid(s.g), cell_block(), 0, st>>>(s.g, s.params, s.ref, (VS*)s.u, (VS*)s.v, (VS*)s.w, s.p,
+                                                           s.wave);
+  });
+}
+
+void launch_divergence(const DevState& s, float* out, float scale, unsigned int* maxbits, cudaStream_t st) {
+  DOB_VEL_DISPATCH(s.prec, {
+    k_divergence<VS><<<cell_grid(s.g), cell_block(), 0, st>>>(s.g, s.ref, (const VS*)s.u, (const VS*)s.v,
+                                                              (const VS*)s.w, out, scale, maxbits);
+  });
+}
+
+void launch_conc_predict(const DevState& s, cudaStream_t st) {
+  DOB_VEL_DISPATCH(s.prec, {
+    k_conc_predict<VS, DS><<<cell_grid(s.gc), cell_block(), 0, st>>>(
+        s.gc, s.g, s.params, s.ref, (const typename Vec4Of<VS>::type*)s.cen,
+        (const typename Vec4Of<DS>::type*)s.conc, (const DS*)s.conc, (DS*)s.pred);
+  });
+}
+
+void launch_conc_resolve(const DevState& s, cudaStream_t st) {
+  DOB_VEL_DISPATCH(s.prec, {
+    if (s.ref) {
+      k_conc_resolve_ref<VS, DS><<<cell_grid(s.gc), cell_block(), 0, st>>>(
+          s.gc, s.g, s.params, (const typename Vec4Of<VS>::type*)s.cen, (const typename Vec4Of<DS>::type*)s.conc,
+          (const DS*)s.pred, s.splatI, s.splatL, (typename Vec4Of<DS>::type*)s.conc2);
+    } else {
+      k_dye_resolve_box<VS, DS><<<cell_grid(s.gc), cell_block(), 0, st>>>(
+          s.gc, s.g, s.params, (const typename Vec4Of<VS>::type*)s.cen, (const DS*)s.conc, (const DS*)s.pred,
+          (DS*)s.conc2);
+    }
+  });
+}
+
+}  // namespace dob

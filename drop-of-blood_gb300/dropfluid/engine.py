@@ -1,0 +1,202 @@
+"""Host-side mirror of the reference engine's physics interface.
+
+``DropFluid`` owns one libdropfluid context (all device memory of one
+simulation) and exposes the operations the reference's ``BloodDropEngine``
+performs for the fluid path (src/engine/BloodDropEngine.ts):
+
+  reference                                   here
+  ------------------------------------------  ------------------------------------
+  BloodDropEngine.create(canvas)  :336        DropFluid(config)
+  resetSimulation(seed, offsetXZ) :1682       reset()  (+ set_uniforms for the seed)
+  queue.writeBuffer(uniforms)     :2602       set_uniforms(block)
+  encodePhysicsStep(enc, spawn)   :1855       step()
+  seekToSimTime / multi-substep   :2142,2634  step_uniforms(blocks)
+  gpuPassTimingsMs (timestamps)   :2400       time_steps(), stats['stage_ms']
+  destroy()                       :2671       close()
+
+Errors follow the reference's engine contract: construction raises, later
+calls raise ``DropFluidError`` carrying the library's status and message.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+from ._lib import DropFluidError, check, load
+
+
+def _fptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+class DropFluid:
+    def __init__(self, config: abi.DobConfig):
+        self._L = load()
+        self.cfg = config.copy()
+        h = C.c_void_p()
+        rc = self._L.dob_create(C.byref(self.cfg), C.byref(h))
+        if rc != 0:
+            msg = self._L.dob_last_error(None)
+            raise DropFluidError(rc, "dob_create", msg.decode() if msg else "")
+        self._h = h
+        r = config.dye_refine
+        self.vdims = (config.nz, config.ny, config.nx)
+        self.cdims = (config.nz * r, config.ny * r, config.nx * r)
+
+    # -- lifecycle ---------------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.dob_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, rc, what):
+        check(rc, what, self._h)
+
+    # -- state ----------------------------------------------------------------------
+    def reset(self):
+        self._ck(self._L.dob_reset(self._h), "dob_reset")
+
+    def set_uniforms(self, block):
+        u = np.ascontiguousarray(block, dtype=np.float32)
+        if u.size != 128:
+            raise ValueError("the uniform block has 128 floats (512 bytes)")
+        self._ck(self._L.dob_set_uniforms(self._h, _fptr(u)), "dob_set_uniforms")
+
+    def inject_sphere(self, center, radius, dye, vel, noise_sigma=0.0, seed=0):
+        c = np.asarray(center, dtype=np.float32)
+        v = np.asarray(vel, dtype=np.float32)
+        self._ck(self._L.dob_inject_sphere(self._h, _fptr(c), float(radius), float(dye), _fptr(v),
+                                           float(noise_sigma), int(seed)), "dob_inject_sphere")
+
+    def set_parcels(self, parcels, offset=0):
+        p = np.ascontiguousarray(parcels, dtype=np.float32).reshape(-1, abi.PARCEL_FLOATS)
+        self._ck(self._L.dob_set_parcels(self._h, _fptr(p), p.shape[0], int(offset)), "dob_set_parcels")
+
+    def get_parcels(self, n=None, offset=0):
+        n = self.cfg.parcel_capacity - offset if n is None else n
+        out = np.empty((n, abi.PARCEL_FLOATS), dtype=np.float32)
+        self._ck(self._L.dob_get_parcels(self._h, _fptr(out), n, int(offset)), "dob_get_parcels")
+        return out
+
+    def set_high_water(self, hw):
+        self._ck(self._L.dob_set_high_water(self._h, int(hw)), "dob_set_high_water")
+
+    def field_shape(self, field):
+        nz, ny, nx = self.vdims
+        cz, cy, cx = self.cdims
+        ref = self.cfg.bc_mode == abi.DOB_BC_REFERENCE
+        return {
+            abi.FIELD_VEL_U: ((nz, ny, nx), np.float32),
+            abi.FIELD_VEL_V: ((nz, ny, nx), np.float32),
+            abi.FIELD_VEL_W: ((nz, ny, nx), np.float32),
+            abi.FIELD_VEL_CENTER: ((nz, ny, nx, 4), np.float32),
+            abi.FIELD_CURL: ((nz, ny, nx, 4), np.float32),
+            abi.FIELD_PRESSURE: ((nz, ny, nx), np.float32),
+            abi.FIELD_RHS: ((nz, ny, nx), np.float32),
+            abi.FIELD_CONC: (((cz, cy, cx, 4) if ref else (cz, cy, cx)), np.float32),
+            abi.FIELD_CONC_PRED: ((cz, cy, cx), np.float32),
+            abi.FIELD_SPLAT_INTACT: ((cz, cy, cx), np.uint32),
+            abi.FIELD_SPLAT_LYSED: ((cz, cy, cx), np.uint32),
+            abi.FIELD_WAVE: ((abi.WAVE_N, abi.WAVE_N, 4), np.float32),
+            abi.FIELD_DIVERGENCE: ((nz, ny, nx), np.float32),
+        }[field]
+
+    def set_field(self, field, arr):
+        shape, dt = self.field_shape(field)
+        a = np.ascontiguousarray(arr, dtype=dt).reshape(shape)
+        self._ck(self._L.dob_set_field(self._h, int(field), a.ctypes.data, a.nbytes), "dob_set_field")
+
+    def get_field(self, field):
+        shape, dt = self.field_shape(field)
+        a = np.empty(shape, dtype=dt)
+        self._ck(self._L.dob_get_field(self._h, int(field), a.ctypes.data, a.nbytes), "dob_get_field")
+        return a
+
+    # -- stepping ----------------------------------------------------------------------
+    def step(self, n=1, stats=False, timing=False, graph=True):
+        flags = (abi.STEP_STATS if stats else 0) | (abi.STEP_TIMING if timing else 0) | \
+                (0 if graph else abi.STEP_NO_GRAPH)
+        st = abi.DobStepStats()
+        want = stats or timing
+        self._ck(self._L.dob_step(self._h, int(n), flags, C.byref(st) if want else None), "dob_step")
+        if not want:
+            return None
+        return {
+            "steps_done": st.steps_done, "vcycles": st.vcycles, "outer_iters": st.outer_iters,
+            "rhs_l2": st.rhs_l2, "residual_l2": st.residual_l2, "max_div": st.max_div,
+            "parcels_alive": st.parcels_alive,
+            "stage_ms": {abi.STAGE_NAMES[k]: st.stage_ms[k] for k in range(abi.STAGE_COUNT)},
+        }
+
+    def step_uniforms(self, blocks, stats=False):
+        b = np.ascontiguousarray(blocks, dtype=np.float32).reshape(-1, 128)
+        st = abi.DobStepStats()
+        flags = abi.STEP_STATS if stats else 0
+        self._ck(self._L.dob_step_uniforms(self._h, _fptr(b), b.shape[0], flags,
+                                           C.byref(st) if stats else None), "dob_step_uniforms")
+
+    def run_stage(self, stage):
+        self._ck(self._L.dob_run_stage(self._h, int(stage)), f"dob_run_stage({stage})")
+
+    def sync(self):
+        self._ck(self._L.dob_sync(self._h), "dob_sync")
+
+    def memory_bytes(self) -> int:
+        b = C.c_uint64()
+        self._ck(self._L.dob_memory_bytes(self._h, C.byref(b)), "dob_memory_bytes")
+        return int(b.value)
+
+    def io_bytes(self):
+        """(host->device bytes per step, device->host bytes of the statistics)."""
+        a, b = C.c_uint64(), C.c_uint64()
+        self._ck(self._L.dob_io_bytes(self._h, C.byref(a), C.byref(b)), "dob_io_bytes")
+        return int(a.value), int(b.value)
+
+    def launches_per_step(self) -> int:
+        n = C.c_int()
+        self._ck(self._L.dob_launches_per_step(self._h, C.byref(n)), "dob_launches_per_step")
+        return int(n.value)
+
+    def time_steps(self, n, graph=True) -> float:
+        ms = C.c_float()
+        flags = 0 if graph else abi.STEP_NO_GRAPH
+        self._ck(self._L.dob_time_steps(self._h, int(n), flags, C.byref(ms)), "dob_time_steps")
+        return float(ms.value)
+
+    def bench_kernel(self, which=0, reps=10):
+        ms = C.c_float()
+        by = C.c_double()
+        self._ck(self._L.dob_bench_kernel(self._h, int(which), int(reps), C.byref(ms), C.byref(by)),
+                 "dob_bench_kernel")
+        return float(ms.value), float(by.value)
+
+    def save_state(self, slot):
+        self._ck(self._L.dob_save_state(self._h, int(slot)), "dob_save_state")
+
+    def load_state(self, slot):
+        self._ck(self._L.dob_load_state(self._h, int(slot)), "dob_load_state")
+
+
+def eval_math(fn: int, x, y=None) -> np.ndarray:
+    """Evaluate the library's own elementary function `fn` on the device."""
+    L = load()
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    yy = None if y is None else np.ascontiguousarray(y, dtype=np.float32)
+    out = np.empty_like(x)
+    rc = L.dob_eval_math(int(fn), _fptr(x), None if yy is None else _fptr(yy), _fptr(out), x.size)
+    check(rc, "dob_eval_math")
+    return out

@@ -1,0 +1,273 @@
+/*
+ * dropfluid.h — C ABI of the GB300-native staggered-MAC fluid step of the
+ * drop-of-blood simulator (semi-Lagrangian advection, Casson viscosity,
+ * divergence, geometric-multigrid pressure solve, projection, Lagrangian
+ * parcel advection/splat and dye transport).
+ *
+ * The reference drives this path from its TypeScript engine class
+ * (src/engine/BloodDropEngine.ts).  Each entry point below names the
+ * reference interface it replaces.  Conventions:
+ *   - every call returns a dob_status; no exception or abort crosses the ABI;
+ *   - caller-owned host buffers are copied synchronously before the call
+ *     returns;
+ *   - a context owns all of its device memory and is not re-entrant; separate
+ *     contexts may be driven from separate threads;
+ *   - grids are x-fastest: index = (z * ny + y) * nx + x.  The MAC faces use
+ *     the reference's upper-face convention: u(i,j,k) lives on the +x face of
+ *     cell (i,j,k), v on the +y face, w on the +z face
+ *     (src/shaders/fluid.ts:96-99).
+ */
+#ifndef DROPFLUID_H
+#define DROPFLUID_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DOB_ABI_VERSION 1
+
+typedef struct dob_ctx dob_ctx;
+
+typedef enum dob_status {
+  DOB_OK = 0,
+  DOB_EINVAL = -1,       /* bad argument (dims, sizes, pointers, NaN dt ...) */
+  DOB_ENOMEM = -2,       /* device or host allocation failed               */
+  DOB_ECUDA = -3,        /* a CUDA runtime call failed                      */
+  DOB_ENOCONVERGE = -4,  /* pressure solve missed its tolerance             */
+  DOB_ETIMEOUT = -5,     /* a bounded device wait ran out                    */
+  DOB_ESTATE = -6        /* call not valid in the context's current state   */
+} dob_status;
+
+/* Boundary conditions of the pressure problem. */
+enum {
+  /* Reference: 5 Neumann walls + Dirichlet free-surface top whose ghost
+     pressure comes from the wave field and the drop necks
+     (src/shaders/fluid.ts:16-77, 561-603). */
+  DOB_BC_REFERENCE = 0,
+  /* Closed box, free-slip walls, pure Neumann pressure (singular problem:
+     FP64 zero-mean compatibility of the right-hand side, pressure mean
+     pinned to zero). */
+  DOB_BC_CLOSED_BOX = 1
+};
+
+/* Storage precision. Arithmetic is FP32 in every mode. */
+enum {
+  DOB_PREC_FP32 = 0,           /* all fields FP32                                   */
+  DOB_PREC_MIXED = 1,          /* FP16 dye, BF16 correction levels, FP64 defect loop */
+  DOB_PREC_REFERENCE_FP16 = 2  /* velocity/curl/dye stored as binary16 like the
+                                  reference's rgba16float textures; pressure FP32  */
+};
+
+/* Physics terms of the reference step (all on in reference mode). */
+enum {
+  DOB_PHYS_VORT_CONF = 1,      /* vorticity confinement (fluid.ts:401-423, 467-472)   */
+  DOB_PHYS_BUOYANCY = 2,       /* Boussinesq buoyancy on y faces (fluid.ts:474-486)   */
+  DOB_PHYS_SPONGE = 4,         /* circular sponge + floor layer (fluid.ts:312-321)    */
+  DOB_PHYS_NECK = 8,           /* drop-neck momentum blend (fluid.ts:198-285)         */
+  DOB_PHYS_SOLENOIDAL = 16,    /* deep-column solenoidal forcing (fluid.ts:488-503)   */
+  DOB_PHYS_SURFACE = 32,       /* Marangoni + kinematic top layers (fluid.ts:287-310) */
+  DOB_PHYS_REFERENCE_ALL = 63
+};
+
+/* Step configuration (plain data, versioned by struct_size). */
+typedef struct dob_config {
+  uint32_t struct_size;        /* = sizeof(dob_config)                              */
+  uint32_t nx, ny, nz;         /* velocity / pressure grid                           */
+  uint32_t dye_refine;         /* 1: dye on the velocity grid; 2: 2x super-resolved
+                                  dye grid (reference: 192x256x192 over 96x128x96)   */
+  float dx;                    /* closed-box cell size (world units)                 */
+  float dt;                    /* closed-box time step (reference mode reads dt from
+                                  the uniform block, clamped to [0, 0.025])          */
+  float domain_min[3];         /* closed-box world box; reference mode takes it from */
+  float domain_max[3];         /* the uniform block's domainBounds                  */
+  int32_t bc_mode;             /* DOB_BC_*                                           */
+  int32_t precision_mode;      /* DOB_PREC_*                                         */
+  int32_t mg_levels;           /* grids in the hierarchy (reference: 4)              */
+  int32_t mg_pre, mg_post;     /* RBGS sweeps before/after coarse correction          */
+  int32_t mg_coarse_sweeps;    /* RBGS sweeps on the coarsest grid (reference: 6)    */
+  int32_t mg_cycles;           /* V-cycles per step (reference: 1)                   */
+  int32_t mg_max_outer;        /* mixed mode: max defect-correction iterations       */
+  double mg_rel_tol;           /* mixed mode: target ||b-Ap||/||b|| (FP64)            */
+  float casson_tau_y;          /* closed-box Casson yield stress                      */
+  float casson_mu_p;           /* closed-box Casson plastic viscosity                 */
+  int32_t physics_flags;       /* DOB_PHYS_*                                          */
+  uint32_t parcel_capacity;    /* parcel ring size (reference: 393216)               */
+  int32_t reference_schedule;  /* 1: L0 uses 1+1 sweeps, coarser levels mg_pre/mg_post,
+                                  exactly the reference's V-cycle (BloodDropEngine.ts:
+                                  1942-2059); 0: mg_pre/mg_post on every level       */
+  float vel_damping;           /* closed box: per-step advection damping (1 = none)   */
+  float dye_sharpness;         /* closed box: MacCormack correction strength          */
+} dob_config;
+
+/* Field identifiers for dob_set_field / dob_get_field.  Host data is always
+   FP32 (float) except the splat accumulators (uint32).  Sizes in elements:
+     VEL_U/V/W, PRESSURE, RHS, DIVERGENCE : nx*ny*nz
+     VEL_CENTER, CURL                     : 4*nx*ny*nz (x,y,z,w interleaved)
+     CONC    (reference mode)             : 4*Nc   (r,g,b,a interleaved)
+     CONC    (closed box: single dye)     : Nc
+     CONC_PRED                            : Nc
+     SPLAT_INTACT, SPLAT_LYSED            : Nc (uint32)
+     WAVE                                 : 4*512*512 (eta, deta/dt, lap, film)
+   with Nc = (dye_refine*nx)*(dye_refine*ny)*(dye_refine*nz). */
+typedef enum dob_field {
+  DOB_FIELD_VEL_U = 0,
+  DOB_FIELD_VEL_V = 1,
+  DOB_FIELD_VEL_W = 2,
+  DOB_FIELD_VEL_CENTER = 3,
+  DOB_FIELD_CURL = 4,
+  DOB_FIELD_PRESSURE = 5,
+  DOB_FIELD_RHS = 6,
+  DOB_FIELD_CONC = 7,
+  DOB_FIELD_CONC_PRED = 8,
+  DOB_FIELD_SPLAT_INTACT = 9,
+  DOB_FIELD_SPLAT_LYSED = 10,
+  DOB_FIELD_WAVE = 11,
+  DOB_FIELD_DIVERGENCE = 12,   /* read-only: MAC divergence of the current velocity */
+  DOB_FIELD_COUNT = 13
+} dob_field;
+
+/* Stages of one step, in the reference's order (BloodDropEngine.ts:1855-2111).
+   dob_run_stage runs exactly one of them on the current state. */
+typedef enum dob_stage {
+  DOB_STAGE_ADVECT_MAC = 0,      /* FLUID_ADVECT_MAC      fluid.ts:144-329  */
+  DOB_STAGE_MAC_TO_CENTER = 1,   /* FLUID_MAC_TO_CENTER   fluid.ts:917-962  */
+  DOB_STAGE_CURL = 2,            /* FLUID_CURL            fluid.ts:331-369  */
+  DOB_STAGE_CASSON_FORCES = 3,   /* FLUID_CASSON_FORCES   fluid.ts:377-511  */
+  DOB_STAGE_MAC_RHS = 4,         /* FLUID_MAC_RHS         fluid.ts:517-555  */
+  DOB_STAGE_PRESSURE_SOLVE = 5,  /* V-cycle schedule      BloodDropEngine.ts:1942-2059 */
+  DOB_STAGE_PROJECT = 6,         /* FLUID_MAC_PROJECT     fluid.ts:863-911  */
+  DOB_STAGE_CLEAR_SPLATS = 7,    /* clearBuffer x2        BloodDropEngine.ts:2074-2075 */
+  DOB_STAGE_PARCEL_EMIT = 8,     /* PARTICLE_EMIT         particles.ts:53-181 */
+  DOB_STAGE_PARCEL_ADVECT = 9,   /* PARTICLE_ADVECT_SPLAT particles.ts:189-462 */
+  DOB_STAGE_CONC_PREDICT = 10,   /* CONC_PREDICT          advect.ts:28-72    */
+  DOB_STAGE_CONC_RESOLVE = 11,   /* CONC_RESOLVE          advect.ts:81-298   */
+  DOB_STAGE_COUNT = 12
+} dob_stage;
+
+/* Flags for dob_step. */
+enum {
+  DOB_STEP_STATS = 1,   /* fill residual norms, max divergence, parcels alive  */
+  DOB_STEP_TIMING = 2,  /* per-stage device milliseconds (runs without a graph) */
+  DOB_STEP_NO_GRAPH = 4 /* launch stage by stage instead of replaying a graph   */
+};
+
+typedef struct dob_step_stats {
+  uint32_t struct_size;
+  int32_t steps_done;
+  int32_t vcycles;              /* V-cycles in the last step                      */
+  int32_t outer_iters;          /* defect-correction iterations in the last step  */
+  double rhs_l2;                /* ||b|| of the last pressure solve (FP64)        */
+  double residual_l2;           /* ||b - A p|| after the last solve (FP64)        */
+  double max_div;               /* max |div u| * dt / dx after projection         */
+  uint32_t parcels_alive;
+  uint32_t pad;
+  float stage_ms[DOB_STAGE_COUNT];
+} dob_step_stats;
+
+/* ---- lifecycle (replaces BloodDropEngine.create / destroy,
+        BloodDropEngine.ts:336-391, 2671-2736) ---------------------------- */
+
+/* Fill *cfg with the reference's own setup: 96x128x96 velocity grid, 2x dye,
+   Dirichlet top, 4-grid V-cycle with the reference schedule, 393216 parcels
+   (src/shaders/common.ts:4-20; BloodDropEngine.ts:88-98). */
+dob_status dob_config_reference(dob_config* cfg);
+/* Fill *cfg with a closed-box synthetic scene of the given grid:
+   FP32, 2+2 RBGS on every level, 4 grids, 4 cycles, Casson tau_y=0.005,
+   mu_p=1e-3, dx=1, dt=0.02. */
+dob_status dob_config_closed_box(dob_config* cfg, uint32_t nx, uint32_t ny, uint32_t nz);
+
+dob_status dob_create(const dob_config* cfg, dob_ctx** out);
+void dob_destroy(dob_ctx* ctx);
+/* Last error message of this context (static string if ctx is NULL). */
+const char* dob_last_error(const dob_ctx* ctx);
+int dob_abi_version(void);
+
+/* ---- state (replaces resetSimulation, BloodDropEngine.ts:1682-1763) ---- */
+
+/* Reference mode: FLUID_INIT_VEL on both velocity buffers, center and curl
+   (seed = uniform globalSeed), pressure/MG/conc/parcels/splats cleared.
+   Closed box: fluid at rest, everything zero. */
+dob_status dob_reset(dob_ctx* ctx);
+
+/* The reference's 512-byte SimUniforms block, verbatim (common.ts:26-43,
+   uniformLayout.ts:56-190).  Used by every following reference-mode step. */
+dob_status dob_set_uniforms(dob_ctx* ctx, const float sim_uniforms[128]);
+
+/* Closed box: a sphere of dye `dye` and face velocity vel (world units) plus
+   N(0, noise_sigma) noise per face (seeded SplitMix64 + Box-Muller). */
+dob_status dob_inject_sphere(dob_ctx* ctx, const float center[3], float radius,
+                             float dye, const float vel[3], float noise_sigma,
+                             uint64_t seed);
+
+/* Parcels: AoS, 8 floats (32 B) each = RbcParcel (particles.ts:17-20).
+   dob_set_parcels writes n parcels at ring index `offset` and raises the
+   high-water mark; dob_get_parcels reads n parcels from `offset`. */
+dob_status dob_set_parcels(dob_ctx* ctx, const float* parcels, uint32_t n, uint32_t offset);
+dob_status dob_get_parcels(dob_ctx* ctx, float* parcels, uint32_t n, uint32_t offset);
+dob_status dob_set_high_water(dob_ctx* ctx, uint32_t high_water);
+
+dob_status dob_set_field(dob_ctx* ctx, int field, const void* host, size_t bytes);
+dob_status dob_get_field(dob_ctx* ctx, int field, void* host, size_t bytes);
+
+/* ---- stepping (replaces encodePhysicsStep / seekToSimTime,
+        BloodDropEngine.ts:1855-2111, 2142-2179) ------------------------- */
+
+/* Run nsteps full steps with the current uniform block.  `stats` may be
+   NULL.  In reference mode the spawn count and cursor come from the uniform
+   block (particleParams.y/.z) and the high-water mark advances by the spawn
+   count like BloodDropEngine.ts:1832-1840. */
+dob_status dob_step(dob_ctx* ctx, int nsteps, uint32_t flags, dob_step_stats* stats);
+
+/* Reference mode: nsteps substeps, each with its own 128-float block
+   (the reference's multi-substep staging path, BloodDropEngine.ts:2634-2651). */
+dob_status dob_step_uniforms(dob_ctx* ctx, const float* blocks, int nsteps,
+                             uint32_t flags, dob_step_stats* stats);
+
+/* Run exactly one stage of the step on the current state (parity tests). */
+dob_status dob_run_stage(dob_ctx* ctx, int stage);
+
+/* Device time of nsteps steps (dob_step with `flags`), measured with CUDA
+   events on the context's stream; replaces the reference's per-pass GPU
+   timestamp queries (BloodDropEngine.ts:2400-2456). */
+dob_status dob_time_steps(dob_ctx* ctx, int nsteps, uint32_t flags, float* ms);
+
+/* Kernel micro-benchmark on the current state: launches the step's dominant
+   kernel (which = 0: the level-0 pressure smoother pass) `reps` times with
+   CUDA events around each launch; returns the mean device ms per launch and
+   the kernel's algorithmic bytes per launch (minimum HBM traffic of one
+   pass).  No counterpart in the reference. */
+dob_status dob_bench_kernel(dob_ctx* ctx, int which, int reps, float* avg_ms, double* bytes_per_launch);
+
+/* Block until all queued device work of this context is done. */
+dob_status dob_sync(dob_ctx* ctx);
+
+/* Kernels launched by one step (kernel nodes of the captured step graph). */
+dob_status dob_launches_per_step(dob_ctx* ctx, int* n);
+
+/* Host<->device bytes of one step through this ABI: the per-step parameter
+   block copied host->device before each step, and the statistics read back
+   device->host by a dob_step with DOB_STEP_STATS. */
+dob_status dob_io_bytes(const dob_ctx* ctx, uint64_t* h2d_per_step, uint64_t* d2h_stats);
+
+/* Device memory held by this context, in bytes. */
+dob_status dob_memory_bytes(const dob_ctx* ctx, uint64_t* bytes);
+
+/* Copy of the whole simulation state into snapshot slot 0..7 (device memory)
+   and back.  Slots are allocated on first use. */
+dob_status dob_save_state(dob_ctx* ctx, int slot);
+dob_status dob_load_state(dob_ctx* ctx, int slot);
+
+/* Evaluate the library's own elementary functions on the device (used to
+   check them against the host build bit for bit).  fn: 0 sin, 1 cos, 2 exp,
+   3 log, 4 pow(x,y), 5 atan2(x,y), 6 tanh, 7 f32->f16->f32 round trip,
+   8 f32->bf16->f32 round trip. */
+dob_status dob_eval_math(int fn, const float* x, const float* y, float* out, uint32_t n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DROPFLUID_H */

@@ -1,0 +1,460 @@
+"""Parity of the CUDA path (through the C ABI) with the oracle.
+
+Each stage of the step runs on the same seeded inputs on the device and in
+the CPU restatement; fields must agree to the tolerance stated per test
+(FP32 arithmetic with and without multiply-add contraction differs in the
+last bits, so stage results are compared in relative L2).  Parcel positions
+and splat accumulators are compared bit for bit.
+"""
+import numpy as np
+import pytest
+
+from helpers import bits_equal, rel_l2, smooth_field
+
+pytestmark = pytest.mark.gpu
+
+STAGE_TOL = 2e-5      # one stage, FP32 with vs without FMA contraction
+STEP_TOL = 1e-4       # spec bar: relative L2 after N full steps
+
+
+def _abi():
+    from dropfluid import abi
+    return abi
+
+
+def ref_block(sim_time=0.4, spawn=2048, cursor=0, dt=1.0 / 60.0):
+    from dropfluid import uniforms as U
+    snap = U.DropSnapshot(sim_time=sim_time, active_count=2)
+    snap.slots[0] = U.DropSlot(active=True, center=(0.03, 0.285, -0.02), radius=0.05, vel_y=-0.3,
+                               oscillation=0.01, vol_drain_rate=0.42, seed=1.5)
+    snap.slots[1] = U.DropSlot(active=True, center=(-0.12, 0.31, 0.09), radius=0.03, vel_y=-0.5,
+                               oscillation=0.0, vol_drain_rate=0.05, seed=2.7)
+    return U.SimUniformPacker().pack(drops=snap, dt=dt, global_seed=1.5, spawn_cursor=cursor,
+                                     spawn_count=spawn).copy()
+
+
+def ref_config(nx=32, ny=48, nz=32, prec=0):
+    abi = _abi()
+    c = abi.config_reference()
+    c.nx, c.ny, c.nz = nx, ny, nz
+    c.mg_levels = 3
+    c.parcel_capacity = 16384
+    c.precision_mode = prec
+    return c
+
+
+def box_config(n=(32, 32, 32), prec=0):
+    abi = _abi()
+    c = abi.config_closed_box(*n)
+    c.mg_levels = 3
+    c.parcel_capacity = 4096
+    c.precision_mode = prec
+    return c
+
+
+def ref_state(cfg, seed=0):
+    """Seeded reference-mode state: velocities ~0.3 m/s, positive conc, a
+    small wave field, parcels around the drops."""
+    abi = _abi()
+    nz, ny, nx = cfg.nz, cfg.ny, cfg.nx
+    r = cfg.dye_refine
+    st = {}
+    st[abi.FIELD_VEL_U] = smooth_field((nz, ny, nx), seed + 1, 0.3)
+    st[abi.FIELD_VEL_V] = smooth_field((nz, ny, nx), seed + 2, 0.3)
+    st[abi.FIELD_VEL_W] = smooth_field((nz, ny, nx), seed + 3, 0.3)
+    cen = np.zeros((nz, ny, nx, 4), np.float32)
+    for k in range(3):
+        cen[..., k] = smooth_field((nz, ny, nx), seed + 10 + k, 0.3)
+    st[abi.FIELD_VEL_CENTER] = cen
+    curl = np.zeros((nz, ny, nx, 4), np.float32)
+    for k in range(3):
+        curl[..., k] = smooth_field((nz, ny, nx), seed + 20 + k, 2.0)
+    curl[..., 3] = np.sqrt((curl[..., :3] ** 2).sum(-1))
+    st[abi.FIELD_CURL] = curl
+    st[abi.FIELD_PRESSURE] = smooth_field((nz, ny, nx), seed + 30, 0.01)
+    conc = np.zeros((nz * r, ny * r, nx * r, 4), np.float32)
+    for k in range(4):
+        conc[..., k] = np.abs(smooth_field((nz * r, ny * r, nx * r), seed + 40 + k, 0.6))
+    st[abi.FIELD_CONC] = conc
+    wave = np.zeros((512, 512, 4), np.float32)
+    wave[..., 0] = smooth_field((512, 512), seed + 50, 0.01)
+    wave[..., 1] = smooth_field((512, 512), seed + 51, 0.05)
+    wave[..., 2] = smooth_field((512, 512), seed + 52, 0.01)
+    wave[..., 3] = np.abs(smooth_field((512, 512), seed + 53, 0.9))
+    st[abi.FIELD_WAVE] = wave
+    return st
+
+
+def ref_parcels(n, seed=0):
+    rng = np.random.default_rng(seed)
+    p = np.zeros((n, 8), np.float32)
+    p[:, 0] = rng.uniform(-0.3, 0.3, n)
+    p[:, 1] = rng.uniform(-0.95, 0.29, n)
+    p[:, 2] = rng.uniform(-0.3, 0.3, n)
+    p[:, 3] = np.where(rng.uniform(size=n) < 0.9, 0.134, 0.0)
+    p[:, 4:7] = rng.normal(0, 0.004, (n, 3))
+    p[:, 7] = np.floor(rng.uniform(0, 4000, n)) + rng.uniform(0, 0.9, n)
+    return p
+
+
+def load_state(eng, st):
+    for f, a in st.items():
+        eng.set_field(f, a)
+
+
+@pytest.fixture(scope="module")
+def both(oracle_mod, gpu_lib):
+    from dropfluid import DropFluid
+
+    def make(cfg):
+        return DropFluid(cfg), oracle_mod.OracleSim(cfg)
+    return make
+
+
+# ---------------------------------------------------------------------------------------------
+def test_eval_math_bit_exact(oracle_mod, gpu_lib):
+    """The library's own elementary functions give the same bits on the
+    device and on the host (the basis of bit-exact parcel bins)."""
+    from dropfluid import eval_math
+    rng = np.random.default_rng(5)
+    cases = {
+        0: rng.uniform(-200, 200, 20000), 1: rng.uniform(-200, 200, 20000), 2: rng.uniform(-80, 80, 20000),
+        3: np.exp(rng.uniform(-80, 80, 20000)), 6: rng.uniform(-10, 10, 20000),
+        7: rng.normal(0, 100, 20000), 8: rng.normal(0, 1e5, 20000),
+    }
+    for fn, x in cases.items():
+        x = x.astype(np.float32)
+        assert bits_equal(eval_math(fn, x), oracle_mod.eval_math(fn, x)), fn
+    x = rng.uniform(0, 3, 20000).astype(np.float32)
+    y = rng.uniform(0, 2, 20000).astype(np.float32)
+    assert bits_equal(eval_math(4, x, y), oracle_mod.eval_math(4, x, y))
+    a = rng.normal(0, 1, 20000).astype(np.float32)
+    b = rng.normal(0, 1, 20000).astype(np.float32)
+    assert bits_equal(eval_math(5, a, b), oracle_mod.eval_math(5, a, b))
+
+
+def test_binary16_store_matches_host_rounding(oracle_mod, gpu_lib):
+    """__float2half_rn on the device == the host IEEE RNE restatement,
+    including subnormals, ties and overflow."""
+    from dropfluid import eval_math
+    rng = np.random.default_rng(9)
+    x = np.concatenate([rng.normal(0, s, 5000) for s in (1e-7, 1e-5, 1e-2, 1, 1e3, 7e4)]).astype(np.float32)
+    x = np.concatenate([x, np.array([0.0, -0.0, 1.0, 65504.0, 65520.0, 65519.99, 5.96e-8, 2.98e-8, 1e-9],
+                                    np.float32)])
+    dev = eval_math(7, x)
+    assert bits_equal(dev, oracle_mod.eval_math(7, x))
+    np.testing.assert_array_equal(dev, x.astype(np.float16).astype(np.float32))
+
+
+# ---- closed box, stage by stage ------------------------------------------------------------
+def box_state(cfg, seed=0, amp=40.0):
+    abi = _abi()
+    nz, ny, nx = cfg.nz, cfg.ny, cfg.nx
+    st = {abi.FIELD_VEL_U: smooth_field((nz, ny, nx), seed + 1, amp),
+          abi.FIELD_VEL_V: smooth_field((nz, ny, nx), seed + 2, amp),
+          abi.FIELD_VEL_W: smooth_field((nz, ny, nx), seed + 3, amp)}
+    cen = np.zeros((nz, ny, nx, 4), np.float32)
+    for k in range(3):
+        cen[..., k] = smooth_field((nz, ny, nx), seed + 10 + k, amp)
+    st[abi.FIELD_VEL_CENTER] = cen
+    st[abi.FIELD_PRESSURE] = smooth_field((nz, ny, nx), seed + 30, 1.0)
+    st[abi.FIELD_CONC] = np.abs(smooth_field((nz, ny, nx), seed + 40, 1.0))
+    return st
+
+
+BOX_STAGE_OUT = {
+    0: ("VEL_U", "VEL_V", "VEL_W"), 1: ("VEL_CENTER",), 3: ("VEL_U", "VEL_V", "VEL_W"), 4: ("RHS",),
+    6: ("VEL_U", "VEL_V", "VEL_W"), 10: ("CONC_PRED",),
+}
+
+
+@pytest.mark.parametrize("stage", sorted(BOX_STAGE_OUT))
+def test_box_stage_parity(both, stage):
+    abi = _abi()
+    cfg = box_config()
+    g, o = both(cfg)
+    st = box_state(cfg)
+    load_state(g, st)
+    load_state(o, st)
+    g.run_stage(stage)
+    o.run_stage(stage)
+    for name in BOX_STAGE_OUT[stage]:
+        f = getattr(abi, "FIELD_" + name)
+        err = rel_l2(g.get_field(f), o.get_field(f))
+        assert err < STAGE_TOL, (stage, name, err)
+
+
+def test_box_pressure_solve_parity(both):
+    abi = _abi()
+    cfg = box_config()
+    g, o = both(cfg)
+    st = box_state(cfg)
+    load_state(g, st)
+    load_state(o, st)
+    for e in (g, o):
+        e.run_stage(abi.STAGE_MAC_RHS)
+        e.run_stage(abi.STAGE_PRESSURE_SOLVE)
+    assert rel_l2(g.get_field(abi.FIELD_PRESSURE), o.get_field(abi.FIELD_PRESSURE)) < STAGE_TOL
+    # the FP64 compatibility sum leaves a zero-mean right-hand side and pressure
+    assert abs(float(g.get_field(abi.FIELD_RHS).astype(np.float64).mean())) < 1e-5
+    assert abs(float(g.get_field(abi.FIELD_PRESSURE).astype(np.float64).mean())) < 1e-5
+
+
+def test_box_dye_resolve_parity(both):
+    abi = _abi()
+    cfg = box_config()
+    g, o = both(cfg)
+    st = box_state(cfg)
+    st[abi.FIELD_CONC_PRED] = np.abs(smooth_field((cfg.nz, cfg.ny, cfg.nx), 77, 1.0))
+    load_state(g, st)
+    load_state(o, st)
+    g.run_stage(abi.STAGE_CONC_RESOLVE)
+    o.run_stage(abi.STAGE_CONC_RESOLVE)
+    assert rel_l2(g.get_field(abi.FIELD_CONC), o.get_field(abi.FIELD_CONC)) < STAGE_TOL
+
+
+def test_box_parcels_bit_exact(both):
+    """Same centre velocity + parcels -> identical positions and splat bins."""
+    abi = _abi()
+    from dropfluid import scenes
+    cfg = box_config()
+    g, o = both(cfg)
+    st = box_state(cfg)
+    load_state(g, st)
+    load_state(o, st)
+    p = scenes.parcels_in_sphere((16.0, 20.0, 15.0), 6.0, 4096, 3)
+    g.set_parcels(p)
+    o.set_parcels(p)
+    for e in (g, o):
+        e.run_stage(abi.STAGE_CLEAR_SPLATS)
+        e.run_stage(abi.STAGE_PARCEL_ADVECT)
+    assert bits_equal(g.get_parcels(), o.get_parcels())
+    assert bits_equal(g.get_field(abi.FIELD_SPLAT_INTACT), o.get_field(abi.FIELD_SPLAT_INTACT))
+
+
+# ---- reference mode, stage by stage -----------------------------------------------------------
+REF_STAGE_OUT = {
+    0: ("VEL_U", "VEL_V", "VEL_W"), 1: ("VEL_CENTER",), 2: ("CURL",), 3: ("VEL_U", "VEL_V", "VEL_W"),
+    4: ("RHS",), 6: ("VEL_U", "VEL_V", "VEL_W"), 10: ("CONC_PRED",),
+}
+
+
+@pytest.mark.parametrize("stage", sorted(REF_STAGE_OUT))
+def test_reference_stage_parity(both, stage):
+    abi = _abi()
+    cfg = ref_config()
+    g, o = both(cfg)
+    st = ref_state(cfg)
+    blk = ref_block()
+    for e in (g, o):
+        e.set_uniforms(blk)
+        load_state(e, st)
+        e.run_stage(stage)
+    for name in REF_STAGE_OUT[stage]:
+        f = getattr(abi, "FIELD_" + name)
+        err = rel_l2(g.get_field(f), o.get_field(f))
+        assert err < STAGE_TOL, (stage, name, err)
+
+
+def test_reference_pressure_solve_parity(both):
+    abi = _abi()
+    cfg = ref_config()
+    g, o = both(cfg)
+    st = ref_state(cfg)
+    blk = ref_block()
+    for e in (g, o):
+        e.set_uniforms(blk)
+        load_state(e, st)
+        e.run_stage(abi.STAGE_MAC_RHS)
+        e.run_stage(abi.STAGE_PRESSURE_SOLVE)
+    assert rel_l2(g.get_field(abi.FIELD_PRESSURE), o.get_field(abi.FIELD_PRESSURE)) < STAGE_TOL
+
+
+def test_reference_conc_resolve_parity(both):
+    abi = _abi()
+    cfg = ref_config()
+    g, o = both(cfg)
+    st = ref_state(cfg)
+    r = cfg.dye_refine
+    shape = (cfg.nz * r, cfg.ny * r, cfg.nx * r)
+    st[abi.FIELD_CONC_PRED] = np.abs(smooth_field(shape, 91, 0.5))
+    rng = np.random.default_rng(4)
+    st[abi.FIELD_SPLAT_INTACT] = np.where(rng.uniform(size=shape) < 0.3, rng.integers(0, 20000, shape), 0).astype(np.uint32)
+    st[abi.FIELD_SPLAT_LYSED] = np.where(rng.uniform(size=shape) < 0.3, rng.integers(0, 9000, shape), 0).astype(np.uint32)
+    blk = ref_block()
+    for e in (g, o):
+        e.set_uniforms(blk)
+        load_state(e, st)
+        e.run_stage(abi.STAGE_CONC_RESOLVE)
+    assert rel_l2(g.get_field(abi.FIELD_CONC), o.get_field(abi.FIELD_CONC)) < STAGE_TOL
+
+
+def test_reference_parcels_bit_exact(both):
+    """PARTICLE_EMIT + PARTICLE_ADVECT_SPLAT: parcels, and therefore their
+    splat bins and fixed-point sums, identical to the host restatement."""
+    abi = _abi()
+    cfg = ref_config()
+    g, o = both(cfg)
+    st = ref_state(cfg)
+    blk = ref_block(spawn=2048, cursor=1000)
+    p = ref_parcels(cfg.parcel_capacity, 1)
+    for e in (g, o):
+        e.set_uniforms(blk)
+        load_state(e, st)
+        e.set_parcels(p)
+        e.run_stage(abi.STAGE_CLEAR_SPLATS)
+        e.run_stage(abi.STAGE_PARCEL_EMIT)
+    assert bits_equal(g.get_parcels(), o.get_parcels())
+    assert bits_equal(g.get_field(abi.FIELD_SPLAT_LYSED), o.get_field(abi.FIELD_SPLAT_LYSED))
+    for e in (g, o):
+        e.run_stage(abi.STAGE_PARCEL_ADVECT)
+    gp, op = g.get_parcels(), o.get_parcels()
+    assert bits_equal(gp, op), int((gp.view(np.uint32) != op.view(np.uint32)).any(axis=1).sum())
+    assert bits_equal(g.get_field(abi.FIELD_SPLAT_INTACT), o.get_field(abi.FIELD_SPLAT_INTACT))
+    assert bits_equal(g.get_field(abi.FIELD_SPLAT_LYSED), o.get_field(abi.FIELD_SPLAT_LYSED))
+    assert g.get_field(abi.FIELD_SPLAT_INTACT).sum() > 0
+
+
+# ---- full steps ------------------------------------------------------------------------------
+def test_box48_scene_parity_and_divergence(oracle_mod, gpu_lib):
+    """The 48x64x48 drop scene, 20 full steps: every field within relative L2
+    1e-4 of the FP32 oracle, error against the FP64 oracle reported, and the
+    projected velocity's max |div u| dt/dx <= 1e-5 at the end."""
+    abi = _abi()
+    from dropfluid import DropFluid, scenes
+    sc = scenes.box48()
+    g = DropFluid(sc.config)
+    o32 = oracle_mod.OracleSim(sc.config)
+    o64 = oracle_mod.OracleSim(sc.config, fp64=True)
+    for e in (g, o32, o64):
+        scenes.run(sc, e)
+    for name in ("VEL_U", "VEL_V", "VEL_W", "PRESSURE", "CONC"):
+        f = getattr(abi, "FIELD_" + name)
+        e32 = rel_l2(g.get_field(f), o32.get_field(f))
+        e64 = rel_l2(g.get_field(f), o64.get_field(f))
+        print(f"box48 {name}: rel L2 vs FP32 oracle {e32:.2e}, vs FP64 oracle {e64:.2e}")
+        assert e32 < STEP_TOL, (name, e32)
+        assert e64 < 1e-3, (name, e64)
+    gp, op = g.get_parcels()[:, :3], o32.get_parcels()[:, :3]
+    assert rel_l2(gp, op) < STEP_TOL
+    st = g.step(1, stats=True)
+    assert st["max_div"] <= 1e-5, st
+
+
+def test_reference_mode_steps_parity(oracle_mod, gpu_lib):
+    """Reference setup (Dirichlet free-surface top, drops, parcels, 2x dye),
+    8 substeps at a reduced grid: relative L2 <= 1e-4 against the oracle."""
+    abi = _abi()
+    from dropfluid import DropFluid
+    cfg = ref_config()
+    g = DropFluid(cfg)
+    o = oracle_mod.OracleSim(cfg)
+    st = ref_state(cfg, seed=3)
+    del st[abi.FIELD_CURL]
+    for k, e in enumerate((g, o)):
+        e.set_uniforms(ref_block(sim_time=0.5, spawn=0))
+        e.reset()
+        e.set_field(abi.FIELD_WAVE, st[abi.FIELD_WAVE])
+    for k in range(8):
+        blk = ref_block(sim_time=0.5 + k / 60.0, spawn=512, cursor=512 * k)
+        for e in (g, o):
+            e.set_uniforms(blk)
+            e.step(1)
+    for name in ("VEL_U", "VEL_V", "VEL_W", "PRESSURE", "CONC"):
+        f = getattr(abi, "FIELD_" + name)
+        err = rel_l2(g.get_field(f), o.get_field(f))
+        print(f"reference {name}: rel L2 {err:.2e}")
+        assert err < STEP_TOL, (name, err)
+
+
+def test_graph_replay_equals_stage_launches(gpu_lib):
+    """A step replayed from the captured graph gives the same bits as the
+    same step launched stage by stage."""
+    abi = _abi()
+    from dropfluid import DropFluid, scenes
+    sc = scenes.box48()
+    a, b = DropFluid(sc.config), DropFluid(sc.config)
+    sc.release(a, 0)
+    sc.release(b, 0)
+    a.step(5, graph=True)
+    b.step(5, graph=False)
+    for f in (abi.FIELD_VEL_U, abi.FIELD_VEL_V, abi.FIELD_PRESSURE, abi.FIELD_CONC):
+        assert bits_equal(a.get_field(f), b.get_field(f)), f
+    assert bits_equal(a.get_parcels(), b.get_parcels())
+
+
+def test_save_load_state_roundtrip(gpu_lib):
+    abi = _abi()
+    from dropfluid import DropFluid, scenes
+    sc = scenes.box48()
+    a = DropFluid(sc.config)
+    sc.release(a, 0)
+    a.step(2)
+    a.save_state(0)
+    a.step(3)
+    u5 = a.get_field(abi.FIELD_VEL_V)
+    a.load_state(0)
+    a.step(3)
+    assert bits_equal(a.get_field(abi.FIELD_VEL_V), u5)
+
+
+def test_fp16_reference_storage_parity(both):
+    """rgba16float storage (reference-faithful mode): the device's binary16
+    stores match the oracle's emulated RNE rounding."""
+    abi = _abi()
+    cfg = ref_config(prec=abi.DOB_PREC_REFERENCE_FP16)
+    g, o = both(cfg)
+    st = ref_state(cfg, seed=8)
+    blk = ref_block()
+    for e in (g, o):
+        e.set_uniforms(blk)
+        load_state(e, st)
+    for stage in (abi.STAGE_ADVECT_MAC, abi.STAGE_MAC_TO_CENTER, abi.STAGE_CASSON_FORCES):
+        g.run_stage(stage)
+        o.run_stage(stage)
+        for f in (abi.FIELD_VEL_U, abi.FIELD_VEL_V, abi.FIELD_VEL_W):
+            assert rel_l2(g.get_field(f), o.get_field(f)) < 2e-3, (stage, f)
+
+
+def test_mixed_precision_defect_loop(both):
+    """Mixed mode: FP64 residual + BF16 correction V-cycles reach the
+    requested relative residual, like the oracle's restatement."""
+    abi = _abi()
+    cfg = box_config(prec=abi.DOB_PREC_MIXED)
+    cfg.mg_cycles = 1
+    cfg.mg_rel_tol = 1e-6
+    cfg.mg_max_outer = 16
+    g, o = both(cfg)
+    st = box_state(cfg)
+    load_state(g, st)
+    load_state(o, st)
+    for e in (g, o):
+        e.run_stage(abi.STAGE_MAC_RHS)
+        e.run_stage(abi.STAGE_PRESSURE_SOLVE)
+    assert rel_l2(g.get_field(abi.FIELD_PRESSURE), o.get_field(abi.FIELD_PRESSURE)) < 1e-3
+
+
+def test_error_paths(gpu_lib):
+    abi = _abi()
+    from dropfluid import DropFluid, DropFluidError
+    bad = abi.config_closed_box(30, 32, 32)  # not divisible by 2^(levels-1)
+    with pytest.raises(DropFluidError) as ei:
+        DropFluid(bad)
+    assert ei.value.status == abi.DOB_EINVAL
+    cfg = box_config()
+    g = DropFluid(cfg)
+    with pytest.raises(DropFluidError) as ei:
+        g.set_field(abi.FIELD_VEL_U, np.zeros(10, np.float32))
+    assert ei.value.status == abi.DOB_EINVAL
+    with pytest.raises(DropFluidError) as ei:
+        g.set_parcels(np.zeros((cfg.parcel_capacity + 1, 8), np.float32))
+    assert ei.value.status == abi.DOB_EINVAL
+    r = DropFluid(ref_config())
+    with pytest.raises(DropFluidError) as ei:
+        r.inject_sphere((0, 0, 0), 0.1, 1.0, (0, 0, 0))
+    assert ei.value.status == abi.DOB_ESTATE
+    blk = ref_block()
+    blk[38] = np.nan
+    with pytest.raises(DropFluidError) as ei:
+        r.set_uniforms(blk)
+    assert ei.value.status == abi.DOB_EINVAL
