@@ -88,6 +88,8 @@ static bool valid_config(const dob_config* c, std::string* why) {
   if (c->nx > 2048 || c->ny > 2048 || c->nz > 2048) return no("grid dims must be <= 2048");
   if (c->nx % 2 || c->ny % 2 || c->nz % 2) return no("grid dims must be even");
   if (c->dye_refine != 1 && c->dye_refine != 2) return no("dye_refine must be 1 or 2");
+  const uint64_t r3 = (uint64_t)c->dye_refine * c->dye_refine * c->dye_refine;
+  if ((uint64_t)c->nx * c->ny * c->nz * r3 >= (1ull << 31)) return no("grid too large (the dye grid must have < 2^31 cells)");
   if (c->mg_levels < 1 || c->mg_levels > kMaxLevels) return no("mg_levels out of range");
   const uint32_t m = 1u << (c->mg_levels - 1);
   if (c->nx % m || c->ny % m || c->nz % m) return no("dims not divisible by 2^(mg_levels-1)");
@@ -380,7 +382,7 @@ dob_status dob_config_closed_box(dob_config* c, uint32_t nx, uint32_t ny, uint32
   c->domain_max[0] = (float)nx; c->domain_max[1] = (float)ny; c->domain_max[2] = (float)nz;
   c->bc_mode = DOB_BC_CLOSED_BOX;
   c->precision_mode = DOB_PREC_FP32;
-  c->mg_levels = 4; c->mg_pre = 2; c->mg_post = 2; c->mg_coarse_sweeps = 16; c->mg_cycles = 4;
+  c->mg_levels = 4; c->mg_pre = 2; c->mg_post = 2; c->mg_coarse_sweeps = 6; c->mg_cycles = 4;
   c->mg_max_outer = 8; c->mg_rel_tol = 1e-8;
   c->casson_tau_y = 0.005f; c->casson_mu_p = 1e-3f;
   c->physics_flags = 0;
@@ -594,7 +596,7 @@ namespace {
 struct FieldDesc {
   void* dev;
   size_t count;     // host elements
-  int kind;         // 0: VS, 1: DS, 2: f32, 3: u32
+  int kind;         // 0: VS, 1: DS, 2: f32, 3: u32, 4: f32 red-black split
 };
 }  // namespace
 
@@ -607,8 +609,8 @@ static bool field_desc(dob_ctx* ctx, int field, FieldDesc* f) {
     case DOB_FIELD_VEL_W: *f = {s.w, N, 0}; return true;
     case DOB_FIELD_VEL_CENTER: *f = {s.cen, 4 * N, 0}; return true;
     case DOB_FIELD_CURL: *f = {s.curl, 4 * N, 0}; return s.curl != nullptr;
-    case DOB_FIELD_PRESSURE: *f = {s.p, N, 2}; return true;
-    case DOB_FIELD_RHS: *f = {s.rhs, N, 2}; return true;
+    case DOB_FIELD_PRESSURE: *f = {s.p, N, 4}; return true;
+    case DOB_FIELD_RHS: *f = {s.rhs, N, 4}; return true;
     case DOB_FIELD_CONC: *f = {s.conc, (s.ref ? 4 : 1) * Nc, 1}; return true;
     case DOB_FIELD_CONC_PRED: *f = {s.pred, Nc, 1}; return true;
     case DOB_FIELD_SPLAT_INTACT: *f = {s.splatI, Nc, 3}; return true;
@@ -625,7 +627,17 @@ dob_status dob_set_field(dob_ctx* ctx, int field, const void* host, size_t bytes
   if (bytes != f.count * 4) return fail(ctx, DOB_EINVAL, "dob_set_field", "byte count does not match the field");
   CK(cudaStreamSynchronize(ctx->stream));
   const size_t eb = f.kind == 0 ? vs_bytes(ctx->s.prec) : f.kind == 1 ? ds_bytes(ctx->s.prec) : 4;
-  if (eb == 4) {
+  if (f.kind == 4) {
+    float* tmp = nullptr;
+    CK(cudaMalloc(&tmp, bytes));
+    cudaError_t e = cudaMemcpy(tmp, host, bytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+      launch_split(tmp, (float*)f.dev, ctx->s.g, true, ctx->stream);
+      e = cudaStreamSynchronize(ctx->stream);
+    }
+    cudaFree(tmp);
+    if (e != cudaSuccess) return fail(ctx, DOB_ECUDA, "dob_set_field", cudaGetErrorString(e));
+  } else if (eb == 4) {
     CK(cudaMemcpy(f.dev, host, bytes, cudaMemcpyHostToDevice));
   } else {
     std::vector<uint16_t> tmp(f.count);
@@ -655,7 +667,15 @@ dob_status dob_get_field(dob_ctx* ctx, int field, void* host, size_t bytes) {
   if (!field_desc(ctx, field, &f)) return fail(ctx, DOB_EINVAL, "dob_get_field", "unknown field");
   if (bytes != f.count * 4) return fail(ctx, DOB_EINVAL, "dob_get_field", "byte count does not match the field");
   const size_t eb = f.kind == 0 ? vs_bytes(ctx->s.prec) : f.kind == 1 ? ds_bytes(ctx->s.prec) : 4;
-  if (eb == 4) {
+  if (f.kind == 4) {
+    float* tmp = nullptr;
+    CK(cudaMalloc(&tmp, bytes));
+    launch_split((const float*)f.dev, tmp, ctx->s.g, false, ctx->stream);
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpy(host, tmp, bytes, cudaMemcpyDeviceToHost);
+    cudaFree(tmp);
+    if (e != cudaSuccess) return fail(ctx, DOB_ECUDA, "dob_get_field", cudaGetErrorString(e));
+  } else if (eb == 4) {
     CK(cudaMemcpy(host, f.dev, bytes, cudaMemcpyDeviceToHost));
   } else {
     std::vector<uint16_t> tmp(f.count);

@@ -90,8 +90,10 @@ __device__ __forceinline__ void st4(half4* p, float4 v) {
 }
 
 // ---- WebGPU linear / clamp-to-edge sampling (texel = uvw*dims - 0.5) ----------
+// The 8 taps are base + {0,ox} + {0,oy} + {0,oz} with 32-bit offsets (grids
+// are limited to < 2^31 cells); clamping to the edge makes an offset 0.
 struct Taps {
-  size_t i[8];
+  uint32_t base, ox, oy, oz;
   float fx, fy, fz;
 };
 __device__ __forceinline__ Taps make_taps(const Grid& g, float u, float v, float w) {
@@ -103,51 +105,46 @@ __device__ __forceinline__ Taps make_taps(const Grid& g, float u, float v, float
   const int x0 = dob_clampi(ix, 0, g.nx - 1), x1 = dob_clampi(ix + 1, 0, g.nx - 1);
   const int y0 = dob_clampi(iy, 0, g.ny - 1), y1 = dob_clampi(iy + 1, 0, g.ny - 1);
   const int z0 = dob_clampi(iz, 0, g.nz - 1), z1 = dob_clampi(iz + 1, 0, g.nz - 1);
-  t.i[0] = g.at(x0, y0, z0); t.i[1] = g.at(x1, y0, z0);
-  t.i[2] = g.at(x0, y1, z0); t.i[3] = g.at(x1, y1, z0);
-  t.i[4] = g.at(x0, y0, z1); t.i[5] = g.at(x1, y0, z1);
-  t.i[6] = g.at(x0, y1, z1); t.i[7] = g.at(x1, y1, z1);
+  const uint32_t sy = (uint32_t)g.nx, sz = (uint32_t)g.nx * (uint32_t)g.ny;
+  t.base = (uint32_t)z0 * sz + (uint32_t)y0 * sy + (uint32_t)x0;
+  t.ox = (uint32_t)(x1 - x0);
+  t.oy = (uint32_t)(y1 - y0) * sy;
+  t.oz = (uint32_t)(z1 - z0) * sz;
   return t;
 }
 template <class S> __device__ __forceinline__ float lerp8(const Taps& t, const S* a) {
-  const float x00 = dob_mix(ldf(a + t.i[0]), ldf(a + t.i[1]), t.fx);
-  const float x10 = dob_mix(ldf(a + t.i[2]), ldf(a + t.i[3]), t.fx);
-  const float x01 = dob_mix(ldf(a + t.i[4]), ldf(a + t.i[5]), t.fx);
-  const float x11 = dob_mix(ldf(a + t.i[6]), ldf(a + t.i[7]), t.fx);
+  const S* p = a + t.base;
+  const float x00 = dob_mix(ldf(p), ldf(p + t.ox), t.fx);
+  const float x10 = dob_mix(ldf(p + t.oy), ldf(p + t.oy + t.ox), t.fx);
+  const float x01 = dob_mix(ldf(p + t.oz), ldf(p + t.oz + t.ox), t.fx);
+  const float x11 = dob_mix(ldf(p + t.oz + t.oy), ldf(p + t.oz + t.oy + t.ox), t.fx);
   const float y0 = dob_mix(x00, x10, t.fy);
   const float y1 = dob_mix(x01, x11, t.fy);
   return dob_mix(y0, y1, t.fz);
 }
-template <class V4> __device__ __forceinline__ float4 lerp8x4(const Taps& t, const V4* a) {
-  float4 c[8];
-#pragma unroll
-  for (int k = 0; k < 8; ++k) c[k] = ld4(a + t.i[k]);
+__device__ __forceinline__ float tri(float c000, float c100, float c010, float c110, float c001, float c101,
+                                     float c011, float c111, const Taps& t) {
+  const float x00 = dob_mix(c000, c100, t.fx), x10 = dob_mix(c010, c110, t.fx);
+  const float x01 = dob_mix(c001, c101, t.fx), x11 = dob_mix(c011, c111, t.fx);
+  return dob_mix(dob_mix(x00, x10, t.fy), dob_mix(x01, x11, t.fy), t.fz);
+}
+// Interpolate the first `NC` channels (3 or 4) of a 4-wide AoS field.
+template <int NC, class V4> __device__ __forceinline__ float4 lerp8xn(const Taps& t, const V4* a) {
+  const V4* p = a + t.base;
+  const float4 c0 = ld4(p), c1 = ld4(p + t.ox), c2 = ld4(p + t.oy), c3 = ld4(p + t.oy + t.ox);
+  const float4 c4 = ld4(p + t.oz), c5 = ld4(p + t.oz + t.ox), c6 = ld4(p + t.oz + t.oy);
+  const float4 c7 = ld4(p + t.oz + t.oy + t.ox);
   float4 r;
-  {
-    const float x00 = dob_mix(c[0].x, c[1].x, t.fx), x10 = dob_mix(c[2].x, c[3].x, t.fx);
-    const float x01 = dob_mix(c[4].x, c[5].x, t.fx), x11 = dob_mix(c[6].x, c[7].x, t.fx);
-    r.x = dob_mix(dob_mix(x00, x10, t.fy), dob_mix(x01, x11, t.fy), t.fz);
-  }
-  {
-    const float x00 = dob_mix(c[0].y, c[1].y, t.fx), x10 = dob_mix(c[2].y, c[3].y, t.fx);
-    const float x01 = dob_mix(c[4].y, c[5].y, t.fx), x11 = dob_mix(c[6].y, c[7].y, t.fx);
-    r.y = dob_mix(dob_mix(x00, x10, t.fy), dob_mix(x01, x11, t.fy), t.fz);
-  }
-  {
-    const float x00 = dob_mix(c[0].z, c[1].z, t.fx), x10 = dob_mix(c[2].z, c[3].z, t.fx);
-    const float x01 = dob_mix(c[4].z, c[5].z, t.fx), x11 = dob_mix(c[6].z, c[7].z, t.fx);
-    r.z = dob_mix(dob_mix(x00, x10, t.fy), dob_mix(x01, x11, t.fy), t.fz);
-  }
-  {
-    const float x00 = dob_mix(c[0].w, c[1].w, t.fx), x10 = dob_mix(c[2].w, c[3].w, t.fx);
-    const float x01 = dob_mix(c[4].w, c[5].w, t.fx), x11 = dob_mix(c[6].w, c[7].w, t.fx);
-    r.w = dob_mix(dob_mix(x00, x10, t.fy), dob_mix(x01, x11, t.fy), t.fz);
-  }
+  r.x = tri(c0.x, c1.x, c2.x, c3.x, c4.x, c5.x, c6.x, c7.x, t);
+  r.y = tri(c0.y, c1.y, c2.y, c3.y, c4.y, c5.y, c6.y, c7.y, t);
+  r.z = tri(c0.z, c1.z, c2.z, c3.z, c4.z, c5.z, c6.z, c7.z, t);
+  r.w = NC == 4 ? tri(c0.w, c1.w, c2.w, c3.w, c4.w, c5.w, c6.w, c7.w, t) : 0.0f;
   return r;
 }
+template <class V4> __device__ __forceinline__ float4 lerp8x4(const Taps& t, const V4* a) { return lerp8xn<4>(t, a); }
 template <class V4> __device__ __forceinline__ dob_v3 sample_center(const Grid& g, const V4* cen, dob_v3 uvw) {
   const Taps t = make_taps(g, uvw.x, uvw.y, uvw.z);
-  const float4 r = lerp8x4(t, cen);
+  const float4 r = lerp8xn<3>(t, cen);
   return v3(r.x, r.y, r.z);
 }
 

@@ -19,9 +19,17 @@ struct MgLevel {
   float h2;
   float* e;            // correction (levels >= 1), FP32
   float* b;            // right-hand side (levels >= 1), FP32
-  __nv_bfloat16* eh;   // BF16 copies used by the mixed-precision inner solve
+  __nv_bfloat16* eh;   // BF16 arrays used by the mixed-precision inner solve
   __nv_bfloat16* bh;
 };
+
+// Red-black split index of cell (x,y,z): colour c = (x+y+z)&1 selects the
+// half, and inside a half the cells are row-major with x/2 fastest.  Every
+// multigrid array (p, rhs, corrections) is stored this way.
+__host__ __device__ __forceinline__ size_t rb_index(const Grid& d, int x, int y, int z) {
+  const size_t half = d.n() >> 1;
+  return (size_t)((x + y + z) & 1) * half + ((size_t)z * d.ny + y) * (size_t)(d.nx >> 1) + (size_t)(x >> 1);
+}
 
 struct DevState {
   Grid g;    // velocity / pressure grid
@@ -33,7 +41,7 @@ struct DevState {
   StepParams* params;            // device copy of this step's parameters
   void *u, *v, *w, *u2, *v2, *w2;  // MAC faces (VS)
   void *cen, *curl;              // 4 x VS AoS
-  float *p, *rhs;
+  float *p, *rhs;                // red-black split layout (rb_index)
   void *conc, *conc2, *pred;     // dye (DS)
   uint32_t *splatI, *splatL;
   float4* wave;
@@ -45,7 +53,7 @@ struct DevState {
   MgLevel lv[kMaxLevels];
   int pre0, post0, pre, post, coarse_sweeps, cycles;
   // mixed-precision defect correction
-  __nv_bfloat16 *e0h, *r0h;      // level-0 correction and residual (BF16)
+  __nv_bfloat16 *e0h, *r0h;      // level-0 correction and residual (BF16, split layout)
   int max_outer;
   double rel_tol;
 };
@@ -136,6 +144,8 @@ void launch_residual_norm(const DevState& s, double* out, cudaStream_t st);
 void launch_sum(const float* a, size_t n, double* out, int num_sms, cudaStream_t st);
 void launch_sub_mean(float* a, size_t n, const double* sum, int num_sms, cudaStream_t st);
 void launch_sumsq(const float* a, size_t n, double* out, int num_sms, cudaStream_t st);
+// Natural <-> red-black split copy of a level-0 array (field I/O).
+void launch_split(const float* src, float* dst, const Grid& d, bool to_split, cudaStream_t st);
 // One pass of the level-0 pressure smoother on the current state; returns the
 // pass's algorithmic HBM bytes (read p and b, write p once).
 double smoother_pass(const DevState& s, cudaStream_t st);

@@ -397,7 +397,7 @@ __global__ void __launch_bounds__(256) k_mac_rhs(Grid g, const StepParams* __res
     const float wBack = z == 0 ? 0.0f : ldf(w + i - (size_t)g.nx * g.ny);
     float r = (uRight - uLeft) + (vTop - vBot) + (wFront - wBack);
     if (ref && y == g.ny - 1) r = r - top_pressure(g, *Pp, wave, x, z);
-    rhs[i] = r;
+    rhs[rb_index(g, x, y, z)] = r;
     part = (double)r;
   }
   if (sum) block_sum_atomic(part, sum);
@@ -409,12 +409,13 @@ __global__ void __launch_bounds__(256) k_project(Grid g, const StepParams* __res
                                                  const float* __restrict__ p, const float4* __restrict__ wave) {
   CELL_INDEX
   float mx = ldv(u + i), my = ldv(v + i), mz = ldv(w + i);
-  const float pC = p[i];
-  if (x < g.nx - 1) mx = mx - (p[i + 1] - pC); else mx = 0.0f;
-  if (y < g.ny - 1) my = my - (p[i + g.nx] - pC);
+  // p is red-black split: the +x, +y, +z neighbours are in the other half
+  const float pC = __ldg(p + rb_index(g, x, y, z));
+  if (x < g.nx - 1) mx = mx - (__ldg(p + rb_index(g, x + 1, y, z)) - pC); else mx = 0.0f;
+  if (y < g.ny - 1) my = my - (__ldg(p + rb_index(g, x, y + 1, z)) - pC);
   else if (ref) my = my - (top_pressure(g, *Pp, wave, x, z) - pC);
   else my = 0.0f;
-  if (z < g.nz - 1) mz = mz - (p[i + (size_t)g.nx * g.ny] - pC); else mz = 0.0f;
+  if (z < g.nz - 1) mz = mz - (__ldg(p + rb_index(g, x, y, z + 1)) - pC); else mz = 0.0f;
   if (ref) {
     mx = dob_clampf(mx, -2.0f, 2.0f); my = dob_clampf(my, -2.0f, 2.0f); mz = dob_clampf(mz, -2.0f, 2.0f);
   }
@@ -706,13 +707,14 @@ void launch_casson(const DevState& s, cudaStream_t st) {
 }
 
 void launch_mac_rhs(const DevState& s, cudaStream_t st) {
-  if (!s.ref) cudaMemsetAsync(s.red + RED_RHS_SUM, 0, sizeof(double), st);
   DOB_VEL_DISPATCH(s.prec, {
     k_mac_rhs<VS><<<cell_grid(s.g), cell_block(), 0, st>>>(s.g, s.params, s.ref, (const VS*)s.u, (const VS*)s.v,
-                                                           (const VS*)s.w, s.wave, s.rhs,
-                                                           s.ref ? nullptr : s.red + RED_RHS_SUM);
+                                                           (const VS*)s.w, s.wave, s.rhs, nullptr);
   });
-  if (!s.ref) launch_sub_mean(s.rhs, s.g.n(), s.red + RED_RHS_SUM, s.num_sms, st);
+  if (!s.ref) {  // compatibility of the pure-Neumann problem: zero-mean right-hand side
+    launch_sum(s.rhs, s.g.n(), s.red + RED_RHS_SUM, s.num_sms, st);
+    launch_sub_mean(s.rhs, s.g.n(), s.red + RED_RHS_SUM, s.num_sms, st);
+  }
 }
 
 void launch_project(const DevState& s, cudaStream_t st) {

@@ -3,23 +3,36 @@
 // grids, any pre/post sweep counts and several V-cycles per step, plus the
 // FP64 pieces: compatibility / mean sums and the mixed-precision defect loop.
 //
+// Memory layout: every multigrid array (pressure, right-hand side, the
+// corrections and right-hand sides of the coarse levels) is stored
+// red-black split: the cells of colour c = (x+y+z)&1 occupy half c of the
+// array, row-major with x/2 fastest (rb_index).  A half-sweep of one colour
+// then reads only the other half plus its own right-hand side and writes its
+// own half, with consecutive threads on consecutive words: 3 x N/2 words of
+// traffic instead of touching every line of both colours.
+//
 // Kernels:
-//   k_rbgs             one colour of red-black Gauss-Seidel, in place
-//                      (one thread per cell of that colour)
-//   k_residual_restrict residual b - A e of 8 fine cells averaged into one
-//                      coarse right-hand side (MG_RESIDUAL + MG_RESTRICT fused:
-//                      the fine residual is never stored)
-//   k_prolong_add      e_f += trilinear(e_c), cell-centred
-//   k_coarse_smem      all sweeps of the coarsest grid in one CTA's shared memory
-//   k_defect           FP64 residual of the FP32 pressure -> BF16, with its norm
+//   k_rbgs_split        one colour of red-black Gauss-Seidel (one thread per
+//                       cell of that colour, in place)
+//   k_residual_restrict residual b - A e of the 8 fine cells of a coarse cell,
+//                       averaged into its right-hand side (MG_RESIDUAL +
+//                       MG_RESTRICT fused: the fine residual is never stored)
+//   k_prolong_add       e_f += trilinear(e_c), cell-centred
+//   k_coarse_cluster    every sweep of the coarsest grid inside one
+//                       thread-block cluster: each CTA keeps a slab of planes in
+//                       shared memory, reads the neighbour slabs' boundary
+//                       planes through distributed shared memory, and the
+//                       half-sweeps are separated by hardware cluster barriers
+//   k_defect            FP64 residual of the FP32 pressure -> BF16, with its norm
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include "dob_kernels.cuh"
 
+namespace cg = cooperative_groups;
+
 namespace dob {
 
-// Round a value to the precision of the storage type T (the coarse solve keeps
-// its grid in FP32 shared memory but must reproduce T-typed storage).
 template <class T> __device__ __forceinline__ float as_stored(float v);
 template <> __device__ __forceinline__ float as_stored<float>(float v) { return v; }
 template <> __device__ __forceinline__ float as_stored<__nv_bfloat16>(float v) {
@@ -28,42 +41,150 @@ template <> __device__ __forceinline__ float as_stored<__nv_bfloat16>(float v) {
 
 __device__ __forceinline__ bool skip_now(const unsigned int* skip) { return skip != nullptr && *skip != 0u; }
 
-// evalMgStencil (fluid.ts:568-602): neighbour sum and diagonal count, in the
-// order x-, x+, y-, y+, z-, z+.  Reference BCs count the top face always
-// (Dirichlet 0 ghost); the closed box counts only existing neighbours.
+// evalMgStencil (fluid.ts:568-602) on a red-black split array: neighbour sum
+// and diagonal count in the order x-, x+, y-, y+, z-, z+.  Reference BCs
+// count the top face always (Dirichlet 0 ghost); the closed box counts only
+// existing neighbours.  `oth` is the other colour's half, `r` the row base
+// and k = x/2 of the cell.
 template <class T>
-__device__ __forceinline__ void stencil(const T* a, const Grid& d, int x, int y, int z, size_t i, int ref, float& sumN,
-                                        float& diag) {
+__device__ __forceinline__ void stencil_rb(const T* oth, const Grid& d, int x, int y, int z, size_t r, int k, int ref,
+                                           float& sumN, float& diag) {
+  const int hx = d.nx >> 1;
   sumN = 0.0f;
   diag = ref ? 1.0f : 0.0f;
-  const size_t sy = d.nx, sz = (size_t)d.nx * d.ny;
-  if (x > 0) { sumN = sumN + ldv(a + i - 1); diag = diag + 1.0f; }
-  if (x < d.nx - 1) { sumN = sumN + ldv(a + i + 1); diag = diag + 1.0f; }
-  if (y > 0) { sumN = sumN + ldv(a + i - sy); diag = diag + 1.0f; }
-  if (y < d.ny - 1) { sumN = sumN + ldv(a + i + sy); if (!ref) diag = diag + 1.0f; }
-  if (z > 0) { sumN = sumN + ldv(a + i - sz); diag = diag + 1.0f; }
-  if (z < d.nz - 1) { sumN = sumN + ldv(a + i + sz); diag = diag + 1.0f; }
+  if (x > 0) { sumN = sumN + ldv(oth + r + ((x - 1) >> 1)); diag = diag + 1.0f; }
+  if (x < d.nx - 1) { sumN = sumN + ldv(oth + r + ((x + 1) >> 1)); diag = diag + 1.0f; }
+  if (y > 0) { sumN = sumN + ldv(oth + r - hx + k); diag = diag + 1.0f; }
+  if (y < d.ny - 1) { sumN = sumN + ldv(oth + r + hx + k); if (!ref) diag = diag + 1.0f; }
+  if (z > 0) { sumN = sumN + ldv(oth + r - (size_t)d.ny * hx + k); diag = diag + 1.0f; }
+  if (z < d.nz - 1) { sumN = sumN + ldv(oth + r + (size_t)d.ny * hx + k); diag = diag + 1.0f; }
 }
 
-// One colour of RBGS (createMgRbgsShader, fluid.ts:605-681), in place: a
-// cell of one colour reads only cells of the other colour.
+// Value of the split array at natural coordinates.
 template <class T>
-__global__ void __launch_bounds__(256) k_rbgs(Grid d, int color, float h2, int ref, T* __restrict__ a,
-                                              const T* __restrict__ b, const unsigned int* __restrict__ skip) {
+__device__ __forceinline__ float rb_at(const T* a, const Grid& d, int x, int y, int z) {
+  return ldv(a + rb_index(d, x, y, z));
+}
+
+// One colour of RBGS (createMgRbgsShader, fluid.ts:605-681), in place.
+template <class T>
+__global__ void __launch_bounds__(256) k_rbgs_split(Grid d, int color, float h2, int ref, T* __restrict__ a,
+                                                    const T* __restrict__ b, const unsigned int* __restrict__ skip) {
   if (skip_now(skip)) return;
-  const int tx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int z = blockIdx.z;
-  const int x = 2 * tx + ((y + z + color) & 1);
-  if (x >= d.nx || y >= d.ny) return;
-  const size_t i = d.at(x, y, z);
-  float sumN, diag;
-  stencil(a, d, x, y, z, i, ref, sumN, diag);
-  stf(a + i, (sumN - h2 * ldv(b + i)) / diag);
+  const int hx = d.nx >> 1;
+  if (k >= hx || y >= d.ny) return;
+  const int x = 2 * k + ((y + z + color) & 1);
+  const size_t half = d.n() >> 1;
+  T* own = a + (size_t)color * half;
+  const T* oth = a + (size_t)(1 - color) * half;
+  const size_t r = ((size_t)z * d.ny + y) * hx;
+  const size_t i = r + k;
+  const float bv = ldv(b + (size_t)color * half + i);
+  float val;
+  if (x > 0 && x < d.nx - 1 && y > 0 && y < d.ny - 1 && z > 0 && z < d.nz - 1) {
+    // interior: six neighbours, diagonal 6 in both boundary modes
+    const size_t sz = (size_t)d.ny * hx;
+    const float sumN = ((((ldv(oth + r + ((x - 1) >> 1)) + ldv(oth + r + ((x + 1) >> 1))) + ldv(oth + i - hx)) +
+                         ldv(oth + i + hx)) + ldv(oth + i - sz)) + ldv(oth + i + sz);
+    val = (sumN - h2 * bv) * (1.0f / 6.0f);
+  } else {
+    float sumN, diag;
+    stencil_rb(oth, d, x, y, z, r, k, ref, sumN, diag);
+    val = (sumN - h2 * bv) / diag;
+  }
+  stf(own + i, val);
+}
+
+// Four consecutive cells of one colour in one row: (x, y, z) with
+// x = 2k + p, k = k0..k0+3 and the same parity p = (y + z + colour) & 1 for
+// all four, so their +-x neighbours in the other colour are words k0-1+p ..
+// k0+3+p of the same row (one 16-byte vector plus one scalar) and their
+// +-y / +-z neighbours and right-hand sides are 16-byte vectors too.
+template <class T> struct Vec4Ld;
+template <> struct Vec4Ld<float> {
+  __device__ __forceinline__ static float4 ld(const float* p) { return *reinterpret_cast<const float4*>(p); }
+  __device__ __forceinline__ static void st(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
+};
+template <> struct Vec4Ld<__nv_bfloat16> {
+  __device__ __forceinline__ static float4 ld(const __nv_bfloat16* p) {
+    const uint2 r = *reinterpret_cast<const uint2*>(p);
+    const __nv_bfloat162 a = *reinterpret_cast<const __nv_bfloat162*>(&r.x);
+    const __nv_bfloat162 b = *reinterpret_cast<const __nv_bfloat162*>(&r.y);
+    const float2 fa = __bfloat1622float2(a), fb = __bfloat1622float2(b);
+    return make_float4(fa.x, fa.y, fb.x, fb.y);
+  }
+  __device__ __forceinline__ static void st(__nv_bfloat16* p, float4 v) {
+    const __nv_bfloat162 a = __floats2bfloat162_rn(v.x, v.y);
+    const __nv_bfloat162 b = __floats2bfloat162_rn(v.z, v.w);
+    uint2 r;
+    r.x = *reinterpret_cast<const uint32_t*>(&a);
+    r.y = *reinterpret_cast<const uint32_t*>(&b);
+    *reinterpret_cast<uint2*>(p) = r;
+  }
+};
+__device__ __forceinline__ float f4get(const float4& v, int j) {
+  return j == 0 ? v.x : (j == 1 ? v.y : (j == 2 ? v.z : v.w));
+}
+
+// One colour of RBGS, four cells per thread (rows with nx % 8 == 0).
+template <class T>
+__global__ void __launch_bounds__(256) k_rbgs_v4(Grid d, int color, float h2, int ref, T* __restrict__ a,
+                                                 const T* __restrict__ b, const unsigned int* __restrict__ skip) {
+  if (skip_now(skip)) return;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  const int hx = d.nx >> 1;
+  const int k0 = 4 * q;
+  if (k0 >= hx || y >= d.ny) return;
+  const int p = (y + z + color) & 1;
+  const size_t half = d.n() >> 1;
+  T* own = a + (size_t)color * half;
+  const T* oth = a + (size_t)(1 - color) * half;
+  const size_t r = ((size_t)z * d.ny + y) * hx;
+  const size_t sz = (size_t)d.ny * hx;
+  const float4 bv = Vec4Ld<T>::ld(b + (size_t)color * half + r + k0);
+  const float4 cm = Vec4Ld<T>::ld(oth + r + k0);  // words k0..k0+3 of the other colour, same row
+  const bool yz_in = y > 0 && y < d.ny - 1 && z > 0 && z < d.nz - 1;
+  const bool x_in = (p == 1 || k0 > 0) && (p == 0 || k0 + 4 < hx);
+  float4 out;
+  if (yz_in && x_in) {
+    const float4 ym = Vec4Ld<T>::ld(oth + r - hx + k0), yp = Vec4Ld<T>::ld(oth + r + hx + k0);
+    const float4 zm = Vec4Ld<T>::ld(oth + r - sz + k0), zp = Vec4Ld<T>::ld(oth + r + sz + k0);
+    const float ex = p == 0 ? ldv(oth + r + k0 - 1) : ldv(oth + r + k0 + 4);  // the word outside the vector
+    float res[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const float xm = p == 0 ? (j == 0 ? ex : f4get(cm, j - 1)) : f4get(cm, j);
+      const float xp = p == 0 ? f4get(cm, j) : (j == 3 ? ex : f4get(cm, j + 1));
+      const float sumN = ((((xm + xp) + f4get(ym, j)) + f4get(yp, j)) + f4get(zm, j)) + f4get(zp, j);
+      res[j] = (sumN - h2 * f4get(bv, j)) * (1.0f / 6.0f);
+    }
+    out = make_float4(res[0], res[1], res[2], res[3]);
+  } else {
+    float res[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int k = k0 + j;
+      const int x = 2 * k + p;
+      float sumN, diag;
+      stencil_rb(oth, d, x, y, z, r, k, ref, sumN, diag);
+      res[j] = (sumN - h2 * f4get(bv, j)) / diag;
+    }
+    out = make_float4(res[0], res[1], res[2], res[3]);
+  }
+  Vec4Ld<T>::st(own + r + k0, out);
 }
 
 // MG_RESIDUAL + MG_RESTRICT (fluid.ts:744-800) fused: each thread owns one
-// coarse cell and averages the residual of its 8 fine cells (dz, dy, dx order).
+// coarse cell and averages the residual of its 8 fine cells (dz, dy, dx
+// order).  The 8 fine cells and the 24 cells around the faces of the 2x2x2
+// block are loaded once into registers (all at split index x/2 = X, except
+// the x-neighbours at X-1 and X+1), then the 8 residuals follow the
+// reference's stencil order exactly.
 template <class T, class TC>
 __global__ void __launch_bounds__(256) k_residual_restrict(Grid f, Grid c, float h2, int ref, const T* __restrict__ a,
                                                            const T* __restrict__ b, TC* __restrict__ bc,
@@ -73,6 +194,30 @@ __global__ void __launch_bounds__(256) k_residual_restrict(Grid f, Grid c, float
   const int Y = blockIdx.y * blockDim.y + threadIdx.y;
   const int Z = blockIdx.z;
   if (X >= c.nx || Y >= c.ny) return;
+  const size_t half = f.n() >> 1;
+  const int hx = f.nx >> 1;
+  const int x0 = 2 * X, y0 = 2 * Y, z0 = 2 * Z;
+  // value at fine (x0+ix, y0+iy, z0+iz), ix, iy, iz in [-1, 2]; 0 outside
+  auto P = [&](int ix, int iy, int iz) -> float {
+    const int x = x0 + ix, y = y0 + iy, z = z0 + iz;
+    if (x < 0 || x >= f.nx || y < 0 || y >= f.ny || z < 0 || z >= f.nz) return 0.0f;
+    return ldv(a + (size_t)((x + y + z) & 1) * half + ((size_t)z * f.ny + y) * hx + (x >> 1));
+  };
+  float blk[2][2][2], xm[2][2], xp[2][2], ym[2][2], yp[2][2], zm[2][2], zp[2][2];
+#pragma unroll
+  for (int dz = 0; dz < 2; ++dz)
+#pragma unroll
+    for (int dy = 0; dy < 2; ++dy)
+#pragma unroll
+      for (int dx = 0; dx < 2; ++dx) blk[dz][dy][dx] = P(dx, dy, dz);
+#pragma unroll
+  for (int u = 0; u < 2; ++u)
+#pragma unroll
+    for (int v = 0; v < 2; ++v) {
+      xm[u][v] = P(-1, v, u); xp[u][v] = P(2, v, u);
+      ym[u][v] = P(v, -1, u); yp[u][v] = P(v, 2, u);
+      zm[u][v] = P(v, u, -1); zp[u][v] = P(v, u, 2);
+    }
   float sum = 0.0f;
 #pragma unroll
   for (int dz = 0; dz < 2; ++dz)
@@ -80,14 +225,25 @@ __global__ void __launch_bounds__(256) k_residual_restrict(Grid f, Grid c, float
     for (int dy = 0; dy < 2; ++dy)
 #pragma unroll
       for (int dx = 0; dx < 2; ++dx) {
-        const int x = 2 * X + dx, y = 2 * Y + dy, z = 2 * Z + dz;
-        const size_t i = f.at(x, y, z);
-        float sumN, diag;
-        stencil(a, f, x, y, z, i, ref, sumN, diag);
-        const float lapScaled = (sumN - diag * ldv(a + i)) / h2;
-        sum = sum + (ldv(b + i) - lapScaled);
+        const int x = x0 + dx, y = y0 + dy, z = z0 + dz;
+        const float nxm = dx ? blk[dz][dy][0] : xm[dz][dy];
+        const float nxp = dx ? xp[dz][dy] : blk[dz][dy][1];
+        const float nym = dy ? blk[dz][0][dx] : ym[dz][dx];
+        const float nyp = dy ? yp[dz][dx] : blk[dz][1][dx];
+        const float nzm = dz ? blk[0][dy][dx] : zm[dy][dx];
+        const float nzp = dz ? zp[dy][dx] : blk[1][dy][dx];
+        float sumN = 0.0f, diag = ref ? 1.0f : 0.0f;
+        if (x > 0) { sumN = sumN + nxm; diag = diag + 1.0f; }
+        if (x < f.nx - 1) { sumN = sumN + nxp; diag = diag + 1.0f; }
+        if (y > 0) { sumN = sumN + nym; diag = diag + 1.0f; }
+        if (y < f.ny - 1) { sumN = sumN + nyp; if (!ref) diag = diag + 1.0f; }
+        if (z > 0) { sumN = sumN + nzm; diag = diag + 1.0f; }
+        if (z < f.nz - 1) { sumN = sumN + nzp; diag = diag + 1.0f; }
+        const float lapScaled = (sumN - diag * blk[dz][dy][dx]) / h2;
+        const float bv = ldv(b + (size_t)((x + y + z) & 1) * half + ((size_t)z * f.ny + y) * hx + X);
+        sum = sum + (bv - lapScaled);
       }
-  stf(bc + c.at(X, Y, Z), sum * 0.125f);
+  stf(bc + rb_index(c, X, Y, Z), sum * 0.125f);
 }
 
 // MG_PROLONG_ADD (fluid.ts:806-855): cell-centred trilinear interpolation of
@@ -96,31 +252,49 @@ __global__ void __launch_bounds__(256) k_residual_restrict(Grid f, Grid c, float
 template <class TC>
 __device__ __forceinline__ float coarse_err(const TC* e, const Grid& c, int ref, int x, int y, int z) {
   if (ref && y >= c.ny) return 0.0f;
-  return ldv(e + c.at(dob_clampi(x, 0, c.nx - 1), dob_clampi(y, 0, c.ny - 1), dob_clampi(z, 0, c.nz - 1)));
+  return rb_at(e, c, dob_clampi(x, 0, c.nx - 1), dob_clampi(y, 0, c.ny - 1), dob_clampi(z, 0, c.nz - 1));
 }
+// One thread per coarse cell (X,Y,Z) updates its 8 fine cells
+// (2X+dx, 2Y+dy, 2Z+dz): their trilinear taps all lie in the 3x3x3 coarse
+// neighbourhood, loaded once.  Each fine cell's coordinate and weights come
+// from the same per-cell formula as MG_PROLONG_ADD.
 template <class T, class TC>
 __global__ void __launch_bounds__(256) k_prolong_add(Grid f, Grid c, int ref, T* __restrict__ a,
                                                      const TC* __restrict__ e, const unsigned int* __restrict__ skip) {
   if (skip_now(skip)) return;
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = blockIdx.y * blockDim.y + threadIdx.y;
-  const int z = blockIdx.z;
-  if (x >= f.nx || y >= f.ny) return;
-  const float cx = (((float)x + 0.5f) / (float)f.nx) * (float)c.nx - 0.5f;
-  const float cy = (((float)y + 0.5f) / (float)f.ny) * (float)c.ny - 0.5f;
-  const float cz = (((float)z + 0.5f) / (float)f.nz) * (float)c.nz - 0.5f;
-  const float bx = floorf(cx), by = floorf(cy), bz = floorf(cz);
-  const int ix = (int)bx, iy = (int)by, iz = (int)bz;
-  const float fx = cx - bx, fy = cy - by, fz = cz - bz;
-  const float c000 = coarse_err(e, c, ref, ix, iy, iz), c100 = coarse_err(e, c, ref, ix + 1, iy, iz);
-  const float c010 = coarse_err(e, c, ref, ix, iy + 1, iz), c110 = coarse_err(e, c, ref, ix + 1, iy + 1, iz);
-  const float c001 = coarse_err(e, c, ref, ix, iy, iz + 1), c101 = coarse_err(e, c, ref, ix + 1, iy, iz + 1);
-  const float c011 = coarse_err(e, c, ref, ix, iy + 1, iz + 1), c111 = coarse_err(e, c, ref, ix + 1, iy + 1, iz + 1);
-  const float x00 = dob_mix(c000, c100, fx), x10 = dob_mix(c010, c110, fx);
-  const float x01 = dob_mix(c001, c101, fx), x11 = dob_mix(c011, c111, fx);
-  const float corr = dob_mix(dob_mix(x00, x10, fy), dob_mix(x01, x11, fy), fz);
-  const size_t i = f.at(x, y, z);
-  stf(a + i, ldv(a + i) + corr);
+  const int X = blockIdx.x * blockDim.x + threadIdx.x;
+  const int Y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int Z = blockIdx.z;
+  if (X >= c.nx || Y >= c.ny) return;
+  float t[3][3][3];  // coarse taps at (X-1+i, Y-1+j, Z-1+k)
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+      for (int i = 0; i < 3; ++i) t[k][j][i] = coarse_err(e, c, ref, X - 1 + i, Y - 1 + j, Z - 1 + k);
+  const size_t half = f.n() >> 1;
+  const int hx = f.nx >> 1;
+#pragma unroll
+  for (int dz = 0; dz < 2; ++dz)
+#pragma unroll
+    for (int dy = 0; dy < 2; ++dy)
+#pragma unroll
+      for (int dx = 0; dx < 2; ++dx) {
+        const int x = 2 * X + dx, y = 2 * Y + dy, z = 2 * Z + dz;
+        const float cx = (((float)x + 0.5f) / (float)f.nx) * (float)c.nx - 0.5f;
+        const float cy = (((float)y + 0.5f) / (float)f.ny) * (float)c.ny - 0.5f;
+        const float cz = (((float)z + 0.5f) / (float)f.nz) * (float)c.nz - 0.5f;
+        const float fx = cx - floorf(cx), fy = cy - floorf(cy), fz = cz - floorf(cz);
+        // base tap = X-1+dx (same for y, z): index dx, dy, dz into t
+        const float x00 = dob_mix(t[dz][dy][dx], t[dz][dy][dx + 1], fx);
+        const float x10 = dob_mix(t[dz][dy + 1][dx], t[dz][dy + 1][dx + 1], fx);
+        const float x01 = dob_mix(t[dz + 1][dy][dx], t[dz + 1][dy][dx + 1], fx);
+        const float x11 = dob_mix(t[dz + 1][dy + 1][dx], t[dz + 1][dy + 1][dx + 1], fx);
+        const float corr = dob_mix(dob_mix(x00, x10, fy), dob_mix(x01, x11, fy), fz);
+        const size_t i = (size_t)((x + y + z) & 1) * half + ((size_t)z * f.ny + y) * hx + X;
+        stf(a + i, ldv(a + i) + corr);
+      }
 }
 
 template <class T>
@@ -130,50 +304,96 @@ __global__ void k_fill_zero(T* __restrict__ a, size_t n, const unsigned int* __r
     a[i] = T(0.0f);
 }
 
-// MG_COARSE_SOLVE_L3 (fluid.ts:687-739) for any coarsest grid that fits in
-// shared memory: zero start, `sweeps` red-black sweeps, one CTA.
-template <class T>
-__global__ void __launch_bounds__(1024) k_coarse_smem(Grid d, float h2, int ref, int sweeps, T* __restrict__ e,
-                                                      const T* __restrict__ b, const unsigned int* __restrict__ skip) {
-  if (skip_now(skip)) return;
-  extern __shared__ float smem[];
-  const int n = (int)d.n();
-  float* se = smem;
-  float* sb = smem + n;
-  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+// MG_COARSE_SOLVE_L3 (fluid.ts:687-739) spread over a thread-block cluster of
+// CS CTAs: CTA r owns z-planes [r*pz, (r+1)*pz) of the coarsest grid (pz =
+// nz/CS) in its shared memory (natural layout), zero start, `sweeps` sweeps.
+// Neighbouring planes of other CTAs are read through distributed shared
+// memory; every half-sweep ends with a cluster barrier, so a colour only
+// ever reads the other colour's finished values, exactly like the
+// reference's single-workgroup solve.
+template <class T, int CS>
+__global__ void __cluster_dims__(CS, 1, 1) __launch_bounds__(512)
+    k_coarse_cluster(Grid d, float h2, int ref, int sweeps, T* __restrict__ e, const T* __restrict__ b,
+                     const unsigned int* __restrict__ skip) {
+  cg::cluster_group cl = cg::this_cluster();
+  extern __shared__ float csm[];
+  const int rank = (int)cl.block_rank();
+  const int pz = d.nz / CS;
+  const int plane = d.nx * d.ny;
+  const int nloc = pz * plane;
+  float* se = csm;
+  float* sb = csm + nloc;
+  const bool skipping = skip_now(skip);  // uniform: every CTA takes the same path
+  const int z0 = rank * pz;
+  for (int k = threadIdx.x; k < nloc; k += blockDim.x) {
+    const int zl = k / plane, rem = k - zl * plane;
+    const int y = rem / d.nx, x = rem - y * d.nx;
     se[k] = 0.0f;
-    sb[k] = ldv(b + k);
+    sb[k] = skipping ? 0.0f : rb_at(b, d, x, y, z0 + zl);
   }
-  __syncthreads();
-  const int sy = d.nx, sz = d.nx * d.ny;
-  for (int s = 0; s < sweeps; ++s) {
+  const float* below = rank > 0 ? cl.map_shared_rank(se, rank - 1) + (pz - 1) * plane : nullptr;
+  const float* above = rank < CS - 1 ? cl.map_shared_rank(se, rank + 1) : nullptr;
+  cl.sync();
+  const int nsw = skipping ? 0 : sweeps;
+  for (int s = 0; s < nsw; ++s) {
     for (int color = 0; color < 2; ++color) {
-      for (int k = threadIdx.x; k < n; k += blockDim.x) {
-        const int x = k % d.nx;
-        const int y = (k / d.nx) % d.ny;
-        const int z = k / sz;
-        if (((x + y + z) & 1) != color) continue;
+      const int hxc = d.nx >> 1;
+      for (int q = threadIdx.x; q < (nloc >> 1); q += blockDim.x) {  // the cells of this colour
+        const int row = q / hxc, kx = q - row * hxc;
+        const int zl = row / d.ny, y = row - zl * d.ny;
+        const int z = z0 + zl;
+        const int x = 2 * kx + ((y + z + color) & 1);
+        const int rem = y * d.nx + x;
+        const int k = zl * plane + rem;
         float sumN = 0.0f, diag = ref ? 1.0f : 0.0f;
         if (x > 0) { sumN = sumN + se[k - 1]; diag = diag + 1.0f; }
         if (x < d.nx - 1) { sumN = sumN + se[k + 1]; diag = diag + 1.0f; }
-        if (y > 0) { sumN = sumN + se[k - sy]; diag = diag + 1.0f; }
-        if (y < d.ny - 1) { sumN = sumN + se[k + sy]; if (!ref) diag = diag + 1.0f; }
-        if (z > 0) { sumN = sumN + se[k - sz]; diag = diag + 1.0f; }
-        if (z < d.nz - 1) { sumN = sumN + se[k + sz]; diag = diag + 1.0f; }
+        if (y > 0) { sumN = sumN + se[k - d.nx]; diag = diag + 1.0f; }
+        if (y < d.ny - 1) { sumN = sumN + se[k + d.nx]; if (!ref) diag = diag + 1.0f; }
+        if (z > 0) { sumN = sumN + (zl > 0 ? se[k - plane] : below[rem]); diag = diag + 1.0f; }
+        if (z < d.nz - 1) { sumN = sumN + (zl < pz - 1 ? se[k + plane] : above[rem]); diag = diag + 1.0f; }
         se[k] = as_stored<T>((sumN - h2 * sb[k]) / diag);
       }
-      __syncthreads();
+      cl.sync();
     }
   }
-  for (int k = threadIdx.x; k < n; k += blockDim.x) stf(e + k, se[k]);
+  if (!skipping)
+    for (int k = threadIdx.x; k < nloc; k += blockDim.x) {
+      const int zl = k / plane, rem = k - zl * plane;
+      const int y = rem / d.nx, x = rem - y * d.nx;
+      stf(e + rb_index(d, x, y, z0 + zl), se[k]);
+    }
+  cl.sync();  // keep this CTA's shared memory alive until its neighbours are done reading it
 }
 
 // ---- FP64 pieces ---------------------------------------------------------------------
+// Sum of a float array for the FP64 compatibility / mean sums.  Each thread
+// accumulates its strided elements as an unevaluated pair hi + lo of floats
+// with error-free TwoSum updates (Knuth, TAOCP vol. 2, 4.2.2), which keeps
+// the partial exact to about 2^-48 relative without FP64 work per element
+// (GB300's FP64 rate is a small fraction of its FP32 rate); the partials are
+// then reduced in FP64.
+__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
+  const float s = hi + x;
+  const float bp = s - hi;
+  const float err = (hi - (s - bp)) + (x - bp);
+  hi = s;
+  lo = lo + err;
+}
 __global__ void k_sum64(const float* __restrict__ a, size_t n, double* __restrict__ out) {
-  double s = 0.0;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    s += (double)a[i];
-  block_sum_atomic(s, out);
+  float hi = 0.0f, lo = 0.0f;
+  const size_t n4 = n >> 2;
+  const float4* a4 = reinterpret_cast<const float4*>(a);
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n4; i += (size_t)gridDim.x * blockDim.x) {
+    const float4 v = a4[i];
+    two_sum_acc(hi, lo, v.x);
+    two_sum_acc(hi, lo, v.y);
+    two_sum_acc(hi, lo, v.z);
+    two_sum_acc(hi, lo, v.w);
+  }
+  for (size_t i = 4 * n4 + blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    two_sum_acc(hi, lo, a[i]);
+  block_sum_atomic((double)hi + (double)lo, out);
 }
 __global__ void k_sumsq64(const float* __restrict__ a, size_t n, double* __restrict__ out) {
   double s = 0.0;
@@ -183,13 +403,25 @@ __global__ void k_sumsq64(const float* __restrict__ a, size_t n, double* __restr
   }
   block_sum_atomic(s, out);
 }
+// a[i] -= mean, with the mean summed in FP64 and applied in FP32.
 __global__ void k_sub_mean(float* __restrict__ a, size_t n, const double* __restrict__ sum) {
-  const double mean = *sum / (double)n;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    a[i] = (float)((double)a[i] - mean);
+  __shared__ float s_mean;
+  if (threadIdx.x == 0) s_mean = (float)(*sum / (double)n);
+  __syncthreads();
+  const float mean = s_mean;
+  const size_t n4 = n >> 2;
+  float4* a4 = reinterpret_cast<float4*>(a);
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n4; i += (size_t)gridDim.x * blockDim.x) {
+    float4 v = a4[i];
+    v.x = v.x - mean; v.y = v.y - mean; v.z = v.z - mean; v.w = v.w - mean;
+    a4[i] = v;
+  }
+  for (size_t i = 4 * n4 + blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    a[i] = a[i] - mean;
 }
 
-// r = b - A p in FP64 (FP32 inputs); optionally stored as BF16; ||r||^2 summed.
+// r = b - A p in FP64 (FP32 inputs, split layout); optionally stored as BF16
+// (split layout); ||r||^2 summed.
 __global__ void __launch_bounds__(256) k_defect(Grid d, float h2f, int ref, const float* __restrict__ p,
                                                 const float* __restrict__ b, __nv_bfloat16* __restrict__ r_out,
                                                 double* __restrict__ norm2, const unsigned int* __restrict__ skip) {
@@ -199,15 +431,14 @@ __global__ void __launch_bounds__(256) k_defect(Grid d, float h2f, int ref, cons
   const int z = blockIdx.z;
   double rr = 0.0;
   if (x < d.nx && y < d.ny) {
-    const size_t i = d.at(x, y, z);
-    const size_t sy = d.nx, sz = (size_t)d.nx * d.ny;
     double sumN = 0.0, diag = ref ? 1.0 : 0.0;
-    if (x > 0) { sumN += (double)p[i - 1]; diag += 1.0; }
-    if (x < d.nx - 1) { sumN += (double)p[i + 1]; diag += 1.0; }
-    if (y > 0) { sumN += (double)p[i - sy]; diag += 1.0; }
-    if (y < d.ny - 1) { sumN += (double)p[i + sy]; if (!ref) diag += 1.0; }
-    if (z > 0) { sumN += (double)p[i - sz]; diag += 1.0; }
-    if (z < d.nz - 1) { sumN += (double)p[i + sz]; diag += 1.0; }
+    if (x > 0) { sumN += (double)rb_at(p, d, x - 1, y, z); diag += 1.0; }
+    if (x < d.nx - 1) { sumN += (double)rb_at(p, d, x + 1, y, z); diag += 1.0; }
+    if (y > 0) { sumN += (double)rb_at(p, d, x, y - 1, z); diag += 1.0; }
+    if (y < d.ny - 1) { sumN += (double)rb_at(p, d, x, y + 1, z); if (!ref) diag += 1.0; }
+    if (z > 0) { sumN += (double)rb_at(p, d, x, y, z - 1); diag += 1.0; }
+    if (z < d.nz - 1) { sumN += (double)rb_at(p, d, x, y, z + 1); diag += 1.0; }
+    const size_t i = rb_index(d, x, y, z);
     const double r = (double)b[i] - (sumN - diag * (double)p[i]) / (double)h2f;
     if (r_out) r_out[i] = __float2bfloat16_rn((float)r);
     rr = r * r;
@@ -225,7 +456,7 @@ __global__ void k_defect_check(const double* __restrict__ rnorm2, const double* 
   else *iters += 1u;
 }
 
-// p += e (FP32 pressure, BF16 correction)
+// p += e (FP32 pressure, BF16 correction; same layout)
 __global__ void k_add_correction(float* __restrict__ p, const __nv_bfloat16* __restrict__ e, size_t n,
                                  const unsigned int* __restrict__ skip) {
   if (skip_now(skip)) return;
@@ -233,16 +464,46 @@ __global__ void k_add_correction(float* __restrict__ p, const __nv_bfloat16* __r
     p[i] = p[i] + __bfloat162float(e[i]);
 }
 
+// Natural <-> red-black split layout (host field I/O).
+__global__ void k_to_split(const float* __restrict__ nat, float* __restrict__ rb, Grid d) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  if (x >= d.nx || y >= d.ny) return;
+  rb[rb_index(d, x, y, z)] = nat[d.at(x, y, z)];
+}
+__global__ void k_from_split(const float* __restrict__ rb, float* __restrict__ nat, Grid d) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  if (x >= d.nx || y >= d.ny) return;
+  nat[d.at(x, y, z)] = rb[rb_index(d, x, y, z)];
+}
+
 // ---- host side ----------------------------------------------------------------------
 static inline dim3 g_cells(const Grid& d) { return dim3((d.nx + 31) / 32, (d.ny + 7) / 8, d.nz); }
 static inline dim3 g_half(const Grid& d) { return dim3((d.nx / 2 + 31) / 32, (d.ny + 7) / 8, d.nz); }
 static inline dim3 b_cells() { return dim3(32, 8, 1); }
 
+void launch_split(const float* src, float* dst, const Grid& d, bool to_split, cudaStream_t st) {
+  if (to_split) k_to_split<<<g_cells(d), b_cells(), 0, st>>>(src, dst, d);
+  else k_from_split<<<g_cells(d), b_cells(), 0, st>>>(src, dst, d);
+}
+
+template <class T, int CS>
+static cudaError_t cluster_attr() {
+  return cudaFuncSetAttribute(k_coarse_cluster<T, CS>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+}
+
 cudaError_t mg_prepare() {
-  const int bytes = 200 * 1024;
-  cudaError_t e = cudaFuncSetAttribute(k_coarse_smem<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_coarse_smem<__nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaError_t e = cluster_attr<float, 8>();
+  if (e == cudaSuccess) e = cluster_attr<float, 4>();
+  if (e == cudaSuccess) e = cluster_attr<float, 2>();
+  if (e == cudaSuccess) e = cluster_attr<float, 1>();
+  if (e == cudaSuccess) e = cluster_attr<__nv_bfloat16, 8>();
+  if (e == cudaSuccess) e = cluster_attr<__nv_bfloat16, 4>();
+  if (e == cudaSuccess) e = cluster_attr<__nv_bfloat16, 2>();
+  if (e == cudaSuccess) e = cluster_attr<__nv_bfloat16, 1>();
   return e;
 }
 
@@ -257,57 +518,77 @@ void launch_sumsq(const float* a, size_t n, double* out, int num_sms, cudaStream
   k_sumsq64<<<num_sms * 4, 256, 0, st>>>(a, n, out);
 }
 
+// `sweeps` red-black sweeps on level l, in place.  zero_first: the input is
+// zero (fill it); ec: coarse correction to add first.
 template <class T>
-static void smooth(const DevState& s, int l, T* a, const T* b, int sweeps, const unsigned int* skip, cudaStream_t st) {
+static void smooth(const DevState& s, int l, T* a, const T* b, int sweeps, bool zero_first, const T* ec,
+                   const unsigned int* skip, cudaStream_t st) {
   const MgLevel& L = s.lv[l];
-  for (int k = 0; k < sweeps; ++k) {
-    k_rbgs<T><<<g_half(L.d), b_cells(), 0, st>>>(L.d, 0, L.h2, s.ref, a, b, skip);
-    k_rbgs<T><<<g_half(L.d), b_cells(), 0, st>>>(L.d, 1, L.h2, s.ref, a, b, skip);
+  if (zero_first) k_fill_zero<T><<<s.num_sms * 2, 256, 0, st>>>(a, L.d.n(), skip);
+  if (ec) {
+    const Grid dc = s.lv[l + 1].d;
+    k_prolong_add<T, T><<<g_cells(dc), b_cells(), 0, st>>>(L.d, dc, s.ref, a, ec, skip);
   }
+  const bool v4 = (L.d.nx % 8) == 0;
+  const dim3 gq((L.d.nx / 8 + 31) / 32, (L.d.ny + 7) / 8, L.d.nz);
+  for (int k = 0; k < sweeps; ++k) {
+    for (int c = 0; c < 2; ++c) {
+      if (v4) k_rbgs_v4<T><<<gq, b_cells(), 0, st>>>(L.d, c, L.h2, s.ref, a, b, skip);
+      else k_rbgs_split<T><<<g_half(L.d), b_cells(), 0, st>>>(L.d, c, L.h2, s.ref, a, b, skip);
+    }
+  }
+}
+
+template <class T, int CS>
+static void launch_cluster(const MgLevel& L, int ref, int sweeps, T* e, const T* b, const unsigned int* skip,
+                           cudaStream_t st) {
+  const size_t smem = 2 * (L.d.n() / CS) * sizeof(float);
+  k_coarse_cluster<T, CS><<<CS, 512, smem, st>>>(L.d, L.h2, ref, sweeps, e, b, skip);
 }
 
 template <class T>
 static void coarse_solve(const DevState& s, int l, T* e, const T* b, const unsigned int* skip, cudaStream_t st) {
   const MgLevel& L = s.lv[l];
-  const size_t bytes = 2 * L.d.n() * sizeof(float);
-  if (bytes <= 200 * 1024) {
-    k_coarse_smem<T><<<1, 1024, bytes, st>>>(L.d, L.h2, s.ref, s.coarse_sweeps, e, b, skip);
-  } else {
-    k_fill_zero<T><<<s.num_sms, 256, 0, st>>>(e, L.d.n(), skip);
-    smooth<T>(s, l, e, b, s.coarse_sweeps, skip, st);
+  int cs = 0;
+  for (int c : {8, 4, 2, 1})
+    if (L.d.nz % c == 0 && 2 * (L.d.n() / c) * sizeof(float) <= 200 * 1024) { cs = c; break; }
+  switch (cs) {
+    case 8: launch_cluster<T, 8>(L, s.ref, s.coarse_sweeps, e, b, skip, st); break;
+    case 4: launch_cluster<T, 4>(L, s.ref, s.coarse_sweeps, e, b, skip, st); break;
+    case 2: launch_cluster<T, 2>(L, s.ref, s.coarse_sweeps, e, b, skip, st); break;
+    case 1: launch_cluster<T, 1>(L, s.ref, s.coarse_sweeps, e, b, skip, st); break;
+    default: smooth<T>(s, l, e, b, s.coarse_sweeps, true, nullptr, skip, st); break;
   }
 }
 
 // One V-cycle on (x0, b0); per-level arrays E[l], B[l] for l >= 1.
+// zero0: x0 is zero on entry.
 template <class T>
-static void vcycle(const DevState& s, T* x0, const T* b0, T* const* E, T* const* B, const unsigned int* skip,
-                   cudaStream_t st) {
+static void vcycle(const DevState& s, T* x0, const T* b0, T* const* E, T* const* B, bool zero0,
+                   const unsigned int* skip, cudaStream_t st) {
   const int L = s.nlev;
   if (L == 1) {
-    smooth<T>(s, 0, x0, b0, s.pre + s.post, skip, st);
+    smooth<T>(s, 0, x0, b0, s.pre + s.post, zero0, nullptr, skip, st);
     return;
   }
-  smooth<T>(s, 0, x0, b0, s.pre0, skip, st);
+  smooth<T>(s, 0, x0, b0, s.pre0, zero0, nullptr, skip, st);
   k_residual_restrict<T, T><<<g_cells(s.lv[1].d), b_cells(), 0, st>>>(s.lv[0].d, s.lv[1].d, s.lv[0].h2, s.ref, x0, b0,
                                                                       B[1], skip);
   for (int l = 1; l < L - 1; ++l) {
-    k_fill_zero<T><<<s.num_sms, 256, 0, st>>>(E[l], s.lv[l].d.n(), skip);
-    smooth<T>(s, l, E[l], B[l], s.pre, skip, st);
+    smooth<T>(s, l, E[l], B[l], s.pre, true, nullptr, skip, st);
     k_residual_restrict<T, T><<<g_cells(s.lv[l + 1].d), b_cells(), 0, st>>>(s.lv[l].d, s.lv[l + 1].d, s.lv[l].h2,
                                                                             s.ref, E[l], B[l], B[l + 1], skip);
   }
   coarse_solve<T>(s, L - 1, E[L - 1], B[L - 1], skip, st);
-  for (int l = L - 2; l >= 1; --l) {
-    k_prolong_add<T, T><<<g_cells(s.lv[l].d), b_cells(), 0, st>>>(s.lv[l].d, s.lv[l + 1].d, s.ref, E[l], E[l + 1], skip);
-    smooth<T>(s, l, E[l], B[l], s.post, skip, st);
-  }
-  k_prolong_add<T, T><<<g_cells(s.lv[0].d), b_cells(), 0, st>>>(s.lv[0].d, s.lv[1].d, s.ref, x0, E[1], skip);
-  smooth<T>(s, 0, x0, b0, s.post0, skip, st);
+  for (int l = L - 2; l >= 1; --l) smooth<T>(s, l, E[l], B[l], s.post, false, E[l + 1], skip, st);
+  smooth<T>(s, 0, x0, b0, s.post0, false, E[1], skip, st);
 }
 
 double smoother_pass(const DevState& s, cudaStream_t st) {
-  smooth<float>(s, 0, s.p, s.rhs, 1, nullptr, st);
-  return 12.0 * (double)s.g.n();
+  smooth<float>(s, 0, s.p, s.rhs, 1, false, nullptr, nullptr, st);
+  // a red and a black half-sweep each read the other colour's half and their
+  // own right-hand-side half and write their own half: 3 x N/2 words each
+  return 2.0 * 3.0 * 0.5 * 4.0 * (double)s.g.n();
 }
 
 void launch_residual_norm(const DevState& s, double* out, cudaStream_t st) {
@@ -316,32 +597,29 @@ void launch_residual_norm(const DevState& s, double* out, cudaStream_t st) {
 }
 
 void launch_pressure_solve(const DevState& s, cudaStream_t st) {
+  const size_t n = s.g.n();
   if (s.prec == DOB_PREC_MIXED) {
-    __nv_bfloat16* E[kMaxLevels];
-    __nv_bfloat16* B[kMaxLevels];
+    __nv_bfloat16 *E[kMaxLevels], *B[kMaxLevels];
     for (int l = 0; l < s.nlev; ++l) { E[l] = s.lv[l].eh; B[l] = s.lv[l].bh; }
     unsigned int* done = s.redu + REDU_DONE;
     cudaMemsetAsync(s.redu + REDU_DONE, 0, 2 * sizeof(unsigned int), st);  // done, iters
     cudaMemsetAsync(s.red + RED_RHS_NORM2, 0, sizeof(double) * (RED_COUNT - RED_RHS_NORM2), st);
-    k_sumsq64<<<s.num_sms * 4, 256, 0, st>>>(s.rhs, s.g.n(), s.red + RED_RHS_NORM2);
-    const size_t n = s.g.n();
+    k_sumsq64<<<s.num_sms * 4, 256, 0, st>>>(s.rhs, n, s.red + RED_RHS_NORM2);
     for (int it = 0; it < s.max_outer; ++it) {
       double* rn2 = s.red + RED_DEFECT_NORM2 + (it < 31 ? it : 31);
       k_defect<<<g_cells(s.g), b_cells(), 0, st>>>(s.g, s.lv[0].h2, s.ref, s.p, s.rhs, s.r0h, rn2, done);
       k_defect_check<<<1, 1, 0, st>>>(rn2, s.red + RED_RHS_NORM2, s.rel_tol, done, s.redu + REDU_ITERS);
-      k_fill_zero<__nv_bfloat16><<<s.num_sms * 4, 256, 0, st>>>(s.e0h, n, done);
-      for (int c = 0; c < s.cycles; ++c) vcycle<__nv_bfloat16>(s, s.e0h, s.r0h, E, B, done, st);
+      for (int c = 0; c < s.cycles; ++c) vcycle<__nv_bfloat16>(s, s.e0h, s.r0h, E, B, c == 0, done, st);
       k_add_correction<<<s.num_sms * 4, 256, 0, st>>>(s.p, s.e0h, n, done);
     }
   } else {
-    float* E[kMaxLevels];
-    float* B[kMaxLevels];
+    float *E[kMaxLevels], *B[kMaxLevels];
     for (int l = 0; l < s.nlev; ++l) { E[l] = s.lv[l].e; B[l] = s.lv[l].b; }
-    for (int c = 0; c < s.cycles; ++c) vcycle<float>(s, s.p, s.rhs, E, B, nullptr, st);
+    for (int c = 0; c < s.cycles; ++c) vcycle<float>(s, s.p, s.rhs, E, B, false, nullptr, st);
   }
   if (!s.ref) {
-    launch_sum(s.p, s.g.n(), s.red + RED_P_SUM, s.num_sms, st);
-    launch_sub_mean(s.p, s.g.n(), s.red + RED_P_SUM, s.num_sms, st);
+    launch_sum(s.p, n, s.red + RED_P_SUM, s.num_sms, st);
+    launch_sub_mean(s.p, n, s.red + RED_P_SUM, s.num_sms, st);
   }
 }
 

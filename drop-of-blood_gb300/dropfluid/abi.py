@@ -182,7 +182,7 @@ def config_closed_box(nx: int, ny: int, nz: int) -> DobConfig:
     c.mg_levels = 4
     c.mg_pre = 2
     c.mg_post = 2
-    c.mg_coarse_sweeps = 16
+    c.mg_coarse_sweeps = 6
     c.mg_cycles = 4
     c.mg_max_outer = 8
     c.mg_rel_tol = 1e-8

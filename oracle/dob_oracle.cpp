@@ -661,8 +661,8 @@ template <class R> class Sim {
           rhs[dv.at(x, y, z)] = r;
         }
     if (!ref) {  // compatibility: FP64 zero-mean right-hand side
-      const double mean = sum64(rhs) / (double)rhs.size();
-      for (auto& r : rhs) r = (R)((double)r - mean);
+      const R mean = (R)(sum64(rhs) / (double)rhs.size());
+      for (auto& r : rhs) r = r - mean;
     }
   }
   static double sum64(const std::vector<R>& a) {
@@ -845,8 +845,8 @@ template <class R> class Sim {
       for (int c = 0; c < cfg.mg_cycles; ++c) { vcycle(p.data(), rhs.data(), false); ++cycles; }
     }
     if (!ref) {  // pin the pressure mean (FP64 sum)
-      const double mean = sum64(p) / (double)p.size();
-      for (auto& q : p) q = (R)((double)q - mean);
+      const R mean = (R)(sum64(p) / (double)p.size());
+      for (auto& q : p) q = q - mean;
     }
     last_stats[3] = cycles;
     last_stats[4] = outer;
