@@ -855,3 +855,11 @@ dob_status dob_eval_math(int fn, const float* x, const float* y, float* out, uin
 }
 
 }  // extern "C"
+
+namespace dob {
+// Context-free error record for entry points defined in other translation
+// units; read back with dob_last_error(NULL).
+dob_status record_static_error(dob_status st, const char* what, const char* detail) {
+  return fail(nullptr, st, what, detail);
+}
+}  // namespace dob

@@ -43,6 +43,7 @@ SIGNATURES = {
     "dob_save_state": (C.c_int, [P, C.c_int]),
     "dob_load_state": (C.c_int, [P, C.c_int]),
     "dob_eval_math": (C.c_int, [C.c_int, FP, FP, FP, C.c_uint32]),
+    "dob_pressure_solve_noalloc": (C.c_int, [C.POINTER(abi.DobConfig), P, P, P]),
 }
 
 _lib = None

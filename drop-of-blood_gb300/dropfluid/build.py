@@ -25,6 +25,7 @@ UNITS = {
     "k_fluid.cu": [],
     "k_mg.cu": [],
     "k_exact.cu": ["-fmad=false"],
+    "dob_noalloc.cu": [],
 }
 
 

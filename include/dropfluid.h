@@ -266,6 +266,37 @@ dob_status dob_load_state(dob_ctx* ctx, int slot);
    8 f32->bf16->f32 round trip. */
 dob_status dob_eval_math(int fn, const float* x, const float* y, float* out, uint32_t n);
 
+/* ---- pressure solve without allocation (no counterpart in the reference) --
+
+   The multigrid pressure solve of one step (the same V-cycles as
+   DOB_STAGE_PRESSURE_SOLVE, including the zero-mean pressure of the closed
+   box) on caller-owned device buffers, for callers that cannot allocate
+   device memory: hosts whose own allocator owns the whole GPU, plugins
+   running inside such hosts, and frame loops that must not call cudaMalloc
+   or cudaFree (both synchronise the device and can fail mid-frame).  No
+   context is needed and nothing is allocated: the working arrays (split
+   copies, coarse grids, reduction slots) live in one fixed device array of
+   about 20 MiB that is part of the library and stays resident on every GPU
+   that loads it until the process exits.
+
+   rhs and pressure are device pointers of the current device, nx*ny*nz
+   floats each in the natural x-fastest layout; pressure is the initial
+   guess on entry and the solution on return.  From cfg only nx, ny, nz,
+   bc_mode, precision_mode (DOB_PREC_FP32 or DOB_PREC_REFERENCE_FP16; the
+   pressure is FP32 in both), mg_levels, mg_pre, mg_post, mg_coarse_sweeps,
+   mg_cycles and reference_schedule are read.  At most 2^21 cells
+   (2097152, e.g. 96x128x96 or 128^3): larger grids return DOB_EINVAL.
+   The work is queued on `stream` (a cudaStream_t; NULL is the default
+   stream) and the call returns without waiting for it.
+
+   Every call shares the one array and leaves its contents there: calls whose
+   work overlaps on the GPU (unordered streams, concurrent host threads)
+   race; order them on one stream.  The first call on each device performs a
+   one-time set-up with that device current (cudaGetSymbolAddress of the
+   array, the coarse-grid kernel's shared-memory limit); make it before any
+   stream capture.  Errors: dob_last_error(NULL). */
+dob_status dob_pressure_solve_noalloc(const dob_config* cfg, const float* rhs, float* pressure, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
