@@ -221,6 +221,9 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--profile-run", action="store_true",
+                    help="run only the FP32 scene (warm-up + steps, untimed) and exit: the command "
+                         "the ncu launch lists and kernel captures are taken with")
     args = ap.parse_args()
     rank, world, local = rank_info()
     if args.impl == "reference":
@@ -238,6 +241,10 @@ def main():
     eng = DropFluid(sc.config)
     run_scene_steps(sc, eng, 0, args.warmup, timed=False)
     eng.sync()
+    if args.profile_run:
+        run_scene_steps(sc, eng, args.warmup, args.steps, timed=False)
+        eng.sync()
+        return 0
     clocks = ClockSampler()
     clocks.start()
     dist.barrier()
