@@ -130,6 +130,14 @@ __device__ __forceinline__ float f4get(const float4& v, int j) {
 }
 
 // One colour of RBGS, four cells per thread (rows with nx % 8 == 0).
+// Block (bx, by): threadIdx.x runs over the Q = nx/8 quads of a row and
+// threadIdx.y over rows, so a warp holds whole rows back to back with no idle
+// lanes.  Boundaries are handled without divergence: a missing neighbour is
+// loaded from a clamped in-range address and enters the sum with weight 0
+// (adding an exact 0 leaves the sum unchanged, so the sum equals the
+// neighbour-skipping evalMgStencil order); only lanes whose diagonal is not 6
+// take the short IEEE-division branch.  Offsets are 32-bit (split halves have
+// fewer than 2^30 words).
 template <class T>
 __global__ void __launch_bounds__(256) k_rbgs_v4(Grid d, int color, float h2, int ref, T* __restrict__ a,
                                                  const T* __restrict__ b, const unsigned int* __restrict__ skip) {
@@ -137,46 +145,51 @@ __global__ void __launch_bounds__(256) k_rbgs_v4(Grid d, int color, float h2, in
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int z = blockIdx.z;
-  const int hx = d.nx >> 1;
-  const int k0 = 4 * q;
+  const uint32_t hx = (uint32_t)d.nx >> 1;
+  const uint32_t k0 = 4u * (uint32_t)q;
   if (k0 >= hx || y >= d.ny) return;
   const int p = (y + z + color) & 1;
-  const size_t half = d.n() >> 1;
-  T* own = a + (size_t)color * half;
-  const T* oth = a + (size_t)(1 - color) * half;
-  const size_t r = ((size_t)z * d.ny + y) * hx;
-  const size_t sz = (size_t)d.ny * hx;
-  const float4 bv = Vec4Ld<T>::ld(b + (size_t)color * half + r + k0);
+  const uint32_t half = (uint32_t)(d.n() >> 1);
+  const uint32_t sz = (uint32_t)d.ny * hx;
+  const uint32_t r = (uint32_t)z * sz + (uint32_t)y * hx;
+  T* own = a + (color ? half : 0u);
+  const T* oth = a + (color ? 0u : half);
+  // neighbour rows, clamped to the own row when absent (weight 0)
+  const bool has_ym = y > 0, has_yp = y < d.ny - 1, has_zm = z > 0, has_zp = z < d.nz - 1;
+  const uint32_t rym = has_ym ? r - hx : r, ryp = has_yp ? r + hx : r;
+  const uint32_t rzm = has_zm ? r - sz : r, rzp = has_zp ? r + sz : r;
+  const float4 bv = Vec4Ld<T>::ld(b + (color ? half : 0u) + r + k0);
   const float4 cm = Vec4Ld<T>::ld(oth + r + k0);  // words k0..k0+3 of the other colour, same row
-  const bool yz_in = y > 0 && y < d.ny - 1 && z > 0 && z < d.nz - 1;
-  const bool x_in = (p == 1 || k0 > 0) && (p == 0 || k0 + 4 < hx);
-  float4 out;
-  if (yz_in && x_in) {
-    const float4 ym = Vec4Ld<T>::ld(oth + r - hx + k0), yp = Vec4Ld<T>::ld(oth + r + hx + k0);
-    const float4 zm = Vec4Ld<T>::ld(oth + r - sz + k0), zp = Vec4Ld<T>::ld(oth + r + sz + k0);
-    const float ex = p == 0 ? ldv(oth + r + k0 - 1) : ldv(oth + r + k0 + 4);  // the word outside the vector
-    float res[4];
+  const float4 ym = Vec4Ld<T>::ld(oth + rym + k0), yp = Vec4Ld<T>::ld(oth + ryp + k0);
+  const float4 zm = Vec4Ld<T>::ld(oth + rzm + k0), zp = Vec4Ld<T>::ld(oth + rzp + k0);
+  // the word outside the vector: k0-1 (p = 0) or k0+4 (p = 1), absent at the row ends
+  const bool has_ex = p == 0 ? k0 > 0 : k0 + 4 < hx;
+  const uint32_t kex = p == 0 ? (has_ex ? k0 - 1 : k0) : (has_ex ? k0 + 4 : k0 + 3);
+  const float ex = ldv(oth + r + kex);
+  const float wex = has_ex ? 1.0f : 0.0f;
+  const float wym = has_ym ? 1.0f : 0.0f, wyp = has_yp ? 1.0f : 0.0f;
+  const float wzm = has_zm ? 1.0f : 0.0f, wzp = has_zp ? 1.0f : 0.0f;
+  // diagonal without the x neighbours: y-, z-, z+ faces that exist, plus the
+  // +y face (always counted with the reference's Dirichlet top)
+  const float dyz = (wym + wzm + wzp) + (ref ? 1.0f : wyp);
+  float res[4];
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const float xm = p == 0 ? (j == 0 ? ex : f4get(cm, j - 1)) : f4get(cm, j);
-      const float xp = p == 0 ? f4get(cm, j) : (j == 3 ? ex : f4get(cm, j + 1));
-      const float sumN = ((((xm + xp) + f4get(ym, j)) + f4get(yp, j)) + f4get(zm, j)) + f4get(zp, j);
-      res[j] = (sumN - h2 * f4get(bv, j)) * (1.0f / 6.0f);
-    }
-    out = make_float4(res[0], res[1], res[2], res[3]);
-  } else {
-    float res[4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int k = k0 + j;
-      const int x = 2 * k + p;
-      float sumN, diag;
-      stencil_rb(oth, d, x, y, z, r, k, ref, sumN, diag);
-      res[j] = (sumN - h2 * f4get(bv, j)) / diag;
-    }
-    out = make_float4(res[0], res[1], res[2], res[3]);
+  for (int j = 0; j < 4; ++j) {
+    const float xm = p == 0 ? (j == 0 ? ex : f4get(cm, j - 1)) : f4get(cm, j);
+    const float xp = p == 0 ? f4get(cm, j) : (j == 3 ? ex : f4get(cm, j + 1));
+    const float wxm = (p == 0 && j == 0) ? wex : 1.0f;
+    const float wxp = (p == 1 && j == 3) ? wex : 1.0f;
+    float sumN = wxm * xm;
+    sumN = fmaf(wxp, xp, sumN);
+    sumN = fmaf(wym, f4get(ym, j), sumN);
+    sumN = fmaf(wyp, f4get(yp, j), sumN);
+    sumN = fmaf(wzm, f4get(zm, j), sumN);
+    sumN = fmaf(wzp, f4get(zp, j), sumN);
+    const float diag = dyz + (wxm + wxp);
+    const float t = sumN - h2 * f4get(bv, j);
+    res[j] = diag == 6.0f ? t * (1.0f / 6.0f) : t / diag;
   }
-  Vec4Ld<T>::st(own + r + k0, out);
+  Vec4Ld<T>::st(own + r + k0, make_float4(res[0], res[1], res[2], res[3]));
 }
 
 // MG_RESIDUAL + MG_RESTRICT (fluid.ts:744-800) fused: each thread owns one
@@ -484,6 +497,18 @@ __global__ void k_from_split(const float* __restrict__ rb, float* __restrict__ n
 static inline dim3 g_cells(const Grid& d) { return dim3((d.nx + 31) / 32, (d.ny + 7) / 8, d.nz); }
 static inline dim3 g_half(const Grid& d) { return dim3((d.nx / 2 + 31) / 32, (d.ny + 7) / 8, d.nz); }
 static inline dim3 b_cells() { return dim3(32, 8, 1); }
+// k_rbgs_v4 launch shape: x over the nx/8 quads of a row, y over rows.
+static inline dim3 quad_block(const Grid& d) {
+  const int q = d.nx / 8;
+  const int bx = q < 256 ? q : 256;
+  int by = 256 / bx;
+  if (by > d.ny) by = d.ny;
+  return dim3(bx, by, 1);
+}
+static inline dim3 quad_grid(const Grid& d, const dim3& b) {
+  const int q = d.nx / 8;
+  return dim3((q + b.x - 1) / b.x, (d.ny + b.y - 1) / b.y, d.nz);
+}
 
 void launch_split(const float* src, float* dst, const Grid& d, bool to_split, cudaStream_t st) {
   if (to_split) k_to_split<<<g_cells(d), b_cells(), 0, st>>>(src, dst, d);
@@ -530,10 +555,10 @@ static void smooth(const DevState& s, int l, T* a, const T* b, int sweeps, bool 
     k_prolong_add<T, T><<<g_cells(dc), b_cells(), 0, st>>>(L.d, dc, s.ref, a, ec, skip);
   }
   const bool v4 = (L.d.nx % 8) == 0;
-  const dim3 gq((L.d.nx / 8 + 31) / 32, (L.d.ny + 7) / 8, L.d.nz);
+  const dim3 bq = quad_block(L.d), gq = quad_grid(L.d, bq);
   for (int k = 0; k < sweeps; ++k) {
     for (int c = 0; c < 2; ++c) {
-      if (v4) k_rbgs_v4<T><<<gq, b_cells(), 0, st>>>(L.d, c, L.h2, s.ref, a, b, skip);
+      if (v4) k_rbgs_v4<T><<<gq, bq, 0, st>>>(L.d, c, L.h2, s.ref, a, b, skip);
       else k_rbgs_split<T><<<g_half(L.d), b_cells(), 0, st>>>(L.d, c, L.h2, s.ref, a, b, skip);
     }
   }
