@@ -310,6 +310,194 @@ __global__ void __launch_bounds__(256) k_prolong_add(Grid f, Grid c, int ref, T*
       }
 }
 
+// ---- two coarse cells per thread (fine rows with nx % 4 == 0) ----------------------------
+// Thread q owns coarse cells X = 2q, 2q+1 of coarse row (Y, Z), i.e. fine
+// cells x = 4q..4q+3 of the fine rows y0+dy, z0+dz.  In the split layout the
+// even cells x = 4q, 4q+2 of a fine row are words 2q, 2q+1 of one half and the
+// odd cells x = 4q+1, 4q+3 the same words of the other half, so each fine row
+// is two 8-byte loads; consecutive threads read consecutive words.
+template <class T> struct Pair;
+template <> struct Pair<float> {
+  __device__ __forceinline__ static float2 ld(const float* p) { return *reinterpret_cast<const float2*>(p); }
+  __device__ __forceinline__ static void st(float* p, float2 v) { *reinterpret_cast<float2*>(p) = v; }
+};
+template <> struct Pair<__nv_bfloat16> {
+  __device__ __forceinline__ static float2 ld(const __nv_bfloat16* p) {
+    return __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(p));
+  }
+  __device__ __forceinline__ static void st(__nv_bfloat16* p, float2 v) {
+    *reinterpret_cast<__nv_bfloat162*>(p) = __floats2bfloat162_rn(v.x, v.y);
+  }
+};
+// The four cells x = 4q..4q+3 of fine row (y, z) in natural order.
+struct Row4 {
+  float v[4];
+};
+template <class T>
+__device__ __forceinline__ Row4 ld_row4(const T* a, uint32_t half, uint32_t r, uint32_t w, int par) {
+  // par = (y + z) & 1: colour of the even cells
+  const float2 e = Pair<T>::ld(a + (par ? half : 0u) + r + w);
+  const float2 o = Pair<T>::ld(a + (par ? 0u : half) + r + w);
+  Row4 R;
+  R.v[0] = e.x; R.v[1] = o.x; R.v[2] = e.y; R.v[3] = o.y;
+  return R;
+}
+
+// MG_RESIDUAL + MG_RESTRICT fused, two coarse cells per thread.  Per fine
+// cell the neighbour sum follows evalMgStencil's order (x-, x+, y-, y+, z-,
+// z+) with absent neighbours entering as exact zeros, so every residual and
+// the (dz, dy, dx) averaging order match k_residual_restrict.  1/h2 is a power
+// of two, so scaling by it equals the division.
+template <class T, class TC>
+__global__ void __launch_bounds__(256) k_residual_restrict2(Grid f, Grid c, float inv_h2, int ref,
+                                                            const T* __restrict__ a, const T* __restrict__ b,
+                                                            TC* __restrict__ bc, const unsigned int* __restrict__ skip) {
+  if (skip_now(skip)) return;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int Y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int Z = blockIdx.z;
+  if (2 * q >= c.nx || Y >= c.ny) return;
+  const uint32_t hx = (uint32_t)f.nx >> 1, half = (uint32_t)(f.n() >> 1), sz = (uint32_t)f.ny * hx;
+  const uint32_t w = 2u * (uint32_t)q;
+  const int y0 = 2 * Y, z0 = 2 * Z;
+  auto rowb = [&](int y, int z) -> uint32_t { return (uint32_t)z * sz + (uint32_t)y * hx; };
+  // block rows B[dz][dy], their x-neighbours, and the rows around the block
+  Row4 B[2][2], Bb[2][2], Ym[2], Yp[2], Zm[2], Zp[2];
+  float exm[2][2], exp_[2][2];
+  const bool has_xm = q > 0, has_xp = 2 * q + 2 < c.nx;
+#pragma unroll
+  for (int dz = 0; dz < 2; ++dz)
+#pragma unroll
+    for (int dy = 0; dy < 2; ++dy) {
+      const int y = y0 + dy, z = z0 + dz, par = (y + z) & 1;
+      const uint32_t r = rowb(y, z);
+      B[dz][dy] = ld_row4(a, half, r, w, par);
+      Bb[dz][dy] = ld_row4(b, half, r, w, par);
+      // x = 4q-1 is odd (half !par, word 2q-1); x = 4q+4 is even (half par, word 2q+2)
+      exm[dz][dy] = ldv(a + (par ? 0u : half) + r + (has_xm ? w - 1 : w));
+      exp_[dz][dy] = ldv(a + (par ? half : 0u) + r + (has_xp ? w + 2 : w + 1));
+    }
+  const bool has_ym = y0 > 0, has_yp = y0 + 2 < f.ny, has_zm = z0 > 0, has_zp = z0 + 2 < f.nz;
+#pragma unroll
+  for (int u = 0; u < 2; ++u) {
+    const int ym = has_ym ? y0 - 1 : y0, yp = has_yp ? y0 + 2 : y0 + 1;
+    const int zm = has_zm ? z0 - 1 : z0, zp = has_zp ? z0 + 2 : z0 + 1;
+    Ym[u] = ld_row4(a, half, rowb(ym, z0 + u), w, (ym + z0 + u) & 1);
+    Yp[u] = ld_row4(a, half, rowb(yp, z0 + u), w, (yp + z0 + u) & 1);
+    Zm[u] = ld_row4(a, half, rowb(y0 + u, zm), w, (y0 + u + zm) & 1);
+    Zp[u] = ld_row4(a, half, rowb(y0 + u, zp), w, (y0 + u + zp) & 1);
+  }
+  const float wxm0 = has_xm ? 1.0f : 0.0f, wxp3 = has_xp ? 1.0f : 0.0f;
+  float sum[2] = {0.0f, 0.0f};
+#pragma unroll
+  for (int dz = 0; dz < 2; ++dz)
+#pragma unroll
+    for (int dy = 0; dy < 2; ++dy) {
+      const float wym = (dy == 1 || has_ym) ? 1.0f : 0.0f;
+      const float wyp = (dy == 0 || has_yp) ? 1.0f : 0.0f;
+      const float wzm = (dz == 1 || has_zm) ? 1.0f : 0.0f;
+      const float wzp = (dz == 0 || has_zp) ? 1.0f : 0.0f;
+      const float dyz = (wym + wzm + wzp) + (ref ? 1.0f : wyp);
+      const Row4& P = B[dz][dy];
+      const Row4& Pym = dy ? B[dz][0] : Ym[dz];
+      const Row4& Pyp = dy ? Yp[dz] : B[dz][1];
+      const Row4& Pzm = dz ? B[0][dy] : Zm[dy];
+      const Row4& Pzp = dz ? Zp[dy] : B[1][dy];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const float xm = i > 0 ? P.v[i - 1] : exm[dz][dy];
+        const float xp = i < 3 ? P.v[i + 1] : exp_[dz][dy];
+        const float wxm = i == 0 ? wxm0 : 1.0f;
+        const float wxp = i == 3 ? wxp3 : 1.0f;
+        float sumN = wxm * xm;
+        sumN = fmaf(wxp, xp, sumN);
+        sumN = fmaf(wym, Pym.v[i], sumN);
+        sumN = fmaf(wyp, Pyp.v[i], sumN);
+        sumN = fmaf(wzm, Pzm.v[i], sumN);
+        sumN = fmaf(wzp, Pzp.v[i], sumN);
+        const float diag = dyz + (wxm + wxp);
+        const float lap = (sumN - diag * P.v[i]) * inv_h2;
+        sum[i >> 1] = sum[i >> 1] + (Bb[dz][dy].v[i] - lap);
+      }
+    }
+  const uint32_t hc = (uint32_t)c.nx >> 1, halfc = (uint32_t)(c.n() >> 1);
+  const uint32_t rc = ((uint32_t)Z * c.ny + Y) * hc + (uint32_t)q;
+  const int pc = (Y + Z) & 1;  // colour of coarse X = 2q
+  stf(bc + (pc ? halfc : 0u) + rc, sum[0] * 0.125f);
+  stf(bc + (pc ? 0u : halfc) + rc, sum[1] * 0.125f);
+}
+
+// MG_PROLONG_ADD, two coarse cells per thread: the coarse taps X-1..X+2 x
+// Y-1..Y+1 x Z-1..Z+1 (clamped; 0 above a Dirichlet top) are loaded once and
+// the 16 fine cells are updated with two 8-byte read-modify-writes per fine
+// row.  Weights use the same per-cell formula as k_prolong_add.
+template <class T, class TC>
+__global__ void __launch_bounds__(256) k_prolong_add2(Grid f, Grid c, int ref, T* __restrict__ a,
+                                                      const TC* __restrict__ e, const unsigned int* __restrict__ skip) {
+  if (skip_now(skip)) return;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int Y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int Z = blockIdx.z;
+  if (2 * q >= c.nx || Y >= c.ny) return;
+  const uint32_t hc = (uint32_t)c.nx >> 1, halfc = (uint32_t)(c.n() >> 1);
+  float t[3][3][4];  // coarse taps at (2q-1+i, Y-1+j, Z-1+k)
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const int yy = Y - 1 + j, zz = dob_clampi(Z - 1 + k, 0, c.nz - 1);
+      const bool zero_row = ref && yy >= c.ny;
+      const int yc = dob_clampi(yy, 0, c.ny - 1);
+      const uint32_t rc = ((uint32_t)zz * c.ny + yc) * hc;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int xx = dob_clampi(2 * q - 1 + i, 0, c.nx - 1);
+        const float v = ldf(e + (((xx + yc + zz) & 1) ? halfc : 0u) + rc + (uint32_t)(xx >> 1));
+        t[k][j][i] = zero_row ? 0.0f : v;
+      }
+    }
+  const uint32_t hx = (uint32_t)f.nx >> 1, half = (uint32_t)(f.n() >> 1), sz = (uint32_t)f.ny * hx;
+  const uint32_t w = 2u * (uint32_t)q;
+  // fractional coordinates: x = 4q + i, y = 2Y + dy, z = 2Z + dz
+  float fxv[4], fyv[2], fzv[2];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const float cx = (((float)(4 * q + i) + 0.5f) / (float)f.nx) * (float)c.nx - 0.5f;
+    fxv[i] = cx - floorf(cx);
+  }
+#pragma unroll
+  for (int d = 0; d < 2; ++d) {
+    const float cy = (((float)(2 * Y + d) + 0.5f) / (float)f.ny) * (float)c.ny - 0.5f;
+    const float cz = (((float)(2 * Z + d) + 0.5f) / (float)f.nz) * (float)c.nz - 0.5f;
+    fyv[d] = cy - floorf(cy);
+    fzv[d] = cz - floorf(cz);
+  }
+#pragma unroll
+  for (int dz = 0; dz < 2; ++dz)
+#pragma unroll
+    for (int dy = 0; dy < 2; ++dy) {
+      const int y = 2 * Y + dy, z = 2 * Z + dz, par = (y + z) & 1;
+      const uint32_t r = (uint32_t)z * sz + (uint32_t)y * hx + w;
+      float corr[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        // fine x = 4q+i: base coarse tap 2q-1 + (i+1)/2 -> index (i+1)>>1 into t
+        const int bi = (i + 1) >> 1;
+        const float fx = fxv[i], fy = fyv[dy], fz = fzv[dz];
+        const float x00 = dob_mix(t[dz][dy][bi], t[dz][dy][bi + 1], fx);
+        const float x10 = dob_mix(t[dz][dy + 1][bi], t[dz][dy + 1][bi + 1], fx);
+        const float x01 = dob_mix(t[dz + 1][dy][bi], t[dz + 1][dy][bi + 1], fx);
+        const float x11 = dob_mix(t[dz + 1][dy + 1][bi], t[dz + 1][dy + 1][bi + 1], fx);
+        corr[i] = dob_mix(dob_mix(x00, x10, fy), dob_mix(x01, x11, fy), fz);
+      }
+      T* pe = a + (par ? half : 0u) + r;
+      T* po = a + (par ? 0u : half) + r;
+      const float2 ve = Pair<T>::ld(pe), vo = Pair<T>::ld(po);
+      Pair<T>::st(pe, make_float2(ve.x + corr[0], ve.y + corr[2]));
+      Pair<T>::st(po, make_float2(vo.x + corr[1], vo.y + corr[3]));
+    }
+}
+
 template <class T>
 __global__ void k_fill_zero(T* __restrict__ a, size_t n, const unsigned int* __restrict__ skip) {
   if (skip_now(skip)) return;
@@ -505,6 +693,30 @@ static inline dim3 quad_block(const Grid& d) {
   if (by > d.ny) by = d.ny;
   return dim3(bx, by, 1);
 }
+// k_residual_restrict2 / k_prolong_add2 launch shape over the coarse grid:
+// x over the nx/2 coarse pairs of a row, y over coarse rows.
+static inline dim3 pair_block(const Grid& c) {
+  const int q = c.nx / 2;
+  const int bx = q < 256 ? q : 256;
+  int by = 256 / bx;
+  if (by > c.ny) by = c.ny;
+  return dim3(bx, by, 1);
+}
+static inline dim3 pair_grid(const Grid& c, const dim3& b) {
+  const int q = c.nx / 2;
+  return dim3((q + b.x - 1) / b.x, (c.ny + b.y - 1) / b.y, c.nz);
+}
+template <class T>
+static void restrict_level(const DevState& s, int l, const T* x, const T* b, T* bc, const unsigned int* skip,
+                           cudaStream_t st) {
+  const Grid f = s.lv[l].d, c = s.lv[l + 1].d;
+  if (f.nx % 4 == 0) {
+    const dim3 bp = pair_block(c);
+    k_residual_restrict2<T, T><<<pair_grid(c, bp), bp, 0, st>>>(f, c, 1.0f / s.lv[l].h2, s.ref, x, b, bc, skip);
+  } else {
+    k_residual_restrict<T, T><<<g_cells(c), b_cells(), 0, st>>>(f, c, s.lv[l].h2, s.ref, x, b, bc, skip);
+  }
+}
 static inline dim3 quad_grid(const Grid& d, const dim3& b) {
   const int q = d.nx / 8;
   return dim3((q + b.x - 1) / b.x, (d.ny + b.y - 1) / b.y, d.nz);
@@ -552,7 +764,12 @@ static void smooth(const DevState& s, int l, T* a, const T* b, int sweeps, bool 
   if (zero_first) k_fill_zero<T><<<s.num_sms * 2, 256, 0, st>>>(a, L.d.n(), skip);
   if (ec) {
     const Grid dc = s.lv[l + 1].d;
-    k_prolong_add<T, T><<<g_cells(dc), b_cells(), 0, st>>>(L.d, dc, s.ref, a, ec, skip);
+    if (L.d.nx % 4 == 0) {
+      const dim3 bp = pair_block(dc);
+      k_prolong_add2<T, T><<<pair_grid(dc, bp), bp, 0, st>>>(L.d, dc, s.ref, a, ec, skip);
+    } else {
+      k_prolong_add<T, T><<<g_cells(dc), b_cells(), 0, st>>>(L.d, dc, s.ref, a, ec, skip);
+    }
   }
   const bool v4 = (L.d.nx % 8) == 0;
   const dim3 bq = quad_block(L.d), gq = quad_grid(L.d, bq);
@@ -597,12 +814,10 @@ static void vcycle(const DevState& s, T* x0, const T* b0, T* const* E, T* const*
     return;
   }
   smooth<T>(s, 0, x0, b0, s.pre0, zero0, nullptr, skip, st);
-  k_residual_restrict<T, T><<<g_cells(s.lv[1].d), b_cells(), 0, st>>>(s.lv[0].d, s.lv[1].d, s.lv[0].h2, s.ref, x0, b0,
-                                                                      B[1], skip);
+  restrict_level<T>(s, 0, x0, b0, B[1], skip, st);
   for (int l = 1; l < L - 1; ++l) {
     smooth<T>(s, l, E[l], B[l], s.pre, true, nullptr, skip, st);
-    k_residual_restrict<T, T><<<g_cells(s.lv[l + 1].d), b_cells(), 0, st>>>(s.lv[l].d, s.lv[l + 1].d, s.lv[l].h2,
-                                                                            s.ref, E[l], B[l], B[l + 1], skip);
+    restrict_level<T>(s, l, E[l], B[l], B[l + 1], skip, st);
   }
   coarse_solve<T>(s, L - 1, E[L - 1], B[L - 1], skip, st);
   for (int l = L - 2; l >= 1; --l) smooth<T>(s, l, E[l], B[l], s.post, false, E[l + 1], skip, st);
