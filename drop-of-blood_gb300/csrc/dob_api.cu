@@ -21,42 +21,7 @@
 
 using namespace dob;
 
-namespace {
-
-constexpr int kParamRing = 16;
-constexpr int kSnapshots = 8;
-
-struct Snapshot {
-  std::vector<void*> bufs;
-  std::vector<size_t> sizes;
-  uint32_t high_water = 0;
-  int step_index = 0;
-  bool valid = false;
-};
-
-}  // namespace
-
-struct dob_ctx {
-  dob_config cfg;
-  DevState s;
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  std::string err;
-  float U[128];
-  StepParams* host_params = nullptr;  // pinned ring
-  cudaEvent_t param_ev[kParamRing];
-  int param_slot = 0;
-  uint32_t high_water = 0;
-  int step_index = 0;
-  std::vector<void*> allocs;
-  uint64_t bytes = 0;
-  cudaGraphExec_t graph[4] = {nullptr, nullptr, nullptr, nullptr};
-  void* graph_conc[4] = {nullptr, nullptr, nullptr, nullptr};  // conc pointer each graph was captured with
-  int kernels_per_step = 0;
-  Snapshot snaps[kSnapshots];
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  cudaEvent_t stage_ev[DOB_STAGE_COUNT + 1];
-};
+#include "dob_ctx.h"
 
 static const char* g_static_err = "no error";
 
@@ -75,6 +40,10 @@ static dob_status fail(dob_ctx* ctx, dob_status st, const char* what, const char
     g_static_err = msg.c_str();
   }
   return st;
+}
+
+dob_status dob::record_error(dob_ctx* ctx, dob_status st, const char* what, const char* detail) {
+  return fail(ctx, st, what, detail);
 }
 
 static size_t vs_bytes(int prec) { return prec == DOB_PREC_REFERENCE_FP16 ? 2 : 4; }
@@ -490,6 +459,7 @@ void dob_destroy(dob_ctx* ctx) {
   if (!ctx) return;
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   drop_graphs(ctx);
+  adjoint_free(ctx);
   for (auto& sn : ctx->snaps)
     for (void* p : sn.bufs) cudaFree(p);
   for (void* p : ctx->allocs) cudaFree(p);
@@ -616,8 +586,14 @@ static bool field_desc(dob_ctx* ctx, int field, FieldDesc* f) {
     case DOB_FIELD_SPLAT_INTACT: *f = {s.splatI, Nc, 3}; return true;
     case DOB_FIELD_SPLAT_LYSED: *f = {s.splatL, Nc, 3}; return true;
     case DOB_FIELD_WAVE: *f = {s.wave, (size_t)4 * kWaveN * kWaveN, 2}; return true;
-    default: return false;
+    default: break;
   }
+  void* dev = nullptr;
+  size_t count = 0;
+  int kind = 0;
+  if (!adjoint_field(ctx, field, &dev, &count, &kind)) return false;
+  *f = {dev, count, kind};
+  return true;
 }
 
 dob_status dob_set_field(dob_ctx* ctx, int field, const void* host, size_t bytes) {

@@ -58,6 +58,21 @@ struct DevState {
   double rel_tol;
 };
 
+// Adjoint (transpose-Jacobian) arrays of the closed-box FP32 step, all FP32.
+// Pressure / right-hand side / multigrid adjoints are red-black split like
+// their forward arrays; the rest use the natural layout.
+struct AdjState {
+  float *au, *av, *aw;     // adjoint of the MAC faces a stage reads
+  float *au2, *av2, *aw2;  // adjoint of the faces advection / Casson write
+  float4* acen;            // adjoint of the centre velocity (x, y, z, unused)
+  float *ac, *ac2, *apred; // dye (input), resolved dye (output), predictor
+  float *ap, *arhs;        // pressure, right-hand side (split)
+  float* le[kMaxLevels];   // coarse corrections (split, levels >= 1)
+  float* lb[kMaxLevels];   // coarse right-hand sides (split, levels >= 1)
+  float *alpha, *gq;       // Casson adjoint scratch: per-cell alpha, 2 dL/dQ
+  double* red;             // FP64 reduction slots (mean removal)
+};
+
 // reduction slot indices in DevState::red / redu
 enum {
   RED_RHS_SUM = 0,
@@ -157,5 +172,18 @@ void launch_count_alive(const DevState& s, unsigned int* out, cudaStream_t st);
 void launch_inject_sphere(const DevState& s, const float c[3], float r, float dye, const float vel[3], float sigma,
                           uint64_t seed, cudaStream_t st);
 cudaError_t eval_math_device(int fn, const float* x, const float* y, float* out, uint32_t n);
+// sum of a . vel over the MAC faces k_inject_sphere sets (FP64, into *out)
+void launch_sphere_impulse(const DevState& s, const float* a_u, const float* a_v, const float* a_w, const float c[3],
+                           float r, const float vel[3], double* out, cudaStream_t st);
+
+// ---- launchers (k_adjoint.cu): transpose of each closed-box FP32 stage ------------------
+void launch_adj_advect_mac(const DevState& s, const AdjState& a, cudaStream_t st);
+void launch_adj_mac_to_center(const DevState& s, const AdjState& a, cudaStream_t st);
+void launch_adj_casson(const DevState& s, const AdjState& a, cudaStream_t st);
+void launch_adj_mac_rhs(const DevState& s, const AdjState& a, cudaStream_t st);
+void launch_adj_pressure_solve(const DevState& s, const AdjState& a, cudaStream_t st);
+void launch_adj_project(const DevState& s, const AdjState& a, cudaStream_t st);
+void launch_adj_conc_predict(const DevState& s, const AdjState& a, cudaStream_t st);
+void launch_adj_conc_resolve(const DevState& s, const AdjState& a, cudaStream_t st);
 
 }  // namespace dob

@@ -1,0 +1,589 @@
+// k_adjoint.cu — discrete adjoint (transpose of the Jacobian) of every stage
+// of the closed-box FP32 step.
+//
+// Each kernel is the exact transpose of the linearisation of one forward
+// kernel at the forward state it is given (the "tape"):
+//   advection        transpose of the trilinear interpolation of the face
+//                    values at the departure point, plus the chain through
+//                    the RK2 departure point into the centre velocity
+//                    (scattered with atomics: several cells can sample the
+//                    same texel)
+//   centre average   transpose of the face -> centre average
+//   Casson viscosity explicit Laplacian with coefficient alpha(|grad u|, c):
+//                    transpose of the stencil plus the alpha chain (two
+//                    passes: per-cell coefficients, then a gather)
+//   divergence / projection  D^T and G^T with the wall masks
+//   pressure solve   every V-cycle run backwards with the transposed
+//                    smoother half-sweeps, restriction and prolongation
+//   dye predict / MacCormack resolve  transposed samples; the limiter passes
+//                    the adjoint through, or to the neighbourhood tap that
+//                    supplied the clamped value
+// Where the forward is not differentiable (clamps at their bounds, the
+// limiter's min/max selection, |grad u| = 0) the adjoint takes the branch the
+// forward took, i.e. the one-sided derivative of the executed expression.
+//
+// Adjoint arrays are FP32, natural layout except the pressure / right-hand
+// side / multigrid ones (red-black split like their forward arrays).
+#include <cuda_runtime.h>
+
+#include "dob_kernels.cuh"
+
+namespace dob {
+
+// ---- trilinear helpers --------------------------------------------------------------------
+__device__ __forceinline__ void tri_w(const Taps& t, float w[8]) {
+  const float gx = 1.0f - t.fx, gy = 1.0f - t.fy, gz = 1.0f - t.fz;
+  w[0] = gx * gy * gz; w[1] = t.fx * gy * gz; w[2] = gx * t.fy * gz; w[3] = t.fx * t.fy * gz;
+  w[4] = gx * gy * t.fz; w[5] = t.fx * gy * t.fz; w[6] = gx * t.fy * t.fz; w[7] = t.fx * t.fy * t.fz;
+}
+__device__ __forceinline__ uint32_t tap_at(const Taps& t, int k) {
+  return t.base + ((k & 1) ? t.ox : 0u) + ((k & 2) ? t.oy : 0u) + ((k & 4) ? t.oz : 0u);
+}
+// d lerp8 / d(fx, fy, fz) of a scalar field
+__device__ __forceinline__ dob_v3 lerp8_dfrac(const Taps& t, const float* a) {
+  const float* p = a + t.base;
+  const float c0 = p[0], c1 = p[t.ox], c2 = p[t.oy], c3 = p[t.oy + t.ox];
+  const float c4 = p[t.oz], c5 = p[t.oz + t.ox], c6 = p[t.oz + t.oy], c7 = p[t.oz + t.oy + t.ox];
+  const float x00 = dob_mix(c0, c1, t.fx), x10 = dob_mix(c2, c3, t.fx);
+  const float x01 = dob_mix(c4, c5, t.fx), x11 = dob_mix(c6, c7, t.fx);
+  const float dfx = dob_mix(dob_mix(c1 - c0, c3 - c2, t.fy), dob_mix(c5 - c4, c7 - c6, t.fy), t.fz);
+  const float dfy = dob_mix(x10 - x00, x11 - x01, t.fz);
+  const float dfz = dob_mix(x01, x11, t.fy) - dob_mix(x00, x10, t.fy);
+  return v3(dfx, dfy, dfz);
+}
+// sum over the xyz channels of a float4 field: sum_ch g_ch * d lerp8_ch / d(fx, fy, fz)
+__device__ __forceinline__ dob_v3 lerp8x3_dfrac(const Taps& t, const float4* a, dob_v3 g) {
+  const float4* p = a + t.base;
+  const float4 c0 = p[0], c1 = p[t.ox], c2 = p[t.oy], c3 = p[t.oy + t.ox];
+  const float4 c4 = p[t.oz], c5 = p[t.oz + t.ox], c6 = p[t.oz + t.oy], c7 = p[t.oz + t.oy + t.ox];
+  // contract the channels first: the derivative is linear in the values
+  const float s0 = g.x * c0.x + g.y * c0.y + g.z * c0.z, s1 = g.x * c1.x + g.y * c1.y + g.z * c1.z;
+  const float s2 = g.x * c2.x + g.y * c2.y + g.z * c2.z, s3 = g.x * c3.x + g.y * c3.y + g.z * c3.z;
+  const float s4 = g.x * c4.x + g.y * c4.y + g.z * c4.z, s5 = g.x * c5.x + g.y * c5.y + g.z * c5.z;
+  const float s6 = g.x * c6.x + g.y * c6.y + g.z * c6.z, s7 = g.x * c7.x + g.y * c7.y + g.z * c7.z;
+  const float x00 = dob_mix(s0, s1, t.fx), x10 = dob_mix(s2, s3, t.fx);
+  const float x01 = dob_mix(s4, s5, t.fx), x11 = dob_mix(s6, s7, t.fx);
+  const float dfx = dob_mix(dob_mix(s1 - s0, s3 - s2, t.fy), dob_mix(s5 - s4, s7 - s6, t.fy), t.fz);
+  const float dfy = dob_mix(x10 - x00, x11 - x01, t.fz);
+  const float dfz = dob_mix(x01, x11, t.fy) - dob_mix(x00, x10, t.fy);
+  return v3(dfx, dfy, dfz);
+}
+// transpose of lerp8: a[tap k] += g * w_k
+__device__ __forceinline__ void scatter8(float* a, const Taps& t, float g) {
+  if (g == 0.0f) return;
+  float w[8];
+  tri_w(t, w);
+#pragma unroll
+  for (int k = 0; k < 8; ++k)
+    if (w[k] != 0.0f) atomicAdd(a + tap_at(t, k), g * w[k]);
+}
+__device__ __forceinline__ void scatter8v(float4* a, const Taps& t, dob_v3 g) {
+  if (g.x == 0.0f && g.y == 0.0f && g.z == 0.0f) return;
+  float w[8];
+  tri_w(t, w);
+#pragma unroll
+  for (int k = 0; k < 8; ++k)
+    if (w[k] != 0.0f) atomicAdd(a + tap_at(t, k), make_float4(g.x * w[k], g.y * w[k], g.z * w[k], 0.0f));
+}
+// derivative mask of dob_clampf(v, lo, hi): 1 where the value passed through
+__device__ __forceinline__ float pass(float v, float lo, float hi) { return (v > lo && v < hi) ? 1.0f : 0.0f; }
+__device__ __forceinline__ dob_v3 pass3(dob_v3 v, float lo, float hi) {
+  return v3(pass(v.x, lo, hi), pass(v.y, lo, hi), pass(v.z, lo, hi));
+}
+
+#define ADJ_CELL                                     \
+  const int x = blockIdx.x * blockDim.x + threadIdx.x; \
+  const int y = blockIdx.y * blockDim.y + threadIdx.y; \
+  const int z = blockIdx.z;                          \
+  if (x >= g.nx || y >= g.ny) return;                \
+  const size_t i = g.at(x, y, z);
+
+// ---- FLUID_ADVECT_MAC (closed box) ------------------------------------------------------------
+// Forward per face: B = trace_back(cen, F) (RK2 with clamps), value =
+// damp * lerp8(u_k, clamp(B - half-cell offset)).  Adjoint of the output
+// au2 -> au (face values) and acen (centre velocity).
+__device__ __forceinline__ void adj_face(const Grid& g, const float* uk, const float4* cen, float4* acen, float* auk,
+                                         dob_v3 F, int comp, float gout, float dtv, dob_v3 dom, dob_v3 dims) {
+  if (gout == 0.0f) return;
+  // forward recompute
+  const dob_v3 F0 = clamp3(F, 0.002f, 0.998f);
+  const Taps t0 = make_taps(g, F0.x, F0.y, F0.z);
+  const float4 v0r = lerp8xn<3>(t0, cen);
+  const dob_v3 v0 = v3(v0r.x, v0r.y, v0r.z);
+  const dob_v3 M = F - (0.5f * (v0 * dtv)) / dom;
+  const dob_v3 Mc = clamp3(M, 0.002f, 0.998f);
+  const Taps tM = make_taps(g, Mc.x, Mc.y, Mc.z);
+  const float4 vmr = lerp8xn<3>(tM, cen);
+  const dob_v3 vMid = v3(vmr.x, vmr.y, vmr.z);
+  const dob_v3 B = F - (vMid * dtv) / dom;
+  const dob_v3 Bc = clamp3(B, 0.002f, 0.998f);
+  dob_v3 S = Bc;
+  if (comp == 0) S.x = S.x - 0.5f / (float)g.nx;
+  if (comp == 1) S.y = S.y - 0.5f / (float)g.ny;
+  if (comp == 2) S.z = S.z - 0.5f / (float)g.nz;
+  const dob_v3 Sc = clamp3(S, 0.001f, 0.999f);
+  const Taps tS = make_taps(g, Sc.x, Sc.y, Sc.z);
+  // backward
+  scatter8(auk, tS, gout);
+  const dob_v3 gS = (gout * lerp8_dfrac(tS, uk)) * dims * pass3(S, 0.001f, 0.999f);
+  const dob_v3 gB = gS * pass3(B, 0.002f, 0.998f);
+  const dob_v3 gvMid = -(gB * dtv) / dom;
+  scatter8v(acen, tM, gvMid);
+  const dob_v3 gM = lerp8x3_dfrac(tM, cen, gvMid) * dims * pass3(M, 0.002f, 0.998f);
+  const dob_v3 gv0 = -(0.5f * (gM * dtv)) / dom;
+  scatter8v(acen, t0, gv0);
+}
+
+__global__ void __launch_bounds__(256) k_adj_advect_mac(Grid g, const StepParams* __restrict__ Pp,
+                                                        const float* __restrict__ u, const float* __restrict__ v,
+                                                        const float* __restrict__ w, const float4* __restrict__ cen,
+                                                        const float* __restrict__ au2, const float* __restrict__ av2,
+                                                        const float* __restrict__ aw2, float* au, float* av, float* aw,
+                                                        float4* acen) {
+  ADJ_CELL
+  const StepParams& P = *Pp;
+  const dob_v3 dims = v3((float)g.nx, (float)g.ny, (float)g.nz);
+  const float dtv = P.dt;
+  const dob_v3 dom = dsize_of(P);
+  const float damp = P.damp;
+  const float gx = x >= g.nx - 1 ? 0.0f : au2[i] * damp;
+  const float gy = y >= g.ny - 1 ? 0.0f : av2[i] * damp;
+  const float gz = z >= g.nz - 1 ? 0.0f : aw2[i] * damp;
+  adj_face(g, u, cen, acen, au, v3((float)x + 1.0f, (float)y + 0.5f, (float)z + 0.5f) / dims, 0, gx, dtv, dom, dims);
+  adj_face(g, v, cen, acen, av, v3((float)x + 0.5f, (float)y + 1.0f, (float)z + 0.5f) / dims, 1, gy, dtv, dom, dims);
+  adj_face(g, w, cen, acen, aw, v3((float)x + 0.5f, (float)y + 0.5f, (float)z + 1.0f) / dims, 2, gz, dtv, dom, dims);
+}
+
+// ---- FLUID_MAC_TO_CENTER (closed box): au += C^T acen ---------------------------------------
+__global__ void __launch_bounds__(256) k_adj_mac_to_center(Grid g, const float4* __restrict__ acen, float* au,
+                                                           float* av, float* aw) {
+  ADJ_CELL
+  const float4 c = acen[i];
+  if (x < g.nx - 1) au[i] += 0.5f * c.x + 0.5f * acen[i + 1].x;
+  if (y < g.ny - 1) av[i] += 0.5f * c.y + 0.5f * acen[i + g.nx].y;
+  if (z < g.nz - 1) aw[i] += 0.5f * c.z + 0.5f * acen[i + (size_t)g.nx * g.ny].z;
+}
+
+// ---- FLUID_CASSON_FORCES (closed box) ----------------------------------------------------------
+__device__ __forceinline__ dob_v3 ldm(const Grid& g, const float* u, const float* v, const float* w, int x, int y,
+                                      int z) {
+  const size_t j = g.at(dob_clampi(x, 0, g.nx - 1), dob_clampi(y, 0, g.ny - 1), dob_clampi(z, 0, g.nz - 1));
+  return v3(u[j], v[j], w[j]);
+}
+__device__ __forceinline__ dob_v3 out_adj(const Grid& g, const float* au2, const float* av2, const float* aw2, int x,
+                                          int y, int z) {
+  const size_t j = g.at(x, y, z);
+  return v3(x >= g.nx - 1 ? 0.0f : au2[j], y >= g.ny - 1 ? 0.0f : av2[j], z >= g.nz - 1 ? 0.0f : aw2[j]);
+}
+// Pass 1: per cell, alpha and G = 2 dL/dQ (Q = |grad u|^2 of the Casson
+// shear rate); the dye adjoint of the cell.
+__global__ void __launch_bounds__(256) k_adj_casson1(Grid g, const StepParams* __restrict__ Pp,
+                                                     const float* __restrict__ u, const float* __restrict__ v,
+                                                     const float* __restrict__ w, const float* __restrict__ dye,
+                                                     const float* __restrict__ au2, const float* __restrict__ av2,
+                                                     const float* __restrict__ aw2, float* __restrict__ alpha_out,
+                                                     float* __restrict__ gq_out, float* ac) {
+  ADJ_CELL
+  const StepParams& P = *Pp;
+  const float dtv = P.dt;
+  const dob_v3 mac = v3(u[i], v[i], w[i]);
+  const dob_v3 mXp = ldm(g, u, v, w, x + 1, y, z), mXn = ldm(g, u, v, w, x - 1, y, z);
+  const dob_v3 mYp = ldm(g, u, v, w, x, y + 1, z), mYn = ldm(g, u, v, w, x, y - 1, z);
+  const dob_v3 mZp = ldm(g, u, v, w, x, y, z + 1), mZn = ldm(g, u, v, w, x, y, z - 1);
+  const dob_v3 du = mXp - mXn, dv = mYp - mYn, dw = mZp - mZn;
+  const dob_v3 lap = (mXp + mXn + mYp + mYn + mZp + mZn) - 6.0f * mac;
+  const float cval = dye[i];
+  const float c = dob_clampf(cval, 0.0f, 1.5f);
+  const float dxv = P.dx;
+  const float Q = dot3(du, du) + dot3(dv, dv) + dot3(dw, dw);
+  const float gdot = dob_sqrt(Q) / (2.0f * dxv);
+  const float sqrtMu = dob_sqrt(P.mu_p);
+  const float S = dob_sqrt(P.tau_y * c * c / (gdot + 0.4f));
+  const float nu = (sqrtMu + S) * (sqrtMu + S);
+  const float araw = nu * dtv / (dxv * dxv);
+  const float alpha = dob_minf(araw, 0.125f);
+  alpha_out[i] = alpha;
+  float G = 0.0f;
+  if (araw < 0.125f) {
+    const dob_v3 o = out_adj(g, au2, av2, aw2, x, y, z);
+    const float ab = dot3(o, lap);
+    const float nub = ab * dtv / (dxv * dxv);
+    const float Sb = nub * 2.0f * (sqrtMu + S);
+    const float K = dob_sqrt(P.tau_y / (gdot + 0.4f));
+    ac[i] += Sb * K * pass(cval, 0.0f, 1.5f);
+    const float gb = Sb * (-S / (2.0f * (gdot + 0.4f)));
+    if (Q > 0.0f) G = 2.0f * (gb / (2.0f * dxv)) / (2.0f * dob_sqrt(Q));
+  }
+  gq_out[i] = G;
+}
+// Pass 2: gather the adjoint of each face value from the cells whose
+// (clamped) stencils read it.
+__global__ void __launch_bounds__(256) k_adj_casson2(Grid g, const float* __restrict__ u, const float* __restrict__ v,
+                                                     const float* __restrict__ w, const float* __restrict__ au2,
+                                                     const float* __restrict__ av2, const float* __restrict__ aw2,
+                                                     const float* __restrict__ alpha, const float* __restrict__ gq,
+                                                     float* au, float* av, float* aw) {
+  ADJ_CELL
+  const int n[3] = {g.nx, g.ny, g.nz};
+  const int jc[3] = {x, y, z};
+  const dob_v3 o = out_adj(g, au2, av2, aw2, x, y, z);
+  const float aj = alpha[i], Gj = gq[i];
+  const dob_v3 mj = v3(u[i], v[i], w[i]);
+  int ncl = 0;
+  dob_v3 acc = v3(0.0f, 0.0f, 0.0f);
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    int e[3] = {0, 0, 0};
+    e[d] = 1;
+    if (jc[d] > 0) {  // i = j - e_d: j is its + neighbour
+      const int ix = x - e[0], iy = y - e[1], iz = z - e[2];
+      const size_t ii = g.at(ix, iy, iz);
+      const dob_v3 oi = out_adj(g, au2, av2, aw2, ix, iy, iz);
+      const dob_v3 mm = ldm(g, u, v, w, x - 2 * e[0], y - 2 * e[1], z - 2 * e[2]);
+      acc = acc + alpha[ii] * oi + gq[ii] * (mj - mm);
+    } else {
+      ++ncl;  // the - neighbour of j clamps onto j
+      const dob_v3 mp = ldm(g, u, v, w, x + e[0], y + e[1], z + e[2]);
+      acc = acc - Gj * (mp - mj);
+    }
+    if (jc[d] < n[d] - 1) {  // i = j + e_d: j is its - neighbour
+      const int ix = x + e[0], iy = y + e[1], iz = z + e[2];
+      const size_t ii = g.at(ix, iy, iz);
+      const dob_v3 oi = out_adj(g, au2, av2, aw2, ix, iy, iz);
+      const dob_v3 mp = ldm(g, u, v, w, x + 2 * e[0], y + 2 * e[1], z + 2 * e[2]);
+      acc = acc + alpha[ii] * oi - gq[ii] * (mp - mj);
+    } else {
+      ++ncl;  // the + neighbour of j clamps onto j
+      const dob_v3 mm = ldm(g, u, v, w, x - e[0], y - e[1], z - e[2]);
+      acc = acc + Gj * (mj - mm);
+    }
+  }
+  const float self = 1.0f - 6.0f * aj + aj * (float)ncl;
+  acc = acc + self * o;
+  au[i] += acc.x;
+  av[i] += acc.y;
+  aw[i] += acc.z;
+}
+
+// ---- FLUID_MAC_RHS (closed box): au += D^T arhs (arhs already mean-free) -----------------------
+__global__ void __launch_bounds__(256) k_adj_mac_rhs(Grid g, const float* __restrict__ arhs, float* au, float* av,
+                                                     float* aw) {
+  ADJ_CELL
+  const float bj = arhs[rb_index(g, x, y, z)];
+  if (x < g.nx - 1) au[i] += bj - arhs[rb_index(g, x + 1, y, z)];
+  if (y < g.ny - 1) av[i] += bj - arhs[rb_index(g, x, y + 1, z)];
+  if (z < g.nz - 1) aw[i] += bj - arhs[rb_index(g, x, y, z + 1)];
+}
+
+// ---- FLUID_MAC_PROJECT (closed box): au <- W au, ap += D(W au) --------------------------------
+__global__ void __launch_bounds__(256) k_adj_project(Grid g, float* au, float* av, float* aw, float* ap) {
+  ADJ_CELL
+  const float ox = x < g.nx - 1 ? au[i] : 0.0f;
+  const float oy = y < g.ny - 1 ? av[i] : 0.0f;
+  const float oz = z < g.nz - 1 ? aw[i] : 0.0f;
+  const float oxm = x > 0 ? au[i - 1] : 0.0f;
+  const float oym = y > 0 ? av[i - g.nx] : 0.0f;
+  const float ozm = z > 0 ? aw[i - (size_t)g.nx * g.ny] : 0.0f;
+  ap[rb_index(g, x, y, z)] += (ox - oxm) + (oy - oym) + (oz - ozm);
+  // wall faces are zeroed by the forward; no neighbour reads them
+  if (x == g.nx - 1) au[i] = 0.0f;
+  if (y == g.ny - 1) av[i] = 0.0f;
+  if (z == g.nz - 1) aw[i] = 0.0f;
+}
+
+// ---- multigrid transposes (red-black split arrays) ---------------------------------------------
+__device__ __forceinline__ float mg_diag(const Grid& d, int ref, int x, int y, int z) {
+  float s = ref ? 1.0f : 0.0f;
+  s += (x > 0 ? 1.0f : 0.0f) + (x < d.nx - 1 ? 1.0f : 0.0f) + (y > 0 ? 1.0f : 0.0f);
+  s += (!ref && y < d.ny - 1) ? 1.0f : 0.0f;
+  s += (z > 0 ? 1.0f : 0.0f) + (z < d.nz - 1 ? 1.0f : 0.0f);
+  return s;
+}
+// sum over the existing neighbours n of (x,y,z) of xb(n) / diag(n)
+__device__ __forceinline__ float nbr_scaled_sum(const float* xb, const Grid& d, int ref, int x, int y, int z) {
+  float s = 0.0f;
+  if (x > 0) s += xb[rb_index(d, x - 1, y, z)] / mg_diag(d, ref, x - 1, y, z);
+  if (x < d.nx - 1) s += xb[rb_index(d, x + 1, y, z)] / mg_diag(d, ref, x + 1, y, z);
+  if (y > 0) s += xb[rb_index(d, x, y - 1, z)] / mg_diag(d, ref, x, y - 1, z);
+  if (y < d.ny - 1) s += xb[rb_index(d, x, y + 1, z)] / mg_diag(d, ref, x, y + 1, z);
+  if (z > 0) s += xb[rb_index(d, x, y, z - 1)] / mg_diag(d, ref, x, y, z - 1);
+  if (z < d.nz - 1) s += xb[rb_index(d, x, y, z + 1)] / mg_diag(d, ref, x, y, z + 1);
+  return s;
+}
+enum { ADJ_SWEEP_FIRST = 0, ADJ_SWEEP_FUSED = 1, ADJ_SWEEP_FINAL = 2 };
+// One step of a transposed run of red-black half-sweeps, over the cells of
+// colour `color`:
+//   FIRST  xb += sum_n xb(n)/diag(n)               (first half of the last
+//                                                    half-sweep's transpose)
+//   FUSED  bb += -h2 xb/diag; xb = sum_n xb(n)/diag(n)
+//   FINAL  bb += -h2 xb/diag; xb = 0
+__global__ void __launch_bounds__(256) k_adj_rbgs(Grid d, int color, float h2, int ref, int mode, float* xb, float* bb) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  if (k >= (d.nx >> 1) || y >= d.ny) return;
+  const int x = 2 * k + ((y + z + color) & 1);
+  const size_t j = rb_index(d, x, y, z);
+  if (mode == ADJ_SWEEP_FIRST) {
+    xb[j] += nbr_scaled_sum(xb, d, ref, x, y, z);
+    return;
+  }
+  const float diag = mg_diag(d, ref, x, y, z);
+  bb[j] += -h2 * xb[j] / diag;
+  xb[j] = mode == ADJ_SWEEP_FUSED ? nbr_scaled_sum(xb, d, ref, x, y, z) : 0.0f;
+}
+// Transpose of the fused residual + restriction B_c = 0.125 sum (b - A'x/h2):
+// per fine cell, bb += 0.125 Bb(parent); xb -= (A' rbar)/h2 with
+// rbar(n) = 0.125 Bb(parent(n)).
+__global__ void __launch_bounds__(256) k_adj_restrict(Grid f, Grid c, float h2, int ref, const float* __restrict__ Bb,
+                                                      float* xb, float* bb) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  if (x >= f.nx || y >= f.ny) return;
+  auto rbar = [&](int xx, int yy, int zz) { return 0.125f * Bb[rb_index(c, xx >> 1, yy >> 1, zz >> 1)]; };
+  const float r0 = rbar(x, y, z);
+  const size_t j = rb_index(f, x, y, z);
+  float sumN = 0.0f;
+  if (x > 0) sumN += rbar(x - 1, y, z);
+  if (x < f.nx - 1) sumN += rbar(x + 1, y, z);
+  if (y > 0) sumN += rbar(x, y - 1, z);
+  if (y < f.ny - 1) sumN += rbar(x, y + 1, z);
+  if (z > 0) sumN += rbar(x, y, z - 1);
+  if (z < f.nz - 1) sumN += rbar(x, y, z + 1);
+  bb[j] += r0;
+  xb[j] -= (sumN - mg_diag(f, ref, x, y, z) * r0) / h2;
+}
+// weight of coarse index J in the cell-centred linear interpolation at fine
+// index xf (the forward's clamped taps; 0 above a Dirichlet top when `top0`)
+__device__ __forceinline__ float prolong_w(int xf, int nf, int nc, int J, bool top0) {
+  const float cx = (((float)xf + 0.5f) / (float)nf) * (float)nc - 0.5f;
+  const float bx = floorf(cx);
+  const float fx = cx - bx;
+  const int i0 = (int)bx, i1 = i0 + 1;
+  float wsum = 0.0f;
+  if (dob_clampi(i0, 0, nc - 1) == J && !(top0 && i0 >= nc)) wsum += 1.0f - fx;
+  if (dob_clampi(i1, 0, nc - 1) == J && !(top0 && i1 >= nc)) wsum += fx;
+  return wsum;
+}
+// Transpose of e_f += P e_c: Eb(J) += sum over the 4x4x4 fine cells around
+// J of their interpolation weight on J times xb.
+__global__ void __launch_bounds__(256) k_adj_prolong(Grid f, Grid c, int ref, const float* __restrict__ xb, float* Eb) {
+  const int X = blockIdx.x * blockDim.x + threadIdx.x;
+  const int Y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int Z = blockIdx.z;
+  if (X >= c.nx || Y >= c.ny) return;
+  float wx[4], wy[4], wz[4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    const int fxi = 2 * X - 1 + a, fyi = 2 * Y - 1 + a, fzi = 2 * Z - 1 + a;
+    wx[a] = (fxi >= 0 && fxi < f.nx) ? prolong_w(fxi, f.nx, c.nx, X, false) : 0.0f;
+    wy[a] = (fyi >= 0 && fyi < f.ny) ? prolong_w(fyi, f.ny, c.ny, Y, ref != 0) : 0.0f;
+    wz[a] = (fzi >= 0 && fzi < f.nz) ? prolong_w(fzi, f.nz, c.nz, Z, false) : 0.0f;
+  }
+  float acc = 0.0f;
+  for (int cz = 0; cz < 4; ++cz) {
+    if (wz[cz] == 0.0f) continue;
+    for (int by = 0; by < 4; ++by) {
+      if (wy[by] == 0.0f) continue;
+      for (int ax = 0; ax < 4; ++ax) {
+        if (wx[ax] == 0.0f) continue;
+        acc += wx[ax] * wy[by] * wz[cz] * xb[rb_index(f, 2 * X - 1 + ax, 2 * Y - 1 + by, 2 * Z - 1 + cz)];
+      }
+    }
+  }
+  Eb[rb_index(c, X, Y, Z)] += acc;
+}
+
+// ---- CONC_PREDICT (closed box) ------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_adj_conc_predict(Grid gc, Grid g, const StepParams* __restrict__ Pp,
+                                                          const float4* __restrict__ cen, const float* __restrict__ dye,
+                                                          const float* __restrict__ apred, float* ac, float4* acen) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  if (x >= gc.nx || y >= gc.ny) return;
+  const size_t i = gc.at(x, y, z);
+  const float gout = apred[i];
+  if (gout == 0.0f) return;
+  const StepParams& P = *Pp;
+  const dob_v3 dimsc = v3((float)gc.nx, (float)gc.ny, (float)gc.nz);
+  const dob_v3 dimsg = v3((float)g.nx, (float)g.ny, (float)g.nz);
+  const float dtv = P.dt;
+  const dob_v3 dom = dsize_of(P);
+  const dob_v3 uvw = (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / dimsc;
+  const Taps t0 = make_taps(g, uvw.x, uvw.y, uvw.z);
+  const float4 v0r = lerp8xn<3>(t0, cen);
+  const dob_v3 v0 = v3(v0r.x, v0r.y, v0r.z);
+  const dob_v3 M = uvw - (0.5f * (v0 * dtv)) / dom;
+  const dob_v3 Mc = clamp3(M, 0.001f, 0.999f);
+  const Taps tM = make_taps(g, Mc.x, Mc.y, Mc.z);
+  const float4 vmr = lerp8xn<3>(tM, cen);
+  const dob_v3 vMid = v3(vmr.x, vmr.y, vmr.z);
+  const dob_v3 B = uvw - (vMid * dtv) / dom;
+  const dob_v3 Bc = clamp3(B, 0.001f, 0.999f);
+  const Taps tB = make_taps(gc, Bc.x, Bc.y, Bc.z);
+  scatter8(ac, tB, gout);
+  const dob_v3 gB = (gout * lerp8_dfrac(tB, dye)) * dimsc * pass3(B, 0.001f, 0.999f);
+  const dob_v3 gvMid = -(gB * dtv) / dom;
+  scatter8v(acen, tM, gvMid);
+  const dob_v3 gM = lerp8x3_dfrac(tM, cen, gvMid) * dimsg * pass3(M, 0.001f, 0.999f);
+  const dob_v3 gv0 = -(0.5f * (gM * dtv)) / dom;
+  scatter8v(acen, t0, gv0);
+}
+
+// ---- CONC_RESOLVE (closed box: MacCormack with the 8-tap limiter) -----------------------------
+__global__ void __launch_bounds__(256) k_adj_dye_resolve(Grid gc, Grid g, const StepParams* __restrict__ Pp,
+                                                         const float4* __restrict__ cen, const float* __restrict__ dye,
+                                                         const float* __restrict__ pred, const float* __restrict__ ac2,
+                                                         float* ac, float* apred, float4* acen) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  if (x >= gc.nx || y >= gc.ny) return;
+  const size_t i = gc.at(x, y, z);
+  const float gout = ac2[i];
+  if (gout == 0.0f) return;
+  const StepParams& P = *Pp;
+  const dob_v3 dims = v3((float)gc.nx, (float)gc.ny, (float)gc.nz);
+  const float dtv = P.dt;
+  const dob_v3 dom = dsize_of(P);
+  const dob_v3 uvw = (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / dims;
+  const Taps t0 = make_taps(g, uvw.x, uvw.y, uvw.z);
+  const float4 v0r = lerp8xn<3>(t0, cen);
+  const dob_v3 v0 = v3(v0r.x, v0r.y, v0r.z);
+  const dob_v3 uvwMid = clamp3(uvw - (0.5f * (v0 * dtv)) / dom, 0.001f, 0.999f);
+  const float4 vmr = lerp8xn<3>(make_taps(g, uvwMid.x, uvwMid.y, uvwMid.z), cen);
+  const dob_v3 vMid = v3(vmr.x, vmr.y, vmr.z);
+  const dob_v3 uvwBack = clamp3(uvw - (vMid * dtv) / dom, 0.001f, 0.999f);
+  const dob_v3 Fw = uvw + (v0 * dtv) / dom;
+  const dob_v3 uvwFwd = clamp3(Fw, 0.001f, 0.999f);
+  const Taps tF = make_taps(gc, uvwFwd.x, uvwFwd.y, uvwFwd.z);
+  const float gBackEst = lerp8(tF, pred);
+  const float kap = 0.45f * P.sharp;
+  const float gCorr = pred[i] + kap * (dye[i] - gBackEst);
+  const dob_v3 tc = uvwBack * dims - v3(0.5f, 0.5f, 0.5f);
+  const int bx = (int)floorf(tc.x), by = (int)floorf(tc.y), bz = (int)floorf(tc.z);
+  size_t id[8];
+  float s[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    id[k] = gc.at(dob_clampi(bx + (k & 1), 0, gc.nx - 1), dob_clampi(by + ((k >> 1) & 1), 0, gc.ny - 1),
+                  dob_clampi(bz + ((k >> 2) & 1), 0, gc.nz - 1));
+    s[k] = dye[id[k]];
+  }
+  // the forward's min/max trees (dob_minf/dob_maxf keep the second operand on ties)
+  auto pick_min = [&](int a, int b) { return s[a] < s[b] ? a : b; };
+  auto pick_max = [&](int a, int b) { return s[a] > s[b] ? a : b; };
+  const int kmin = pick_min(pick_min(pick_min(0, 1), pick_min(2, 3)), pick_min(pick_min(4, 5), pick_min(6, 7)));
+  const int kmax = pick_max(pick_max(pick_max(0, 1), pick_max(2, 3)), pick_max(pick_max(4, 5), pick_max(6, 7)));
+  const float minG = s[kmin], maxG = s[kmax];
+  if (!(gCorr > minG)) {
+    atomicAdd(ac + id[kmin], gout);
+  } else if (!(gCorr < maxG)) {
+    atomicAdd(ac + id[kmax], gout);
+  } else {
+    atomicAdd(apred + i, gout);
+    atomicAdd(ac + i, kap * gout);
+    const float gE = -kap * gout;
+    scatter8(apred, tF, gE);
+    const dob_v3 gF = (gE * lerp8_dfrac(tF, pred)) * dims * pass3(Fw, 0.001f, 0.999f);
+    const dob_v3 gv0 = (gF * dtv) / dom;
+    scatter8v(acen, t0, gv0);
+  }
+}
+
+// ---- launchers ----------------------------------------------------------------------------------
+static inline dim3 cgrid(const Grid& g) { return dim3((g.nx + 31) / 32, (g.ny + 7) / 8, g.nz); }
+static inline dim3 cblock() { return dim3(32, 8, 1); }
+static inline dim3 hgrid(const Grid& g) { return dim3((g.nx / 2 + 31) / 32, (g.ny + 7) / 8, g.nz); }
+
+void launch_adj_advect_mac(const DevState& s, const AdjState& a, cudaStream_t st) {
+  k_adj_advect_mac<<<cgrid(s.g), cblock(), 0, st>>>(s.g, s.params, (const float*)s.u, (const float*)s.v,
+                                                    (const float*)s.w, (const float4*)s.cen, a.au2, a.av2, a.aw2, a.au,
+                                                    a.av, a.aw, a.acen);
+}
+void launch_adj_mac_to_center(const DevState& s, const AdjState& a, cudaStream_t st) {
+  k_adj_mac_to_center<<<cgrid(s.g), cblock(), 0, st>>>(s.g, a.acen, a.au, a.av, a.aw);
+}
+void launch_adj_casson(const DevState& s, const AdjState& a, cudaStream_t st) {
+  k_adj_casson1<<<cgrid(s.g), cblock(), 0, st>>>(s.g, s.params, (const float*)s.u, (const float*)s.v,
+                                                 (const float*)s.w, (const float*)s.conc, a.au2, a.av2, a.aw2,
+                                                 a.alpha, a.gq, a.ac);
+  k_adj_casson2<<<cgrid(s.g), cblock(), 0, st>>>(s.g, (const float*)s.u, (const float*)s.v, (const float*)s.w, a.au2,
+                                                 a.av2, a.aw2, a.alpha, a.gq, a.au, a.av, a.aw);
+}
+void launch_adj_mac_rhs(const DevState& s, const AdjState& a, cudaStream_t st) {
+  // transpose of the mean removal (a symmetric projection), then D^T
+  launch_sum(a.arhs, s.g.n(), a.red + 0, s.num_sms, st);
+  launch_sub_mean(a.arhs, s.g.n(), a.red + 0, s.num_sms, st);
+  k_adj_mac_rhs<<<cgrid(s.g), cblock(), 0, st>>>(s.g, a.arhs, a.au, a.av, a.aw);
+}
+void launch_adj_project(const DevState& s, const AdjState& a, cudaStream_t st) {
+  k_adj_project<<<cgrid(s.g), cblock(), 0, st>>>(s.g, a.au, a.av, a.aw, a.ap);
+}
+
+// transpose of `sweeps` red-black sweeps (red then black each) on one level
+static void adj_smooth(const Grid& d, float h2, int ref, int sweeps, float* xb, float* bb, cudaStream_t st) {
+  const int K = 2 * sweeps;
+  if (K == 0) return;
+  auto color_of = [](int k) { return (k - 1) & 1; };  // half-sweep k = 1..K
+  k_adj_rbgs<<<hgrid(d), cblock(), 0, st>>>(d, 1 - color_of(K), h2, ref, ADJ_SWEEP_FIRST, xb, bb);
+  for (int k = K; k >= 2; --k)
+    k_adj_rbgs<<<hgrid(d), cblock(), 0, st>>>(d, color_of(k), h2, ref, ADJ_SWEEP_FUSED, xb, bb);
+  k_adj_rbgs<<<hgrid(d), cblock(), 0, st>>>(d, color_of(1), h2, ref, ADJ_SWEEP_FINAL, xb, bb);
+}
+static void adj_restrict(const DevState& s, const AdjState& a, int l, float* xb, float* bb, cudaStream_t st) {
+  const Grid f = s.lv[l].d, c = s.lv[l + 1].d;
+  k_adj_restrict<<<cgrid(f), cblock(), 0, st>>>(f, c, s.lv[l].h2, s.ref, a.lb[l + 1], xb, bb);
+  cudaMemsetAsync(a.lb[l + 1], 0, c.n() * sizeof(float), st);
+}
+static void adj_prolong(const DevState& s, const AdjState& a, int l, const float* xb, cudaStream_t st) {
+  const Grid f = s.lv[l].d, c = s.lv[l + 1].d;
+  k_adj_prolong<<<cgrid(c), cblock(), 0, st>>>(f, c, s.ref, xb, a.le[l + 1]);
+}
+// Transpose of one V-cycle (k_mg.cu vcycle) on (ap, arhs); the coarse
+// adjoint arrays are zero on entry and on exit.
+static void adj_vcycle(const DevState& s, const AdjState& a, cudaStream_t st) {
+  const int L = s.nlev;
+  const MgLevel& L0 = s.lv[0];
+  if (L == 1) {
+    adj_smooth(L0.d, L0.h2, s.ref, s.pre + s.post, a.ap, a.arhs, st);
+    return;
+  }
+  adj_smooth(L0.d, L0.h2, s.ref, s.post0, a.ap, a.arhs, st);
+  adj_prolong(s, a, 0, a.ap, st);
+  for (int l = 1; l < L - 1; ++l) {
+    adj_smooth(s.lv[l].d, s.lv[l].h2, s.ref, s.post, a.le[l], a.lb[l], st);
+    adj_prolong(s, a, l, a.le[l], st);
+  }
+  const MgLevel& LC = s.lv[L - 1];
+  adj_smooth(LC.d, LC.h2, s.ref, s.coarse_sweeps, a.le[L - 1], a.lb[L - 1], st);
+  cudaMemsetAsync(a.le[L - 1], 0, LC.d.n() * sizeof(float), st);
+  for (int l = L - 2; l >= 1; --l) {
+    adj_restrict(s, a, l, a.le[l], a.lb[l], st);
+    adj_smooth(s.lv[l].d, s.lv[l].h2, s.ref, s.pre, a.le[l], a.lb[l], st);
+    cudaMemsetAsync(a.le[l], 0, s.lv[l].d.n() * sizeof(float), st);
+  }
+  adj_restrict(s, a, 0, a.ap, a.arhs, st);
+  adj_smooth(L0.d, L0.h2, s.ref, s.pre0, a.ap, a.arhs, st);
+}
+void launch_adj_pressure_solve(const DevState& s, const AdjState& a, cudaStream_t st) {
+  const size_t n = s.g.n();
+  if (!s.ref) {
+    launch_sum(a.ap, n, a.red + 1, s.num_sms, st);
+    launch_sub_mean(a.ap, n, a.red + 1, s.num_sms, st);
+  }
+  for (int c = 0; c < s.cycles; ++c) adj_vcycle(s, a, st);
+}
+void launch_adj_conc_predict(const DevState& s, const AdjState& a, cudaStream_t st) {
+  k_adj_conc_predict<<<cgrid(s.gc), cblock(), 0, st>>>(s.gc, s.g, s.params, (const float4*)s.cen,
+                                                       (const float*)s.conc, a.apred, a.ac, a.acen);
+}
+void launch_adj_conc_resolve(const DevState& s, const AdjState& a, cudaStream_t st) {
+  k_adj_dye_resolve<<<cgrid(s.gc), cblock(), 0, st>>>(s.gc, s.g, s.params, (const float4*)s.cen,
+                                                      (const float*)s.conc, (const float*)s.pred, a.ac2, a.ac,
+                                                      a.apred, a.acen);
+}
+
+}  // namespace dob

@@ -368,6 +368,32 @@ __global__ void __launch_bounds__(256) k_inject_sphere(Grid g, Grid gc, const St
   }
 }
 
+// d loss / d s for injected face velocities s * vel: the sum of the face
+// adjoints times vel over exactly the faces k_inject_sphere writes (same
+// FMA-free predicate).
+__global__ void __launch_bounds__(256) k_sphere_impulse(Grid g, const StepParams* __restrict__ Pp,
+                                                        const float* __restrict__ au, const float* __restrict__ av,
+                                                        const float* __restrict__ aw, float cx, float cy, float cz,
+                                                        float rr, float vx, float vy, float vz, double* out) {
+  const StepParams& P = *Pp;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  double part = 0.0;
+  if (x < g.nx && y < g.ny) {
+    const dob_v3 cc = v3(cx, cy, cz);
+    const size_t i = g.at(x, y, z);
+    const dob_v3 dims = v3((float)g.nx, (float)g.ny, (float)g.nz);
+    const dob_v3 fx = to_world(P, v3((float)x + 1.0f, (float)y + 0.5f, (float)z + 0.5f) / dims);
+    const dob_v3 fy = to_world(P, v3((float)x + 0.5f, (float)y + 1.0f, (float)z + 0.5f) / dims);
+    const dob_v3 fz = to_world(P, v3((float)x + 0.5f, (float)y + 0.5f, (float)z + 1.0f) / dims);
+    if (x < g.nx - 1 && length3(fx - cc) <= rr) part += (double)au[i] * (double)vx;
+    if (y < g.ny - 1 && length3(fy - cc) <= rr) part += (double)av[i] * (double)vy;
+    if (z < g.nz - 1 && length3(fz - cc) <= rr) part += (double)aw[i] * (double)vz;
+  }
+  block_sum_atomic(part, out);
+}
+
 __global__ void k_eval_math(int fn, const float* __restrict__ x, const float* __restrict__ y, float* __restrict__ out,
                             uint32_t n) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -426,6 +452,14 @@ void launch_inject_sphere(const DevState& s, const float c[3], float r, float dy
                                                             (DS*)s.conc, c[0], c[1], c[2], r, dye, vel[0], vel[1],
                                                             vel[2], sigma, seed);
   });
+}
+
+void launch_sphere_impulse(const DevState& s, const float* a_u, const float* a_v, const float* a_w, const float c[3],
+                           float r, const float vel[3], double* out, cudaStream_t st) {
+  const dim3 grid((s.g.nx + 31) / 32, (s.g.ny + 7) / 8, s.g.nz);
+  cudaMemsetAsync(out, 0, sizeof(double), st);
+  k_sphere_impulse<<<grid, dim3(32, 8, 1), 0, st>>>(s.g, s.params, a_u, a_v, a_w, c[0], c[1], c[2], r, vel[0], vel[1],
+                                                    vel[2], out);
 }
 
 cudaError_t eval_math_device(int fn, const float* x, const float* y, float* out, uint32_t n) {

@@ -52,6 +52,47 @@ FIELD_SPLAT_INTACT = 9
 FIELD_SPLAT_LYSED = 10
 FIELD_WAVE = 11
 FIELD_DIVERGENCE = 12
+# adjoint fields (closed box, FP32, dye_refine 1)
+FIELD_ADJ_VEL_U = 16
+FIELD_ADJ_VEL_V = 17
+FIELD_ADJ_VEL_W = 18
+FIELD_ADJ_VEL_U2 = 19
+FIELD_ADJ_VEL_V2 = 20
+FIELD_ADJ_VEL_W2 = 21
+FIELD_ADJ_CENTER = 22
+FIELD_ADJ_CONC = 23
+FIELD_ADJ_CONC2 = 24
+FIELD_ADJ_PRED = 25
+FIELD_ADJ_PRESSURE = 26
+FIELD_ADJ_RHS = 27
+ADJ_VEL_FIELDS = (FIELD_ADJ_VEL_U, FIELD_ADJ_VEL_V, FIELD_ADJ_VEL_W)
+ADJ_VEL2_FIELDS = (FIELD_ADJ_VEL_U2, FIELD_ADJ_VEL_V2, FIELD_ADJ_VEL_W2)
+
+
+def field_shapes(vdims, cdims, ref):
+    """Host array shape and dtype of every field id (include/dropfluid.h)."""
+    nz, ny, nx = vdims
+    cz, cy, cx = cdims
+    import numpy as np
+    v = ((nz, ny, nx), np.float32)
+    c = ((cz, cy, cx), np.float32)
+    return {
+        FIELD_VEL_U: v, FIELD_VEL_V: v, FIELD_VEL_W: v,
+        FIELD_VEL_CENTER: ((nz, ny, nx, 4), np.float32),
+        FIELD_CURL: ((nz, ny, nx, 4), np.float32),
+        FIELD_PRESSURE: v, FIELD_RHS: v,
+        FIELD_CONC: (((cz, cy, cx, 4) if ref else (cz, cy, cx)), np.float32),
+        FIELD_CONC_PRED: c,
+        FIELD_SPLAT_INTACT: ((cz, cy, cx), np.uint32),
+        FIELD_SPLAT_LYSED: ((cz, cy, cx), np.uint32),
+        FIELD_WAVE: ((WAVE_N, WAVE_N, 4), np.float32),
+        FIELD_DIVERGENCE: v,
+        FIELD_ADJ_VEL_U: v, FIELD_ADJ_VEL_V: v, FIELD_ADJ_VEL_W: v,
+        FIELD_ADJ_VEL_U2: v, FIELD_ADJ_VEL_V2: v, FIELD_ADJ_VEL_W2: v,
+        FIELD_ADJ_CENTER: ((nz, ny, nx, 4), np.float32),
+        FIELD_ADJ_CONC: c, FIELD_ADJ_CONC2: c, FIELD_ADJ_PRED: c,
+        FIELD_ADJ_PRESSURE: v, FIELD_ADJ_RHS: v,
+    }
 
 # dob_stage (BloodDropEngine.ts:1855-2111 order)
 STAGE_ADVECT_MAC = 0

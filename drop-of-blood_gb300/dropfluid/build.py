@@ -26,6 +26,8 @@ UNITS = {
     "k_mg.cu": [],
     "k_exact.cu": ["-fmad=false"],
     "dob_noalloc.cu": [],
+    "dob_tape.cu": [],
+    "k_adjoint.cu": [],
 }
 
 

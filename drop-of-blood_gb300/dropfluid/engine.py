@@ -96,24 +96,8 @@ class DropFluid:
         self._ck(self._L.dob_set_high_water(self._h, int(hw)), "dob_set_high_water")
 
     def field_shape(self, field):
-        nz, ny, nx = self.vdims
-        cz, cy, cx = self.cdims
         ref = self.cfg.bc_mode == abi.DOB_BC_REFERENCE
-        return {
-            abi.FIELD_VEL_U: ((nz, ny, nx), np.float32),
-            abi.FIELD_VEL_V: ((nz, ny, nx), np.float32),
-            abi.FIELD_VEL_W: ((nz, ny, nx), np.float32),
-            abi.FIELD_VEL_CENTER: ((nz, ny, nx, 4), np.float32),
-            abi.FIELD_CURL: ((nz, ny, nx, 4), np.float32),
-            abi.FIELD_PRESSURE: ((nz, ny, nx), np.float32),
-            abi.FIELD_RHS: ((nz, ny, nx), np.float32),
-            abi.FIELD_CONC: (((cz, cy, cx, 4) if ref else (cz, cy, cx)), np.float32),
-            abi.FIELD_CONC_PRED: ((cz, cy, cx), np.float32),
-            abi.FIELD_SPLAT_INTACT: ((cz, cy, cx), np.uint32),
-            abi.FIELD_SPLAT_LYSED: ((cz, cy, cx), np.uint32),
-            abi.FIELD_WAVE: ((abi.WAVE_N, abi.WAVE_N, 4), np.float32),
-            abi.FIELD_DIVERGENCE: ((nz, ny, nx), np.float32),
-        }[field]
+        return abi.field_shapes(self.vdims, self.cdims, ref)[field]
 
     def set_field(self, field, arr):
         shape, dt = self.field_shape(field)
@@ -183,6 +167,34 @@ class DropFluid:
         self._ck(self._L.dob_bench_kernel(self._h, int(which), int(reps), C.byref(ms), C.byref(by)),
                  "dob_bench_kernel")
         return float(ms.value), float(by.value)
+
+    # -- discrete adjoint (closed box, FP32, dye_refine 1) ------------------------------------
+    def adjoint_stage(self, stage):
+        """Transpose of the Jacobian of one stage at the current forward state
+        (field conventions of dob_adjoint_stage)."""
+        self._ck(self._L.dob_adjoint_stage(self._h, int(stage)), f"dob_adjoint_stage({stage})")
+
+    def tape_forward(self, nsteps, checkpoint_every=8):
+        self._ck(self._L.dob_tape_forward(self._h, int(nsteps), int(checkpoint_every)), "dob_tape_forward")
+
+    def tape_backward(self, dye_grad):
+        shape, _ = self.field_shape(abi.FIELD_ADJ_CONC)
+        g = np.ascontiguousarray(dye_grad, dtype=np.float32).reshape(shape)
+        self._ck(self._L.dob_tape_backward(self._h, _fptr(g), g.nbytes), "dob_tape_backward")
+
+    def gradients(self):
+        """d loss / d (initial u, v, w, dye, pressure) after tape_backward."""
+        return {"u": self.get_field(abi.FIELD_ADJ_VEL_U), "v": self.get_field(abi.FIELD_ADJ_VEL_V),
+                "w": self.get_field(abi.FIELD_ADJ_VEL_W), "dye": self.get_field(abi.FIELD_ADJ_CONC),
+                "p": self.get_field(abi.FIELD_ADJ_PRESSURE)}
+
+    def sphere_impulse(self, center, radius, vel) -> float:
+        c = (C.c_float * 3)(*center)
+        v = (C.c_float * 3)(*vel)
+        out = C.c_double(0.0)
+        self._ck(self._L.dob_adjoint_sphere_impulse(self._h, c, C.c_float(radius), v, C.byref(out)),
+                 "dob_adjoint_sphere_impulse")
+        return out.value
 
     def save_state(self, slot):
         self._ck(self._L.dob_save_state(self._h, int(slot)), "dob_save_state")

@@ -126,7 +126,26 @@ typedef enum dob_field {
   DOB_FIELD_SPLAT_LYSED = 10,
   DOB_FIELD_WAVE = 11,
   DOB_FIELD_DIVERGENCE = 12,   /* read-only: MAC divergence of the current velocity */
-  DOB_FIELD_COUNT = 13
+  DOB_FIELD_COUNT = 13,
+  /* Adjoint fields (closed box, FP32, dye_refine 1; see dob_adjoint_stage).
+     Host FP32, natural layout.  ADJ_VEL_U/V/W: adjoint of the MAC faces a
+     stage reads (after dob_tape_backward: d loss / d initial velocity);
+     ADJ_VEL_U2/V2/W2: adjoint of the faces advection / Casson write to
+     their second buffer; ADJ_CENTER: 4*nx*ny*nz (x, y, z, 0); ADJ_CONC
+     (after dob_tape_backward: d loss / d initial dye), ADJ_CONC2 (adjoint
+     of the resolved dye), ADJ_PRED: Nc; ADJ_PRESSURE, ADJ_RHS: nx*ny*nz. */
+  DOB_FIELD_ADJ_VEL_U = 16,
+  DOB_FIELD_ADJ_VEL_V = 17,
+  DOB_FIELD_ADJ_VEL_W = 18,
+  DOB_FIELD_ADJ_VEL_U2 = 19,
+  DOB_FIELD_ADJ_VEL_V2 = 20,
+  DOB_FIELD_ADJ_VEL_W2 = 21,
+  DOB_FIELD_ADJ_CENTER = 22,
+  DOB_FIELD_ADJ_CONC = 23,
+  DOB_FIELD_ADJ_CONC2 = 24,
+  DOB_FIELD_ADJ_PRED = 25,
+  DOB_FIELD_ADJ_PRESSURE = 26,
+  DOB_FIELD_ADJ_RHS = 27
 } dob_field;
 
 /* Stages of one step, in the reference's order (BloodDropEngine.ts:1855-2111).
@@ -259,6 +278,45 @@ dob_status dob_memory_bytes(const dob_ctx* ctx, uint64_t* bytes);
    and back.  Slots are allocated on first use. */
 dob_status dob_save_state(dob_ctx* ctx, int slot);
 dob_status dob_load_state(dob_ctx* ctx, int slot);
+
+/* ---- discrete adjoint (no counterpart in the reference; closed box, FP32,
+        dye_refine 1) ------------------------------------------------------
+
+   dob_adjoint_stage runs the transpose of the Jacobian of one stage at the
+   current forward state (the state the forward stage would read), on the
+   adjoint fields:
+     ADVECT_MAC      ADJ_VEL_*2 -> ADJ_VEL_*, ADJ_CENTER   (accumulate)
+     MAC_TO_CENTER   ADJ_CENTER -> ADJ_VEL_*
+     CASSON_FORCES   ADJ_VEL_*2 -> ADJ_VEL_*, ADJ_CONC
+     MAC_RHS         ADJ_RHS -> ADJ_VEL_* (ADJ_RHS is made mean-free in place)
+     PRESSURE_SOLVE  ADJ_PRESSURE -> ADJ_PRESSURE (replaced), ADJ_RHS
+     PROJECT         ADJ_VEL_* -> ADJ_VEL_* (replaced), ADJ_PRESSURE
+     CONC_PREDICT    ADJ_PRED -> ADJ_CONC, ADJ_CENTER
+     CONC_RESOLVE    ADJ_CONC2 -> ADJ_CONC, ADJ_PRED, ADJ_CENTER
+   Other stages return DOB_EINVAL.  Where the forward is not differentiable
+   (clamps at their bounds, the dye limiter, |grad u| = 0) the adjoint takes
+   the branch the forward executed. */
+dob_status dob_adjoint_stage(dob_ctx* ctx, int stage);
+
+/* Forward half of the forward/backward pair: sets the centre velocity from
+   the MAC faces (so the trajectory's state is velocity, dye and pressure),
+   then runs nsteps steps, keeping a checkpoint of (velocity, dye, pressure)
+   every `checkpoint_every` steps in device memory.  The context ends in the
+   final state, as after dob_step. */
+dob_status dob_tape_forward(dob_ctx* ctx, int nsteps, int checkpoint_every);
+
+/* Backward half: given d loss / d final dye (Nc floats, host), recomputes
+   each checkpoint segment and runs the adjoint of every step in reverse.
+   Leaves d loss / d initial MAC velocity in DOB_FIELD_ADJ_VEL_U/V/W,
+   d loss / d initial dye in DOB_FIELD_ADJ_CONC and d loss / d initial
+   pressure in DOB_FIELD_ADJ_PRESSURE.  The forward state is not changed. */
+dob_status dob_tape_backward(dob_ctx* ctx, const float* dye_grad, size_t bytes);
+
+/* Sum over the MAC faces dob_inject_sphere(center, radius, ..) sets of
+   ADJ_VEL . vel: d loss / d s when the injected face velocity is s * vel
+   (+ noise). */
+dob_status dob_adjoint_sphere_impulse(dob_ctx* ctx, const float center[3], float radius, const float vel[3],
+                                      double* out);
 
 /* Evaluate the library's own elementary functions on the device (used to
    check them against the host build bit for bit).  fn: 0 sin, 1 cos, 2 exp,

@@ -1461,6 +1461,8 @@ template <class R> class Sim {
     conc_predict();
     if (ref) conc_resolve_ref(); else dye_resolve_box();
   }
+
+#include "dob_oracle_adjoint.inc"
 };
 
 struct AnySim {
@@ -1468,6 +1470,23 @@ struct AnySim {
   Sim<float>* sf = nullptr;
   Sim<double>* sd = nullptr;
 };
+
+template <class R> std::vector<R>* adj_array(Sim<R>& s, int field) {
+  switch (field) {
+    case DOB_FIELD_ADJ_VEL_U: return &s.au;
+    case DOB_FIELD_ADJ_VEL_V: return &s.av;
+    case DOB_FIELD_ADJ_VEL_W: return &s.aw;
+    case DOB_FIELD_ADJ_VEL_U2: return &s.au2;
+    case DOB_FIELD_ADJ_VEL_V2: return &s.av2;
+    case DOB_FIELD_ADJ_VEL_W2: return &s.aw2;
+    case DOB_FIELD_ADJ_CONC: return &s.ac;
+    case DOB_FIELD_ADJ_CONC2: return &s.ac2;
+    case DOB_FIELD_ADJ_PRED: return &s.apred;
+    case DOB_FIELD_ADJ_PRESSURE: return &s.ap;
+    case DOB_FIELD_ADJ_RHS: return &s.arhs;
+    default: return nullptr;
+  }
+}
 
 template <class R> int set_field(Sim<R>& s, int field, const void* host, size_t bytes) {
   const size_t N = s.dv.n(), Nc = s.dc.n();
@@ -1505,8 +1524,21 @@ template <class R> int set_field(Sim<R>& s, int field, const void* host, size_t 
       if (bytes != s.wave.size() * 4) return DOB_EINVAL;
       memcpy(s.wave.data(), host, bytes);
       return DOB_OK;
-    default: return DOB_EINVAL;
+    default: break;
   }
+  if (field >= DOB_FIELD_ADJ_VEL_U && field <= DOB_FIELD_ADJ_RHS) {
+    s.adj_alloc();
+    if (field == DOB_FIELD_ADJ_CENTER) {
+      if (bytes != N * 4 * sizeof(float)) return DOB_EINVAL;
+      const float* f = (const float*)host;
+      for (size_t i = 0; i < N; ++i)
+        for (int c = 0; c < 3; ++c) s.acen[c][i] = (R)f[i * 4 + c];
+      return DOB_OK;
+    }
+    std::vector<R>* a = adj_array(s, field);
+    return put(*a, a->size());
+  }
+  return DOB_EINVAL;
 }
 
 template <class R> int get_field(Sim<R>& s, int field, void* host, size_t bytes) {
@@ -1553,8 +1585,61 @@ template <class R> int get_field(Sim<R>& s, int field, void* host, size_t bytes)
           for (int x = 0; x < s.dv.nx; ++x) f[s.dv.at(x, y, z)] = (float)s.divergence(x, y, z);
       return DOB_OK;
     }
-    default: return DOB_EINVAL;
+    default: break;
   }
+  if (field >= DOB_FIELD_ADJ_VEL_U && field <= DOB_FIELD_ADJ_RHS) {
+    s.adj_alloc();
+    if (field == DOB_FIELD_ADJ_CENTER) {
+      if (bytes != N * 4 * sizeof(float)) return DOB_EINVAL;
+      float* f = (float*)host;
+      for (size_t i = 0; i < N; ++i) {
+        for (int c = 0; c < 3; ++c) f[i * 4 + c] = (float)s.acen[c][i];
+        f[i * 4 + 3] = 0.0f;
+      }
+      return DOB_OK;
+    }
+    const std::vector<R>* a = adj_array(s, field);
+    return get(*a, a->size());
+  }
+  return DOB_EINVAL;
+}
+// Channel arrays of a field for the double-precision interface: returns the
+// channel count (0 if the field has no FP64 access).
+template <class R> int field_arrays(Sim<R>& s, int field, std::vector<R>* a[4]) {
+  switch (field) {
+    case DOB_FIELD_VEL_U: a[0] = &s.u; return 1;
+    case DOB_FIELD_VEL_V: a[0] = &s.v; return 1;
+    case DOB_FIELD_VEL_W: a[0] = &s.w; return 1;
+    case DOB_FIELD_VEL_CENTER: for (int c = 0; c < 4; ++c) a[c] = &s.cen[c]; return 4;
+    case DOB_FIELD_PRESSURE: a[0] = &s.p; return 1;
+    case DOB_FIELD_RHS: a[0] = &s.rhs; return 1;
+    case DOB_FIELD_CONC: if (s.nconc != 1) return 0; a[0] = &s.conc[0]; return 1;
+    case DOB_FIELD_CONC_PRED: a[0] = &s.pred; return 1;
+    default: break;
+  }
+  if (field >= DOB_FIELD_ADJ_VEL_U && field <= DOB_FIELD_ADJ_RHS && field != DOB_FIELD_ADJ_CENTER) {
+    s.adj_alloc();
+    a[0] = adj_array(s, field);
+    return 1;
+  }
+  return 0;
+}
+// double-precision field access (interleaved channels like the float API)
+template <class R> int get_field64(Sim<R>& s, int field, double* host, size_t n) {
+  std::vector<R>* a[4];
+  const int nch = field_arrays(s, field, a);
+  if (nch == 0 || n != a[0]->size() * nch) return DOB_EINVAL;
+  for (size_t i = 0; i < a[0]->size(); ++i)
+    for (int c = 0; c < nch; ++c) host[i * nch + c] = (double)(*a[c])[i];
+  return DOB_OK;
+}
+template <class R> int set_field64(Sim<R>& s, int field, const double* host, size_t n) {
+  std::vector<R>* a[4];
+  const int nch = field_arrays(s, field, a);
+  if (nch == 0 || n != a[0]->size() * nch) return DOB_EINVAL;
+  for (size_t i = 0; i < a[0]->size(); ++i)
+    for (int c = 0; c < nch; ++c) (*a[c])[i] = (R)host[i * nch + c];
+  return DOB_OK;
 }
 
 bool valid_config(const dob_config* c) {
@@ -1656,6 +1741,25 @@ void orc_set_threads(int n) {
   if (n > 0) omp_set_num_threads(n);
 }
 int orc_get_threads(void) { return omp_get_max_threads(); }
+
+int orc_adjoint_stage(orc_sim* s, int stage) { return DISPATCH(s, adjoint_stage(stage)); }
+int orc_tape_forward(orc_sim* s, int nsteps) { return DISPATCH(s, tape_forward(nsteps)); }
+int orc_tape_backward(orc_sim* s, const float* dye_grad, size_t bytes) {
+  const size_t nc = s->a.f64 ? s->a.sd->dc.n() : s->a.sf->dc.n();
+  if (!dye_grad || bytes != nc * sizeof(float)) return DOB_EINVAL;
+  return DISPATCH(s, tape_backward(dye_grad));
+}
+int orc_sphere_impulse(orc_sim* s, const float c[3], float radius, const float vel[3], double* out) {
+  if (!out) return DOB_EINVAL;
+  *out = DISPATCH(s, sphere_impulse(c, radius, vel));
+  return DOB_OK;
+}
+int orc_get_field64(orc_sim* s, int field, double* host, size_t n) {
+  return s->a.f64 ? get_field64(*s->a.sd, field, host, n) : get_field64(*s->a.sf, field, host, n);
+}
+int orc_set_field64(orc_sim* s, int field, const double* host, size_t n) {
+  return s->a.f64 ? set_field64(*s->a.sd, field, host, n) : set_field64(*s->a.sf, field, host, n);
+}
 
 int orc_eval_math(int fn, const float* x, const float* y, float* out, uint32_t n) {
   for (uint32_t i = 0; i < n; ++i) {

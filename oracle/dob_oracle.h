@@ -39,6 +39,18 @@ int orc_step(orc_sim* s, int nsteps, double* stats);
 int orc_run_stage(orc_sim* s, int stage);
 void orc_set_threads(int n);
 int orc_get_threads(void);
+/* Discrete adjoint of the closed-box step (same conventions as
+   dob_adjoint_stage / dob_tape_forward / dob_tape_backward; the oracle's
+   tape keeps every step, no checkpoints). */
+int orc_adjoint_stage(orc_sim* s, int stage);
+int orc_tape_forward(orc_sim* s, int nsteps);
+int orc_tape_backward(orc_sim* s, const float* dye_grad, size_t bytes);
+int orc_sphere_impulse(orc_sim* s, const float center[3], float radius, const float vel[3], double* out);
+/* double-precision access to the velocity, centre, pressure, rhs, dye,
+   predictor and adjoint fields (n = element count incl. channels; not
+   ADJ_CENTER), for finite differences below float32 resolution */
+int orc_get_field64(orc_sim* s, int field, double* host, size_t n);
+int orc_set_field64(orc_sim* s, int field, const double* host, size_t n);
 /* Host evaluation of the library's elementary functions (same ids as
    dob_eval_math). */
 int orc_eval_math(int fn, const float* x, const float* y, float* out, uint32_t n);

@@ -59,6 +59,13 @@ def lib():
         L.orc_run_stage.argtypes = [P, C.c_int]
         L.orc_set_threads.argtypes = [C.c_int]
         L.orc_get_threads.restype = C.c_int
+        L.orc_adjoint_stage.argtypes = [P, C.c_int]
+        L.orc_tape_forward.argtypes = [P, C.c_int]
+        L.orc_tape_backward.argtypes = [P, C.POINTER(C.c_float), C.c_size_t]
+        L.orc_sphere_impulse.argtypes = [P, C.POINTER(C.c_float), C.c_float, C.POINTER(C.c_float),
+                                         C.POINTER(C.c_double)]
+        L.orc_get_field64.argtypes = [P, C.c_int, C.c_void_p, C.c_size_t]
+        L.orc_set_field64.argtypes = [P, C.c_int, C.c_void_p, C.c_size_t]
         L.orc_eval_math.argtypes = [C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float),
                                     C.POINTER(C.c_float), C.c_uint32]
         _lib = L
@@ -144,24 +151,11 @@ class OracleSim:
         _check(lib().orc_set_high_water(self._h, int(hw)), "set_high_water")
 
     def _field_shape(self, field):
-        nz, ny, nx = self.vdims
-        cz, cy, cx = self.cdims
         ref = self.cfg.bc_mode == abi.DOB_BC_REFERENCE
-        return {
-            abi.FIELD_VEL_U: ((nz, ny, nx), np.float32),
-            abi.FIELD_VEL_V: ((nz, ny, nx), np.float32),
-            abi.FIELD_VEL_W: ((nz, ny, nx), np.float32),
-            abi.FIELD_VEL_CENTER: ((nz, ny, nx, 4), np.float32),
-            abi.FIELD_CURL: ((nz, ny, nx, 4), np.float32),
-            abi.FIELD_PRESSURE: ((nz, ny, nx), np.float32),
-            abi.FIELD_RHS: ((nz, ny, nx), np.float32),
-            abi.FIELD_CONC: (((cz, cy, cx, 4) if ref else (cz, cy, cx)), np.float32),
-            abi.FIELD_CONC_PRED: ((cz, cy, cx), np.float32),
-            abi.FIELD_SPLAT_INTACT: ((cz, cy, cx), np.uint32),
-            abi.FIELD_SPLAT_LYSED: ((cz, cy, cx), np.uint32),
-            abi.FIELD_WAVE: ((abi.WAVE_N, abi.WAVE_N, 4), np.float32),
-            abi.FIELD_DIVERGENCE: ((nz, ny, nx), np.float32),
-        }[field]
+        return abi.field_shapes(self.vdims, self.cdims, ref)[field]
+
+    def field_shape(self, field):
+        return self._field_shape(field)
 
     def set_field(self, field, arr):
         shape, dt = self._field_shape(field)
@@ -185,3 +179,38 @@ class OracleSim:
 
     def run_stage(self, stage):
         _check(lib().orc_run_stage(self._h, int(stage)), f"run_stage({stage})")
+
+    # -- discrete adjoint (closed box, dye_refine 1) ---------------------------------------
+    def adjoint_stage(self, stage):
+        _check(lib().orc_adjoint_stage(self._h, int(stage)), f"adjoint_stage({stage})")
+
+    def tape_forward(self, nsteps, checkpoint_every=None):
+        _check(lib().orc_tape_forward(self._h, int(nsteps)), "tape_forward")
+
+    def tape_backward(self, dye_grad):
+        shape, _ = self._field_shape(abi.FIELD_ADJ_CONC)
+        g = np.ascontiguousarray(dye_grad, dtype=np.float32).reshape(shape)
+        _check(lib().orc_tape_backward(self._h, _fptr(g), g.nbytes), "tape_backward")
+
+    def get_field64(self, field):
+        shape, _ = self._field_shape(field)
+        a = np.empty(shape, dtype=np.float64)
+        _check(lib().orc_get_field64(self._h, int(field), a.ctypes.data, a.size), "get_field64")
+        return a
+
+    def set_field64(self, field, arr):
+        shape, _ = self._field_shape(field)
+        a = np.ascontiguousarray(arr, dtype=np.float64).reshape(shape)
+        _check(lib().orc_set_field64(self._h, int(field), a.ctypes.data, a.size), "set_field64")
+
+    def gradients(self):
+        return {"u": self.get_field64(abi.FIELD_ADJ_VEL_U), "v": self.get_field64(abi.FIELD_ADJ_VEL_V),
+                "w": self.get_field64(abi.FIELD_ADJ_VEL_W), "dye": self.get_field64(abi.FIELD_ADJ_CONC),
+                "p": self.get_field64(abi.FIELD_ADJ_PRESSURE)}
+
+    def sphere_impulse(self, center, radius, vel) -> float:
+        c = (C.c_float * 3)(*center)
+        v = (C.c_float * 3)(*vel)
+        out = C.c_double(0.0)
+        _check(lib().orc_sphere_impulse(self._h, c, C.c_float(radius), v, C.byref(out)), "sphere_impulse")
+        return out.value

@@ -1,0 +1,117 @@
+"""The CUDA discrete adjoint (k_adjoint.cu, dob_tape.cu) through the C ABI.
+
+Per stage, the adjoint of the same forward state and cotangents is compared
+with the FP64 oracle's; the linear stages also pass the dot-product test on
+the device.  A recorded drop trajectory (checkpointed forward, segment
+recomputation, reverse pass) gives the drop-impulse gradient within 1e-3 of
+the FP64 oracle's and of central differences of the loss on the device,
+independently of the checkpoint interval.
+"""
+import numpy as np
+import pytest
+
+import adjoint_cases as AC
+from dropfluid import abi
+from helpers import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+# FP32 device adjoint vs FP64 oracle adjoint at the same (float32) state.  The
+# pressure adjoint is the difference of nearly equal terms (mean removal and
+# contracting V-cycles), so its relative error is larger.
+STAGE_TOL = 1e-5
+PRESSURE_TOL = 1e-3
+
+
+@pytest.fixture(scope="module")
+def pair(gpu_lib, oracle_mod):
+    from dropfluid import DropFluid
+    cfg = AC.box_config((16, 24, 16))
+    g = DropFluid(cfg)
+    o = oracle_mod.OracleSim(cfg, fp64=True)
+    yield cfg, g, o, AC.stage_state(cfg, seed=3)
+    g.close()
+
+
+@pytest.mark.parametrize("stage", sorted(AC.STAGES))
+def test_stage_adjoint_matches_fp64_oracle(pair, stage):
+    cfg, g, o, st = pair
+    ins, outs, _, _ = AC.STAGES[stage]
+    ys = AC.seeded_cotangents(g, outs, 100 + stage)
+    rg = AC.run_stage_adjoint(g, st, stage, ys)
+    ro = AC.run_stage_adjoint(o, st, stage, ys)
+    for f in ins:
+        tol = PRESSURE_TOL if (stage == abi.STAGE_PRESSURE_SOLVE and f == abi.FIELD_PRESSURE) else STAGE_TOL
+        assert rel_l2(rg[f], ro[f]) < tol, (abi.STAGE_NAMES[stage], f, rel_l2(rg[f], ro[f]))
+
+
+@pytest.mark.parametrize("stage", AC.LINEAR)
+def test_linear_stage_dot_product_on_device(pair, stage):
+    cfg, g, o, st = pair
+    ins, outs, _, _ = AC.STAGES[stage]
+    xs = AC.seeded_cotangents(g, ins, 10 + stage)
+    ys = AC.seeded_cotangents(g, outs, 20 + stage)
+    AC.load(g, st)
+    for f, a in xs.items():
+        g.set_field(f, a)
+    g.run_stage(stage)
+    lhs = sum(float(np.sum(g.get_field(f).astype(np.float64) * ys[f])) for f in outs)
+    adj = AC.run_stage_adjoint(g, st, stage, ys)
+    rhs = sum(float(np.sum(xs[f].astype(np.float64) * adj[f])) for f in ins)
+    assert abs(lhs - rhs) <= 1e-4 * abs(lhs), (lhs, rhs)
+
+
+def test_trajectory_gradient(gpu_lib, oracle_mod):
+    from dropfluid import DropFluid
+    cfg, center, r = AC.drop_scene((24, 32, 24))
+    g = DropFluid(cfg)
+    o = oracle_mod.OracleSim(cfg, fp64=True)
+    steps = 8
+    AC.init_drop(o, center, r, 1.1)
+    o.tape_forward(steps)
+    target = o.get_field(abi.FIELD_CONC).astype(np.float64)
+
+    def run(e, imp, k):
+        AC.init_drop(e, center, r, imp)
+        e.tape_forward(steps, k)
+        d = e.get_field(abi.FIELD_CONC).astype(np.float64) - target
+        return float(np.sum(d * d)), d
+
+    grads = {}
+    for name, e, k in (("gpu3", g, 3), ("gpu8", g, 8), ("orc", o, None)):
+        _, d = run(e, 1.0, k)
+        e.tape_backward((2 * d).astype(np.float32))
+        grads[name] = (e.gradients(), e.sphere_impulse(center, r, [0.0, -2.0, 0.0]))
+    gi, oi = grads["gpu3"][1], grads["orc"][1]
+    assert abs(gi - oi) <= 1e-3 * abs(oi), (gi, oi)
+    # checkpoint interval 3 (three segments, the last one partial) vs 8
+    assert rel_l2(grads["gpu3"][0]["u"], grads["gpu8"][0]["u"]) < 1e-5
+    assert abs(grads["gpu3"][1] - grads["gpu8"][1]) <= 1e-5 * abs(oi)
+    # field gradients: FP32 vs FP64 trajectories take different limiter
+    # branches at a few cells, which the per-cell gradient sees
+    for k in ("u", "v", "w"):
+        assert rel_l2(grads["gpu3"][0][k], grads["orc"][0][k]) < 5e-2, k
+    # central differences of the device loss in the impulse
+    h = 1e-2
+    fd = (run(g, 1.0 + h, 8)[0] - run(g, 1.0 - h, 8)[0]) / (2 * h)
+    assert abs(fd - gi) <= 1e-3 * abs(fd), (fd, gi)
+    g.close()
+
+
+def test_adjoint_rejects_other_modes(gpu_lib):
+    from dropfluid import DropFluid, DropFluidError
+    cfg = abi.config_reference()
+    cfg.nx, cfg.ny, cfg.nz = 32, 32, 32
+    cfg.mg_levels = 3
+    cfg.parcel_capacity = 1024
+    with DropFluid(cfg) as sim:
+        with pytest.raises(DropFluidError):
+            sim.adjoint_stage(abi.STAGE_PROJECT)
+        with pytest.raises(DropFluidError):
+            sim.tape_forward(2, 1)
+    cfg = AC.box_config((16, 24, 16))
+    with DropFluid(cfg) as sim:
+        with pytest.raises(DropFluidError):
+            sim.tape_backward(np.zeros((16, 24, 16), np.float32))  # nothing recorded
+        with pytest.raises(DropFluidError):
+            sim.adjoint_stage(abi.STAGE_CLEAR_SPLATS)
