@@ -60,10 +60,10 @@ static bool valid_config(const dob_config* c, std::string* why) {
   const uint64_t r3 = (uint64_t)c->dye_refine * c->dye_refine * c->dye_refine;
   if ((uint64_t)c->nx * c->ny * c->nz * r3 >= (1ull << 31)) return no("grid too large (the dye grid must have < 2^31 cells)");
   if (c->mg_levels < 1 || c->mg_levels > kMaxLevels) return no("mg_levels out of range");
-  const uint32_t m = 1u << (c->mg_levels - 1);
-  if (c->nx % m || c->ny % m || c->nz % m) return no("dims not divisible by 2^(mg_levels-1)");
-  if ((c->nx >> (c->mg_levels - 1)) < 2 || (c->ny >> (c->mg_levels - 1)) < 2 || (c->nz >> (c->mg_levels - 1)) < 2)
-    return no("coarsest grid smaller than 2");
+  // every grid of the hierarchy has even dims (red-black split rows)
+  const uint32_t m = 1u << c->mg_levels;
+  if (c->nx % m || c->ny % m || c->nz % m)
+    return no("dims not divisible by 2^mg_levels (every multigrid level needs even dims)");
   if (c->bc_mode != DOB_BC_REFERENCE && c->bc_mode != DOB_BC_CLOSED_BOX) return no("bad bc_mode");
   if (c->precision_mode < 0 || c->precision_mode > 2) return no("bad precision_mode");
   if (c->mg_pre < 0 || c->mg_post < 0 || c->mg_coarse_sweeps < 0 || c->mg_cycles < 0) return no("negative sweeps");

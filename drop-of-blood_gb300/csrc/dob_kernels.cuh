@@ -185,5 +185,7 @@ void launch_adj_pressure_solve(const DevState& s, const AdjState& a, cudaStream_
 void launch_adj_project(const DevState& s, const AdjState& a, cudaStream_t st);
 void launch_adj_conc_predict(const DevState& s, const AdjState& a, cudaStream_t st);
 void launch_adj_conc_resolve(const DevState& s, const AdjState& a, cudaStream_t st);
+// Raise the dynamic shared-memory limit of the transposed coarse solve.
+cudaError_t adj_prepare();
 
 }  // namespace dob

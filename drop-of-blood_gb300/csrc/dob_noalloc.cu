@@ -116,10 +116,9 @@ extern "C" dob_status dob_pressure_solve_noalloc(const dob_config* cfg, const fl
   if (n > kNoAllocMaxCells)
     return bad("grid larger than the fixed scratch array allows (at most 2^21 = 2097152 cells)");
   if (cfg->mg_levels < 1 || cfg->mg_levels > kMaxLevels) return bad("mg_levels out of range");
-  const uint32_t m = 1u << (cfg->mg_levels - 1);
-  if (nx % m || ny % m || nz % m) return bad("dims not divisible by 2^(mg_levels-1)");
-  if ((nx >> (cfg->mg_levels - 1)) < 2 || (ny >> (cfg->mg_levels - 1)) < 2 || (nz >> (cfg->mg_levels - 1)) < 2)
-    return bad("coarsest grid smaller than 2");
+  const uint32_t m = 1u << cfg->mg_levels;
+  if (nx % m || ny % m || nz % m)
+    return bad("dims not divisible by 2^mg_levels (every multigrid level needs even dims)");
   if (cfg->bc_mode != DOB_BC_REFERENCE && cfg->bc_mode != DOB_BC_CLOSED_BOX) return bad("bad bc_mode");
   if (cfg->precision_mode == DOB_PREC_MIXED)
     return bad("the mixed-precision solve is not available without allocation; use DOB_PREC_FP32");

@@ -76,6 +76,8 @@ dob_status alloc(dob_ctx* ctx, std::vector<void*>& list, void** p, size_t bytes)
 // Adjoint arrays, allocated (zeroed) on first use.
 dob_status ensure_adj(dob_ctx* ctx) {
   if (ctx->adj) return DOB_OK;
+  cudaError_t pe = adj_prepare();
+  if (pe != cudaSuccess) return record_error(ctx, DOB_ECUDA, "adj_prepare", cudaGetErrorString(pe));
   AdjCtx* A = new AdjCtx();
   memset(&A->a, 0, sizeof(A->a));
   ctx->adj = A;

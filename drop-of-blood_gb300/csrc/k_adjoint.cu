@@ -24,9 +24,12 @@
 //
 // Adjoint arrays are FP32, natural layout except the pressure / right-hand
 // side / multigrid ones (red-black split like their forward arrays).
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include "dob_kernels.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace dob {
 
@@ -332,28 +335,169 @@ __global__ void __launch_bounds__(256) k_adj_rbgs(Grid d, int color, float h2, i
   bb[j] += -h2 * xb[j] / diag;
   xb[j] = mode == ADJ_SWEEP_FUSED ? nbr_scaled_sum(xb, d, ref, x, y, z) : 0.0f;
 }
-// Transpose of the fused residual + restriction B_c = 0.125 sum (b - A'x/h2):
-// per fine cell, bb += 0.125 Bb(parent); xb -= (A' rbar)/h2 with
-// rbar(n) = 0.125 Bb(parent(n)).
-__global__ void __launch_bounds__(256) k_adj_restrict(Grid f, Grid c, float h2, int ref, const float* __restrict__ Bb,
-                                                      float* xb, float* bb) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+// Vectorised form of the transposed half-sweeps for rows with nx % 8 == 0,
+// same thread layout as the forward k_rbgs_v4 (four cells of one colour
+// per thread, rows packed into warps, branch-free boundaries).  Within a
+// transposed run the adjoint is kept scaled by the diagonal, y = xb / diag,
+// so a cell only needs its own diagonal:
+//   SCALE    y = xb / diag                      (colour of the last half-sweep)
+//   FIRST    y = (xb + sum_n y(n)) / diag       (xb: the unscaled own value)
+//   FUSED    bb += -h2 y;  y = sum_n y(n) / diag
+//   FINAL    bb += -h2 y;  y = 0
+//   UNSCALE  xb = y * diag                      (the other colour, at the end)
+enum { ADJ4_SCALE = 0, ADJ4_FIRST = 1, ADJ4_FUSED = 2, ADJ4_FINAL = 3, ADJ4_UNSCALE = 4 };
+__device__ __forceinline__ float4 ld4f(const float* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ float f4at(const float4& v, int j) {
+  return j == 0 ? v.x : (j == 1 ? v.y : (j == 2 ? v.z : v.w));
+}
+__global__ void __launch_bounds__(256) k_adj_rbgs_v4(Grid d, int color, float h2, int ref, int mode, float* __restrict__ a,
+                                                     float* __restrict__ bb) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int z = blockIdx.z;
-  if (x >= f.nx || y >= f.ny) return;
-  auto rbar = [&](int xx, int yy, int zz) { return 0.125f * Bb[rb_index(c, xx >> 1, yy >> 1, zz >> 1)]; };
-  const float r0 = rbar(x, y, z);
-  const size_t j = rb_index(f, x, y, z);
-  float sumN = 0.0f;
-  if (x > 0) sumN += rbar(x - 1, y, z);
-  if (x < f.nx - 1) sumN += rbar(x + 1, y, z);
-  if (y > 0) sumN += rbar(x, y - 1, z);
-  if (y < f.ny - 1) sumN += rbar(x, y + 1, z);
-  if (z > 0) sumN += rbar(x, y, z - 1);
-  if (z < f.nz - 1) sumN += rbar(x, y, z + 1);
-  bb[j] += r0;
-  xb[j] -= (sumN - mg_diag(f, ref, x, y, z) * r0) / h2;
+  const uint32_t hx = (uint32_t)d.nx >> 1;
+  const uint32_t k0 = 4u * (uint32_t)q;
+  if (k0 >= hx || y >= d.ny) return;
+  const int p = (y + z + color) & 1;
+  const uint32_t half = (uint32_t)(d.n() >> 1);
+  const uint32_t sz = (uint32_t)d.ny * hx;
+  const uint32_t r = (uint32_t)z * sz + (uint32_t)y * hx;
+  float* own = a + (color ? half : 0u) + r + k0;
+  const float* oth = a + (color ? 0u : half);
+  const bool has_ym = y > 0, has_yp = y < d.ny - 1, has_zm = z > 0, has_zp = z < d.nz - 1;
+  const bool has_ex = p == 0 ? k0 > 0 : k0 + 4 < hx;
+  const float wex = has_ex ? 1.0f : 0.0f;
+  const float wym = has_ym ? 1.0f : 0.0f, wyp = has_yp ? 1.0f : 0.0f;
+  const float wzm = has_zm ? 1.0f : 0.0f, wzp = has_zp ? 1.0f : 0.0f;
+  const float dyz = (wym + wzm + wzp) + (ref ? 1.0f : wyp);
+  float diag[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const float wxm = (p == 0 && j == 0) ? wex : 1.0f;
+    const float wxp = (p == 1 && j == 3) ? wex : 1.0f;
+    diag[j] = dyz + (wxm + wxp);
+  }
+  const float4 ov = ld4f(own);
+  float res[4];
+  if (mode == ADJ4_SCALE || mode == ADJ4_UNSCALE) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) res[j] = mode == ADJ4_SCALE ? f4at(ov, j) / diag[j] : f4at(ov, j) * diag[j];
+  } else if (mode == ADJ4_FINAL) {
+    float* bp = bb + (color ? half : 0u) + r + k0;
+    const float4 bv = ld4f(bp);
+    *reinterpret_cast<float4*>(bp) =
+        make_float4(bv.x - h2 * ov.x, bv.y - h2 * ov.y, bv.z - h2 * ov.z, bv.w - h2 * ov.w);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) res[j] = 0.0f;
+  } else {
+    const uint32_t rym = has_ym ? r - hx : r, ryp = has_yp ? r + hx : r;
+    const uint32_t rzm = has_zm ? r - sz : r, rzp = has_zp ? r + sz : r;
+    const float4 cm = ld4f(oth + r + k0);
+    const float4 ym = ld4f(oth + rym + k0), yp = ld4f(oth + ryp + k0);
+    const float4 zm = ld4f(oth + rzm + k0), zp = ld4f(oth + rzp + k0);
+    const uint32_t kex = p == 0 ? (has_ex ? k0 - 1 : k0) : (has_ex ? k0 + 4 : k0 + 3);
+    const float ex = oth[r + kex];
+    if (mode == ADJ4_FUSED) {
+      float* bp = bb + (color ? half : 0u) + r + k0;
+      const float4 bv = ld4f(bp);
+      *reinterpret_cast<float4*>(bp) =
+          make_float4(bv.x - h2 * ov.x, bv.y - h2 * ov.y, bv.z - h2 * ov.z, bv.w - h2 * ov.w);
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const float xm = p == 0 ? (j == 0 ? ex : f4at(cm, j - 1)) : f4at(cm, j);
+      const float xp = p == 0 ? f4at(cm, j) : (j == 3 ? ex : f4at(cm, j + 1));
+      const float wxm = (p == 0 && j == 0) ? wex : 1.0f;
+      const float wxp = (p == 1 && j == 3) ? wex : 1.0f;
+      float sumN = mode == ADJ4_FIRST ? f4at(ov, j) : 0.0f;
+      sumN = fmaf(wxm, xm, sumN);
+      sumN = fmaf(wxp, xp, sumN);
+      sumN = fmaf(wym, f4at(ym, j), sumN);
+      sumN = fmaf(wyp, f4at(yp, j), sumN);
+      sumN = fmaf(wzm, f4at(zm, j), sumN);
+      sumN = fmaf(wzp, f4at(zp, j), sumN);
+      res[j] = sumN / diag[j];
+    }
+  }
+  *reinterpret_cast<float4*>(own) = make_float4(res[0], res[1], res[2], res[3]);
 }
+
+// Transposed coarse solve (zero start + `sweeps` red-black sweeps) inside
+// one thread-block cluster, the mirror of k_coarse_cluster: CTA r keeps the
+// scaled adjoint y and the right-hand-side adjoint of its z-slab in shared
+// memory and reads the neighbouring slabs' boundary planes through
+// distributed shared memory; one cluster barrier per transposed half-sweep.
+// On exit Ebar = 0 (the forward's zero start) and Bbar += its adjoint.
+template <int CS>
+__global__ void __cluster_dims__(CS, 1, 1) __launch_bounds__(512)
+    k_adj_coarse_cluster(Grid d, float h2, int ref, int sweeps, float* __restrict__ eb, float* __restrict__ bb) {
+  cg::cluster_group cl = cg::this_cluster();
+  extern __shared__ float asm_[];
+  const int rank = (int)cl.block_rank();
+  const int pz = d.nz / CS;
+  const int plane = d.nx * d.ny;
+  const int nloc = pz * plane;
+  float* sy = asm_;
+  float* sb = asm_ + nloc;
+  const int z0 = rank * pz;
+  const int K = 2 * sweeps;
+  auto color_of = [](int k) { return (k - 1) & 1; };
+  auto diag_at = [&](int x, int y, int z) {
+    float s = ref ? 1.0f : 0.0f;
+    s += (x > 0 ? 1.0f : 0.0f) + (x < d.nx - 1 ? 1.0f : 0.0f) + (y > 0 ? 1.0f : 0.0f);
+    s += (!ref && y < d.ny - 1) ? 1.0f : 0.0f;
+    s += (z > 0 ? 1.0f : 0.0f) + (z < d.nz - 1 ? 1.0f : 0.0f);
+    return s;
+  };
+  // load: y = Ebar / diag on the colour of the last half-sweep, Ebar elsewhere
+  for (int k = threadIdx.x; k < nloc; k += blockDim.x) {
+    const int zl = k / plane, rem = k - zl * plane;
+    const int y = rem / d.nx, x = rem - y * d.nx;
+    const int z = z0 + zl;
+    const float v = K > 0 ? eb[rb_index(d, x, y, z)] : 0.0f;
+    sy[k] = (K > 0 && ((x + y + z) & 1) == color_of(K)) ? v / diag_at(x, y, z) : v;
+    sb[k] = 0.0f;
+  }
+  const float* below = rank > 0 ? cl.map_shared_rank(sy, rank - 1) + (pz - 1) * plane : nullptr;
+  const float* above = rank < CS - 1 ? cl.map_shared_rank(sy, rank + 1) : nullptr;
+  cl.sync();
+  const int hxc = d.nx >> 1;
+  // phases: FIRST over the other colour, FUSED for k = K..2, FINAL for k = 1
+  for (int ph = 0; ph <= K && K > 0; ++ph) {
+    const int mode = ph == 0 ? 0 : (ph < K ? 1 : 2);  // 0 FIRST, 1 FUSED, 2 FINAL
+    const int color = ph == 0 ? 1 - color_of(K) : color_of(K + 1 - ph);
+    for (int q = threadIdx.x; q < (nloc >> 1); q += blockDim.x) {
+      const int row = q / hxc, kx = q - row * hxc;
+      const int zl = row / d.ny, y = row - zl * d.ny;
+      const int z = z0 + zl;
+      const int x = 2 * kx + ((y + z + color) & 1);
+      const int rem = y * d.nx + x;
+      const int k = zl * plane + rem;
+      const float dg = diag_at(x, y, z);
+      const float own = sy[k];
+      if (mode != 0) sb[k] += -h2 * own;
+      if (mode == 2) { sy[k] = 0.0f; continue; }
+      float sumN = mode == 0 ? own : 0.0f;
+      if (x > 0) sumN += sy[k - 1];
+      if (x < d.nx - 1) sumN += sy[k + 1];
+      if (y > 0) sumN += sy[k - d.nx];
+      if (y < d.ny - 1) sumN += sy[k + d.nx];
+      if (z > 0) sumN += zl > 0 ? sy[k - plane] : below[rem];
+      if (z < d.nz - 1) sumN += zl < pz - 1 ? sy[k + plane] : above[rem];
+      sy[k] = sumN / dg;
+    }
+    cl.sync();
+  }
+  for (int k = threadIdx.x; k < nloc; k += blockDim.x) {
+    const int zl = k / plane, rem = k - zl * plane;
+    const int y = rem / d.nx, x = rem - y * d.nx;
+    const size_t j = rb_index(d, x, y, z0 + zl);
+    bb[j] += sb[k];
+    eb[j] = 0.0f;
+  }
+  cl.sync();  // keep this CTA's shared memory alive until its neighbours are done reading it
+}
+
 // weight of coarse index J in the cell-centred linear interpolation at fine
 // index xf (the forward's clamped taps; 0 above a Dirichlet top when `top0`)
 __device__ __forceinline__ float prolong_w(int xf, int nf, int nc, int J, bool top0) {
@@ -366,33 +510,137 @@ __device__ __forceinline__ float prolong_w(int xf, int nf, int nc, int J, bool t
   if (dob_clampi(i1, 0, nc - 1) == J && !(top0 && i1 >= nc)) wsum += fx;
   return wsum;
 }
-// Transpose of e_f += P e_c: Eb(J) += sum over the 4x4x4 fine cells around
-// J of their interpolation weight on J times xb.
-__global__ void __launch_bounds__(256) k_adj_prolong(Grid f, Grid c, int ref, const float* __restrict__ xb, float* Eb) {
-  const int X = blockIdx.x * blockDim.x + threadIdx.x;
+// ---- two coarse cells per thread (fine rows with nx % 4 == 0) ------------------------------
+// Thread q owns coarse cells X = 2q, 2q+1 of coarse row (Y, Z); in the split
+// layout the even fine cells x = 4q, 4q+2 of a fine row are words 2q, 2q+1 of
+// one half and the odd cells the same words of the other half (8-byte pairs).
+__device__ __forceinline__ float2 ld2f(const float* p) { return *reinterpret_cast<const float2*>(p); }
+__device__ __forceinline__ void st2f(float* p, float2 v) { *reinterpret_cast<float2*>(p) = v; }
+// coarse split value at (X, Y, Z) (in range)
+__device__ __forceinline__ float cval(const float* a, const Grid& c, uint32_t halfc, int X, int Y, int Z) {
+  const uint32_t hc = (uint32_t)c.nx >> 1;
+  return a[(((X + Y + Z) & 1) ? halfc : 0u) + ((uint32_t)Z * c.ny + Y) * hc + (uint32_t)(X >> 1)];
+}
+// Transposed residual + restriction, the mirror of k_residual_restrict2.
+__global__ void __launch_bounds__(256) k_adj_restrict2(Grid f, Grid c, float inv_h2, int ref, const float* __restrict__ Bb,
+                                                       float* __restrict__ xb, float* __restrict__ bb) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
   const int Y = blockIdx.y * blockDim.y + threadIdx.y;
   const int Z = blockIdx.z;
-  if (X >= c.nx || Y >= c.ny) return;
-  float wx[4], wy[4], wz[4];
+  if (2 * q >= c.nx || Y >= c.ny) return;
+  const uint32_t halfc = (uint32_t)(c.n() >> 1);
+  const bool has_xm = q > 0, has_xp = 2 * q + 2 < c.nx;
+  const int y0 = 2 * Y, z0 = 2 * Z;
+  const bool has_ym = y0 > 0, has_yp = y0 + 2 < f.ny, has_zm = z0 > 0, has_zp = z0 + 2 < f.nz;
+  // 0.125 * Bbar at the parents: the block row X' = 2q-1..2q+2 and the
+  // neighbouring coarse rows X' = 2q, 2q+1 (clamped reads when absent)
+  float cr[4], cym[2], cyp[2], czm[2], czp[2];
+#pragma unroll
+  for (int a = 0; a < 4; ++a) cr[a] = 0.125f * cval(Bb, c, halfc, dob_clampi(2 * q - 1 + a, 0, c.nx - 1), Y, Z);
+#pragma unroll
+  for (int a = 0; a < 2; ++a) {
+    cym[a] = 0.125f * cval(Bb, c, halfc, 2 * q + a, has_ym ? Y - 1 : Y, Z);
+    cyp[a] = 0.125f * cval(Bb, c, halfc, 2 * q + a, has_yp ? Y + 1 : Y, Z);
+    czm[a] = 0.125f * cval(Bb, c, halfc, 2 * q + a, Y, has_zm ? Z - 1 : Z);
+    czp[a] = 0.125f * cval(Bb, c, halfc, 2 * q + a, Y, has_zp ? Z + 1 : Z);
+  }
+  const float wxm0 = has_xm ? 1.0f : 0.0f, wxp3 = has_xp ? 1.0f : 0.0f;
+  const uint32_t hx = (uint32_t)f.nx >> 1, half = (uint32_t)(f.n() >> 1), sz = (uint32_t)f.ny * hx;
+  const uint32_t w = 2u * (uint32_t)q;
+#pragma unroll
+  for (int dz = 0; dz < 2; ++dz)
+#pragma unroll
+    for (int dy = 0; dy < 2; ++dy) {
+      const float wym = (dy == 1 || has_ym) ? 1.0f : 0.0f;
+      const float wyp = (dy == 0 || has_yp) ? 1.0f : 0.0f;
+      const float wzm = (dz == 1 || has_zm) ? 1.0f : 0.0f;
+      const float wzp = (dz == 0 || has_zp) ? 1.0f : 0.0f;
+      const float dyz = (wym + wzm + wzp) + (ref ? 1.0f : wyp);
+      float dx_[4], db_[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int pi = i >> 1;  // parent among 2q, 2q+1
+        const float r0 = cr[1 + pi];
+        const float rxm = i > 0 ? cr[1 + ((i - 1) >> 1)] : cr[0];
+        const float rxp = i < 3 ? cr[1 + ((i + 1) >> 1)] : cr[3];
+        const float rym = dy ? r0 : cym[pi];
+        const float ryp = dy ? cyp[pi] : r0;
+        const float rzm = dz ? r0 : czm[pi];
+        const float rzp = dz ? czp[pi] : r0;
+        const float wxm = i == 0 ? wxm0 : 1.0f;
+        const float wxp = i == 3 ? wxp3 : 1.0f;
+        float sumN = wxm * rxm;
+        sumN = fmaf(wxp, rxp, sumN);
+        sumN = fmaf(wym, rym, sumN);
+        sumN = fmaf(wyp, ryp, sumN);
+        sumN = fmaf(wzm, rzm, sumN);
+        sumN = fmaf(wzp, rzp, sumN);
+        const float diag = dyz + (wxm + wxp);
+        dx_[i] = (sumN - diag * r0) * inv_h2;
+        db_[i] = r0;
+      }
+      const int y = y0 + dy, z = z0 + dz, par = (y + z) & 1;
+      const uint32_t r = (uint32_t)z * sz + (uint32_t)y * hx + w;
+      float* xe = xb + (par ? half : 0u) + r;
+      float* xo = xb + (par ? 0u : half) + r;
+      float* be = bb + (par ? half : 0u) + r;
+      float* bo = bb + (par ? 0u : half) + r;
+      const float2 vxe = ld2f(xe), vxo = ld2f(xo), vbe = ld2f(be), vbo = ld2f(bo);
+      st2f(xe, make_float2(vxe.x - dx_[0], vxe.y - dx_[2]));
+      st2f(xo, make_float2(vxo.x - dx_[1], vxo.y - dx_[3]));
+      st2f(be, make_float2(vbe.x + db_[0], vbe.y + db_[2]));
+      st2f(bo, make_float2(vbo.x + db_[1], vbo.y + db_[3]));
+    }
+}
+// Transposed prolongation, the mirror of k_prolong_add2: Ebar(X) += sum of
+// the interpolation weight on X times xb over the fine cells 2X-1..2X+2 of
+// each axis.
+__global__ void __launch_bounds__(256) k_adj_prolong2(Grid f, Grid c, int ref, const float* __restrict__ xb,
+                                                      float* __restrict__ Eb) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int Y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int Z = blockIdx.z;
+  if (2 * q >= c.nx || Y >= c.ny) return;
+  float wx0[4], wx1[4], wy[4], wz[4];
 #pragma unroll
   for (int a = 0; a < 4; ++a) {
-    const int fxi = 2 * X - 1 + a, fyi = 2 * Y - 1 + a, fzi = 2 * Z - 1 + a;
-    wx[a] = (fxi >= 0 && fxi < f.nx) ? prolong_w(fxi, f.nx, c.nx, X, false) : 0.0f;
-    wy[a] = (fyi >= 0 && fyi < f.ny) ? prolong_w(fyi, f.ny, c.ny, Y, ref != 0) : 0.0f;
-    wz[a] = (fzi >= 0 && fzi < f.nz) ? prolong_w(fzi, f.nz, c.nz, Z, false) : 0.0f;
+    const int x0 = 4 * q - 1 + a, x1 = 4 * q + 1 + a;
+    wx0[a] = (x0 >= 0 && x0 < f.nx) ? prolong_w(x0, f.nx, c.nx, 2 * q, false) : 0.0f;
+    wx1[a] = (x1 >= 0 && x1 < f.nx) ? prolong_w(x1, f.nx, c.nx, 2 * q + 1, false) : 0.0f;
+    const int yf = 2 * Y - 1 + a, zf = 2 * Z - 1 + a;
+    wy[a] = (yf >= 0 && yf < f.ny) ? prolong_w(yf, f.ny, c.ny, Y, ref != 0) : 0.0f;
+    wz[a] = (zf >= 0 && zf < f.nz) ? prolong_w(zf, f.nz, c.nz, Z, false) : 0.0f;
   }
-  float acc = 0.0f;
+  const uint32_t hx = (uint32_t)f.nx >> 1, half = (uint32_t)(f.n() >> 1), sz = (uint32_t)f.ny * hx;
+  const uint32_t w = 2u * (uint32_t)q;
+  const bool has_lo = q > 0, has_hi = 4 * q + 4 < f.nx;
+  float acc0 = 0.0f, acc1 = 0.0f;
+#pragma unroll
   for (int cz = 0; cz < 4; ++cz) {
     if (wz[cz] == 0.0f) continue;
+#pragma unroll
     for (int by = 0; by < 4; ++by) {
       if (wy[by] == 0.0f) continue;
-      for (int ax = 0; ax < 4; ++ax) {
-        if (wx[ax] == 0.0f) continue;
-        acc += wx[ax] * wy[by] * wz[cz] * xb[rb_index(f, 2 * X - 1 + ax, 2 * Y - 1 + by, 2 * Z - 1 + cz)];
-      }
+      const int yf = 2 * Y - 1 + by, zf = 2 * Z - 1 + cz, par = (yf + zf) & 1;
+      const uint32_t r = (uint32_t)zf * sz + (uint32_t)yf * hx + w;
+      const float* pe = xb + (par ? half : 0u) + r;  // even cells 4q, 4q+2 (words 2q, 2q+1)
+      const float* po = xb + (par ? 0u : half) + r;  // odd cells 4q+1, 4q+3
+      const float2 e = ld2f(pe), o = ld2f(po);
+      const float lo = has_lo ? po[-1] : 0.0f;      // x = 4q-1 (odd, word 2q-1)
+      const float hi = has_hi ? pe[2] : 0.0f;       // x = 4q+4 (even, word 2q+2)
+      const float v[6] = {lo, e.x, o.x, e.y, o.y, hi};
+      const float s0 = wx0[0] * v[0] + wx0[1] * v[1] + wx0[2] * v[2] + wx0[3] * v[3];
+      const float s1 = wx1[0] * v[2] + wx1[1] * v[3] + wx1[2] * v[4] + wx1[3] * v[5];
+      const float wyz = wy[by] * wz[cz];
+      acc0 = fmaf(wyz, s0, acc0);
+      acc1 = fmaf(wyz, s1, acc1);
     }
   }
-  Eb[rb_index(c, X, Y, Z)] += acc;
+  const uint32_t hc = (uint32_t)c.nx >> 1, halfc = (uint32_t)(c.n() >> 1);
+  const uint32_t rc = ((uint32_t)Z * c.ny + Y) * hc + (uint32_t)q;
+  const int pc = (Y + Z) & 1;
+  Eb[(pc ? halfc : 0u) + rc] += acc0;
+  Eb[(pc ? 0u : halfc) + rc] += acc1;
 }
 
 // ---- CONC_PREDICT (closed box) ------------------------------------------------------------------
@@ -523,24 +771,86 @@ void launch_adj_project(const DevState& s, const AdjState& a, cudaStream_t st) {
   k_adj_project<<<cgrid(s.g), cblock(), 0, st>>>(s.g, a.au, a.av, a.aw, a.ap);
 }
 
+static inline dim3 qblock(const Grid& d) {
+  const int q = d.nx / 8;
+  const int bx = q < 256 ? q : 256;
+  int by = 256 / bx;
+  if (by > d.ny) by = d.ny;
+  return dim3(bx, by, 1);
+}
+static inline dim3 qgrid(const Grid& d, const dim3& b) {
+  return dim3((d.nx / 8 + b.x - 1) / b.x, (d.ny + b.y - 1) / b.y, d.nz);
+}
 // transpose of `sweeps` red-black sweeps (red then black each) on one level
 static void adj_smooth(const Grid& d, float h2, int ref, int sweeps, float* xb, float* bb, cudaStream_t st) {
   const int K = 2 * sweeps;
   if (K == 0) return;
   auto color_of = [](int k) { return (k - 1) & 1; };  // half-sweep k = 1..K
+  if (d.nx % 8 == 0) {
+    const dim3 b = qblock(d), g = qgrid(d, b);
+    k_adj_rbgs_v4<<<g, b, 0, st>>>(d, color_of(K), h2, ref, ADJ4_SCALE, xb, bb);
+    k_adj_rbgs_v4<<<g, b, 0, st>>>(d, 1 - color_of(K), h2, ref, ADJ4_FIRST, xb, bb);
+    for (int k = K; k >= 2; --k) k_adj_rbgs_v4<<<g, b, 0, st>>>(d, color_of(k), h2, ref, ADJ4_FUSED, xb, bb);
+    k_adj_rbgs_v4<<<g, b, 0, st>>>(d, color_of(1), h2, ref, ADJ4_FINAL, xb, bb);
+    k_adj_rbgs_v4<<<g, b, 0, st>>>(d, 1 - color_of(1), h2, ref, ADJ4_UNSCALE, xb, bb);
+    return;
+  }
   k_adj_rbgs<<<hgrid(d), cblock(), 0, st>>>(d, 1 - color_of(K), h2, ref, ADJ_SWEEP_FIRST, xb, bb);
   for (int k = K; k >= 2; --k)
     k_adj_rbgs<<<hgrid(d), cblock(), 0, st>>>(d, color_of(k), h2, ref, ADJ_SWEEP_FUSED, xb, bb);
   k_adj_rbgs<<<hgrid(d), cblock(), 0, st>>>(d, color_of(1), h2, ref, ADJ_SWEEP_FINAL, xb, bb);
 }
+template <int CS>
+static void adj_cluster(const MgLevel& L, int ref, int sweeps, float* eb, float* bb, cudaStream_t st) {
+  const size_t smem = 2 * (L.d.n() / CS) * sizeof(float);
+  k_adj_coarse_cluster<CS><<<CS, 512, smem, st>>>(L.d, L.h2, ref, sweeps, eb, bb);
+}
+// Transpose of the coarsest-grid solve; Ebar is zero on return.
+static void adj_coarse(const MgLevel& L, int ref, int sweeps, float* eb, float* bb, cudaStream_t st) {
+  int cs = 0;
+  for (int c : {8, 4, 2, 1})
+    if (L.d.nz % c == 0 && 2 * (L.d.n() / c) * sizeof(float) <= 200 * 1024) { cs = c; break; }
+  switch (cs) {
+    case 8: adj_cluster<8>(L, ref, sweeps, eb, bb, st); break;
+    case 4: adj_cluster<4>(L, ref, sweeps, eb, bb, st); break;
+    case 2: adj_cluster<2>(L, ref, sweeps, eb, bb, st); break;
+    case 1: adj_cluster<1>(L, ref, sweeps, eb, bb, st); break;
+    default:
+      adj_smooth(L.d, L.h2, ref, sweeps, eb, bb, st);
+      cudaMemsetAsync(eb, 0, L.d.n() * sizeof(float), st);
+      break;
+  }
+}
+cudaError_t adj_prepare() {
+  cudaError_t e = cudaFuncSetAttribute(k_adj_coarse_cluster<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_adj_coarse_cluster<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_adj_coarse_cluster<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_adj_coarse_cluster<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  return e;
+}
+static inline dim3 pblock(const Grid& c) {
+  const int q = c.nx / 2;
+  const int bx = q < 256 ? q : 256;
+  int by = 256 / bx;
+  if (by > c.ny) by = c.ny;
+  return dim3(bx, by, 1);
+}
+static inline dim3 pgrid(const Grid& c, const dim3& b) {
+  return dim3((c.nx / 2 + b.x - 1) / b.x, (c.ny + b.y - 1) / b.y, c.nz);
+}
 static void adj_restrict(const DevState& s, const AdjState& a, int l, float* xb, float* bb, cudaStream_t st) {
-  const Grid f = s.lv[l].d, c = s.lv[l + 1].d;
-  k_adj_restrict<<<cgrid(f), cblock(), 0, st>>>(f, c, s.lv[l].h2, s.ref, a.lb[l + 1], xb, bb);
+  const Grid f = s.lv[l].d, c = s.lv[l + 1].d;  // nx % 4 == 0 on every transfer level
+  const dim3 b = pblock(c);
+  k_adj_restrict2<<<pgrid(c, b), b, 0, st>>>(f, c, 1.0f / s.lv[l].h2, s.ref, a.lb[l + 1], xb, bb);
   cudaMemsetAsync(a.lb[l + 1], 0, c.n() * sizeof(float), st);
 }
 static void adj_prolong(const DevState& s, const AdjState& a, int l, const float* xb, cudaStream_t st) {
   const Grid f = s.lv[l].d, c = s.lv[l + 1].d;
-  k_adj_prolong<<<cgrid(c), cblock(), 0, st>>>(f, c, s.ref, xb, a.le[l + 1]);
+  const dim3 b = pblock(c);
+  k_adj_prolong2<<<pgrid(c, b), b, 0, st>>>(f, c, s.ref, xb, a.le[l + 1]);
 }
 // Transpose of one V-cycle (k_mg.cu vcycle) on (ap, arhs); the coarse
 // adjoint arrays are zero on entry and on exit.
@@ -558,8 +868,7 @@ static void adj_vcycle(const DevState& s, const AdjState& a, cudaStream_t st) {
     adj_prolong(s, a, l, a.le[l], st);
   }
   const MgLevel& LC = s.lv[L - 1];
-  adj_smooth(LC.d, LC.h2, s.ref, s.coarse_sweeps, a.le[L - 1], a.lb[L - 1], st);
-  cudaMemsetAsync(a.le[L - 1], 0, LC.d.n() * sizeof(float), st);
+  adj_coarse(LC, s.ref, s.coarse_sweeps, a.le[L - 1], a.lb[L - 1], st);
   for (int l = L - 2; l >= 1; --l) {
     adj_restrict(s, a, l, a.le[l], a.lb[l], st);
     adj_smooth(s.lv[l].d, s.lv[l].h2, s.ref, s.pre, a.le[l], a.lb[l], st);

@@ -14,10 +14,12 @@
 // Kernels:
 //   k_rbgs_split        one colour of red-black Gauss-Seidel (one thread per
 //                       cell of that colour, in place)
-//   k_residual_restrict residual b - A e of the 8 fine cells of a coarse cell,
-//                       averaged into its right-hand side (MG_RESIDUAL +
-//                       MG_RESTRICT fused: the fine residual is never stored)
-//   k_prolong_add       e_f += trilinear(e_c), cell-centred
+//   k_residual_restrict2 residual b - A e of the 8 fine cells of each of two
+//                       coarse cells, averaged into their right-hand sides
+//                       (MG_RESIDUAL + MG_RESTRICT fused: the fine residual is
+//                       never stored)
+//   k_prolong_add2      e_f += trilinear(e_c), cell-centred, two coarse cells
+//                       per thread
 //   k_coarse_cluster    every sweep of the coarsest grid inside one
 //                       thread-block cluster: each CTA keeps a slab of planes in
 //                       shared memory, reads the neighbour slabs' boundary
@@ -190,124 +192,6 @@ __global__ void __launch_bounds__(256) k_rbgs_v4(Grid d, int color, float h2, in
     res[j] = diag == 6.0f ? t * (1.0f / 6.0f) : t / diag;
   }
   Vec4Ld<T>::st(own + r + k0, make_float4(res[0], res[1], res[2], res[3]));
-}
-
-// MG_RESIDUAL + MG_RESTRICT (fluid.ts:744-800) fused: each thread owns one
-// coarse cell and averages the residual of its 8 fine cells (dz, dy, dx
-// order).  The 8 fine cells and the 24 cells around the faces of the 2x2x2
-// block are loaded once into registers (all at split index x/2 = X, except
-// the x-neighbours at X-1 and X+1), then the 8 residuals follow the
-// reference's stencil order exactly.
-template <class T, class TC>
-__global__ void __launch_bounds__(256) k_residual_restrict(Grid f, Grid c, float h2, int ref, const T* __restrict__ a,
-                                                           const T* __restrict__ b, TC* __restrict__ bc,
-                                                           const unsigned int* __restrict__ skip) {
-  if (skip_now(skip)) return;
-  const int X = blockIdx.x * blockDim.x + threadIdx.x;
-  const int Y = blockIdx.y * blockDim.y + threadIdx.y;
-  const int Z = blockIdx.z;
-  if (X >= c.nx || Y >= c.ny) return;
-  const size_t half = f.n() >> 1;
-  const int hx = f.nx >> 1;
-  const int x0 = 2 * X, y0 = 2 * Y, z0 = 2 * Z;
-  // value at fine (x0+ix, y0+iy, z0+iz), ix, iy, iz in [-1, 2]; 0 outside
-  auto P = [&](int ix, int iy, int iz) -> float {
-    const int x = x0 + ix, y = y0 + iy, z = z0 + iz;
-    if (x < 0 || x >= f.nx || y < 0 || y >= f.ny || z < 0 || z >= f.nz) return 0.0f;
-    return ldv(a + (size_t)((x + y + z) & 1) * half + ((size_t)z * f.ny + y) * hx + (x >> 1));
-  };
-  float blk[2][2][2], xm[2][2], xp[2][2], ym[2][2], yp[2][2], zm[2][2], zp[2][2];
-#pragma unroll
-  for (int dz = 0; dz < 2; ++dz)
-#pragma unroll
-    for (int dy = 0; dy < 2; ++dy)
-#pragma unroll
-      for (int dx = 0; dx < 2; ++dx) blk[dz][dy][dx] = P(dx, dy, dz);
-#pragma unroll
-  for (int u = 0; u < 2; ++u)
-#pragma unroll
-    for (int v = 0; v < 2; ++v) {
-      xm[u][v] = P(-1, v, u); xp[u][v] = P(2, v, u);
-      ym[u][v] = P(v, -1, u); yp[u][v] = P(v, 2, u);
-      zm[u][v] = P(v, u, -1); zp[u][v] = P(v, u, 2);
-    }
-  float sum = 0.0f;
-#pragma unroll
-  for (int dz = 0; dz < 2; ++dz)
-#pragma unroll
-    for (int dy = 0; dy < 2; ++dy)
-#pragma unroll
-      for (int dx = 0; dx < 2; ++dx) {
-        const int x = x0 + dx, y = y0 + dy, z = z0 + dz;
-        const float nxm = dx ? blk[dz][dy][0] : xm[dz][dy];
-        const float nxp = dx ? xp[dz][dy] : blk[dz][dy][1];
-        const float nym = dy ? blk[dz][0][dx] : ym[dz][dx];
-        const float nyp = dy ? yp[dz][dx] : blk[dz][1][dx];
-        const float nzm = dz ? blk[0][dy][dx] : zm[dy][dx];
-        const float nzp = dz ? zp[dy][dx] : blk[1][dy][dx];
-        float sumN = 0.0f, diag = ref ? 1.0f : 0.0f;
-        if (x > 0) { sumN = sumN + nxm; diag = diag + 1.0f; }
-        if (x < f.nx - 1) { sumN = sumN + nxp; diag = diag + 1.0f; }
-        if (y > 0) { sumN = sumN + nym; diag = diag + 1.0f; }
-        if (y < f.ny - 1) { sumN = sumN + nyp; if (!ref) diag = diag + 1.0f; }
-        if (z > 0) { sumN = sumN + nzm; diag = diag + 1.0f; }
-        if (z < f.nz - 1) { sumN = sumN + nzp; diag = diag + 1.0f; }
-        const float lapScaled = (sumN - diag * blk[dz][dy][dx]) / h2;
-        const float bv = ldv(b + (size_t)((x + y + z) & 1) * half + ((size_t)z * f.ny + y) * hx + X);
-        sum = sum + (bv - lapScaled);
-      }
-  stf(bc + rb_index(c, X, Y, Z), sum * 0.125f);
-}
-
-// MG_PROLONG_ADD (fluid.ts:806-855): cell-centred trilinear interpolation of
-// the coarse correction; above the top the reference's Dirichlet ghost is 0,
-// the closed box clamps (Neumann).
-template <class TC>
-__device__ __forceinline__ float coarse_err(const TC* e, const Grid& c, int ref, int x, int y, int z) {
-  if (ref && y >= c.ny) return 0.0f;
-  return rb_at(e, c, dob_clampi(x, 0, c.nx - 1), dob_clampi(y, 0, c.ny - 1), dob_clampi(z, 0, c.nz - 1));
-}
-// One thread per coarse cell (X,Y,Z) updates its 8 fine cells
-// (2X+dx, 2Y+dy, 2Z+dz): their trilinear taps all lie in the 3x3x3 coarse
-// neighbourhood, loaded once.  Each fine cell's coordinate and weights come
-// from the same per-cell formula as MG_PROLONG_ADD.
-template <class T, class TC>
-__global__ void __launch_bounds__(256) k_prolong_add(Grid f, Grid c, int ref, T* __restrict__ a,
-                                                     const TC* __restrict__ e, const unsigned int* __restrict__ skip) {
-  if (skip_now(skip)) return;
-  const int X = blockIdx.x * blockDim.x + threadIdx.x;
-  const int Y = blockIdx.y * blockDim.y + threadIdx.y;
-  const int Z = blockIdx.z;
-  if (X >= c.nx || Y >= c.ny) return;
-  float t[3][3][3];  // coarse taps at (X-1+i, Y-1+j, Z-1+k)
-#pragma unroll
-  for (int k = 0; k < 3; ++k)
-#pragma unroll
-    for (int j = 0; j < 3; ++j)
-#pragma unroll
-      for (int i = 0; i < 3; ++i) t[k][j][i] = coarse_err(e, c, ref, X - 1 + i, Y - 1 + j, Z - 1 + k);
-  const size_t half = f.n() >> 1;
-  const int hx = f.nx >> 1;
-#pragma unroll
-  for (int dz = 0; dz < 2; ++dz)
-#pragma unroll
-    for (int dy = 0; dy < 2; ++dy)
-#pragma unroll
-      for (int dx = 0; dx < 2; ++dx) {
-        const int x = 2 * X + dx, y = 2 * Y + dy, z = 2 * Z + dz;
-        const float cx = (((float)x + 0.5f) / (float)f.nx) * (float)c.nx - 0.5f;
-        const float cy = (((float)y + 0.5f) / (float)f.ny) * (float)c.ny - 0.5f;
-        const float cz = (((float)z + 0.5f) / (float)f.nz) * (float)c.nz - 0.5f;
-        const float fx = cx - floorf(cx), fy = cy - floorf(cy), fz = cz - floorf(cz);
-        // base tap = X-1+dx (same for y, z): index dx, dy, dz into t
-        const float x00 = dob_mix(t[dz][dy][dx], t[dz][dy][dx + 1], fx);
-        const float x10 = dob_mix(t[dz][dy + 1][dx], t[dz][dy + 1][dx + 1], fx);
-        const float x01 = dob_mix(t[dz + 1][dy][dx], t[dz + 1][dy][dx + 1], fx);
-        const float x11 = dob_mix(t[dz + 1][dy + 1][dx], t[dz + 1][dy + 1][dx + 1], fx);
-        const float corr = dob_mix(dob_mix(x00, x10, fy), dob_mix(x01, x11, fy), fz);
-        const size_t i = (size_t)((x + y + z) & 1) * half + ((size_t)z * f.ny + y) * hx + X;
-        stf(a + i, ldv(a + i) + corr);
-      }
 }
 
 // ---- two coarse cells per thread (fine rows with nx % 4 == 0) ----------------------------
@@ -709,13 +593,9 @@ static inline dim3 pair_grid(const Grid& c, const dim3& b) {
 template <class T>
 static void restrict_level(const DevState& s, int l, const T* x, const T* b, T* bc, const unsigned int* skip,
                            cudaStream_t st) {
-  const Grid f = s.lv[l].d, c = s.lv[l + 1].d;
-  if (f.nx % 4 == 0) {
-    const dim3 bp = pair_block(c);
-    k_residual_restrict2<T, T><<<pair_grid(c, bp), bp, 0, st>>>(f, c, 1.0f / s.lv[l].h2, s.ref, x, b, bc, skip);
-  } else {
-    k_residual_restrict<T, T><<<g_cells(c), b_cells(), 0, st>>>(f, c, s.lv[l].h2, s.ref, x, b, bc, skip);
-  }
+  const Grid f = s.lv[l].d, c = s.lv[l + 1].d;  // nx % 4 == 0 on every transfer level
+  const dim3 bp = pair_block(c);
+  k_residual_restrict2<T, T><<<pair_grid(c, bp), bp, 0, st>>>(f, c, 1.0f / s.lv[l].h2, s.ref, x, b, bc, skip);
 }
 static inline dim3 quad_grid(const Grid& d, const dim3& b) {
   const int q = d.nx / 8;
@@ -764,12 +644,8 @@ static void smooth(const DevState& s, int l, T* a, const T* b, int sweeps, bool 
   if (zero_first) k_fill_zero<T><<<s.num_sms * 2, 256, 0, st>>>(a, L.d.n(), skip);
   if (ec) {
     const Grid dc = s.lv[l + 1].d;
-    if (L.d.nx % 4 == 0) {
-      const dim3 bp = pair_block(dc);
-      k_prolong_add2<T, T><<<pair_grid(dc, bp), bp, 0, st>>>(L.d, dc, s.ref, a, ec, skip);
-    } else {
-      k_prolong_add<T, T><<<g_cells(dc), b_cells(), 0, st>>>(L.d, dc, s.ref, a, ec, skip);
-    }
+    const dim3 bp = pair_block(dc);  // every transfer level has nx % 4 == 0
+    k_prolong_add2<T, T><<<pair_grid(dc, bp), bp, 0, st>>>(L.d, dc, s.ref, a, ec, skip);
   }
   const bool v4 = (L.d.nx % 8) == 0;
   const dim3 bq = quad_block(L.d), gq = quad_grid(L.d, bq);

@@ -85,7 +85,9 @@ typedef struct dob_config {
   float domain_max[3];         /* the uniform block's domainBounds                  */
   int32_t bc_mode;             /* DOB_BC_*                                           */
   int32_t precision_mode;      /* DOB_PREC_*                                         */
-  int32_t mg_levels;           /* grids in the hierarchy (reference: 4)              */
+  int32_t mg_levels;           /* grids in the hierarchy (reference: 4); nx, ny, nz
+                                  must be divisible by 2^mg_levels so that every grid
+                                  has even dims                                      */
   int32_t mg_pre, mg_post;     /* RBGS sweeps before/after coarse correction          */
   int32_t mg_coarse_sweeps;    /* RBGS sweeps on the coarsest grid (reference: 6)    */
   int32_t mg_cycles;           /* V-cycles per step (reference: 1)                   */

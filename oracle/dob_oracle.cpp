@@ -1647,9 +1647,8 @@ bool valid_config(const dob_config* c) {
   if (c->nx < 4 || c->ny < 4 || c->nz < 4) return false;
   if (c->dye_refine != 1 && c->dye_refine != 2) return false;
   if (c->mg_levels < 1 || c->mg_levels > 10) return false;
-  const uint32_t m = 1u << (c->mg_levels - 1);
+  const uint32_t m = 1u << c->mg_levels;  // even dims on every level, like the library
   if (c->nx % m || c->ny % m || c->nz % m) return false;
-  if ((c->nx >> (c->mg_levels - 1)) < 2 || (c->ny >> (c->mg_levels - 1)) < 2 || (c->nz >> (c->mg_levels - 1)) < 2) return false;
   if (c->bc_mode != DOB_BC_REFERENCE && c->bc_mode != DOB_BC_CLOSED_BOX) return false;
   if (c->precision_mode < 0 || c->precision_mode > 2) return false;
   if (c->parcel_capacity < 1) return false;

@@ -45,6 +45,23 @@ def test_stage_adjoint_matches_fp64_oracle(pair, stage):
         assert rel_l2(rg[f], ro[f]) < tol, (abi.STAGE_NAMES[stage], f, rel_l2(rg[f], ro[f]))
 
 
+@pytest.mark.parametrize("dims,levels", [((20, 24, 16), 2), ((40, 32, 48), 3), ((48, 32, 48), 4)])
+def test_pressure_adjoint_other_grids(gpu_lib, oracle_mod, dims, levels):
+    """Levels whose rows take the scalar smoother (nx not a multiple of 8),
+    and deeper hierarchies."""
+    from dropfluid import DropFluid
+    cfg = AC.box_config(dims, levels=levels)
+    st = AC.stage_state(cfg, seed=5)
+    stage = abi.STAGE_PRESSURE_SOLVE
+    with DropFluid(cfg) as g:
+        o = oracle_mod.OracleSim(cfg, fp64=True)
+        ys = AC.seeded_cotangents(g, [abi.FIELD_PRESSURE], 7)
+        rg = AC.run_stage_adjoint(g, st, stage, ys)
+        ro = AC.run_stage_adjoint(o, st, stage, ys)
+        assert rel_l2(rg[abi.FIELD_RHS], ro[abi.FIELD_RHS]) < 1e-4
+        assert rel_l2(rg[abi.FIELD_PRESSURE], ro[abi.FIELD_PRESSURE]) < PRESSURE_TOL
+
+
 @pytest.mark.parametrize("stage", AC.LINEAR)
 def test_linear_stage_dot_product_on_device(pair, stage):
     cfg, g, o, st = pair

@@ -76,6 +76,7 @@ def test_config_builders_match_python(lib):
     lambda c: setattr(c, "struct_size", 4),
     lambda c: setattr(c, "nx", 30),
     lambda c: setattr(c, "mg_levels", 0),
+    lambda c: setattr(c, "mg_levels", 6),  # 32 / 2^5 = 1: odd coarse grid
     lambda c: setattr(c, "dye_refine", 3),
     lambda c: setattr(c, "bc_mode", 7),
     lambda c: setattr(c, "dt", float("nan")),
