@@ -38,6 +38,14 @@ struct AdjCtx {
   float* Tp = nullptr;
   float* Trhs = nullptr;
   double* dred = nullptr;   // reduction slot of dob_adjoint_sphere_impulse
+  // captured "recompute + reverse" graph of a segment, per (length, parity of
+  // the dye adjoint ping-pong at its start)
+  std::vector<cudaGraphExec_t> seg_graphs;
+  void drop_graphs() {
+    for (cudaGraphExec_t& g : seg_graphs)
+      if (g) cudaGraphExecDestroy(g);
+    seg_graphs.clear();
+  }
 };
 
 void adjoint_free(dob_ctx* ctx) {
@@ -46,6 +54,7 @@ void adjoint_free(dob_ctx* ctx) {
   for (void* p : A->bufs) cudaFree(p);
   for (void* p : A->tbufs) cudaFree(p);
   for (float* p : A->ck) cudaFree(p);
+  A->drop_graphs();
   delete A;
   ctx->adj = nullptr;
 }
@@ -119,6 +128,7 @@ dob_status ensure_tape(dob_ctx* ctx, int k, int nseg) {
   const DevState& s = ctx->s;
   const size_t N = s.g.n(), Nc = s.gc.n();
   if (A->k != k) {
+    A->drop_graphs();
     for (void* p : A->tbufs) cudaFree(p);
     A->tbufs.clear();
     A->Tu.assign(k + 1, nullptr); A->Tv.assign(k + 1, nullptr); A->Tw.assign(k + 1, nullptr);
@@ -172,7 +182,7 @@ void save_checkpoint(dob_ctx* ctx, int seg) {
 
 // Recompute steps [0, len) of segment `seg` from its checkpoint, recording
 // the linearisation points in the tape buffers.
-void replay_segment(dob_ctx* ctx, int seg, int len) {
+void restore_checkpoint(dob_ctx* ctx, int seg) {
   AdjCtx* A = ctx->adj;
   const DevState& s = ctx->s;
   const size_t N = s.g.n(), Nc = s.gc.n();
@@ -183,6 +193,13 @@ void replay_segment(dob_ctx* ctx, int seg, int len) {
   cudaMemcpyAsync(A->Tw[0], c[2], N * 4, cudaMemcpyDeviceToDevice, st);
   cudaMemcpyAsync(A->Tc[0], c[3], Nc * 4, cudaMemcpyDeviceToDevice, st);
   cudaMemcpyAsync(A->Tp, c[4], N * 4, cudaMemcpyDeviceToDevice, st);
+}
+// From the restored checkpoint state in the first tape slot: recompute
+// `len` steps recording their linearisation points.
+void replay_segment(dob_ctx* ctx, int len) {
+  AdjCtx* A = ctx->adj;
+  const DevState& s = ctx->s;
+  cudaStream_t st = ctx->stream;
   DevState t = s;
   t.u = A->Tu[0]; t.v = A->Tv[0]; t.w = A->Tw[0]; t.cen = A->Tcen[0];
   launch_mac_to_center(t, st);  // the centre velocity at a step's start is C(u)
@@ -347,12 +364,40 @@ dob_status dob_tape_backward(dob_ctx* ctx, const float* dye_grad, size_t bytes) 
   TCK(cudaMemcpyAsync(A->a.ac, dye_grad, bytes, cudaMemcpyHostToDevice, st));
   const int k = A->k;
   const int nseg = (A->nsteps + k - 1) / k;
+  if (A->seg_graphs.size() != (size_t)(2 * (k + 1))) {
+    A->drop_graphs();
+    A->seg_graphs.assign(2 * (k + 1), nullptr);
+  }
   for (int seg = nseg - 1; seg >= 0; --seg) {
     const int len = (seg == nseg - 1) ? A->nsteps - seg * k : k;
-    replay_segment(ctx, seg, len);
-    for (int j = len - 1; j >= 0; --j) backward_step(ctx, j);
-    TCK(cudaGetLastError());
+    restore_checkpoint(ctx, seg);
+    // The segment's launches only depend on (len, which dye adjoint buffer is
+    // current): capture them once as a graph and replay it.
+    const int parity = A->a.ac < A->a.ac2 ? 0 : 1;
+    cudaGraphExec_t& ge = A->seg_graphs[2 * len + parity];
+    const AdjState before = A->a;
+    if (!ge) {
+      TCK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+      replay_segment(ctx, len);
+      for (int j = len - 1; j >= 0; --j) backward_step(ctx, j);
+      cudaGraph_t g = nullptr;
+      TCK(cudaStreamEndCapture(st, &g));
+      cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) {
+        ge = nullptr;
+        return record_error(ctx, DOB_ECUDA, "cudaGraphInstantiate", cudaGetErrorString(e));
+      }
+      // capturing applied the segment's buffer swaps to the host copy;
+      // start from the pre-capture assignment and replay the graph
+      A->a = before;
+    }
+    TCK(cudaGraphLaunch(ge, st));
+    // the swaps the segment performs: dye adjoint ping-pong once per step,
+    // velocity adjoints twice per step (net none)
+    if (len & 1) std::swap(A->a.ac, A->a.ac2);
   }
+  TCK(cudaGetLastError());
   // the trajectory starts from cen = C(u(0))
   DevState t = s;
   launch_adj_mac_to_center(t, A->a, st);
