@@ -187,6 +187,99 @@ def cpu_baseline(scene_fn, steps, threads):
     return steps / dt, dt
 
 
+def adjoint_leg(fd_dirs: int = 16):
+    """Forward/backward pair of the discrete adjoint.
+
+    box96 (96x128x96, one r=8 drop with N(0, 0.05) face noise, 32 steps,
+    checkpoints every 8): loss =
+    ||dye - target||^2 with the target from the same scene at 1.1x the drop
+    impulse; gradient w.r.t. the initial MAC velocity and the impulse, checked
+    against central differences (impulse, and 16 seeded random directions of
+    the initial velocity).  box192 (three r=12 drops injected at step 0, 64
+    steps, checkpoints every 16) gives the full-size cost.  The ratio is the
+    wall time of dob_tape_backward per step (segment recomputation included)
+    over the device time of one forward step of the same scene."""
+    import numpy as np
+    from dropfluid import DropFluid, abi, scenes
+    from dropfluid.adjoint import DropTrajectory, l2_loss
+
+    def cost(scene, k, release_all=False):
+        eng = DropFluid(scene.config)
+        traj = DropTrajectory(eng, k)
+
+        def fwd(sc, pert=None):
+            eng.reset()
+            for j in (range(len(sc.drops)) if release_all else sc.releases_at(0)):
+                sc.release(eng, j)
+            if pert is not None:
+                for f, d in pert.items():
+                    eng.set_field(f, eng.get_field(f) + d)
+            return traj.forward(sc.steps)
+        return eng, traj, fwd
+
+    out = {}
+    # ---- box96 -----------------------------------------------------------------------------------
+    sc = scenes.box96()
+    eng, traj, fwd = cost(sc, 8)
+    target = fwd(scenes.box96(impulse_scale=1.1)).astype(np.float64)
+    loss, g = l2_loss(fwd(sc), target)
+    grads = traj.backward(g)  # first call captures the segment graphs
+    eng.sync()
+    t0 = time.perf_counter()
+    fwd(sc)
+    eng.sync()
+    t_tape_fwd = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    grads = traj.backward(g)
+    eng.sync()
+    t_bwd = time.perf_counter() - t0
+    d_imp = traj.drop_impulse_grad(sc, sc.drops[0])
+    fwd_ms = eng.time_steps(sc.steps) / sc.steps  # state after the run: same scene, same cost
+    h = 1e-3
+    lp = l2_loss(fwd(scenes.box96(impulse_scale=1.0 + h)), target)[0]
+    lm = l2_loss(fwd(scenes.box96(impulse_scale=1.0 - h)), target)[0]
+    fd_imp = (lp - lm) / (2 * h)
+    rng = np.random.default_rng(12345)
+    eps = 1e-3 * 75.0  # 0.1 % of the injected face speed (1.5 cells/step = 75 world units)
+    errs = []
+    shape = eng.field_shape(abi.FIELD_VEL_U)[0]
+    for _ in range(fd_dirs):
+        d = {f: rng.standard_normal(shape).astype(np.float32) for f in
+             (abi.FIELD_VEL_U, abi.FIELD_VEL_V, abi.FIELD_VEL_W)}
+        ad = sum(float(np.sum(grads[k].astype(np.float64) * d[f])) for k, f in
+                 (("u", abi.FIELD_VEL_U), ("v", abi.FIELD_VEL_V), ("w", abi.FIELD_VEL_W)))
+        lp = l2_loss(fwd(sc, {f: eps * a for f, a in d.items()}), target)[0]
+        lm = l2_loss(fwd(sc, {f: -eps * a for f, a in d.items()}), target)[0]
+        fd = (lp - lm) / (2 * eps)
+        errs.append(abs(fd - ad) / max(abs(fd), 1e-30))
+    out["box96"] = {
+        "steps": sc.steps, "checkpoint_every": 8, "loss": loss,
+        "forward_step_ms": fwd_ms, "tape_forward_ms_per_step": 1e3 * t_tape_fwd / sc.steps,
+        "backward_ms_per_step": 1e3 * t_bwd / sc.steps,
+        "ratio": 1e3 * t_bwd / sc.steps / fwd_ms,
+        "impulse_grad": d_imp, "impulse_fd": fd_imp, "impulse_rel_err": abs(d_imp - fd_imp) / abs(fd_imp),
+        "fd_dirs": fd_dirs, "fd_eps": eps, "fd_rel_err_max": max(errs), "fd_rel_err_median": float(np.median(errs)),
+    }
+    eng.close()
+    # ---- box192, three drops at step 0, 64 steps ------------------------------------------------
+    sc = scenes.box192()
+    sc.steps = 64
+    eng, traj, fwd = cost(sc, 16, release_all=True)
+    _, g = l2_loss(fwd(sc), np.zeros(eng.field_shape(abi.FIELD_CONC)[0]))
+    traj.backward(g)
+    eng.sync()
+    t0 = time.perf_counter()
+    traj.backward(g)
+    eng.sync()
+    t_bwd = time.perf_counter() - t0
+    fwd_ms = eng.time_steps(8) / 8
+    out["box192"] = {"steps": sc.steps, "checkpoint_every": 16, "forward_step_ms": fwd_ms,
+                     "backward_ms_per_step": 1e3 * t_bwd / sc.steps, "ratio": 1e3 * t_bwd / sc.steps / fwd_ms,
+                     "loss": "||dye||^2 (cost only)", "drops": "all three injected at step 0"}
+    eng.close()
+    return out
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return 0
@@ -221,6 +314,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--profile-run", action="store_true",
                     help="run only the FP32 scene (warm-up + steps, untimed) and exit: the command "
                          "the ncu launch lists and kernel captures are taken with")
@@ -298,6 +392,11 @@ def main():
                  "precision": "FP16 dye, BF16 correction levels, FP64 defect residual, FP32 compute"}
         em.close()
 
+    # ---- discrete adjoint (forward/backward pair) ---------------------------------------------------
+    adj = None
+    if not args.no_adjoint:
+        adj = adjoint_leg()
+
     # ---- CPU baseline (rank 0, N=1 only) ----------------------------------------------------------
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -322,7 +421,8 @@ def main():
             "cell_updates_per_s": value * 192 * 256 * 192,
             "max_div": st["max_div"], "residual_l2": st["residual_l2"], "rhs_l2": st["rhs_l2"],
             "mixed": mixed,
-            "adjoint_forward_ratio": None,
+            "adjoint_forward_ratio": adj["box96"]["ratio"] if adj else None,
+            "adjoint": adj,
             "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "path": "DropFluid.step(1, stats=True) per step: params host->device, step graph, "
                             "statistics device->host, synchronize"},

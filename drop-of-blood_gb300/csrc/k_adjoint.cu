@@ -42,34 +42,89 @@ __device__ __forceinline__ void tri_w(const Taps& t, float w[8]) {
 __device__ __forceinline__ uint32_t tap_at(const Taps& t, int k) {
   return t.base + ((k & 1) ? t.ox : 0u) + ((k & 2) ? t.oy : 0u) + ((k & 4) ? t.oz : 0u);
 }
-// d lerp8 / d(fx, fy, fz) of a scalar field
-__device__ __forceinline__ dob_v3 lerp8_dfrac(const Taps& t, const float* a) {
-  const float* p = a + t.base;
-  const float c0 = p[0], c1 = p[t.ox], c2 = p[t.oy], c3 = p[t.oy + t.ox];
-  const float c4 = p[t.oz], c5 = p[t.oz + t.ox], c6 = p[t.oz + t.oy], c7 = p[t.oz + t.oy + t.ox];
+// d lerp8 / d(fx, fy, fz) of a scalar field.  Linear interpolation has a
+// slope kink at every grid node; where a sample sits on a node along an axis
+// (e.g. a departure point of fluid at rest) the slope along that axis is the
+// mean of the slopes on either side, the value central differences see.  "On
+// a node" means a fraction of exactly 0 (kNodeBand = 0; a positive band would
+// also catch samples within that many texel units of a node from either side).
+// NodeLo gives the element offsets from the base node to the node below it
+// and from the node above the base to the next one (0 where clamp-to-edge
+// makes the function flat).
+constexpr float kNodeBand = 0.0f;
+struct NodeLo {
+  uint32_t lx, ly, lz;  // base -> base - 1
+  uint32_t hx, hy, hz;  // base + 1 -> base + 2
+};
+__device__ __forceinline__ NodeLo node_lo(const Grid& g, float u, float v, float w) {
+  const int ix = dob_clampi((int)floorf(u * (float)g.nx - 0.5f), 0, g.nx - 1);
+  const int iy = dob_clampi((int)floorf(v * (float)g.ny - 0.5f), 0, g.ny - 1);
+  const int iz = dob_clampi((int)floorf(w * (float)g.nz - 0.5f), 0, g.nz - 1);
+  const uint32_t sy = (uint32_t)g.nx, sz = (uint32_t)g.nx * (uint32_t)g.ny;
+  NodeLo n;
+  n.lx = ix > 0 ? 1u : 0u;
+  n.ly = iy > 0 ? sy : 0u;
+  n.lz = iz > 0 ? sz : 0u;
+  n.hx = ix + 2 <= g.nx - 1 ? 1u : 0u;
+  n.hy = iy + 2 <= g.ny - 1 ? sy : 0u;
+  n.hz = iz + 2 <= g.nz - 1 ? sz : 0u;
+  return n;
+}
+template <class F>
+__device__ __forceinline__ dob_v3 dfrac_core(const Taps& t, const NodeLo& n, F val) {
+  const uint32_t b = t.base;
+  const float c0 = val(b), c1 = val(b + t.ox), c2 = val(b + t.oy), c3 = val(b + t.oy + t.ox);
+  const float c4 = val(b + t.oz), c5 = val(b + t.oz + t.ox), c6 = val(b + t.oz + t.oy);
+  const float c7 = val(b + t.oz + t.oy + t.ox);
   const float x00 = dob_mix(c0, c1, t.fx), x10 = dob_mix(c2, c3, t.fx);
   const float x01 = dob_mix(c4, c5, t.fx), x11 = dob_mix(c6, c7, t.fx);
-  const float dfx = dob_mix(dob_mix(c1 - c0, c3 - c2, t.fy), dob_mix(c5 - c4, c7 - c6, t.fy), t.fz);
-  const float dfy = dob_mix(x10 - x00, x11 - x01, t.fz);
-  const float dfz = dob_mix(x01, x11, t.fy) - dob_mix(x00, x10, t.fy);
+  float dfx = dob_mix(dob_mix(c1 - c0, c3 - c2, t.fy), dob_mix(c5 - c4, c7 - c6, t.fy), t.fz);
+  float dfy = dob_mix(x10 - x00, x11 - x01, t.fz);
+  const float y0 = dob_mix(x00, x10, t.fy), y1 = dob_mix(x01, x11, t.fy);
+  float dfz = y1 - y0;
+  if (t.fx <= kNodeBand) {  // node at the base: slope below it from base - 1
+    const uint32_t o = b - n.lx;
+    const float l0 = val(o), l2 = val(o + t.oy), l4 = val(o + t.oz), l6 = val(o + t.oz + t.oy);
+    dfx = 0.5f * (dfx + dob_mix(dob_mix(c0 - l0, c2 - l2, t.fy), dob_mix(c4 - l4, c6 - l6, t.fy), t.fz));
+  } else if (t.fx >= 1.0f - kNodeBand) {  // node at base + 1: slope above it to base + 2
+    const uint32_t o = b + t.ox + n.hx;
+    const float h0 = val(o), h2 = val(o + t.oy), h4 = val(o + t.oz), h6 = val(o + t.oz + t.oy);
+    dfx = 0.5f * (dfx + dob_mix(dob_mix(h0 - c1, h2 - c3, t.fy), dob_mix(h4 - c5, h6 - c7, t.fy), t.fz));
+  }
+  if (t.fy <= kNodeBand) {
+    const uint32_t o = b - n.ly;
+    const float l00 = dob_mix(val(o), val(o + t.ox), t.fx);
+    const float l01 = dob_mix(val(o + t.oz), val(o + t.oz + t.ox), t.fx);
+    dfy = 0.5f * (dfy + dob_mix(x00 - l00, x01 - l01, t.fz));
+  } else if (t.fy >= 1.0f - kNodeBand) {
+    const uint32_t o = b + t.oy + n.hy;
+    const float h00 = dob_mix(val(o), val(o + t.ox), t.fx);
+    const float h01 = dob_mix(val(o + t.oz), val(o + t.oz + t.ox), t.fx);
+    dfy = 0.5f * (dfy + dob_mix(h00 - x10, h01 - x11, t.fz));
+  }
+  if (t.fz <= kNodeBand) {
+    const uint32_t o = b - n.lz;
+    const float m0 = dob_mix(val(o), val(o + t.ox), t.fx);
+    const float m1 = dob_mix(val(o + t.oy), val(o + t.oy + t.ox), t.fx);
+    dfz = 0.5f * (dfz + (y0 - dob_mix(m0, m1, t.fy)));
+  } else if (t.fz >= 1.0f - kNodeBand) {
+    const uint32_t o = b + t.oz + n.hz;
+    const float m0 = dob_mix(val(o), val(o + t.ox), t.fx);
+    const float m1 = dob_mix(val(o + t.oy), val(o + t.oy + t.ox), t.fx);
+    dfz = 0.5f * (dfz + (dob_mix(m0, m1, t.fy) - y1));
+  }
   return v3(dfx, dfy, dfz);
 }
+__device__ __forceinline__ dob_v3 lerp8_dfrac(const Taps& t, const NodeLo& n, const float* a) {
+  return dfrac_core(t, n, [&](uint32_t k) { return a[k]; });
+}
 // sum over the xyz channels of a float4 field: sum_ch g_ch * d lerp8_ch / d(fx, fy, fz)
-__device__ __forceinline__ dob_v3 lerp8x3_dfrac(const Taps& t, const float4* a, dob_v3 g) {
-  const float4* p = a + t.base;
-  const float4 c0 = p[0], c1 = p[t.ox], c2 = p[t.oy], c3 = p[t.oy + t.ox];
-  const float4 c4 = p[t.oz], c5 = p[t.oz + t.ox], c6 = p[t.oz + t.oy], c7 = p[t.oz + t.oy + t.ox];
-  // contract the channels first: the derivative is linear in the values
-  const float s0 = g.x * c0.x + g.y * c0.y + g.z * c0.z, s1 = g.x * c1.x + g.y * c1.y + g.z * c1.z;
-  const float s2 = g.x * c2.x + g.y * c2.y + g.z * c2.z, s3 = g.x * c3.x + g.y * c3.y + g.z * c3.z;
-  const float s4 = g.x * c4.x + g.y * c4.y + g.z * c4.z, s5 = g.x * c5.x + g.y * c5.y + g.z * c5.z;
-  const float s6 = g.x * c6.x + g.y * c6.y + g.z * c6.z, s7 = g.x * c7.x + g.y * c7.y + g.z * c7.z;
-  const float x00 = dob_mix(s0, s1, t.fx), x10 = dob_mix(s2, s3, t.fx);
-  const float x01 = dob_mix(s4, s5, t.fx), x11 = dob_mix(s6, s7, t.fx);
-  const float dfx = dob_mix(dob_mix(s1 - s0, s3 - s2, t.fy), dob_mix(s5 - s4, s7 - s6, t.fy), t.fz);
-  const float dfy = dob_mix(x10 - x00, x11 - x01, t.fz);
-  const float dfz = dob_mix(x01, x11, t.fy) - dob_mix(x00, x10, t.fy);
-  return v3(dfx, dfy, dfz);
+// (the derivative is linear in the values, so the channels are contracted first)
+__device__ __forceinline__ dob_v3 lerp8x3_dfrac(const Taps& t, const NodeLo& n, const float4* a, dob_v3 g) {
+  return dfrac_core(t, n, [&](uint32_t k) {
+    const float4 c = a[k];
+    return g.x * c.x + g.y * c.y + g.z * c.z;
+  });
 }
 // transpose of lerp8: a[tap k] += g * w_k
 __device__ __forceinline__ void scatter8(float* a, const Taps& t, float g) {
@@ -128,11 +183,11 @@ __device__ __forceinline__ void adj_face(const Grid& g, const float* uk, const f
   const Taps tS = make_taps(g, Sc.x, Sc.y, Sc.z);
   // backward
   scatter8(auk, tS, gout);
-  const dob_v3 gS = (gout * lerp8_dfrac(tS, uk)) * dims * pass3(S, 0.001f, 0.999f);
+  const dob_v3 gS = (gout * lerp8_dfrac(tS, node_lo(g, Sc.x, Sc.y, Sc.z), uk)) * dims * pass3(S, 0.001f, 0.999f);
   const dob_v3 gB = gS * pass3(B, 0.002f, 0.998f);
   const dob_v3 gvMid = -(gB * dtv) / dom;
   scatter8v(acen, tM, gvMid);
-  const dob_v3 gM = lerp8x3_dfrac(tM, cen, gvMid) * dims * pass3(M, 0.002f, 0.998f);
+  const dob_v3 gM = lerp8x3_dfrac(tM, node_lo(g, Mc.x, Mc.y, Mc.z), cen, gvMid) * dims * pass3(M, 0.002f, 0.998f);
   const dob_v3 gv0 = -(0.5f * (gM * dtv)) / dom;
   scatter8v(acen, t0, gv0);
 }
@@ -672,10 +727,10 @@ __global__ void __launch_bounds__(256) k_adj_conc_predict(Grid gc, Grid g, const
   const dob_v3 Bc = clamp3(B, 0.001f, 0.999f);
   const Taps tB = make_taps(gc, Bc.x, Bc.y, Bc.z);
   scatter8(ac, tB, gout);
-  const dob_v3 gB = (gout * lerp8_dfrac(tB, dye)) * dimsc * pass3(B, 0.001f, 0.999f);
+  const dob_v3 gB = (gout * lerp8_dfrac(tB, node_lo(gc, Bc.x, Bc.y, Bc.z), dye)) * dimsc * pass3(B, 0.001f, 0.999f);
   const dob_v3 gvMid = -(gB * dtv) / dom;
   scatter8v(acen, tM, gvMid);
-  const dob_v3 gM = lerp8x3_dfrac(tM, cen, gvMid) * dimsg * pass3(M, 0.001f, 0.999f);
+  const dob_v3 gM = lerp8x3_dfrac(tM, node_lo(g, Mc.x, Mc.y, Mc.z), cen, gvMid) * dimsg * pass3(M, 0.001f, 0.999f);
   const dob_v3 gv0 = -(0.5f * (gM * dtv)) / dom;
   scatter8v(acen, t0, gv0);
 }
@@ -735,7 +790,8 @@ __global__ void __launch_bounds__(256) k_adj_dye_resolve(Grid gc, Grid g, const 
     atomicAdd(ac + i, kap * gout);
     const float gE = -kap * gout;
     scatter8(apred, tF, gE);
-    const dob_v3 gF = (gE * lerp8_dfrac(tF, pred)) * dims * pass3(Fw, 0.001f, 0.999f);
+    const dob_v3 gF = (gE * lerp8_dfrac(tF, node_lo(gc, uvwFwd.x, uvwFwd.y, uvwFwd.z), pred)) * dims *
+                      pass3(Fw, 0.001f, 0.999f);
     const dob_v3 gv0 = (gF * dtv) / dom;
     scatter8v(acen, t0, gv0);
   }

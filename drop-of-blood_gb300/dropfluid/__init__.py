@@ -6,8 +6,9 @@ side: ctypes binding, the engine-style wrapper, the uniform-block packer and
 the seeded benchmark scenes.
 """
 from . import abi  # noqa: F401
+from . import adjoint  # noqa: F401
 from ._lib import DropFluidError, load  # noqa: F401
 from .abi import config_closed_box, config_reference  # noqa: F401
 from .engine import DropFluid, eval_math  # noqa: F401
 
-__all__ = ["abi", "DropFluid", "DropFluidError", "config_closed_box", "config_reference", "eval_math", "load"]
+__all__ = ["abi", "adjoint", "DropFluid", "DropFluidError", "config_closed_box", "config_reference", "eval_math", "load"]

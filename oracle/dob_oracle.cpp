@@ -102,6 +102,8 @@ struct Tap {
 template <class R> struct Taps {
   size_t i[8];
   R fx, fy, fz;
+  size_t lx, ly, lz;  // element offset base -> base - 1 (0 at the lower edge)
+  size_t hx, hy, hz;  // element offset base + 1 -> base + 2 (0 at the upper edge)
 };
 template <class R> inline Taps<R> taps(const Dims& d, R u, R v, R w) {
   Taps<R> t;
@@ -116,6 +118,12 @@ template <class R> inline Taps<R> taps(const Dims& d, R u, R v, R w) {
   t.i[2] = d.at(x0, y1, z0); t.i[3] = d.at(x1, y1, z0);
   t.i[4] = d.at(x0, y0, z1); t.i[5] = d.at(x1, y0, z1);
   t.i[6] = d.at(x0, y1, z1); t.i[7] = d.at(x1, y1, z1);
+  t.lx = x0 > 0 ? 1 : 0;
+  t.ly = y0 > 0 ? (size_t)d.nx : 0;
+  t.lz = z0 > 0 ? (size_t)d.nx * d.ny : 0;
+  t.hx = x0 + 2 <= d.nx - 1 ? 1 : 0;
+  t.hy = y0 + 2 <= d.ny - 1 ? (size_t)d.nx : 0;
+  t.hz = z0 + 2 <= d.nz - 1 ? (size_t)d.nx * d.ny : 0;
   return t;
 }
 template <class R> inline R lerp8(const Taps<R>& t, const R* a) {

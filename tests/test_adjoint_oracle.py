@@ -90,3 +90,44 @@ def test_trajectory_impulse_gradient_matches_central_differences(oracle_mod):
     # the initial pressure does not influence the trajectory's dye in the
     # closed box beyond its warm start; its gradient exists and is finite
     assert np.isfinite(o.gradients()["p"]).all()
+
+
+def test_trajectory_random_directions_match_central_differences(oracle_mod):
+    """A -1.5 cells/step drop with N(0, 0.05) face noise (the benchmark
+    drops), 8 steps: <grad, d> against central differences of the FP64 loss
+    for seeded random directions of the initial MAC velocity."""
+    from dropfluid import scenes
+    sc = scenes.box48()
+    sc.drops[0].n_parcels = 0
+    sc.drops[0].w_cells_per_step = -1.5
+    sc.drops[0].noise_cells_per_step = 0.05
+    o = oracle_mod.OracleSim(sc.config, fp64=True)
+    steps = 8
+
+    def fwd(scale=1.0, pert=None):
+        o.reset()
+        w0 = sc.drops[0].w_cells_per_step
+        sc.drops[0].w_cells_per_step = w0 * scale
+        sc.release(o, 0)
+        sc.drops[0].w_cells_per_step = w0
+        for f, d in (pert or {}).items():
+            o.set_field64(f, o.get_field64(f) + d)
+        o.tape_forward(steps)
+        return o.get_field64(abi.FIELD_CONC)
+
+    target = fwd(1.1)
+    d0 = fwd() - target
+    o.tape_backward((2 * d0).astype(np.float32))
+    g = o.gradients()
+    rng = np.random.default_rng(2)
+    shape = g["u"].shape
+    eps = 1e-6
+    for _ in range(3):
+        d = {f: rng.standard_normal(shape) for f in (abi.FIELD_VEL_U, abi.FIELD_VEL_V, abi.FIELD_VEL_W)}
+        ad = sum(float(np.sum(g[k] * d[f])) for k, f in
+                 (("u", abi.FIELD_VEL_U), ("v", abi.FIELD_VEL_V), ("w", abi.FIELD_VEL_W)))
+        lp = float(np.sum((fwd(pert={f: eps * a for f, a in d.items()}) - target) ** 2))
+        lm = float(np.sum((fwd(pert={f: -eps * a for f, a in d.items()}) - target) ** 2))
+        fd = (lp - lm) / (2 * eps)
+        assert abs(fd - ad) <= 1e-3 * abs(fd), (fd, ad)
+
