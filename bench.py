@@ -374,23 +374,50 @@ def main():
     e2e_s = dist.max(time.perf_counter() - t0)
     e2e_value = world * args.steps / e2e_s
 
-    # ---- mixed precision on the same scene -----------------------------------------------------
+    # ---- projection accuracy per step, and the mixed-precision solve ---------------------------
+    # The timed window is replayed from a snapshot with statistics on, so the
+    # divergence of every timed step is known.  FP32 with a fixed 4 V-cycles
+    # stalls near max |div| dt/dx ~ 1e-5 (the FP32 rounding of a pressure of
+    # ~1e3); the mixed solve iterates each step until max |div| <= 1e-5.
+    eng.close()
     mixed = None
     if not args.no_mixed:
-        eng.close()
-        scm = scenes.box192(abi.DOB_PREC_MIXED)
-        em = DropFluid(scm.config)
-        run_scene_steps(scm, em, 0, args.warmup, timed=False)
-        em.sync()
-        dist.barrier()
-        ms_m = dist.max(run_scene_steps(scm, em, args.warmup, args.steps, timed=True))
-        stm = em.step(1, stats=True)
-        mixed = {"value": world * args.steps / (ms_m / 1000.0), "unit": "steps/s",
-                 "speedup_vs_fp32": (world * args.steps / (ms_m / 1000.0)) / value,
-                 "max_div": stm["max_div"], "outer_iters": stm["outer_iters"],
-                 "rel_residual": stm["residual_l2"] / max(stm["rhs_l2"], 1e-300),
-                 "precision": "FP16 dye, BF16 correction levels, FP64 defect residual, FP32 compute"}
-        em.close()
+        def window(scene, timed_value=None):
+            e = DropFluid(scene.config)
+            run_scene_steps(scene, e, 0, args.warmup, timed=False)
+            e.save_state(0)
+            e.sync()
+            dist.barrier()
+            ms_w = dist.max(run_scene_steps(scene, e, args.warmup, args.steps, timed=True))
+            e.load_state(0)
+            divs, iters = [], []
+            for k in range(args.warmup, args.warmup + args.steps):
+                for d in scene.releases_at(k):
+                    scene.release(e, d)
+                stw = e.step(1, stats=True)
+                divs.append(stw["max_div"])
+                iters.append(stw["outer_iters"])
+            e.close()
+            v = world * args.steps / (ms_w / 1000.0)
+            return {"value": v, "unit": "steps/s", "ms_per_step": ms_w / args.steps,
+                    "max_div_max": max(divs), "max_div_median": statistics.median(divs),
+                    "steps_div_le_1e-5": sum(1 for dv in divs if dv <= 1e-5), "steps": len(divs),
+                    "outer_iters_mean": statistics.mean(iters)}
+        fp32_w = window(scenes.box192())
+        sc8 = scenes.box192()
+        sc8.config.mg_cycles = 8
+        fp32_8 = window(sc8)
+        mx = window(scenes.box192(abi.DOB_PREC_MIXED))
+        m8 = window(scenes.box192_mixed_1e8())
+        mixed = dict(mx)
+        mixed.update({
+            "speedup_vs_fp32": mx["value"] / fp32_w["value"],
+            "speedup_vs_fp32_8cycles": mx["value"] / fp32_8["value"],
+            "precision": "FP16 dye; pressure as an FP32 pair (double-float) corrected by an error-free residual "
+                         "loop, 1 V-cycle per iteration with BF16 levels 2-3; stop at max |div| dt/dx <= 1e-5",
+            "fp32_4cycles": fp32_w, "fp32_8cycles": fp32_8,
+            "mixed_rel_1e-8": m8,
+        })
 
     # ---- discrete adjoint (forward/backward pair) ---------------------------------------------------
     adj = None

@@ -66,8 +66,16 @@ static bool valid_config(const dob_config* c, std::string* why) {
     return no("dims not divisible by 2^mg_levels (every multigrid level needs even dims)");
   if (c->bc_mode != DOB_BC_REFERENCE && c->bc_mode != DOB_BC_CLOSED_BOX) return no("bad bc_mode");
   if (c->precision_mode < 0 || c->precision_mode > 2) return no("bad precision_mode");
-  if (c->mg_pre < 0 || c->mg_post < 0 || c->mg_coarse_sweeps < 0 || c->mg_cycles < 0) return no("negative sweeps");
+  if (c->mg_pre < 0 || c->mg_post < 0 || c->mg_coarse_sweeps < -1 || c->mg_cycles < 0) return no("negative sweeps");
+  if (c->mg_coarse_sweeps == -1) {
+    const uint64_t cc = (uint64_t)(c->nx >> (c->mg_levels - 1)) * (c->ny >> (c->mg_levels - 1)) *
+                        (c->nz >> (c->mg_levels - 1));
+    if (cc > (uint64_t)kDenseCoarseMax)
+      return no("mg_coarse_sweeps = -1 (exact coarsest solve) needs a coarsest grid of at most 1024 cells");
+  }
   if (c->precision_mode == DOB_PREC_MIXED && (c->mg_max_outer < 1 || c->mg_max_outer > 32)) return no("mg_max_outer must be 1..32");
+  if (!(c->mg_rel_tol >= 0.0) || !(c->mg_div_tol >= 0.0) || !isfinite(c->mg_rel_tol) || !isfinite(c->mg_div_tol))
+    return no("mg_rel_tol and mg_div_tol must be finite and >= 0");
   if (c->parcel_capacity < 1 || c->parcel_capacity > (1u << 26)) return no("parcel_capacity out of range");
   if (c->bc_mode == DOB_BC_CLOSED_BOX) {
     if (!(c->dt > 0.0f) || !isfinite(c->dt)) return no("dt must be finite and > 0");
@@ -331,7 +339,7 @@ dob_status dob_config_reference(dob_config* c) {
   c->bc_mode = DOB_BC_REFERENCE;
   c->precision_mode = DOB_PREC_FP32;
   c->mg_levels = 4; c->mg_pre = 2; c->mg_post = 2; c->mg_coarse_sweeps = 6; c->mg_cycles = 1;
-  c->mg_max_outer = 1; c->mg_rel_tol = 0.0;
+  c->mg_max_outer = 1; c->mg_rel_tol = 0.0; c->mg_div_tol = 0.0;
   c->physics_flags = DOB_PHYS_REFERENCE_ALL;
   c->parcel_capacity = 393216;
   c->reference_schedule = 1;
@@ -351,8 +359,19 @@ dob_status dob_config_closed_box(dob_config* c, uint32_t nx, uint32_t ny, uint32
   c->domain_max[0] = (float)nx; c->domain_max[1] = (float)ny; c->domain_max[2] = (float)nz;
   c->bc_mode = DOB_BC_CLOSED_BOX;
   c->precision_mode = DOB_PREC_FP32;
-  c->mg_levels = 4; c->mg_pre = 2; c->mg_post = 2; c->mg_coarse_sweeps = 6; c->mg_cycles = 4;
-  c->mg_max_outer = 8; c->mg_rel_tol = 1e-8;
+  // the hierarchy is deepened until the coarsest grid has at most 512 cells,
+  // which are solved exactly (dense inverse); 2+2 sweeps elsewhere
+  int levels = 1, coarse = 6;
+  for (int L = 2; L <= kMaxLevels; ++L) {
+    const uint32_t m = 1u << L;
+    if (nx % m || ny % m || nz % m) break;
+    const uint64_t cells = (uint64_t)(nx >> (L - 1)) * (ny >> (L - 1)) * (nz >> (L - 1));
+    levels = L;
+    coarse = cells <= (uint64_t)kDenseCoarseMax ? -1 : 6;
+    if (cells <= 512) break;
+  }
+  c->mg_levels = levels; c->mg_pre = 2; c->mg_post = 2; c->mg_coarse_sweeps = coarse; c->mg_cycles = 4;
+  c->mg_max_outer = 16; c->mg_rel_tol = 0.0; c->mg_div_tol = 1e-5;
   c->casson_tau_y = 0.005f; c->casson_mu_p = 1e-3f;
   c->physics_flags = 0;
   c->parcel_capacity = 8192;
@@ -412,15 +431,26 @@ dob_status dob_create(const dob_config* cfg, dob_ctx** out) {
     const float sc = (float)s.g.nx / (float)L.d.nx;
     L.h2 = sc * sc;
     if (l == 0) { L.e = s.p; L.b = s.rhs; continue; }
-    if (s.prec == DOB_PREC_MIXED) {
+    if (s.prec == DOB_PREC_MIXED && l >= kMixedBF16Level) {
       A((void**)&L.eh, L.d.n() * 2); A((void**)&L.bh, L.d.n() * 2);
     } else {
       A((void**)&L.e, L.d.n() * 4); A((void**)&L.b, L.d.n() * 4);
     }
   }
   if (s.prec == DOB_PREC_MIXED) {
-    A((void**)&s.e0h, N * 2); A((void**)&s.r0h, N * 2);
-    s.lv[0].eh = s.e0h; s.lv[0].bh = s.r0h;
+    A((void**)&s.plo, N * 4); A((void**)&s.e0, N * 4); A((void**)&s.r0, N * 4);
+  }
+  if (cfg->mg_coarse_sweeps < 0 && st == DOB_OK) {
+    const MgLevel& C = s.lv[s.nlev - 1];
+    const std::vector<float> inv = coarse_inverse(C.d, C.h2, s.ref);
+    float* d = nullptr;
+    A((void**)&d, inv.size() * sizeof(float));
+    if (st == DOB_OK) {
+      cudaError_t ce = cudaMemcpy(d, inv.data(), inv.size() * sizeof(float), cudaMemcpyHostToDevice);
+      if (ce != cudaSuccess) st = fail(ctx, DOB_ECUDA, "coarse inverse upload", cudaGetErrorString(ce));
+    }
+    s.cinv = d;
+    s.cn = (int)C.d.n();
   }
   s.pre0 = cfg->reference_schedule ? 1 : cfg->mg_pre;
   s.post0 = cfg->reference_schedule ? 1 : cfg->mg_post;
@@ -429,6 +459,9 @@ dob_status dob_create(const dob_config* cfg, dob_ctx** out) {
   s.cycles = cfg->mg_cycles;
   s.max_outer = cfg->mg_max_outer;
   s.rel_tol = cfg->mg_rel_tol;
+  // max |b - A p| target: the projected divergence is b - A p, reported as
+  // max |div| dt/dx in the closed box and unscaled in reference mode
+  s.div_tol_r = (float)(s.ref ? cfg->mg_div_tol : cfg->mg_div_tol * cfg->dx / cfg->dt);
   if (st != DOB_OK) {
     *out = nullptr;
     std::string keep = ctx->err;
@@ -497,8 +530,8 @@ dob_status dob_reset(dob_ctx* ctx) {
     if (s.lv[l].eh) CK(cudaMemsetAsync(s.lv[l].eh, 0, n * 2, ctx->stream));
     if (s.lv[l].bh) CK(cudaMemsetAsync(s.lv[l].bh, 0, n * 2, ctx->stream));
   }
-  if (s.e0h) CK(cudaMemsetAsync(s.e0h, 0, N * 2, ctx->stream));
-  if (s.r0h) CK(cudaMemsetAsync(s.r0h, 0, N * 2, ctx->stream));
+  for (float* a : {s.plo, s.e0, s.r0})
+    if (a) CK(cudaMemsetAsync(a, 0, N * 4, ctx->stream));
   CK(cudaMemsetAsync(s.conc, 0, Nc * nch * dsb, ctx->stream));
   CK(cudaMemsetAsync(s.conc2, 0, Nc * nch * dsb, ctx->stream));
   CK(cudaMemsetAsync(s.pred, 0, Nc * dsb, ctx->stream));
@@ -562,6 +595,12 @@ dob_status dob_set_high_water(dob_ctx* ctx, uint32_t hw) {
 }
 
 // ---- field I/O -----------------------------------------------------------------------
+__global__ void k_add_arrays(const float* __restrict__ a, const float* __restrict__ b, float* __restrict__ out,
+                             size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = a[i] + b[i];
+}
+
 namespace {
 struct FieldDesc {
   void* dev;
@@ -609,7 +648,9 @@ dob_status dob_set_field(dob_ctx* ctx, int field, const void* host, size_t bytes
     cudaError_t e = cudaMemcpy(tmp, host, bytes, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) {
       launch_split(tmp, (float*)f.dev, ctx->s.g, true, ctx->stream);
-      e = cudaStreamSynchronize(ctx->stream);
+      // a pressure set from FP32 data has no low part
+      if (field == DOB_FIELD_PRESSURE && ctx->s.plo) e = cudaMemsetAsync(ctx->s.plo, 0, bytes, ctx->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     }
     cudaFree(tmp);
     if (e != cudaSuccess) return fail(ctx, DOB_ECUDA, "dob_set_field", cudaGetErrorString(e));
@@ -646,8 +687,21 @@ dob_status dob_get_field(dob_ctx* ctx, int field, void* host, size_t bytes) {
   if (f.kind == 4) {
     float* tmp = nullptr;
     CK(cudaMalloc(&tmp, bytes));
-    launch_split((const float*)f.dev, tmp, ctx->s.g, false, ctx->stream);
-    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    cudaError_t e = cudaSuccess;
+    if (field == DOB_FIELD_PRESSURE && ctx->s.plo) {
+      // double-float pressure: read p + plo rounded to FP32
+      float* sum = nullptr;
+      e = cudaMalloc(&sum, bytes);
+      if (e == cudaSuccess) {
+        k_add_arrays<<<ctx->s.num_sms * 4, 256, 0, ctx->stream>>>(ctx->s.p, ctx->s.plo, sum, f.count);
+        launch_split(sum, tmp, ctx->s.g, false, ctx->stream);
+        e = cudaStreamSynchronize(ctx->stream);
+        cudaFree(sum);
+      }
+    } else {
+      launch_split((const float*)f.dev, tmp, ctx->s.g, false, ctx->stream);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e == cudaSuccess) e = cudaMemcpy(host, tmp, bytes, cudaMemcpyDeviceToHost);
     cudaFree(tmp);
     if (e != cudaSuccess) return fail(ctx, DOB_ECUDA, "dob_get_field", cudaGetErrorString(e));
@@ -781,9 +835,9 @@ dob_status dob_save_state(dob_ctx* ctx, int slot) {
   const size_t N = s.g.n(), Nc = s.gc.n();
   const size_t vsb = vs_bytes(s.prec), dsb = ds_bytes(s.prec);
   const int nch = s.ref ? 4 : 1;
-  void* src[] = {s.u, s.v, s.w, s.cen, s.curl, s.p, s.conc, s.parcels};
+  void* src[] = {s.u, s.v, s.w, s.cen, s.curl, s.p, s.conc, s.parcels, s.plo};
   const size_t sz[] = {N * vsb, N * vsb, N * vsb, N * 4 * vsb, s.curl ? N * 4 * vsb : 0, N * 4, Nc * nch * dsb,
-                       (size_t)s.cap * 32};
+                       (size_t)s.cap * 32, s.plo ? N * 4 : 0};
   Snapshot& sn = ctx->snaps[slot];
   if (!sn.valid) {
     for (size_t k = 0; k < sizeof(sz) / sizeof(sz[0]); ++k) {
@@ -813,7 +867,7 @@ dob_status dob_load_state(dob_ctx* ctx, int slot) {
   Snapshot& sn = ctx->snaps[slot];
   if (!sn.valid) return fail(ctx, DOB_ESTATE, "dob_load_state", "empty snapshot slot");
   DevState& s = ctx->s;
-  void* dst[] = {s.u, s.v, s.w, s.cen, s.curl, s.p, s.conc, s.parcels};
+  void* dst[] = {s.u, s.v, s.w, s.cen, s.curl, s.p, s.conc, s.parcels, s.plo};
   for (size_t k = 0; k < sn.bufs.size(); ++k)
     if (sn.sizes[k]) CK(cudaMemcpyAsync(dst[k], sn.bufs[k], sn.sizes[k], cudaMemcpyDeviceToDevice, ctx->stream));
   ctx->high_water = sn.high_water;

@@ -4,6 +4,8 @@
 
 #include <cuda_runtime.h>
 
+#include <vector>
+
 #include "../../include/dropfluid.h"
 #include "dob_device.cuh"
 
@@ -52,11 +54,20 @@ struct DevState {
   int nlev;
   MgLevel lv[kMaxLevels];
   int pre0, post0, pre, post, coarse_sweeps, cycles;
-  // mixed-precision defect correction
-  __nv_bfloat16 *e0h, *r0h;      // level-0 correction and residual (BF16, split layout)
+  // exact coarsest-grid solve (coarse_sweeps < 0): the symmetric (pseudo-)
+  // inverse of the coarsest operator, n x n FP32, natural cell order
+  const float* cinv;
+  int cn;
+  // mixed-precision defect correction: the pressure is the unevaluated sum
+  // p + plo of two FP32 arrays (double-float); the correction solve runs on
+  // e0 / r0 (FP32, split layout) with BF16 storage from level kMixedBF16Level
+  float* plo;
+  float *e0, *r0;
   int max_outer;
-  double rel_tol;
+  double rel_tol;   // stop when ||b - A p|| <= rel_tol ||b|| (0: off)
+  float div_tol_r;  // stop when max |b - A p| <= div_tol_r (0: off)
 };
+constexpr int kMixedBF16Level = 2;
 
 // Adjoint (transpose-Jacobian) arrays of the closed-box FP32 step, all FP32.
 // Pressure / right-hand side / multigrid adjoints are red-black split like
@@ -87,7 +98,8 @@ enum {
   REDU_ALIVE = 1,
   REDU_DONE = 2,          // defect loop converged (kernels of later iterations exit)
   REDU_ITERS = 3,         // defect iterations executed
-  REDU_COUNT = 8
+  REDU_DEFECT_MAX = 8,    // base of per-outer-iteration max |r| (float bits)
+  REDU_COUNT = 8 + 32
 };
 
 // ---- block reductions ---------------------------------------------------------------
@@ -150,6 +162,14 @@ void launch_project(const DevState& s, cudaStream_t st);
 void launch_divergence(const DevState& s, float* out, float scale, unsigned int* maxbits, cudaStream_t st);
 void launch_conc_predict(const DevState& s, cudaStream_t st);
 void launch_conc_resolve(const DevState& s, cudaStream_t st);
+
+// Largest coarsest grid solved exactly by the dense inverse.
+constexpr int kDenseCoarseMax = 1024;
+// Symmetric (pseudo-)inverse of the coarsest-grid operator
+// A e = (sum of neighbours - diag e) / h2 (pure Neumann: the minimum-norm
+// inverse on zero-mean data; Dirichlet top: the inverse), n x n FP32 in
+// natural cell order.  Host code, double precision Gauss-Jordan.
+std::vector<float> coarse_inverse(const Grid& c, float h2, int ref);
 
 // ---- launchers (k_mg.cu) ---------------------------------------------------------------
 // Raise the dynamic shared-memory limit of the coarse-grid kernel (once per process).

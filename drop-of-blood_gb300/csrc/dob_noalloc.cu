@@ -16,7 +16,7 @@
 // Limits and sharing rules:
 //   * at most kNoAllocMaxCells = 2^21 cells (e.g. the reference's 96x128x96
 //     grid, or 128^3); larger grids are rejected with DOB_EINVAL;
-//   * the array (about 20 MiB) is part of the library's device image: every
+//   * the array (about 24 MiB) is part of the library's device image: every
 //     GPU that loads the library holds it until the process exits;
 //   * every call, from any thread and on any stream, works in the same array
 //     and leaves the last call's contents there.  Two calls whose work overlaps
@@ -32,6 +32,7 @@
 #include <string.h>
 
 #include <mutex>
+#include <vector>
 
 #include "dob_kernels.cuh"
 
@@ -52,7 +53,10 @@ constexpr size_t kSlotBytes = 1024;  // FP64 + u32 reduction slots at the front
 // right-hand side of every coarser grid, each rounded up to 256 bytes.  The
 // coarser grids hold fewer than n/7 cells together, so 10 bytes per cell
 // bounds the whole layout for every accepted grid.
-constexpr size_t kScratchBytes = kSlotBytes + 10 * kNoAllocMaxCells;
+// The dense inverse of an exactly solved coarsest grid (up to
+// kDenseCoarseMax cells) follows the multigrid arrays.
+constexpr size_t kDenseBytes = (size_t)kDenseCoarseMax * kDenseCoarseMax * sizeof(float);
+constexpr size_t kScratchBytes = kSlotBytes + 10 * kNoAllocMaxCells + kDenseBytes;
 
 static_assert(RED_COUNT * sizeof(double) <= 512, "reduction slots exceed their area");
 static_assert(REDU_COUNT * sizeof(unsigned int) <= kSlotBytes - 512, "flag slots exceed their area");
@@ -65,6 +69,8 @@ constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
 void* g_scratch_ptr[kMaxDevices] = {};
 int g_num_sms[kMaxDevices] = {};
+// which coarsest-grid inverse each device's array holds (nx, ny, nz, ref)
+int g_inv_key[kMaxDevices][4] = {};
 
 size_t round_up(size_t b) { return (b + kAlign - 1) / kAlign * kAlign; }
 
@@ -124,8 +130,12 @@ extern "C" dob_status dob_pressure_solve_noalloc(const dob_config* cfg, const fl
     return bad("the mixed-precision solve is not available without allocation; use DOB_PREC_FP32");
   if (cfg->precision_mode != DOB_PREC_FP32 && cfg->precision_mode != DOB_PREC_REFERENCE_FP16)
     return bad("bad precision_mode");
-  if (cfg->mg_pre < 0 || cfg->mg_post < 0 || cfg->mg_coarse_sweeps < 0 || cfg->mg_cycles < 0)
+  if (cfg->mg_pre < 0 || cfg->mg_post < 0 || cfg->mg_coarse_sweeps < -1 || cfg->mg_cycles < 0)
     return bad("negative sweeps");
+  const int cl = cfg->mg_levels - 1;
+  if (cfg->mg_coarse_sweeps == -1 &&
+      (uint64_t)(nx >> cl) * (ny >> cl) * (nz >> cl) > (uint64_t)kDenseCoarseMax)
+    return bad("mg_coarse_sweeps = -1 (exact coarsest solve) needs a coarsest grid of at most 1024 cells");
 
   int device = 0;
   cudaError_t e = cudaGetDevice(&device);
@@ -175,7 +185,30 @@ extern "C" dob_status dob_pressure_solve_noalloc(const dob_config* cfg, const fl
     L.e = take(L.d.n());
     L.b = take(L.d.n());
   }
-  if (used > kScratchBytes) return bad("internal: scratch layout exceeds the array");
+  if (cfg->mg_coarse_sweeps < 0) {
+    // the coarsest grid's inverse sits at the end of the array; it is
+    // recomputed on the host only when the grid differs from the last call's
+    const MgLevel& C = s.lv[s.nlev - 1];
+    float* inv = reinterpret_cast<float*>(cur + kScratchBytes - kDenseBytes);
+    const int key[4] = {C.d.nx, C.d.ny, C.d.nz, s.ref};
+    bool same = true;
+    {
+      std::lock_guard<std::mutex> lock(g_setup_mutex);
+      for (int k = 0; k < 4; ++k) same = same && g_inv_key[device][k] == key[k];
+    }
+    if (!same) {
+      const std::vector<float> h = coarse_inverse(C.d, C.h2, s.ref);
+      e = cudaMemcpyAsync(inv, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice,
+                          static_cast<cudaStream_t>(stream));
+      if (e == cudaSuccess) e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
+      if (e != cudaSuccess) return cuda_fail("coarse inverse upload", e);
+      std::lock_guard<std::mutex> lock(g_setup_mutex);
+      for (int k = 0; k < 4; ++k) g_inv_key[device][k] = key[k];
+    }
+    s.cinv = inv;
+    s.cn = (int)C.d.n();
+  }
+  if (used > kScratchBytes - kDenseBytes) return bad("internal: scratch layout exceeds the array");
   s.pre0 = cfg->reference_schedule ? 1 : cfg->mg_pre;
   s.post0 = cfg->reference_schedule ? 1 : cfg->mg_post;
   s.pre = cfg->mg_pre;

@@ -861,8 +861,28 @@ static void adj_cluster(const MgLevel& L, int ref, int sweeps, float* eb, float*
   const size_t smem = 2 * (L.d.n() / CS) * sizeof(float);
   k_adj_coarse_cluster<CS><<<CS, 512, smem, st>>>(L.d, L.h2, ref, sweeps, eb, bb);
 }
+// Transpose of the exact coarsest solve e = M b (M symmetric):
+// Bbar += M Ebar, Ebar = 0.
+__global__ void __launch_bounds__(1024) k_adj_coarse_dense(Grid d, const float* __restrict__ M, int n,
+                                                           float* __restrict__ eb, float* __restrict__ bb) {
+  extern __shared__ float sev[];
+  const int j = threadIdx.x;
+  const int x = j % d.nx, y = (j / d.nx) % d.ny, z = j / (d.nx * d.ny);
+  const size_t rj = rb_index(d, x, y, z);
+  sev[j] = eb[rj];
+  __syncthreads();
+  eb[rj] = 0.0f;
+  float acc = 0.0f;
+  for (int i = 0; i < n; ++i) acc = fmaf(M[(size_t)i * n + j], sev[i], acc);
+  bb[rj] += acc;
+}
 // Transpose of the coarsest-grid solve; Ebar is zero on return.
-static void adj_coarse(const MgLevel& L, int ref, int sweeps, float* eb, float* bb, cudaStream_t st) {
+static void adj_coarse(const DevState& s, const MgLevel& L, int ref, int sweeps, float* eb, float* bb,
+                       cudaStream_t st) {
+  if (s.coarse_sweeps < 0) {
+    k_adj_coarse_dense<<<1, s.cn, s.cn * sizeof(float), st>>>(L.d, s.cinv, s.cn, eb, bb);
+    return;
+  }
   int cs = 0;
   for (int c : {8, 4, 2, 1})
     if (L.d.nz % c == 0 && 2 * (L.d.n() / c) * sizeof(float) <= 200 * 1024) { cs = c; break; }
@@ -924,7 +944,7 @@ static void adj_vcycle(const DevState& s, const AdjState& a, cudaStream_t st) {
     adj_prolong(s, a, l, a.le[l], st);
   }
   const MgLevel& LC = s.lv[L - 1];
-  adj_coarse(LC, s.ref, s.coarse_sweeps, a.le[L - 1], a.lb[L - 1], st);
+  adj_coarse(s, LC, s.ref, s.coarse_sweeps, a.le[L - 1], a.lb[L - 1], st);
   for (int l = L - 2; l >= 1; --l) {
     adj_restrict(s, a, l, a.le[l], a.lb[l], st);
     adj_smooth(s.lv[l].d, s.lv[l].h2, s.ref, s.pre, a.le[l], a.lb[l], st);

@@ -406,16 +406,22 @@ __global__ void __launch_bounds__(256) k_mac_rhs(Grid g, const StepParams* __res
 // ---- FLUID_MAC_PROJECT (fluid.ts:863-911), in place ----------------------------------------
 template <class VS>
 __global__ void __launch_bounds__(256) k_project(Grid g, const StepParams* __restrict__ Pp, int ref, VS* u, VS* v, VS* w,
-                                                 const float* __restrict__ p, const float4* __restrict__ wave) {
+                                                 const float* __restrict__ p, const float* __restrict__ plo,
+                                                 const float4* __restrict__ wave) {
   CELL_INDEX
   float mx = ldv(u + i), my = ldv(v + i), mz = ldv(w + i);
-  // p is red-black split: the +x, +y, +z neighbours are in the other half
-  const float pC = __ldg(p + rb_index(g, x, y, z));
-  if (x < g.nx - 1) mx = mx - (__ldg(p + rb_index(g, x + 1, y, z)) - pC); else mx = 0.0f;
-  if (y < g.ny - 1) my = my - (__ldg(p + rb_index(g, x, y + 1, z)) - pC);
+  // p is red-black split: the +x, +y, +z neighbours are in the other half.
+  // With a double-float pressure (p + plo) the differences of the high parts
+  // are taken first, then the low parts added.
+  const size_t ic = rb_index(g, x, y, z);
+  const float pC = __ldg(p + ic);
+  const float lC = plo ? __ldg(plo + ic) : 0.0f;
+  auto dp = [&](size_t j) { return plo ? (__ldg(p + j) - pC) + (__ldg(plo + j) - lC) : (__ldg(p + j) - pC); };
+  if (x < g.nx - 1) mx = mx - dp(rb_index(g, x + 1, y, z)); else mx = 0.0f;
+  if (y < g.ny - 1) my = my - dp(rb_index(g, x, y + 1, z));
   else if (ref) my = my - (top_pressure(g, *Pp, wave, x, z) - pC);
   else my = 0.0f;
-  if (z < g.nz - 1) mz = mz - (__ldg(p + rb_index(g, x, y, z + 1)) - pC); else mz = 0.0f;
+  if (z < g.nz - 1) mz = mz - dp(rb_index(g, x, y, z + 1)); else mz = 0.0f;
   if (ref) {
     mx = dob_clampf(mx, -2.0f, 2.0f); my = dob_clampf(my, -2.0f, 2.0f); mz = dob_clampf(mz, -2.0f, 2.0f);
   }
@@ -720,7 +726,7 @@ void launch_mac_rhs(const DevState& s, cudaStream_t st) {
 void launch_project(const DevState& s, cudaStream_t st) {
   DOB_VEL_DISPATCH(s.prec, {
     k_project<VS><<<cell_grid(s.g), cell_block(), 0, st>>>(s.g, s.params, s.ref, (VS*)s.u, (VS*)s.v, (VS*)s.w, s.p,
-                                                           s.wave);
+                                                           s.plo, s.wave);
   });
 }
 

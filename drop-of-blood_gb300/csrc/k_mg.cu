@@ -25,9 +25,15 @@
 //                       shared memory, reads the neighbour slabs' boundary
 //                       planes through distributed shared memory, and the
 //                       half-sweeps are separated by hardware cluster barriers
-//   k_defect            FP64 residual of the FP32 pressure -> BF16, with its norm
+//   k_defect            FP64 norm of the residual of the FP32 pressure (statistics)
+//   k_defect_df         mixed precision: residual of the double-float pressure
+//                       (FP32 pairs, error-free transformations), its max and norm
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
+
+#include <cmath>
+#include <utility>
+#include <vector>
 
 #include "dob_kernels.cuh"
 
@@ -382,6 +388,26 @@ __global__ void __launch_bounds__(256) k_prolong_add2(Grid f, Grid c, int ref, T
     }
 }
 
+// Exact coarsest-grid solve e = M b with the dense symmetric inverse M
+// (n <= 1024 cells, one CTA of n threads): b is gathered into shared memory
+// in natural order, thread j forms row j (M is symmetric: column j, read
+// with consecutive threads on consecutive words).
+template <class T>
+__global__ void __launch_bounds__(1024) k_coarse_dense(Grid d, const float* __restrict__ M, int n,
+                                                       T* __restrict__ e, const T* __restrict__ b,
+                                                       const unsigned int* __restrict__ skip) {
+  if (skip_now(skip)) return;
+  extern __shared__ float sbv[];
+  const int j = threadIdx.x;
+  const int x = j % d.nx, y = (j / d.nx) % d.ny, z = j / (d.nx * d.ny);
+  const size_t rj = rb_index(d, x, y, z);
+  sbv[j] = ldv(b + rj);
+  __syncthreads();
+  float acc = 0.0f;
+  for (int i = 0; i < n; ++i) acc = fmaf(M[(size_t)i * n + j], sbv[i], acc);
+  stf(e + rj, acc);
+}
+
 template <class T>
 __global__ void k_fill_zero(T* __restrict__ a, size_t n, const unsigned int* __restrict__ skip) {
   if (skip_now(skip)) return;
@@ -531,22 +557,145 @@ __global__ void __launch_bounds__(256) k_defect(Grid d, float h2f, int ref, cons
   if (norm2) block_sum_atomic(rr, norm2);
 }
 
-// Converged when ||r|| <= tol ||b||: sets the skip flag every later kernel of
+// ---- mixed precision: double-float pressure --------------------------------------------
+// The pressure is p + plo (two FP32 arrays, |plo| <= ulp(p)/2), updated with
+// error-free transformations, so the residual b - A p can fall far below the
+// FP32 rounding of p itself (~1e-5 relative for this problem) with FP32
+// arithmetic only.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bp = s - a;
+  e = (a - (s - bp)) + (b - bp);
+}
+__device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e) {  // |a| >= |b|
+  s = a + b;
+  e = b - (s - a);
+}
+// r = b - A (p + plo) at level 0 (h2 = 1): the neighbour sum of p and
+// diag * p are formed exactly as double-float, so the cancellation against b
+// loses nothing; r is stored FP32 (split layout, the correction solve's
+// right-hand side), max |r| and ||r||^2 are reduced.
+__global__ void __launch_bounds__(256) k_defect_df(Grid d, int ref, const float* __restrict__ p,
+                                                   const float* __restrict__ plo, const float* __restrict__ b,
+                                                   float* __restrict__ r_out, double* __restrict__ norm2,
+                                                   unsigned int* __restrict__ maxbits,
+                                                   const unsigned int* __restrict__ skip) {
+  if (skip_now(skip)) return;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  double rr = 0.0;
+  float ra = 0.0f;
+  if (x < d.nx && y < d.ny) {
+    float sh = 0.0f, sl = 0.0f, low = 0.0f, diag = ref ? 1.0f : 0.0f;
+    auto add = [&](int xx, int yy, int zz) {
+      const size_t j = rb_index(d, xx, yy, zz);
+      float e;
+      two_sum(sh, p[j], sh, e);
+      sl += e;
+      low += plo[j];
+      diag += 1.0f;
+    };
+    if (x > 0) add(x - 1, y, z);
+    if (x < d.nx - 1) add(x + 1, y, z);
+    if (y > 0) add(x, y - 1, z);
+    if (y < d.ny - 1) {
+      const size_t j = rb_index(d, x, y + 1, z);
+      float e;
+      two_sum(sh, p[j], sh, e);
+      sl += e;
+      low += plo[j];
+      if (!ref) diag += 1.0f;
+    }
+    if (z > 0) add(x, y, z - 1);
+    if (z < d.nz - 1) add(x, y, z + 1);
+    const size_t i = rb_index(d, x, y, z);
+    const float pc = p[i];
+    const float prod = diag * pc;
+    const float perr = fmaf(diag, pc, -prod);  // diag * pc = prod + perr exactly
+    float th, te;
+    two_sum(sh, -prod, th, te);                // A p = th + (te + sl - perr + low - diag plo)
+    const float tl = ((te + sl) - perr) + (low - diag * plo[i]);
+    const float r = (b[i] - th) - tl;
+    if (r_out) r_out[i] = r;
+    rr = (double)r * (double)r;
+    ra = fabsf(r);
+  }
+  if (norm2) block_sum_atomic(rr, norm2);
+  if (maxbits) block_max_atomic(ra, maxbits);
+}
+
+// Converged when max |r| <= div_tol_r and ||r|| <= rel_tol ||b|| (a zero
+// tolerance switches its test off): sets the skip flag every later kernel of
 // the defect loop reads, and counts executed iterations.
-__global__ void k_defect_check(const double* __restrict__ rnorm2, const double* __restrict__ bnorm2, double tol,
+__global__ void k_defect_check(const unsigned int* __restrict__ maxbits, const double* __restrict__ rnorm2,
+                               const double* __restrict__ bnorm2, float div_tol_r, double rel_tol,
                                unsigned int* __restrict__ done, unsigned int* __restrict__ iters) {
   if (*done) return;
+  const bool div_ok = div_tol_r <= 0.0f || __uint_as_float(*maxbits) <= div_tol_r;
   const double rn = sqrt(*rnorm2), bn = sqrt(*bnorm2);
-  if (bn == 0.0 || rn <= tol * bn) *done = 1u;
+  const bool rel_ok = rel_tol <= 0.0 || bn == 0.0 || rn <= rel_tol * bn;
+  if (div_ok && rel_ok) *done = 1u;
   else *iters += 1u;
 }
 
-// p += e (FP32 pressure, BF16 correction; same layout)
-__global__ void k_add_correction(float* __restrict__ p, const __nv_bfloat16* __restrict__ e, size_t n,
-                                 const unsigned int* __restrict__ skip) {
+// (p, plo) += e, error-free (same split layout)
+__global__ void k_add_df(float* __restrict__ p, float* __restrict__ plo, const float* __restrict__ e, size_t n,
+                         const unsigned int* __restrict__ skip) {
   if (skip_now(skip)) return;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    p[i] = p[i] + __bfloat162float(e[i]);
+  const size_t n4 = n >> 2;
+  float4* p4 = reinterpret_cast<float4*>(p);
+  float4* l4 = reinterpret_cast<float4*>(plo);
+  const float4* e4 = reinterpret_cast<const float4*>(e);
+  auto upd = [](float& hi, float& lo, float ev) {
+    float s, err;
+    two_sum(hi, ev, s, err);
+    fast_two_sum(s, err + lo, hi, lo);
+  };
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n4; i += (size_t)gridDim.x * blockDim.x) {
+    float4 h = p4[i], l = l4[i];
+    const float4 ev = e4[i];
+    upd(h.x, l.x, ev.x); upd(h.y, l.y, ev.y); upd(h.z, l.z, ev.z); upd(h.w, l.w, ev.w);
+    p4[i] = h;
+    l4[i] = l;
+  }
+  for (size_t i = 4 * n4 + blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    float h = p[i], l = plo[i];
+    upd(h, l, e[i]);
+    p[i] = h;
+    plo[i] = l;
+  }
+}
+// sum of p + plo (per-thread double-float, FP64 across threads)
+__global__ void k_sum_df(const float* __restrict__ p, const float* __restrict__ plo, size_t n,
+                         double* __restrict__ out) {
+  float hi = 0.0f, lo = 0.0f;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    float e;
+    two_sum(hi, p[i], hi, e);
+    lo += e + plo[i];
+  }
+  block_sum_atomic((double)hi + (double)lo, out);
+}
+// (p, plo) -= mean, with the mean as a double-float pair
+__global__ void k_sub_mean_df(float* __restrict__ p, float* __restrict__ plo, size_t n,
+                              const double* __restrict__ sum) {
+  __shared__ float s_mh, s_ml;
+  if (threadIdx.x == 0) {
+    const double m = *sum / (double)n;
+    s_mh = (float)m;
+    s_ml = (float)(m - (double)s_mh);
+  }
+  __syncthreads();
+  const float mh = s_mh, ml = s_ml;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    float s, err;
+    two_sum(p[i], -mh, s, err);
+    float h, l;
+    fast_two_sum(s, (err + plo[i]) - ml, h, l);
+    p[i] = h;
+    plo[i] = l;
+  }
 }
 
 // Natural <-> red-black split layout (host field I/O).
@@ -590,12 +739,12 @@ static inline dim3 pair_grid(const Grid& c, const dim3& b) {
   const int q = c.nx / 2;
   return dim3((q + b.x - 1) / b.x, (c.ny + b.y - 1) / b.y, c.nz);
 }
-template <class T>
-static void restrict_level(const DevState& s, int l, const T* x, const T* b, T* bc, const unsigned int* skip,
+template <class T, class TC = T>
+static void restrict_level(const DevState& s, int l, const T* x, const T* b, TC* bc, const unsigned int* skip,
                            cudaStream_t st) {
   const Grid f = s.lv[l].d, c = s.lv[l + 1].d;  // nx % 4 == 0 on every transfer level
   const dim3 bp = pair_block(c);
-  k_residual_restrict2<T, T><<<pair_grid(c, bp), bp, 0, st>>>(f, c, 1.0f / s.lv[l].h2, s.ref, x, b, bc, skip);
+  k_residual_restrict2<T, TC><<<pair_grid(c, bp), bp, 0, st>>>(f, c, 1.0f / s.lv[l].h2, s.ref, x, b, bc, skip);
 }
 static inline dim3 quad_grid(const Grid& d, const dim3& b) {
   const int q = d.nx / 8;
@@ -637,15 +786,15 @@ void launch_sumsq(const float* a, size_t n, double* out, int num_sms, cudaStream
 
 // `sweeps` red-black sweeps on level l, in place.  zero_first: the input is
 // zero (fill it); ec: coarse correction to add first.
-template <class T>
-static void smooth(const DevState& s, int l, T* a, const T* b, int sweeps, bool zero_first, const T* ec,
+template <class T, class TC = T>
+static void smooth(const DevState& s, int l, T* a, const T* b, int sweeps, bool zero_first, const TC* ec,
                    const unsigned int* skip, cudaStream_t st) {
   const MgLevel& L = s.lv[l];
   if (zero_first) k_fill_zero<T><<<s.num_sms * 2, 256, 0, st>>>(a, L.d.n(), skip);
   if (ec) {
     const Grid dc = s.lv[l + 1].d;
     const dim3 bp = pair_block(dc);  // every transfer level has nx % 4 == 0
-    k_prolong_add2<T, T><<<pair_grid(dc, bp), bp, 0, st>>>(L.d, dc, s.ref, a, ec, skip);
+    k_prolong_add2<T, TC><<<pair_grid(dc, bp), bp, 0, st>>>(L.d, dc, s.ref, a, ec, skip);
   }
   const bool v4 = (L.d.nx % 8) == 0;
   const dim3 bq = quad_block(L.d), gq = quad_grid(L.d, bq);
@@ -667,6 +816,10 @@ static void launch_cluster(const MgLevel& L, int ref, int sweeps, T* e, const T*
 template <class T>
 static void coarse_solve(const DevState& s, int l, T* e, const T* b, const unsigned int* skip, cudaStream_t st) {
   const MgLevel& L = s.lv[l];
+  if (s.coarse_sweeps < 0) {  // exact: e = M b with the precomputed inverse
+    k_coarse_dense<T><<<1, s.cn, s.cn * sizeof(float), st>>>(L.d, s.cinv, s.cn, e, b, skip);
+    return;
+  }
   int cs = 0;
   for (int c : {8, 4, 2, 1})
     if (L.d.nz % c == 0 && 2 * (L.d.n() / c) * sizeof(float) <= 200 * 1024) { cs = c; break; }
@@ -675,7 +828,7 @@ static void coarse_solve(const DevState& s, int l, T* e, const T* b, const unsig
     case 4: launch_cluster<T, 4>(L, s.ref, s.coarse_sweeps, e, b, skip, st); break;
     case 2: launch_cluster<T, 2>(L, s.ref, s.coarse_sweeps, e, b, skip, st); break;
     case 1: launch_cluster<T, 1>(L, s.ref, s.coarse_sweeps, e, b, skip, st); break;
-    default: smooth<T>(s, l, e, b, s.coarse_sweeps, true, nullptr, skip, st); break;
+    default: smooth<T, T>(s, l, e, b, s.coarse_sweeps, true, nullptr, skip, st); break;
   }
 }
 
@@ -686,22 +839,65 @@ static void vcycle(const DevState& s, T* x0, const T* b0, T* const* E, T* const*
                    const unsigned int* skip, cudaStream_t st) {
   const int L = s.nlev;
   if (L == 1) {
-    smooth<T>(s, 0, x0, b0, s.pre + s.post, zero0, nullptr, skip, st);
+    smooth<T, T>(s, 0, x0, b0, s.pre + s.post, zero0, nullptr, skip, st);
     return;
   }
-  smooth<T>(s, 0, x0, b0, s.pre0, zero0, nullptr, skip, st);
+  smooth<T, T>(s, 0, x0, b0, s.pre0, zero0, nullptr, skip, st);
   restrict_level<T>(s, 0, x0, b0, B[1], skip, st);
   for (int l = 1; l < L - 1; ++l) {
-    smooth<T>(s, l, E[l], B[l], s.pre, true, nullptr, skip, st);
+    smooth<T, T>(s, l, E[l], B[l], s.pre, true, nullptr, skip, st);
     restrict_level<T>(s, l, E[l], B[l], B[l + 1], skip, st);
   }
   coarse_solve<T>(s, L - 1, E[L - 1], B[L - 1], skip, st);
-  for (int l = L - 2; l >= 1; --l) smooth<T>(s, l, E[l], B[l], s.post, false, E[l + 1], skip, st);
-  smooth<T>(s, 0, x0, b0, s.post0, false, E[1], skip, st);
+  for (int l = L - 2; l >= 1; --l) smooth<T, T>(s, l, E[l], B[l], s.post, false, E[l + 1], skip, st);
+  smooth<T, T>(s, 0, x0, b0, s.post0, false, E[1], skip, st);
+}
+
+// ---- the mixed-precision correction solve --------------------------------------------------
+// Level arrays of the correction V-cycle: FP32 below kMixedBF16Level, BF16
+// from it on (the coarse levels carry only the smooth part of the error).
+struct MixLv {
+  float *ef, *bf;
+  __nv_bfloat16 *eh, *bh;
+  bool h;
+};
+static void mix_smooth(const DevState& s, int l, const MixLv* M, int sweeps, bool zero, bool add_coarse,
+                       const unsigned int* skip, cudaStream_t st) {
+  const bool ch = add_coarse && M[l + 1].h;
+  if (M[l].h) {
+    smooth<__nv_bfloat16, __nv_bfloat16>(s, l, M[l].eh, M[l].bh, sweeps, zero, add_coarse ? M[l + 1].eh : nullptr,
+                                         skip, st);
+  } else if (ch) {
+    smooth<float, __nv_bfloat16>(s, l, M[l].ef, M[l].bf, sweeps, zero, M[l + 1].eh, skip, st);
+  } else {
+    smooth<float, float>(s, l, M[l].ef, M[l].bf, sweeps, zero, add_coarse ? M[l + 1].ef : nullptr, skip, st);
+  }
+}
+static void mix_restrict(const DevState& s, int l, const MixLv* M, const unsigned int* skip, cudaStream_t st) {
+  if (M[l].h) restrict_level<__nv_bfloat16, __nv_bfloat16>(s, l, M[l].eh, M[l].bh, M[l + 1].bh, skip, st);
+  else if (M[l + 1].h) restrict_level<float, __nv_bfloat16>(s, l, M[l].ef, M[l].bf, M[l + 1].bh, skip, st);
+  else restrict_level<float, float>(s, l, M[l].ef, M[l].bf, M[l + 1].bf, skip, st);
+}
+static void mix_vcycle(const DevState& s, const MixLv* M, bool zero0, const unsigned int* skip, cudaStream_t st) {
+  const int L = s.nlev;
+  if (L == 1) {
+    mix_smooth(s, 0, M, s.pre + s.post, zero0, false, skip, st);
+    return;
+  }
+  mix_smooth(s, 0, M, s.pre0, zero0, false, skip, st);
+  mix_restrict(s, 0, M, skip, st);
+  for (int l = 1; l < L - 1; ++l) {
+    mix_smooth(s, l, M, s.pre, true, false, skip, st);
+    mix_restrict(s, l, M, skip, st);
+  }
+  if (M[L - 1].h) coarse_solve<__nv_bfloat16>(s, L - 1, M[L - 1].eh, M[L - 1].bh, skip, st);
+  else coarse_solve<float>(s, L - 1, M[L - 1].ef, M[L - 1].bf, skip, st);
+  for (int l = L - 2; l >= 1; --l) mix_smooth(s, l, M, s.post, false, true, skip, st);
+  mix_smooth(s, 0, M, s.post0, false, true, skip, st);
 }
 
 double smoother_pass(const DevState& s, cudaStream_t st) {
-  smooth<float>(s, 0, s.p, s.rhs, 1, false, nullptr, nullptr, st);
+  smooth<float, float>(s, 0, s.p, s.rhs, 1, false, nullptr, nullptr, st);
   // a red and a black half-sweep each read the other colour's half and their
   // own right-hand-side half and write their own half: 3 x N/2 words each
   return 2.0 * 3.0 * 0.5 * 4.0 * (double)s.g.n();
@@ -709,30 +905,117 @@ double smoother_pass(const DevState& s, cudaStream_t st) {
 
 void launch_residual_norm(const DevState& s, double* out, cudaStream_t st) {
   cudaMemsetAsync(out, 0, sizeof(double), st);
-  k_defect<<<g_cells(s.g), b_cells(), 0, st>>>(s.g, s.lv[0].h2, s.ref, s.p, s.rhs, nullptr, out, nullptr);
+  if (s.plo) {
+    k_defect_df<<<g_cells(s.g), b_cells(), 0, st>>>(s.g, s.ref, s.p, s.plo, s.rhs, nullptr, out, nullptr, nullptr);
+  } else {
+    k_defect<<<g_cells(s.g), b_cells(), 0, st>>>(s.g, s.lv[0].h2, s.ref, s.p, s.rhs, nullptr, out, nullptr);
+  }
+}
+
+// Mixed precision: defect correction.  Each outer iteration forms the
+// residual of the double-float pressure, stops the loop (device flag: the
+// kernels of the remaining iterations return at once, so the step stays one
+// captured graph) once max |r| and/or ||r|| / ||b|| meet their targets, else
+// solves A e = r with `cycles` V-cycles from zero (FP32 levels 0-1, BF16
+// coarser) and adds e to the pressure without rounding loss.
+static void mixed_solve(const DevState& s, cudaStream_t st) {
+  const size_t n = s.g.n();
+  MixLv M[kMaxLevels];
+  M[0] = {s.e0, s.r0, nullptr, nullptr, false};
+  for (int l = 1; l < s.nlev; ++l) {
+    const bool h = l >= kMixedBF16Level;
+    M[l] = {h ? nullptr : s.lv[l].e, h ? nullptr : s.lv[l].b, h ? s.lv[l].eh : nullptr, h ? s.lv[l].bh : nullptr, h};
+  }
+  unsigned int* done = s.redu + REDU_DONE;
+  cudaMemsetAsync(s.redu + REDU_DONE, 0, 2 * sizeof(unsigned int), st);  // done, iters
+  cudaMemsetAsync(s.redu + REDU_DEFECT_MAX, 0, 32 * sizeof(unsigned int), st);
+  cudaMemsetAsync(s.red + RED_RHS_NORM2, 0, sizeof(double) * (RED_COUNT - RED_RHS_NORM2), st);
+  k_sumsq64<<<s.num_sms * 4, 256, 0, st>>>(s.rhs, n, s.red + RED_RHS_NORM2);
+  for (int it = 0; it < s.max_outer; ++it) {
+    const int slot = it < 31 ? it : 31;
+    double* rn2 = s.red + RED_DEFECT_NORM2 + slot;
+    unsigned int* rmax = s.redu + REDU_DEFECT_MAX + slot;
+    k_defect_df<<<g_cells(s.g), b_cells(), 0, st>>>(s.g, s.ref, s.p, s.plo, s.rhs, s.r0, rn2, rmax, done);
+    k_defect_check<<<1, 1, 0, st>>>(rmax, rn2, s.red + RED_RHS_NORM2, s.div_tol_r, s.rel_tol, done,
+                                    s.redu + REDU_ITERS);
+    for (int c = 0; c < s.cycles; ++c) mix_vcycle(s, M, c == 0, done, st);
+    k_add_df<<<s.num_sms * 4, 256, 0, st>>>(s.p, s.plo, s.e0, n, done);
+  }
+  if (!s.ref) {
+    cudaMemsetAsync(s.red + RED_P_SUM, 0, sizeof(double), st);
+    k_sum_df<<<s.num_sms * 4, 256, 0, st>>>(s.p, s.plo, n, s.red + RED_P_SUM);
+    k_sub_mean_df<<<s.num_sms * 4, 256, 0, st>>>(s.p, s.plo, n, s.red + RED_P_SUM);
+  }
+}
+
+std::vector<float> coarse_inverse(const Grid& c, float h2, int ref) {
+  const int n = (int)c.n();
+  // A + J/n (Neumann: adds the null space back) in double, then Gauss-Jordan
+  std::vector<double> a((size_t)n * n, 0.0), inv((size_t)n * n, 0.0);
+  auto at = [&](int x, int y, int z) { return (z * c.ny + y) * c.nx + x; };
+  for (int z = 0; z < c.nz; ++z)
+    for (int y = 0; y < c.ny; ++y)
+      for (int x = 0; x < c.nx; ++x) {
+        const int i = at(x, y, z);
+        double diag = ref ? 1.0 : 0.0;
+        auto nb = [&](int j) { a[(size_t)i * n + j] += 1.0 / h2; diag += 1.0; };
+        if (x > 0) nb(at(x - 1, y, z));
+        if (x < c.nx - 1) nb(at(x + 1, y, z));
+        if (y > 0) nb(at(x, y - 1, z));
+        if (y < c.ny - 1) {
+          a[(size_t)i * n + at(x, y + 1, z)] += 1.0 / h2;
+          if (!ref) diag += 1.0;
+        }
+        if (z > 0) nb(at(x, y, z - 1));
+        if (z < c.nz - 1) nb(at(x, y, z + 1));
+        a[(size_t)i * n + i] -= diag / h2;
+      }
+  if (!ref)
+    for (auto& v : a) v += 1.0 / n;
+  for (int i = 0; i < n; ++i) inv[(size_t)i * n + i] = 1.0;
+  for (int col = 0; col < n; ++col) {
+    int piv = col;
+    for (int r = col + 1; r < n; ++r)
+      if (std::fabs(a[(size_t)r * n + col]) > std::fabs(a[(size_t)piv * n + col])) piv = r;
+    if (piv != col)
+      for (int k = 0; k < n; ++k) {
+        std::swap(a[(size_t)piv * n + k], a[(size_t)col * n + k]);
+        std::swap(inv[(size_t)piv * n + k], inv[(size_t)col * n + k]);
+      }
+    const double d = a[(size_t)col * n + col];
+    for (int k = 0; k < n; ++k) {
+      a[(size_t)col * n + k] /= d;
+      inv[(size_t)col * n + k] /= d;
+    }
+    for (int r = 0; r < n; ++r) {
+      if (r == col) continue;
+      const double f = a[(size_t)r * n + col];
+      if (f == 0.0) continue;
+      for (int k = 0; k < n; ++k) {
+        a[(size_t)r * n + k] -= f * a[(size_t)col * n + k];
+        inv[(size_t)r * n + k] -= f * inv[(size_t)col * n + k];
+      }
+    }
+  }
+  std::vector<float> out((size_t)n * n);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      double v = 0.5 * (inv[(size_t)i * n + j] + inv[(size_t)j * n + i]);
+      if (!ref) v -= 1.0 / n;  // (A + J/n)^-1 - J/n: the minimum-norm inverse
+      out[(size_t)i * n + j] = (float)v;
+    }
+  return out;
 }
 
 void launch_pressure_solve(const DevState& s, cudaStream_t st) {
-  const size_t n = s.g.n();
   if (s.prec == DOB_PREC_MIXED) {
-    __nv_bfloat16 *E[kMaxLevels], *B[kMaxLevels];
-    for (int l = 0; l < s.nlev; ++l) { E[l] = s.lv[l].eh; B[l] = s.lv[l].bh; }
-    unsigned int* done = s.redu + REDU_DONE;
-    cudaMemsetAsync(s.redu + REDU_DONE, 0, 2 * sizeof(unsigned int), st);  // done, iters
-    cudaMemsetAsync(s.red + RED_RHS_NORM2, 0, sizeof(double) * (RED_COUNT - RED_RHS_NORM2), st);
-    k_sumsq64<<<s.num_sms * 4, 256, 0, st>>>(s.rhs, n, s.red + RED_RHS_NORM2);
-    for (int it = 0; it < s.max_outer; ++it) {
-      double* rn2 = s.red + RED_DEFECT_NORM2 + (it < 31 ? it : 31);
-      k_defect<<<g_cells(s.g), b_cells(), 0, st>>>(s.g, s.lv[0].h2, s.ref, s.p, s.rhs, s.r0h, rn2, done);
-      k_defect_check<<<1, 1, 0, st>>>(rn2, s.red + RED_RHS_NORM2, s.rel_tol, done, s.redu + REDU_ITERS);
-      for (int c = 0; c < s.cycles; ++c) vcycle<__nv_bfloat16>(s, s.e0h, s.r0h, E, B, c == 0, done, st);
-      k_add_correction<<<s.num_sms * 4, 256, 0, st>>>(s.p, s.e0h, n, done);
-    }
-  } else {
-    float *E[kMaxLevels], *B[kMaxLevels];
-    for (int l = 0; l < s.nlev; ++l) { E[l] = s.lv[l].e; B[l] = s.lv[l].b; }
-    for (int c = 0; c < s.cycles; ++c) vcycle<float>(s, s.p, s.rhs, E, B, false, nullptr, st);
+    mixed_solve(s, st);
+    return;
   }
+  const size_t n = s.g.n();
+  float *E[kMaxLevels], *B[kMaxLevels];
+  for (int l = 0; l < s.nlev; ++l) { E[l] = s.lv[l].e; B[l] = s.lv[l].b; }
+  for (int c = 0; c < s.cycles; ++c) vcycle<float>(s, s.p, s.rhs, E, B, false, nullptr, st);
   if (!s.ref) {
     launch_sum(s.p, n, s.red + RED_P_SUM, s.num_sms, st);
     launch_sub_mean(s.p, n, s.red + RED_P_SUM, s.num_sms, st);

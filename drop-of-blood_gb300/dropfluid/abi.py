@@ -135,6 +135,7 @@ class DobConfig(C.Structure):
         ("mg_coarse_sweeps", C.c_int32), ("mg_cycles", C.c_int32),
         ("mg_max_outer", C.c_int32),
         ("mg_rel_tol", C.c_double),
+        ("mg_div_tol", C.c_double),
         ("casson_tau_y", C.c_float), ("casson_mu_p", C.c_float),
         ("physics_flags", C.c_int32),
         ("parcel_capacity", C.c_uint32),
@@ -196,6 +197,7 @@ def config_reference() -> DobConfig:
     c.mg_cycles = 1
     c.mg_max_outer = 1
     c.mg_rel_tol = 0.0
+    c.mg_div_tol = 0.0
     c.casson_tau_y = 0.0
     c.casson_mu_p = 0.0
     c.physics_flags = DOB_PHYS_REFERENCE_ALL
@@ -206,10 +208,34 @@ def config_reference() -> DobConfig:
     return c
 
 
+DENSE_COARSE_MAX = 1024
+
+
+def closed_box_levels(nx: int, ny: int, nz: int):
+    """(mg_levels, mg_coarse_sweeps) of the closed-box configuration: the
+    hierarchy is deepened (every grid keeping even dims) until the coarsest
+    grid has at most 512 cells, which are solved exactly (-1: dense inverse;
+    6 RBGS sweeps when no depth gets below 1024 cells)."""
+    levels, coarse = 1, 6
+    for L in range(2, 11):
+        m = 1 << L
+        if nx % m or ny % m or nz % m:
+            break
+        cells = (nx >> (L - 1)) * (ny >> (L - 1)) * (nz >> (L - 1))
+        levels = L
+        coarse = -1 if cells <= DENSE_COARSE_MAX else 6
+        if cells <= 512:
+            break
+    return levels, coarse
+
+
 def config_closed_box(nx: int, ny: int, nz: int) -> DobConfig:
     """Closed box, free-slip walls, pure-Neumann pressure; FP32; 2+2 RBGS on
-    every level of a 4-grid hierarchy; 4 V-cycles per step; Casson
-    tau_y = 0.005, mu_p = 1e-3; dx = 1, dt = 0.02 (the synthetic drop scenes)."""
+    every level of a hierarchy deep enough for an exact coarsest solve
+    (closed_box_levels); 4 V-cycles per step; Casson
+    tau_y = 0.005, mu_p = 1e-3; dx = 1, dt = 0.02 (the synthetic drop scenes).
+    In the mixed mode the defect loop stops at max |div| dt/dx <= 1e-5 (at
+    most 16 outer iterations of mg_cycles V-cycles each)."""
     c = DobConfig()
     c.struct_size = C.sizeof(DobConfig)
     c.nx, c.ny, c.nz = nx, ny, nz
@@ -220,13 +246,13 @@ def config_closed_box(nx: int, ny: int, nz: int) -> DobConfig:
     c.domain_max[:] = [float(nx), float(ny), float(nz)]
     c.bc_mode = DOB_BC_CLOSED_BOX
     c.precision_mode = DOB_PREC_FP32
-    c.mg_levels = 4
+    c.mg_levels, c.mg_coarse_sweeps = closed_box_levels(nx, ny, nz)
     c.mg_pre = 2
     c.mg_post = 2
-    c.mg_coarse_sweeps = 6
     c.mg_cycles = 4
-    c.mg_max_outer = 8
-    c.mg_rel_tol = 1e-8
+    c.mg_max_outer = 16
+    c.mg_rel_tol = 0.0
+    c.mg_div_tol = 1e-5
     c.casson_tau_y = 0.005
     c.casson_mu_p = 1e-3
     c.physics_flags = 0

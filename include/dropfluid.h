@@ -56,7 +56,9 @@ enum {
 /* Storage precision. Arithmetic is FP32 in every mode. */
 enum {
   DOB_PREC_FP32 = 0,           /* all fields FP32                                   */
-  DOB_PREC_MIXED = 1,          /* FP16 dye, BF16 correction levels, FP64 defect loop */
+  DOB_PREC_MIXED = 1,          /* FP16 dye; pressure as an FP32 pair (double-float)
+                                  corrected by an error-free residual loop whose
+                                  V-cycles store levels >= 2 as BF16                */
   DOB_PREC_REFERENCE_FP16 = 2  /* velocity/curl/dye stored as binary16 like the
                                   reference's rgba16float textures; pressure FP32  */
 };
@@ -89,10 +91,15 @@ typedef struct dob_config {
                                   must be divisible by 2^mg_levels so that every grid
                                   has even dims                                      */
   int32_t mg_pre, mg_post;     /* RBGS sweeps before/after coarse correction          */
-  int32_t mg_coarse_sweeps;    /* RBGS sweeps on the coarsest grid (reference: 6)    */
+  int32_t mg_coarse_sweeps;    /* RBGS sweeps on the coarsest grid (reference: 6);
+                                  -1: exact solve with a dense (pseudo-)inverse,
+                                  coarsest grid of at most 1024 cells              */
   int32_t mg_cycles;           /* V-cycles per step (reference: 1)                   */
   int32_t mg_max_outer;        /* mixed mode: max defect-correction iterations       */
-  double mg_rel_tol;           /* mixed mode: target ||b-Ap||/||b|| (FP64)            */
+  double mg_rel_tol;           /* mixed mode: stop at ||b-Ap||/||b|| <= this (0: off)  */
+  double mg_div_tol;           /* mixed mode: stop at max |b-Ap| (= the projected max
+                                  |div u|) scaled like dob_step_stats.max_div <= this
+                                  (0: off); both targets must hold                  */
   float casson_tau_y;          /* closed-box Casson yield stress                      */
   float casson_mu_p;           /* closed-box Casson plastic viscosity                 */
   int32_t physics_flags;       /* DOB_PHYS_*                                          */
@@ -196,8 +203,10 @@ typedef struct dob_step_stats {
    (src/shaders/common.ts:4-20; BloodDropEngine.ts:88-98). */
 dob_status dob_config_reference(dob_config* cfg);
 /* Fill *cfg with a closed-box synthetic scene of the given grid:
-   FP32, 2+2 RBGS on every level, 4 grids, 4 cycles, Casson tau_y=0.005,
-   mu_p=1e-3, dx=1, dt=0.02. */
+   FP32, 2+2 RBGS on every level, 4 cycles, the hierarchy deepened (even dims
+   on every grid) until the coarsest grid has at most 512 cells, solved
+   exactly (mg_coarse_sweeps = -1); Casson tau_y=0.005, mu_p=1e-3, dx=1,
+   dt=0.02; mixed mode: stop at max |div| dt/dx <= 1e-5, <= 16 iterations. */
 dob_status dob_config_closed_box(dob_config* cfg, uint32_t nx, uint32_t ny, uint32_t nz);
 
 dob_status dob_create(const dob_config* cfg, dob_ctx** out);
@@ -336,7 +345,7 @@ dob_status dob_eval_math(int fn, const float* x, const float* y, float* out, uin
    or cudaFree (both synchronise the device and can fail mid-frame).  No
    context is needed and nothing is allocated: the working arrays (split
    copies, coarse grids, reduction slots) live in one fixed device array of
-   about 20 MiB that is part of the library and stays resident on every GPU
+   about 24 MiB that is part of the library and stays resident on every GPU
    that loads it until the process exits.
 
    rhs and pressure are device pointers of the current device, nx*ny*nz

@@ -149,6 +149,7 @@ template <class R> class Sim {
   std::vector<R> u, v, w, u2, v2, w2;
   std::vector<R> cen[4], curl[4];
   std::vector<R> p, rhs;
+  std::vector<double> p64;  // mixed mode: the pressure the defect loop carries (the device's p + plo)
   struct Level {
     Dims d;
     std::vector<R> e, b, r;
@@ -340,6 +341,7 @@ template <class R> class Sim {
     for (int c = 0; c < 4; ++c) { std::fill(cen[c].begin(), cen[c].end(), R(0)); std::fill(curl[c].begin(), curl[c].end(), R(0)); }
     if (ref) init_vel();
     std::fill(p.begin(), p.end(), R(0));
+    if (mixed()) p64.assign(p.size(), 0.0);
     std::fill(rhs.begin(), rhs.end(), R(0));
     for (auto& L : lv) { std::fill(L.e.begin(), L.e.end(), R(0)); std::fill(L.b.begin(), L.b.end(), R(0)); std::fill(L.r.begin(), L.r.end(), R(0)); }
     for (int c = 0; c < nconc; ++c) { std::fill(conc[c].begin(), conc[c].end(), R(0)); std::fill(concN[c].begin(), concN[c].end(), R(0)); }
@@ -681,12 +683,10 @@ template <class R> class Sim {
   }
 
   // ---- multigrid (fluid.ts:561-855; schedule BloodDropEngine.ts:1942-2059) ---------------
-  // Storage rounding of a level's correction arrays (mixed mode: BF16 at
-  // every correction level, FP32 compute).
-  bool bf16_level(int l, bool inner) const {
-    if (fp64 || cfg.precision_mode != DOB_PREC_MIXED) return false;
-    return inner || l >= 1;
-  }
+  // Mixed mode (float oracle only): defect correction of a higher-precision
+  // pressure p64 whose correction V-cycles store levels >= 2 as BF16.
+  bool mixed() const { return !fp64 && cfg.precision_mode == DOB_PREC_MIXED; }
+  bool bf16_level(int l, bool inner) const { return inner && mixed() && l >= 2; }
   R h2(const Dims& d) const {
     const R s = (R)dv.nx / (R)d.nx;
     return s * s;
@@ -778,6 +778,71 @@ template <class R> class Sim {
           a[i] = bf16 ? (R)dob_round_bf16((float)val) : val;
         }
   }
+  // Exact coarsest solve (mg_coarse_sweeps = -1): e = M b with M the
+  // symmetric (pseudo-)inverse of the coarsest operator, built once by
+  // Gauss-Jordan in double on A + J/n (pure Neumann; J/n removed afterwards)
+  // or on A (Dirichlet top).  The float oracle applies M rounded to float.
+  std::vector<double> cinv;
+  void build_cinv(const Dims& c) {
+    const int n = (int)c.n();
+    const double hh = (double)h2(c);
+    std::vector<double> a((size_t)n * n, 0.0), inv((size_t)n * n, 0.0);
+    for (int z = 0; z < c.nz; ++z)
+      for (int y = 0; y < c.ny; ++y)
+        for (int x = 0; x < c.nx; ++x) {
+          const int i = (int)c.at(x, y, z);
+          double diag = ref ? 1.0 : 0.0;
+          auto nb = [&](int xx, int yy, int zz, bool count) {
+            a[(size_t)i * n + c.at(xx, yy, zz)] += 1.0 / hh;
+            if (count) diag += 1.0;
+          };
+          if (x > 0) nb(x - 1, y, z, true);
+          if (x < c.nx - 1) nb(x + 1, y, z, true);
+          if (y > 0) nb(x, y - 1, z, true);
+          if (y < c.ny - 1) nb(x, y + 1, z, !ref);
+          if (z > 0) nb(x, y, z - 1, true);
+          if (z < c.nz - 1) nb(x, y, z + 1, true);
+          a[(size_t)i * n + i] -= diag / hh;
+        }
+    if (!ref)
+      for (auto& v : a) v += 1.0 / n;
+    for (int i = 0; i < n; ++i) inv[(size_t)i * n + i] = 1.0;
+    for (int col = 0; col < n; ++col) {
+      int piv = col;
+      for (int r = col + 1; r < n; ++r)
+        if (std::fabs(a[(size_t)r * n + col]) > std::fabs(a[(size_t)piv * n + col])) piv = r;
+      if (piv != col)
+        for (int k = 0; k < n; ++k) {
+          std::swap(a[(size_t)piv * n + k], a[(size_t)col * n + k]);
+          std::swap(inv[(size_t)piv * n + k], inv[(size_t)col * n + k]);
+        }
+      const double d = a[(size_t)col * n + col];
+      for (int k = 0; k < n; ++k) { a[(size_t)col * n + k] /= d; inv[(size_t)col * n + k] /= d; }
+      for (int r = 0; r < n; ++r) {
+        if (r == col) continue;
+        const double f = a[(size_t)r * n + col];
+        if (f == 0.0) continue;
+        for (int k = 0; k < n; ++k) {
+          a[(size_t)r * n + k] -= f * a[(size_t)col * n + k];
+          inv[(size_t)r * n + k] -= f * inv[(size_t)col * n + k];
+        }
+      }
+    }
+    cinv.assign((size_t)n * n, 0.0);
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j)
+        cinv[(size_t)i * n + j] = 0.5 * (inv[(size_t)i * n + j] + inv[(size_t)j * n + i]) - (ref ? 0.0 : 1.0 / n);
+  }
+  R cinv_at(size_t k) const { return fp64 ? (R)cinv[k] : (R)(float)cinv[k]; }
+  void coarse_exact(R* e, const R* b, const Dims& c, bool bf16) {
+    const size_t n = c.n();
+    if (cinv.size() != n * n) build_cinv(c);
+    for (size_t j = 0; j < n; ++j) {
+      R acc = R(0);
+      for (size_t i = 0; i < n; ++i) acc = acc + cinv_at(i * n + j) * b[i];
+      e[j] = bf16 ? (R)dob_round_bf16((float)acc) : acc;
+    }
+  }
   int sweeps_pre(int l) const { return (l == 0 && cfg.reference_schedule) ? 1 : cfg.mg_pre; }
   int sweeps_post(int l) const { return (l == 0 && cfg.reference_schedule) ? 1 : cfg.mg_post; }
 
@@ -800,7 +865,8 @@ template <class R> class Sim {
     }
     Level& C = lv[L - 1];
     std::fill(C.e.begin(), C.e.end(), R(0));
-    smooth(C.e.data(), C.b.data(), C.d, cfg.mg_coarse_sweeps, bf16_level(L - 1, inner));
+    if (cfg.mg_coarse_sweeps < 0) coarse_exact(C.e.data(), C.b.data(), C.d, bf16_level(L - 1, inner));
+    else smooth(C.e.data(), C.b.data(), C.d, cfg.mg_coarse_sweeps, bf16_level(L - 1, inner));
     for (int l = L - 2; l >= 1; --l) {
       prolong_add(lv[l].e.data(), lv[l].d, lv[l + 1].e.data(), lv[l + 1].d, bf16_level(l, inner));
       smooth(lv[l].e.data(), lv[l].b.data(), lv[l].d, cfg.mg_post, bf16_level(l, inner));
@@ -832,29 +898,65 @@ template <class R> class Sim {
     return sqrt(s);
   }
 
+  // ||b - A p64|| and max |b - A p64| in double (the mixed loop's residual)
+  double residual64(std::vector<double>* out, double* rmax) {
+    const Dims& d = lv[0].d;
+    double s = 0.0, m = 0.0;
+#pragma omp parallel for reduction(+ : s) reduction(max : m) schedule(static)
+    for (int z = 0; z < d.nz; ++z)
+      for (int y = 0; y < d.ny; ++y)
+        for (int x = 0; x < d.nx; ++x) {
+          double sumN = 0.0, diag = ref ? 1.0 : 0.0;
+          if (x > 0) { sumN += p64[d.at(x - 1, y, z)]; diag += 1.0; }
+          if (x < d.nx - 1) { sumN += p64[d.at(x + 1, y, z)]; diag += 1.0; }
+          if (y > 0) { sumN += p64[d.at(x, y - 1, z)]; diag += 1.0; }
+          if (y < d.ny - 1) { sumN += p64[d.at(x, y + 1, z)]; if (!ref) diag += 1.0; }
+          if (z > 0) { sumN += p64[d.at(x, y, z - 1)]; diag += 1.0; }
+          if (z < d.nz - 1) { sumN += p64[d.at(x, y, z + 1)]; diag += 1.0; }
+          const double r = (double)rhs[d.at(x, y, z)] - (sumN - diag * p64[d.at(x, y, z)]);
+          if (out) (*out)[d.at(x, y, z)] = r;
+          s += r * r;
+          m = std::max(m, std::fabs(r));
+        }
+    if (rmax) *rmax = m;
+    return sqrt(s);
+  }
+
   void pressure_solve() {
     int cycles = 0, outer = 0;
-    if (!fp64 && cfg.precision_mode == DOB_PREC_MIXED) {
-      // Defect correction: FP64 residual of the FP32 pressure, BF16-stored
-      // V-cycle on the correction, FP32 update.
+    if (mixed()) {
+      // Defect correction: residual of the high-precision pressure, stop at
+      // max |r| (the projected divergence) and/or ||r|| / ||b||, else an
+      // FP32 correction V-cycle (BF16 storage from level 2) added to p64.
       const double bnorm = sqrt(dot64(rhs, rhs));
+      const double div_r = ref ? cfg.mg_div_tol : cfg.mg_div_tol * (double)cfg.dx / (double)cfg.dt;
       std::vector<double> r64(p.size());
       std::vector<R> rin(p.size()), e(p.size());
       const int max_outer = std::max(1, cfg.mg_max_outer);
       for (outer = 0; outer < max_outer; ++outer) {
-        const double rn = residual_l2(p, rhs, &r64);
-        if (bnorm == 0.0 || rn <= cfg.mg_rel_tol * bnorm) break;
-        for (size_t i = 0; i < p.size(); ++i) rin[i] = (R)dob_round_bf16((float)r64[i]);
+        double rmax = 0.0;
+        const double rn = residual64(&r64, &rmax);
+        const bool div_ok = cfg.mg_div_tol <= 0.0 || rmax <= (double)(float)div_r;
+        const bool rel_ok = cfg.mg_rel_tol <= 0.0 || bnorm == 0.0 || rn <= cfg.mg_rel_tol * bnorm;
+        if (div_ok && rel_ok) break;
+        for (size_t i = 0; i < p.size(); ++i) rin[i] = (R)r64[i];
         std::fill(e.begin(), e.end(), R(0));
         for (int c = 0; c < cfg.mg_cycles; ++c) { vcycle(e.data(), rin.data(), true); ++cycles; }
-        for (size_t i = 0; i < p.size(); ++i) p[i] = p[i] + e[i];
+        for (size_t i = 0; i < p.size(); ++i) p64[i] += (double)e[i];
       }
+      if (!ref) {
+        double s = 0.0;
+        for (double q : p64) s += q;
+        const double mean = s / (double)p64.size();
+        for (auto& q : p64) q -= mean;
+      }
+      for (size_t i = 0; i < p.size(); ++i) p[i] = (R)p64[i];
     } else {
       for (int c = 0; c < cfg.mg_cycles; ++c) { vcycle(p.data(), rhs.data(), false); ++cycles; }
-    }
-    if (!ref) {  // pin the pressure mean (FP64 sum)
-      const R mean = (R)(sum64(p) / (double)p.size());
-      for (auto& q : p) q = q - mean;
+      if (!ref) {  // pin the pressure mean (FP64 sum)
+        const R mean = (R)(sum64(p) / (double)p.size());
+        for (auto& q : p) q = q - mean;
+      }
     }
     last_stats[3] = cycles;
     last_stats[4] = outer;
@@ -875,11 +977,13 @@ template <class R> class Sim {
           const size_t i = dv.at(x, y, z);
           V3<R> mac = mk(u[i], v[i], w[i]);
           const R pC = p[i];
-          if (x < dv.nx - 1) mac.x = mac.x - (p[dv.at(x + 1, y, z)] - pC); else mac.x = R(0);
-          if (y < dv.ny - 1) mac.y = mac.y - (p[dv.at(x, y + 1, z)] - pC);
+          // mixed mode: pressure differences of the high-precision pressure
+          auto dp = [&](size_t j) { return mixed() ? (R)(p64[j] - p64[i]) : p[j] - pC; };
+          if (x < dv.nx - 1) mac.x = mac.x - dp(dv.at(x + 1, y, z)); else mac.x = R(0);
+          if (y < dv.ny - 1) mac.y = mac.y - dp(dv.at(x, y + 1, z));
           else if (ref) mac.y = mac.y - (top_pressure(x, z) - pC);
           else mac.y = R(0);
-          if (z < dv.nz - 1) mac.z = mac.z - (p[dv.at(x, y, z + 1)] - pC); else mac.z = R(0);
+          if (z < dv.nz - 1) mac.z = mac.z - dp(dv.at(x, y, z + 1)); else mac.z = R(0);
           if (ref) mac = ClampV(mac, R(-2), R(2));
           u[i] = st_vel(mac.x); v[i] = st_vel(mac.y); w[i] = st_vel(mac.z);
         }
@@ -1458,7 +1562,7 @@ template <class R> class Sim {
     mac_rhs();
     if (want_stats) last_stats[0] = sqrt(dot64(rhs, rhs));
     pressure_solve();
-    if (want_stats) last_stats[1] = residual_l2(p, rhs, nullptr);
+    if (want_stats) last_stats[1] = mixed() ? residual64(nullptr, nullptr) : residual_l2(p, rhs, nullptr);
     project();
     if (want_stats) last_stats[2] = max_div();
     mac_to_center();
@@ -1517,7 +1621,11 @@ template <class R> int set_field(Sim<R>& s, int field, const void* host, size_t 
     case DOB_FIELD_VEL_W: return put(s.w, N);
     case DOB_FIELD_VEL_CENTER: return put4(s.cen, 4, N);
     case DOB_FIELD_CURL: return put4(s.curl, 4, N);
-    case DOB_FIELD_PRESSURE: return put(s.p, N);
+    case DOB_FIELD_PRESSURE: {
+      const int rc = put(s.p, N);
+      if (rc == DOB_OK && s.mixed()) for (size_t i = 0; i < N; ++i) s.p64[i] = (double)s.p[i];
+      return rc;
+    }
     case DOB_FIELD_RHS: return put(s.rhs, N);
     case DOB_FIELD_CONC: return s.nconc == 4 ? put4(s.conc, 4, Nc) : put(s.conc[0], Nc);
     case DOB_FIELD_CONC_PRED: return put(s.pred, Nc);
@@ -1570,7 +1678,13 @@ template <class R> int get_field(Sim<R>& s, int field, void* host, size_t bytes)
     case DOB_FIELD_VEL_W: return get(s.w, N);
     case DOB_FIELD_VEL_CENTER: return get4(s.cen, 4, N);
     case DOB_FIELD_CURL: return get4(s.curl, 4, N);
-    case DOB_FIELD_PRESSURE: return get(s.p, N);
+    case DOB_FIELD_PRESSURE:
+      if (s.mixed()) {
+        if (bytes != N * sizeof(float)) return DOB_EINVAL;
+        for (size_t i = 0; i < N; ++i) ((float*)host)[i] = (float)s.p64[i];
+        return DOB_OK;
+      }
+      return get(s.p, N);
     case DOB_FIELD_RHS: return get(s.rhs, N);
     case DOB_FIELD_CONC: return s.nconc == 4 ? get4(s.conc, 4, Nc) : get(s.conc[0], Nc);
     case DOB_FIELD_CONC_PRED: return get(s.pred, Nc);
@@ -1634,6 +1748,11 @@ template <class R> int field_arrays(Sim<R>& s, int field, std::vector<R>* a[4]) 
 }
 // double-precision field access (interleaved channels like the float API)
 template <class R> int get_field64(Sim<R>& s, int field, double* host, size_t n) {
+  if (field == DOB_FIELD_PRESSURE && s.mixed()) {  // the defect loop's high-precision pressure
+    if (n != s.p64.size()) return DOB_EINVAL;
+    for (size_t i = 0; i < n; ++i) host[i] = s.p64[i];
+    return DOB_OK;
+  }
   std::vector<R>* a[4];
   const int nch = field_arrays(s, field, a);
   if (nch == 0 || n != a[0]->size() * nch) return DOB_EINVAL;
@@ -1642,6 +1761,11 @@ template <class R> int get_field64(Sim<R>& s, int field, double* host, size_t n)
   return DOB_OK;
 }
 template <class R> int set_field64(Sim<R>& s, int field, const double* host, size_t n) {
+  if (field == DOB_FIELD_PRESSURE && s.mixed()) {
+    if (n != s.p64.size()) return DOB_EINVAL;
+    for (size_t i = 0; i < n; ++i) { s.p64[i] = host[i]; s.p[i] = (R)host[i]; }
+    return DOB_OK;
+  }
   std::vector<R>* a[4];
   const int nch = field_arrays(s, field, a);
   if (nch == 0 || n != a[0]->size() * nch) return DOB_EINVAL;
@@ -1657,6 +1781,10 @@ bool valid_config(const dob_config* c) {
   if (c->mg_levels < 1 || c->mg_levels > 10) return false;
   const uint32_t m = 1u << c->mg_levels;  // even dims on every level, like the library
   if (c->nx % m || c->ny % m || c->nz % m) return false;
+  if (c->mg_coarse_sweeps < -1) return false;
+  if (c->mg_coarse_sweeps == -1 &&
+      (uint64_t)(c->nx >> (c->mg_levels - 1)) * (c->ny >> (c->mg_levels - 1)) * (c->nz >> (c->mg_levels - 1)) > 1024)
+    return false;
   if (c->bc_mode != DOB_BC_REFERENCE && c->bc_mode != DOB_BC_CLOSED_BOX) return false;
   if (c->precision_mode < 0 || c->precision_mode > 2) return false;
   if (c->parcel_capacity < 1) return false;

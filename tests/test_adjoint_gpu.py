@@ -17,13 +17,11 @@ from helpers import rel_l2
 pytestmark = pytest.mark.gpu
 
 # FP32 device adjoint vs FP64 oracle adjoint at the same (float32) state.  The
-# pressure adjoint is the difference of nearly equal terms (mean removal and
-# contracting V-cycles), so its relative error is larger.  The centre-velocity
+# centre-velocity
 # adjoints of the dye stages see a few departure points that FP32 rounds onto
 # a grid node (a sub-ulp displacement) where FP64 does not; the two then take
 # different one-sided / mean slopes of the interpolation at that node.
 STAGE_TOL = 1e-5
-PRESSURE_TOL = 1e-3
 NODE_TOL = 1e-3
 
 
@@ -45,11 +43,13 @@ def test_stage_adjoint_matches_fp64_oracle(pair, stage):
     rg = AC.run_stage_adjoint(g, st, stage, ys)
     ro = AC.run_stage_adjoint(o, st, stage, ys)
     for f in ins:
-        tol = STAGE_TOL
         if stage == abi.STAGE_PRESSURE_SOLVE and f == abi.FIELD_PRESSURE:
-            tol = PRESSURE_TOL
-        elif f == abi.FIELD_VEL_CENTER:
-            tol = NODE_TOL
+            # the warm-start adjoint is what survives the contracting
+            # V-cycles: compare its error with the incoming cotangent's size
+            err = np.linalg.norm((rg[f] - ro[f]).ravel()) / np.linalg.norm(ys[f].ravel())
+            assert err < STAGE_TOL, (abi.STAGE_NAMES[stage], f, err)
+            continue
+        tol = NODE_TOL if f == abi.FIELD_VEL_CENTER else STAGE_TOL
         assert rel_l2(rg[f], ro[f]) < tol, (abi.STAGE_NAMES[stage], f, rel_l2(rg[f], ro[f]))
 
 
@@ -67,7 +67,8 @@ def test_pressure_adjoint_other_grids(gpu_lib, oracle_mod, dims, levels):
         rg = AC.run_stage_adjoint(g, st, stage, ys)
         ro = AC.run_stage_adjoint(o, st, stage, ys)
         assert rel_l2(rg[abi.FIELD_RHS], ro[abi.FIELD_RHS]) < 1e-4
-        assert rel_l2(rg[abi.FIELD_PRESSURE], ro[abi.FIELD_PRESSURE]) < PRESSURE_TOL
+        dp = rg[abi.FIELD_PRESSURE] - ro[abi.FIELD_PRESSURE]
+        assert np.linalg.norm(dp.ravel()) / np.linalg.norm(ys[abi.FIELD_PRESSURE].ravel()) < 1e-5
 
 
 @pytest.mark.parametrize("stage", AC.LINEAR)

@@ -115,23 +115,35 @@ def test_box48_divergence_after_projection(oracle_mod):
     assert st["vcycles"] == sc.config.mg_cycles
 
 
-def test_mixed_defect_loop_reaches_tolerance(oracle_mod):
+@pytest.mark.parametrize("rel_tol,div_tol", [(1e-8, 0.0), (0.0, 1e-5), (1e-8, 1e-5)])
+def test_mixed_defect_loop_reaches_tolerance(oracle_mod, rel_tol, div_tol):
+    """The defect loop of a high-precision pressure reaches a relative
+    residual of 1e-8 and/or a max-norm divergence target, below the FP32
+    rounding of the pressure itself."""
     c = abi.config_closed_box(32, 32, 32)
     c.mg_levels = 4
     c.precision_mode = abi.DOB_PREC_MIXED
     c.mg_cycles = 1
-    c.mg_rel_tol = 1e-7
-    c.mg_max_outer = 20
+    c.mg_rel_tol = rel_tol
+    c.mg_div_tol = div_tol
+    c.mg_max_outer = 30
     c.parcel_capacity = 16
     s = oracle_mod.OracleSim(c)
     for f, sd in ((abi.FIELD_VEL_U, 1), (abi.FIELD_VEL_V, 2), (abi.FIELD_VEL_W, 3)):
         s.set_field(f, smooth_field((32, 32, 32), sd, 40.0))
     s.run_stage(abi.STAGE_MAC_RHS)
-    b = s.get_field(abi.FIELD_RHS)
+    b = s.get_field64(abi.FIELD_RHS)
     s.run_stage(abi.STAGE_PRESSURE_SOLVE)
-    p = s.get_field(abi.FIELD_PRESSURE)
-    r = b.astype(np.float64) - apply_laplacian(p, False)
-    assert np.linalg.norm(r) / np.linalg.norm(b) < 5e-7
+    p = s.get_field64(abi.FIELD_PRESSURE)
+    r = b - apply_laplacian(p, False)
+    if rel_tol:
+        assert np.linalg.norm(r) / np.linalg.norm(b) <= rel_tol
+    if div_tol:
+        assert np.abs(r).max() * c.dt / c.dx <= div_tol
+    # the FP32-rounded pressure alone could not get there
+    r32 = b - apply_laplacian(p.astype(np.float32).astype(np.float64), False)
+    if rel_tol:
+        assert np.linalg.norm(r32) / np.linalg.norm(b) > 10 * rel_tol
 
 
 def test_oracle_is_deterministic(oracle_mod):

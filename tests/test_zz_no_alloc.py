@@ -26,6 +26,8 @@ def _abi():
 
 
 def _config(mode, dims):
+    """Closed box: the library's default hierarchy for the grid (exact
+    coarsest solve); reference mode: 4 grids with 6 coarse sweeps."""
     abi = _abi()
     if mode == "box":
         c = abi.config_closed_box(*dims)
@@ -34,7 +36,7 @@ def _config(mode, dims):
         c = abi.config_reference()
         c.nx, c.ny, c.nz = dims
         c.parcel_capacity = 1024
-    c.mg_levels = 4
+        c.mg_levels = 4
     return c
 
 
@@ -100,7 +102,6 @@ def test_noalloc_smaller_grid_after_larger(gpu_lib):
         pytest.skip("no CUDA device")
     big = _config("box", (128, 128, 64))
     small = _config("box", (32, 32, 32))
-    small.mg_levels = 3
     _noalloc_solve(gpu_lib, torch, big, _rhs(big, 21), np.zeros((64, 128, 128), np.float32))
     for seed in (22, 23):
         rhs = _rhs(small, seed)
