@@ -400,7 +400,9 @@ dob_status dob_create(const dob_config* cfg, dob_ctx** out) {
   CK(cudaGetDevice(&ctx->device));
   CK(cudaDeviceGetAttribute(&s.num_sms, cudaDevAttrMultiProcessorCount, ctx->device));
   CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+  CK(cudaStreamCreateWithFlags(&ctx->aux_stream, cudaStreamNonBlocking));
   CK(mg_prepare());
+  s.aux = ctx->aux_stream;
   s.g = Grid{(int)cfg->nx, (int)cfg->ny, (int)cfg->nz};
   s.gc = Grid{(int)(cfg->nx * cfg->dye_refine), (int)(cfg->ny * cfg->dye_refine), (int)(cfg->nz * cfg->dye_refine)};
   s.prec = cfg->precision_mode;
@@ -504,6 +506,7 @@ void dob_destroy(dob_ctx* ctx) {
   for (int k = 0; k <= DOB_STAGE_COUNT; ++k)
     if (ctx->stage_ev[k]) cudaEventDestroy(ctx->stage_ev[k]);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  if (ctx->aux_stream) cudaStreamDestroy(ctx->aux_stream);
   delete ctx;
 }
 

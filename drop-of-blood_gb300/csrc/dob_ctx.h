@@ -31,6 +31,7 @@ struct dob_ctx {
   dob::DevState s;
   int device = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t aux_stream = nullptr;  // body capture of conditional graph nodes
   std::string err;
   float U[128];
   dob::StepParams* host_params = nullptr;  // pinned ring

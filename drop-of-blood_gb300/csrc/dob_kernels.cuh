@@ -66,6 +66,9 @@ struct DevState {
   int max_outer;
   double rel_tol;   // stop when ||b - A p|| <= rel_tol ||b|| (0: off)
   float div_tol_r;  // stop when max |b - A p| <= div_tol_r (0: off)
+  // second stream of the context: captures the body of the defect loop's
+  // conditional while-node when the step is captured into a graph
+  cudaStream_t aux;
 };
 constexpr int kMixedBF16Level = 2;
 

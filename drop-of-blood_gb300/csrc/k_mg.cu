@@ -625,18 +625,33 @@ __global__ void __launch_bounds__(256) k_defect_df(Grid d, int ref, const float*
   if (maxbits) block_max_atomic(ra, maxbits);
 }
 
-// Converged when max |r| <= div_tol_r and ||r|| <= rel_tol ||b|| (a zero
-// tolerance switches its test off): sets the skip flag every later kernel of
-// the defect loop reads, and counts executed iterations.
-__global__ void k_defect_check(const unsigned int* __restrict__ maxbits, const double* __restrict__ rnorm2,
-                               const double* __restrict__ bnorm2, float div_tol_r, double rel_tol,
-                               unsigned int* __restrict__ done, unsigned int* __restrict__ iters) {
-  if (*done) return;
+// One check of the defect loop: converged when max |r| <= div_tol_r and
+// ||r|| <= rel_tol ||b|| (a zero tolerance switches its test off).  On
+// convergence it sets the skip flag the rest of the iteration reads; it
+// counts corrections and stops the loop after max_outer of them.  Inside a
+// captured graph the loop is a conditional while-node and `cond` ends it;
+// the reduction slots are cleared for the next iteration.
+__global__ void k_defect_check(unsigned int* __restrict__ maxbits, double* __restrict__ rnorm2,
+                               const double* __restrict__ bnorm2, float div_tol_r, double rel_tol, int max_outer,
+                               unsigned int* __restrict__ done, unsigned int* __restrict__ iters,
+                               cudaGraphConditionalHandle cond, int use_cond) {
+  if (*done) {
+    if (use_cond) cudaGraphSetConditional(cond, 0u);
+    return;
+  }
   const bool div_ok = div_tol_r <= 0.0f || __uint_as_float(*maxbits) <= div_tol_r;
   const double rn = sqrt(*rnorm2), bn = sqrt(*bnorm2);
   const bool rel_ok = rel_tol <= 0.0 || bn == 0.0 || rn <= rel_tol * bn;
-  if (div_ok && rel_ok) *done = 1u;
-  else *iters += 1u;
+  *maxbits = 0u;
+  *rnorm2 = 0.0;
+  if (div_ok && rel_ok) {
+    *done = 1u;
+    if (use_cond) cudaGraphSetConditional(cond, 0u);
+    return;
+  }
+  const unsigned int n = *iters + 1u;
+  *iters = n;
+  if (use_cond && n >= (unsigned int)max_outer) cudaGraphSetConditional(cond, 0u);  // this correction is the last
 }
 
 // (p, plo) += e, error-free (same split layout)
@@ -927,19 +942,47 @@ static void mixed_solve(const DevState& s, cudaStream_t st) {
     M[l] = {h ? nullptr : s.lv[l].e, h ? nullptr : s.lv[l].b, h ? s.lv[l].eh : nullptr, h ? s.lv[l].bh : nullptr, h};
   }
   unsigned int* done = s.redu + REDU_DONE;
+  double* rn2 = s.red + RED_DEFECT_NORM2;
+  unsigned int* rmax = s.redu + REDU_DEFECT_MAX;
   cudaMemsetAsync(s.redu + REDU_DONE, 0, 2 * sizeof(unsigned int), st);  // done, iters
-  cudaMemsetAsync(s.redu + REDU_DEFECT_MAX, 0, 32 * sizeof(unsigned int), st);
+  cudaMemsetAsync(rmax, 0, sizeof(unsigned int), st);
   cudaMemsetAsync(s.red + RED_RHS_NORM2, 0, sizeof(double) * (RED_COUNT - RED_RHS_NORM2), st);
   k_sumsq64<<<s.num_sms * 4, 256, 0, st>>>(s.rhs, n, s.red + RED_RHS_NORM2);
-  for (int it = 0; it < s.max_outer; ++it) {
-    const int slot = it < 31 ? it : 31;
-    double* rn2 = s.red + RED_DEFECT_NORM2 + slot;
-    unsigned int* rmax = s.redu + REDU_DEFECT_MAX + slot;
-    k_defect_df<<<g_cells(s.g), b_cells(), 0, st>>>(s.g, s.ref, s.p, s.plo, s.rhs, s.r0, rn2, rmax, done);
-    k_defect_check<<<1, 1, 0, st>>>(rmax, rn2, s.red + RED_RHS_NORM2, s.div_tol_r, s.rel_tol, done,
-                                    s.redu + REDU_ITERS);
-    for (int c = 0; c < s.cycles; ++c) mix_vcycle(s, M, c == 0, done, st);
-    k_add_df<<<s.num_sms * 4, 256, 0, st>>>(s.p, s.plo, s.e0, n, done);
+  auto iteration = [&](cudaStream_t q, cudaGraphConditionalHandle cond, int use_cond) {
+    k_defect_df<<<g_cells(s.g), b_cells(), 0, q>>>(s.g, s.ref, s.p, s.plo, s.rhs, s.r0, rn2, rmax, done);
+    k_defect_check<<<1, 1, 0, q>>>(rmax, rn2, s.red + RED_RHS_NORM2, s.div_tol_r, s.rel_tol, s.max_outer, done,
+                                   s.redu + REDU_ITERS, cond, use_cond);
+    for (int c = 0; c < s.cycles; ++c) mix_vcycle(s, M, c == 0, done, q);
+    k_add_df<<<s.num_sms * 4, 256, 0, q>>>(s.p, s.plo, s.e0, n, done);
+  };
+  // Inside a stream capture the loop becomes a conditional while-node, so a
+  // step runs only the iterations it needs; otherwise all max_outer
+  // iterations are enqueued and the converged ones return at once.
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaGraph_t graph = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t ndeps = 0;
+  if (s.aux && cudaStreamGetCaptureInfo(st, &cs, nullptr, &graph, &deps, nullptr, &ndeps) != cudaSuccess) {
+    cudaGetLastError();
+    cs = cudaStreamCaptureStatusNone;
+  }
+  if (cs == cudaStreamCaptureStatusActive) {
+    cudaGraphConditionalHandle cond;
+    cudaGraphConditionalHandleCreate(&cond, graph, 1u, cudaGraphCondAssignDefault);
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = cond;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    cudaGraphAddNode(&node, graph, deps, nullptr, ndeps, &np);
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    cudaStreamBeginCaptureToGraph(s.aux, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+    iteration(s.aux, cond, 1);
+    cudaStreamEndCapture(s.aux, &body);
+    cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+  } else {
+    for (int it = 0; it < s.max_outer; ++it) iteration(st, 0, 0);
   }
   if (!s.ref) {
     cudaMemsetAsync(s.red + RED_P_SUM, 0, sizeof(double), st);
