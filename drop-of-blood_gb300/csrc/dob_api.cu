@@ -292,15 +292,7 @@ static dob_status one_step(dob_ctx* ctx, uint32_t flags, float* stage_ms) {
   return DOB_OK;
 }
 
-static dob_status finish_stats(dob_ctx* ctx, dob_step_stats* stats, int steps) {
-  if (!stats) return DOB_OK;
-  DevState& s = ctx->s;
-  double red[RED_COUNT];
-  unsigned int redu[REDU_COUNT];
-  launch_count_alive(s, s.redu + REDU_ALIVE, ctx->stream);
-  CK(cudaMemcpyAsync(red, s.red, sizeof(red), cudaMemcpyDeviceToHost, ctx->stream));
-  CK(cudaMemcpyAsync(redu, s.redu, sizeof(redu), cudaMemcpyDeviceToHost, ctx->stream));
-  CK(cudaStreamSynchronize(ctx->stream));
+static void fill_stats(dob_ctx* ctx, const double* red, const unsigned int* redu, dob_step_stats* stats, int steps) {
   stats->struct_size = sizeof(dob_step_stats);
   stats->steps_done = steps;
   const int levels_cycles = ctx->cfg.mg_cycles;
@@ -317,6 +309,18 @@ static dob_status finish_stats(dob_ctx* ctx, dob_step_stats* stats, int steps) {
   memcpy(&md, &redu[REDU_MAXDIV], 4);
   stats->max_div = (double)md;
   stats->parcels_alive = redu[REDU_ALIVE];
+}
+
+static dob_status finish_stats(dob_ctx* ctx, dob_step_stats* stats, int steps) {
+  if (!stats) return DOB_OK;
+  DevState& s = ctx->s;
+  double red[RED_COUNT];
+  unsigned int redu[REDU_COUNT];
+  launch_count_alive(s, s.redu + REDU_ALIVE, ctx->stream);
+  CK(cudaMemcpyAsync(red, s.red, sizeof(red), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(redu, s.redu, sizeof(redu), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  fill_stats(ctx, red, redu, stats, steps);
   return DOB_OK;
 }
 
@@ -505,6 +509,11 @@ void dob_destroy(dob_ctx* ctx) {
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   for (int k = 0; k <= DOB_STAGE_COUNT; ++k)
     if (ctx->stage_ev[k]) cudaEventDestroy(ctx->stage_ev[k]);
+  for (auto& a : ctx->async_slots) {
+    if (a.red) cudaFreeHost(a.red);
+    if (a.redu) cudaFreeHost(a.redu);
+    if (a.done) cudaEventDestroy(a.done);
+  }
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   if (ctx->aux_stream) cudaStreamDestroy(ctx->aux_stream);
   delete ctx;
@@ -745,6 +754,39 @@ dob_status dob_step(dob_ctx* ctx, int nsteps, uint32_t flags, dob_step_stats* st
   return DOB_OK;
 }
 
+dob_status dob_step_async(dob_ctx* ctx, int slot) {
+  if (!ctx || slot < 0 || slot >= 8) return DOB_EINVAL;
+  if (ctx->cfg.bc_mode == DOB_BC_REFERENCE && !isfinite(ctx->U[38]))
+    return fail(ctx, DOB_EINVAL, "dob_step_async", "non-finite dt");
+  dob_ctx::AsyncSlot& a = ctx->async_slots[slot];
+  if (a.pending) return fail(ctx, DOB_ESTATE, "dob_step_async", "result slot still pending");
+  if (!a.red) {
+    CK(cudaMallocHost((void**)&a.red, RED_COUNT * sizeof(double)));
+    CK(cudaMallocHost((void**)&a.redu, REDU_COUNT * sizeof(unsigned int)));
+    CK(cudaEventCreateWithFlags(&a.done, cudaEventDisableTiming));
+  }
+  dob_status st = one_step(ctx, DOB_STEP_STATS, nullptr);
+  if (st != DOB_OK) return st;
+  DevState& s = ctx->s;
+  launch_count_alive(s, s.redu + REDU_ALIVE, ctx->stream);
+  CK(cudaMemcpyAsync(a.red, s.red, RED_COUNT * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(a.redu, s.redu, REDU_COUNT * sizeof(unsigned int), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaEventRecord(a.done, ctx->stream));
+  a.pending = true;
+  return DOB_OK;
+}
+
+dob_status dob_step_result(dob_ctx* ctx, int slot, dob_step_stats* stats) {
+  if (!ctx || !stats || slot < 0 || slot >= 8) return DOB_EINVAL;
+  dob_ctx::AsyncSlot& a = ctx->async_slots[slot];
+  if (!a.pending) return fail(ctx, DOB_ESTATE, "dob_step_result", "no step pending in this slot");
+  CK(cudaEventSynchronize(a.done));
+  a.pending = false;
+  memset(stats, 0, sizeof(*stats));
+  fill_stats(ctx, a.red, a.redu, stats, 1);
+  return DOB_OK;
+}
+
 dob_status dob_step_uniforms(dob_ctx* ctx, const float* blocks, int nsteps, uint32_t flags, dob_step_stats* stats) {
   if (!ctx || (!blocks && nsteps) || nsteps < 0) return DOB_EINVAL;
   for (int k = 0; k < nsteps; ++k) {
@@ -805,7 +847,7 @@ dob_status dob_time_steps(dob_ctx* ctx, int nsteps, uint32_t flags, float* ms) {
   CK(cudaStreamSynchronize(ctx->stream));
   CK(cudaEventRecord(ctx->ev0, ctx->stream));
   for (int k = 0; k < nsteps; ++k) {
-    dob_status st = one_step(ctx, flags & ~(uint32_t)(DOB_STEP_STATS | DOB_STEP_TIMING), nullptr);
+    dob_status st = one_step(ctx, flags & ~(uint32_t)DOB_STEP_TIMING, nullptr);
     if (st != DOB_OK) return st;
   }
   CK(cudaEventRecord(ctx->ev1, ctx->stream));

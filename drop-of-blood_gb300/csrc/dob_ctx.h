@@ -48,6 +48,13 @@ struct dob_ctx {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t stage_ev[DOB_STAGE_COUNT + 1];
   dob::AdjCtx* adj = nullptr;
+  // results of dob_step_async: pinned statistics slots and their events
+  struct AsyncSlot {
+    double* red = nullptr;        // pinned, RED_COUNT
+    unsigned int* redu = nullptr; // pinned, REDU_COUNT
+    cudaEvent_t done = nullptr;
+    bool pending = false;
+  } async_slots[8];
 };
 
 namespace dob {

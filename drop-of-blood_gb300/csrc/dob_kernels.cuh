@@ -130,6 +130,23 @@ __device__ __forceinline__ void block_sum_atomic(double v, double* out) {
     if (tid == 0 && s != 0.0) atomicAdd(out, s);
   }
 }
+// Sum of non-negative FP32 values `v` over the block into *out: FP32 within
+// each warp, FP64 across warps (one FP64 operation per warp, not per thread:
+// GB300's FP64 rate is a small fraction of its FP32 rate).
+__device__ __forceinline__ void block_sum_atomic_f(float v, double* out) {
+  __shared__ double part[32];
+  const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  const int nthreads = blockDim.x * blockDim.y * blockDim.z;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((tid & 31) == 0) part[tid >> 5] = (double)v;
+  __syncthreads();
+  if (tid == 0) {
+    double s = 0.0;
+    for (int w = 0; w < (nthreads + 31) / 32; ++w) s += part[w];
+    if (s != 0.0) atomicAdd(out, s);
+  }
+}
 // Max of non-negative floats via their bit patterns.
 __device__ __forceinline__ void block_max_atomic(float v, unsigned int* out) {
   __shared__ float part[32];

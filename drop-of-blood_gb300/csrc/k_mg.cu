@@ -25,9 +25,9 @@
 //                       shared memory, reads the neighbour slabs' boundary
 //                       planes through distributed shared memory, and the
 //                       half-sweeps are separated by hardware cluster barriers
-//   k_defect            FP64 norm of the residual of the FP32 pressure (statistics)
-//   k_defect_df         mixed precision: residual of the double-float pressure
-//                       (FP32 pairs, error-free transformations), its max and norm
+//   k_defect_df         residual of the pressure (double-float in the mixed
+//                       mode) formed with error-free FP32 transformations, its
+//                       max and norm (statistics and the mixed defect loop)
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
@@ -506,13 +506,16 @@ __global__ void k_sum64(const float* __restrict__ a, size_t n, double* __restric
     two_sum_acc(hi, lo, a[i]);
   block_sum_atomic((double)hi + (double)lo, out);
 }
+// sum of squares: per-thread error-free FP32 accumulation, FP64 across threads
 __global__ void k_sumsq64(const float* __restrict__ a, size_t n, double* __restrict__ out) {
-  double s = 0.0;
+  float hi = 0.0f, lo = 0.0f;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    const double v = (double)a[i];
-    s += v * v;
+    const float v = a[i];
+    const float sq = v * v;
+    two_sum_acc(hi, lo, sq);
+    lo += fmaf(v, v, -sq);  // the rounding error of the square
   }
-  block_sum_atomic(s, out);
+  block_sum_atomic((double)hi + (double)lo, out);
 }
 // a[i] -= mean, with the mean summed in FP64 and applied in FP32.
 __global__ void k_sub_mean(float* __restrict__ a, size_t n, const double* __restrict__ sum) {
@@ -529,32 +532,6 @@ __global__ void k_sub_mean(float* __restrict__ a, size_t n, const double* __rest
   }
   for (size_t i = 4 * n4 + blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     a[i] = a[i] - mean;
-}
-
-// r = b - A p in FP64 (FP32 inputs, split layout); optionally stored as BF16
-// (split layout); ||r||^2 summed.
-__global__ void __launch_bounds__(256) k_defect(Grid d, float h2f, int ref, const float* __restrict__ p,
-                                                const float* __restrict__ b, __nv_bfloat16* __restrict__ r_out,
-                                                double* __restrict__ norm2, const unsigned int* __restrict__ skip) {
-  if (skip_now(skip)) return;
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = blockIdx.y * blockDim.y + threadIdx.y;
-  const int z = blockIdx.z;
-  double rr = 0.0;
-  if (x < d.nx && y < d.ny) {
-    double sumN = 0.0, diag = ref ? 1.0 : 0.0;
-    if (x > 0) { sumN += (double)rb_at(p, d, x - 1, y, z); diag += 1.0; }
-    if (x < d.nx - 1) { sumN += (double)rb_at(p, d, x + 1, y, z); diag += 1.0; }
-    if (y > 0) { sumN += (double)rb_at(p, d, x, y - 1, z); diag += 1.0; }
-    if (y < d.ny - 1) { sumN += (double)rb_at(p, d, x, y + 1, z); if (!ref) diag += 1.0; }
-    if (z > 0) { sumN += (double)rb_at(p, d, x, y, z - 1); diag += 1.0; }
-    if (z < d.nz - 1) { sumN += (double)rb_at(p, d, x, y, z + 1); diag += 1.0; }
-    const size_t i = rb_index(d, x, y, z);
-    const double r = (double)b[i] - (sumN - diag * (double)p[i]) / (double)h2f;
-    if (r_out) r_out[i] = __float2bfloat16_rn((float)r);
-    rr = r * r;
-  }
-  if (norm2) block_sum_atomic(rr, norm2);
 }
 
 // ---- mixed precision: double-float pressure --------------------------------------------
@@ -584,8 +561,7 @@ __global__ void __launch_bounds__(256) k_defect_df(Grid d, int ref, const float*
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int z = blockIdx.z;
-  double rr = 0.0;
-  float ra = 0.0f;
+  float rr = 0.0f, ra = 0.0f;
   if (x < d.nx && y < d.ny) {
     float sh = 0.0f, sl = 0.0f, low = 0.0f, diag = ref ? 1.0f : 0.0f;
     auto add = [&](int xx, int yy, int zz) {
@@ -593,7 +569,7 @@ __global__ void __launch_bounds__(256) k_defect_df(Grid d, int ref, const float*
       float e;
       two_sum(sh, p[j], sh, e);
       sl += e;
-      low += plo[j];
+      if (plo) low += plo[j];
       diag += 1.0f;
     };
     if (x > 0) add(x - 1, y, z);
@@ -604,7 +580,7 @@ __global__ void __launch_bounds__(256) k_defect_df(Grid d, int ref, const float*
       float e;
       two_sum(sh, p[j], sh, e);
       sl += e;
-      low += plo[j];
+      if (plo) low += plo[j];
       if (!ref) diag += 1.0f;
     }
     if (z > 0) add(x, y, z - 1);
@@ -615,13 +591,13 @@ __global__ void __launch_bounds__(256) k_defect_df(Grid d, int ref, const float*
     const float perr = fmaf(diag, pc, -prod);  // diag * pc = prod + perr exactly
     float th, te;
     two_sum(sh, -prod, th, te);                // A p = th + (te + sl - perr + low - diag plo)
-    const float tl = ((te + sl) - perr) + (low - diag * plo[i]);
+    const float tl = ((te + sl) - perr) + (low - (plo ? diag * plo[i] : 0.0f));
     const float r = (b[i] - th) - tl;
     if (r_out) r_out[i] = r;
-    rr = (double)r * (double)r;
+    rr = r * r;
     ra = fabsf(r);
   }
-  if (norm2) block_sum_atomic(rr, norm2);
+  if (norm2) block_sum_atomic_f(rr, norm2);
   if (maxbits) block_max_atomic(ra, maxbits);
 }
 
@@ -919,12 +895,9 @@ double smoother_pass(const DevState& s, cudaStream_t st) {
 }
 
 void launch_residual_norm(const DevState& s, double* out, cudaStream_t st) {
+  // the error-free residual of p (+ plo in the mixed mode) in FP32 arithmetic
   cudaMemsetAsync(out, 0, sizeof(double), st);
-  if (s.plo) {
-    k_defect_df<<<g_cells(s.g), b_cells(), 0, st>>>(s.g, s.ref, s.p, s.plo, s.rhs, nullptr, out, nullptr, nullptr);
-  } else {
-    k_defect<<<g_cells(s.g), b_cells(), 0, st>>>(s.g, s.lv[0].h2, s.ref, s.p, s.rhs, nullptr, out, nullptr);
-  }
+  k_defect_df<<<g_cells(s.g), b_cells(), 0, st>>>(s.g, s.ref, s.p, s.plo, s.rhs, nullptr, out, nullptr, nullptr);
 }
 
 // Mixed precision: defect correction.  Each outer iteration forms the

@@ -44,6 +44,8 @@ SIGNATURES = {
     "dob_load_state": (C.c_int, [P, C.c_int]),
     "dob_eval_math": (C.c_int, [C.c_int, FP, FP, FP, C.c_uint32]),
     "dob_pressure_solve_noalloc": (C.c_int, [C.POINTER(abi.DobConfig), P, P, P]),
+    "dob_step_async": (C.c_int, [P, C.c_int]),
+    "dob_step_result": (C.c_int, [P, C.c_int, C.POINTER(abi.DobStepStats)]),
     "dob_adjoint_stage": (C.c_int, [P, C.c_int]),
     "dob_tape_forward": (C.c_int, [P, C.c_int, C.c_int]),
     "dob_tape_backward": (C.c_int, [P, FP, C.c_size_t]),

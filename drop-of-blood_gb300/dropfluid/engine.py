@@ -119,12 +119,38 @@ class DropFluid:
         self._ck(self._L.dob_step(self._h, int(n), flags, C.byref(st) if want else None), "dob_step")
         if not want:
             return None
+        return self._stats_dict(st)
+
+    @staticmethod
+    def _stats_dict(st):
         return {
             "steps_done": st.steps_done, "vcycles": st.vcycles, "outer_iters": st.outer_iters,
             "rhs_l2": st.rhs_l2, "residual_l2": st.residual_l2, "max_div": st.max_div,
             "parcels_alive": st.parcels_alive,
             "stage_ms": {abi.STAGE_NAMES[k]: st.stage_ms[k] for k in range(abi.STAGE_COUNT)},
         }
+
+    def step_async(self, slot):
+        """Enqueue one step with statistics into result slot 0..7."""
+        self._ck(self._L.dob_step_async(self._h, int(slot)), "dob_step_async")
+
+    def step_result(self, slot):
+        """Wait for the step of `slot` and return its statistics."""
+        st = abi.DobStepStats()
+        st.struct_size = C.sizeof(abi.DobStepStats)
+        self._ck(self._L.dob_step_result(self._h, int(slot), C.byref(st)), "dob_step_result")
+        return self._stats_dict(st)
+
+    def run_pipelined(self, n, depth=2):
+        """n steps, each step's statistics read back while the next runs."""
+        out = []
+        for k in range(n):
+            self.step_async(k % 8)
+            if k >= depth - 1:
+                out.append(self.step_result((k - depth + 1) % 8))
+        for k in range(max(0, n - depth + 1), n):
+            out.append(self.step_result(k % 8))
+        return out
 
     def step_uniforms(self, blocks, stats=False):
         b = np.ascontiguousarray(blocks, dtype=np.float32).reshape(-1, 128)

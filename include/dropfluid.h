@@ -251,6 +251,16 @@ dob_status dob_get_field(dob_ctx* ctx, int field, void* host, size_t bytes);
    count like BloodDropEngine.ts:1832-1840. */
 dob_status dob_step(dob_ctx* ctx, int nsteps, uint32_t flags, dob_step_stats* stats);
 
+/* Pipelined stepping: dob_step_async enqueues one step with statistics
+   (as DOB_STEP_STATS) whose results land in pinned result slot `slot`
+   (0..7) and returns without waiting; dob_step_result waits for that step
+   and fills *stats.  Keeping one or two steps in flight hides the host's
+   wait behind the next step's device work (the reference reads its GPU
+   timestamps back asynchronously the same way, BloodDropEngine.ts:2400-2456).
+   A slot must be read back before it is reused. */
+dob_status dob_step_async(dob_ctx* ctx, int slot);
+dob_status dob_step_result(dob_ctx* ctx, int slot, dob_step_stats* stats);
+
 /* Reference mode: nsteps substeps, each with its own 128-float block
    (the reference's multi-substep staging path, BloodDropEngine.ts:2634-2651). */
 dob_status dob_step_uniforms(dob_ctx* ctx, const float* blocks, int nsteps,
@@ -259,7 +269,8 @@ dob_status dob_step_uniforms(dob_ctx* ctx, const float* blocks, int nsteps,
 /* Run exactly one stage of the step on the current state (parity tests). */
 dob_status dob_run_stage(dob_ctx* ctx, int stage);
 
-/* Device time of nsteps steps (dob_step with `flags`), measured with CUDA
+/* Device time of nsteps steps (dob_step with `flags`; with DOB_STEP_STATS
+   the statistics kernels run but nothing is read back), measured with CUDA
    events on the context's stream; replaces the reference's per-pass GPU
    timestamp queries (BloodDropEngine.ts:2400-2456). */
 dob_status dob_time_steps(dob_ctx* ctx, int nsteps, uint32_t flags, float* ms);

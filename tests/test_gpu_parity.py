@@ -521,3 +521,28 @@ def test_pressure_solve_parity_wide_tiles(both, mode):
         e.run_stage(abi.STAGE_MAC_RHS)
         e.run_stage(abi.STAGE_PRESSURE_SOLVE)
     assert rel_l2(g.get_field(abi.FIELD_PRESSURE), o.get_field(abi.FIELD_PRESSURE)) < STAGE_TOL
+
+
+def test_pipelined_steps_match_synchronous(gpu_lib):
+    """dob_step_async / dob_step_result give the same steps and statistics
+    as dob_step with statistics, and refuse a slot that is still pending or
+    was never filled."""
+    abi = _abi()
+    from dropfluid import DropFluid, DropFluidError, scenes
+    sc = scenes.box48()
+    a, b = DropFluid(sc.config), DropFluid(sc.config)
+    for e in (a, b):
+        sc.release(e, 0)
+    sync = [a.step(1, stats=True) for _ in range(5)]
+    piped = b.run_pipelined(5, depth=2)
+    assert [s["max_div"] for s in sync] == [s["max_div"] for s in piped]
+    assert [s["parcels_alive"] for s in sync] == [s["parcels_alive"] for s in piped]
+    assert bits_equal(a.get_field(abi.FIELD_VEL_V), b.get_field(abi.FIELD_VEL_V))
+    with pytest.raises(DropFluidError):
+        b.step_result(3)  # nothing pending there
+    b.step_async(0)
+    with pytest.raises(DropFluidError):
+        b.step_async(0)  # still pending
+    b.step_result(0)
+    a.close()
+    b.close()
