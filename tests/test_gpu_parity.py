@@ -501,8 +501,11 @@ def test_error_paths(gpu_lib):
 
 @pytest.mark.parametrize("mode", ["box", "ref"])
 def test_pressure_solve_parity_wide_tiles(both, mode):
-    """Grids wide enough for the 64x16 smoother tiles and several z-chunks:
-    the temporally blocked smoother reproduces the oracle's in-place sweeps."""
+    """A wide, deep grid (128x64x96, five grids in the closed box): the
+    4-cells-per-thread smoother on levels whose rows fill several warps, the
+    paired transfers and the exact coarsest solve (closed box) or the
+    cluster's coarse sweeps (reference mode) reproduce the oracle's
+    in-place sweeps."""
     abi = _abi()
     if mode == "box":
         cfg = box_config(n=(128, 64, 96))
