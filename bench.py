@@ -4,10 +4,12 @@
 Workload (one "step" = one full fluid step of the scene, inputs resident in
 HBM): the 192x256x192 closed-box drop scene with three r=12 drops released
 at steps 0/40/80 and 393216 parcels, FP32 storage, 4 V-cycles of 2+2
-red-black sweeps on 4 grids per step (dropfluid.scenes.box192).  The
-mixed-precision variant of the same scene is measured beside it.
+red-black sweeps per step on 6 grids with an exact solve of the 6x8x6
+coarsest grid (dropfluid.scenes.box192).  The mixed-precision variant of the
+same scene and the discrete adjoint are measured beside it.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+  python bench.py --accuracy      # FP32 and mixed vs an FP64 run at steps 50/100/200
 
 Multi-GPU: the step does not exchange data between replicas on this pool
 (one GPU per box): N ranks run N independent replicas ("scaling": "weak");
@@ -280,6 +282,56 @@ def adjoint_leg(fd_dirs: int = 16):
     return out
 
 
+ACC_STEPS = (50, 100, 200)
+ACC_FIELDS = ("u", "v", "w", "p", "dye")
+
+
+def accuracy_run():
+    """FP32 and mixed-precision (||b - Ap|| / ||b|| <= 1e-8) runs of the
+    box192 scene on the GPU against an FP64 run of the same seed: the oracle
+    in double arithmetic with 12 V-cycles per step (a pressure solve
+    converged to the FP64 floor: the V-cycle contracts 0.1 per cycle), on the
+    host cores.  Relative L2 errors of u, v, w, p and dye at steps 50, 100
+    and 200."""
+    import numpy as np
+    import oracle
+    from dropfluid import DropFluid, abi, scenes
+    F = {"u": abi.FIELD_VEL_U, "v": abi.FIELD_VEL_V, "w": abi.FIELD_VEL_W, "p": abi.FIELD_PRESSURE,
+         "dye": abi.FIELD_CONC}
+
+    def trajectory(scene, eng):
+        snaps, k = {}, 0
+        for s in ACC_STEPS:
+            run_scene_steps(scene, eng, k, s - k, timed=False)
+            k = s
+            get = getattr(eng, "get_field64", eng.get_field)  # the oracle's double fields unrounded
+            snaps[s] = {n: np.asarray(get(f), np.float64) for n, f in F.items()}
+        return snaps
+
+    t0 = time.perf_counter()
+    runs = {}
+    for name, sc in (("fp32", scenes.box192()), ("mixed_rel_1e-8", scenes.box192_mixed_1e8())):
+        with DropFluid(sc.config) as eng:
+            runs[name] = trajectory(sc, eng)
+    t_gpu = time.perf_counter() - t0
+    oracle.build()
+    oracle.set_threads(os.cpu_count() or 1)
+    ref_sc = scenes.box192()
+    ref_sc.config.mg_cycles = 12
+    t0 = time.perf_counter()
+    ref = trajectory(ref_sc, oracle.OracleSim(ref_sc.config, fp64=True))
+    t_cpu = time.perf_counter() - t0
+
+    def rel(a, b):
+        return float(np.linalg.norm((a - b).ravel()) / max(np.linalg.norm(b.ravel()), 1e-300))
+    out = {name: {str(s): {n: rel(r[s][n], ref[s][n]) for n in ACC_FIELDS} for s in ACC_STEPS}
+           for name, r in runs.items()}
+    return {"accuracy_vs_fp64": out, "steps": list(ACC_STEPS),
+            "reference": "FP64 oracle (CPU, double arithmetic), same scene and seed, 12 V-cycles per step",
+            "metric": "relative L2 error vs the FP64 run; pressure mean-free (closed box)",
+            "gpu_s": t_gpu, "fp64_cpu_s": t_cpu}
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return 0
@@ -293,7 +345,8 @@ def run_reference(args, rank, world):
         "steps": steps, "warmup": 1, "ms_per_step": 1000.0 / value, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "box192: 192x256x192 closed-box MAC step, 3 drops r=12, 393216 parcels, FP32, "
-                               "4 V-cycles of 2+2 RBGS on 4 grids (dropfluid.scenes.box192)",
+                               "4 V-cycles of 2+2 RBGS on 6 grids, exact 6x8x6 coarsest solve "
+                               "(dropfluid.scenes.box192)",
                    "grid": [192, 256, 192], "parallelism": "replicas"},
         "cpu_baseline": {"value": value, "unit": "steps/s", "cores": threads, "kind": "port",
                          "sample": f"{steps} steps of box192 after drop 0 released and 1 warm-up step "
@@ -315,6 +368,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--accuracy", action="store_true",
+                    help="error of the FP32 and mixed runs against an FP64 run at steps 50/100/200, then exit")
     ap.add_argument("--profile-run", action="store_true",
                     help="run only the FP32 scene (warm-up + steps, untimed) and exit: the command "
                          "the ncu launch lists and kernel captures are taken with")
@@ -328,6 +383,10 @@ def main():
 
     from dropfluid import DropFluid, abi, build, scenes
     build.build()
+    if args.accuracy:
+        if rank == 0:
+            print(json.dumps(accuracy_run()), flush=True)
+        return 0
     dist = Dist(world)
 
     # ---- FP32 drop-in step (the headline) ----------------------------------------------------
@@ -380,9 +439,9 @@ def main():
 
     # ---- projection accuracy per step, and the mixed-precision solve ---------------------------
     # The timed window is replayed from a snapshot with statistics on, so the
-    # divergence of every timed step is known.  FP32 with a fixed 4 V-cycles
-    # stalls near max |div| dt/dx ~ 1e-5 (the FP32 rounding of a pressure of
-    # ~1e3); the mixed solve iterates each step until max |div| <= 1e-5.
+    # divergence of every timed step is known.  The mixed solve iterates each
+    # step until max |div| dt/dx <= 1e-5 (and, for mixed_rel_1e-8, until
+    # ||b - Ap|| / ||b|| <= 1e-8, below the FP32 pressure's rounding floor).
     eng.close()
     mixed = None
     if not args.no_mixed:
@@ -418,7 +477,7 @@ def main():
             "speedup_vs_fp32": mx["value"] / fp32_w["value"],
             "speedup_vs_fp32_8cycles": mx["value"] / fp32_8["value"],
             "precision": "FP16 dye; pressure as an FP32 pair (double-float) corrected by an error-free residual "
-                         "loop, 1 V-cycle per iteration with BF16 levels 2-3; stop at max |div| dt/dx <= 1e-5",
+                         "loop, 1 V-cycle per iteration with BF16 levels >= 2; stop at max |div| dt/dx <= 1e-5",
             "fp32_4cycles": fp32_w, "fp32_8cycles": fp32_8,
             "mixed_rel_1e-8": m8,
         })
@@ -444,7 +503,8 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "box192: 192x256x192 closed-box MAC step, 3 drops r=12 released at "
                                    "steps 0/40/80, 393216 parcels, FP32 storage, 4 V-cycles of 2+2 RBGS on "
-                                   "4 grids, Casson tau_y=0.005 mu_p=1e-3, dx=1 dt=0.02",
+                                   "6 grids with an exact 6x8x6 coarsest solve, Casson tau_y=0.005 "
+                                   "mu_p=1e-3, dx=1 dt=0.02",
                        "grid": [192, 256, 192], "parallelism": "replicas" if world > 1 else "single",
                        "l2": "inputs larger than L2 (>=12 fields x 37.7 MB per step), no flush",
                        "timed": "device time of K graph-replayed steps (CUDA events on the library stream); "

@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include <utility>
 #include <vector>
 
 #include "../../include/dropfluid.h"
@@ -116,6 +117,33 @@ __device__ __forceinline__ float warp_maxf(float v) {
   for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
   return v;
 }
+// ---- programmatic dependent launch -------------------------------------------
+// The multigrid kernels form long chains of small dependent launches (about
+// 50 per V-cycle, most under 5 us).  Launched with launch_pdl, a kernel may
+// be scheduled while its predecessor still runs: pdl_wait() (first statement
+// of such a kernel, before any memory access) blocks until the predecessor
+// grid has completed and its writes are visible, and pdl_trigger() lets the
+// successor's launch begin once every CTA of this grid has started.  Both are
+// no-ops for a kernel launched without the attribute.  The wait is the
+// hardware grid dependency, not a spin: it ends when the predecessor ends.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+template <class... KArgs, class... Args>
+inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                              Args&&... args) {
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
 // Sum `v` over the block and add it to *out with one FP64 atomic per block.
 __device__ __forceinline__ void block_sum_atomic(double v, double* out) {
   __shared__ double part[32];

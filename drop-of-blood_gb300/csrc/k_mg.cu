@@ -75,9 +75,15 @@ __device__ __forceinline__ float rb_at(const T* a, const Grid& d, int x, int y, 
 }
 
 // One colour of RBGS (createMgRbgsShader, fluid.ts:605-681), in place.
+// zoth: the other colour is zero (the first half-sweep from a zero guess), so
+// its values are not read; the result has the same bits as with zeroed
+// memory.
 template <class T>
-__global__ void __launch_bounds__(256) k_rbgs_split(Grid d, int color, float h2, int ref, T* __restrict__ a,
-                                                    const T* __restrict__ b, const unsigned int* __restrict__ skip) {
+__global__ void __launch_bounds__(256) k_rbgs_split(Grid d, int color, float h2, int ref, int zoth,
+                                                    T* __restrict__ a, const T* __restrict__ b,
+                                                    const unsigned int* __restrict__ skip) {
+  pdl_wait();
+  pdl_trigger();
   if (skip_now(skip)) return;
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
@@ -92,7 +98,13 @@ __global__ void __launch_bounds__(256) k_rbgs_split(Grid d, int color, float h2,
   const size_t i = r + k;
   const float bv = ldv(b + (size_t)color * half + i);
   float val;
-  if (x > 0 && x < d.nx - 1 && y > 0 && y < d.ny - 1 && z > 0 && z < d.nz - 1) {
+  if (zoth) {
+    const bool in = x > 0 && x < d.nx - 1 && y > 0 && y < d.ny - 1 && z > 0 && z < d.nz - 1;
+    const float diag = (ref ? 1.0f : 0.0f) + (x > 0 ? 1.0f : 0.0f) + (x < d.nx - 1 ? 1.0f : 0.0f) +
+                       (y > 0 ? 1.0f : 0.0f) + ((y < d.ny - 1 && !ref) ? 1.0f : 0.0f) + (z > 0 ? 1.0f : 0.0f) +
+                       (z < d.nz - 1 ? 1.0f : 0.0f);
+    val = in ? (0.0f - h2 * bv) * (1.0f / 6.0f) : (0.0f - h2 * bv) / diag;
+  } else if (x > 0 && x < d.nx - 1 && y > 0 && y < d.ny - 1 && z > 0 && z < d.nz - 1) {
     // interior: six neighbours, diagonal 6 in both boundary modes
     const size_t sz = (size_t)d.ny * hx;
     const float sumN = ((((ldv(oth + r + ((x - 1) >> 1)) + ldv(oth + r + ((x + 1) >> 1))) + ldv(oth + i - hx)) +
@@ -137,67 +149,85 @@ __device__ __forceinline__ float f4get(const float4& v, int j) {
   return j == 0 ? v.x : (j == 1 ? v.y : (j == 2 ? v.z : v.w));
 }
 
-// One colour of RBGS, four cells per thread (rows with nx % 8 == 0).
+// One colour of RBGS, four cells per thread and ZC planes per thread (rows
+// with nx % 8 == 0, nz % ZC == 0).
 // Block (bx, by): threadIdx.x runs over the Q = nx/8 quads of a row and
 // threadIdx.y over rows, so a warp holds whole rows back to back with no idle
-// lanes.  Boundaries are handled without divergence: a missing neighbour is
-// loaded from a clamped in-range address and enters the sum with weight 0
-// (adding an exact 0 leaves the sum unchanged, so the sum equals the
-// neighbour-skipping evalMgStencil order); only lanes whose diagonal is not 6
-// take the short IEEE-division branch.  Offsets are 32-bit (split halves have
-// fewer than 2^30 words).
-template <class T>
-__global__ void __launch_bounds__(256) k_rbgs_v4(Grid d, int color, float h2, int ref, T* __restrict__ a,
-                                                 const T* __restrict__ b, const unsigned int* __restrict__ skip) {
+// lanes; blockIdx.z picks ZC consecutive planes.  The other colour's words
+// k0..k0+3 of row (y, z') are the x-neighbour source of plane z' and the
+// z-neighbours of planes z' - 1 and z' + 1, so marching over ZC planes loads
+// each of them once: per plane one centre vector, two y-neighbour vectors,
+// one scalar and the right-hand side instead of six vectors and a scalar, and
+// every thread has ZC planes of loads in flight.  Boundaries are handled
+// without divergence: a missing neighbour is loaded from a clamped in-range
+// address and enters the sum with weight 0 (adding an exact 0 leaves the sum
+// unchanged, so the sum equals the neighbour-skipping evalMgStencil order);
+// only lanes whose diagonal is not 6 take the short IEEE-division branch.
+// Offsets are 32-bit (split halves have fewer than 2^30 words).  `own` and
+// `oth` are the two halves of the level's array (disjoint).  ZOTH: the other
+// colour is zero (first half-sweep from a zero guess) and is not read.
+template <class T, int ZC, bool ZOTH>
+__global__ void __launch_bounds__(256) k_rbgs_v4(Grid d, int color, float h2, int ref, T* __restrict__ own,
+                                                 const T* __restrict__ oth, const T* __restrict__ bown,
+                                                 const unsigned int* __restrict__ skip) {
+  pdl_wait();
+  pdl_trigger();
   if (skip_now(skip)) return;
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
-  const int z = blockIdx.z;
+  const int z0 = blockIdx.z * ZC;
   const uint32_t hx = (uint32_t)d.nx >> 1;
   const uint32_t k0 = 4u * (uint32_t)q;
   if (k0 >= hx || y >= d.ny) return;
-  const int p = (y + z + color) & 1;
-  const uint32_t half = (uint32_t)(d.n() >> 1);
   const uint32_t sz = (uint32_t)d.ny * hx;
-  const uint32_t r = (uint32_t)z * sz + (uint32_t)y * hx;
-  T* own = a + (color ? half : 0u);
-  const T* oth = a + (color ? 0u : half);
-  // neighbour rows, clamped to the own row when absent (weight 0)
-  const bool has_ym = y > 0, has_yp = y < d.ny - 1, has_zm = z > 0, has_zp = z < d.nz - 1;
-  const uint32_t rym = has_ym ? r - hx : r, ryp = has_yp ? r + hx : r;
-  const uint32_t rzm = has_zm ? r - sz : r, rzp = has_zp ? r + sz : r;
-  const float4 bv = Vec4Ld<T>::ld(b + (color ? half : 0u) + r + k0);
-  const float4 cm = Vec4Ld<T>::ld(oth + r + k0);  // words k0..k0+3 of the other colour, same row
-  const float4 ym = Vec4Ld<T>::ld(oth + rym + k0), yp = Vec4Ld<T>::ld(oth + ryp + k0);
-  const float4 zm = Vec4Ld<T>::ld(oth + rzm + k0), zp = Vec4Ld<T>::ld(oth + rzp + k0);
-  // the word outside the vector: k0-1 (p = 0) or k0+4 (p = 1), absent at the row ends
-  const bool has_ex = p == 0 ? k0 > 0 : k0 + 4 < hx;
-  const uint32_t kex = p == 0 ? (has_ex ? k0 - 1 : k0) : (has_ex ? k0 + 4 : k0 + 3);
-  const float ex = ldv(oth + r + kex);
-  const float wex = has_ex ? 1.0f : 0.0f;
+  const uint32_t r0 = (uint32_t)z0 * sz + (uint32_t)y * hx + k0;
+  const bool has_ym = y > 0, has_yp = y < d.ny - 1;
+  const bool has_zlo = z0 > 0, has_zhi = z0 + ZC < d.nz;
+  const uint32_t oym = has_ym ? hx : 0u, oyp = has_yp ? hx : 0u;
+  // the word outside the vector: k0-1 (parity 0) or k0+4 (parity 1), absent at the row ends
+  const bool has_e0 = k0 > 0, has_e1 = k0 + 4 < hx;
+  const uint32_t ke0 = has_e0 ? k0 - 1 : k0, ke1 = has_e1 ? k0 + 4 : k0 + 3;
   const float wym = has_ym ? 1.0f : 0.0f, wyp = has_yp ? 1.0f : 0.0f;
-  const float wzm = has_zm ? 1.0f : 0.0f, wzp = has_zp ? 1.0f : 0.0f;
-  // diagonal without the x neighbours: y-, z-, z+ faces that exist, plus the
-  // +y face (always counted with the reference's Dirichlet top)
-  const float dyz = (wym + wzm + wzp) + (ref ? 1.0f : wyp);
-  float res[4];
+  const float dy = wym + (ref ? 1.0f : wyp);  // +y face always counted with the Dirichlet top
+  const int p0 = (y + z0 + color) & 1;
+  const float4 zero4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  float4 C[ZC + 2];  // C[i + 1] = other colour, plane z0 + i, words k0..k0+3
+  C[0] = ZOTH ? zero4 : Vec4Ld<T>::ld(oth + (has_zlo ? r0 - sz : r0));
 #pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    const float xm = p == 0 ? (j == 0 ? ex : f4get(cm, j - 1)) : f4get(cm, j);
-    const float xp = p == 0 ? f4get(cm, j) : (j == 3 ? ex : f4get(cm, j + 1));
-    const float wxm = (p == 0 && j == 0) ? wex : 1.0f;
-    const float wxp = (p == 1 && j == 3) ? wex : 1.0f;
-    float sumN = wxm * xm;
-    sumN = fmaf(wxp, xp, sumN);
-    sumN = fmaf(wym, f4get(ym, j), sumN);
-    sumN = fmaf(wyp, f4get(yp, j), sumN);
-    sumN = fmaf(wzm, f4get(zm, j), sumN);
-    sumN = fmaf(wzp, f4get(zp, j), sumN);
-    const float diag = dyz + (wxm + wxp);
-    const float t = sumN - h2 * f4get(bv, j);
-    res[j] = diag == 6.0f ? t * (1.0f / 6.0f) : t / diag;
+  for (int i = 0; i < ZC; ++i) C[i + 1] = ZOTH ? zero4 : Vec4Ld<T>::ld(oth + r0 + i * sz);
+  C[ZC + 1] = ZOTH ? zero4 : Vec4Ld<T>::ld(oth + (has_zhi ? r0 + ZC * sz : r0 + (ZC - 1) * sz));
+#pragma unroll
+  for (int i = 0; i < ZC; ++i) {
+    const uint32_t r = r0 + i * sz;
+    const int p = p0 ^ (i & 1);
+    const float4 bv = Vec4Ld<T>::ld(bown + r);
+    const float4 ym = ZOTH ? zero4 : Vec4Ld<T>::ld(oth + r - oym);
+    const float4 yp = ZOTH ? zero4 : Vec4Ld<T>::ld(oth + r + oyp);
+    const float ex = ZOTH ? 0.0f : ldv(oth + r - k0 + (p == 0 ? ke0 : ke1));
+    const float wex = (p == 0 ? has_e0 : has_e1) ? 1.0f : 0.0f;
+    const float wzm = (i > 0 || has_zlo) ? 1.0f : 0.0f;
+    const float wzp = (i < ZC - 1 || has_zhi) ? 1.0f : 0.0f;
+    const float dyz = dy + (wzm + wzp);
+    const float4 cm = C[i + 1], zm = C[i], zp = C[i + 2];
+    float res[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const float xm = p == 0 ? (j == 0 ? ex : f4get(cm, j - 1)) : f4get(cm, j);
+      const float xp = p == 0 ? f4get(cm, j) : (j == 3 ? ex : f4get(cm, j + 1));
+      const float wxm = (p == 0 && j == 0) ? wex : 1.0f;
+      const float wxp = (p == 1 && j == 3) ? wex : 1.0f;
+      float sumN = wxm * xm;
+      sumN = fmaf(wxp, xp, sumN);
+      sumN = fmaf(wym, f4get(ym, j), sumN);
+      sumN = fmaf(wyp, f4get(yp, j), sumN);
+      sumN = fmaf(wzm, f4get(zm, j), sumN);
+      sumN = fmaf(wzp, f4get(zp, j), sumN);
+      const float diag = dyz + (wxm + wxp);
+      const float t = sumN - h2 * f4get(bv, j);
+      res[j] = diag == 6.0f ? t * (1.0f / 6.0f) : t / diag;
+    }
+    Vec4Ld<T>::st(own + r, make_float4(res[0], res[1], res[2], res[3]));
   }
-  Vec4Ld<T>::st(own + r + k0, make_float4(res[0], res[1], res[2], res[3]));
 }
 
 // ---- two coarse cells per thread (fine rows with nx % 4 == 0) ----------------------------
@@ -242,6 +272,8 @@ template <class T, class TC>
 __global__ void __launch_bounds__(256) k_residual_restrict2(Grid f, Grid c, float inv_h2, int ref,
                                                             const T* __restrict__ a, const T* __restrict__ b,
                                                             TC* __restrict__ bc, const unsigned int* __restrict__ skip) {
+  pdl_wait();
+  pdl_trigger();
   if (skip_now(skip)) return;
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   const int Y = blockIdx.y * blockDim.y + threadIdx.y;
@@ -324,6 +356,8 @@ __global__ void __launch_bounds__(256) k_residual_restrict2(Grid f, Grid c, floa
 template <class T, class TC>
 __global__ void __launch_bounds__(256) k_prolong_add2(Grid f, Grid c, int ref, T* __restrict__ a,
                                                       const TC* __restrict__ e, const unsigned int* __restrict__ skip) {
+  pdl_wait();
+  pdl_trigger();
   if (skip_now(skip)) return;
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   const int Y = blockIdx.y * blockDim.y + threadIdx.y;
@@ -389,27 +423,48 @@ __global__ void __launch_bounds__(256) k_prolong_add2(Grid f, Grid c, int ref, T
 }
 
 // Exact coarsest-grid solve e = M b with the dense symmetric inverse M
-// (n <= 1024 cells, one CTA of n threads): b is gathered into shared memory
-// in natural order, thread j forms row j (M is symmetric: column j, read
-// with consecutive threads on consecutive words).
+// (n <= 1024 cells).  CTA c forms rows 32c..32c+31 of e: b is gathered into
+// shared memory in natural order, lane l of warp w sums M[i][32c + l] b[i]
+// over i = w, w + 8, ... (M is symmetric, so column 32c + l is row 32c + l;
+// each warp reads 128 consecutive bytes per i), and the eight warps' partial
+// sums are added in shared memory.  n/32 CTAs read M (up to 4 MB, resident
+// in L2 across cycles) in parallel instead of one SM reading all of it.
 template <class T>
-__global__ void __launch_bounds__(1024) k_coarse_dense(Grid d, const float* __restrict__ M, int n,
-                                                       T* __restrict__ e, const T* __restrict__ b,
-                                                       const unsigned int* __restrict__ skip) {
+__global__ void __launch_bounds__(256) k_coarse_dense(Grid d, const float* __restrict__ M, int n,
+                                                      T* __restrict__ e, const T* __restrict__ b,
+                                                      const unsigned int* __restrict__ skip) {
+  pdl_wait();
+  pdl_trigger();
   if (skip_now(skip)) return;
-  extern __shared__ float sbv[];
-  const int j = threadIdx.x;
-  const int x = j % d.nx, y = (j / d.nx) % d.ny, z = j / (d.nx * d.ny);
-  const size_t rj = rb_index(d, x, y, z);
-  sbv[j] = ldv(b + rj);
+  extern __shared__ float sbv[];  // b in natural order (n), then 8 x 32 partial sums
+  float* part = sbv + n;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const int x = i % d.nx, y = (i / d.nx) % d.ny, z = i / (d.nx * d.ny);
+    sbv[i] = ldv(b + rb_index(d, x, y, z));
+  }
   __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int j = blockIdx.x * 32 + lane;
   float acc = 0.0f;
-  for (int i = 0; i < n; ++i) acc = fmaf(M[(size_t)i * n + j], sbv[i], acc);
-  stf(e + rj, acc);
+  if (j < n) {
+#pragma unroll 4
+    for (int i = w; i < n; i += 8) acc = fmaf(M[(size_t)i * n + j], sbv[i], acc);
+  }
+  part[w * 32 + lane] = acc;
+  __syncthreads();
+  if (w == 0 && j < n) {
+    float sum = part[lane];
+#pragma unroll
+    for (int k = 1; k < 8; ++k) sum += part[k * 32 + lane];
+    const int x = j % d.nx, y = (j / d.nx) % d.ny, z = j / (d.nx * d.ny);
+    stf(e + rb_index(d, x, y, z), sum);
+  }
 }
 
 template <class T>
 __global__ void k_fill_zero(T* __restrict__ a, size_t n, const unsigned int* __restrict__ skip) {
+  pdl_wait();
+  pdl_trigger();
   if (skip_now(skip)) return;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     a[i] = T(0.0f);
@@ -426,6 +481,8 @@ template <class T, int CS>
 __global__ void __cluster_dims__(CS, 1, 1) __launch_bounds__(512)
     k_coarse_cluster(Grid d, float h2, int ref, int sweeps, T* __restrict__ e, const T* __restrict__ b,
                      const unsigned int* __restrict__ skip) {
+  pdl_wait();
+  pdl_trigger();
   cg::cluster_group cl = cg::this_cluster();
   extern __shared__ float csm[];
   const int rank = (int)cl.block_rank();
@@ -735,7 +792,7 @@ static void restrict_level(const DevState& s, int l, const T* x, const T* b, TC*
                            cudaStream_t st) {
   const Grid f = s.lv[l].d, c = s.lv[l + 1].d;  // nx % 4 == 0 on every transfer level
   const dim3 bp = pair_block(c);
-  k_residual_restrict2<T, TC><<<pair_grid(c, bp), bp, 0, st>>>(f, c, 1.0f / s.lv[l].h2, s.ref, x, b, bc, skip);
+  launch_pdl(k_residual_restrict2<T, TC>, pair_grid(c, bp), bp, 0, st, f, c, 1.0f / s.lv[l].h2, s.ref, x, b, bc, skip);
 }
 static inline dim3 quad_grid(const Grid& d, const dim3& b) {
   const int q = d.nx / 8;
@@ -775,40 +832,75 @@ void launch_sumsq(const float* a, size_t n, double* out, int num_sms, cudaStream
   k_sumsq64<<<num_sms * 4, 256, 0, st>>>(a, n, out);
 }
 
+// One half-sweep of colour c on level l: k_rbgs_v4 on rows with nx % 8 == 0,
+// else the scalar kernel.  Planes per thread: the most of 4, 2, 1 that still
+// leaves two waves of 1024 threads per SM (measured at 192x256x192: 20.5 us
+// per red+black pass with 2 planes against 24.6 us with 1; at 96x128x96 one
+// plane per thread is fastest).  Every level has even dims, so nz % 2 == 0.
+// zoth: the other colour is zero and is not read.
+template <class T, bool ZOTH>
+static void half_sweep_v4(const DevState& s, const MgLevel& L, int c, T* own, const T* oth, const T* bown,
+                          const unsigned int* skip, cudaStream_t st) {
+  const dim3 bq = quad_block(L.d);
+  dim3 gq = quad_grid(L.d, bq);
+  const size_t threads = (L.d.n() >> 1) / 4, wave2 = (size_t)s.num_sms * 2048;
+  if (L.d.nz % 4 == 0 && threads / 4 >= wave2) {
+    gq.z = L.d.nz / 4;
+    launch_pdl(k_rbgs_v4<T, 4, ZOTH>, gq, bq, 0, st, L.d, c, L.h2, s.ref, own, oth, bown, skip);
+  } else if (threads / 2 >= wave2) {
+    gq.z = L.d.nz / 2;
+    launch_pdl(k_rbgs_v4<T, 2, ZOTH>, gq, bq, 0, st, L.d, c, L.h2, s.ref, own, oth, bown, skip);
+  } else {
+    launch_pdl(k_rbgs_v4<T, 1, ZOTH>, gq, bq, 0, st, L.d, c, L.h2, s.ref, own, oth, bown, skip);
+  }
+}
+template <class T>
+static void half_sweep(const DevState& s, int l, int c, bool zoth, T* a, const T* b, const unsigned int* skip,
+                       cudaStream_t st) {
+  const MgLevel& L = s.lv[l];
+  if (L.d.nx % 8 != 0) {
+    launch_pdl(k_rbgs_split<T>, g_half(L.d), b_cells(), 0, st, L.d, c, L.h2, s.ref, zoth ? 1 : 0, a, b, skip);
+    return;
+  }
+  const size_t half = L.d.n() >> 1;
+  T* own = a + (c ? half : 0);
+  const T* oth = a + (c ? 0 : half);
+  const T* bown = b + (c ? half : 0);
+  if (zoth) half_sweep_v4<T, true>(s, L, c, own, oth, bown, skip, st);
+  else half_sweep_v4<T, false>(s, L, c, own, oth, bown, skip, st);
+}
+
 // `sweeps` red-black sweeps on level l, in place.  zero_first: the input is
-// zero (fill it); ec: coarse correction to add first.
+// zero (the first red half-sweep then reads no neighbours, and the black
+// half-sweep never reads its own old values, so nothing is filled unless
+// there are no sweeps); ec: coarse correction to add first.
 template <class T, class TC = T>
 static void smooth(const DevState& s, int l, T* a, const T* b, int sweeps, bool zero_first, const TC* ec,
                    const unsigned int* skip, cudaStream_t st) {
   const MgLevel& L = s.lv[l];
-  if (zero_first) k_fill_zero<T><<<s.num_sms * 2, 256, 0, st>>>(a, L.d.n(), skip);
+  if (zero_first && sweeps == 0) launch_pdl(k_fill_zero<T>, dim3(s.num_sms * 2), dim3(256), 0, st, a, L.d.n(), skip);
   if (ec) {
     const Grid dc = s.lv[l + 1].d;
     const dim3 bp = pair_block(dc);  // every transfer level has nx % 4 == 0
-    k_prolong_add2<T, TC><<<pair_grid(dc, bp), bp, 0, st>>>(L.d, dc, s.ref, a, ec, skip);
+    launch_pdl(k_prolong_add2<T, TC>, pair_grid(dc, bp), bp, 0, st, L.d, dc, s.ref, a, ec, skip);
   }
-  const bool v4 = (L.d.nx % 8) == 0;
-  const dim3 bq = quad_block(L.d), gq = quad_grid(L.d, bq);
-  for (int k = 0; k < sweeps; ++k) {
-    for (int c = 0; c < 2; ++c) {
-      if (v4) k_rbgs_v4<T><<<gq, bq, 0, st>>>(L.d, c, L.h2, s.ref, a, b, skip);
-      else k_rbgs_split<T><<<g_half(L.d), b_cells(), 0, st>>>(L.d, c, L.h2, s.ref, a, b, skip);
-    }
-  }
+  for (int k = 0; k < sweeps; ++k)
+    for (int c = 0; c < 2; ++c) half_sweep<T>(s, l, c, zero_first && k == 0 && c == 0, a, b, skip, st);
 }
 
 template <class T, int CS>
 static void launch_cluster(const MgLevel& L, int ref, int sweeps, T* e, const T* b, const unsigned int* skip,
                            cudaStream_t st) {
   const size_t smem = 2 * (L.d.n() / CS) * sizeof(float);
-  k_coarse_cluster<T, CS><<<CS, 512, smem, st>>>(L.d, L.h2, ref, sweeps, e, b, skip);
+  launch_pdl(k_coarse_cluster<T, CS>, dim3(CS), dim3(512), smem, st, L.d, L.h2, ref, sweeps, e, b, skip);
 }
 
 template <class T>
 static void coarse_solve(const DevState& s, int l, T* e, const T* b, const unsigned int* skip, cudaStream_t st) {
   const MgLevel& L = s.lv[l];
   if (s.coarse_sweeps < 0) {  // exact: e = M b with the precomputed inverse
-    k_coarse_dense<T><<<1, s.cn, s.cn * sizeof(float), st>>>(L.d, s.cinv, s.cn, e, b, skip);
+    launch_pdl(k_coarse_dense<T>, dim3((s.cn + 31) / 32), dim3(256), (s.cn + 256) * sizeof(float), st, L.d, s.cinv,
+               s.cn, e, b, skip);
     return;
   }
   int cs = 0;
