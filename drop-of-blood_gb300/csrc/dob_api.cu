@@ -5,10 +5,13 @@
 // A step is the reference's encodePhysicsStep (BloodDropEngine.ts:1855-2111)
 // minus the wave and lighting passes: advect -> centre -> [curl] -> Casson/
 // forces -> divergence -> V-cycles -> project -> centre -> clear splats ->
-// parcel emit -> parcel advect/splat -> dye predict -> dye resolve.  The
-// stage sequence is captured once into a CUDA graph per dye ping-pong parity
-// and replayed; the per-step parameters reach the device by one 600-byte
-// copy from a pinned ring before each replay.
+// parcel emit -> parcel advect/splat -> dye predict -> dye resolve.  In the
+// closed box nothing reads the centre velocity between advection and the
+// projection (no curl), so that centre pass is left out, and the projection
+// and the following centre pass run as one kernel.  The stage sequence is
+// captured once into a CUDA graph per (dye, velocity) ping-pong state and
+// replayed; the per-step parameters reach the device by one 592-byte copy
+// from a pinned ring before each replay.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdio.h>
@@ -201,8 +204,16 @@ static void enqueue_step_body(dob_ctx* ctx, DevState& s, cudaStream_t st, float*
   for (int k = 0; k < n; ++k) {
     const int stage = kStepOrder[k];
     if (stage == DOB_STAGE_CURL && !(s.ref && (s.flags & DOB_PHYS_VORT_CONF))) continue;
+    // closed box: the centre after advection has no reader, and the centre
+    // after the projection comes out of the fused projection kernel
+    if (!s.ref && stage == DOB_STAGE_MAC_TO_CENTER) continue;
     if (stage_ms) cudaEventRecord(ctx->stage_ev[0], st);
-    enqueue_stage(ctx, s, stage, st);
+    if (!s.ref && stage == DOB_STAGE_PROJECT) {
+      launch_project_center(s, st);
+      swap_vel(s);
+    } else {
+      enqueue_stage(ctx, s, stage, st);
+    }
     if (stage_ms) {
       cudaEventRecord(ctx->stage_ev[1], st);
       cudaEventSynchronize(ctx->stage_ev[1]);
@@ -225,16 +236,34 @@ static void enqueue_step_body(dob_ctx* ctx, DevState& s, cudaStream_t st, float*
   }
 }
 
-// Graphs are cached per (dye ping-pong parity, statistics on/off).
-static dob_status get_graph(dob_ctx* ctx, bool stats, cudaGraphExec_t* out) {
-  const int base = stats ? 2 : 0;
-  for (int k = base; k < base + 2; ++k) {
-    if (ctx->graph[k] && ctx->graph_conc[k] == ctx->s.conc) {
-      *out = ctx->graph[k];
+// Graphs are cached per (statistics on/off, dye and velocity buffers at the
+// step's start).
+static void pingpong_get(const DevState& s, void** out) {
+  out[0] = s.u; out[1] = s.v; out[2] = s.w; out[3] = s.u2; out[4] = s.v2; out[5] = s.w2;
+  out[6] = s.conc; out[7] = s.conc2;
+}
+static void pingpong_set(DevState& s, void* const* in) {
+  s.u = in[0]; s.v = in[1]; s.w = in[2]; s.u2 = in[3]; s.v2 = in[4]; s.w2 = in[5];
+  s.conc = in[6]; s.conc2 = in[7];
+}
+
+static dob_status get_graph(dob_ctx* ctx, bool stats, dob_ctx::StepGraph** out) {
+  const int nslots = (int)(sizeof(ctx->graphs) / sizeof(ctx->graphs[0]));
+  int slot = -1;
+  for (int k = 0; k < nslots; ++k) {
+    dob_ctx::StepGraph& G = ctx->graphs[k];
+    if (G.ex && G.stats == stats && G.conc == ctx->s.conc && G.u == ctx->s.u) {
+      *out = &G;
       return DOB_OK;
     }
+    if (!G.ex && slot < 0) slot = k;
   }
-  const int slot = ctx->graph[base] ? base + 1 : base;
+  if (slot < 0) {
+    slot = ctx->graph_next;
+    ctx->graph_next = (slot + 1) % nslots;
+    cudaGraphExecDestroy(ctx->graphs[slot].ex);
+    ctx->graphs[slot].ex = nullptr;
+  }
   DevState s = ctx->s;
   cudaGraph_t g = nullptr;
   CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
@@ -255,18 +284,22 @@ static dob_status get_graph(dob_ctx* ctx, bool stats, cudaGraphExec_t* out) {
   e = cudaGraphInstantiate(&ex, g, 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return fail(ctx, DOB_ECUDA, "cudaGraphInstantiate", cudaGetErrorString(e));
-  ctx->graph[slot] = ex;
-  ctx->graph_conc[slot] = ctx->s.conc;
-  *out = ex;
+  dob_ctx::StepGraph& G = ctx->graphs[slot];
+  G.ex = ex;
+  G.stats = stats;
+  G.conc = ctx->s.conc;
+  G.u = ctx->s.u;
+  pingpong_get(s, G.after);
+  *out = &G;
   return DOB_OK;
 }
 
 static void drop_graphs(dob_ctx* ctx) {
-  for (int k = 0; k < 4; ++k) {
-    if (ctx->graph[k]) cudaGraphExecDestroy(ctx->graph[k]);
-    ctx->graph[k] = nullptr;
-    ctx->graph_conc[k] = nullptr;
+  for (auto& G : ctx->graphs) {
+    if (G.ex) cudaGraphExecDestroy(G.ex);
+    G = dob_ctx::StepGraph();
   }
+  ctx->graph_next = 0;
 }
 
 static dob_status one_step(dob_ctx* ctx, uint32_t flags, float* stage_ms) {
@@ -281,11 +314,11 @@ static dob_status one_step(dob_ctx* ctx, uint32_t flags, float* stage_ms) {
   if (stage_ms || (flags & DOB_STEP_NO_GRAPH)) {
     enqueue_step_body(ctx, ctx->s, ctx->stream, stage_ms, stats);
   } else {
-    cudaGraphExec_t ex = nullptr;
-    st = get_graph(ctx, stats, &ex);
+    dob_ctx::StepGraph* G = nullptr;
+    st = get_graph(ctx, stats, &G);
     if (st != DOB_OK) return st;
-    CK(cudaGraphLaunch(ex, ctx->stream));
-    std::swap(ctx->s.conc, ctx->s.conc2);  // the graph's resolve wrote conc2
+    CK(cudaGraphLaunch(G->ex, ctx->stream));
+    pingpong_set(ctx->s, G->after);  // the buffers the captured step wrote last
   }
   CK(cudaGetLastError());
   ctx->step_index++;
@@ -821,8 +854,8 @@ dob_status dob_launches_per_step(dob_ctx* ctx, int* n) {
   if (!ctx || !n) return DOB_EINVAL;
   if (!ctx->kernels_per_step) {
     // capture the plain step graph once (no launch) to count its kernel nodes
-    cudaGraphExec_t ex = nullptr;
-    dob_status st = get_graph(ctx, false, &ex);
+    dob_ctx::StepGraph* G = nullptr;
+    dob_status st = get_graph(ctx, false, &G);
     if (st != DOB_OK) return st;
   }
   *n = ctx->kernels_per_step;

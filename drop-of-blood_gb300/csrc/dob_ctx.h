@@ -41,8 +41,16 @@ struct dob_ctx {
   int step_index = 0;
   std::vector<void*> allocs;
   uint64_t bytes = 0;
-  cudaGraphExec_t graph[4] = {nullptr, nullptr, nullptr, nullptr};
-  void* graph_conc[4] = {nullptr, nullptr, nullptr, nullptr};  // conc pointer each graph was captured with
+  // Captured step graphs, keyed by statistics on/off and the ping-pong
+  // buffers current at capture (dye and velocity alternate between steps);
+  // `after` holds the ping-pong pointers the captured step leaves behind.
+  struct StepGraph {
+    cudaGraphExec_t ex = nullptr;
+    bool stats = false;
+    void *conc = nullptr, *u = nullptr;
+    void* after[8] = {};  // u, v, w, u2, v2, w2, conc, conc2
+  } graphs[8];
+  int graph_next = 0;  // round-robin replacement when all slots are taken
   int kernels_per_step = 0;
   dob::Snapshot snaps[dob::kSnapshots];
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;

@@ -207,6 +207,9 @@ void launch_curl(const DevState& s, cudaStream_t st);
 void launch_casson(const DevState& s, cudaStream_t st);
 void launch_mac_rhs(const DevState& s, cudaStream_t st);
 void launch_project(const DevState& s, cudaStream_t st);
+// closed box: projection of (u, v, w) into (u2, v2, w2) and the centre
+// velocity of the projected faces, one pass (the caller swaps the buffers)
+void launch_project_center(const DevState& s, cudaStream_t st);
 void launch_divergence(const DevState& s, float* out, float scale, unsigned int* maxbits, cudaStream_t st);
 void launch_conc_predict(const DevState& s, cudaStream_t st);
 void launch_conc_resolve(const DevState& s, cudaStream_t st);
