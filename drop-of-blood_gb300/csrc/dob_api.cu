@@ -7,8 +7,10 @@
 // forces -> divergence -> V-cycles -> project -> centre -> clear splats ->
 // parcel emit -> parcel advect/splat -> dye predict -> dye resolve.  In the
 // closed box nothing reads the centre velocity between advection and the
-// projection (no curl), so that centre pass is left out, and the projection
-// and the following centre pass run as one kernel.  The stage sequence is
+// projection (no curl), so that centre pass is left out, the projection and
+// the following centre pass run as one kernel, and Casson, divergence and
+// projection use the z-column kernels of k_box.cu (same bits as the general
+// kernels the stage-level interface runs).  The stage sequence is
 // captured once into a CUDA graph per (dye, velocity) ping-pong state and
 // replayed; the per-step parameters reach the device by one 592-byte copy
 // from a pinned ring before each replay.
@@ -209,7 +211,12 @@ static void enqueue_step_body(dob_ctx* ctx, DevState& s, cudaStream_t st, float*
     if (!s.ref && stage == DOB_STAGE_MAC_TO_CENTER) continue;
     if (stage_ms) cudaEventRecord(ctx->stage_ev[0], st);
     if (!s.ref && stage == DOB_STAGE_PROJECT) {
-      launch_project_center(s, st);
+      launch_project_center_box(s, st);
+      swap_vel(s);
+    } else if (!s.ref && stage == DOB_STAGE_MAC_RHS) {
+      launch_mac_rhs_box(s, st);
+    } else if (stage == DOB_STAGE_CASSON_FORCES && box_casson_applies(s)) {
+      launch_casson_box(s, st);
       swap_vel(s);
     } else {
       enqueue_stage(ctx, s, stage, st);

@@ -207,9 +207,15 @@ void launch_curl(const DevState& s, cudaStream_t st);
 void launch_casson(const DevState& s, cudaStream_t st);
 void launch_mac_rhs(const DevState& s, cudaStream_t st);
 void launch_project(const DevState& s, cudaStream_t st);
-// closed box: projection of (u, v, w) into (u2, v2, w2) and the centre
-// velocity of the projected faces, one pass (the caller swaps the buffers)
-void launch_project_center(const DevState& s, cudaStream_t st);
+// ---- closed-box column kernels of the step graph (k_box.cu) ------------------------------
+// Same results as launch_casson / launch_mac_rhs / launch_project followed by
+// launch_mac_to_center.  Casson needs dye on the velocity grid.
+bool box_casson_applies(const DevState& s);
+void launch_casson_box(const DevState& s, cudaStream_t st);   // u -> u2 (caller swaps)
+void launch_mac_rhs_box(const DevState& s, cudaStream_t st);  // with the zero-mean correction
+// projection of (u, v, w) into (u2, v2, w2) and the centre velocity of the
+// projected faces, one pass (the caller swaps the buffers)
+void launch_project_center_box(const DevState& s, cudaStream_t st);
 void launch_divergence(const DevState& s, float* out, float scale, unsigned int* maxbits, cudaStream_t st);
 void launch_conc_predict(const DevState& s, cudaStream_t st);
 void launch_conc_resolve(const DevState& s, cudaStream_t st);

@@ -1,0 +1,237 @@
+// k_box.cu — the closed-box stencil kernels of the step (Casson viscosity,
+// divergence, projection + centre velocity) on z-columns.
+//
+// Block 32 x 8: a warp is 32 consecutive cells of one row and every thread
+// walks kColZ planes of its (x, y) column.  The z-neighbours of a plane are
+// the previous and next planes' values, kept in registers; the x-neighbours
+// are the neighbouring lanes' values, passed by warp shuffles (only the
+// first and last lane of a warp load them); the y-neighbours are loads of
+// the adjacent rows, which the neighbouring warps of the block bring into
+// L1.  Offsets are 32-bit (grids have fewer than 2^31 cells).
+//
+// Each kernel computes exactly the expressions of its general counterpart in
+// k_fluid.cu (k_casson's closed-box branch, k_mac_rhs, k_project followed by
+// k_mac_to_center), in the same order, so the results are the same bits;
+// the step graph of the closed box uses these, the stage-level interface the
+// general kernels.
+#include "dob_kernels.cuh"
+
+namespace dob {
+namespace {
+
+constexpr int kColZ = 8;
+constexpr unsigned kFull = 0xffffffffu;
+
+// Cell of this thread, clamped into the grid (lanes past the last column or
+// row compute a copy of the edge cell and store nothing, so every lane takes
+// part in the shuffles).
+struct Col {
+  int lane, x, y, z0, zend;
+  bool valid;
+  uint32_t sy, sz, i;  // row and plane strides, index of (x, y, z0)
+};
+__device__ __forceinline__ Col column(const Grid& g) {
+  Col c;
+  c.lane = threadIdx.x;
+  const int xr = blockIdx.x * 32 + threadIdx.x, yr = blockIdx.y * 8 + threadIdx.y;
+  c.valid = xr < g.nx && yr < g.ny;
+  c.x = xr < g.nx ? xr : g.nx - 1;
+  c.y = yr < g.ny ? yr : g.ny - 1;
+  c.z0 = blockIdx.z * kColZ;
+  c.zend = min(c.z0 + kColZ, g.nz);
+  c.sy = (uint32_t)g.nx;
+  c.sz = (uint32_t)g.nx * (uint32_t)g.ny;
+  c.i = (uint32_t)c.z0 * c.sz + (uint32_t)c.y * c.sy + (uint32_t)c.x;
+  return c;
+}
+// value of cell x - 1 (clamped: x = 0 gives the own value) and x + 1
+template <class S>
+__device__ __forceinline__ float x_minus(const Col& c, float own, const S* a, uint32_t i) {
+  const float sh = __shfl_up_sync(kFull, own, 1);
+  if (c.x == 0) return own;
+  return c.lane == 0 ? ldf(a + i - 1) : sh;
+}
+template <class S>
+__device__ __forceinline__ float x_plus(const Col& c, const Grid& g, float own, const S* a, uint32_t i) {
+  const float sh = __shfl_down_sync(kFull, own, 1);
+  if (c.x == g.nx - 1) return own;
+  return c.lane == 31 ? ldf(a + i + 1) : sh;
+}
+template <class VS>
+__device__ __forceinline__ dob_v3 ld3(const VS* u, const VS* v, const VS* w, uint32_t j) {
+  return v3(ldf(u + j), ldf(v + j), ldf(w + j));
+}
+template <class VS> __device__ __forceinline__ float vs_round(float v);
+template <> __device__ __forceinline__ float vs_round<float>(float v) { return v; }
+template <> __device__ __forceinline__ float vs_round<__half>(float v) { return __half2float(__float2half_rn(v)); }
+
+// ---- Casson viscosity, closed box (k_casson's closed-box branch) -------------------------
+template <class VS, class DS>
+__global__ void __launch_bounds__(256) k_casson_box(Grid g, const StepParams* __restrict__ Pp,
+                                                    const VS* __restrict__ u, const VS* __restrict__ v,
+                                                    const VS* __restrict__ w, const DS* __restrict__ dye,
+                                                    VS* __restrict__ uo, VS* __restrict__ vo, VS* __restrict__ wo) {
+  const Col c = column(g);
+  if (c.z0 >= g.nz) return;  // uniform over the block
+  const StepParams& P = *Pp;
+  const float dtv = P.dt, dxv = P.dx;
+  const float sqrtMu = dob_sqrt(P.mu_p);
+  const int dym = c.y > 0 ? -(int)c.sy : 0, dyp = c.y < g.ny - 1 ? (int)c.sy : 0;
+  uint32_t i = c.i;
+  dob_v3 mZn = ld3(u, v, w, c.z0 > 0 ? i - c.sz : i);
+  dob_v3 mac = ld3(u, v, w, i);
+  for (int z = c.z0; z < c.zend; ++z) {
+    const dob_v3 mZp = ld3(u, v, w, z < g.nz - 1 ? i + c.sz : i);
+    const dob_v3 mXn = v3(x_minus(c, mac.x, u, i), x_minus(c, mac.y, v, i), x_minus(c, mac.z, w, i));
+    const dob_v3 mXp = v3(x_plus(c, g, mac.x, u, i), x_plus(c, g, mac.y, v, i), x_plus(c, g, mac.z, w, i));
+    const dob_v3 mYp = ld3(u, v, w, i + dyp), mYn = ld3(u, v, w, i + dym);
+    const dob_v3 du = mXp - mXn, dv = mYp - mYn, dw = mZp - mZn;
+    const dob_v3 lapMac = (mXp + mXn + mYp + mYn + mZp + mZn) - 6.0f * mac;
+    const float cval = ldf(dye + i);
+    const float cc = dob_clampf(cval, 0.0f, 1.5f);
+    const float gdot = dob_sqrt(dot3(du, du) + dot3(dv, dv) + dot3(dw, dw)) / (2.0f * dxv);
+    const float sqrtYield = dob_sqrt(P.tau_y * cc * cc / (gdot + 0.4f));
+    const float nu = (sqrtMu + sqrtYield) * (sqrtMu + sqrtYield);
+    const float alpha = dob_minf(nu * dtv / (dxv * dxv), 0.125f);
+    dob_v3 out = mac + alpha * lapMac;
+    if (c.x >= g.nx - 1) out.x = 0.0f;
+    if (z >= g.nz - 1) out.z = 0.0f;
+    if (c.y >= g.ny - 1) out.y = 0.0f;
+    if (c.valid) { stf(uo + i, out.x); stf(vo + i, out.y); stf(wo + i, out.z); }
+    mZn = mac;
+    mac = mZp;
+    i += c.sz;
+  }
+}
+
+// ---- divergence into the split right-hand side (k_mac_rhs, closed box) ------------------
+template <class VS>
+__global__ void __launch_bounds__(256) k_rhs_box(Grid g, const VS* __restrict__ u, const VS* __restrict__ v,
+                                                 const VS* __restrict__ w, float* __restrict__ rhs) {
+  const Col c = column(g);
+  if (c.z0 >= g.nz) return;
+  const uint32_t half = (uint32_t)(g.n() >> 1), hx = (uint32_t)g.nx >> 1;
+  uint32_t i = c.i;
+  float wBack = c.z0 > 0 ? ldf(w + i - c.sz) : 0.0f;
+  for (int z = c.z0; z < c.zend; ++z) {
+    const float uo_ = ldf(u + i), vo_ = ldf(v + i), wo_ = ldf(w + i);
+    const float uL = x_minus(c, uo_, u, i);
+    const float uRight = c.x >= g.nx - 1 ? 0.0f : uo_;
+    const float uLeft = c.x == 0 ? 0.0f : uL;
+    const float vTop = c.y >= g.ny - 1 ? 0.0f : vo_;
+    const float vBot = c.y == 0 ? 0.0f : ldf(v + i - c.sy);
+    const float wFront = z >= g.nz - 1 ? 0.0f : wo_;
+    const float r = (uRight - uLeft) + (vTop - vBot) + (wFront - wBack);
+    if (c.valid) {
+      const uint32_t k = ((uint32_t)(c.x + c.y + z) & 1u) * half + ((uint32_t)z * (uint32_t)g.ny + c.y) * hx +
+                         ((uint32_t)c.x >> 1);
+      rhs[k] = r;
+    }
+    wBack = wo_;
+    i += c.sz;
+  }
+}
+
+// ---- projection + centre velocity (k_project then k_mac_to_center, closed box) ----------
+// The projected faces go to uo/vo/wo (each cell also reads the old faces
+// below it); each cell forms its lower faces' projected values with the
+// arithmetic of the cell below, stored with the velocity storage's rounding.
+template <class VS>
+__global__ void __launch_bounds__(256) k_project_center_box(Grid g, const VS* __restrict__ u,
+                                                            const VS* __restrict__ v, const VS* __restrict__ w,
+                                                            const float* __restrict__ p,
+                                                            const float* __restrict__ plo, VS* __restrict__ uo,
+                                                            VS* __restrict__ vo, VS* __restrict__ wo,
+                                                            typename Vec4Of<VS>::type* __restrict__ cen) {
+  const Col c = column(g);
+  if (c.z0 >= g.nz) return;
+  const uint32_t half = (uint32_t)(g.n() >> 1), hx = (uint32_t)g.nx >> 1;
+  const bool df = plo != nullptr;
+  auto pidx = [&](int x, int y, int z) {  // rb_index in 32 bits
+    return ((uint32_t)(x + y + z) & 1u) * half + ((uint32_t)z * (uint32_t)g.ny + (uint32_t)y) * hx + ((uint32_t)x >> 1);
+  };
+  auto ldp = [&](uint32_t k, float& pv, float& lv) {
+    pv = __ldg(p + k);
+    lv = df ? __ldg(plo + k) : 0.0f;
+  };
+  const bool has_ym = c.y > 0, has_yp = c.y < g.ny - 1, has_xm = c.x > 0, has_xp = c.x < g.nx - 1;
+  uint32_t i = c.i;
+  float pZn = 0.0f, lZn = 0.0f, wBold = 0.0f;  // column at z - 1
+  if (c.z0 > 0) {
+    ldp(pidx(c.x, c.y, c.z0 - 1), pZn, lZn);
+    wBold = ldf(w + i - c.sz);
+  }
+  float pC, lC;
+  ldp(pidx(c.x, c.y, c.z0), pC, lC);
+  for (int z = c.z0; z < c.zend; ++z) {
+    const bool has_zp = z < g.nz - 1;
+    float pZp = 0.0f, lZp = 0.0f;
+    if (has_zp) ldp(pidx(c.x, c.y, z + 1), pZp, lZp);
+    // x neighbours from the neighbouring lanes; the edge lanes of a warp load them
+    float pXp = __shfl_down_sync(kFull, pC, 1), lXp = __shfl_down_sync(kFull, lC, 1);
+    float pXn = __shfl_up_sync(kFull, pC, 1), lXn = __shfl_up_sync(kFull, lC, 1);
+    if (c.lane == 31 && has_xp) ldp(pidx(c.x + 1, c.y, z), pXp, lXp);
+    if (c.lane == 0 && has_xm) ldp(pidx(c.x - 1, c.y, z), pXn, lXn);
+    float pYp = 0.0f, lYp = 0.0f, pYn = 0.0f, lYn = 0.0f;
+    if (has_yp) ldp(pidx(c.x, c.y + 1, z), pYp, lYp);
+    if (has_ym) ldp(pidx(c.x, c.y - 1, z), pYn, lYn);
+    const float uOwn = ldf(u + i), vOwn = ldf(v + i), wOwn = ldf(w + i);
+    const float uSh = __shfl_up_sync(kFull, uOwn, 1);
+    const float uLold = has_xm ? (c.lane == 0 ? ldf(u + i - 1) : uSh) : 0.0f;
+    const float vDold = has_ym ? ldf(v + i - c.sy) : 0.0f;
+    // upper faces: p(hi) - p(this) (+ low parts), as k_project
+    auto dp_up = [&](float ph, float lh) { return df ? (ph - pC) + (lh - lC) : (ph - pC); };
+    // lower faces: p(this) - p(lo), as the cell below forms it
+    auto dp_dn = [&](float pl, float ll) { return df ? (pC - pl) + (lC - ll) : (pC - pl); };
+    const float mx = has_xp ? uOwn - dp_up(pXp, lXp) : 0.0f;
+    const float my = has_yp ? vOwn - dp_up(pYp, lYp) : 0.0f;
+    const float mz = has_zp ? wOwn - dp_up(pZp, lZp) : 0.0f;
+    const float uL = has_xm ? vs_round<VS>(uLold - dp_dn(pXn, lXn)) : 0.0f;
+    const float vD = has_ym ? vs_round<VS>(vDold - dp_dn(pYn, lYn)) : 0.0f;
+    const float wB = z > 0 ? vs_round<VS>(wBold - dp_dn(pZn, lZn)) : 0.0f;
+    if (c.valid) {
+      stf(uo + i, mx); stf(vo + i, my); stf(wo + i, mz);
+      const float uR = vs_round<VS>(mx), vU = vs_round<VS>(my), wF = vs_round<VS>(mz);
+      st4(cen + i, make_float4(0.5f * (uL + uR), 0.5f * (vD + vU), 0.5f * (wB + wF), 0.0f));
+    }
+    pZn = pC; lZn = lC;
+    pC = pZp; lC = lZp;
+    wBold = wOwn;
+    i += c.sz;
+  }
+}
+
+inline dim3 col_grid(const Grid& g) { return dim3((g.nx + 31) / 32, (g.ny + 7) / 8, (g.nz + kColZ - 1) / kColZ); }
+
+}  // namespace
+
+bool box_casson_applies(const DevState& s) {
+  return !s.ref && s.gc.nx == s.g.nx && s.gc.ny == s.g.ny && s.gc.nz == s.g.nz;
+}
+
+void launch_casson_box(const DevState& s, cudaStream_t st) {
+  DOB_VEL_DISPATCH(s.prec, {
+    k_casson_box<VS, DS><<<col_grid(s.g), dim3(32, 8), 0, st>>>(s.g, s.params, (const VS*)s.u, (const VS*)s.v,
+                                                                (const VS*)s.w, (const DS*)s.conc, (VS*)s.u2,
+                                                                (VS*)s.v2, (VS*)s.w2);
+  });
+}
+
+void launch_mac_rhs_box(const DevState& s, cudaStream_t st) {
+  DOB_VEL_DISPATCH(s.prec, {
+    k_rhs_box<VS><<<col_grid(s.g), dim3(32, 8), 0, st>>>(s.g, (const VS*)s.u, (const VS*)s.v, (const VS*)s.w,
+                                                         s.rhs);
+  });
+  launch_sum(s.rhs, s.g.n(), s.red + RED_RHS_SUM, s.num_sms, st);
+  launch_sub_mean(s.rhs, s.g.n(), s.red + RED_RHS_SUM, s.num_sms, st);
+}
+
+void launch_project_center_box(const DevState& s, cudaStream_t st) {
+  DOB_VEL_DISPATCH(s.prec, {
+    k_project_center_box<VS><<<col_grid(s.g), dim3(32, 8), 0, st>>>(
+        s.g, (const VS*)s.u, (const VS*)s.v, (const VS*)s.w, s.p, s.plo, (VS*)s.u2, (VS*)s.v2, (VS*)s.w2,
+        (typename Vec4Of<VS>::type*)s.cen);
+  });
+}
+
+}  // namespace dob

@@ -428,45 +428,6 @@ __global__ void __launch_bounds__(256) k_project(Grid g, const StepParams* __res
   stf(u + i, mx); stf(v + i, my); stf(w + i, mz);
 }
 
-// FLUID_MAC_PROJECT followed by FLUID_MAC_TO_CENTER, closed box, in one
-// pass.  The projected faces go to uo/vo/wo (out of place: each cell also
-// reads the old faces below it), and each cell forms its three lower faces'
-// projected values with the arithmetic the cell below uses for them, stored
-// with the velocity storage's rounding, so faces and centre velocity equal
-// the two-pass result bit for bit.
-template <class VS> __device__ __forceinline__ float vs_round(float v);
-template <> __device__ __forceinline__ float vs_round<float>(float v) { return v; }
-template <> __device__ __forceinline__ float vs_round<__half>(float v) { return __half2float(__float2half_rn(v)); }
-template <class VS>
-__global__ void __launch_bounds__(256) k_project_center(Grid g, const VS* __restrict__ u, const VS* __restrict__ v,
-                                                        const VS* __restrict__ w, const float* __restrict__ p,
-                                                        const float* __restrict__ plo, VS* __restrict__ uo,
-                                                        VS* __restrict__ vo, VS* __restrict__ wo,
-                                                        typename Vec4Of<VS>::type* __restrict__ cen) {
-  CELL_INDEX
-  const size_t sy = (size_t)g.nx, sz = (size_t)g.nx * g.ny;
-  const size_t ic = rb_index(g, x, y, z);
-  const float pC = __ldg(p + ic);
-  const float lC = plo ? __ldg(plo + ic) : 0.0f;
-  // p(hi) - p(lo) as k_project forms it for the face between cells lo and hi
-  auto dp = [&](size_t jhi, float plo_v, float llo_v) {
-    return plo ? (__ldg(p + jhi) - plo_v) + (__ldg(plo + jhi) - llo_v) : (__ldg(p + jhi) - plo_v);
-  };
-  auto dp_below = [&](size_t jlo) {  // face between cell jlo (below) and this cell
-    const float pl = __ldg(p + jlo);
-    return plo ? (pC - pl) + (lC - __ldg(plo + jlo)) : (pC - pl);
-  };
-  const float mx = x < g.nx - 1 ? ldf(u + i) - dp(rb_index(g, x + 1, y, z), pC, lC) : 0.0f;
-  const float my = y < g.ny - 1 ? ldf(v + i) - dp(rb_index(g, x, y + 1, z), pC, lC) : 0.0f;
-  const float mz = z < g.nz - 1 ? ldf(w + i) - dp(rb_index(g, x, y, z + 1), pC, lC) : 0.0f;
-  const float uL = x > 0 ? vs_round<VS>(ldf(u + i - 1) - dp_below(rb_index(g, x - 1, y, z))) : 0.0f;
-  const float vD = y > 0 ? vs_round<VS>(ldf(v + i - sy) - dp_below(rb_index(g, x, y - 1, z))) : 0.0f;
-  const float wB = z > 0 ? vs_round<VS>(ldf(w + i - sz) - dp_below(rb_index(g, x, y, z - 1))) : 0.0f;
-  stf(uo + i, mx); stf(vo + i, my); stf(wo + i, mz);
-  const float uR = vs_round<VS>(mx), vU = vs_round<VS>(my), wF = vs_round<VS>(mz);
-  st4(cen + i, make_float4(0.5f * (uL + uR), 0.5f * (vD + vU), 0.5f * (wB + wF), 0.0f));
-}
-
 // ---- divergence field and its max (statistics) -----------------------------------------
 template <class VS>
 __global__ void __launch_bounds__(256) k_divergence(Grid g, int ref, const VS* __restrict__ u, const VS* __restrict__ v,
@@ -766,14 +727,6 @@ void launch_project(const DevState& s, cudaStream_t st) {
   DOB_VEL_DISPATCH(s.prec, {
     k_project<VS><<<cell_grid(s.g), cell_block(), 0, st>>>(s.g, s.params, s.ref, (VS*)s.u, (VS*)s.v, (VS*)s.w, s.p,
                                                            s.plo, s.wave);
-  });
-}
-
-void launch_project_center(const DevState& s, cudaStream_t st) {
-  DOB_VEL_DISPATCH(s.prec, {
-    k_project_center<VS><<<cell_grid(s.g), cell_block(), 0, st>>>(
-        s.g, (const VS*)s.u, (const VS*)s.v, (const VS*)s.w, s.p, s.plo, (VS*)s.u2, (VS*)s.v2, (VS*)s.w2,
-        (typename Vec4Of<VS>::type*)s.cen);
   });
 }
 

@@ -23,6 +23,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
 UNITS = {
     "dob_api.cu": [],
     "k_fluid.cu": [],
+    "k_box.cu": [],
     "k_mg.cu": [],
     "k_exact.cu": ["-fmad=false"],
     "dob_noalloc.cu": [],
