@@ -197,8 +197,10 @@ def adjoint_leg(fd_dirs: int = 16):
     ||dye - target||^2 with the target from the same scene at 1.1x the drop
     impulse; gradient w.r.t. the initial MAC velocity and the impulse, checked
     against central differences (impulse, and 16 seeded random directions of
-    the initial velocity).  box192 (three r=12 drops injected at step 0, 64
-    steps, checkpoints every 16) gives the full-size cost.  The ratio is the
+    the initial velocity).  box192 (three soft-edged r=12 drops injected at
+    step 0, 64 steps, checkpoints every 16): the full-size cost and the
+    gradient in the three impulses and release positions, against central
+    differences.  The ratio is the
     wall time of dob_tape_backward per step (segment recomputation included)
     over the device time of one forward step of the same scene."""
     import numpy as np
@@ -263,21 +265,59 @@ def adjoint_leg(fd_dirs: int = 16):
         "fd_dirs": fd_dirs, "fd_eps": eps, "fd_rel_err_max": max(errs), "fd_rel_err_median": float(np.median(errs)),
     }
     eng.close()
-    # ---- box192, three drops at step 0, 64 steps ------------------------------------------------
-    sc = scenes.box192()
-    sc.steps = 64
-    eng, traj, fwd = cost(sc, 16, release_all=True)
-    _, g = l2_loss(fwd(sc), np.zeros(eng.field_shape(abi.FIELD_CONC)[0]))
-    traj.backward(g)
+    # ---- box192, three soft-edged drops at step 0, 64 steps, checkpoints every 16 --------------
+    # gradient in the three impulses and the three release positions, each
+    # checked against central differences of the device loss
+    sc = scenes.box192_adjoint()
+    eng = DropFluid(sc.config)
+    traj = DropTrajectory(eng, 16)
+
+    def fwd192(scene):
+        eng.reset()
+        for j in range(len(scene.drops)):
+            scene.release(eng, j)
+        return traj.forward(scene.steps)
+    shifts = ((0.5, -0.3, 0.2), (-0.4, 0.2, 0.3), (0.3, 0.4, -0.5))
+    target = fwd192(scenes.box192_adjoint(impulse_scale=(1.1, 0.9, 1.05), shift=shifts)).astype(np.float64)
+    loss, g = l2_loss(fwd192(sc), target)
+    traj.backward(g)  # first call captures the segment graphs
     eng.sync()
     t0 = time.perf_counter()
     traj.backward(g)
     eng.sync()
     t_bwd = time.perf_counter() - t0
+    drop_g = [traj.drop_grads(sc, k) for k in range(len(sc.drops))]
     fwd_ms = eng.time_steps(8) / 8
+    h, eps = 1e-2, 5e-2
+    imp_err, pos_err, fd_pos = [], [], []
+    for k in range(len(sc.drops)):
+        sp = [1.0] * 3
+        sm = [1.0] * 3
+        sp[k], sm[k] = 1.0 + h, 1.0 - h
+        fd = (l2_loss(fwd192(scenes.box192_adjoint(impulse_scale=sp)), target)[0] -
+              l2_loss(fwd192(scenes.box192_adjoint(impulse_scale=sm)), target)[0]) / (2 * h)
+        imp_err.append(abs(fd - drop_g[k]["impulse"]) / abs(fd))
+        fdk = []
+        for j in range(3):
+            shp = [[0.0] * 3 for _ in range(3)]
+            shm = [[0.0] * 3 for _ in range(3)]
+            shp[k][j], shm[k][j] = eps, -eps
+            fd = (l2_loss(fwd192(scenes.box192_adjoint(shift=shp)), target)[0] -
+                  l2_loss(fwd192(scenes.box192_adjoint(shift=shm)), target)[0]) / (2 * eps)
+            fdk.append(fd)
+        gp = drop_g[k]["position"]
+        fd_pos.append(fdk)
+        pos_err.append(float(np.linalg.norm(np.asarray(fdk) - gp) / np.linalg.norm(gp)))
     out["box192"] = {"steps": sc.steps, "checkpoint_every": 16, "forward_step_ms": fwd_ms,
                      "backward_ms_per_step": 1e3 * t_bwd / sc.steps, "ratio": 1e3 * t_bwd / sc.steps / fwd_ms,
-                     "loss": "||dye||^2 (cost only)", "drops": "all three injected at step 0"}
+                     "loss": loss, "drops": "three soft-edged drops (edge 2 cells) injected at step 0, 393216 parcels",
+                     "target": "same drops with impulses x(1.1, 0.9, 1.05) and centres shifted by up to 0.5 cells",
+                     "impulse_grad": [d["impulse"] for d in drop_g],
+                     "position_grad": [d["position"].tolist() for d in drop_g],
+                     "position_fd": fd_pos,
+                     "impulse_fd_rel_err_max": max(imp_err),
+                     "position_fd_rel_err_max": max(pos_err),
+                     "fd_steps": {"impulse": h, "position_world": eps}}
     eng.close()
     return out
 

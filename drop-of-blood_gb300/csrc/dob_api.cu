@@ -623,6 +623,22 @@ dob_status dob_inject_sphere(dob_ctx* ctx, const float c[3], float r, float dye,
   return DOB_OK;
 }
 
+dob_status dob_inject_sphere_soft(dob_ctx* ctx, const float c[3], float r, float edge, float dye, const float vel[3],
+                                  float sigma, uint64_t seed) {
+  if (!ctx || !c || !vel) return DOB_EINVAL;
+  if (ctx->cfg.bc_mode != DOB_BC_CLOSED_BOX)
+    return fail(ctx, DOB_ESTATE, "dob_inject_sphere_soft", "sphere injection is a closed-box operation");
+  if (!(r > 0.0f) || !(edge > 0.0f) || !isfinite(r) || !isfinite(edge) || !isfinite(dye) || !isfinite(sigma) ||
+      !isfinite(vel[0]) || !isfinite(vel[1]) || !isfinite(vel[2]))
+    return fail(ctx, DOB_EINVAL, "dob_inject_sphere_soft", "bad radius/edge/dye/velocity/sigma");
+  dob_status st = upload_params(ctx, 0);
+  if (st != DOB_OK) return st;
+  launch_inject_sphere_soft(ctx->s, c, r, edge, dye, vel, sigma, seed, ctx->stream);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  return DOB_OK;
+}
+
 dob_status dob_set_parcels(dob_ctx* ctx, const float* p, uint32_t n, uint32_t off) {
   if (!ctx || (!p && n)) return DOB_EINVAL;
   if ((uint64_t)off + n > ctx->s.cap) return fail(ctx, DOB_EINVAL, "dob_set_parcels", "range exceeds capacity");

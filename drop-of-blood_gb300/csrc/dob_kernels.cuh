@@ -252,6 +252,13 @@ cudaError_t eval_math_device(int fn, const float* x, const float* y, float* out,
 // sum of a . vel over the MAC faces k_inject_sphere sets (FP64, into *out)
 void launch_sphere_impulse(const DevState& s, const float* a_u, const float* a_v, const float* a_w, const float c[3],
                            float r, const float vel[3], double* out, cudaStream_t st);
+// soft-edged drop (additive) and the gradient of the loss in its impulse
+// scale and centre from the adjoint fields right after it (out[4], FP64)
+void launch_inject_sphere_soft(const DevState& s, const float c[3], float r, float h, float dye, const float vel[3],
+                               float sigma, uint64_t seed, cudaStream_t st);
+void launch_sphere_soft_grad(const DevState& s, const float* a_u, const float* a_v, const float* a_w,
+                             const float* a_c, const float c[3], float r, float h, float dye, const float vel[3],
+                             float sigma, uint64_t seed, double* out, cudaStream_t st);
 
 // ---- launchers (k_adjoint.cu): transpose of each closed-box FP32 stage ------------------
 void launch_adj_advect_mac(const DevState& s, const AdjState& a, cudaStream_t st);

@@ -317,3 +317,21 @@ DOB_HD dob_v3 mix3(dob_v3 a, dob_v3 b, float t) {
   return v3(dob_mix(a.x, b.x, t), dob_mix(a.y, b.y, t), dob_mix(a.z, b.z, t));
 }
 DOB_HD float length2f(float x, float y) { return dob_sqrt(x * x + y * y); }
+
+// Soft-edged sphere of radius r and edge width h around c at point p: the
+// weight is 1 for |p - c| <= r - h/2, 0 for |p - c| >= r + h/2 and the
+// smoothstep t^2 (3 - 2t), t = (r + h/2 - |p - c|) / h, in between, so it is
+// continuously differentiable in c; *g receives d weight / d c.  Compiled
+// without FMA contraction on the device, so host and device agree bit for bit.
+DOB_HD float dob_soft_sphere(dob_v3 p, dob_v3 c, float r, float h, dob_v3* g) {
+  const dob_v3 dpc = p - c;
+  const float d = length3(dpc);
+  const float t = (r + 0.5f * h - d) / h;
+  if (!(t > 0.0f) || t >= 1.0f) {
+    *g = v3(0.0f, 0.0f, 0.0f);
+    return t >= 1.0f ? 1.0f : 0.0f;
+  }
+  const float s = d > 0.0f ? 6.0f * t * (1.0f - t) / (h * d) : 0.0f;
+  *g = dpc * s;
+  return t * t * (3.0f - 2.0f * t);
+}

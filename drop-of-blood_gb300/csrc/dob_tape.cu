@@ -13,6 +13,7 @@
 // Parcels are passive tracers in the closed box (nothing reads their splat)
 // and are not recomputed.
 #include <cuda_runtime.h>
+#include <math.h>
 #include <string.h>
 
 #include <vector>
@@ -37,7 +38,7 @@ struct AdjCtx {
   std::vector<float*> Tua, Tva, Twa, Tpred;  // k entries
   float* Tp = nullptr;
   float* Trhs = nullptr;
-  double* dred = nullptr;   // reduction slot of dob_adjoint_sphere_impulse
+  double* dred = nullptr;   // reduction slots of the drop gradients (4 doubles)
   // captured "recompute + reverse" graph of a segment, per (length, parity of
   // the dye adjoint ping-pong at its start)
   std::vector<cudaGraphExec_t> seg_graphs;
@@ -106,7 +107,7 @@ dob_status ensure_adj(dob_ctx* ctx) {
     F(&a.lb[l], s.lv[l].d.n());
   }
   if (st == DOB_OK) st = alloc(ctx, A->bufs, (void**)&a.red, 8 * sizeof(double));
-  if (st == DOB_OK) st = alloc(ctx, A->bufs, (void**)&A->dred, sizeof(double));
+  if (st == DOB_OK) st = alloc(ctx, A->bufs, (void**)&A->dred, 4 * sizeof(double));
   if (st != DOB_OK) adjoint_free(ctx);
   return st;
 }
@@ -417,6 +418,24 @@ dob_status dob_adjoint_sphere_impulse(dob_ctx* ctx, const float center[3], float
   launch_sphere_impulse(ctx->s, a.au, a.av, a.aw, center, radius, vel, ctx->adj->dred, ctx->stream);
   TCK(cudaGetLastError());
   TCK(cudaMemcpyAsync(out, ctx->adj->dred, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  TCK(cudaStreamSynchronize(ctx->stream));
+  return DOB_OK;
+}
+
+dob_status dob_adjoint_sphere_soft(dob_ctx* ctx, const float center[3], float radius, float edge, float dye,
+                                   const float vel[3], float noise_sigma, uint64_t seed, double out[4]) {
+  if (!ctx || !center || !vel || !out) return DOB_EINVAL;
+  dob_status st = need_box_fp32(ctx, "dob_adjoint_sphere_soft");
+  if (st != DOB_OK) return st;
+  if (!(radius > 0.0f) || !(edge > 0.0f) || !isfinite(radius) || !isfinite(edge) || !isfinite(dye) ||
+      !isfinite(noise_sigma))
+    return record_error(ctx, DOB_EINVAL, "dob_adjoint_sphere_soft", "bad radius/edge/dye/sigma");
+  if ((st = ensure_adj(ctx)) != DOB_OK) return st;
+  const AdjState& a = ctx->adj->a;
+  launch_sphere_soft_grad(ctx->s, a.au, a.av, a.aw, a.ac, center, radius, edge, dye, vel, noise_sigma, seed,
+                          ctx->adj->dred, ctx->stream);
+  TCK(cudaGetLastError());
+  TCK(cudaMemcpyAsync(out, ctx->adj->dred, 4 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   TCK(cudaStreamSynchronize(ctx->stream));
   return DOB_OK;
 }

@@ -2,7 +2,7 @@
 // divergence, projection + centre velocity) on z-columns.
 //
 // Block 32 x 8: a warp is 32 consecutive cells of one row and every thread
-// walks kColZ planes of its (x, y) column.  The z-neighbours of a plane are
+// walks ZC planes of its (x, y) column.  The z-neighbours of a plane are
 // the previous and next planes' values, kept in registers; the x-neighbours
 // are the neighbouring lanes' values, passed by warp shuffles (only the
 // first and last lane of a warp load them); the y-neighbours are loads of
@@ -19,7 +19,6 @@
 namespace dob {
 namespace {
 
-constexpr int kColZ = 8;
 constexpr unsigned kFull = 0xffffffffu;
 
 // Cell of this thread, clamped into the grid (lanes past the last column or
@@ -30,6 +29,7 @@ struct Col {
   bool valid;
   uint32_t sy, sz, i;  // row and plane strides, index of (x, y, z0)
 };
+template <int ZC>
 __device__ __forceinline__ Col column(const Grid& g) {
   Col c;
   c.lane = threadIdx.x;
@@ -37,8 +37,8 @@ __device__ __forceinline__ Col column(const Grid& g) {
   c.valid = xr < g.nx && yr < g.ny;
   c.x = xr < g.nx ? xr : g.nx - 1;
   c.y = yr < g.ny ? yr : g.ny - 1;
-  c.z0 = blockIdx.z * kColZ;
-  c.zend = min(c.z0 + kColZ, g.nz);
+  c.z0 = blockIdx.z * ZC;
+  c.zend = min(c.z0 + ZC, g.nz);
   c.sy = (uint32_t)g.nx;
   c.sz = (uint32_t)g.nx * (uint32_t)g.ny;
   c.i = (uint32_t)c.z0 * c.sz + (uint32_t)c.y * c.sy + (uint32_t)c.x;
@@ -66,12 +66,12 @@ template <> __device__ __forceinline__ float vs_round<float>(float v) { return v
 template <> __device__ __forceinline__ float vs_round<__half>(float v) { return __half2float(__float2half_rn(v)); }
 
 // ---- Casson viscosity, closed box (k_casson's closed-box branch) -------------------------
-template <class VS, class DS>
+template <class VS, class DS, int ZC>
 __global__ void __launch_bounds__(256) k_casson_box(Grid g, const StepParams* __restrict__ Pp,
                                                     const VS* __restrict__ u, const VS* __restrict__ v,
                                                     const VS* __restrict__ w, const DS* __restrict__ dye,
                                                     VS* __restrict__ uo, VS* __restrict__ vo, VS* __restrict__ wo) {
-  const Col c = column(g);
+  const Col c = column<ZC>(g);
   if (c.z0 >= g.nz) return;  // uniform over the block
   const StepParams& P = *Pp;
   const float dtv = P.dt, dxv = P.dx;
@@ -105,10 +105,10 @@ __global__ void __launch_bounds__(256) k_casson_box(Grid g, const StepParams* __
 }
 
 // ---- divergence into the split right-hand side (k_mac_rhs, closed box) ------------------
-template <class VS>
+template <class VS, int ZC>
 __global__ void __launch_bounds__(256) k_rhs_box(Grid g, const VS* __restrict__ u, const VS* __restrict__ v,
                                                  const VS* __restrict__ w, float* __restrict__ rhs) {
-  const Col c = column(g);
+  const Col c = column<ZC>(g);
   if (c.z0 >= g.nz) return;
   const uint32_t half = (uint32_t)(g.n() >> 1), hx = (uint32_t)g.nx >> 1;
   uint32_t i = c.i;
@@ -136,14 +136,14 @@ __global__ void __launch_bounds__(256) k_rhs_box(Grid g, const VS* __restrict__ 
 // The projected faces go to uo/vo/wo (each cell also reads the old faces
 // below it); each cell forms its lower faces' projected values with the
 // arithmetic of the cell below, stored with the velocity storage's rounding.
-template <class VS>
+template <class VS, int ZC>
 __global__ void __launch_bounds__(256) k_project_center_box(Grid g, const VS* __restrict__ u,
                                                             const VS* __restrict__ v, const VS* __restrict__ w,
                                                             const float* __restrict__ p,
                                                             const float* __restrict__ plo, VS* __restrict__ uo,
                                                             VS* __restrict__ vo, VS* __restrict__ wo,
                                                             typename Vec4Of<VS>::type* __restrict__ cen) {
-  const Col c = column(g);
+  const Col c = column<ZC>(g);
   if (c.z0 >= g.nz) return;
   const uint32_t half = (uint32_t)(g.n() >> 1), hx = (uint32_t)g.nx >> 1;
   const bool df = plo != nullptr;
@@ -201,7 +201,9 @@ __global__ void __launch_bounds__(256) k_project_center_box(Grid g, const VS* __
   }
 }
 
-inline dim3 col_grid(const Grid& g) { return dim3((g.nx + 31) / 32, (g.ny + 7) / 8, (g.nz + kColZ - 1) / kColZ); }
+template <int ZC>
+inline dim3 col_grid(const Grid& g) { return dim3((g.nx + 31) / 32, (g.ny + 7) / 8, (g.nz + ZC - 1) / ZC); }
+constexpr int kCassonZ = 8, kRhsZ = 8, kProjectZ = 4;  // planes per thread (measured at 192x256x192)
 
 }  // namespace
 
@@ -211,7 +213,7 @@ bool box_casson_applies(const DevState& s) {
 
 void launch_casson_box(const DevState& s, cudaStream_t st) {
   DOB_VEL_DISPATCH(s.prec, {
-    k_casson_box<VS, DS><<<col_grid(s.g), dim3(32, 8), 0, st>>>(s.g, s.params, (const VS*)s.u, (const VS*)s.v,
+    k_casson_box<VS, DS, kCassonZ><<<col_grid<kCassonZ>(s.g), dim3(32, 8), 0, st>>>(s.g, s.params, (const VS*)s.u, (const VS*)s.v,
                                                                 (const VS*)s.w, (const DS*)s.conc, (VS*)s.u2,
                                                                 (VS*)s.v2, (VS*)s.w2);
   });
@@ -219,7 +221,7 @@ void launch_casson_box(const DevState& s, cudaStream_t st) {
 
 void launch_mac_rhs_box(const DevState& s, cudaStream_t st) {
   DOB_VEL_DISPATCH(s.prec, {
-    k_rhs_box<VS><<<col_grid(s.g), dim3(32, 8), 0, st>>>(s.g, (const VS*)s.u, (const VS*)s.v, (const VS*)s.w,
+    k_rhs_box<VS, kRhsZ><<<col_grid<kRhsZ>(s.g), dim3(32, 8), 0, st>>>(s.g, (const VS*)s.u, (const VS*)s.v, (const VS*)s.w,
                                                          s.rhs);
   });
   launch_sum(s.rhs, s.g.n(), s.red + RED_RHS_SUM, s.num_sms, st);
@@ -228,7 +230,7 @@ void launch_mac_rhs_box(const DevState& s, cudaStream_t st) {
 
 void launch_project_center_box(const DevState& s, cudaStream_t st) {
   DOB_VEL_DISPATCH(s.prec, {
-    k_project_center_box<VS><<<col_grid(s.g), dim3(32, 8), 0, st>>>(
+    k_project_center_box<VS, kProjectZ><<<col_grid<kProjectZ>(s.g), dim3(32, 8), 0, st>>>(
         s.g, (const VS*)s.u, (const VS*)s.v, (const VS*)s.w, s.p, s.plo, (VS*)s.u2, (VS*)s.v2, (VS*)s.w2,
         (typename Vec4Of<VS>::type*)s.cen);
   });

@@ -394,6 +394,96 @@ __global__ void __launch_bounds__(256) k_sphere_impulse(Grid g, const StepParams
   block_sum_atomic(part, out);
 }
 
+// Soft-edged drop (dob_soft_sphere weight w): dye += w dyev on the dye grid
+// and face += w (vel + sigma noise) on the MAC faces below the upper walls.
+// Additive, so the result does not depend on what the faces held before and
+// the derivative in the centre needs no earlier state.
+template <class VS, class DS>
+__global__ void __launch_bounds__(256) k_inject_sphere_soft(Grid g, Grid gc, const StepParams* __restrict__ Pp, VS* u,
+                                                            VS* v, VS* w, DS* dye, float cx, float cy, float cz,
+                                                            float rr, float hh, float dyev, float vx, float vy,
+                                                            float vz, float sigma, uint64_t seed) {
+  const StepParams& P = *Pp;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  const dob_v3 cc = v3(cx, cy, cz);
+  dob_v3 gw;
+  if (x < gc.nx && y < gc.ny && z < gc.nz) {
+    const dob_v3 cdm = v3((float)gc.nx, (float)gc.ny, (float)gc.nz);
+    const dob_v3 pw = to_world(P, (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / cdm);
+    const float wt = dob_soft_sphere(pw, cc, rr, hh, &gw);
+    if (wt > 0.0f) {
+      const size_t k = gc.at(x, y, z);
+      stf(dye + k, ldv(dye + k) + wt * dyev);
+    }
+  }
+  if (x < g.nx && y < g.ny && z < g.nz) {
+    const size_t i = g.at(x, y, z);
+    const dob_v3 dims = v3((float)g.nx, (float)g.ny, (float)g.nz);
+    const dob_v3 fx = to_world(P, v3((float)x + 1.0f, (float)y + 0.5f, (float)z + 0.5f) / dims);
+    const dob_v3 fy = to_world(P, v3((float)x + 0.5f, (float)y + 1.0f, (float)z + 0.5f) / dims);
+    const dob_v3 fz = to_world(P, v3((float)x + 0.5f, (float)y + 0.5f, (float)z + 1.0f) / dims);
+    float wt = dob_soft_sphere(fx, cc, rr, hh, &gw);
+    if (x < g.nx - 1 && wt > 0.0f) stf(u + i, ldv(u + i) + wt * (vx + sigma * dob_sphere_noise(seed, i, 0)));
+    wt = dob_soft_sphere(fy, cc, rr, hh, &gw);
+    if (y < g.ny - 1 && wt > 0.0f) stf(v + i, ldv(v + i) + wt * (vy + sigma * dob_sphere_noise(seed, i, 1)));
+    wt = dob_soft_sphere(fz, cc, rr, hh, &gw);
+    if (z < g.nz - 1 && wt > 0.0f) stf(w + i, ldv(w + i) + wt * (vz + sigma * dob_sphere_noise(seed, i, 2)));
+  }
+}
+
+// Gradient of the loss in the soft drop's parameters from the adjoints of
+// the fields right after the injection: out[0] = sum over faces of
+// w (adj . vel) (d loss / d s for injected velocity s vel, at s = 1), out[1..3]
+// = d loss / d centre = sum over cells of adj_dye dyev dw/dc plus sum over
+// faces of adj_face (vel + sigma noise) dw/dc.  Per-thread FP64 sums, one
+// FP64 atomic per block and output.
+__global__ void __launch_bounds__(256) k_sphere_soft_grad(Grid g, Grid gc, const StepParams* __restrict__ Pp,
+                                                          const float* __restrict__ au, const float* __restrict__ av,
+                                                          const float* __restrict__ aw, const float* __restrict__ ac,
+                                                          float cx, float cy, float cz, float rr, float hh,
+                                                          float dyev, float vx, float vy, float vz, float sigma,
+                                                          uint64_t seed, double* out) {
+  const StepParams& P = *Pp;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  const dob_v3 cc = v3(cx, cy, cz);
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+  dob_v3 gw;
+  if (x < gc.nx && y < gc.ny && z < gc.nz) {
+    const dob_v3 cdm = v3((float)gc.nx, (float)gc.ny, (float)gc.nz);
+    const dob_v3 pw = to_world(P, (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / cdm);
+    dob_soft_sphere(pw, cc, rr, hh, &gw);
+    const double a = (double)ac[gc.at(x, y, z)] * (double)dyev;
+    s1 += a * gw.x; s2 += a * gw.y; s3 += a * gw.z;
+  }
+  if (x < g.nx && y < g.ny && z < g.nz) {
+    const size_t i = g.at(x, y, z);
+    const dob_v3 dims = v3((float)g.nx, (float)g.ny, (float)g.nz);
+    const dob_v3 fp[3] = {to_world(P, v3((float)x + 1.0f, (float)y + 0.5f, (float)z + 0.5f) / dims),
+                          to_world(P, v3((float)x + 0.5f, (float)y + 1.0f, (float)z + 0.5f) / dims),
+                          to_world(P, v3((float)x + 0.5f, (float)y + 0.5f, (float)z + 1.0f) / dims)};
+    const bool inside[3] = {x < g.nx - 1, y < g.ny - 1, z < g.nz - 1};
+    const float* adj[3] = {au, av, aw};
+    const float vel[3] = {vx, vy, vz};
+    for (int k = 0; k < 3; ++k) {
+      if (!inside[k]) continue;
+      const float wt = dob_soft_sphere(fp[k], cc, rr, hh, &gw);
+      if (!(wt > 0.0f)) continue;
+      const double a = (double)adj[k][i];
+      s0 += a * (double)wt * (double)vel[k];
+      const double val = (double)(vel[k] + sigma * dob_sphere_noise(seed, i, k));
+      s1 += a * val * gw.x; s2 += a * val * gw.y; s3 += a * val * gw.z;
+    }
+  }
+  block_sum_atomic(s0, out + 0);
+  block_sum_atomic(s1, out + 1);
+  block_sum_atomic(s2, out + 2);
+  block_sum_atomic(s3, out + 3);
+}
+
 __global__ void k_eval_math(int fn, const float* __restrict__ x, const float* __restrict__ y, float* __restrict__ out,
                             uint32_t n) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -460,6 +550,31 @@ void launch_sphere_impulse(const DevState& s, const float* a_u, const float* a_v
   cudaMemsetAsync(out, 0, sizeof(double), st);
   k_sphere_impulse<<<grid, dim3(32, 8, 1), 0, st>>>(s.g, s.params, a_u, a_v, a_w, c[0], c[1], c[2], r, vel[0], vel[1],
                                                     vel[2], out);
+}
+
+void launch_inject_sphere_soft(const DevState& s, const float c[3], float r, float h, float dye, const float vel[3],
+                               float sigma, uint64_t seed, cudaStream_t st) {
+  const int nx = s.gc.nx > s.g.nx ? s.gc.nx : s.g.nx;
+  const int ny = s.gc.ny > s.g.ny ? s.gc.ny : s.g.ny;
+  const int nz = s.gc.nz > s.g.nz ? s.gc.nz : s.g.nz;
+  const dim3 grid((nx + 31) / 32, (ny + 7) / 8, nz);
+  DOB_VEL_DISPATCH(s.prec, {
+    k_inject_sphere_soft<VS, DS><<<grid, dim3(32, 8, 1), 0, st>>>(s.g, s.gc, s.params, (VS*)s.u, (VS*)s.v,
+                                                                 (VS*)s.w, (DS*)s.conc, c[0], c[1], c[2], r, h, dye,
+                                                                 vel[0], vel[1], vel[2], sigma, seed);
+  });
+}
+
+void launch_sphere_soft_grad(const DevState& s, const float* a_u, const float* a_v, const float* a_w,
+                             const float* a_c, const float c[3], float r, float h, float dye, const float vel[3],
+                             float sigma, uint64_t seed, double* out, cudaStream_t st) {
+  const int nx = s.gc.nx > s.g.nx ? s.gc.nx : s.g.nx;
+  const int ny = s.gc.ny > s.g.ny ? s.gc.ny : s.g.ny;
+  const int nz = s.gc.nz > s.g.nz ? s.gc.nz : s.g.nz;
+  const dim3 grid((nx + 31) / 32, (ny + 7) / 8, nz);
+  cudaMemsetAsync(out, 0, 4 * sizeof(double), st);
+  k_sphere_soft_grad<<<grid, dim3(32, 8, 1), 0, st>>>(s.g, s.gc, s.params, a_u, a_v, a_w, a_c, c[0], c[1], c[2], r,
+                                                      h, dye, vel[0], vel[1], vel[2], sigma, seed, out);
 }
 
 cudaError_t eval_math_device(int fn, const float* x, const float* y, float* out, uint32_t n) {

@@ -26,6 +26,7 @@ SIGNATURES = {
     "dob_reset": (C.c_int, [P]),
     "dob_set_uniforms": (C.c_int, [P, FP]),
     "dob_inject_sphere": (C.c_int, [P, FP, C.c_float, C.c_float, FP, C.c_float, C.c_uint64]),
+    "dob_inject_sphere_soft": (C.c_int, [P, FP, C.c_float, C.c_float, C.c_float, FP, C.c_float, C.c_uint64]),
     "dob_set_parcels": (C.c_int, [P, FP, C.c_uint32, C.c_uint32]),
     "dob_get_parcels": (C.c_int, [P, FP, C.c_uint32, C.c_uint32]),
     "dob_set_high_water": (C.c_int, [P, C.c_uint32]),
@@ -51,6 +52,8 @@ SIGNATURES = {
     "dob_tape_backward": (C.c_int, [P, FP, C.c_size_t]),
     "dob_adjoint_sphere_impulse": (C.c_int, [P, C.POINTER(C.c_float), C.c_float, C.POINTER(C.c_float),
                                              C.POINTER(C.c_double)]),
+    "dob_adjoint_sphere_soft": (C.c_int, [P, FP, C.c_float, C.c_float, C.c_float, FP, C.c_float, C.c_uint64,
+                                          C.POINTER(C.c_double)]),
 }
 
 _lib = None

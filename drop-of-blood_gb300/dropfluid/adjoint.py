@@ -4,7 +4,8 @@
     dye = traj.forward(32)                 # dob_tape_forward
     loss, g = l2_loss(dye, target)
     grads = traj.backward(g)               # dob_tape_backward -> d loss / d initial state
-    d_imp = traj.drop_impulse_grad(scene, drop)
+    d_imp = traj.drop_impulse_grad(scene, drop)      # hard-edged drop: impulse
+    g = traj.drop_grads(scene, 0)                    # soft-edged drop: impulse and centre
 
 The forward keeps a checkpoint of (velocity, dye, pressure) every
 `checkpoint_every` steps on the device; the backward recomputes one segment
@@ -43,6 +44,20 @@ class DropTrajectory:
             raise RuntimeError("backward before forward")
         self.sim.tape_backward(dye_grad)
         return self.sim.gradients()
+
+    def drop_grads(self, scene, drop) -> dict:
+        """For a soft-edged drop (edge_cells > 0) injected into the
+        trajectory's initial state, after backward: d loss / d s for its
+        velocity scaled by s (at s = 1) and d loss / d centre (world units)."""
+        d = scene.drops[drop] if isinstance(drop, int) else drop
+        if not d.edge_cells > 0.0:
+            raise ValueError("position gradients need a soft-edged drop (edge_cells > 0)")
+        c = scene.config
+        scale = c.dx / c.dt
+        g_imp, g_pos = self.sim.sphere_soft_grad(d.center, d.radius, d.edge_cells * c.dx, 1.0,
+                                                 (0.0, d.w_cells_per_step * scale, 0.0),
+                                                 d.noise_cells_per_step * scale, d.seed)
+        return {"impulse": g_imp, "position": g_pos}
 
     def drop_impulse_grad(self, scene, drop) -> float:
         """d loss / d s for the drop's injected face velocity s * vel (the

@@ -82,6 +82,13 @@ class DropFluid:
         self._ck(self._L.dob_inject_sphere(self._h, _fptr(c), float(radius), float(dye), _fptr(v),
                                            float(noise_sigma), int(seed)), "dob_inject_sphere")
 
+    def inject_sphere_soft(self, center, radius, edge, dye, vel, noise_sigma=0.0, seed=0):
+        """Soft-edged additive drop (dob_inject_sphere_soft)."""
+        c = np.asarray(center, dtype=np.float32)
+        v = np.asarray(vel, dtype=np.float32)
+        self._ck(self._L.dob_inject_sphere_soft(self._h, _fptr(c), float(radius), float(edge), float(dye), _fptr(v),
+                                                float(noise_sigma), int(seed)), "dob_inject_sphere_soft")
+
     def set_parcels(self, parcels, offset=0):
         p = np.ascontiguousarray(parcels, dtype=np.float32).reshape(-1, abi.PARCEL_FLOATS)
         self._ck(self._L.dob_set_parcels(self._h, _fptr(p), p.shape[0], int(offset)), "dob_set_parcels")
@@ -221,6 +228,16 @@ class DropFluid:
         self._ck(self._L.dob_adjoint_sphere_impulse(self._h, c, C.c_float(radius), v, C.byref(out)),
                  "dob_adjoint_sphere_impulse")
         return out.value
+
+    def sphere_soft_grad(self, center, radius, edge, dye, vel, noise_sigma=0.0, seed=0):
+        """(d loss / d s at s = 1 for injected velocity s vel, d loss / d centre[3])
+        of a soft drop, from the adjoint fields (dob_adjoint_sphere_soft)."""
+        c = np.asarray(center, dtype=np.float32)
+        v = np.asarray(vel, dtype=np.float32)
+        out = (C.c_double * 4)()
+        self._ck(self._L.dob_adjoint_sphere_soft(self._h, _fptr(c), float(radius), float(edge), float(dye), _fptr(v),
+                                                 float(noise_sigma), int(seed), out), "dob_adjoint_sphere_soft")
+        return out[0], np.array(out[1:4], dtype=np.float64)
 
     def save_state(self, slot):
         self._ck(self._L.dob_save_state(self._h, int(slot)), "dob_save_state")

@@ -95,6 +95,7 @@ class Drop:
     seed: int
     n_parcels: int
     parcel_seed: int
+    edge_cells: float = 0.0  # > 0: soft-edged additive drop (dob_inject_sphere_soft) of this edge width
 
 
 @dataclass
@@ -112,8 +113,12 @@ class Scene:
         d = self.drops[k]
         c = self.config
         scale = c.dx / c.dt  # cells/step -> world units
-        engine.inject_sphere(d.center, d.radius, 1.0, (0.0, d.w_cells_per_step * scale, 0.0),
-                             d.noise_cells_per_step * scale, d.seed)
+        if d.edge_cells > 0.0:
+            engine.inject_sphere_soft(d.center, d.radius, d.edge_cells * c.dx, 1.0,
+                                      (0.0, d.w_cells_per_step * scale, 0.0), d.noise_cells_per_step * scale, d.seed)
+        else:
+            engine.inject_sphere(d.center, d.radius, 1.0, (0.0, d.w_cells_per_step * scale, 0.0),
+                                 d.noise_cells_per_step * scale, d.seed)
         if d.n_parcels:
             engine.set_parcels(parcels_in_sphere(d.center, d.radius, d.n_parcels, d.parcel_seed),
                                self.parcel_offset(k))
@@ -171,6 +176,22 @@ def box96(seed: int = 7, impulse_scale: float = 1.0) -> Scene:
                                          16384, seed + 2)])
 
 
+def box192_adjoint(impulse_scale=(1.0, 1.0, 1.0), shift=((0.0, 0.0, 0.0),) * 3, edge_cells: float = 2.0) -> Scene:
+    """The box192 drops, all released at step 0 as soft-edged drops (edge
+    `edge_cells` wide, so the loss is differentiable in their centres), 64
+    steps: the full-size forward + adjoint case.  impulse_scale / shift
+    perturb each drop's velocity and centre (for targets and differences)."""
+    sc = box192()
+    sc.name = "box192_adjoint"
+    sc.steps = 64
+    for k, d in enumerate(sc.drops):
+        d.release_step = 0
+        d.edge_cells = edge_cells
+        d.w_cells_per_step *= impulse_scale[k]
+        d.center = tuple(float(d.center[j] + shift[k][j]) for j in range(3))
+    return sc
+
+
 def box192_mixed_1e8() -> Scene:
     sc = box192(abi.DOB_PREC_MIXED)
     sc.name = "box192_mixed_1e8"
@@ -179,5 +200,5 @@ def box192_mixed_1e8() -> Scene:
     return sc
 
 
-SCENES = {"box48": box48, "box192": box192, "box96": box96,
+SCENES = {"box48": box48, "box192": box192, "box96": box96, "box192_adjoint": box192_adjoint,
           "box192_mixed": lambda: box192(abi.DOB_PREC_MIXED), "box192_mixed_1e8": box192_mixed_1e8}

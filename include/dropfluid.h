@@ -232,6 +232,16 @@ dob_status dob_inject_sphere(dob_ctx* ctx, const float center[3], float radius,
                              float dye, const float vel[3], float noise_sigma,
                              uint64_t seed);
 
+/* Closed box, no counterpart in the reference: a soft-edged drop added to
+   the fields.  Weight w = 1 within radius - edge/2 of the centre, 0 beyond
+   radius + edge/2, smoothstep in between (continuously differentiable in the
+   centre); dye += w dye on the dye grid and each MAC face += w (vel +
+   N(0, noise_sigma) noise).  Additive, so its derivative in the drop's
+   parameters does not depend on the state it is added to
+   (dob_adjoint_sphere_soft).  edge > 0. */
+dob_status dob_inject_sphere_soft(dob_ctx* ctx, const float center[3], float radius, float edge,
+                                  float dye, const float vel[3], float noise_sigma, uint64_t seed);
+
 /* Parcels: AoS, 8 floats (32 B) each = RbcParcel (particles.ts:17-20).
    dob_set_parcels writes n parcels at ring index `offset` and raises the
    high-water mark; dob_get_parcels reads n parcels from `offset`. */
@@ -339,6 +349,15 @@ dob_status dob_tape_backward(dob_ctx* ctx, const float* dye_grad, size_t bytes);
    (+ noise). */
 dob_status dob_adjoint_sphere_impulse(dob_ctx* ctx, const float center[3], float radius, const float vel[3],
                                       double* out);
+
+/* Gradient of the loss in the parameters of a dob_inject_sphere_soft drop
+   (same arguments) from the adjoint fields DOB_FIELD_ADJ_VEL_U/V/W and
+   DOB_FIELD_ADJ_CONC of the state right after the drop (after
+   dob_tape_backward: the trajectory's initial state).  out[0] = d loss / d s
+   for injected velocity s * vel at s = 1 (the noise is not scaled); out[1..3]
+   = d loss / d center (world units).  Closed box, FP32, dye_refine 1. */
+dob_status dob_adjoint_sphere_soft(dob_ctx* ctx, const float center[3], float radius, float edge, float dye,
+                                   const float vel[3], float noise_sigma, uint64_t seed, double out[4]);
 
 /* Evaluate the library's own elementary functions on the device (used to
    check them against the host build bit for bit).  fn: 0 sin, 1 cos, 2 exp,

@@ -87,6 +87,20 @@ template <class R> inline V3<R> MixV(V3<R> a, V3<R> b, R t) {
 }
 template <class R> inline V3<R> Normalize(V3<R> a) { return a / Len(a); }
 template <class R> inline R Len2(R x, R y) { return Sqrt(x * x + y * y); }
+// dob_soft_sphere (dob_math.h) in R arithmetic: same operations, so the
+// float instance has the device's bits
+template <class R> inline R SoftSphere(V3<R> p, V3<R> c, R r, R h, V3<R>& g) {
+  const V3<R> dpc = p - c;
+  const R d = Len(dpc);
+  const R t = (r + R(0.5) * h - d) / h;
+  if (!(t > R(0)) || t >= R(1)) {
+    g = mk(R(0), R(0), R(0));
+    return t >= R(1) ? R(1) : R(0);
+  }
+  const R sc = d > R(0) ? R(6) * t * (R(1) - t) / (h * d) : R(0);
+  g = dpc * sc;
+  return t * t * (R(3) - R(2) * t);
+}
 
 struct Dims {
   int nx = 0, ny = 0, nz = 0;
@@ -1512,6 +1526,38 @@ template <class R> class Sim {
         }
   }
 
+  // soft-edged additive drop (dob_inject_sphere_soft)
+  void inject_sphere_soft(const float c[3], float radius, float edge, float dye, const float vel[3], float sigma,
+                          uint64_t seed) {
+    const V3<R> cc = mk((R)c[0], (R)c[1], (R)c[2]);
+    const R rr = (R)radius, hh = (R)edge;
+    const V3<R> dims = vdims();
+    const V3<R> cdm = cdims();
+    V3<R> g;
+    for (int z = 0; z < dc.nz; ++z)
+      for (int y = 0; y < dc.ny; ++y)
+        for (int x = 0; x < dc.nx; ++x) {
+          const V3<R> pw = to_world((mk((R)x, (R)y, (R)z) + mk(R(0.5), R(0.5), R(0.5))) / cdm);
+          const R wt = SoftSphere(pw, cc, rr, hh, g);
+          const size_t k = dc.at(x, y, z);
+          if (wt > R(0)) conc[0][k] = st_dye(conc[0][k] + wt * (R)dye);
+        }
+    for (int z = 0; z < dv.nz; ++z)
+      for (int y = 0; y < dv.ny; ++y)
+        for (int x = 0; x < dv.nx; ++x) {
+          const size_t i = dv.at(x, y, z);
+          const V3<R> fx = to_world(mk((R)x + R(1), (R)y + R(0.5), (R)z + R(0.5)) / dims);
+          const V3<R> fy = to_world(mk((R)x + R(0.5), (R)y + R(1), (R)z + R(0.5)) / dims);
+          const V3<R> fz = to_world(mk((R)x + R(0.5), (R)y + R(0.5), (R)z + R(1)) / dims);
+          R wt = SoftSphere(fx, cc, rr, hh, g);
+          if (x < dv.nx - 1 && wt > R(0)) u[i] = st_vel(u[i] + wt * (R)(vel[0] + sigma * dob_sphere_noise(seed, i, 0)));
+          wt = SoftSphere(fy, cc, rr, hh, g);
+          if (y < dv.ny - 1 && wt > R(0)) v[i] = st_vel(v[i] + wt * (R)(vel[1] + sigma * dob_sphere_noise(seed, i, 1)));
+          wt = SoftSphere(fz, cc, rr, hh, g);
+          if (z < dv.nz - 1 && wt > R(0)) w[i] = st_vel(w[i] + wt * (R)(vel[2] + sigma * dob_sphere_noise(seed, i, 2)));
+        }
+  }
+
   // ---- statistics -------------------------------------------------------------------------------
   double max_div() const {
     const double scale = ref ? 1.0 : (double)cfg.dt / (double)cfg.dx;
@@ -1840,6 +1886,13 @@ int orc_inject_sphere(orc_sim* s, const float c[3], float r, float dye, const fl
   DISPATCH(s, inject_sphere(c, r, dye, vel, sigma, seed));
   return DOB_OK;
 }
+int orc_inject_sphere_soft(orc_sim* s, const float c[3], float r, float edge, float dye, const float vel[3],
+                           float sigma, uint64_t seed) {
+  if (DISPATCH(s, ref)) return DOB_ESTATE;
+  if (!(r > 0.0f) || !(edge > 0.0f)) return DOB_EINVAL;
+  DISPATCH(s, inject_sphere_soft(c, r, edge, dye, vel, sigma, seed));
+  return DOB_OK;
+}
 int orc_set_parcels(orc_sim* s, const float* p, uint32_t n, uint32_t off) {
   return s->a.f64 ? set_par(s->a.sd, p, n, off) : set_par(s->a.sf, p, n, off);
 }
@@ -1887,6 +1940,12 @@ int orc_tape_backward(orc_sim* s, const float* dye_grad, size_t bytes) {
 int orc_sphere_impulse(orc_sim* s, const float c[3], float radius, const float vel[3], double* out) {
   if (!out) return DOB_EINVAL;
   *out = DISPATCH(s, sphere_impulse(c, radius, vel));
+  return DOB_OK;
+}
+int orc_sphere_soft_grad(orc_sim* s, const float c[3], float radius, float edge, float dye, const float vel[3],
+                         float sigma, uint64_t seed, double out[4]) {
+  if (!out || !(radius > 0.0f) || !(edge > 0.0f)) return DOB_EINVAL;
+  DISPATCH(s, sphere_soft_grad(c, radius, edge, dye, vel, sigma, seed, out));
   return DOB_OK;
 }
 int orc_get_field64(orc_sim* s, int field, double* host, size_t n) {

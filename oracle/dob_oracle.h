@@ -29,6 +29,8 @@ int orc_reset(orc_sim* s);
 int orc_set_uniforms(orc_sim* s, const float u[128]);
 int orc_inject_sphere(orc_sim* s, const float center[3], float radius, float dye,
                       const float vel[3], float noise_sigma, uint64_t seed);
+int orc_inject_sphere_soft(orc_sim* s, const float center[3], float radius, float edge, float dye,
+                           const float vel[3], float noise_sigma, uint64_t seed);
 int orc_set_parcels(orc_sim* s, const float* p, uint32_t n, uint32_t offset);
 int orc_get_parcels(orc_sim* s, float* p, uint32_t n, uint32_t offset);
 int orc_set_high_water(orc_sim* s, uint32_t hw);
@@ -46,6 +48,8 @@ int orc_adjoint_stage(orc_sim* s, int stage);
 int orc_tape_forward(orc_sim* s, int nsteps);
 int orc_tape_backward(orc_sim* s, const float* dye_grad, size_t bytes);
 int orc_sphere_impulse(orc_sim* s, const float center[3], float radius, const float vel[3], double* out);
+int orc_sphere_soft_grad(orc_sim* s, const float center[3], float radius, float edge, float dye,
+                         const float vel[3], float noise_sigma, uint64_t seed, double out[4]);
 /* double-precision access to the velocity, centre, pressure, rhs, dye,
    predictor and adjoint fields (n = element count incl. channels; not
    ADJ_CENTER), for finite differences below float32 resolution */

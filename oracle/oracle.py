@@ -50,6 +50,10 @@ def lib():
         L.orc_set_uniforms.argtypes = [P, C.POINTER(C.c_float)]
         L.orc_inject_sphere.argtypes = [P, C.POINTER(C.c_float), C.c_float, C.c_float,
                                         C.POINTER(C.c_float), C.c_float, C.c_uint64]
+        L.orc_inject_sphere_soft.argtypes = [P, C.POINTER(C.c_float), C.c_float, C.c_float, C.c_float,
+                                             C.POINTER(C.c_float), C.c_float, C.c_uint64]
+        L.orc_sphere_soft_grad.argtypes = [P, C.POINTER(C.c_float), C.c_float, C.c_float, C.c_float,
+                                           C.POINTER(C.c_float), C.c_float, C.c_uint64, C.POINTER(C.c_double)]
         L.orc_set_parcels.argtypes = [P, C.POINTER(C.c_float), C.c_uint32, C.c_uint32]
         L.orc_get_parcels.argtypes = [P, C.POINTER(C.c_float), C.c_uint32, C.c_uint32]
         L.orc_set_high_water.argtypes = [P, C.c_uint32]
@@ -136,6 +140,20 @@ class OracleSim:
         v = np.asarray(vel, dtype=np.float32)
         _check(lib().orc_inject_sphere(self._h, _fptr(c), float(radius), float(dye), _fptr(v),
                                        float(noise_sigma), int(seed)), "inject_sphere")
+
+    def inject_sphere_soft(self, center, radius, edge, dye, vel, noise_sigma=0.0, seed=0):
+        c = np.asarray(center, dtype=np.float32)
+        v = np.asarray(vel, dtype=np.float32)
+        _check(lib().orc_inject_sphere_soft(self._h, _fptr(c), float(radius), float(edge), float(dye), _fptr(v),
+                                            float(noise_sigma), int(seed)), "inject_sphere_soft")
+
+    def sphere_soft_grad(self, center, radius, edge, dye, vel, noise_sigma=0.0, seed=0):
+        c = np.asarray(center, dtype=np.float32)
+        v = np.asarray(vel, dtype=np.float32)
+        out = (C.c_double * 4)()
+        _check(lib().orc_sphere_soft_grad(self._h, _fptr(c), float(radius), float(edge), float(dye), _fptr(v),
+                                          float(noise_sigma), int(seed), out), "sphere_soft_grad")
+        return out[0], np.array(out[1:4], dtype=np.float64)
 
     def set_parcels(self, parcels, offset=0):
         p = np.ascontiguousarray(parcels, dtype=np.float32).reshape(-1, 8)

@@ -112,3 +112,18 @@ def drop_scene(n=(24, 32, 24), levels=3):
 def init_drop(engine, center, radius, impulse=1.0):
     engine.reset()
     engine.inject_sphere(center, radius, 1.0, [0.0, -2.0 * impulse, 0.0], 0.05, 7)
+
+
+SOFT_EDGE = 2.0  # world units (cells at dx = 1)
+
+
+def init_soft_drop(engine, center, radius, impulse=1.0, edge=SOFT_EDGE):
+    """Rest state plus a soft-edged drop (dob_inject_sphere_soft) moving down
+    at 2 cells/step times `impulse`, with N(0, 0.05) face noise."""
+    engine.reset()
+    engine.inject_sphere_soft(center, radius, edge, 1.0, [0.0, -2.0 * impulse, 0.0], 0.05, 7)
+
+
+def soft_drop_grad(engine, center, radius, edge=SOFT_EDGE):
+    """(d loss / d impulse, d loss / d centre) after tape_backward."""
+    return engine.sphere_soft_grad(center, radius, edge, 1.0, [0.0, -2.0, 0.0], 0.05, 7)

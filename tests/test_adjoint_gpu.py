@@ -141,3 +141,63 @@ def test_adjoint_rejects_other_modes(gpu_lib):
             sim.tape_backward(np.zeros((16, 24, 16), np.float32))  # nothing recorded
         with pytest.raises(DropFluidError):
             sim.adjoint_stage(abi.STAGE_CLEAR_SPLATS)
+
+
+def test_soft_injection_bit_exact(gpu_lib, oracle_mod):
+    """dob_inject_sphere_soft (compiled without FMA contraction) adds the
+    same bits as the FP32 oracle's restatement, also on top of a drop that
+    is already there."""
+    from dropfluid import DropFluid
+    cfg, center, r = AC.drop_scene((24, 32, 24))
+    g = DropFluid(cfg)
+    o = oracle_mod.OracleSim(cfg, fp64=False)
+    for e in (g, o):
+        AC.init_soft_drop(e, center, r, 1.0)
+        e.inject_sphere_soft([center[0] + 1.3, center[1], center[2] - 0.7], 3.0, 1.5, 0.5, [0.5, -1.0, 0.25], 0.1, 3)
+    for f in (abi.FIELD_VEL_U, abi.FIELD_VEL_V, abi.FIELD_VEL_W, abi.FIELD_CONC):
+        a, b = g.get_field(f), o.get_field(f)
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), f
+    assert np.count_nonzero(g.get_field(abi.FIELD_CONC)) > 0
+    g.close()
+
+
+def test_soft_drop_gradient(gpu_lib, oracle_mod):
+    """Impulse and centre gradient of a soft drop's trajectory: the device
+    against the FP64 oracle (1e-3), and against central differences of the
+    device loss (impulse 1e-3; centre, whose FP32 differences need a 0.05-cell
+    step, 1e-2 of the gradient's norm)."""
+    from dropfluid import DropFluid
+    cfg, center, r = AC.drop_scene((24, 32, 24))
+    g = DropFluid(cfg)
+    o = oracle_mod.OracleSim(cfg, fp64=True)
+    steps = 8
+    shifted = [center[0] + 0.3, center[1] - 0.2, center[2] + 0.25]
+    AC.init_soft_drop(o, shifted, r, 1.1)
+    o.tape_forward(steps)
+    target = o.get_field64(abi.FIELD_CONC)
+
+    def run(e, c, imp, k=None):
+        AC.init_soft_drop(e, c, r, imp)
+        e.tape_forward(steps, k or steps)
+        d = np.asarray(e.get_field(abi.FIELD_CONC), np.float64) - target
+        return float(np.sum(d * d)), d
+
+    grads = {}
+    for name, e, k in (("gpu", g, 4), ("orc", o, None)):
+        _, d = run(e, center, 1.0, k)
+        e.tape_backward((2 * d).astype(np.float32))
+        grads[name] = AC.soft_drop_grad(e, center, r)
+    (gi, gp), (oi, op) = grads["gpu"], grads["orc"]
+    assert abs(gi - oi) <= 1e-3 * abs(oi), (gi, oi)
+    assert np.linalg.norm(gp - op) <= 1e-3 * np.linalg.norm(op), (gp, op)
+    h = 1e-2
+    fd = (run(g, center, 1.0 + h, 4)[0] - run(g, center, 1.0 - h, 4)[0]) / (2 * h)
+    assert abs(fd - gi) <= 1e-3 * abs(fd), (fd, gi)
+    eps = 5e-2
+    for k in range(3):
+        cp, cm = list(center), list(center)
+        cp[k] = float(np.float32(center[k] + eps))
+        cm[k] = float(np.float32(center[k] - eps))
+        fdk = (run(g, cp, 1.0, 4)[0] - run(g, cm, 1.0, 4)[0]) / (cp[k] - cm[k])
+        assert abs(fdk - gp[k]) <= 1e-2 * np.linalg.norm(gp), (k, fdk, gp)
+    g.close()
