@@ -38,6 +38,7 @@ struct AdjCtx {
   std::vector<float*> Tua, Tva, Twa, Tpred;  // k entries
   float* Tp = nullptr;
   float* Trhs = nullptr;
+  float* Tsc[3] = {nullptr, nullptr, nullptr};  // Casson's output during recomputation (no adjoint reads it)
   double* dred = nullptr;   // reduction slots of the drop gradients (4 doubles)
   // captured "recompute + reverse" graph of a segment, per (length, parity of
   // the dye adjoint ping-pong at its start)
@@ -150,6 +151,7 @@ dob_status ensure_tape(dob_ctx* ctx, int k, int nseg) {
     }
     F((void**)&A->Tp, N * 4);
     F((void**)&A->Trhs, N * 4);
+    for (int c = 0; c < 3; ++c) F((void**)&A->Tsc[c], N * 4);
     if (st != DOB_OK) return st;
     A->k = k;
   }
@@ -210,15 +212,18 @@ void replay_segment(dob_ctx* ctx, int len) {
     t.u = A->Tu[j]; t.v = A->Tv[j]; t.w = A->Tw[j]; t.cen = A->Tcen[j];
     t.u2 = A->Tua[j]; t.v2 = A->Tva[j]; t.w2 = A->Twa[j];
     launch_advect_mac(t, st);
+    // Casson's output (the unprojected velocity, which no adjoint stage
+    // reads) goes to scratch; the projection writes the next step's velocity
+    // and centre velocity into the tape.  The column kernels give the bits of
+    // the step graph's.
     t.u = A->Tua[j]; t.v = A->Tva[j]; t.w = A->Twa[j]; t.conc = A->Tc[j];
-    t.u2 = A->Tu[j + 1]; t.v2 = A->Tv[j + 1]; t.w2 = A->Tw[j + 1];
-    launch_casson(t, st);
-    t.u = A->Tu[j + 1]; t.v = A->Tv[j + 1]; t.w = A->Tw[j + 1];
-    launch_mac_rhs(t, st);
+    t.u2 = A->Tsc[0]; t.v2 = A->Tsc[1]; t.w2 = A->Tsc[2];
+    launch_casson_box(t, st);
+    t.u = A->Tsc[0]; t.v = A->Tsc[1]; t.w = A->Tsc[2];
+    launch_mac_rhs_box(t, st);
     launch_pressure_solve(t, st);
-    launch_project(t, st);
-    t.cen = A->Tcen[j + 1];
-    launch_mac_to_center(t, st);
+    t.u2 = A->Tu[j + 1]; t.v2 = A->Tv[j + 1]; t.w2 = A->Tw[j + 1]; t.cen = A->Tcen[j + 1];
+    launch_project_center_box(t, st);
     t.conc = A->Tc[j]; t.pred = A->Tpred[j]; t.conc2 = A->Tc[j + 1];
     launch_conc_predict(t, st);
     launch_conc_resolve(t, st);

@@ -376,6 +376,8 @@ enum { ADJ_SWEEP_FIRST = 0, ADJ_SWEEP_FUSED = 1, ADJ_SWEEP_FINAL = 2 };
 //   FUSED  bb += -h2 xb/diag; xb = sum_n xb(n)/diag(n)
 //   FINAL  bb += -h2 xb/diag; xb = 0
 __global__ void __launch_bounds__(256) k_adj_rbgs(Grid d, int color, float h2, int ref, int mode, float* xb, float* bb) {
+  pdl_wait();
+  pdl_trigger();
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int z = blockIdx.z;
@@ -407,6 +409,8 @@ __device__ __forceinline__ float f4at(const float4& v, int j) {
 }
 __global__ void __launch_bounds__(256) k_adj_rbgs_v4(Grid d, int color, float h2, int ref, int mode, float* __restrict__ a,
                                                      float* __restrict__ bb) {
+  pdl_wait();
+  pdl_trigger();
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int z = blockIdx.z;
@@ -486,6 +490,8 @@ __global__ void __launch_bounds__(256) k_adj_rbgs_v4(Grid d, int color, float h2
 template <int CS>
 __global__ void __cluster_dims__(CS, 1, 1) __launch_bounds__(512)
     k_adj_coarse_cluster(Grid d, float h2, int ref, int sweeps, float* __restrict__ eb, float* __restrict__ bb) {
+  pdl_wait();
+  pdl_trigger();
   cg::cluster_group cl = cg::this_cluster();
   extern __shared__ float asm_[];
   const int rank = (int)cl.block_rank();
@@ -579,6 +585,8 @@ __device__ __forceinline__ float cval(const float* a, const Grid& c, uint32_t ha
 // Transposed residual + restriction, the mirror of k_residual_restrict2.
 __global__ void __launch_bounds__(256) k_adj_restrict2(Grid f, Grid c, float inv_h2, int ref, const float* __restrict__ Bb,
                                                        float* __restrict__ xb, float* __restrict__ bb) {
+  pdl_wait();
+  pdl_trigger();
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   const int Y = blockIdx.y * blockDim.y + threadIdx.y;
   const int Z = blockIdx.z;
@@ -652,6 +660,8 @@ __global__ void __launch_bounds__(256) k_adj_restrict2(Grid f, Grid c, float inv
 // each axis.
 __global__ void __launch_bounds__(256) k_adj_prolong2(Grid f, Grid c, int ref, const float* __restrict__ xb,
                                                       float* __restrict__ Eb) {
+  pdl_wait();
+  pdl_trigger();
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   const int Y = blockIdx.y * blockDim.y + threadIdx.y;
   const int Z = blockIdx.z;
@@ -844,43 +854,63 @@ static void adj_smooth(const Grid& d, float h2, int ref, int sweeps, float* xb, 
   auto color_of = [](int k) { return (k - 1) & 1; };  // half-sweep k = 1..K
   if (d.nx % 8 == 0) {
     const dim3 b = qblock(d), g = qgrid(d, b);
-    k_adj_rbgs_v4<<<g, b, 0, st>>>(d, color_of(K), h2, ref, ADJ4_SCALE, xb, bb);
-    k_adj_rbgs_v4<<<g, b, 0, st>>>(d, 1 - color_of(K), h2, ref, ADJ4_FIRST, xb, bb);
-    for (int k = K; k >= 2; --k) k_adj_rbgs_v4<<<g, b, 0, st>>>(d, color_of(k), h2, ref, ADJ4_FUSED, xb, bb);
-    k_adj_rbgs_v4<<<g, b, 0, st>>>(d, color_of(1), h2, ref, ADJ4_FINAL, xb, bb);
-    k_adj_rbgs_v4<<<g, b, 0, st>>>(d, 1 - color_of(1), h2, ref, ADJ4_UNSCALE, xb, bb);
+    launch_pdl(k_adj_rbgs_v4, g, b, 0, st, d, color_of(K), h2, ref, (int)ADJ4_SCALE, xb, bb);
+    launch_pdl(k_adj_rbgs_v4, g, b, 0, st, d, 1 - color_of(K), h2, ref, (int)ADJ4_FIRST, xb, bb);
+    for (int k = K; k >= 2; --k) launch_pdl(k_adj_rbgs_v4, g, b, 0, st, d, color_of(k), h2, ref, (int)ADJ4_FUSED, xb, bb);
+    launch_pdl(k_adj_rbgs_v4, g, b, 0, st, d, color_of(1), h2, ref, (int)ADJ4_FINAL, xb, bb);
+    launch_pdl(k_adj_rbgs_v4, g, b, 0, st, d, 1 - color_of(1), h2, ref, (int)ADJ4_UNSCALE, xb, bb);
     return;
   }
-  k_adj_rbgs<<<hgrid(d), cblock(), 0, st>>>(d, 1 - color_of(K), h2, ref, ADJ_SWEEP_FIRST, xb, bb);
+  launch_pdl(k_adj_rbgs, hgrid(d), cblock(), 0, st, d, 1 - color_of(K), h2, ref, (int)ADJ_SWEEP_FIRST, xb, bb);
   for (int k = K; k >= 2; --k)
-    k_adj_rbgs<<<hgrid(d), cblock(), 0, st>>>(d, color_of(k), h2, ref, ADJ_SWEEP_FUSED, xb, bb);
-  k_adj_rbgs<<<hgrid(d), cblock(), 0, st>>>(d, color_of(1), h2, ref, ADJ_SWEEP_FINAL, xb, bb);
+    launch_pdl(k_adj_rbgs, hgrid(d), cblock(), 0, st, d, color_of(k), h2, ref, (int)ADJ_SWEEP_FUSED, xb, bb);
+  launch_pdl(k_adj_rbgs, hgrid(d), cblock(), 0, st, d, color_of(1), h2, ref, (int)ADJ_SWEEP_FINAL, xb, bb);
 }
 template <int CS>
 static void adj_cluster(const MgLevel& L, int ref, int sweeps, float* eb, float* bb, cudaStream_t st) {
   const size_t smem = 2 * (L.d.n() / CS) * sizeof(float);
-  k_adj_coarse_cluster<CS><<<CS, 512, smem, st>>>(L.d, L.h2, ref, sweeps, eb, bb);
+  launch_pdl(k_adj_coarse_cluster<CS>, dim3(CS), dim3(512), smem, st, L.d, L.h2, ref, sweeps, eb, bb);
 }
 // Transpose of the exact coarsest solve e = M b (M symmetric):
-// Bbar += M Ebar, Ebar = 0.
-__global__ void __launch_bounds__(1024) k_adj_coarse_dense(Grid d, const float* __restrict__ M, int n,
-                                                           float* __restrict__ eb, float* __restrict__ bb) {
-  extern __shared__ float sev[];
-  const int j = threadIdx.x;
-  const int x = j % d.nx, y = (j / d.nx) % d.ny, z = j / (d.nx * d.ny);
-  const size_t rj = rb_index(d, x, y, z);
-  sev[j] = eb[rj];
+// Bbar += M Ebar (Ebar is cleared by the caller afterwards).  CTA c forms
+// rows 32c..32c+31 like k_coarse_dense: lane l of warp w sums
+// M[i][32c + l] Ebar[i] over i = w, w + 8, ..., the warps' partial sums are
+// added in shared memory.
+__global__ void __launch_bounds__(256) k_adj_coarse_dense(Grid d, const float* __restrict__ M, int n,
+                                                          const float* __restrict__ eb, float* __restrict__ bb) {
+  pdl_wait();
+  pdl_trigger();
+  extern __shared__ float sev[];  // Ebar in natural order (n), then 8 x 32 partial sums
+  float* part = sev + n;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const int x = i % d.nx, y = (i / d.nx) % d.ny, z = i / (d.nx * d.ny);
+    sev[i] = eb[rb_index(d, x, y, z)];
+  }
   __syncthreads();
-  eb[rj] = 0.0f;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int j = blockIdx.x * 32 + lane;
   float acc = 0.0f;
-  for (int i = 0; i < n; ++i) acc = fmaf(M[(size_t)i * n + j], sev[i], acc);
-  bb[rj] += acc;
+  if (j < n) {
+#pragma unroll 4
+    for (int i = w; i < n; i += 8) acc = fmaf(M[(size_t)i * n + j], sev[i], acc);
+  }
+  part[w * 32 + lane] = acc;
+  __syncthreads();
+  if (w == 0 && j < n) {
+    float sum = part[lane];
+#pragma unroll
+    for (int k = 1; k < 8; ++k) sum += part[k * 32 + lane];
+    const int x = j % d.nx, y = (j / d.nx) % d.ny, z = j / (d.nx * d.ny);
+    bb[rb_index(d, x, y, z)] += sum;
+  }
 }
 // Transpose of the coarsest-grid solve; Ebar is zero on return.
 static void adj_coarse(const DevState& s, const MgLevel& L, int ref, int sweeps, float* eb, float* bb,
                        cudaStream_t st) {
   if (s.coarse_sweeps < 0) {
-    k_adj_coarse_dense<<<1, s.cn, s.cn * sizeof(float), st>>>(L.d, s.cinv, s.cn, eb, bb);
+    launch_pdl(k_adj_coarse_dense, dim3((s.cn + 31) / 32), dim3(256), (s.cn + 256) * sizeof(float), st, L.d, s.cinv,
+               s.cn, (const float*)eb, bb);
+    cudaMemsetAsync(eb, 0, L.d.n() * sizeof(float), st);
     return;
   }
   int cs = 0;
@@ -920,13 +950,13 @@ static inline dim3 pgrid(const Grid& c, const dim3& b) {
 static void adj_restrict(const DevState& s, const AdjState& a, int l, float* xb, float* bb, cudaStream_t st) {
   const Grid f = s.lv[l].d, c = s.lv[l + 1].d;  // nx % 4 == 0 on every transfer level
   const dim3 b = pblock(c);
-  k_adj_restrict2<<<pgrid(c, b), b, 0, st>>>(f, c, 1.0f / s.lv[l].h2, s.ref, a.lb[l + 1], xb, bb);
+  launch_pdl(k_adj_restrict2, pgrid(c, b), b, 0, st, f, c, 1.0f / s.lv[l].h2, s.ref, a.lb[l + 1], xb, bb);
   cudaMemsetAsync(a.lb[l + 1], 0, c.n() * sizeof(float), st);
 }
 static void adj_prolong(const DevState& s, const AdjState& a, int l, const float* xb, cudaStream_t st) {
   const Grid f = s.lv[l].d, c = s.lv[l + 1].d;
   const dim3 b = pblock(c);
-  k_adj_prolong2<<<pgrid(c, b), b, 0, st>>>(f, c, s.ref, xb, a.le[l + 1]);
+  launch_pdl(k_adj_prolong2, pgrid(c, b), b, 0, st, f, c, s.ref, xb, a.le[l + 1]);
 }
 // Transpose of one V-cycle (k_mg.cu vcycle) on (ap, arhs); the coarse
 // adjoint arrays are zero on entry and on exit.
