@@ -359,7 +359,7 @@ __global__ void __launch_bounds__(256) k_residual_restrict2(Grid f, Grid c, floa
 // Y-1..Y+1 x Z-1..Z+1 (clamped; 0 above a Dirichlet top) are loaded once and
 // the 16 fine cells are updated with two 8-byte read-modify-writes per fine
 // row.  Weights use the same per-cell formula as k_prolong_add.
-template <class T, class TC>
+template <class T, class TC, bool BLACK>
 __global__ void __launch_bounds__(256) k_prolong_add2(Grid f, Grid c, int ref, T* __restrict__ a,
                                                       const TC* __restrict__ e, const unsigned int* __restrict__ skip) {
   pdl_wait();
@@ -420,29 +420,35 @@ __global__ void __launch_bounds__(256) k_prolong_add2(Grid f, Grid c, int ref, T
         const float x11 = dob_mix(t[dz + 1][dy + 1][bi], t[dz + 1][dy + 1][bi + 1], fx);
         corr[i] = dob_mix(dob_mix(x00, x10, fy), dob_mix(x01, x11, fy), fz);
       }
-      T* pe = a + (par ? half : 0u) + r;
-      T* po = a + (par ? 0u : half) + r;
-      const float2 ve = Pair<T>::ld(pe), vo = Pair<T>::ld(po);
-      Pair<T>::st(pe, make_float2(ve.x + corr[0], ve.y + corr[2]));
-      Pair<T>::st(po, make_float2(vo.x + corr[1], vo.y + corr[3]));
+      if (BLACK) {  // only the colour-1 pair of the row: cells x = 4q + par, 4q + par + 2
+        T* pb = a + half + r;
+        const float2 vb = Pair<T>::ld(pb);
+        Pair<T>::st(pb, par ? make_float2(vb.x + corr[0], vb.y + corr[2]) : make_float2(vb.x + corr[1], vb.y + corr[3]));
+      } else {
+        T* pe = a + (par ? half : 0u) + r;
+        T* po = a + (par ? 0u : half) + r;
+        const float2 ve = Pair<T>::ld(pe), vo = Pair<T>::ld(po);
+        Pair<T>::st(pe, make_float2(ve.x + corr[0], ve.y + corr[2]));
+        Pair<T>::st(po, make_float2(vo.x + corr[1], vo.y + corr[3]));
+      }
     }
 }
 
 // Exact coarsest-grid solve e = M b with the dense symmetric inverse M
 // (n <= 1024 cells).  CTA c forms rows 32c..32c+31 of e: b is gathered into
 // shared memory in natural order, lane l of warp w sums M[i][32c + l] b[i]
-// over i = w, w + 8, ... (M is symmetric, so column 32c + l is row 32c + l;
-// each warp reads 128 consecutive bytes per i), and the eight warps' partial
-// sums are added in shared memory.  n/32 CTAs read M (up to 4 MB, resident
+// over i = w, w + 32, ... (M is symmetric, so column 32c + l is row 32c + l;
+// each warp reads 128 consecutive bytes per i; 32 warps keep n/32 loads per
+// lane independent), and the warps' partial sums are added in shared memory.  n/32 CTAs read M (up to 4 MB, resident
 // in L2 across cycles) in parallel instead of one SM reading all of it.
 template <class T>
-__global__ void __launch_bounds__(256) k_coarse_dense(Grid d, const float* __restrict__ M, int n,
+__global__ void __launch_bounds__(1024) k_coarse_dense(Grid d, const float* __restrict__ M, int n,
                                                       T* __restrict__ e, const T* __restrict__ b,
                                                       const unsigned int* __restrict__ skip) {
   pdl_wait();
   pdl_trigger();
   if (skip_now(skip)) return;
-  extern __shared__ float sbv[];  // b in natural order (n), then 8 x 32 partial sums
+  extern __shared__ float sbv[];  // b in natural order (n), then 32 x 32 partial sums
   float* part = sbv + n;
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     const int x = i % d.nx, y = (i / d.nx) % d.ny, z = i / (d.nx * d.ny);
@@ -453,15 +459,15 @@ __global__ void __launch_bounds__(256) k_coarse_dense(Grid d, const float* __res
   const int j = blockIdx.x * 32 + lane;
   float acc = 0.0f;
   if (j < n) {
-#pragma unroll 4
-    for (int i = w; i < n; i += 8) acc = fmaf(M[(size_t)i * n + j], sbv[i], acc);
+#pragma unroll 8
+    for (int i = w; i < n; i += 32) acc = fmaf(M[(size_t)i * n + j], sbv[i], acc);
   }
   part[w * 32 + lane] = acc;
   __syncthreads();
   if (w == 0 && j < n) {
     float sum = part[lane];
 #pragma unroll
-    for (int k = 1; k < 8; ++k) sum += part[k * 32 + lane];
+    for (int k = 1; k < 32; ++k) sum += part[k * 32 + lane];
     const int x = j % d.nx, y = (j / d.nx) % d.ny, z = j / (d.nx * d.ny);
     stf(e + rb_index(d, x, y, z), sum);
   }
@@ -991,9 +997,13 @@ static void smooth(const DevState& s, int l, T* a, const T* b, int sweeps, bool 
   const MgLevel& L = s.lv[l];
   if (zero_first && sweeps == 0) launch_pdl(k_fill_zero<T>, dim3(s.num_sms * 2), dim3(256), 0, st, a, L.d.n(), skip);
   if (ec) {
+    // With a sweep to follow, only the black cells need the correction: the
+    // red half-sweep overwrites every red cell without reading it, and the
+    // black half-sweep then overwrites the black ones (same bits either way).
     const Grid dc = s.lv[l + 1].d;
     const dim3 bp = pair_block(dc);  // every transfer level has nx % 4 == 0
-    launch_pdl(k_prolong_add2<T, TC>, pair_grid(dc, bp), bp, 0, st, L.d, dc, s.ref, a, ec, skip);
+    if (sweeps > 0) launch_pdl(k_prolong_add2<T, TC, true>, pair_grid(dc, bp), bp, 0, st, L.d, dc, s.ref, a, ec, skip);
+    else launch_pdl(k_prolong_add2<T, TC, false>, pair_grid(dc, bp), bp, 0, st, L.d, dc, s.ref, a, ec, skip);
   }
   for (int k = 0; k < sweeps; ++k)
     for (int c = 0; c < 2; ++c) half_sweep<T>(s, l, c, zero_first && k == 0 && c == 0, a, b, skip, st);
@@ -1010,8 +1020,8 @@ template <class T>
 static void coarse_solve(const DevState& s, int l, T* e, const T* b, const unsigned int* skip, cudaStream_t st) {
   const MgLevel& L = s.lv[l];
   if (s.coarse_sweeps < 0) {  // exact: e = M b with the precomputed inverse
-    launch_pdl(k_coarse_dense<T>, dim3((s.cn + 31) / 32), dim3(256), (s.cn + 256) * sizeof(float), st, L.d, s.cinv,
-               s.cn, e, b, skip);
+    launch_pdl(k_coarse_dense<T>, dim3((s.cn + 31) / 32), dim3(1024), (s.cn + 1024) * sizeof(float), st, L.d,
+               s.cinv, s.cn, e, b, skip);
     return;
   }
   int cs = 0;
