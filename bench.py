@@ -10,6 +10,7 @@ same scene and the discrete adjoint are measured beside it.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
   python bench.py --accuracy      # FP32 and mixed vs an FP64 run at steps 50/100/200
+  python bench.py --configs       # per-configuration GPU and host-core throughput
 
 Multi-GPU: the step does not exchange data between replicas on this pool
 (one GPU per box): N ranks run N independent replicas ("scaling": "weak");
@@ -372,6 +373,81 @@ def accuracy_run():
             "gpu_s": t_gpu, "fp64_cpu_s": t_cpu}
 
 
+def reference_block(sim_time=0.5, spawn=512, cursor=0):
+    """Uniform block of the reference-mode scene: two active drop slots
+    draining into the free surface (a fixed stand-in for the reference's
+    drop-lifecycle model, which is host input), dt = 1/60."""
+    from dropfluid import uniforms as U
+    snap = U.DropSnapshot(sim_time=sim_time, active_count=2)
+    snap.slots[0] = U.DropSlot(active=True, center=(0.03, 0.285, -0.02), radius=0.05, vel_y=-0.3,
+                               oscillation=0.01, vol_drain_rate=0.42, seed=1.5)
+    snap.slots[1] = U.DropSlot(active=True, center=(-0.12, 0.31, 0.09), radius=0.03, vel_y=-0.5,
+                               oscillation=0.0, vol_drain_rate=0.05, seed=2.7)
+    return U.SimUniformPacker().pack(drops=snap, dt=U.FIXED_SIM_DT, global_seed=1.5, spawn_cursor=cursor,
+                                     spawn_count=spawn).copy()
+
+
+def configs_report():
+    """Per configuration: GPU steps/s (graph replays, device time) and the
+    oracle on the host cores (FP32 on all cores and on one, FP64 on all),
+    each the median of 3 runs after 2 warm-up steps; cell-updates/s counts
+    velocity cells."""
+    import oracle
+    from dropfluid import DropFluid, abi, scenes
+    oracle.build()
+    ncores = os.cpu_count() or 1
+
+    def reference96():
+        cfg = abi.config_reference()  # 96x128x96 velocity, 192x256x192 dye, 393216 parcels
+        blk = reference_block()
+
+        def setup(e):
+            e.set_uniforms(blk)
+            e.reset()
+        return cfg, setup
+
+    def scene_setup(sc):
+        def setup(e):
+            for d in sc.releases_at(0):
+                sc.release(e, d)
+        return sc.config, setup
+
+    cases = [("cfg0 box48 (48x64x48, FP32)", scene_setup(scenes.box48()), 20, (20, 20, 20)),
+             ("cfg1 box192 (192x256x192, FP32)", scene_setup(scenes.box192()), 20, (3, 1, 3)),
+             ("cfg3 box96 (96x128x96, FP32)", scene_setup(scenes.box96()), 32, (8, 2, 8)),
+             ("reference mode (96x128x96 velocity, 192x256x192 dye, free-surface top, 2 drops)", reference96(), 20,
+              (2, 1, 2))]
+    out = []
+    for name, (cfg, setup), gsteps, (n32, n1, n64) in cases:
+        cells = cfg.nx * cfg.ny * cfg.nz
+        with DropFluid(cfg) as e:
+            setup(e)
+            e.step(3)
+            ms = e.time_steps(gsteps)
+        gpu = gsteps / (ms / 1e3)
+
+        def cpu(fp64, threads, n):
+            oracle.set_threads(threads)
+            o = oracle.OracleSim(cfg, fp64=fp64)
+            setup(o)
+            o.step(2)
+            runs = []
+            for _ in range(3):
+                t0 = time.perf_counter()
+                o.step(n)
+                runs.append(n / (time.perf_counter() - t0))
+            o.close()
+            v = statistics.median(runs)
+            return {"steps_per_s": v, "cell_updates_per_s": v * cells, "threads": threads,
+                    "sample": f"median of 3 runs of {n} steps"}
+        out.append({"config": name, "cells": cells,
+                    "gpu": {"steps_per_s": gpu, "cell_updates_per_s": gpu * cells, "steps": gsteps},
+                    "cpu_fp32": cpu(False, ncores, n32), "cpu_fp32_1thread": cpu(False, 1, n1),
+                    "cpu_fp64": cpu(True, ncores, n64)})
+        print(json.dumps(out[-1]), flush=True)
+    return {"configs": out, "host_cores": ncores}
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return 0
@@ -410,6 +486,8 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--accuracy", action="store_true",
                     help="error of the FP32 and mixed runs against an FP64 run at steps 50/100/200, then exit")
+    ap.add_argument("--configs", action="store_true",
+                    help="per-configuration GPU and host-core throughput (FP32, FP32 1 thread, FP64), then exit")
     ap.add_argument("--profile-run", action="store_true",
                     help="run only the FP32 scene (warm-up + steps, untimed) and exit: the command "
                          "the ncu launch lists and kernel captures are taken with")
@@ -426,6 +504,10 @@ def main():
     if args.accuracy:
         if rank == 0:
             print(json.dumps(accuracy_run()), flush=True)
+        return 0
+    if args.configs:
+        if rank == 0:
+            print(json.dumps(configs_report()), flush=True)
         return 0
     dist = Dist(world)
 

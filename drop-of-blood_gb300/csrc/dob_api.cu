@@ -76,7 +76,7 @@ static bool valid_config(const dob_config* c, std::string* why) {
     const uint64_t cc = (uint64_t)(c->nx >> (c->mg_levels - 1)) * (c->ny >> (c->mg_levels - 1)) *
                         (c->nz >> (c->mg_levels - 1));
     if (cc > (uint64_t)kDenseCoarseMax)
-      return no("mg_coarse_sweeps = -1 (exact coarsest solve) needs a coarsest grid of at most 1024 cells");
+      return no("mg_coarse_sweeps = -1 (exact coarsest solve) needs a coarsest grid of at most 4096 cells");
   }
   if (c->precision_mode == DOB_PREC_MIXED && (c->mg_max_outer < 1 || c->mg_max_outer > 32)) return no("mg_max_outer must be 1..32");
   if (!(c->mg_rel_tol >= 0.0) || !(c->mg_div_tol >= 0.0) || !isfinite(c->mg_rel_tol) || !isfinite(c->mg_div_tol))
@@ -403,8 +403,9 @@ dob_status dob_config_closed_box(dob_config* c, uint32_t nx, uint32_t ny, uint32
   c->domain_max[0] = (float)nx; c->domain_max[1] = (float)ny; c->domain_max[2] = (float)nz;
   c->bc_mode = DOB_BC_CLOSED_BOX;
   c->precision_mode = DOB_PREC_FP32;
-  // the hierarchy is deepened until the coarsest grid has at most 512 cells,
-  // which are solved exactly (dense inverse); 2+2 sweeps elsewhere
+  // the hierarchy is deepened until the coarsest grid has at most
+  // kDenseCoarseTarget cells, which are solved exactly (dense inverse); 2+2
+  // sweeps elsewhere
   int levels = 1, coarse = 6;
   for (int L = 2; L <= kMaxLevels; ++L) {
     const uint32_t m = 1u << L;
@@ -412,7 +413,7 @@ dob_status dob_config_closed_box(dob_config* c, uint32_t nx, uint32_t ny, uint32
     const uint64_t cells = (uint64_t)(nx >> (L - 1)) * (ny >> (L - 1)) * (nz >> (L - 1));
     levels = L;
     coarse = cells <= (uint64_t)kDenseCoarseMax ? -1 : 6;
-    if (cells <= 512) break;
+    if (cells <= (uint64_t)kDenseCoarseTarget) break;
   }
   c->mg_levels = levels; c->mg_pre = 2; c->mg_post = 2; c->mg_coarse_sweeps = coarse; c->mg_cycles = 4;
   c->mg_max_outer = 16; c->mg_rel_tol = 0.0; c->mg_div_tol = 1e-5;

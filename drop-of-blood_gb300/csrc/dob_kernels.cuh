@@ -220,8 +220,13 @@ void launch_divergence(const DevState& s, float* out, float scale, unsigned int*
 void launch_conc_predict(const DevState& s, cudaStream_t st);
 void launch_conc_resolve(const DevState& s, cudaStream_t st);
 
-// Largest coarsest grid solved exactly by the dense inverse.
-constexpr int kDenseCoarseMax = 1024;
+// Largest coarsest grid solved exactly by the dense inverse (64 MB of FP32),
+// and the size the closed-box configuration deepens its hierarchy to: one
+// dense solve of up to 12 x 16 x 12 cells (a 21 MB matrix read by all SMs)
+// costs less than another level of latency-bound sweeps plus a smaller
+// dense solve.
+constexpr int kDenseCoarseMax = 4096;
+constexpr int kDenseCoarseTarget = 2304;
 // Symmetric (pseudo-)inverse of the coarsest-grid operator
 // A e = (sum of neighbours - diag e) / h2 (pure Neumann: the minimum-norm
 // inverse on zero-mean data; Dirichlet top: the inverse), n x n FP32 in

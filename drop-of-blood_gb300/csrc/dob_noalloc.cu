@@ -16,7 +16,7 @@
 // Limits and sharing rules:
 //   * at most kNoAllocMaxCells = 2^21 cells (e.g. the reference's 96x128x96
 //     grid, or 128^3); larger grids are rejected with DOB_EINVAL;
-//   * the array (about 24 MiB) is part of the library's device image: every
+//   * the array (about 40 MiB) is part of the library's device image: every
 //     GPU that loads the library holds it until the process exits;
 //   * every call, from any thread and on any stream, works in the same array
 //     and leaves the last call's contents there.  Two calls whose work overlaps
@@ -54,8 +54,10 @@ constexpr size_t kSlotBytes = 1024;  // FP64 + u32 reduction slots at the front
 // coarser grids hold fewer than n/7 cells together, so 10 bytes per cell
 // bounds the whole layout for every accepted grid.
 // The dense inverse of an exactly solved coarsest grid (up to
-// kDenseCoarseMax cells) follows the multigrid arrays.
-constexpr size_t kDenseBytes = (size_t)kDenseCoarseMax * kDenseCoarseMax * sizeof(float);
+// kNoAllocDenseMax cells, the closed-box configuration's target) follows the
+// multigrid arrays.
+constexpr int kNoAllocDenseMax = kDenseCoarseTarget;
+constexpr size_t kDenseBytes = (size_t)kNoAllocDenseMax * kNoAllocDenseMax * sizeof(float);
 constexpr size_t kScratchBytes = kSlotBytes + 10 * kNoAllocMaxCells + kDenseBytes;
 
 static_assert(RED_COUNT * sizeof(double) <= 512, "reduction slots exceed their area");
@@ -134,8 +136,8 @@ extern "C" dob_status dob_pressure_solve_noalloc(const dob_config* cfg, const fl
     return bad("negative sweeps");
   const int cl = cfg->mg_levels - 1;
   if (cfg->mg_coarse_sweeps == -1 &&
-      (uint64_t)(nx >> cl) * (ny >> cl) * (nz >> cl) > (uint64_t)kDenseCoarseMax)
-    return bad("mg_coarse_sweeps = -1 (exact coarsest solve) needs a coarsest grid of at most 1024 cells");
+      (uint64_t)(nx >> cl) * (ny >> cl) * (nz >> cl) > (uint64_t)kNoAllocDenseMax)
+    return bad("mg_coarse_sweeps = -1 (exact coarsest solve) needs a coarsest grid of at most 2304 cells");
 
   int device = 0;
   cudaError_t e = cudaGetDevice(&device);

@@ -435,7 +435,7 @@ __global__ void __launch_bounds__(256) k_prolong_add2(Grid f, Grid c, int ref, T
 }
 
 // Exact coarsest-grid solve e = M b with the dense symmetric inverse M
-// (n <= 1024 cells).  CTA c forms rows 32c..32c+31 of e: b is gathered into
+// (n <= 4096 cells).  CTA c forms rows 32c..32c+31 of e: b is gathered into
 // shared memory in natural order, lane l of warp w sums M[i][32c + l] b[i]
 // over i = w, w + 32, ... (M is symmetric, so column 32c + l is row 32c + l;
 // each warp reads 128 consecutive bytes per i; 32 warps keep n/32 loads per
@@ -1194,62 +1194,82 @@ static void mixed_solve(const DevState& s, cudaStream_t st) {
   }
 }
 
-std::vector<float> coarse_inverse(const Grid& c, float h2, int ref) {
-  const int n = (int)c.n();
-  // A + J/n (Neumann: adds the null space back) in double, then Gauss-Jordan
-  std::vector<double> a((size_t)n * n, 0.0), inv((size_t)n * n, 0.0);
-  auto at = [&](int x, int y, int z) { return (z * c.ny + y) * c.nx + x; };
-  for (int z = 0; z < c.nz; ++z)
-    for (int y = 0; y < c.ny; ++y)
-      for (int x = 0; x < c.nx; ++x) {
-        const int i = at(x, y, z);
-        double diag = ref ? 1.0 : 0.0;
-        auto nb = [&](int j) { a[(size_t)i * n + j] += 1.0 / h2; diag += 1.0; };
-        if (x > 0) nb(at(x - 1, y, z));
-        if (x < c.nx - 1) nb(at(x + 1, y, z));
-        if (y > 0) nb(at(x, y - 1, z));
-        if (y < c.ny - 1) {
-          a[(size_t)i * n + at(x, y + 1, z)] += 1.0 / h2;
-          if (!ref) diag += 1.0;
-        }
-        if (z > 0) nb(at(x, y, z - 1));
-        if (z < c.nz - 1) nb(at(x, y, z + 1));
-        a[(size_t)i * n + i] -= diag / h2;
-      }
-  if (!ref)
-    for (auto& v : a) v += 1.0 / n;
-  for (int i = 0; i < n; ++i) inv[(size_t)i * n + i] = 1.0;
-  for (int col = 0; col < n; ++col) {
-    int piv = col;
-    for (int r = col + 1; r < n; ++r)
-      if (std::fabs(a[(size_t)r * n + col]) > std::fabs(a[(size_t)piv * n + col])) piv = r;
-    if (piv != col)
-      for (int k = 0; k < n; ++k) {
-        std::swap(a[(size_t)piv * n + k], a[(size_t)col * n + k]);
-        std::swap(inv[(size_t)piv * n + k], inv[(size_t)col * n + k]);
-      }
-    const double d = a[(size_t)col * n + col];
-    for (int k = 0; k < n; ++k) {
-      a[(size_t)col * n + k] /= d;
-      inv[(size_t)col * n + k] /= d;
+// Eigenpairs of the 1D coarse operator along one axis (graph Laplacian of a
+// row of n cells, V[k * n + i] = eigenvector k at cell i, orthonormal):
+// Neumann at both ends (closed box; x and z of the reference mode):
+// cos(pi k (i + 1/2) / n), 2 - 2 cos(pi k / n); Neumann below and the
+// Dirichlet ghost above the top cell (y of the reference mode):
+// cos(t (i + 1/2)) with t = pi (k + 1/2) / (n + 1/2), 2 - 2 cos t.
+static void axis_eigen(int n, bool dirichlet_top, std::vector<double>& V, std::vector<double>& mu) {
+  const double pi = 3.14159265358979323846;
+  V.assign((size_t)n * n, 0.0);
+  mu.assign(n, 0.0);
+  for (int k = 0; k < n; ++k) {
+    const double t = dirichlet_top ? pi * (k + 0.5) / (n + 0.5) : pi * k / n;
+    mu[k] = 2.0 - 2.0 * std::cos(t);
+    double nrm = 0.0;
+    for (int i = 0; i < n; ++i) {
+      const double v = std::cos(t * (i + 0.5));
+      V[(size_t)k * n + i] = v;
+      nrm += v * v;
     }
-    for (int r = 0; r < n; ++r) {
-      if (r == col) continue;
-      const double f = a[(size_t)r * n + col];
-      if (f == 0.0) continue;
-      for (int k = 0; k < n; ++k) {
-        a[(size_t)r * n + k] -= f * a[(size_t)col * n + k];
-        inv[(size_t)r * n + k] -= f * inv[(size_t)col * n + k];
-      }
-    }
+    nrm = 1.0 / std::sqrt(nrm);
+    for (int i = 0; i < n; ++i) V[(size_t)k * n + i] *= nrm;
   }
+  if (!dirichlet_top) mu[0] = 0.0;  // the constant mode, exactly
+}
+
+// Dense (pseudo-)inverse of the coarsest operator A = -L / h2, L the 7-point
+// graph Laplacian with the level's boundary terms, in natural cell order.
+// L is the Kronecker sum of the three axis operators, so with their
+// eigenpairs (v, mu) M = -h2 sum over modes with mu_x + mu_y + mu_z > 0 of
+// phi phi^T / (mu_x + mu_y + mu_z), phi = v_x (x) v_y (x) v_z; the zero mode
+// of the closed box (the constants) is left out, which gives the
+// minimum-norm inverse.  Each column is formed by three 1D transforms:
+// O(n (nx + ny + nz)) per column instead of Gauss-Jordan's O(n^2).
+std::vector<float> coarse_inverse(const Grid& c, float h2, int ref) {
+  const int nx = c.nx, ny = c.ny, nz = c.nz, n = (int)c.n();
+  std::vector<double> Vx, Vy, Vz, mx, my, mz;
+  axis_eigen(nx, false, Vx, mx);
+  axis_eigen(ny, ref != 0, Vy, my);
+  axis_eigen(nz, false, Vz, mz);
   std::vector<float> out((size_t)n * n);
-  for (int i = 0; i < n; ++i)
-    for (int j = 0; j < n; ++j) {
-      double v = 0.5 * (inv[(size_t)i * n + j] + inv[(size_t)j * n + i]);
-      if (!ref) v -= 1.0 / n;  // (A + J/n)^-1 - J/n: the minimum-norm inverse
-      out[(size_t)i * n + j] = (float)v;
-    }
+  std::vector<double> coef((size_t)n), t1((size_t)n), t2((size_t)n);
+  for (int bz = 0; bz < nz; ++bz)
+    for (int by = 0; by < ny; ++by)
+      for (int bx = 0; bx < nx; ++bx) {
+        const int b = (bz * ny + by) * nx + bx;
+        // coef[l][j][i] = v_i(bx) v_j(by) v_l(bz) / mu_ijl
+        for (int l = 0; l < nz; ++l)
+          for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+              const double m = mx[i] + my[j] + mz[l];
+              coef[((size_t)l * ny + j) * nx + i] =
+                  m > 0.0 ? Vx[(size_t)i * nx + bx] * Vy[(size_t)j * ny + by] * Vz[(size_t)l * nz + bz] / m : 0.0;
+            }
+        // back to cells: x, then y, then z
+        for (int l = 0; l < nz; ++l)
+          for (int j = 0; j < ny; ++j)
+            for (int ax = 0; ax < nx; ++ax) {
+              double acc = 0.0;
+              for (int i = 0; i < nx; ++i) acc += Vx[(size_t)i * nx + ax] * coef[((size_t)l * ny + j) * nx + i];
+              t1[((size_t)l * ny + j) * nx + ax] = acc;
+            }
+        for (int l = 0; l < nz; ++l)
+          for (int ay = 0; ay < ny; ++ay)
+            for (int ax = 0; ax < nx; ++ax) {
+              double acc = 0.0;
+              for (int j = 0; j < ny; ++j) acc += Vy[(size_t)j * ny + ay] * t1[((size_t)l * ny + j) * nx + ax];
+              t2[((size_t)l * ny + ay) * nx + ax] = acc;
+            }
+        for (int az = 0; az < nz; ++az)
+          for (int ay = 0; ay < ny; ++ay)
+            for (int ax = 0; ax < nx; ++ax) {
+              double acc = 0.0;
+              for (int l = 0; l < nz; ++l) acc += Vz[(size_t)l * nz + az] * t2[((size_t)l * ny + ay) * nx + ax];
+              out[(size_t)((az * ny + ay) * nx + ax) * n + b] = (float)(-(double)h2 * acc);
+            }
+      }
   return out;
 }
 

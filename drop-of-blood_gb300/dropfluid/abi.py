@@ -208,14 +208,16 @@ def config_reference() -> DobConfig:
     return c
 
 
-DENSE_COARSE_MAX = 1024
+DENSE_COARSE_MAX = 4096     # largest coarsest grid of the exact dense solve
+DENSE_COARSE_TARGET = 2304  # the closed-box hierarchy is deepened to this
 
 
 def closed_box_levels(nx: int, ny: int, nz: int):
     """(mg_levels, mg_coarse_sweeps) of the closed-box configuration: the
     hierarchy is deepened (every grid keeping even dims) until the coarsest
-    grid has at most 512 cells, which are solved exactly (-1: dense inverse;
-    6 RBGS sweeps when no depth gets below 1024 cells)."""
+    grid has at most DENSE_COARSE_TARGET cells, which are solved exactly (-1:
+    dense inverse; 6 RBGS sweeps when no depth gets below DENSE_COARSE_MAX
+    cells)."""
     levels, coarse = 1, 6
     for L in range(2, 11):
         m = 1 << L
@@ -224,7 +226,7 @@ def closed_box_levels(nx: int, ny: int, nz: int):
         cells = (nx >> (L - 1)) * (ny >> (L - 1)) * (nz >> (L - 1))
         levels = L
         coarse = -1 if cells <= DENSE_COARSE_MAX else 6
-        if cells <= 512:
+        if cells <= DENSE_COARSE_TARGET:
             break
     return levels, coarse
 

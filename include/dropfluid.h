@@ -93,7 +93,7 @@ typedef struct dob_config {
   int32_t mg_pre, mg_post;     /* RBGS sweeps before/after coarse correction          */
   int32_t mg_coarse_sweeps;    /* RBGS sweeps on the coarsest grid (reference: 6);
                                   -1: exact solve with a dense (pseudo-)inverse,
-                                  coarsest grid of at most 1024 cells              */
+                                  coarsest grid of at most 4096 cells              */
   int32_t mg_cycles;           /* V-cycles per step (reference: 1)                   */
   int32_t mg_max_outer;        /* mixed mode: max defect-correction iterations       */
   double mg_rel_tol;           /* mixed mode: stop at ||b-Ap||/||b|| <= this (0: off)  */
@@ -204,7 +204,7 @@ typedef struct dob_step_stats {
 dob_status dob_config_reference(dob_config* cfg);
 /* Fill *cfg with a closed-box synthetic scene of the given grid:
    FP32, 2+2 RBGS on every level, 4 cycles, the hierarchy deepened (even dims
-   on every grid) until the coarsest grid has at most 512 cells, solved
+   on every grid) until the coarsest grid has at most 2304 cells, solved
    exactly (mg_coarse_sweeps = -1); Casson tau_y=0.005, mu_p=1e-3, dx=1,
    dt=0.02; mixed mode: stop at max |div| dt/dx <= 1e-5, <= 16 iterations. */
 dob_status dob_config_closed_box(dob_config* cfg, uint32_t nx, uint32_t ny, uint32_t nz);
@@ -375,7 +375,7 @@ dob_status dob_eval_math(int fn, const float* x, const float* y, float* out, uin
    or cudaFree (both synchronise the device and can fail mid-frame).  No
    context is needed and nothing is allocated: the working arrays (split
    copies, coarse grids, reduction slots) live in one fixed device array of
-   about 24 MiB that is part of the library and stays resident on every GPU
+   about 40 MiB that is part of the library and stays resident on every GPU
    that loads it until the process exits.
 
    rhs and pressure are device pointers of the current device, nx*ny*nz
@@ -384,7 +384,9 @@ dob_status dob_eval_math(int fn, const float* x, const float* y, float* out, uin
    bc_mode, precision_mode (DOB_PREC_FP32 or DOB_PREC_REFERENCE_FP16; the
    pressure is FP32 in both), mg_levels, mg_pre, mg_post, mg_coarse_sweeps,
    mg_cycles and reference_schedule are read.  At most 2^21 cells
-   (2097152, e.g. 96x128x96 or 128^3): larger grids return DOB_EINVAL.
+   (2097152, e.g. 96x128x96 or 128^3): larger grids return DOB_EINVAL, and
+   so does an exact coarsest solve (mg_coarse_sweeps = -1) on a coarsest
+   grid of more than 2304 cells.
    The work is queued on `stream` (a cudaStream_t; NULL is the default
    stream) and the call returns without waiting for it.
 

@@ -152,6 +152,126 @@ template <class R> inline R lerp8(const Taps<R>& t, const R* a) {
 
 int g_threads = 0;
 
+// Dense (pseudo-)inverse of the coarsest operator A = -L / h2 (L: 7-point
+// graph Laplacian with the level's boundary terms; the reference mode counts
+// the +y face of every cell, the Dirichlet ghost above the top), natural cell
+// order, in double.  Gauss-Jordan on A + J/n (closed box: J/n restores the
+// null space, removed again afterwards), symmetrised: O(n^3), used to check
+// the separable form below on small grids.
+inline std::vector<double> cinv_direct(const Dims& c, double hh, int ref) {
+  const int n = (int)c.n();
+  std::vector<double> a((size_t)n * n, 0.0), inv((size_t)n * n, 0.0);
+  for (int z = 0; z < c.nz; ++z)
+    for (int y = 0; y < c.ny; ++y)
+      for (int x = 0; x < c.nx; ++x) {
+        const int i = (int)c.at(x, y, z);
+        double diag = ref ? 1.0 : 0.0;
+        auto nb = [&](int xx, int yy, int zz, bool count) {
+          a[(size_t)i * n + c.at(xx, yy, zz)] += 1.0 / hh;
+          if (count) diag += 1.0;
+        };
+        if (x > 0) nb(x - 1, y, z, true);
+        if (x < c.nx - 1) nb(x + 1, y, z, true);
+        if (y > 0) nb(x, y - 1, z, true);
+        if (y < c.ny - 1) nb(x, y + 1, z, !ref);
+        if (z > 0) nb(x, y, z - 1, true);
+        if (z < c.nz - 1) nb(x, y, z + 1, true);
+        a[(size_t)i * n + i] -= diag / hh;
+      }
+  if (!ref)
+    for (auto& v : a) v += 1.0 / n;
+  for (int i = 0; i < n; ++i) inv[(size_t)i * n + i] = 1.0;
+  for (int col = 0; col < n; ++col) {
+    int piv = col;
+    for (int r = col + 1; r < n; ++r)
+      if (std::fabs(a[(size_t)r * n + col]) > std::fabs(a[(size_t)piv * n + col])) piv = r;
+    if (piv != col)
+      for (int k = 0; k < n; ++k) {
+        std::swap(a[(size_t)piv * n + k], a[(size_t)col * n + k]);
+        std::swap(inv[(size_t)piv * n + k], inv[(size_t)col * n + k]);
+      }
+    const double d = a[(size_t)col * n + col];
+    for (int k = 0; k < n; ++k) { a[(size_t)col * n + k] /= d; inv[(size_t)col * n + k] /= d; }
+    for (int r = 0; r < n; ++r) {
+      if (r == col) continue;
+      const double f = a[(size_t)r * n + col];
+      if (f == 0.0) continue;
+      for (int k = 0; k < n; ++k) {
+        a[(size_t)r * n + k] -= f * a[(size_t)col * n + k];
+        inv[(size_t)r * n + k] -= f * inv[(size_t)col * n + k];
+      }
+    }
+  }
+  std::vector<double> out((size_t)n * n);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j)
+      out[(size_t)i * n + j] = 0.5 * (inv[(size_t)i * n + j] + inv[(size_t)j * n + i]) - (ref ? 0.0 : 1.0 / n);
+  return out;
+}
+// The same inverse from the eigenpairs of the three axis operators (L is
+// their Kronecker sum): closed box and reference x/z, Neumann at both ends:
+// vectors cos(pi k (i + 1/2) / m), values 2 - 2 cos(pi k / m); reference y,
+// Neumann below and the Dirichlet ghost above: cos(t (i + 1/2)),
+// t = pi (k + 1/2) / (m + 1/2), 2 - 2 cos t.  M = -h2 sum over the modes with
+// a nonzero value of phi phi^T / value (the closed box's constant mode is
+// left out: the minimum-norm inverse).  Column b: its mode coefficients
+// phi(b) / value, taken back to cells one axis at a time,
+// O(n (nx + ny + nz)) per column.
+inline std::vector<double> cinv_separable(const Dims& c, double hh, int ref) {
+  const double pi = 3.14159265358979323846;
+  auto eig = [&](int m, bool dir, std::vector<double>& V, std::vector<double>& mu) {
+    V.assign((size_t)m * m, 0.0);
+    mu.assign(m, 0.0);
+    for (int k = 0; k < m; ++k) {
+      const double t = dir ? pi * (k + 0.5) / (m + 0.5) : pi * k / m;
+      mu[k] = (!dir && k == 0) ? 0.0 : 2.0 - 2.0 * std::cos(t);
+      double s2 = 0.0;
+      for (int i = 0; i < m; ++i) s2 += std::cos(t * (i + 0.5)) * std::cos(t * (i + 0.5));
+      for (int i = 0; i < m; ++i) V[(size_t)k * m + i] = std::cos(t * (i + 0.5)) / std::sqrt(s2);
+    }
+  };
+  std::vector<double> X, Y, Z, mx, my, mz;
+  const int nx = c.nx, ny = c.ny, nz = c.nz;
+  eig(nx, false, X, mx);
+  eig(ny, ref != 0, Y, my);
+  eig(nz, false, Z, mz);
+  const size_t n = c.n();
+  std::vector<double> out(n * n, 0.0);
+#pragma omp parallel for schedule(dynamic)
+  for (long b = 0; b < (long)n; ++b) {
+    const int bx = (int)(b % nx), by = (int)((b / nx) % ny), bz = (int)(b / ((size_t)nx * ny));
+    std::vector<double> w(n), t(n);
+    for (int k = 0; k < nz; ++k)  // mode coefficients, indexed (k, j, i)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+          const double m = mx[i] + my[j] + mz[k];
+          w[c.at(i, j, k)] = m > 0.0 ? X[(size_t)i * nx + bx] * Y[(size_t)j * ny + by] * Z[(size_t)k * nz + bz] / m : 0.0;
+        }
+    for (int k = 0; k < nz; ++k)  // modes i -> cells x
+      for (int j = 0; j < ny; ++j)
+        for (int x = 0; x < nx; ++x) {
+          double acc = 0.0;
+          for (int i = 0; i < nx; ++i) acc += X[(size_t)i * nx + x] * w[c.at(i, j, k)];
+          t[c.at(x, j, k)] = acc;
+        }
+    for (int k = 0; k < nz; ++k)  // modes j -> cells y
+      for (int y = 0; y < ny; ++y)
+        for (int x = 0; x < nx; ++x) {
+          double acc = 0.0;
+          for (int j = 0; j < ny; ++j) acc += Y[(size_t)j * ny + y] * t[c.at(x, j, k)];
+          w[c.at(x, y, k)] = acc;
+        }
+    for (int z = 0; z < nz; ++z)  // modes k -> cells z
+      for (int y = 0; y < ny; ++y)
+        for (int x = 0; x < nx; ++x) {
+          double acc = 0.0;
+          for (int k = 0; k < nz; ++k) acc += Z[(size_t)k * nz + z] * w[c.at(x, y, k)];
+          out[c.at(x, y, z) * n + (size_t)b] = -hh * acc;
+        }
+  }
+  return out;
+}
+
 template <class R> class Sim {
  public:
   dob_config cfg;
@@ -797,56 +917,7 @@ template <class R> class Sim {
   // Gauss-Jordan in double on A + J/n (pure Neumann; J/n removed afterwards)
   // or on A (Dirichlet top).  The float oracle applies M rounded to float.
   std::vector<double> cinv;
-  void build_cinv(const Dims& c) {
-    const int n = (int)c.n();
-    const double hh = (double)h2(c);
-    std::vector<double> a((size_t)n * n, 0.0), inv((size_t)n * n, 0.0);
-    for (int z = 0; z < c.nz; ++z)
-      for (int y = 0; y < c.ny; ++y)
-        for (int x = 0; x < c.nx; ++x) {
-          const int i = (int)c.at(x, y, z);
-          double diag = ref ? 1.0 : 0.0;
-          auto nb = [&](int xx, int yy, int zz, bool count) {
-            a[(size_t)i * n + c.at(xx, yy, zz)] += 1.0 / hh;
-            if (count) diag += 1.0;
-          };
-          if (x > 0) nb(x - 1, y, z, true);
-          if (x < c.nx - 1) nb(x + 1, y, z, true);
-          if (y > 0) nb(x, y - 1, z, true);
-          if (y < c.ny - 1) nb(x, y + 1, z, !ref);
-          if (z > 0) nb(x, y, z - 1, true);
-          if (z < c.nz - 1) nb(x, y, z + 1, true);
-          a[(size_t)i * n + i] -= diag / hh;
-        }
-    if (!ref)
-      for (auto& v : a) v += 1.0 / n;
-    for (int i = 0; i < n; ++i) inv[(size_t)i * n + i] = 1.0;
-    for (int col = 0; col < n; ++col) {
-      int piv = col;
-      for (int r = col + 1; r < n; ++r)
-        if (std::fabs(a[(size_t)r * n + col]) > std::fabs(a[(size_t)piv * n + col])) piv = r;
-      if (piv != col)
-        for (int k = 0; k < n; ++k) {
-          std::swap(a[(size_t)piv * n + k], a[(size_t)col * n + k]);
-          std::swap(inv[(size_t)piv * n + k], inv[(size_t)col * n + k]);
-        }
-      const double d = a[(size_t)col * n + col];
-      for (int k = 0; k < n; ++k) { a[(size_t)col * n + k] /= d; inv[(size_t)col * n + k] /= d; }
-      for (int r = 0; r < n; ++r) {
-        if (r == col) continue;
-        const double f = a[(size_t)r * n + col];
-        if (f == 0.0) continue;
-        for (int k = 0; k < n; ++k) {
-          a[(size_t)r * n + k] -= f * a[(size_t)col * n + k];
-          inv[(size_t)r * n + k] -= f * inv[(size_t)col * n + k];
-        }
-      }
-    }
-    cinv.assign((size_t)n * n, 0.0);
-    for (int i = 0; i < n; ++i)
-      for (int j = 0; j < n; ++j)
-        cinv[(size_t)i * n + j] = 0.5 * (inv[(size_t)i * n + j] + inv[(size_t)j * n + i]) - (ref ? 0.0 : 1.0 / n);
-  }
+  void build_cinv(const Dims& c) { cinv = cinv_separable(c, (double)h2(c), ref); }
   R cinv_at(size_t k) const { return fp64 ? (R)cinv[k] : (R)(float)cinv[k]; }
   void coarse_exact(R* e, const R* b, const Dims& c, bool bf16) {
     const size_t n = c.n();
@@ -1829,7 +1900,7 @@ bool valid_config(const dob_config* c) {
   if (c->nx % m || c->ny % m || c->nz % m) return false;
   if (c->mg_coarse_sweeps < -1) return false;
   if (c->mg_coarse_sweeps == -1 &&
-      (uint64_t)(c->nx >> (c->mg_levels - 1)) * (c->ny >> (c->mg_levels - 1)) * (c->nz >> (c->mg_levels - 1)) > 1024)
+      (uint64_t)(c->nx >> (c->mg_levels - 1)) * (c->ny >> (c->mg_levels - 1)) * (c->nz >> (c->mg_levels - 1)) > 4096)
     return false;
   if (c->bc_mode != DOB_BC_REFERENCE && c->bc_mode != DOB_BC_CLOSED_BOX) return false;
   if (c->precision_mode < 0 || c->precision_mode > 2) return false;
@@ -1946,6 +2017,14 @@ int orc_sphere_soft_grad(orc_sim* s, const float c[3], float radius, float edge,
                          float sigma, uint64_t seed, double out[4]) {
   if (!out || !(radius > 0.0f) || !(edge > 0.0f)) return DOB_EINVAL;
   DISPATCH(s, sphere_soft_grad(c, radius, edge, dye, vel, sigma, seed, out));
+  return DOB_OK;
+}
+int orc_coarse_inverse(int nx, int ny, int nz, double h2, int ref, int method, double* out) {
+  if (nx < 1 || ny < 1 || nz < 1 || !out || (size_t)nx * ny * nz > 4096) return DOB_EINVAL;
+  Dims c;
+  c.nx = nx; c.ny = ny; c.nz = nz;
+  const std::vector<double> m = method ? cinv_separable(c, h2, ref) : cinv_direct(c, h2, ref);
+  memcpy(out, m.data(), m.size() * sizeof(double));
   return DOB_OK;
 }
 int orc_get_field64(orc_sim* s, int field, double* host, size_t n) {

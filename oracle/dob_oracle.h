@@ -54,6 +54,10 @@ int orc_sphere_soft_grad(orc_sim* s, const float center[3], float radius, float 
    predictor and adjoint fields (n = element count incl. channels; not
    ADJ_CENTER), for finite differences below float32 resolution */
 int orc_get_field64(orc_sim* s, int field, double* host, size_t n);
+/* Dense (pseudo-)inverse of a coarsest-grid operator (n = nx*ny*nz <= 4096
+   cells, out n*n doubles, natural cell order): method 0 Gauss-Jordan,
+   1 the separable form the simulation uses. */
+int orc_coarse_inverse(int nx, int ny, int nz, double h2, int ref, int method, double* out);
 int orc_set_field64(orc_sim* s, int field, const double* host, size_t n);
 /* Host evaluation of the library's elementary functions (same ids as
    dob_eval_math). */

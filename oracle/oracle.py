@@ -70,6 +70,8 @@ def lib():
                                          C.POINTER(C.c_double)]
         L.orc_get_field64.argtypes = [P, C.c_int, C.c_void_p, C.c_size_t]
         L.orc_set_field64.argtypes = [P, C.c_int, C.c_void_p, C.c_size_t]
+        L.orc_coarse_inverse.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int,
+                                         C.POINTER(C.c_double)]
         L.orc_eval_math.argtypes = [C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float),
                                     C.POINTER(C.c_float), C.c_uint32]
         _lib = L
@@ -232,3 +234,14 @@ class OracleSim:
         out = C.c_double(0.0)
         _check(lib().orc_sphere_impulse(self._h, c, C.c_float(radius), v, C.byref(out)), "sphere_impulse")
         return out.value
+
+
+def coarse_inverse(dims, h2, ref, method):
+    """Dense coarsest-grid inverse (n x n, natural cell order): method 0
+    Gauss-Jordan, 1 the separable form the simulation uses."""
+    nx, ny, nz = dims
+    n = nx * ny * nz
+    out = np.zeros((n, n), np.float64)
+    _check(lib().orc_coarse_inverse(nx, ny, nz, float(h2), int(ref), int(method),
+                                    out.ctypes.data_as(C.POINTER(C.c_double))), "coarse_inverse")
+    return out

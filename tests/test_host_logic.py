@@ -47,10 +47,10 @@ def test_box192_scene_matches_configuration():
         assert 0.8 * c.ny <= y <= c.ny - d.radius
         assert d.radius < x < c.nx - d.radius and d.radius < z < c.nz - d.radius
         assert d.w_cells_per_step == -1.5 and d.noise_cells_per_step == 0.05
-    # 2+2 RBGS V-cycles, 4 per step, on a hierarchy deepened to a 6x8x6
+    # 2+2 RBGS V-cycles, 4 per step, on a hierarchy deepened to a 12x16x12
     # coarsest grid that is solved exactly
     assert c.mg_pre == c.mg_post == 2 and c.mg_cycles == 4
-    assert c.mg_levels == 6 and c.mg_coarse_sweeps == -1
+    assert c.mg_levels == 5 and c.mg_coarse_sweeps == -1
     assert scenes.box192(abi.DOB_PREC_MIXED).config.precision_mode == abi.DOB_PREC_MIXED
 
 

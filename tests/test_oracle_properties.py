@@ -183,3 +183,16 @@ def test_single_parcel_splat_sum(oracle_mod):
                 expect += int(np.rint(np.float32(m * np.float32(65536.0)) * wx * wy * wz))
     assert int(sp.sum()) == expect
     assert int(sp[base[2], base[1], base[0]]) > 0
+
+
+@pytest.mark.parametrize("dims,h2,ref", [((2, 2, 2), 1.0, 0), ((6, 8, 6), 1024.0, 0), ((6, 8, 6), 64.0, 1),
+                                         ((4, 6, 4), 1.0, 1), ((3, 4, 3), 16.0, 0), ((8, 4, 6), 4.0, 1)])
+def test_separable_coarse_inverse_matches_gauss_jordan(oracle_mod, dims, h2, ref):
+    """The exact coarsest solve's dense (pseudo-)inverse from the axis
+    eigenpairs equals Gauss-Jordan's, closed box (minimum-norm inverse of the
+    singular Neumann operator) and reference mode (Dirichlet ghost above the
+    top)."""
+    a = oracle_mod.coarse_inverse(dims, h2, ref, 1)
+    b = oracle_mod.coarse_inverse(dims, h2, ref, 0)
+    assert np.abs(a - b).max() <= 1e-10 * np.abs(b).max()
+    assert np.allclose(a, a.T, rtol=0, atol=1e-12 * np.abs(a).max())
