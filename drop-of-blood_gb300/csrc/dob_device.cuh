@@ -96,9 +96,8 @@ struct Taps {
   uint32_t base, ox, oy, oz;
   float fx, fy, fz;
 };
-__device__ __forceinline__ Taps make_taps(const Grid& g, float u, float v, float w) {
+__device__ __forceinline__ Taps taps_at(const Grid& g, float cx, float cy, float cz) {  // texel coordinates
   Taps t;
-  const float cx = u * (float)g.nx - 0.5f, cy = v * (float)g.ny - 0.5f, cz = w * (float)g.nz - 0.5f;
   const float bx = floorf(cx), by = floorf(cy), bz = floorf(cz);
   t.fx = cx - bx; t.fy = cy - by; t.fz = cz - bz;
   const int ix = (int)bx, iy = (int)by, iz = (int)bz;
@@ -111,6 +110,19 @@ __device__ __forceinline__ Taps make_taps(const Grid& g, float u, float v, float
   t.oy = (uint32_t)(y1 - y0) * sy;
   t.oz = (uint32_t)(z1 - z0) * sz;
   return t;
+}
+__device__ __forceinline__ Taps make_taps(const Grid& g, float u, float v, float w) {
+  return taps_at(g, u * (float)g.nx - 0.5f, v * (float)g.ny - 0.5f, w * (float)g.nz - 0.5f);
+}
+// make_taps with the texel coordinate formed without FMA contraction (the
+// rounded product, then the subtraction), as the host oracle forms it.  At
+// a fixed cell-centre or face-centre point uvw * dims rounds back to the
+// exact texel coordinate on the grids used here, so the fractional parts
+// are exact (0 or 1/2) and the taps of weight 0 carry exactly 0, which the
+// adjoint's scatter skips.
+__device__ __forceinline__ Taps make_taps_exact(const Grid& g, float u, float v, float w) {
+  return taps_at(g, __fadd_rn(__fmul_rn(u, (float)g.nx), -0.5f), __fadd_rn(__fmul_rn(v, (float)g.ny), -0.5f),
+                 __fadd_rn(__fmul_rn(w, (float)g.nz), -0.5f));
 }
 template <class S> __device__ __forceinline__ float lerp8(const Taps& t, const S* a) {
   const S* p = a + t.base;
@@ -144,6 +156,12 @@ template <int NC, class V4> __device__ __forceinline__ float4 lerp8xn(const Taps
 template <class V4> __device__ __forceinline__ float4 lerp8x4(const Taps& t, const V4* a) { return lerp8xn<4>(t, a); }
 template <class V4> __device__ __forceinline__ dob_v3 sample_center(const Grid& g, const V4* cen, dob_v3 uvw) {
   const Taps t = make_taps(g, uvw.x, uvw.y, uvw.z);
+  const float4 r = lerp8xn<3>(t, cen);
+  return v3(r.x, r.y, r.z);
+}
+// the same at a fixed cell-centre or face-centre point (make_taps_exact)
+template <class V4> __device__ __forceinline__ dob_v3 sample_center_exact(const Grid& g, const V4* cen, dob_v3 uvw) {
+  const Taps t = make_taps_exact(g, uvw.x, uvw.y, uvw.z);
   const float4 r = lerp8xn<3>(t, cen);
   return v3(r.x, r.y, r.z);
 }

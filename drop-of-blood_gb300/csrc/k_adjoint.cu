@@ -165,7 +165,7 @@ __device__ __forceinline__ void adj_face(const Grid& g, const float* uk, const f
   if (gout == 0.0f) return;
   // forward recompute
   const dob_v3 F0 = clamp3(F, 0.002f, 0.998f);
-  const Taps t0 = make_taps(g, F0.x, F0.y, F0.z);
+  const Taps t0 = make_taps_exact(g, F0.x, F0.y, F0.z);  // as trace_back forms it
   const float4 v0r = lerp8xn<3>(t0, cen);
   const dob_v3 v0 = v3(v0r.x, v0r.y, v0r.z);
   const dob_v3 M = F - (0.5f * (v0 * dtv)) / dom;
@@ -725,7 +725,7 @@ __global__ void __launch_bounds__(256) k_adj_conc_predict(Grid gc, Grid g, const
   const float dtv = P.dt;
   const dob_v3 dom = dsize_of(P);
   const dob_v3 uvw = (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / dimsc;
-  const Taps t0 = make_taps(g, uvw.x, uvw.y, uvw.z);
+  const Taps t0 = make_taps_exact(g, uvw.x, uvw.y, uvw.z);  // the forward's cell-centre sample (dye on the velocity grid)
   const float4 v0r = lerp8xn<3>(t0, cen);
   const dob_v3 v0 = v3(v0r.x, v0r.y, v0r.z);
   const dob_v3 M = uvw - (0.5f * (v0 * dtv)) / dom;
@@ -762,7 +762,7 @@ __global__ void __launch_bounds__(256) k_adj_dye_resolve(Grid gc, Grid g, const 
   const float dtv = P.dt;
   const dob_v3 dom = dsize_of(P);
   const dob_v3 uvw = (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / dims;
-  const Taps t0 = make_taps(g, uvw.x, uvw.y, uvw.z);
+  const Taps t0 = make_taps_exact(g, uvw.x, uvw.y, uvw.z);  // the forward's cell-centre sample (dye on the velocity grid)
   const float4 v0r = lerp8xn<3>(t0, cen);
   const dob_v3 v0 = v3(v0r.x, v0r.y, v0r.z);
   const dob_v3 uvwMid = clamp3(uvw - (0.5f * (v0 * dtv)) / dom, 0.001f, 0.999f);
@@ -874,13 +874,13 @@ static void adj_cluster(const MgLevel& L, int ref, int sweeps, float* eb, float*
 // Transpose of the exact coarsest solve e = M b (M symmetric):
 // Bbar += M Ebar (Ebar is cleared by the caller afterwards).  CTA c forms
 // rows 32c..32c+31 like k_coarse_dense: lane l of warp w sums
-// M[i][32c + l] Ebar[i] over i = w, w + 8, ..., the warps' partial sums are
-// added in shared memory.
-__global__ void __launch_bounds__(256) k_adj_coarse_dense(Grid d, const float* __restrict__ M, int n,
+// M[i][32c + l] Ebar[i] over i = w, w + 32, ..., the 32 warps' partial sums
+// are added in shared memory.
+__global__ void __launch_bounds__(1024) k_adj_coarse_dense(Grid d, const float* __restrict__ M, int n,
                                                           const float* __restrict__ eb, float* __restrict__ bb) {
   pdl_wait();
   pdl_trigger();
-  extern __shared__ float sev[];  // Ebar in natural order (n), then 8 x 32 partial sums
+  extern __shared__ float sev[];  // Ebar in natural order (n), then 32 x 32 partial sums
   float* part = sev + n;
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     const int x = i % d.nx, y = (i / d.nx) % d.ny, z = i / (d.nx * d.ny);
@@ -891,15 +891,15 @@ __global__ void __launch_bounds__(256) k_adj_coarse_dense(Grid d, const float* _
   const int j = blockIdx.x * 32 + lane;
   float acc = 0.0f;
   if (j < n) {
-#pragma unroll 4
-    for (int i = w; i < n; i += 8) acc = fmaf(M[(size_t)i * n + j], sev[i], acc);
+#pragma unroll 8
+    for (int i = w; i < n; i += 32) acc = fmaf(M[(size_t)i * n + j], sev[i], acc);
   }
   part[w * 32 + lane] = acc;
   __syncthreads();
   if (w == 0 && j < n) {
     float sum = part[lane];
 #pragma unroll
-    for (int k = 1; k < 8; ++k) sum += part[k * 32 + lane];
+    for (int k = 1; k < 32; ++k) sum += part[k * 32 + lane];
     const int x = j % d.nx, y = (j / d.nx) % d.ny, z = j / (d.nx * d.ny);
     bb[rb_index(d, x, y, z)] += sum;
   }
@@ -908,8 +908,8 @@ __global__ void __launch_bounds__(256) k_adj_coarse_dense(Grid d, const float* _
 static void adj_coarse(const DevState& s, const MgLevel& L, int ref, int sweeps, float* eb, float* bb,
                        cudaStream_t st) {
   if (s.coarse_sweeps < 0) {
-    launch_pdl(k_adj_coarse_dense, dim3((s.cn + 31) / 32), dim3(256), (s.cn + 256) * sizeof(float), st, L.d, s.cinv,
-               s.cn, (const float*)eb, bb);
+    launch_pdl(k_adj_coarse_dense, dim3((s.cn + 31) / 32), dim3(1024), (s.cn + 1024) * sizeof(float), st, L.d,
+               s.cinv, s.cn, (const float*)eb, bb);
     cudaMemsetAsync(eb, 0, L.d.n() * sizeof(float), st);
     return;
   }

@@ -88,7 +88,7 @@ __device__ __forceinline__ float sample_mac(const Grid& g, const VS* a, dob_v3 u
 }
 template <class V4>
 __device__ __forceinline__ dob_v3 trace_back(const Grid& g, const V4* cen, dob_v3 uvwF, float dtv, dob_v3 dom) {
-  const dob_v3 v0 = sample_center(g, cen, clamp3(uvwF, 0.002f, 0.998f));
+  const dob_v3 v0 = sample_center_exact(g, cen, clamp3(uvwF, 0.002f, 0.998f));
   const dob_v3 uvwMid = clamp3(uvwF - (0.5f * (v0 * dtv)) / dom, 0.002f, 0.998f);
   const dob_v3 vMid = sample_center(g, cen, uvwMid);
   return clamp3(uvwF - (vMid * dtv) / dom, 0.002f, 0.998f);
@@ -484,7 +484,7 @@ __global__ void __launch_bounds__(256) k_conc_predict(Grid gc, Grid g, const Ste
     const Taps t = make_taps(gc, back.x, back.y, back.z);
     stf(pred + i, lerp8x4(t, conc4).y);
   } else {
-    const dob_v3 v0 = sample_center(g, cen, uvw);
+    const dob_v3 v0 = gc.nx == g.nx ? sample_center_exact(g, cen, uvw) : sample_center(g, cen, uvw);
     const dob_v3 mid = clamp3(uvw - (0.5f * (v0 * dtv)) / dom, 0.001f, 0.999f);
     const dob_v3 vMid = sample_center(g, cen, mid);
     const dob_v3 back = clamp3(uvw - (vMid * dtv) / dom, 0.001f, 0.999f);
@@ -647,7 +647,7 @@ __global__ void __launch_bounds__(256) k_dye_resolve_box(Grid gc, Grid g, const 
   const float dtv = P.dt;
   const dob_v3 dom = dsize_of(P);
   const dob_v3 uvw = (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / dims;
-  const dob_v3 v0 = sample_center(g, cen, uvw);
+  const dob_v3 v0 = gc.nx == g.nx ? sample_center_exact(g, cen, uvw) : sample_center(g, cen, uvw);
   const dob_v3 uvwMid = clamp3(uvw - (0.5f * (v0 * dtv)) / dom, 0.001f, 0.999f);
   const dob_v3 vMid = sample_center(g, cen, uvwMid);
   const dob_v3 uvwBack = clamp3(uvw - (vMid * dtv) / dom, 0.001f, 0.999f);
