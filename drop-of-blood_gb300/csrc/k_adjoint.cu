@@ -396,16 +396,24 @@ __global__ void __launch_bounds__(256) k_adj_rbgs(Grid d, int color, float h2, i
 // same thread layout as the forward k_rbgs_v4 (four cells of one colour
 // per thread, rows packed into warps, branch-free boundaries).  Within a
 // transposed run the adjoint is kept scaled by the diagonal, y = xb / diag,
-// so a cell only needs its own diagonal:
-//   SCALE    y = xb / diag                      (colour of the last half-sweep)
-//   FIRST    y = (xb + sum_n y(n)) / diag       (xb: the unscaled own value)
+// so most steps need only their own cell's diagonal:
+//   FIRST    y = (xb + sum_n xb(n) / diag(n)) / diag   (the other colour is
+//            still unscaled: each neighbour is divided by its own diagonal)
 //   FUSED    bb += -h2 y;  y = sum_n y(n) / diag
+//            (OWN_RAW: the own colour is still unscaled, y = xb / diag first;
+//             OUT_RAW: the last step of the run writes xb = sum_n y(n), the
+//             unscaled value, since only the own colour is read after it)
 //   FINAL    bb += -h2 y;  y = 0
-//   UNSCALE  xb = y * diag                      (the other colour, at the end)
-enum { ADJ4_SCALE = 0, ADJ4_FIRST = 1, ADJ4_FUSED = 2, ADJ4_FINAL = 3, ADJ4_UNSCALE = 4 };
+// so the run needs no separate scaling passes.
+enum { ADJ4_FIRST = 1, ADJ4_FUSED = 2, ADJ4_FINAL = 3, ADJ4_OWN_RAW = 8, ADJ4_OUT_RAW = 16 };
 __device__ __forceinline__ float4 ld4f(const float* p) { return *reinterpret_cast<const float4*>(p); }
 __device__ __forceinline__ float f4at(const float4& v, int j) {
   return j == 0 ? v.x : (j == 1 ? v.y : (j == 2 ? v.z : v.w));
+}
+// 1 / k for a diagonal k in 1..6 (the correctly rounded reciprocals)
+__device__ __forceinline__ float rcp_diag(float k) {
+  return k == 6.0f ? 1.0f / 6.0f
+                   : (k == 5.0f ? 0.2f : (k == 4.0f ? 0.25f : (k == 3.0f ? 1.0f / 3.0f : (k == 2.0f ? 0.5f : 1.0f))));
 }
 __global__ void __launch_bounds__(256) k_adj_rbgs_v4(Grid d, int color, float h2, int ref, int mode, float* __restrict__ a,
                                                      float* __restrict__ bb) {
@@ -417,6 +425,7 @@ __global__ void __launch_bounds__(256) k_adj_rbgs_v4(Grid d, int color, float h2
   const uint32_t hx = (uint32_t)d.nx >> 1;
   const uint32_t k0 = 4u * (uint32_t)q;
   if (k0 >= hx || y >= d.ny) return;
+  const int base = mode & 7;
   const int p = (y + z + color) & 1;
   const uint32_t half = (uint32_t)(d.n() >> 1);
   const uint32_t sz = (uint32_t)d.ny * hx;
@@ -438,29 +447,57 @@ __global__ void __launch_bounds__(256) k_adj_rbgs_v4(Grid d, int color, float h2
   }
   const float4 ov = ld4f(own);
   float res[4];
-  if (mode == ADJ4_SCALE || mode == ADJ4_UNSCALE) {
+  float yo[4];  // the own colour, scaled
 #pragma unroll
-    for (int j = 0; j < 4; ++j) res[j] = mode == ADJ4_SCALE ? f4at(ov, j) / diag[j] : f4at(ov, j) * diag[j];
-  } else if (mode == ADJ4_FINAL) {
+  for (int j = 0; j < 4; ++j) yo[j] = (mode & ADJ4_OWN_RAW) ? f4at(ov, j) / diag[j] : f4at(ov, j);
+  if (base == ADJ4_FINAL) {
     float* bp = bb + (color ? half : 0u) + r + k0;
     const float4 bv = ld4f(bp);
     *reinterpret_cast<float4*>(bp) =
-        make_float4(bv.x - h2 * ov.x, bv.y - h2 * ov.y, bv.z - h2 * ov.z, bv.w - h2 * ov.w);
+        make_float4(bv.x - h2 * yo[0], bv.y - h2 * yo[1], bv.z - h2 * yo[2], bv.w - h2 * yo[3]);
 #pragma unroll
     for (int j = 0; j < 4; ++j) res[j] = 0.0f;
   } else {
     const uint32_t rym = has_ym ? r - hx : r, ryp = has_yp ? r + hx : r;
     const uint32_t rzm = has_zm ? r - sz : r, rzp = has_zp ? r + sz : r;
-    const float4 cm = ld4f(oth + r + k0);
-    const float4 ym = ld4f(oth + rym + k0), yp = ld4f(oth + ryp + k0);
-    const float4 zm = ld4f(oth + rzm + k0), zp = ld4f(oth + rzp + k0);
+    float4 cm = ld4f(oth + r + k0);
+    float4 ym = ld4f(oth + rym + k0), yp = ld4f(oth + ryp + k0);
+    float4 zm = ld4f(oth + rzm + k0), zp = ld4f(oth + rzp + k0);
     const uint32_t kex = p == 0 ? (has_ex ? k0 - 1 : k0) : (has_ex ? k0 + 4 : k0 + 3);
-    const float ex = oth[r + kex];
-    if (mode == ADJ4_FUSED) {
+    float ex = oth[r + kex];
+    if (base == ADJ4_FIRST) {
+      // the other colour is unscaled: divide every neighbour by its diagonal
+      // (cells of the other colour at x = 2 (k0 + j) + 1 - p, y +- 1, z +- 1)
+      const float fy = (y > 0 ? 1.0f : 0.0f) + (ref ? 1.0f : wyp), fz = wzm + wzp;
+      const float fym = (y - 1 > 0 ? 1.0f : 0.0f) + (ref ? 1.0f : (y - 1 < d.ny - 1 ? 1.0f : 0.0f));
+      const float fyp = (y + 1 > 0 ? 1.0f : 0.0f) + (ref ? 1.0f : (y + 1 < d.ny - 1 ? 1.0f : 0.0f));
+      const float fzm = (z - 1 > 0 ? 1.0f : 0.0f) + (z - 1 < d.nz - 1 ? 1.0f : 0.0f);
+      const float fzp = (z + 1 > 0 ? 1.0f : 0.0f) + (z + 1 < d.nz - 1 ? 1.0f : 0.0f);
+      auto fx = [&](int xx) { return (xx > 0 ? 1.0f : 0.0f) + (xx < d.nx - 1 ? 1.0f : 0.0f); };
+      float c[4], vym[4], vyp[4], vzm[4], vzp[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int xo = 2 * ((int)k0 + j) + p;  // own cell j
+        const int xn = 2 * ((int)k0 + j) + 1 - p;  // the other colour's cell of word k0 + j
+        c[j] = f4at(cm, j) * rcp_diag(fx(xn) + fy + fz);
+        vym[j] = f4at(ym, j) * rcp_diag(fx(xo) + fym + fz);
+        vyp[j] = f4at(yp, j) * rcp_diag(fx(xo) + fyp + fz);
+        vzm[j] = f4at(zm, j) * rcp_diag(fx(xo) + fy + fzm);
+        vzp[j] = f4at(zp, j) * rcp_diag(fx(xo) + fy + fzp);
+      }
+      cm = make_float4(c[0], c[1], c[2], c[3]);
+      ym = make_float4(vym[0], vym[1], vym[2], vym[3]);
+      yp = make_float4(vyp[0], vyp[1], vyp[2], vyp[3]);
+      zm = make_float4(vzm[0], vzm[1], vzm[2], vzm[3]);
+      zp = make_float4(vzp[0], vzp[1], vzp[2], vzp[3]);
+      const int xe = 2 * (int)kex + 1 - p;  // the other colour's cell of word kex
+      ex = ex * rcp_diag(fx(xe) + fy + fz);
+    }
+    if (base == ADJ4_FUSED) {
       float* bp = bb + (color ? half : 0u) + r + k0;
       const float4 bv = ld4f(bp);
       *reinterpret_cast<float4*>(bp) =
-          make_float4(bv.x - h2 * ov.x, bv.y - h2 * ov.y, bv.z - h2 * ov.z, bv.w - h2 * ov.w);
+          make_float4(bv.x - h2 * yo[0], bv.y - h2 * yo[1], bv.z - h2 * yo[2], bv.w - h2 * yo[3]);
     }
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
@@ -468,14 +505,14 @@ __global__ void __launch_bounds__(256) k_adj_rbgs_v4(Grid d, int color, float h2
       const float xp = p == 0 ? f4at(cm, j) : (j == 3 ? ex : f4at(cm, j + 1));
       const float wxm = (p == 0 && j == 0) ? wex : 1.0f;
       const float wxp = (p == 1 && j == 3) ? wex : 1.0f;
-      float sumN = mode == ADJ4_FIRST ? f4at(ov, j) : 0.0f;
+      float sumN = base == ADJ4_FIRST ? f4at(ov, j) : 0.0f;
       sumN = fmaf(wxm, xm, sumN);
       sumN = fmaf(wxp, xp, sumN);
       sumN = fmaf(wym, f4at(ym, j), sumN);
       sumN = fmaf(wyp, f4at(yp, j), sumN);
       sumN = fmaf(wzm, f4at(zm, j), sumN);
       sumN = fmaf(wzp, f4at(zp, j), sumN);
-      res[j] = sumN / diag[j];
+      res[j] = (mode & ADJ4_OUT_RAW) ? sumN : sumN / diag[j];
     }
   }
   *reinterpret_cast<float4*>(own) = make_float4(res[0], res[1], res[2], res[3]);
@@ -854,11 +891,12 @@ static void adj_smooth(const Grid& d, float h2, int ref, int sweeps, float* xb, 
   auto color_of = [](int k) { return (k - 1) & 1; };  // half-sweep k = 1..K
   if (d.nx % 8 == 0) {
     const dim3 b = qblock(d), g = qgrid(d, b);
-    launch_pdl(k_adj_rbgs_v4, g, b, 0, st, d, color_of(K), h2, ref, (int)ADJ4_SCALE, xb, bb);
     launch_pdl(k_adj_rbgs_v4, g, b, 0, st, d, 1 - color_of(K), h2, ref, (int)ADJ4_FIRST, xb, bb);
-    for (int k = K; k >= 2; --k) launch_pdl(k_adj_rbgs_v4, g, b, 0, st, d, color_of(k), h2, ref, (int)ADJ4_FUSED, xb, bb);
+    for (int k = K; k >= 2; --k) {
+      const int m = ADJ4_FUSED | (k == K ? ADJ4_OWN_RAW : 0) | (k == 2 ? ADJ4_OUT_RAW : 0);
+      launch_pdl(k_adj_rbgs_v4, g, b, 0, st, d, color_of(k), h2, ref, m, xb, bb);
+    }
     launch_pdl(k_adj_rbgs_v4, g, b, 0, st, d, color_of(1), h2, ref, (int)ADJ4_FINAL, xb, bb);
-    launch_pdl(k_adj_rbgs_v4, g, b, 0, st, d, 1 - color_of(1), h2, ref, (int)ADJ4_UNSCALE, xb, bb);
     return;
   }
   launch_pdl(k_adj_rbgs, hgrid(d), cblock(), 0, st, d, 1 - color_of(K), h2, ref, (int)ADJ_SWEEP_FIRST, xb, bb);
