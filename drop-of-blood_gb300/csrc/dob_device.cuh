@@ -159,11 +159,29 @@ template <class V4> __device__ __forceinline__ dob_v3 sample_center(const Grid& 
   const float4 r = lerp8xn<3>(t, cen);
   return v3(r.x, r.y, r.z);
 }
-// the same at a fixed cell-centre or face-centre point (make_taps_exact)
+// First three channels of a 4-wide AoS field at taps of a fixed cell-centre
+// or face-centre point (make_taps_exact).  There at least two of the three
+// fractions are exactly 0, and the 8-tap interpolation reduces to a linear
+// interpolation along the remaining axis (mixing with weight exactly 0
+// returns the first operand), so only two taps are read: the same value (up
+// to the sign of a zero) for a quarter of the loads.  Other taps take the
+// 8-tap path.
+template <class V4> __device__ __forceinline__ dob_v3 lerp8x3_fixed(const Taps& t, const V4* cen) {
+  uint32_t o;
+  float f;
+  if (t.fy == 0.0f && t.fz == 0.0f) { o = t.ox; f = t.fx; }
+  else if (t.fx == 0.0f && t.fz == 0.0f) { o = t.oy; f = t.fy; }
+  else if (t.fx == 0.0f && t.fy == 0.0f) { o = t.oz; f = t.fz; }
+  else {
+    const float4 r = lerp8xn<3>(t, cen);
+    return v3(r.x, r.y, r.z);
+  }
+  const float4 c0 = ld4(cen + t.base), c1 = ld4(cen + t.base + o);
+  return v3(dob_mix(c0.x, c1.x, f), dob_mix(c0.y, c1.y, f), dob_mix(c0.z, c1.z, f));
+}
+// the centre velocity at a fixed cell-centre or face-centre point
 template <class V4> __device__ __forceinline__ dob_v3 sample_center_exact(const Grid& g, const V4* cen, dob_v3 uvw) {
-  const Taps t = make_taps_exact(g, uvw.x, uvw.y, uvw.z);
-  const float4 r = lerp8xn<3>(t, cen);
-  return v3(r.x, r.y, r.z);
+  return lerp8x3_fixed(make_taps_exact(g, uvw.x, uvw.y, uvw.z), cen);
 }
 
 // 512x512 wave texture, bilinear clamp-to-edge, worldXZToWaveUV (common.ts:65-67).

@@ -166,8 +166,7 @@ __device__ __forceinline__ void adj_face(const Grid& g, const float* uk, const f
   // forward recompute
   const dob_v3 F0 = clamp3(F, 0.002f, 0.998f);
   const Taps t0 = make_taps_exact(g, F0.x, F0.y, F0.z);  // as trace_back forms it
-  const float4 v0r = lerp8xn<3>(t0, cen);
-  const dob_v3 v0 = v3(v0r.x, v0r.y, v0r.z);
+  const dob_v3 v0 = lerp8x3_fixed(t0, cen);
   const dob_v3 M = F - (0.5f * (v0 * dtv)) / dom;
   const dob_v3 Mc = clamp3(M, 0.002f, 0.998f);
   const Taps tM = make_taps(g, Mc.x, Mc.y, Mc.z);
@@ -763,8 +762,7 @@ __global__ void __launch_bounds__(256) k_adj_conc_predict(Grid gc, Grid g, const
   const dob_v3 dom = dsize_of(P);
   const dob_v3 uvw = (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / dimsc;
   const Taps t0 = make_taps_exact(g, uvw.x, uvw.y, uvw.z);  // the forward's cell-centre sample (dye on the velocity grid)
-  const float4 v0r = lerp8xn<3>(t0, cen);
-  const dob_v3 v0 = v3(v0r.x, v0r.y, v0r.z);
+  const dob_v3 v0 = lerp8x3_fixed(t0, cen);
   const dob_v3 M = uvw - (0.5f * (v0 * dtv)) / dom;
   const dob_v3 Mc = clamp3(M, 0.001f, 0.999f);
   const Taps tM = make_taps(g, Mc.x, Mc.y, Mc.z);
@@ -800,8 +798,7 @@ __global__ void __launch_bounds__(256) k_adj_dye_resolve(Grid gc, Grid g, const 
   const dob_v3 dom = dsize_of(P);
   const dob_v3 uvw = (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / dims;
   const Taps t0 = make_taps_exact(g, uvw.x, uvw.y, uvw.z);  // the forward's cell-centre sample (dye on the velocity grid)
-  const float4 v0r = lerp8xn<3>(t0, cen);
-  const dob_v3 v0 = v3(v0r.x, v0r.y, v0r.z);
+  const dob_v3 v0 = lerp8x3_fixed(t0, cen);
   const dob_v3 uvwMid = clamp3(uvw - (0.5f * (v0 * dtv)) / dom, 0.001f, 0.999f);
   const float4 vmr = lerp8xn<3>(make_taps(g, uvwMid.x, uvwMid.y, uvwMid.z), cen);
   const dob_v3 vMid = v3(vmr.x, vmr.y, vmr.z);
