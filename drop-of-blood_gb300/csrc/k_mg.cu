@@ -355,11 +355,15 @@ __global__ void __launch_bounds__(256) k_residual_restrict2(Grid f, Grid c, floa
   stf(bc + (pc ? 0u : halfc) + rc, sum[1] * 0.125f);
 }
 
-// MG_PROLONG_ADD, two coarse cells per thread: the coarse taps X-1..X+2 x
-// Y-1..Y+1 x Z-1..Z+1 (clamped; 0 above a Dirichlet top) are loaded once and
-// the 16 fine cells are updated with two 8-byte read-modify-writes per fine
-// row.  Weights use the same per-cell formula as k_prolong_add.
-template <class T, class TC, bool BLACK>
+// MG_PROLONG_ADD, two coarse cells per thread and ZC coarse planes per
+// thread: the coarse taps X-1..X+2 x Y-1..Y+1 of planes Z-1..Z+1 (clamped;
+// 0 above a Dirichlet top) are kept in registers while the thread walks its
+// planes, so each coarse plane's taps are loaded once for three planes; the
+// 16 fine cells of a coarse plane pair are updated with 8-byte
+// read-modify-writes per fine row (BLACK: only the colour-1 pair of each row,
+// for a red half-sweep to follow).  Weights use the same per-cell formula as
+// k_prolong_add.
+template <class T, class TC, bool BLACK, int ZC>
 __global__ void __launch_bounds__(256) k_prolong_add2(Grid f, Grid c, int ref, T* __restrict__ a,
                                                       const TC* __restrict__ e, const unsigned int* __restrict__ skip) {
   pdl_wait();
@@ -367,15 +371,14 @@ __global__ void __launch_bounds__(256) k_prolong_add2(Grid f, Grid c, int ref, T
   if (skip_now(skip)) return;
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   const int Y = blockIdx.y * blockDim.y + threadIdx.y;
-  const int Z = blockIdx.z;
+  const int Z0 = blockIdx.z * ZC;
   if (2 * q >= c.nx || Y >= c.ny) return;
   const uint32_t hc = (uint32_t)c.nx >> 1, halfc = (uint32_t)(c.n() >> 1);
-  float t[3][3][4];  // coarse taps at (2q-1+i, Y-1+j, Z-1+k)
-#pragma unroll
-  for (int k = 0; k < 3; ++k)
+  auto load_plane = [&](int zz, float (&tp)[3][4]) {
+    zz = dob_clampi(zz, 0, c.nz - 1);
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
-      const int yy = Y - 1 + j, zz = dob_clampi(Z - 1 + k, 0, c.nz - 1);
+      const int yy = Y - 1 + j;
       const bool zero_row = ref && yy >= c.ny;
       const int yc = dob_clampi(yy, 0, c.ny - 1);
       const uint32_t rc = ((uint32_t)zz * c.ny + yc) * hc;
@@ -383,13 +386,17 @@ __global__ void __launch_bounds__(256) k_prolong_add2(Grid f, Grid c, int ref, T
       for (int i = 0; i < 4; ++i) {
         const int xx = dob_clampi(2 * q - 1 + i, 0, c.nx - 1);
         const float v = ldf(e + (((xx + yc + zz) & 1) ? halfc : 0u) + rc + (uint32_t)(xx >> 1));
-        t[k][j][i] = zero_row ? 0.0f : v;
+        tp[j][i] = zero_row ? 0.0f : v;
       }
     }
+  };
+  float t[3][3][4];  // coarse taps at (2q-1+i, Y-1+j, Z-1+k)
+  load_plane(Z0 - 1, t[0]);
+  load_plane(Z0, t[1]);
   const uint32_t hx = (uint32_t)f.nx >> 1, half = (uint32_t)(f.n() >> 1), sz = (uint32_t)f.ny * hx;
   const uint32_t w = 2u * (uint32_t)q;
   // fractional coordinates: x = 4q + i, y = 2Y + dy, z = 2Z + dz
-  float fxv[4], fyv[2], fzv[2];
+  float fxv[4], fyv[2];
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
     const float cx = (((float)(4 * q + i) + 0.5f) / (float)f.nx) * (float)c.nx - 0.5f;
@@ -398,40 +405,70 @@ __global__ void __launch_bounds__(256) k_prolong_add2(Grid f, Grid c, int ref, T
 #pragma unroll
   for (int d = 0; d < 2; ++d) {
     const float cy = (((float)(2 * Y + d) + 0.5f) / (float)f.ny) * (float)c.ny - 0.5f;
-    const float cz = (((float)(2 * Z + d) + 0.5f) / (float)f.nz) * (float)c.nz - 0.5f;
     fyv[d] = cy - floorf(cy);
-    fzv[d] = cz - floorf(cz);
   }
 #pragma unroll
-  for (int dz = 0; dz < 2; ++dz)
+  for (int zi = 0; zi < ZC; ++zi) {
+    const int Z = Z0 + zi;
+    load_plane(Z + 1, t[2]);
+    float fzv[2];
 #pragma unroll
-    for (int dy = 0; dy < 2; ++dy) {
-      const int y = 2 * Y + dy, z = 2 * Z + dz, par = (y + z) & 1;
-      const uint32_t r = (uint32_t)z * sz + (uint32_t)y * hx + w;
-      float corr[4];
+    for (int d = 0; d < 2; ++d) {
+      const float cz = (((float)(2 * Z + d) + 0.5f) / (float)f.nz) * (float)c.nz - 0.5f;
+      fzv[d] = cz - floorf(cz);
+    }
+    // the fine rows of this coarse plane, all loaded before any store (the
+    // compiler cannot move a load of `a` above a store through it)
+    float2 ve[2][2], vo[2][2];
+#pragma unroll
+    for (int dz = 0; dz < 2; ++dz)
+#pragma unroll
+      for (int dy = 0; dy < 2; ++dy) {
+        const int y = 2 * Y + dy, z = 2 * Z + dz, par = (y + z) & 1;
+        const uint32_t r = (uint32_t)z * sz + (uint32_t)y * hx + w;
+        if (BLACK) {
+          ve[dz][dy] = Pair<T>::ld(a + half + r);
+        } else {
+          ve[dz][dy] = Pair<T>::ld(a + (par ? half : 0u) + r);
+          vo[dz][dy] = Pair<T>::ld(a + (par ? 0u : half) + r);
+        }
+      }
+#pragma unroll
+    for (int dz = 0; dz < 2; ++dz)
+#pragma unroll
+      for (int dy = 0; dy < 2; ++dy) {
+        const int y = 2 * Y + dy, z = 2 * Z + dz, par = (y + z) & 1;
+        const uint32_t r = (uint32_t)z * sz + (uint32_t)y * hx + w;
+        float corr[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          // fine x = 4q+i: base coarse tap 2q-1 + (i+1)/2 -> index (i+1)>>1 into t
+          const int bi = (i + 1) >> 1;
+          const float fx = fxv[i], fy = fyv[dy], fz = fzv[dz];
+          const float x00 = dob_mix(t[dz][dy][bi], t[dz][dy][bi + 1], fx);
+          const float x10 = dob_mix(t[dz][dy + 1][bi], t[dz][dy + 1][bi + 1], fx);
+          const float x01 = dob_mix(t[dz + 1][dy][bi], t[dz + 1][dy][bi + 1], fx);
+          const float x11 = dob_mix(t[dz + 1][dy + 1][bi], t[dz + 1][dy + 1][bi + 1], fx);
+          corr[i] = dob_mix(dob_mix(x00, x10, fy), dob_mix(x01, x11, fy), fz);
+        }
+        if (BLACK) {  // only the colour-1 pair of the row: cells x = 4q + par, 4q + par + 2
+          const float2 vb = ve[dz][dy];
+          Pair<T>::st(a + half + r,
+                      par ? make_float2(vb.x + corr[0], vb.y + corr[2]) : make_float2(vb.x + corr[1], vb.y + corr[3]));
+        } else {
+          const float2 e2 = ve[dz][dy], o2 = vo[dz][dy];
+          Pair<T>::st(a + (par ? half : 0u) + r, make_float2(e2.x + corr[0], e2.y + corr[2]));
+          Pair<T>::st(a + (par ? 0u : half) + r, make_float2(o2.x + corr[1], o2.y + corr[3]));
+        }
+      }
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
-        // fine x = 4q+i: base coarse tap 2q-1 + (i+1)/2 -> index (i+1)>>1 into t
-        const int bi = (i + 1) >> 1;
-        const float fx = fxv[i], fy = fyv[dy], fz = fzv[dz];
-        const float x00 = dob_mix(t[dz][dy][bi], t[dz][dy][bi + 1], fx);
-        const float x10 = dob_mix(t[dz][dy + 1][bi], t[dz][dy + 1][bi + 1], fx);
-        const float x01 = dob_mix(t[dz + 1][dy][bi], t[dz + 1][dy][bi + 1], fx);
-        const float x11 = dob_mix(t[dz + 1][dy + 1][bi], t[dz + 1][dy + 1][bi + 1], fx);
-        corr[i] = dob_mix(dob_mix(x00, x10, fy), dob_mix(x01, x11, fy), fz);
+        t[0][j][i] = t[1][j][i];
+        t[1][j][i] = t[2][j][i];
       }
-      if (BLACK) {  // only the colour-1 pair of the row: cells x = 4q + par, 4q + par + 2
-        T* pb = a + half + r;
-        const float2 vb = Pair<T>::ld(pb);
-        Pair<T>::st(pb, par ? make_float2(vb.x + corr[0], vb.y + corr[2]) : make_float2(vb.x + corr[1], vb.y + corr[3]));
-      } else {
-        T* pe = a + (par ? half : 0u) + r;
-        T* po = a + (par ? 0u : half) + r;
-        const float2 ve = Pair<T>::ld(pe), vo = Pair<T>::ld(po);
-        Pair<T>::st(pe, make_float2(ve.x + corr[0], ve.y + corr[2]));
-        Pair<T>::st(po, make_float2(vo.x + corr[1], vo.y + corr[3]));
-      }
-    }
+  }
 }
 
 // Exact coarsest-grid solve e = M b with the dense symmetric inverse M
@@ -1002,8 +1039,17 @@ static void smooth(const DevState& s, int l, T* a, const T* b, int sweeps, bool 
     // black half-sweep then overwrites the black ones (same bits either way).
     const Grid dc = s.lv[l + 1].d;
     const dim3 bp = pair_block(dc);  // every transfer level has nx % 4 == 0
-    if (sweeps > 0) launch_pdl(k_prolong_add2<T, TC, true>, pair_grid(dc, bp), bp, 0, st, L.d, dc, s.ref, a, ec, skip);
-    else launch_pdl(k_prolong_add2<T, TC, false>, pair_grid(dc, bp), bp, 0, st, L.d, dc, s.ref, a, ec, skip);
+    dim3 gp = pair_grid(dc, bp);
+    // coarse planes per thread: 2 while that leaves two waves of 1024 threads per SM
+    const bool z2 = dc.nz % 2 == 0 && (size_t)(dc.nx / 2) * dc.ny * (dc.nz / 2) >= (size_t)s.num_sms * 2048;
+    if (z2) gp.z = dc.nz / 2;
+    if (sweeps > 0) {
+      if (z2) launch_pdl(k_prolong_add2<T, TC, true, 2>, gp, bp, 0, st, L.d, dc, s.ref, a, ec, skip);
+      else launch_pdl(k_prolong_add2<T, TC, true, 1>, gp, bp, 0, st, L.d, dc, s.ref, a, ec, skip);
+    } else {
+      if (z2) launch_pdl(k_prolong_add2<T, TC, false, 2>, gp, bp, 0, st, L.d, dc, s.ref, a, ec, skip);
+      else launch_pdl(k_prolong_add2<T, TC, false, 1>, gp, bp, 0, st, L.d, dc, s.ref, a, ec, skip);
+    }
   }
   for (int k = 0; k < sweeps; ++k)
     for (int c = 0; c < 2; ++c) half_sweep<T>(s, l, c, zero_first && k == 0 && c == 0, a, b, skip, st);
