@@ -355,13 +355,14 @@ __global__ void __launch_bounds__(256) k_residual_restrict2(Grid f, Grid c, floa
   stf(bc + (pc ? 0u : halfc) + rc, sum[1] * 0.125f);
 }
 
-// MG_PROLONG_ADD, two coarse cells per thread and ZC coarse planes per
-// thread: the coarse taps X-1..X+2 x Y-1..Y+1 of planes Z-1..Z+1 (clamped;
-// 0 above a Dirichlet top) are kept in registers while the thread walks its
-// planes, so each coarse plane's taps are loaded once for three planes; the
-// 16 fine cells of a coarse plane pair are updated with 8-byte
-// read-modify-writes per fine row (BLACK: only the colour-1 pair of each row,
-// for a red half-sweep to follow).  Weights use the same per-cell formula as
+// MG_PROLONG_ADD, two coarse cells per thread (and ZC coarse planes per
+// thread, keeping the coarse taps X-1..X+2 x Y-1..Y+1 of planes Z-1..Z+1 in
+// registers; clamped, 0 above a Dirichlet top; one plane per thread is used:
+// on box192's largest transfer two planes leave less than two waves): the 16
+// fine cells of a coarse plane pair are updated with 8-byte
+// read-modify-writes per fine row, all rows of a plane loaded before the
+// first store (BLACK: only the colour-1 pair of each row, for a red
+// half-sweep to follow).  Weights use the same per-cell formula as
 // k_prolong_add.
 template <class T, class TC, bool BLACK, int ZC>
 __global__ void __launch_bounds__(256) k_prolong_add2(Grid f, Grid c, int ref, T* __restrict__ a,
@@ -1039,17 +1040,9 @@ static void smooth(const DevState& s, int l, T* a, const T* b, int sweeps, bool 
     // black half-sweep then overwrites the black ones (same bits either way).
     const Grid dc = s.lv[l + 1].d;
     const dim3 bp = pair_block(dc);  // every transfer level has nx % 4 == 0
-    dim3 gp = pair_grid(dc, bp);
-    // coarse planes per thread: 2 while that leaves two waves of 1024 threads per SM
-    const bool z2 = dc.nz % 2 == 0 && (size_t)(dc.nx / 2) * dc.ny * (dc.nz / 2) >= (size_t)s.num_sms * 2048;
-    if (z2) gp.z = dc.nz / 2;
-    if (sweeps > 0) {
-      if (z2) launch_pdl(k_prolong_add2<T, TC, true, 2>, gp, bp, 0, st, L.d, dc, s.ref, a, ec, skip);
-      else launch_pdl(k_prolong_add2<T, TC, true, 1>, gp, bp, 0, st, L.d, dc, s.ref, a, ec, skip);
-    } else {
-      if (z2) launch_pdl(k_prolong_add2<T, TC, false, 2>, gp, bp, 0, st, L.d, dc, s.ref, a, ec, skip);
-      else launch_pdl(k_prolong_add2<T, TC, false, 1>, gp, bp, 0, st, L.d, dc, s.ref, a, ec, skip);
-    }
+    const dim3 gp = pair_grid(dc, bp);
+    if (sweeps > 0) launch_pdl(k_prolong_add2<T, TC, true, 1>, gp, bp, 0, st, L.d, dc, s.ref, a, ec, skip);
+    else launch_pdl(k_prolong_add2<T, TC, false, 1>, gp, bp, 0, st, L.d, dc, s.ref, a, ec, skip);
   }
   for (int k = 0; k < sweeps; ++k)
     for (int c = 0; c < 2; ++c) half_sweep<T>(s, l, c, zero_first && k == 0 && c == 0, a, b, skip, st);
