@@ -13,12 +13,19 @@ namespace dob {
 
 constexpr int kParamRing = 16;
 constexpr int kSnapshots = 8;
+// Steps after an injection that run cfg.mg_cycles_injected V-cycles: the
+// injection step itself and the next, whose right-hand side still carries
+// most of the new drop's divergence (the warm start from the injection
+// step's pressure leaves max |div| near 7e-5 after 4 V-cycles at 192 x 256
+// x 192; the third step is back below 2e-6).
+constexpr int kInjectedSteps = 2;
 
 struct Snapshot {
   std::vector<void*> bufs;
   std::vector<size_t> sizes;
   uint32_t high_water = 0;
   int step_index = 0;
+  int inject_pending = 0;
   bool valid = false;
 };
 
@@ -47,10 +54,15 @@ struct dob_ctx {
   struct StepGraph {
     cudaGraphExec_t ex = nullptr;
     bool stats = false;
+    bool injected = false;  // captured with mg_cycles_injected V-cycles
     void *conc = nullptr, *u = nullptr;
     void* after[8] = {};  // u, v, w, u2, v2, w2, conc, conc2
-  } graphs[8];
+  } graphs[12];
   int graph_next = 0;  // round-robin replacement when all slots are taken
+  // steps left that run cfg.mg_cycles_injected V-cycles (when set and the
+  // pressure is FP32): an injection sets kInjectedSteps
+  int inject_pending = 0;
+  int last_cycles = 0;  // V-cycles of the last step (FP32 pressure)
   int kernels_per_step = 0;
   dob::Snapshot snaps[dob::kSnapshots];
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -62,6 +74,7 @@ struct dob_ctx {
     unsigned int* redu = nullptr; // pinned, REDU_COUNT
     cudaEvent_t done = nullptr;
     bool pending = false;
+    int cycles = 0;               // V-cycles of the step (FP32 pressure)
   } async_slots[8];
 };
 

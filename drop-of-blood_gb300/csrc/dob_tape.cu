@@ -344,6 +344,8 @@ dob_status dob_tape_forward(dob_ctx* ctx, int nsteps, int checkpoint_every) {
   if ((st = ensure_tape(ctx, k, nseg)) != DOB_OK) return st;
   AdjCtx* A = ctx->adj;
   A->recorded = false;
+  // every recorded step runs mg_cycles V-cycles, as the recomputation does
+  ctx->inject_pending = 0;
   TCK(cudaStreamSynchronize(ctx->stream));
   launch_mac_to_center(ctx->s, ctx->stream);
   for (int n = 0; n < nsteps; ++n) {

@@ -109,6 +109,13 @@ typedef struct dob_config {
                                   1942-2059); 0: mg_pre/mg_post on every level       */
   float vel_damping;           /* closed box: per-step advection damping (1 = none)   */
   float dye_sharpness;         /* closed box: MacCormack correction strength          */
+  int32_t mg_cycles_injected;  /* closed box, FP32/FP16 storage: V-cycles of the first
+                                  two steps after dob_inject_sphere /
+                                  dob_inject_sphere_soft (a new divergent source the
+                                  warm start knows nothing about); 0: mg_cycles.
+                                  dob_config_closed_box sets 2 x mg_cycles.
+                                  dob_tape_forward runs every recorded step with
+                                  mg_cycles.                                           */
 } dob_config;
 
 /* Field identifiers for dob_set_field / dob_get_field.  Host data is always

@@ -471,6 +471,7 @@ template <class R> class Sim {
   }
 
   void reset() {
+    inject_pending = 0;
     std::fill(u.begin(), u.end(), R(0)); std::fill(v.begin(), v.end(), R(0)); std::fill(w.begin(), w.end(), R(0));
     for (int c = 0; c < 4; ++c) { std::fill(cen[c].begin(), cen[c].end(), R(0)); std::fill(curl[c].begin(), curl[c].end(), R(0)); }
     if (ref) init_vel();
@@ -1037,7 +1038,8 @@ template <class R> class Sim {
       }
       for (size_t i = 0; i < p.size(); ++i) p[i] = (R)p64[i];
     } else {
-      for (int c = 0; c < cfg.mg_cycles; ++c) { vcycle(p.data(), rhs.data(), false); ++cycles; }
+      const int ncyc = cycles_override > 0 ? cycles_override : cfg.mg_cycles;
+      for (int c = 0; c < ncyc; ++c) { vcycle(p.data(), rhs.data(), false); ++cycles; }
       if (!ref) {  // pin the pressure mean (FP64 sum)
         const R mean = (R)(sum64(p) / (double)p.size());
         for (auto& q : p) q = q - mean;
@@ -1574,6 +1576,7 @@ template <class R> class Sim {
 
   // ---- injection (closed box) ---------------------------------------------------------------------
   void inject_sphere(const float c[3], float radius, float dye, const float vel[3], float sigma, uint64_t seed) {
+    inject_pending = kInjectedSteps;
     const V3<R> cc = mk((R)c[0], (R)c[1], (R)c[2]);
     const R rr = (R)radius;
     const V3<R> dims = vdims();
@@ -1600,6 +1603,7 @@ template <class R> class Sim {
   // soft-edged additive drop (dob_inject_sphere_soft)
   void inject_sphere_soft(const float c[3], float radius, float edge, float dye, const float vel[3], float sigma,
                           uint64_t seed) {
+    inject_pending = kInjectedSteps;
     const V3<R> cc = mk((R)c[0], (R)c[1], (R)c[2]);
     const R rr = (R)radius, hh = (R)edge;
     const V3<R> dims = vdims();
@@ -1667,7 +1671,15 @@ template <class R> class Sim {
       default: break;
     }
   }
+  // steps left that run cfg.mg_cycles_injected V-cycles (FP32 pressure): an
+  // injection covers the injection step and the next, as the library does
+  static constexpr int kInjectedSteps = 2;
+  int inject_pending = 0;
+  int cycles_override = 0;
   void step(bool want_stats) {
+    const bool injected = inject_pending > 0 && cfg.mg_cycles_injected > 0 && !mixed() &&
+                          cfg.mg_cycles_injected != cfg.mg_cycles;
+    if (inject_pending > 0) --inject_pending;
     if (ref) {  // BloodDropEngine.ts:1832-1840: the high-water mark grows by the spawn count first
       const uint64_t hw = (uint64_t)highWater + spawn_count();
       highWater = (uint32_t)(hw < cap ? hw : cap);
@@ -1678,7 +1690,9 @@ template <class R> class Sim {
     casson_forces();
     mac_rhs();
     if (want_stats) last_stats[0] = sqrt(dot64(rhs, rhs));
+    cycles_override = injected ? cfg.mg_cycles_injected : 0;
     pressure_solve();
+    cycles_override = 0;
     if (want_stats) last_stats[1] = mixed() ? residual64(nullptr, nullptr) : residual_l2(p, rhs, nullptr);
     project();
     if (want_stats) last_stats[2] = max_div();

@@ -41,9 +41,10 @@ def test_struct_layout_matches_header():
 #include <stddef.h>
 #include "dropfluid.h"
 int main(void) {
-  printf("%zu %zu %zu %zu %zu %zu\n", sizeof(dob_config), sizeof(dob_step_stats),
+  printf("%zu %zu %zu %zu %zu %zu %zu\n", sizeof(dob_config), sizeof(dob_step_stats),
          offsetof(dob_config, mg_rel_tol), offsetof(dob_config, dye_sharpness),
-         offsetof(dob_step_stats, stage_ms), offsetof(dob_config, mg_div_tol));
+         offsetof(dob_step_stats, stage_ms), offsetof(dob_config, mg_div_tol),
+         offsetof(dob_config, mg_cycles_injected));
   return 0;
 }
 """
@@ -53,13 +54,14 @@ int main(void) {
         open(c, "w").write(prog)
         subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), c, "-o", exe], check=True)
         out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()
-    sz_cfg, sz_st, off_tol, off_sharp, off_ms, off_div = map(int, out)
+    sz_cfg, sz_st, off_tol, off_sharp, off_ms, off_div, off_inj = map(int, out)
     assert C.sizeof(abi.DobConfig) == sz_cfg
     assert C.sizeof(abi.DobStepStats) == sz_st
     assert abi.DobConfig.mg_rel_tol.offset == off_tol
     assert abi.DobConfig.dye_sharpness.offset == off_sharp
     assert abi.DobStepStats.stage_ms.offset == off_ms
     assert abi.DobConfig.mg_div_tol.offset == off_div
+    assert abi.DobConfig.mg_cycles_injected.offset == off_inj
 
 
 def test_config_builders_match_python(lib):

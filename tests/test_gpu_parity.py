@@ -392,6 +392,9 @@ def test_fused_projection_equals_separate_stages(gpu_lib):
     abi = _abi()
     from dropfluid import DropFluid, scenes
     sc = scenes.box48()
+    # the separate stages run the plain V-cycle schedule: compare against
+    # steps without the extra cycles after an injection
+    sc.config.mg_cycles_injected = 0
     a, b = DropFluid(sc.config), DropFluid(sc.config)
     sc.release(a, 0)
     sc.release(b, 0)
@@ -406,6 +409,34 @@ def test_fused_projection_equals_separate_stages(gpu_lib):
                   abi.FIELD_CONC):
             assert bits_equal(a.get_field(f), b.get_field(f)), f
     assert bits_equal(a.get_parcels(), b.get_parcels())
+
+
+def test_injection_step_runs_more_cycles(gpu_lib, oracle_mod):
+    """The two steps after a drop's injection run mg_cycles_injected V-cycles
+    (closed-box default 8): their projections hold max |div| dt/dx <= 1e-5,
+    their results match the oracle following the same rule, and the third
+    step is back to mg_cycles (a graph captured without the extra cycles)."""
+    abi = _abi()
+    from dropfluid import DropFluid, scenes
+    sc = scenes.box48()
+    assert sc.config.mg_cycles_injected == 2 * sc.config.mg_cycles
+    g = DropFluid(sc.config)
+    o = oracle_mod.OracleSim(sc.config)
+    for e in (g, o):
+        sc.release(e, 0)
+    for _ in range(2):
+        st = g.step(1, stats=True)
+        ost = o.step(1, stats=True)
+        assert st["vcycles"] == sc.config.mg_cycles_injected, st
+        assert ost["vcycles"] == sc.config.mg_cycles_injected, ost
+        assert st["max_div"] <= 1e-5, st
+        for f in (abi.FIELD_VEL_V, abi.FIELD_PRESSURE):
+            assert rel_l2(g.get_field(f), o.get_field(f)) < STEP_TOL, f
+    st = g.step(1, stats=True)
+    ost = o.step(1, stats=True)
+    assert st["vcycles"] == sc.config.mg_cycles, st
+    assert ost["vcycles"] == sc.config.mg_cycles, ost
+    g.close()
 
 
 def test_save_load_state_roundtrip(gpu_lib):
