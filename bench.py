@@ -4,8 +4,9 @@
 Workload (one "step" = one full fluid step of the scene, inputs resident in
 HBM): the 192x256x192 closed-box drop scene with three r=12 drops released
 at steps 0/40/80 and 393216 parcels, FP32 storage, 4 V-cycles of 2+2
-red-black sweeps per step on 6 grids with an exact solve of the 6x8x6
-coarsest grid (dropfluid.scenes.box192).  The mixed-precision variant of the
+red-black sweeps per step (8 on the two steps after each release) on 5
+grids with an exact solve of the 12x16x12 coarsest grid
+(dropfluid.scenes.box192).  The mixed-precision variant of the
 same scene and the discrete adjoint are measured beside it.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
@@ -461,7 +462,7 @@ def run_reference(args, rank, world):
         "steps": steps, "warmup": 1, "ms_per_step": 1000.0 / value, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "box192: 192x256x192 closed-box MAC step, 3 drops r=12, 393216 parcels, FP32, "
-                               "4 V-cycles of 2+2 RBGS on 6 grids, exact 6x8x6 coarsest solve "
+                               "4 V-cycles of 2+2 RBGS on 5 grids, exact 12x16x12 coarsest solve "
                                "(dropfluid.scenes.box192)",
                    "grid": [192, 256, 192], "parallelism": "replicas"},
         "cpu_baseline": {"value": value, "unit": "steps/s", "cores": threads, "kind": "port",
@@ -635,7 +636,8 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "box192: 192x256x192 closed-box MAC step, 3 drops r=12 released at "
                                    "steps 0/40/80, 393216 parcels, FP32 storage, 4 V-cycles of 2+2 RBGS on "
-                                   "6 grids with an exact 6x8x6 coarsest solve, Casson tau_y=0.005 "
+                                   "5 grids with an exact 12x16x12 coarsest solve (8 V-cycles on the "
+                                   "two steps after each release), Casson tau_y=0.005 "
                                    "mu_p=1e-3, dx=1 dt=0.02",
                        "grid": [192, 256, 192], "parallelism": "replicas" if world > 1 else "single",
                        "l2": "inputs larger than L2 (>=12 fields x 37.7 MB per step), no flush",
