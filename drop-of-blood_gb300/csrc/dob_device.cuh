@@ -120,9 +120,9 @@ __device__ __forceinline__ Taps make_taps(const Grid& g, float u, float v, float
 // exact texel coordinate on the grids used here, so the fractional parts
 // are exact (0 or 1/2) and the taps of weight 0 carry exactly 0, which the
 // adjoint's scatter skips.
+__device__ __forceinline__ float texel_exact(float u, int n) { return __fadd_rn(__fmul_rn(u, (float)n), -0.5f); }
 __device__ __forceinline__ Taps make_taps_exact(const Grid& g, float u, float v, float w) {
-  return taps_at(g, __fadd_rn(__fmul_rn(u, (float)g.nx), -0.5f), __fadd_rn(__fmul_rn(v, (float)g.ny), -0.5f),
-                 __fadd_rn(__fmul_rn(w, (float)g.nz), -0.5f));
+  return taps_at(g, texel_exact(u, g.nx), texel_exact(v, g.ny), texel_exact(w, g.nz));
 }
 template <class S> __device__ __forceinline__ float lerp8(const Taps& t, const S* a) {
   const S* p = a + t.base;
@@ -183,6 +183,31 @@ template <class V4> __device__ __forceinline__ dob_v3 lerp8x3_fixed(const Taps& 
 template <class V4> __device__ __forceinline__ dob_v3 sample_center_exact(const Grid& g, const V4* cen, dob_v3 uvw) {
   return lerp8x3_fixed(make_taps_exact(g, uvw.x, uvw.y, uvw.z), cen);
 }
+// sample_center_exact at the centre of cell i = (x, y, z) of g, uvw =
+// (index + 1/2) / dims.  When the texel coordinates come out as the cell's
+// indices, all three fractions are 0 and the interpolation is the cell's
+// own value (up to the sign of a zero, which the traces that use it cannot
+// see: they add the displacement to a coordinate of at least 1e-3), read
+// directly instead of forming the taps.
+template <class V4>
+__device__ __forceinline__ dob_v3 center_at_cell(const Grid& g, const V4* cen, dob_v3 uvw, int x, int y, int z,
+                                                 size_t i) {
+  if (texel_exact(uvw.x, g.nx) == (float)x && texel_exact(uvw.y, g.ny) == (float)y &&
+      texel_exact(uvw.z, g.nz) == (float)z) {
+    const float4 c = ld4(cen + i);
+    return v3(c.x, c.y, c.z);
+  }
+  return sample_center_exact(g, cen, uvw);
+}
+// sample_center_exact at the centre of the upper face of cell i normal to
+// one axis (o: the index step to the cell across the face) when the face's
+// texel coordinates are exact (index + 1/2 along the axis, the indices
+// across it): the two taps of weight 1/2 that lerp8x3_fixed reads.
+template <class V4> __device__ __forceinline__ dob_v3 face_mean(const V4* cen, size_t i, size_t o) {
+  const float4 a = ld4(cen + i), b = ld4(cen + i + o);
+  const float h = 0.5f;
+  return v3(dob_mix(a.x, b.x, h), dob_mix(a.y, b.y, h), dob_mix(a.z, b.z, h));
+}
 
 // 512x512 wave texture, bilinear clamp-to-edge, worldXZToWaveUV (common.ts:65-67).
 __device__ __forceinline__ float4 sample_wave(const float4* wave, float x, float z, float lo, float hi) {
@@ -208,5 +233,31 @@ __device__ __forceinline__ dob_v3 dsize_of(const StepParams& P) { return v3(P.ds
 __device__ __forceinline__ dob_v3 to_world(const StepParams& P, dob_v3 uvw) { return dmin_of(P) + uvw * dsize_of(P); }
 __device__ __forceinline__ dob_v3 to_uvw(const StepParams& P, dob_v3 p) { return (p - dmin_of(P)) / dsize_of(P); }
 __device__ __forceinline__ float drop(const StepParams& P, int d, int k) { return P.U[64 + 8 * d + k]; }
+
+// ---- division by a per-launch divisor ----------------------------------------------
+// a / d from the correctly rounded reciprocal rd = 1/d, with one remainder
+// correction (Markstein, "Computation of elementary functions on the IBM
+// RISC System/6000 processor", IBM J. Res. Dev. 34(1), 1990): q = RN(a rd)
+// is within one ulp of a/d, the remainder a - d q is exact in one FMA, and
+// RN(q + (a - d q) rd) is the correctly rounded quotient a/d, barring
+// overflow and subnormal intermediates.  Three instructions against the
+// IEEE division's subroutine.  Used for texture coordinates (cell index /
+// dims, displacement / domain size), which are then added to or subtracted
+// from a coordinate of at least 1e-3: there a subnormal quotient (which may
+// differ in its last place) and -0/d (which gives +0) leave the result
+// unchanged, so the coordinates equal the IEEE division's; and for the
+// adjoints of those displacements, where the two cases change nothing
+// above 2^-126.
+struct Recip3 {
+  dob_v3 d, r;
+};
+__device__ __forceinline__ Recip3 recip3(dob_v3 d) { return {d, v3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z)}; }
+__device__ __forceinline__ float div_by(float a, float d, float rd) {
+  const float q = __fmul_rn(a, rd);
+  return __fmaf_rn(__fmaf_rn(-q, d, a), rd, q);
+}
+__device__ __forceinline__ dob_v3 operator/(dob_v3 a, const Recip3& b) {
+  return v3(div_by(a.x, b.d.x, b.r.x), div_by(a.y, b.d.y, b.r.y), div_by(a.z, b.d.z, b.r.z));
+}
 
 }  // namespace dob

@@ -161,7 +161,8 @@ __device__ __forceinline__ dob_v3 pass3(dob_v3 v, float lo, float hi) {
 // damp * lerp8(u_k, clamp(B - half-cell offset)).  Adjoint of the output
 // au2 -> au (face values) and acen (centre velocity).
 __device__ __forceinline__ void adj_face(const Grid& g, const float* uk, const float4* cen, float4* acen, float* auk,
-                                         dob_v3 F, int comp, float gout, float dtv, dob_v3 dom, dob_v3 dims) {
+                                         dob_v3 F, int comp, float gout, float dtv, const Recip3& dom,
+                                         dob_v3 dims) {
   if (gout == 0.0f) return;
   // forward recompute
   const dob_v3 F0 = clamp3(F, 0.002f, 0.998f);
@@ -200,15 +201,15 @@ __global__ void __launch_bounds__(256) k_adj_advect_mac(Grid g, const StepParams
   ADJ_CELL
   const StepParams& P = *Pp;
   const dob_v3 dims = v3((float)g.nx, (float)g.ny, (float)g.nz);
+  const Recip3 dimr = recip3(dims), dom = recip3(dsize_of(P));
   const float dtv = P.dt;
-  const dob_v3 dom = dsize_of(P);
   const float damp = P.damp;
   const float gx = x >= g.nx - 1 ? 0.0f : au2[i] * damp;
   const float gy = y >= g.ny - 1 ? 0.0f : av2[i] * damp;
   const float gz = z >= g.nz - 1 ? 0.0f : aw2[i] * damp;
-  adj_face(g, u, cen, acen, au, v3((float)x + 1.0f, (float)y + 0.5f, (float)z + 0.5f) / dims, 0, gx, dtv, dom, dims);
-  adj_face(g, v, cen, acen, av, v3((float)x + 0.5f, (float)y + 1.0f, (float)z + 0.5f) / dims, 1, gy, dtv, dom, dims);
-  adj_face(g, w, cen, acen, aw, v3((float)x + 0.5f, (float)y + 0.5f, (float)z + 1.0f) / dims, 2, gz, dtv, dom, dims);
+  adj_face(g, u, cen, acen, au, v3((float)x + 1.0f, (float)y + 0.5f, (float)z + 0.5f) / dimr, 0, gx, dtv, dom, dims);
+  adj_face(g, v, cen, acen, av, v3((float)x + 0.5f, (float)y + 1.0f, (float)z + 0.5f) / dimr, 1, gy, dtv, dom, dims);
+  adj_face(g, w, cen, acen, aw, v3((float)x + 0.5f, (float)y + 0.5f, (float)z + 1.0f) / dimr, 2, gz, dtv, dom, dims);
 }
 
 // ---- FLUID_MAC_TO_CENTER (closed box): au += C^T acen ---------------------------------------
@@ -759,8 +760,8 @@ __global__ void __launch_bounds__(256) k_adj_conc_predict(Grid gc, Grid g, const
   const dob_v3 dimsc = v3((float)gc.nx, (float)gc.ny, (float)gc.nz);
   const dob_v3 dimsg = v3((float)g.nx, (float)g.ny, (float)g.nz);
   const float dtv = P.dt;
-  const dob_v3 dom = dsize_of(P);
-  const dob_v3 uvw = (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / dimsc;
+  const Recip3 dom = recip3(dsize_of(P));
+  const dob_v3 uvw = (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / recip3(dimsc);
   const Taps t0 = make_taps_exact(g, uvw.x, uvw.y, uvw.z);  // the forward's cell-centre sample (dye on the velocity grid)
   const dob_v3 v0 = lerp8x3_fixed(t0, cen);
   const dob_v3 M = uvw - (0.5f * (v0 * dtv)) / dom;
@@ -795,8 +796,8 @@ __global__ void __launch_bounds__(256) k_adj_dye_resolve(Grid gc, Grid g, const 
   const StepParams& P = *Pp;
   const dob_v3 dims = v3((float)gc.nx, (float)gc.ny, (float)gc.nz);
   const float dtv = P.dt;
-  const dob_v3 dom = dsize_of(P);
-  const dob_v3 uvw = (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / dims;
+  const Recip3 dom = recip3(dsize_of(P));
+  const dob_v3 uvw = (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / recip3(dims);
   const Taps t0 = make_taps_exact(g, uvw.x, uvw.y, uvw.z);  // the forward's cell-centre sample (dye on the velocity grid)
   const dob_v3 v0 = lerp8x3_fixed(t0, cen);
   const dob_v3 uvwMid = clamp3(uvw - (0.5f * (v0 * dtv)) / dom, 0.001f, 0.999f);

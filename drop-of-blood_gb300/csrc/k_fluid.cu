@@ -86,9 +86,10 @@ __device__ __forceinline__ float sample_mac(const Grid& g, const VS* a, dob_v3 u
   const Taps t = make_taps(g, uvw.x, uvw.y, uvw.z);
   return lerp8(t, a);
 }
+// midpoint trace from the face centre uvwF, whose centre velocity is v0
 template <class V4>
-__device__ __forceinline__ dob_v3 trace_back(const Grid& g, const V4* cen, dob_v3 uvwF, float dtv, dob_v3 dom) {
-  const dob_v3 v0 = sample_center_exact(g, cen, clamp3(uvwF, 0.002f, 0.998f));
+__device__ __forceinline__ dob_v3 trace_back(const Grid& g, const V4* cen, dob_v3 uvwF, dob_v3 v0, float dtv,
+                                             const Recip3& dom) {
   const dob_v3 uvwMid = clamp3(uvwF - (0.5f * (v0 * dtv)) / dom, 0.002f, 0.998f);
   const dob_v3 vMid = sample_center(g, cen, uvwMid);
   return clamp3(uvwF - (vMid * dtv) / dom, 0.002f, 0.998f);
@@ -108,15 +109,26 @@ __global__ void __launch_bounds__(256) k_advect_mac(Grid g, const StepParams* __
   CELL_INDEX
   const StepParams& P = *Pp;
   const dob_v3 dims = v3((float)g.nx, (float)g.ny, (float)g.nz);
+  const Recip3 dimr = recip3(dims), dom = recip3(dsize_of(P));
   const float dtv = P.dt;
-  const dob_v3 dom = dsize_of(P);
   const float damp = P.damp;
-  const dob_v3 uvwX = v3((float)x + 1.0f, (float)y + 0.5f, (float)z + 0.5f) / dims;
-  const dob_v3 uvwY = v3((float)x + 0.5f, (float)y + 1.0f, (float)z + 0.5f) / dims;
-  const dob_v3 uvwZ = v3((float)x + 0.5f, (float)y + 0.5f, (float)z + 1.0f) / dims;
-  float vx = sample_mac(g, u, trace_back(g, cen, uvwX, dtv, dom), 0) * damp;
-  float vy = sample_mac(g, v, trace_back(g, cen, uvwY, dtv, dom), 1) * damp;
-  float vz = sample_mac(g, w, trace_back(g, cen, uvwZ, dtv, dom), 2) * damp;
+  // a: the cell centre, b: the upper faces; face X is (b.x, a.y, a.z) etc.
+  const dob_v3 a = v3((float)x + 0.5f, (float)y + 0.5f, (float)z + 0.5f) / dimr;
+  const dob_v3 b = v3((float)x + 1.0f, (float)y + 1.0f, (float)z + 1.0f) / dimr;
+  const dob_v3 uvwX = v3(b.x, a.y, a.z), uvwY = v3(a.x, b.y, a.z), uvwZ = v3(a.x, a.y, b.z);
+  // start samples at the (clamped) face centres: where the texel coordinates
+  // are exact the interpolation is the mean of the two cells the face joins
+  const dob_v3 ca = clamp3(a, 0.002f, 0.998f), cb = clamp3(b, 0.002f, 0.998f);
+  const bool ax = texel_exact(ca.x, g.nx) == (float)x, bx = texel_exact(cb.x, g.nx) == (float)x + 0.5f;
+  const bool ay = texel_exact(ca.y, g.ny) == (float)y, by = texel_exact(cb.y, g.ny) == (float)y + 0.5f;
+  const bool az = texel_exact(ca.z, g.nz) == (float)z, bz = texel_exact(cb.z, g.nz) == (float)z + 0.5f;
+  const size_t sy = (size_t)g.nx, sz = (size_t)g.nx * g.ny;
+  const dob_v3 v0X = bx && ay && az ? face_mean(cen, i, 1) : sample_center_exact(g, cen, v3(cb.x, ca.y, ca.z));
+  const dob_v3 v0Y = ax && by && az ? face_mean(cen, i, sy) : sample_center_exact(g, cen, v3(ca.x, cb.y, ca.z));
+  const dob_v3 v0Z = ax && ay && bz ? face_mean(cen, i, sz) : sample_center_exact(g, cen, v3(ca.x, ca.y, cb.z));
+  float vx = sample_mac(g, u, trace_back(g, cen, uvwX, v0X, dtv, dom), 0) * damp;
+  float vy = sample_mac(g, v, trace_back(g, cen, uvwY, v0Y, dtv, dom), 1) * damp;
+  float vz = sample_mac(g, w, trace_back(g, cen, uvwZ, v0Z, dtv, dom), 2) * damp;
   if (ref) {
     const float surfY = P.U[40];
     const dob_v3 pCell = to_world(P, (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / dims);
@@ -464,9 +476,9 @@ __global__ void __launch_bounds__(256) k_conc_predict(Grid gc, Grid g, const Ste
   if (x >= gc.nx || y >= gc.ny) return;
   const size_t i = gc.at(x, y, z);
   const StepParams& P = *Pp;
-  const dob_v3 dims = v3((float)gc.nx, (float)gc.ny, (float)gc.nz);
+  const Recip3 dims = recip3(v3((float)gc.nx, (float)gc.ny, (float)gc.nz));
   const float dtv = P.dt;
-  const dob_v3 dom = dsize_of(P);
+  const Recip3 dom = recip3(dsize_of(P));
   const dob_v3 uvw = (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / dims;
   if (ref) {
     if (x == 0 || x >= gc.nx - 1 || z == 0 || z >= gc.nz - 1 || y >= gc.ny - 1) { stf(pred + i, 0.0f); return; }
@@ -484,7 +496,7 @@ __global__ void __launch_bounds__(256) k_conc_predict(Grid gc, Grid g, const Ste
     const Taps t = make_taps(gc, back.x, back.y, back.z);
     stf(pred + i, lerp8x4(t, conc4).y);
   } else {
-    const dob_v3 v0 = gc.nx == g.nx ? sample_center_exact(g, cen, uvw) : sample_center(g, cen, uvw);
+    const dob_v3 v0 = gc.nx == g.nx ? center_at_cell(g, cen, uvw, x, y, z, i) : sample_center(g, cen, uvw);
     const dob_v3 mid = clamp3(uvw - (0.5f * (v0 * dtv)) / dom, 0.001f, 0.999f);
     const dob_v3 vMid = sample_center(g, cen, mid);
     const dob_v3 back = clamp3(uvw - (vMid * dtv) / dom, 0.001f, 0.999f);
@@ -645,9 +657,9 @@ __global__ void __launch_bounds__(256) k_dye_resolve_box(Grid gc, Grid g, const 
   const StepParams& P = *Pp;
   const dob_v3 dims = v3((float)gc.nx, (float)gc.ny, (float)gc.nz);
   const float dtv = P.dt;
-  const dob_v3 dom = dsize_of(P);
-  const dob_v3 uvw = (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / dims;
-  const dob_v3 v0 = gc.nx == g.nx ? sample_center_exact(g, cen, uvw) : sample_center(g, cen, uvw);
+  const Recip3 dom = recip3(dsize_of(P));
+  const dob_v3 uvw = (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / recip3(dims);
+  const dob_v3 v0 = gc.nx == g.nx ? center_at_cell(g, cen, uvw, x, y, z, i) : sample_center(g, cen, uvw);
   const dob_v3 uvwMid = clamp3(uvw - (0.5f * (v0 * dtv)) / dom, 0.001f, 0.999f);
   const dob_v3 vMid = sample_center(g, cen, uvwMid);
   const dob_v3 uvwBack = clamp3(uvw - (vMid * dtv) / dom, 0.001f, 0.999f);
