@@ -219,6 +219,13 @@ static void enqueue_step_body(dob_ctx* ctx, DevState& s, cudaStream_t st, float*
     } else if (stage == DOB_STAGE_CASSON_FORCES && box_casson_applies(s)) {
       launch_casson_box(s, st);
       swap_vel(s);
+    } else if (!s.ref && stage == DOB_STAGE_CONC_PREDICT) {
+      // closed box: the predictor brackets its taps for the resolve, which
+      // then traces only the forward sample
+      launch_conc_predict(s, st, true);
+    } else if (!s.ref && stage == DOB_STAGE_CONC_RESOLVE) {
+      launch_dye_resolve_lim(s, st);
+      std::swap(s.conc, s.conc2);
     } else {
       enqueue_stage(ctx, s, stage, st);
     }
@@ -481,6 +488,7 @@ dob_status dob_create(const dob_config* cfg, dob_ctx** out) {
   A((void**)&s.p, N * 4); A((void**)&s.rhs, N * 4);
   const int nch = s.ref ? 4 : 1;
   A(&s.conc, Nc * nch * dsb); A(&s.conc2, Nc * nch * dsb); A(&s.pred, Nc * dsb);
+  if (!s.ref) A(&s.lim, Nc * 2 * dsb);
   A((void**)&s.splatI, Nc * 4); A((void**)&s.splatL, Nc * 4);
   A((void**)&s.wave, (size_t)kWaveN * kWaveN * 16);
   A((void**)&s.parcels, (size_t)s.cap * 32);

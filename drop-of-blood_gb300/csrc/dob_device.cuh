@@ -111,8 +111,17 @@ __device__ __forceinline__ Taps taps_at(const Grid& g, float cx, float cy, float
   t.oz = (uint32_t)(z1 - z0) * sz;
   return t;
 }
+// texel coordinate u n - 1/2 as one FMA (the same bits in every kernel;
+// unfused under DOB_UNFUSED)
+__device__ __forceinline__ float texel(float u, int n) {
+#if defined(DOB_UNFUSED)
+  return u * (float)n - 0.5f;
+#else
+  return __fmaf_rn(u, (float)n, -0.5f);
+#endif
+}
 __device__ __forceinline__ Taps make_taps(const Grid& g, float u, float v, float w) {
-  return taps_at(g, u * (float)g.nx - 0.5f, v * (float)g.ny - 0.5f, w * (float)g.nz - 0.5f);
+  return taps_at(g, texel(u, g.nx), texel(v, g.ny), texel(w, g.nz));
 }
 // make_taps with the texel coordinate formed without FMA contraction (the
 // rounded product, then the subtraction), as the host oracle forms it.  At
@@ -133,6 +142,20 @@ template <class S> __device__ __forceinline__ float lerp8(const Taps& t, const S
   const float y0 = dob_mix(x00, x10, t.fy);
   const float y1 = dob_mix(x01, x11, t.fy);
   return dob_mix(y0, y1, t.fz);
+}
+// The 8 taps of a scalar field; lerp8 of them, and their minimum and maximum
+// (the MacCormack limiter's bracket: the trees keep the second operand on
+// ties, in the tap order base, +x, +y, +xy, +z, +xz, +yz, +xyz).
+template <class S> __device__ __forceinline__ void load8(const Taps& t, const S* a, float c[8]) {
+  const S* p = a + t.base;
+  c[0] = ldf(p); c[1] = ldf(p + t.ox); c[2] = ldf(p + t.oy); c[3] = ldf(p + t.oy + t.ox);
+  c[4] = ldf(p + t.oz); c[5] = ldf(p + t.oz + t.ox); c[6] = ldf(p + t.oz + t.oy); c[7] = ldf(p + t.oz + t.oy + t.ox);
+}
+__device__ __forceinline__ float min8(const float c[8]) {
+  return dob_minf(dob_minf(dob_minf(c[0], c[1]), dob_minf(c[2], c[3])), dob_minf(dob_minf(c[4], c[5]), dob_minf(c[6], c[7])));
+}
+__device__ __forceinline__ float max8(const float c[8]) {
+  return dob_maxf(dob_maxf(dob_maxf(c[0], c[1]), dob_maxf(c[2], c[3])), dob_maxf(dob_maxf(c[4], c[5]), dob_maxf(c[6], c[7])));
 }
 __device__ __forceinline__ float tri(float c000, float c100, float c010, float c110, float c001, float c101,
                                      float c011, float c111, const Taps& t) {

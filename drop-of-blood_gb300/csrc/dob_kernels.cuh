@@ -46,6 +46,7 @@ struct DevState {
   void *cen, *curl;              // 4 x VS AoS
   float *p, *rhs;                // red-black split layout (rb_index)
   void *conc, *conc2, *pred;     // dye (DS)
+  void* lim;                     // closed box: the predictor's tap minimum and maximum (2 x DS per cell)
   uint32_t *splatI, *splatL;
   float4* wave;
   float* parcels;
@@ -217,7 +218,10 @@ void launch_mac_rhs_box(const DevState& s, cudaStream_t st);  // with the zero-m
 // projected faces, one pass (the caller swaps the buffers)
 void launch_project_center_box(const DevState& s, cudaStream_t st);
 void launch_divergence(const DevState& s, float* out, float scale, unsigned int* maxbits, cudaStream_t st);
-void launch_conc_predict(const DevState& s, cudaStream_t st);
+// bracket: also write the minimum and maximum of the predictor's 8 dye taps
+// (closed box) for launch_dye_resolve_lim
+void launch_conc_predict(const DevState& s, cudaStream_t st, bool bracket = false);
+void launch_dye_resolve_lim(const DevState& s, cudaStream_t st);
 void launch_conc_resolve(const DevState& s, cudaStream_t st);
 
 // Largest coarsest grid solved exactly by the dense inverse (64 MB of FP32),

@@ -55,7 +55,18 @@ DOB_HD float dob_minf(float a, float b) { return a < b ? a : b; }
 DOB_HD float dob_maxf(float a, float b) { return a > b ? a : b; }
 DOB_HD float dob_clampf(float e, float lo, float hi) { return dob_minf(dob_maxf(e, lo), hi); }
 DOB_HD int dob_clampi(int e, int lo, int hi) { return e < lo ? lo : (e > hi ? hi : e); }
-DOB_HD float dob_mix(float a, float b, float t) { return a * (1.0f - t) + b * t; }
+// On the device one fixed rounding sequence (the rounded a (1 - t), then one
+// FMA with b t), so every kernel that interpolates the same taps gets the
+// same bits whatever the compiler would contract.  A translation unit that
+// must match the host's unfused arithmetic (compiled with -fmad=false)
+// defines DOB_UNFUSED before including this header.
+DOB_HD float dob_mix(float a, float b, float t) {
+#if defined(__CUDA_ARCH__) && !defined(DOB_UNFUSED)
+  return __fmaf_rn(b, t, __fmul_rn(a, 1.0f - t));
+#else
+  return a * (1.0f - t) + b * t;
+#endif
+}
 DOB_HD float dob_smoothstep(float e0, float e1, float x) {
   float t = dob_clampf((x - e0) / (e1 - e0), 0.0f, 1.0f);
   return t * t * (3.0f - 2.0f * t);

@@ -225,8 +225,8 @@ void replay_segment(dob_ctx* ctx, int len) {
     t.u2 = A->Tu[j + 1]; t.v2 = A->Tv[j + 1]; t.w2 = A->Tw[j + 1]; t.cen = A->Tcen[j + 1];
     launch_project_center_box(t, st);
     t.conc = A->Tc[j]; t.pred = A->Tpred[j]; t.conc2 = A->Tc[j + 1];
-    launch_conc_predict(t, st);
-    launch_conc_resolve(t, st);
+    launch_conc_predict(t, st, true);
+    launch_dye_resolve_lim(t, st);
   }
 }
 

@@ -57,9 +57,9 @@ struct NodeLo {
   uint32_t hx, hy, hz;  // base + 1 -> base + 2
 };
 __device__ __forceinline__ NodeLo node_lo(const Grid& g, float u, float v, float w) {
-  const int ix = dob_clampi((int)floorf(u * (float)g.nx - 0.5f), 0, g.nx - 1);
-  const int iy = dob_clampi((int)floorf(v * (float)g.ny - 0.5f), 0, g.ny - 1);
-  const int iz = dob_clampi((int)floorf(w * (float)g.nz - 0.5f), 0, g.nz - 1);
+  const int ix = dob_clampi((int)floorf(texel(u, g.nx)), 0, g.nx - 1);  // as make_taps forms it
+  const int iy = dob_clampi((int)floorf(texel(v, g.ny)), 0, g.ny - 1);
+  const int iz = dob_clampi((int)floorf(texel(w, g.nz)), 0, g.nz - 1);
   const uint32_t sy = (uint32_t)g.nx, sz = (uint32_t)g.nx * (uint32_t)g.ny;
   NodeLo n;
   n.lx = ix > 0 ? 1u : 0u;
@@ -809,9 +809,10 @@ __global__ void __launch_bounds__(256) k_adj_dye_resolve(Grid gc, Grid g, const 
   const Taps tF = make_taps(gc, uvwFwd.x, uvwFwd.y, uvwFwd.z);
   const float gBackEst = lerp8(tF, pred);
   const float kap = 0.45f * P.sharp;
-  const float gCorr = pred[i] + kap * (dye[i] - gBackEst);
-  const dob_v3 tc = uvwBack * dims - v3(0.5f, 0.5f, 0.5f);
-  const int bx = (int)floorf(tc.x), by = (int)floorf(tc.y), bz = (int)floorf(tc.z);
+  const float gCorr = __fmaf_rn(kap, dye[i] - gBackEst, pred[i]);  // as the forward rounds it
+  // the limiter's taps: the forward predictor's (make_taps at the departure point)
+  const int bx = (int)floorf(texel(uvwBack.x, gc.nx)), by = (int)floorf(texel(uvwBack.y, gc.ny));
+  const int bz = (int)floorf(texel(uvwBack.z, gc.nz));
   size_t id[8];
   float s[8];
 #pragma unroll

@@ -8,7 +8,9 @@
 // library's own transcendentals, so a parcel's position, and therefore its
 // splat cell (floor(uvw * dims - 0.5), particles.ts:239-247), is the same on
 // the host and the device for the same inputs.  Splat sums are unsigned
-// integer atomics: their order does not change the result.
+// integer atomics: their order does not change the result.  DOB_UNFUSED
+// keeps the shared sampling helpers in that unfused form here.
+#define DOB_UNFUSED 1
 #include "dob_kernels.cuh"
 
 namespace dob {

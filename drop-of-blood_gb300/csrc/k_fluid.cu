@@ -469,7 +469,8 @@ template <class VS, class DS>
 __global__ void __launch_bounds__(256) k_conc_predict(Grid gc, Grid g, const StepParams* __restrict__ Pp, int ref,
                                                       const typename Vec4Of<VS>::type* __restrict__ cen,
                                                       const typename Vec4Of<DS>::type* __restrict__ conc4,
-                                                      const DS* __restrict__ dye, DS* __restrict__ pred) {
+                                                      const DS* __restrict__ dye, DS* __restrict__ pred,
+                                                      DS* __restrict__ lim) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int z = blockIdx.z;
@@ -500,7 +501,16 @@ __global__ void __launch_bounds__(256) k_conc_predict(Grid gc, Grid g, const Ste
     const dob_v3 mid = clamp3(uvw - (0.5f * (v0 * dtv)) / dom, 0.001f, 0.999f);
     const dob_v3 vMid = sample_center(g, cen, mid);
     const dob_v3 back = clamp3(uvw - (vMid * dtv) / dom, 0.001f, 0.999f);
-    stf(pred + i, lerp8(make_taps(gc, back.x, back.y, back.z), dye));
+    const Taps tb = make_taps(gc, back.x, back.y, back.z);
+    if (lim) {  // also the limiter's bracket for k_dye_resolve_lim
+      float c[8];
+      load8(tb, dye, c);
+      stf(pred + i, tri(c[0], c[1], c[2], c[3], c[4], c[5], c[6], c[7], tb));
+      stf(lim + 2 * i, min8(c));
+      stf(lim + 2 * i + 1, max8(c));
+    } else {
+      stf(pred + i, lerp8(tb, dye));
+    }
   }
 }
 
@@ -666,16 +676,41 @@ __global__ void __launch_bounds__(256) k_dye_resolve_box(Grid gc, Grid g, const 
   const dob_v3 uvwFwd = clamp3(uvw + (v0 * dtv) / dom, 0.001f, 0.999f);
   const float gBackEst = lerp8(make_taps(gc, uvwFwd.x, uvwFwd.y, uvwFwd.z), pred);
   const float gOrig = ldf(dye + i);
-  const float gCorr = ldf(pred + i) + (0.45f * P.sharp) * (gOrig - gBackEst);
-  const dob_v3 tc = uvwBack * dims - v3(0.5f, 0.5f, 0.5f);
-  const int bx = (int)floorf(tc.x), by = (int)floorf(tc.y), bz = (int)floorf(tc.z);
-  const float s000 = ldcs(gc, dye, bx, by, bz), s100 = ldcs(gc, dye, bx + 1, by, bz);
-  const float s010 = ldcs(gc, dye, bx, by + 1, bz), s110 = ldcs(gc, dye, bx + 1, by + 1, bz);
-  const float s001 = ldcs(gc, dye, bx, by, bz + 1), s101 = ldcs(gc, dye, bx + 1, by, bz + 1);
-  const float s011 = ldcs(gc, dye, bx, by + 1, bz + 1), s111 = ldcs(gc, dye, bx + 1, by + 1, bz + 1);
-  const float minG = dob_minf(dob_minf(dob_minf(s000, s100), dob_minf(s010, s110)), dob_minf(dob_minf(s001, s101), dob_minf(s011, s111)));
-  const float maxG = dob_maxf(dob_maxf(dob_maxf(s000, s100), dob_maxf(s010, s110)), dob_maxf(dob_maxf(s001, s101), dob_maxf(s011, s111)));
-  stf(out + i, dob_clampf(gCorr, minG, maxG));
+  // one explicit FMA, so the step's and the stage's resolve (and the
+  // adjoint's replay of it) round the correction alike
+  const float gCorr = __fmaf_rn(0.45f * P.sharp, gOrig - gBackEst, ldf(pred + i));
+  // the limiter's bracket: the 8 dye taps around the departure point (the
+  // predictor's taps)
+  float c[8];
+  load8(make_taps(gc, uvwBack.x, uvwBack.y, uvwBack.z), dye, c);
+  stf(out + i, dob_clampf(gCorr, min8(c), max8(c)));
+}
+
+// The same resolve in the step: the predictor (k_conc_predict with `lim`)
+// has already bracketed its 8 taps, so only the forward sample is traced.
+template <class VS, class DS>
+__global__ void __launch_bounds__(256) k_dye_resolve_lim(Grid gc, Grid g, const StepParams* __restrict__ Pp,
+                                                         const typename Vec4Of<VS>::type* __restrict__ cen,
+                                                         const DS* __restrict__ dye, const DS* __restrict__ pred,
+                                                         const DS* __restrict__ lim, DS* __restrict__ out) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  if (x >= gc.nx || y >= gc.ny) return;
+  const size_t i = gc.at(x, y, z);
+  const StepParams& P = *Pp;
+  const float dtv = P.dt;
+  const Recip3 dom = recip3(dsize_of(P));
+  const dob_v3 uvw = (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) /
+                     recip3(v3((float)gc.nx, (float)gc.ny, (float)gc.nz));
+  const dob_v3 v0 = gc.nx == g.nx ? center_at_cell(g, cen, uvw, x, y, z, i) : sample_center(g, cen, uvw);
+  const dob_v3 uvwFwd = clamp3(uvw + (v0 * dtv) / dom, 0.001f, 0.999f);
+  const float gBackEst = lerp8(make_taps(gc, uvwFwd.x, uvwFwd.y, uvwFwd.z), pred);
+  const float gOrig = ldf(dye + i);
+  // one explicit FMA, so the step's and the stage's resolve (and the
+  // adjoint's replay of it) round the correction alike
+  const float gCorr = __fmaf_rn(0.45f * P.sharp, gOrig - gBackEst, ldf(pred + i));
+  stf(out + i, dob_clampf(gCorr, ldf(lim + 2 * i), ldf(lim + 2 * i + 1)));
 }
 
 // ---- host launchers ------------------------------------------------------------------------------
@@ -749,11 +784,20 @@ void launch_divergence(const DevState& s, float* out, float scale, unsigned int*
   });
 }
 
-void launch_conc_predict(const DevState& s, cudaStream_t st) {
+void launch_conc_predict(const DevState& s, cudaStream_t st, bool bracket) {
   DOB_VEL_DISPATCH(s.prec, {
     k_conc_predict<VS, DS><<<cell_grid(s.gc), cell_block(), 0, st>>>(
         s.gc, s.g, s.params, s.ref, (const typename Vec4Of<VS>::type*)s.cen,
-        (const typename Vec4Of<DS>::type*)s.conc, (const DS*)s.conc, (DS*)s.pred);
+        (const typename Vec4Of<DS>::type*)s.conc, (const DS*)s.conc, (DS*)s.pred,
+        bracket && !s.ref ? (DS*)s.lim : nullptr);
+  });
+}
+
+void launch_dye_resolve_lim(const DevState& s, cudaStream_t st) {
+  DOB_VEL_DISPATCH(s.prec, {
+    k_dye_resolve_lim<VS, DS><<<cell_grid(s.gc), cell_block(), 0, st>>>(
+        s.gc, s.g, s.params, (const typename Vec4Of<VS>::type*)s.cen, (const DS*)s.conc, (const DS*)s.pred,
+        (const DS*)s.lim, (DS*)s.conc2);
   });
 }
 
