@@ -192,24 +192,34 @@ __device__ __forceinline__ void adj_face(const Grid& g, const float* uk, const f
   scatter8v(acen, t0, gv0);
 }
 
-__global__ void __launch_bounds__(256) k_adj_advect_mac(Grid g, const StepParams* __restrict__ Pp,
+// One thread per face (grid z = 3 nz: the face's axis is blockIdx.z % 3,
+// uniform over the block), so a thread holds one face's trace; capped at 64
+// registers (4 blocks per SM, a 12-byte spill): the kernel is bound by the
+// latency of its gathers, and twice the resident warps of the uncapped
+// three-face thread hide more of it.
+__global__ void __launch_bounds__(256, 4) k_adj_advect_mac(Grid g, const StepParams* __restrict__ Pp,
                                                         const float* __restrict__ u, const float* __restrict__ v,
                                                         const float* __restrict__ w, const float4* __restrict__ cen,
                                                         const float* __restrict__ au2, const float* __restrict__ av2,
                                                         const float* __restrict__ aw2, float* au, float* av, float* aw,
                                                         float4* acen) {
-  ADJ_CELL
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int comp = blockIdx.z % 3, z = blockIdx.z / 3;
+  if (x >= g.nx || y >= g.ny) return;
+  const size_t i = g.at(x, y, z);
   const StepParams& P = *Pp;
   const dob_v3 dims = v3((float)g.nx, (float)g.ny, (float)g.nz);
   const Recip3 dimr = recip3(dims), dom = recip3(dsize_of(P));
   const float dtv = P.dt;
   const float damp = P.damp;
-  const float gx = x >= g.nx - 1 ? 0.0f : au2[i] * damp;
-  const float gy = y >= g.ny - 1 ? 0.0f : av2[i] * damp;
-  const float gz = z >= g.nz - 1 ? 0.0f : aw2[i] * damp;
-  adj_face(g, u, cen, acen, au, v3((float)x + 1.0f, (float)y + 0.5f, (float)z + 0.5f) / dimr, 0, gx, dtv, dom, dims);
-  adj_face(g, v, cen, acen, av, v3((float)x + 0.5f, (float)y + 1.0f, (float)z + 0.5f) / dimr, 1, gy, dtv, dom, dims);
-  adj_face(g, w, cen, acen, aw, v3((float)x + 0.5f, (float)y + 0.5f, (float)z + 1.0f) / dimr, 2, gz, dtv, dom, dims);
+  const bool wall = comp == 0 ? x >= g.nx - 1 : comp == 1 ? y >= g.ny - 1 : z >= g.nz - 1;
+  const float* ga = comp == 0 ? au2 : comp == 1 ? av2 : aw2;
+  const float gout = wall ? 0.0f : ga[i] * damp;
+  const dob_v3 F = v3((float)x + (comp == 0 ? 1.0f : 0.5f), (float)y + (comp == 1 ? 1.0f : 0.5f),
+                      (float)z + (comp == 2 ? 1.0f : 0.5f)) / dimr;
+  adj_face(g, comp == 0 ? u : comp == 1 ? v : w, cen, acen, comp == 0 ? au : comp == 1 ? av : aw, F, comp, gout, dtv,
+           dom, dims);
 }
 
 // ---- FLUID_MAC_TO_CENTER (closed box): au += C^T acen ---------------------------------------
@@ -849,7 +859,8 @@ static inline dim3 cblock() { return dim3(32, 8, 1); }
 static inline dim3 hgrid(const Grid& g) { return dim3((g.nx / 2 + 31) / 32, (g.ny + 7) / 8, g.nz); }
 
 void launch_adj_advect_mac(const DevState& s, const AdjState& a, cudaStream_t st) {
-  k_adj_advect_mac<<<cgrid(s.g), cblock(), 0, st>>>(s.g, s.params, (const float*)s.u, (const float*)s.v,
+  const dim3 g3(cgrid(s.g).x, cgrid(s.g).y, 3 * s.g.nz);
+  k_adj_advect_mac<<<g3, cblock(), 0, st>>>(s.g, s.params, (const float*)s.u, (const float*)s.v,
                                                     (const float*)s.w, (const float4*)s.cen, a.au2, a.av2, a.aw2, a.au,
                                                     a.av, a.aw, a.acen);
 }
