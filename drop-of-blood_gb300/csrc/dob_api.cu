@@ -1023,4 +1023,22 @@ namespace dob {
 dob_status record_static_error(dob_status st, const char* what, const char* detail) {
   return fail(nullptr, st, what, detail);
 }
+
+// A step whose body the caller enqueues itself (the adjoint tape records its
+// last segment this way): the host part of one_step before the body (the
+// step's parameters uploaded, the injection count), the parcel stages, and
+// the step count after it.  The V-cycle count of the body is the caller's.
+dob_status step_host_begin(dob_ctx* ctx) {
+  dob_status st = upload_params(ctx, spawn_count(ctx));
+  if (st != DOB_OK) return st;
+  if (ctx->inject_pending > 0) --ctx->inject_pending;
+  ctx->last_cycles = ctx->cfg.mg_cycles;
+  return DOB_OK;
+}
+void enqueue_parcel_stages(dob_ctx* ctx, DevState& s, cudaStream_t st) {
+  enqueue_stage(ctx, s, DOB_STAGE_CLEAR_SPLATS, st);
+  enqueue_stage(ctx, s, DOB_STAGE_PARCEL_EMIT, st);
+  enqueue_stage(ctx, s, DOB_STAGE_PARCEL_ADVECT, st);
+}
+void step_host_end(dob_ctx* ctx) { ctx->step_index++; }
 }  // namespace dob

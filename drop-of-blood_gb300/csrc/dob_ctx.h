@@ -85,4 +85,10 @@ dob_status record_error(dob_ctx* ctx, dob_status st, const char* what, const cha
 // dob_set_field / dob_get_field (kind 2: FP32 natural, 4: FP32 split).
 void adjoint_free(dob_ctx* ctx);
 bool adjoint_field(dob_ctx* ctx, int field, void** dev, size_t* count, int* kind);
+// A closed-box step enqueued by its caller (dob_api.cu): step_host_begin
+// (parameters, bookkeeping), the caller's body with enqueue_parcel_stages
+// after the projection, then step_host_end.
+dob_status step_host_begin(dob_ctx* ctx);
+void enqueue_parcel_stages(dob_ctx* ctx, DevState& s, cudaStream_t st);
+void step_host_end(dob_ctx* ctx);
 }  // namespace dob

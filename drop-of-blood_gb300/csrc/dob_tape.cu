@@ -31,6 +31,9 @@ struct AdjCtx {
   int k = 0;          // steps per checkpoint segment
   int nsteps = 0;     // recorded steps
   bool recorded = false;
+  // the tape slots hold the last segment's linearisation points, recorded by
+  // dob_tape_forward (no recomputation of that segment needed)
+  bool last_in_slots = false;
   std::vector<float*> ck;   // per checkpoint: u, v, w, dye, p (5 arrays)
   std::vector<void*> tbufs; // segment buffers
   std::vector<float*> Tu, Tv, Tw, Tc;  // k + 1 entries
@@ -41,7 +44,8 @@ struct AdjCtx {
   float* Tsc[3] = {nullptr, nullptr, nullptr};  // Casson's output during recomputation (no adjoint reads it)
   double* dred = nullptr;   // reduction slots of the drop gradients (4 doubles)
   // captured "recompute + reverse" graph of a segment, per (length, parity of
-  // the dye adjoint ping-pong at its start)
+  // the dye adjoint ping-pong at its start, recomputation or the recorded
+  // last segment)
   std::vector<cudaGraphExec_t> seg_graphs;
   void drop_graphs() {
     for (cudaGraphExec_t& g : seg_graphs)
@@ -197,37 +201,77 @@ void restore_checkpoint(dob_ctx* ctx, int seg) {
   cudaMemcpyAsync(A->Tc[0], c[3], Nc * 4, cudaMemcpyDeviceToDevice, st);
   cudaMemcpyAsync(A->Tp, c[4], N * 4, cudaMemcpyDeviceToDevice, st);
 }
-// From the restored checkpoint state in the first tape slot: recompute
-// `len` steps recording their linearisation points.
-void replay_segment(dob_ctx* ctx, int len) {
+// Step j of a segment from tape slot j: the step's fluid and dye stages
+// writing their linearisation points into the tape (slot j + 1 receives the
+// step's result).  Casson's output (the unprojected velocity, which no
+// adjoint stage reads) goes to scratch; the projection writes the next
+// step's velocity and centre velocity.  The column kernels give the bits of
+// the step graph's.  parcels: also the parcel stages of the step (recording
+// the forward pass).
+void tape_step(dob_ctx* ctx, int j, bool parcels) {
   AdjCtx* A = ctx->adj;
   const DevState& s = ctx->s;
   cudaStream_t st = ctx->stream;
   DevState t = s;
-  t.u = A->Tu[0]; t.v = A->Tv[0]; t.w = A->Tw[0]; t.cen = A->Tcen[0];
-  launch_mac_to_center(t, st);  // the centre velocity at a step's start is C(u)
-  for (int j = 0; j < len; ++j) {
-    t = s;
-    t.p = A->Tp; t.rhs = A->Trhs;
-    t.u = A->Tu[j]; t.v = A->Tv[j]; t.w = A->Tw[j]; t.cen = A->Tcen[j];
-    t.u2 = A->Tua[j]; t.v2 = A->Tva[j]; t.w2 = A->Twa[j];
-    launch_advect_mac(t, st);
-    // Casson's output (the unprojected velocity, which no adjoint stage
-    // reads) goes to scratch; the projection writes the next step's velocity
-    // and centre velocity into the tape.  The column kernels give the bits of
-    // the step graph's.
-    t.u = A->Tua[j]; t.v = A->Tva[j]; t.w = A->Twa[j]; t.conc = A->Tc[j];
-    t.u2 = A->Tsc[0]; t.v2 = A->Tsc[1]; t.w2 = A->Tsc[2];
-    launch_casson_box(t, st);
-    t.u = A->Tsc[0]; t.v = A->Tsc[1]; t.w = A->Tsc[2];
-    launch_mac_rhs_box(t, st);
-    launch_pressure_solve(t, st);
-    t.u2 = A->Tu[j + 1]; t.v2 = A->Tv[j + 1]; t.w2 = A->Tw[j + 1]; t.cen = A->Tcen[j + 1];
-    launch_project_center_box(t, st);
-    t.conc = A->Tc[j]; t.pred = A->Tpred[j]; t.conc2 = A->Tc[j + 1];
-    launch_conc_predict(t, st, true);
-    launch_dye_resolve_lim(t, st);
+  t.p = A->Tp; t.rhs = A->Trhs;
+  t.u = A->Tu[j]; t.v = A->Tv[j]; t.w = A->Tw[j]; t.cen = A->Tcen[j];
+  t.u2 = A->Tua[j]; t.v2 = A->Tva[j]; t.w2 = A->Twa[j];
+  launch_advect_mac(t, st);
+  t.u = A->Tua[j]; t.v = A->Tva[j]; t.w = A->Twa[j]; t.conc = A->Tc[j];
+  t.u2 = A->Tsc[0]; t.v2 = A->Tsc[1]; t.w2 = A->Tsc[2];
+  launch_casson_box(t, st);
+  t.u = A->Tsc[0]; t.v = A->Tsc[1]; t.w = A->Tsc[2];
+  launch_mac_rhs_box(t, st);
+  launch_pressure_solve(t, st);
+  t.u2 = A->Tu[j + 1]; t.v2 = A->Tv[j + 1]; t.w2 = A->Tw[j + 1]; t.cen = A->Tcen[j + 1];
+  launch_project_center_box(t, st);
+  if (parcels) {
+    DevState tp = s;
+    tp.cen = A->Tcen[j + 1];
+    enqueue_parcel_stages(ctx, tp, st);
   }
+  t.conc = A->Tc[j]; t.pred = A->Tpred[j]; t.conc2 = A->Tc[j + 1];
+  launch_conc_predict(t, st, true);
+  launch_dye_resolve_lim(t, st);
+}
+// From the restored checkpoint state in the first tape slot: recompute
+// `len` steps recording their linearisation points.
+void replay_segment(dob_ctx* ctx, int len) {
+  AdjCtx* A = ctx->adj;
+  DevState t = ctx->s;
+  t.u = A->Tu[0]; t.v = A->Tv[0]; t.w = A->Tw[0]; t.cen = A->Tcen[0];
+  launch_mac_to_center(t, ctx->stream);  // the centre velocity at a step's start is C(u)
+  for (int j = 0; j < len; ++j) tape_step(ctx, j, false);
+}
+// The forward pass's last segment (checkpoint `seg` just saved from the
+// context): its `len` steps computed once, by the recording kernels, with
+// each step's parameters and parcel stages as dob_step runs them; then the
+// context takes the final state from the tape.  The backward finds this
+// segment's linearisation points in the slots and does not recompute it.
+dob_status record_last_segment(dob_ctx* ctx, int seg, int len) {
+  AdjCtx* A = ctx->adj;
+  DevState& s = ctx->s;
+  cudaStream_t st = ctx->stream;
+  const size_t N = s.g.n(), Nc = s.gc.n();
+  restore_checkpoint(ctx, seg);
+  DevState t = s;
+  t.u = A->Tu[0]; t.v = A->Tv[0]; t.w = A->Tw[0]; t.cen = A->Tcen[0];
+  launch_mac_to_center(t, st);
+  for (int j = 0; j < len; ++j) {
+    dob_status e = step_host_begin(ctx);
+    if (e != DOB_OK) return e;
+    tape_step(ctx, j, true);
+    step_host_end(ctx);
+  }
+  cudaMemcpyAsync(s.u, A->Tu[len], N * 4, cudaMemcpyDeviceToDevice, st);
+  cudaMemcpyAsync(s.v, A->Tv[len], N * 4, cudaMemcpyDeviceToDevice, st);
+  cudaMemcpyAsync(s.w, A->Tw[len], N * 4, cudaMemcpyDeviceToDevice, st);
+  cudaMemcpyAsync(s.cen, A->Tcen[len], N * sizeof(float4), cudaMemcpyDeviceToDevice, st);
+  cudaMemcpyAsync(s.conc, A->Tc[len], Nc * 4, cudaMemcpyDeviceToDevice, st);
+  cudaMemcpyAsync(s.pred, A->Tpred[len - 1], Nc * 4, cudaMemcpyDeviceToDevice, st);
+  cudaMemcpyAsync(s.p, A->Tp, N * 4, cudaMemcpyDeviceToDevice, st);
+  cudaMemcpyAsync(s.rhs, A->Trhs, N * 4, cudaMemcpyDeviceToDevice, st);
+  return DOB_OK;
 }
 
 template <class T> void swap3(T& a, T& b, T& c, T& d, T& e, T& f) {
@@ -344,19 +388,25 @@ dob_status dob_tape_forward(dob_ctx* ctx, int nsteps, int checkpoint_every) {
   if ((st = ensure_tape(ctx, k, nseg)) != DOB_OK) return st;
   AdjCtx* A = ctx->adj;
   A->recorded = false;
+  A->last_in_slots = false;
   // every recorded step runs mg_cycles V-cycles, as the recomputation does
   ctx->inject_pending = 0;
   TCK(cudaStreamSynchronize(ctx->stream));
   launch_mac_to_center(ctx->s, ctx->stream);
-  for (int n = 0; n < nsteps; ++n) {
+  const int last = (nseg - 1) * k;  // first step of the last segment
+  for (int n = 0; n < last; ++n) {
     if (n % k == 0) save_checkpoint(ctx, n / k);
     st = dob_step(ctx, 1, 0, nullptr);
     if (st != DOB_OK) return st;
   }
+  save_checkpoint(ctx, nseg - 1);
+  st = record_last_segment(ctx, nseg - 1, nsteps - last);
+  if (st != DOB_OK) return st;
   TCK(cudaGetLastError());
   TCK(cudaStreamSynchronize(ctx->stream));
   A->nsteps = nsteps;
   A->recorded = true;
+  A->last_in_slots = true;
   return DOB_OK;
 }
 
@@ -372,21 +422,24 @@ dob_status dob_tape_backward(dob_ctx* ctx, const float* dye_grad, size_t bytes) 
   TCK(cudaMemcpyAsync(A->a.ac, dye_grad, bytes, cudaMemcpyHostToDevice, st));
   const int k = A->k;
   const int nseg = (A->nsteps + k - 1) / k;
-  if (A->seg_graphs.size() != (size_t)(2 * (k + 1))) {
+  if (A->seg_graphs.size() != (size_t)(4 * (k + 1))) {
     A->drop_graphs();
-    A->seg_graphs.assign(2 * (k + 1), nullptr);
+    A->seg_graphs.assign(4 * (k + 1), nullptr);
   }
   for (int seg = nseg - 1; seg >= 0; --seg) {
     const int len = (seg == nseg - 1) ? A->nsteps - seg * k : k;
-    restore_checkpoint(ctx, seg);
+    // the last segment's points are still in the slots after dob_tape_forward
+    const bool recompute = !(seg == nseg - 1 && A->last_in_slots);
+    if (recompute) restore_checkpoint(ctx, seg);
     // The segment's launches only depend on (len, which dye adjoint buffer is
-    // current): capture them once as a graph and replay it.
+    // current, recomputation or not): capture them once as a graph and
+    // replay it.
     const int parity = A->a.ac < A->a.ac2 ? 0 : 1;
-    cudaGraphExec_t& ge = A->seg_graphs[2 * len + parity];
+    cudaGraphExec_t& ge = A->seg_graphs[(recompute ? 0 : 2 * (k + 1)) + 2 * len + parity];
     const AdjState before = A->a;
     if (!ge) {
       TCK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-      replay_segment(ctx, len);
+      if (recompute) replay_segment(ctx, len);
       for (int j = len - 1; j >= 0; --j) backward_step(ctx, j);
       cudaGraph_t g = nullptr;
       TCK(cudaStreamEndCapture(st, &g));
@@ -404,6 +457,7 @@ dob_status dob_tape_backward(dob_ctx* ctx, const float* dye_grad, size_t bytes) 
     // the swaps the segment performs: dye adjoint ping-pong once per step,
     // velocity adjoints twice per step (net none)
     if (len & 1) std::swap(A->a.ac, A->a.ac2);
+    if (recompute) A->last_in_slots = false;  // the slots now hold this segment
   }
   TCK(cudaGetLastError());
   // the trajectory starts from cen = C(u(0))

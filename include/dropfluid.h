@@ -340,12 +340,15 @@ dob_status dob_adjoint_stage(dob_ctx* ctx, int stage);
 /* Forward half of the forward/backward pair: sets the centre velocity from
    the MAC faces (so the trajectory's state is velocity, dye and pressure),
    then runs nsteps steps, keeping a checkpoint of (velocity, dye, pressure)
-   every `checkpoint_every` steps in device memory.  The context ends in the
-   final state, as after dob_step. */
+   every `checkpoint_every` steps in device memory.  The steps of the last
+   segment also record the linearisation points the backward needs, so the
+   next dob_tape_backward does not recompute that segment.  The context ends
+   in the final state, as after dob_step (same bits). */
 dob_status dob_tape_forward(dob_ctx* ctx, int nsteps, int checkpoint_every);
 
 /* Backward half: given d loss / d final dye (Nc floats, host), recomputes
-   each checkpoint segment and runs the adjoint of every step in reverse.
+   each checkpoint segment (all but the last after dob_tape_forward; every
+   one when called again) and runs the adjoint of every step in reverse.
    Leaves d loss / d initial MAC velocity in DOB_FIELD_ADJ_VEL_U/V/W,
    d loss / d initial dye in DOB_FIELD_ADJ_CONC and d loss / d initial
    pressure in DOB_FIELD_ADJ_PRESSURE.  The forward state is not changed. */

@@ -201,3 +201,39 @@ def test_soft_drop_gradient(gpu_lib, oracle_mod):
         fdk = (run(g, cp, 1.0, 4)[0] - run(g, cm, 1.0, 4)[0]) / (cp[k] - cm[k])
         assert abs(fdk - gp[k]) <= 1e-2 * np.linalg.norm(gp), (k, fdk, gp)
     g.close()
+
+
+def test_recorded_forward_matches_steps_and_repeats(gpu_lib):
+    """dob_tape_forward computes its last segment with the recording kernels
+    (the backward then does not recompute it): the context ends in the same
+    bits as plain steps from the same state, parcels included, and a second
+    backward without a new forward, which recomputes that segment from its
+    checkpoint, gives the same gradients."""
+    from dropfluid import DropFluid, scenes
+    cfg, center, r = AC.drop_scene((24, 32, 24))
+    cfg.parcel_capacity = 512
+    cfg.mg_cycles_injected = 0  # recorded steps run mg_cycles V-cycles
+    a, b = DropFluid(cfg), DropFluid(cfg)
+    p = scenes.parcels_in_sphere(center, r, 512, 5)
+    for e in (a, b):
+        AC.init_drop(e, center, r, 1.0)
+        e.set_parcels(p)
+    steps, k = 7, 3  # three segments, the last one partial
+    a.tape_forward(steps, k)
+    b.run_stage(abi.STAGE_MAC_TO_CENTER)
+    b.step(steps)
+    for f in (abi.FIELD_VEL_U, abi.FIELD_VEL_V, abi.FIELD_VEL_W, abi.FIELD_VEL_CENTER, abi.FIELD_PRESSURE,
+              abi.FIELD_CONC):
+        x, y = a.get_field(f), b.get_field(f)
+        assert np.array_equal(x.view(np.uint32), y.view(np.uint32)), f
+    x, y = a.get_parcels(), b.get_parcels()
+    assert np.array_equal(x.view(np.uint32), y.view(np.uint32))
+    gd = (1e-3 * a.get_field(abi.FIELD_CONC)).astype(np.float32)
+    a.tape_backward(gd)
+    g1 = {c: v.copy() for c, v in a.gradients().items()}
+    a.tape_backward(gd)
+    g2 = a.gradients()
+    for c in ("u", "v", "w", "dye"):
+        assert rel_l2(g2[c], g1[c]) < 1e-6, c
+    a.close()
+    b.close()
