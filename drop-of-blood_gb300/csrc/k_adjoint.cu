@@ -609,7 +609,7 @@ __global__ void __cluster_dims__(CS, 1, 1) __launch_bounds__(512)
 // weight of coarse index J in the cell-centred linear interpolation at fine
 // index xf (the forward's clamped taps; 0 above a Dirichlet top when `top0`)
 __device__ __forceinline__ float prolong_w(int xf, int nf, int nc, int J, bool top0) {
-  const float cx = (((float)xf + 0.5f) / (float)nf) * (float)nc - 0.5f;
+  const float cx = __fmaf_rn(((float)xf + 0.5f) / (float)nf, (float)nc, -0.5f);  // as k_prolong_add2 forms it
   const float bx = floorf(cx);
   const float fx = cx - bx;
   const int i0 = (int)bx, i1 = i0 + 1;
