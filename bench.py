@@ -202,9 +202,11 @@ def adjoint_leg(fd_dirs: int = 16):
     the initial velocity).  box192 (three soft-edged r=12 drops injected at
     step 0, 64 steps, checkpoints every 16): the full-size cost and the
     gradient in the three impulses and release positions, against central
-    differences.  The ratio is the
-    wall time of dob_tape_backward per step (segment recomputation included)
-    over the device time of one forward step of the same scene."""
+    differences.  The ratio is the wall time per step of dob_tape_backward
+    right after its dob_tape_forward (recomputation of every segment but the
+    last, which the forward records) over the device time of one forward
+    step of the same scene; tape_forward_ms_per_step is the wall time per
+    step of that forward (checkpoints and the recorded last segment)."""
     import numpy as np
     from dropfluid import DropFluid, abi, scenes
     from dropfluid.adjoint import DropTrajectory, l2_loss
@@ -284,6 +286,11 @@ def adjoint_leg(fd_dirs: int = 16):
     loss, g = l2_loss(fwd192(sc), target)
     traj.backward(g)  # first call captures the segment graphs
     eng.sync()
+    # the timed backward follows its forward, as in a gradient step
+    t0 = time.perf_counter()
+    fwd192(sc)
+    eng.sync()
+    t_tape_fwd192 = time.perf_counter() - t0
     t0 = time.perf_counter()
     traj.backward(g)
     eng.sync()
@@ -311,6 +318,7 @@ def adjoint_leg(fd_dirs: int = 16):
         fd_pos.append(fdk)
         pos_err.append(float(np.linalg.norm(np.asarray(fdk) - gp) / np.linalg.norm(gp)))
     out["box192"] = {"steps": sc.steps, "checkpoint_every": 16, "forward_step_ms": fwd_ms,
+                     "tape_forward_ms_per_step": 1e3 * t_tape_fwd192 / sc.steps,
                      "backward_ms_per_step": 1e3 * t_bwd / sc.steps, "ratio": 1e3 * t_bwd / sc.steps / fwd_ms,
                      "loss": loss, "drops": "three soft-edged drops (edge 2 cells) injected at step 0, 393216 parcels",
                      "target": "same drops with impulses x(1.1, 0.9, 1.05) and centres shifted by up to 0.5 cells",

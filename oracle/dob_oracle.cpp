@@ -923,6 +923,8 @@ template <class R> class Sim {
   void coarse_exact(R* e, const R* b, const Dims& c, bool bf16) {
     const size_t n = c.n();
     if (cinv.size() != n * n) build_cinv(c);
+    // every output is its own sum (in i order): threads over j give the same bits
+#pragma omp parallel for schedule(static) if (n >= 512)
     for (size_t j = 0; j < n; ++j) {
       R acc = R(0);
       for (size_t i = 0; i < n; ++i) acc = acc + cinv_at(i * n + j) * b[i];
