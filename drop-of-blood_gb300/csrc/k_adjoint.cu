@@ -245,7 +245,7 @@ __device__ __forceinline__ dob_v3 out_adj(const Grid& g, const float* au2, const
 }
 // Pass 1: per cell, alpha and G = 2 dL/dQ (Q = |grad u|^2 of the Casson
 // shear rate); the dye adjoint of the cell.
-__global__ void __launch_bounds__(256) k_adj_casson1(Grid g, const StepParams* __restrict__ Pp,
+__global__ void __launch_bounds__(256, 5) k_adj_casson1(Grid g, const StepParams* __restrict__ Pp,
                                                      const float* __restrict__ u, const float* __restrict__ v,
                                                      const float* __restrict__ w, const float* __restrict__ dye,
                                                      const float* __restrict__ au2, const float* __restrict__ av2,
@@ -425,7 +425,7 @@ __device__ __forceinline__ float rcp_diag(float k) {
   return k == 6.0f ? 1.0f / 6.0f
                    : (k == 5.0f ? 0.2f : (k == 4.0f ? 0.25f : (k == 3.0f ? 1.0f / 3.0f : (k == 2.0f ? 0.5f : 1.0f))));
 }
-__global__ void __launch_bounds__(256) k_adj_rbgs_v4(Grid d, int color, float h2, int ref, int mode, float* __restrict__ a,
+__global__ void __launch_bounds__(256, 5) k_adj_rbgs_v4(Grid d, int color, float h2, int ref, int mode, float* __restrict__ a,
                                                      float* __restrict__ bb) {
   pdl_wait();
   pdl_trigger();
@@ -756,7 +756,11 @@ __global__ void __launch_bounds__(256) k_adj_prolong2(Grid f, Grid c, int ref, c
 }
 
 // ---- CONC_PREDICT (closed box) ------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_adj_conc_predict(Grid gc, Grid g, const StepParams* __restrict__ Pp,
+// The per-cell adjoints below (dye predictor and resolve, the Casson
+// coefficients) and the transposed smoother are capped at 4-5 blocks of 256
+// per SM (a few spilled bytes): latency-bound, they gain more from the
+// resident warps (192x256x192 backward 4.81 -> 4.67 ms per step).
+__global__ void __launch_bounds__(256, 4) k_adj_conc_predict(Grid gc, Grid g, const StepParams* __restrict__ Pp,
                                                           const float4* __restrict__ cen, const float* __restrict__ dye,
                                                           const float* __restrict__ apred, float* ac, float4* acen) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -792,7 +796,7 @@ __global__ void __launch_bounds__(256) k_adj_conc_predict(Grid gc, Grid g, const
 }
 
 // ---- CONC_RESOLVE (closed box: MacCormack with the 8-tap limiter) -----------------------------
-__global__ void __launch_bounds__(256) k_adj_dye_resolve(Grid gc, Grid g, const StepParams* __restrict__ Pp,
+__global__ void __launch_bounds__(256, 5) k_adj_dye_resolve(Grid gc, Grid g, const StepParams* __restrict__ Pp,
                                                          const float4* __restrict__ cen, const float* __restrict__ dye,
                                                          const float* __restrict__ pred, const float* __restrict__ ac2,
                                                          float* ac, float* apred, float4* acen) {

@@ -77,6 +77,10 @@ __global__ void k_init_vel(Grid g, const StepParams* __restrict__ Pp, VS* u, VS*
 }
 
 // ---- FLUID_ADVECT_MAC (fluid.ts:144-329) ------------------------------------------------
+// The semi-Lagrangian kernels (advection, dye predictor and resolve) are
+// bound by the latency of their gathers: their register caps (5, 8 and 8
+// blocks of 256 per SM, a few spilled bytes) buy resident warps, measured
+// at 192x256x192: 336 -> 327, 150 -> 131 and 94 -> 86 us.
 template <class VS>
 __device__ __forceinline__ float sample_mac(const Grid& g, const VS* a, dob_v3 uvw, int comp) {
   if (comp == 0) uvw.x = uvw.x - 0.5f / (float)g.nx;
@@ -100,7 +104,7 @@ __device__ __forceinline__ float azim_neck(float theta, float seed) {
 }
 
 template <class VS>
-__global__ void __launch_bounds__(256) k_advect_mac(Grid g, const StepParams* __restrict__ Pp, int ref, int flags,
+__global__ void __launch_bounds__(256, 5) k_advect_mac(Grid g, const StepParams* __restrict__ Pp, int ref, int flags,
                                                     const VS* __restrict__ u, const VS* __restrict__ v,
                                                     const VS* __restrict__ w,
                                                     const typename Vec4Of<VS>::type* __restrict__ cen,
@@ -466,7 +470,7 @@ __global__ void __launch_bounds__(256) k_divergence(Grid g, int ref, const VS* _
 
 // ---- CONC_PREDICT (advect.ts:28-72) -----------------------------------------------------------
 template <class VS, class DS>
-__global__ void __launch_bounds__(256) k_conc_predict(Grid gc, Grid g, const StepParams* __restrict__ Pp, int ref,
+__global__ void __launch_bounds__(256, 8) k_conc_predict(Grid gc, Grid g, const StepParams* __restrict__ Pp, int ref,
                                                       const typename Vec4Of<VS>::type* __restrict__ cen,
                                                       const typename Vec4Of<DS>::type* __restrict__ conc4,
                                                       const DS* __restrict__ dye, DS* __restrict__ pred,
@@ -689,7 +693,7 @@ __global__ void __launch_bounds__(256) k_dye_resolve_box(Grid gc, Grid g, const 
 // The same resolve in the step: the predictor (k_conc_predict with `lim`)
 // has already bracketed its 8 taps, so only the forward sample is traced.
 template <class VS, class DS>
-__global__ void __launch_bounds__(256) k_dye_resolve_lim(Grid gc, Grid g, const StepParams* __restrict__ Pp,
+__global__ void __launch_bounds__(256, 8) k_dye_resolve_lim(Grid gc, Grid g, const StepParams* __restrict__ Pp,
                                                          const typename Vec4Of<VS>::type* __restrict__ cen,
                                                          const DS* __restrict__ dye, const DS* __restrict__ pred,
                                                          const DS* __restrict__ lim, DS* __restrict__ out) {
