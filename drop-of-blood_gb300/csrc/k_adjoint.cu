@@ -705,6 +705,11 @@ __global__ void __launch_bounds__(256) k_adj_restrict2(Grid f, Grid c, float inv
 // Transposed prolongation, the mirror of k_prolong_add2: Ebar(X) += sum of
 // the interpolation weight on X times xb over the fine cells 2X-1..2X+2 of
 // each axis.
+// BLACK: the fine level's red cotangents are exactly zero (the transposed
+// sweeps that follow a black-only prolongation end with the red cells of
+// their input cleared): only the black cells of each fine row are read, the
+// red terms enter as the same zeros.
+template <bool BLACK>
 __global__ void __launch_bounds__(256) k_adj_prolong2(Grid f, Grid c, int ref, const float* __restrict__ xb,
                                                       float* __restrict__ Eb) {
   pdl_wait();
@@ -737,9 +742,11 @@ __global__ void __launch_bounds__(256) k_adj_prolong2(Grid f, Grid c, int ref, c
       const uint32_t r = (uint32_t)zf * sz + (uint32_t)yf * hx + w;
       const float* pe = xb + (par ? half : 0u) + r;  // even cells 4q, 4q+2 (words 2q, 2q+1)
       const float* po = xb + (par ? 0u : half) + r;  // odd cells 4q+1, 4q+3
-      const float2 e = ld2f(pe), o = ld2f(po);
-      const float lo = has_lo ? po[-1] : 0.0f;      // x = 4q-1 (odd, word 2q-1)
-      const float hi = has_hi ? pe[2] : 0.0f;       // x = 4q+4 (even, word 2q+2)
+      const float2 z2 = make_float2(0.0f, 0.0f);
+      // the even cells are black in rows of odd parity, the odd cells in the others
+      const float2 e = (!BLACK || par) ? ld2f(pe) : z2, o = (!BLACK || !par) ? ld2f(po) : z2;
+      const float lo = (has_lo && (!BLACK || !par)) ? po[-1] : 0.0f;  // x = 4q-1 (odd, word 2q-1)
+      const float hi = (has_hi && (!BLACK || par)) ? pe[2] : 0.0f;    // x = 4q+4 (even, word 2q+2)
       const float v[6] = {lo, e.x, o.x, e.y, o.y, hi};
       const float s0 = wx0[0] * v[0] + wx0[1] * v[1] + wx0[2] * v[2] + wx0[3] * v[3];
       const float s1 = wx1[0] * v[2] + wx1[1] * v[3] + wx1[2] * v[4] + wx1[3] * v[5];
@@ -1005,10 +1012,14 @@ static void adj_restrict(const DevState& s, const AdjState& a, int l, float* xb,
   launch_pdl(k_adj_restrict2, pgrid(c, b), b, 0, st, f, c, 1.0f / s.lv[l].h2, s.ref, a.lb[l + 1], xb, bb);
   cudaMemsetAsync(a.lb[l + 1], 0, c.n() * sizeof(float), st);
 }
-static void adj_prolong(const DevState& s, const AdjState& a, int l, const float* xb, cudaStream_t st) {
+// black: the level's post-smoothing has sweeps (the forward's prolongation
+// then updates only the black cells, and the transposed sweeps leave the
+// red cotangents zero)
+static void adj_prolong(const DevState& s, const AdjState& a, int l, const float* xb, bool black, cudaStream_t st) {
   const Grid f = s.lv[l].d, c = s.lv[l + 1].d;
   const dim3 b = pblock(c);
-  launch_pdl(k_adj_prolong2, pgrid(c, b), b, 0, st, f, c, s.ref, xb, a.le[l + 1]);
+  if (black) launch_pdl(k_adj_prolong2<true>, pgrid(c, b), b, 0, st, f, c, s.ref, xb, a.le[l + 1]);
+  else launch_pdl(k_adj_prolong2<false>, pgrid(c, b), b, 0, st, f, c, s.ref, xb, a.le[l + 1]);
 }
 // Transpose of one V-cycle (k_mg.cu vcycle) on (ap, arhs); the coarse
 // adjoint arrays are zero on entry and on exit.
@@ -1020,10 +1031,10 @@ static void adj_vcycle(const DevState& s, const AdjState& a, cudaStream_t st) {
     return;
   }
   adj_smooth(L0.d, L0.h2, s.ref, s.post0, a.ap, a.arhs, st);
-  adj_prolong(s, a, 0, a.ap, st);
+  adj_prolong(s, a, 0, a.ap, s.post0 > 0, st);
   for (int l = 1; l < L - 1; ++l) {
     adj_smooth(s.lv[l].d, s.lv[l].h2, s.ref, s.post, a.le[l], a.lb[l], st);
-    adj_prolong(s, a, l, a.le[l], st);
+    adj_prolong(s, a, l, a.le[l], s.post > 0, st);
   }
   const MgLevel& LC = s.lv[L - 1];
   adj_coarse(s, LC, s.ref, s.coarse_sweeps, a.le[L - 1], a.lb[L - 1], st);
