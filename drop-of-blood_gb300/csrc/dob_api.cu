@@ -212,10 +212,14 @@ static void enqueue_step_body(dob_ctx* ctx, DevState& s, cudaStream_t st, float*
     if (!s.ref && stage == DOB_STAGE_MAC_TO_CENTER) continue;
     if (stage_ms) cudaEventRecord(ctx->stage_ev[0], st);
     if (!s.ref && stage == DOB_STAGE_PROJECT) {
-      launch_project_center_box(s, st);
+      // with statistics the projection also forms max |div| (no separate pass)
+      if (stats_div) cudaMemsetAsync(s.redu + REDU_MAXDIV, 0, sizeof(unsigned int), st);
+      launch_project_center_box(s, st, ctx->cfg.dt / ctx->cfg.dx, stats_div ? s.redu + REDU_MAXDIV : nullptr);
       swap_vel(s);
     } else if (!s.ref && stage == DOB_STAGE_MAC_RHS) {
-      launch_mac_rhs_box(s, st);
+      // with statistics the mean removal also forms ||rhs||^2
+      if (stats_div) cudaMemsetAsync(s.red + RED_RHS_NORM2, 0, sizeof(double), st);
+      launch_mac_rhs_box(s, st, stats_div ? s.red + RED_RHS_NORM2 : nullptr);
     } else if (stage == DOB_STAGE_CASSON_FORCES && box_casson_applies(s)) {
       launch_casson_box(s, st);
       swap_vel(s);
@@ -236,14 +240,14 @@ static void enqueue_step_body(dob_ctx* ctx, DevState& s, cudaStream_t st, float*
       cudaEventElapsedTime(&ms, ctx->stage_ev[0], ctx->stage_ev[1]);
       stage_ms[stage] += ms;
     }
-    if (stats_div && stage == DOB_STAGE_MAC_RHS) {
+    if (stats_div && stage == DOB_STAGE_MAC_RHS && s.ref) {
       cudaMemsetAsync(s.red + RED_RHS_NORM2, 0, sizeof(double), st);
       launch_sumsq(s.rhs, s.g.n(), s.red + RED_RHS_NORM2, s.num_sms, st);
     }
     if (stats_div && stage == DOB_STAGE_PRESSURE_SOLVE) {
       launch_residual_norm(s, s.red + RED_RES_NORM2, st);
     }
-    if (stats_div && stage == DOB_STAGE_PROJECT) {
+    if (stats_div && stage == DOB_STAGE_PROJECT && s.ref) {
       const float scale = s.ref ? 1.0f : ctx->cfg.dt / ctx->cfg.dx;
       cudaMemsetAsync(s.redu + REDU_MAXDIV, 0, sizeof(unsigned int), st);
       launch_divergence(s, nullptr, scale, s.redu + REDU_MAXDIV, st);

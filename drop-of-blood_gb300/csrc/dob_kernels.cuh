@@ -213,10 +213,14 @@ void launch_project(const DevState& s, cudaStream_t st);
 // launch_mac_to_center.  Casson needs dye on the velocity grid.
 bool box_casson_applies(const DevState& s);
 void launch_casson_box(const DevState& s, cudaStream_t st);   // u -> u2 (caller swaps)
-void launch_mac_rhs_box(const DevState& s, cudaStream_t st);  // with the zero-mean correction
+// sumsq (statistics): the sum of squares of the mean-free right-hand side
+void launch_mac_rhs_box(const DevState& s, cudaStream_t st, double* sumsq = nullptr);  // with the zero-mean correction
 // projection of (u, v, w) into (u2, v2, w2) and the centre velocity of the
 // projected faces, one pass (the caller swaps the buffers)
-void launch_project_center_box(const DevState& s, cudaStream_t st);
+// maxbits: also max |div| * scale of the projected faces (statistics), as
+// launch_divergence forms it
+void launch_project_center_box(const DevState& s, cudaStream_t st, float scale = 0.0f,
+                               unsigned int* maxbits = nullptr);
 void launch_divergence(const DevState& s, float* out, float scale, unsigned int* maxbits, cudaStream_t st);
 // bracket: also write the minimum and maximum of the predictor's 8 dye taps
 // (closed box) for launch_dye_resolve_lim
@@ -243,7 +247,8 @@ cudaError_t mg_prepare();
 void launch_pressure_solve(const DevState& s, cudaStream_t st);
 void launch_residual_norm(const DevState& s, double* out, cudaStream_t st);
 void launch_sum(const float* a, size_t n, double* out, int num_sms, cudaStream_t st);
-void launch_sub_mean(float* a, size_t n, const double* sum, int num_sms, cudaStream_t st);
+// sumsq (statistics): also accumulate the sum of squares of the result there
+void launch_sub_mean(float* a, size_t n, const double* sum, int num_sms, cudaStream_t st, double* sumsq = nullptr);
 void launch_sumsq(const float* a, size_t n, double* out, int num_sms, cudaStream_t st);
 // Natural <-> red-black split copy of a level-0 array (field I/O).
 void launch_split(const float* src, float* dst, const Grid& d, bool to_split, cudaStream_t st);

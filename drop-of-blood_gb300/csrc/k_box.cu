@@ -103,11 +103,13 @@ __global__ void __launch_bounds__(256, 8) k_project_center_box(Grid g, const VS*
                                                             const float* __restrict__ p,
                                                             const float* __restrict__ plo, VS* __restrict__ uo,
                                                             VS* __restrict__ vo, VS* __restrict__ wo,
-                                                            typename Vec4Of<VS>::type* __restrict__ cen) {
+                                                            typename Vec4Of<VS>::type* __restrict__ cen,
+                                                            float scale, unsigned int* __restrict__ maxbits) {
   const Col c = column<ZC>(g);
-  if (c.z0 >= g.nz) return;
+  if (c.z0 >= g.nz) return;  // uniform over the block
   const uint32_t half = (uint32_t)(g.n() >> 1), hx = (uint32_t)g.nx >> 1;
   const bool df = plo != nullptr;
+  float mdiv = 0.0f;  // max |div| dt/dx of the projected faces (maxbits: statistics)
   auto pidx = [&](int x, int y, int z) {  // rb_index in 32 bits
     return ((uint32_t)(x + y + z) & 1u) * half + ((uint32_t)z * (uint32_t)g.ny + (uint32_t)y) * hx + ((uint32_t)x >> 1);
   };
@@ -154,12 +156,15 @@ __global__ void __launch_bounds__(256, 8) k_project_center_box(Grid g, const VS*
       stf(uo + i, mx); stf(vo + i, my); stf(wo + i, mz);
       const float uR = vs_round<VS>(mx), vU = vs_round<VS>(my), wF = vs_round<VS>(mz);
       st4(cen + i, make_float4(0.5f * (uL + uR), 0.5f * (vD + vU), 0.5f * (wB + wF), 0.0f));
+      // k_divergence's expression on the stored faces (walls are 0)
+      if (maxbits) mdiv = dob_maxf(mdiv, fabsf((uR - uL) + (vU - vD) + (wF - wB)) * scale);
     }
     pZn = pC; lZn = lC;
     pC = pZp; lC = lZp;
     wBold = wOwn;
     i += c.sz;
   }
+  if (maxbits) block_max_atomic(mdiv, maxbits);
 }
 
 template <int ZC>
@@ -180,20 +185,20 @@ void launch_casson_box(const DevState& s, cudaStream_t st) {
   });
 }
 
-void launch_mac_rhs_box(const DevState& s, cudaStream_t st) {
+void launch_mac_rhs_box(const DevState& s, cudaStream_t st, double* sumsq) {
   DOB_VEL_DISPATCH(s.prec, {
     k_rhs_box<VS, kRhsZ><<<col_grid<kRhsZ>(s.g), dim3(32, 8), 0, st>>>(s.g, (const VS*)s.u, (const VS*)s.v, (const VS*)s.w,
                                                          s.rhs);
   });
   launch_sum(s.rhs, s.g.n(), s.red + RED_RHS_SUM, s.num_sms, st);
-  launch_sub_mean(s.rhs, s.g.n(), s.red + RED_RHS_SUM, s.num_sms, st);
+  launch_sub_mean(s.rhs, s.g.n(), s.red + RED_RHS_SUM, s.num_sms, st, sumsq);
 }
 
-void launch_project_center_box(const DevState& s, cudaStream_t st) {
+void launch_project_center_box(const DevState& s, cudaStream_t st, float scale, unsigned int* maxbits) {
   DOB_VEL_DISPATCH(s.prec, {
     k_project_center_box<VS, kProjectZ><<<col_grid<kProjectZ>(s.g), dim3(32, 8), 0, st>>>(
         s.g, (const VS*)s.u, (const VS*)s.v, (const VS*)s.w, s.p, s.plo, (VS*)s.u2, (VS*)s.v2, (VS*)s.w2,
-        (typename Vec4Of<VS>::type*)s.cen);
+        (typename Vec4Of<VS>::type*)s.cen, scale, maxbits);
   });
 }
 

@@ -627,21 +627,34 @@ __global__ void k_sumsq64(const float* __restrict__ a, size_t n, double* __restr
   }
   block_sum_atomic((double)hi + (double)lo, out);
 }
-// a[i] -= mean, with the mean summed in FP64 and applied in FP32.
-__global__ void k_sub_mean(float* __restrict__ a, size_t n, const double* __restrict__ sum) {
+// a[i] -= mean, with the mean summed in FP64 and applied in FP32; sumsq
+// (statistics): also the sum of squares of the result, accumulated as
+// k_sumsq64 does (no separate pass over the array).
+__global__ void k_sub_mean(float* __restrict__ a, size_t n, const double* __restrict__ sum,
+                           double* __restrict__ sumsq) {
   __shared__ float s_mean;
   if (threadIdx.x == 0) s_mean = (float)(*sum / (double)n);
   __syncthreads();
   const float mean = s_mean;
   const size_t n4 = n >> 2;
   float4* a4 = reinterpret_cast<float4*>(a);
+  float hi = 0.0f, lo = 0.0f;
+  auto acc = [&](float v) {
+    const float sq = v * v;
+    two_sum_acc(hi, lo, sq);
+    lo += fmaf(v, v, -sq);
+  };
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n4; i += (size_t)gridDim.x * blockDim.x) {
     float4 v = a4[i];
     v.x = v.x - mean; v.y = v.y - mean; v.z = v.z - mean; v.w = v.w - mean;
     a4[i] = v;
+    if (sumsq) { acc(v.x); acc(v.y); acc(v.z); acc(v.w); }
   }
-  for (size_t i = 4 * n4 + blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+  for (size_t i = 4 * n4 + blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     a[i] = a[i] - mean;
+    if (sumsq) acc(a[i]);
+  }
+  if (sumsq) block_sum_atomic((double)hi + (double)lo, sumsq);
 }
 
 // ---- mixed precision: double-float pressure --------------------------------------------
@@ -983,8 +996,8 @@ void launch_sum(const float* a, size_t n, double* out, int num_sms, cudaStream_t
   cudaMemsetAsync(out, 0, sizeof(double), st);
   k_sum64<<<num_sms * 4, 256, 0, st>>>(a, n, out);
 }
-void launch_sub_mean(float* a, size_t n, const double* sum, int num_sms, cudaStream_t st) {
-  k_sub_mean<<<num_sms * 4, 256, 0, st>>>(a, n, sum);
+void launch_sub_mean(float* a, size_t n, const double* sum, int num_sms, cudaStream_t st, double* sumsq) {
+  k_sub_mean<<<num_sms * 4, 256, 0, st>>>(a, n, sum, sumsq);
 }
 void launch_sumsq(const float* a, size_t n, double* out, int num_sms, cudaStream_t st) {
   k_sumsq64<<<num_sms * 4, 256, 0, st>>>(a, n, out);
