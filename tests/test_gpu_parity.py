@@ -341,6 +341,40 @@ def test_box48_scene_parity_and_divergence(oracle_mod, gpu_lib):
     assert st["max_div"] <= 1e-5, st
 
 
+def test_step_statistics_match_fields(gpu_lib):
+    """The closed-box step forms max |div u| dt/dx inside the projection
+    kernel and ||rhs|| inside the mean removal: both equal the same
+    quantities formed from the fields it leaves (the divergence with the
+    same float32 operations, so exactly; the norm to FP64 summation order),
+    with and without the captured graph."""
+    abi = _abi()
+    from dropfluid import DropFluid, scenes
+    sc = scenes.box48()
+    c = sc.config
+    g = DropFluid(c)
+    sc.release(g, 0)
+    g.step(3)
+    for graph in (True, False):
+        st = g.step(1, stats=True, graph=graph)
+        u = g.get_field(abi.FIELD_VEL_U).reshape(c.nz, c.ny, c.nx)
+        v = g.get_field(abi.FIELD_VEL_V).reshape(c.nz, c.ny, c.nx)
+        w = g.get_field(abi.FIELD_VEL_W).reshape(c.nz, c.ny, c.nx)
+        f32 = np.float32
+        uR = u.copy(); uR[:, :, -1] = 0
+        vU = v.copy(); vU[:, -1, :] = 0
+        wF = w.copy(); wF[-1, :, :] = 0
+        uL = np.zeros_like(u); uL[:, :, 1:] = uR[:, :, :-1]
+        vD = np.zeros_like(v); vD[:, 1:, :] = vU[:, :-1, :]
+        wB = np.zeros_like(w); wB[1:, :, :] = wF[:-1, :, :]
+        d = ((uR - uL) + (vU - vD)) + (wF - wB)
+        assert d.dtype == f32
+        md = float(np.max(np.abs(d) * (f32(c.dt) / f32(c.dx))))
+        assert np.float32(st["max_div"]) == np.float32(md), (graph, st["max_div"], md)
+        rhs = g.get_field(abi.FIELD_RHS).astype(np.float64)
+        assert abs(st["rhs_l2"] - np.sqrt(np.sum(rhs * rhs))) <= 1e-9 * st["rhs_l2"], (graph, st["rhs_l2"])
+    g.close()
+
+
 def test_reference_mode_steps_parity(oracle_mod, gpu_lib):
     """Reference setup (Dirichlet free-surface top, drops, parcels, 2x dye),
     8 substeps at a reduced grid: relative L2 <= 1e-4 against the oracle."""
