@@ -268,9 +268,11 @@ __device__ __forceinline__ float drop(const StepParams& P, int d, int k) { retur
 // dims, displacement / domain size), which are then added to or subtracted
 // from a coordinate of at least 1e-3: there a subnormal quotient (which may
 // differ in its last place) and -0/d (which gives +0) leave the result
-// unchanged, so the coordinates equal the IEEE division's; and for the
+// unchanged, so the coordinates equal the IEEE division's; for the
 // adjoints of those displacements, where the two cases change nothing
-// above 2^-126.
+// above 2^-126; and for the Casson coefficients (a shear rate / 2 dx and
+// nu dt / dx^2: non-negative numerators, zero or normal), where the theorem
+// gives the IEEE quotient itself.
 struct Recip3 {
   dob_v3 d, r;
 };

@@ -34,6 +34,10 @@ __global__ void __launch_bounds__(256) k_casson_box(Grid g, const StepParams* __
   const StepParams& P = *Pp;
   const float dtv = P.dt, dxv = P.dx;
   const float sqrtMu = dob_sqrt(P.mu_p);
+  // the two divisions by launch constants, correctly rounded from their
+  // reciprocals (div_by: the IEEE quotients, so the general kernel's bits)
+  const float twoDx = 2.0f * dxv, dx2 = dxv * dxv;
+  const float rTwoDx = 1.0f / twoDx, rDx2 = 1.0f / dx2;
   const int dym = c.y > 0 ? -(int)c.sy : 0, dyp = c.y < g.ny - 1 ? (int)c.sy : 0;
   uint32_t i = c.i;
   dob_v3 mZn = ld3(u, v, w, c.z0 > 0 ? i - c.sz : i);
@@ -47,10 +51,10 @@ __global__ void __launch_bounds__(256) k_casson_box(Grid g, const StepParams* __
     const dob_v3 lapMac = (mXp + mXn + mYp + mYn + mZp + mZn) - 6.0f * mac;
     const float cval = ldf(dye + i);
     const float cc = dob_clampf(cval, 0.0f, 1.5f);
-    const float gdot = dob_sqrt(dot3(du, du) + dot3(dv, dv) + dot3(dw, dw)) / (2.0f * dxv);
+    const float gdot = div_by(dob_sqrt(dot3(du, du) + dot3(dv, dv) + dot3(dw, dw)), twoDx, rTwoDx);
     const float sqrtYield = dob_sqrt(P.tau_y * cc * cc / (gdot + 0.4f));
     const float nu = (sqrtMu + sqrtYield) * (sqrtMu + sqrtYield);
-    const float alpha = dob_minf(nu * dtv / (dxv * dxv), 0.125f);
+    const float alpha = dob_minf(div_by(nu * dtv, dx2, rDx2), 0.125f);
     dob_v3 out = mac + alpha * lapMac;
     if (c.x >= g.nx - 1) out.x = 0.0f;
     if (z >= g.nz - 1) out.z = 0.0f;
