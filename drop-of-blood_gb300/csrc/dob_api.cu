@@ -1012,7 +1012,7 @@ dob_status dob_load_state(dob_ctx* ctx, int slot) {
 }
 
 dob_status dob_eval_math(int fn, const float* x, const float* y, float* out, uint32_t n) {
-  if (!x || !out || fn < 0 || fn > 8 || (fn == 4 || fn == 5) && !y) return DOB_EINVAL;
+  if (!x || !out || fn < 0 || fn > 9 || (fn == 4 || fn == 5 || fn == 9) && !y) return DOB_EINVAL;
   if (n == 0) return DOB_OK;
   cudaError_t e = eval_math_device(fn, x, y, out, n);
   if (e != cudaSuccess) return fail(nullptr, DOB_ECUDA, "dob_eval_math", cudaGetErrorString(e));

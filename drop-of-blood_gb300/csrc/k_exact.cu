@@ -502,6 +502,7 @@ __global__ void k_eval_math(int fn, const float* __restrict__ x, const float* __
     case 6: r = dob_tanh(a); break;
     case 7: r = __half2float(__float2half_rn(a)); break;
     case 8: r = __bfloat162float(__float2bfloat16_rn(a)); break;
+    case 9: r = div_by(a, b, 1.0f / b); break;
     default: break;
   }
   out[i] = r;

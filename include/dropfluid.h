@@ -372,7 +372,9 @@ dob_status dob_adjoint_sphere_soft(dob_ctx* ctx, const float center[3], float ra
 /* Evaluate the library's own elementary functions on the device (used to
    check them against the host build bit for bit).  fn: 0 sin, 1 cos, 2 exp,
    3 log, 4 pow(x,y), 5 atan2(x,y), 6 tanh, 7 f32->f16->f32 round trip,
-   8 f32->bf16->f32 round trip. */
+   8 f32->bf16->f32 round trip, 9 x / y as the kernels divide by a launch
+   constant (the correctly rounded reciprocal and one remainder correction:
+   the IEEE quotient). */
 dob_status dob_eval_math(int fn, const float* x, const float* y, float* out, uint32_t n);
 
 /* ---- pressure solve without allocation (no counterpart in the reference) --

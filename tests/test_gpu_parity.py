@@ -133,6 +133,24 @@ def test_eval_math_bit_exact(oracle_mod, gpu_lib):
     assert bits_equal(eval_math(5, a, b), oracle_mod.eval_math(5, a, b))
 
 
+def test_division_by_launch_constants_is_ieee(gpu_lib):
+    """The kernels divide by launch constants (grid dims, domain size, 2 dx,
+    dx^2) through the correctly rounded reciprocal and one exact remainder
+    correction: every quotient equals the IEEE float32 division, over
+    dividends across many binades and both signs."""
+    from dropfluid import eval_math
+    rng = np.random.default_rng(11)
+    n = 1 << 20
+    a = (rng.uniform(1.0, 2.0, n) * np.exp2(rng.integers(-40, 13, n))).astype(np.float32)
+    a[::2] *= -1
+    a[:4] = [0.0, 1.0, 0.5, 191.5]
+    for d in (192.0, 256.0, 96.0, 128.0, 48.0, 64.0, 24.0, 12.0, 2.0, 1.0, 3.0, 0.02, 7.0, 1.7, 0.3):
+        y = np.full(n, d, np.float32)
+        want = a / y
+        assert want.dtype == np.float32
+        assert bits_equal(eval_math(9, a, y), want), d
+
+
 def test_binary16_store_matches_host_rounding(oracle_mod, gpu_lib):
     """__float2half_rn on the device == the host IEEE RNE restatement,
     including subnormals, ties and overflow."""
