@@ -191,6 +191,35 @@ def cpu_baseline(scene_fn, steps, threads):
     return steps / dt, dt
 
 
+def wave_leg(peak):
+    """The 512x512 wave solver (wave.ts:55-388) on a reference-mode context
+    made with DOB_PHYS_WAVE, one drop at the surface: device time of one
+    substep (its four kernels) over 50 launches after 5 warm-up ones, with
+    88 algorithmic bytes per texel.  Errors are reported in the line, not
+    raised, so the headline number never depends on this leg."""
+    try:
+        from dropfluid import DropFluid, abi, uniforms as U
+        c = abi.config_reference()
+        c.nx, c.ny, c.nz = 32, 48, 32
+        c.mg_levels = 3
+        c.parcel_capacity = 4096
+        c.physics_flags = abi.DOB_PHYS_REFERENCE_ALL | abi.DOB_PHYS_WAVE
+        e = DropFluid(c)
+        snap = U.DropSnapshot(sim_time=0.4, active_count=1)
+        snap.slots[0] = U.DropSlot(active=True, center=(0.03, 0.285, -0.02), radius=0.05, vel_y=-0.3,
+                                   oscillation=0.01, vol_drain_rate=0.42, seed=1.5)
+        e.set_uniforms(U.SimUniformPacker().pack(drops=snap, dt=1.0 / 60.0, global_seed=1.5).copy())
+        e.reset()
+        e.bench_kernel(1, reps=5)
+        ms, nbytes = e.bench_kernel(1, reps=50)
+        gbs = nbytes / (ms * 1e-3) / 1e9
+        return {"us_per_substep": ms * 1e3, "bytes_per_substep": nbytes, "achieved_gbs": gbs,
+                "frac_of_measured_hbm": gbs / peak, "kernels": 4,
+                "note": "2 MB complex spectrum, L2-resident; one substep per step, timed alone"}
+    except Exception as ex:  # reported, never fatal
+        return {"error": f"{type(ex).__name__}: {ex}"}
+
+
 def adjoint_leg(fd_dirs: int = 16):
     """Forward/backward pair of the discrete adjoint.
 
@@ -637,6 +666,8 @@ def main():
                "sample": f"3 steps of box192 (FP32 oracle, OpenMP on {threads} threads) after drop 0 "
                          f"and 1 warm-up step: {csecs:.1f} s"}
 
+    wave = wave_leg(measured_peaks()[0]) if rank == 0 else None
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
@@ -656,6 +687,7 @@ def main():
             "mixed": mixed,
             "adjoint_forward_ratio": adj["box96"]["ratio"] if adj else None,
             "adjoint": adj,
+            "wave": wave,
             "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "path": "DropFluid.run_pipelined (dob_step_async + dob_step_result, 2 steps in flight): "
                             "params host->device from pinned memory, step graph with statistics, statistics "

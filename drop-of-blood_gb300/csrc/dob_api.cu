@@ -204,6 +204,9 @@ static const int kStepOrder[] = {
 
 static void enqueue_step_body(dob_ctx* ctx, DevState& s, cudaStream_t st, float* stage_ms, bool stats_div) {
   const int n = (int)(sizeof(kStepOrder) / sizeof(kStepOrder[0]));
+  // the wave substep comes first and the advection reads its result
+  // (BloodDropEngine.ts:1886-1912)
+  if (s.flags & DOB_PHYS_WAVE) launch_wave_step(s, st);
   for (int k = 0; k < n; ++k) {
     const int stage = kStepOrder[k];
     if (stage == DOB_STAGE_CURL && !(s.ref && (s.flags & DOB_PHYS_VORT_CONF))) continue;
@@ -495,6 +498,10 @@ dob_status dob_create(const dob_config* cfg, dob_ctx** out) {
   if (!s.ref) A(&s.lim, Nc * 2 * dsb);
   A((void**)&s.splatI, Nc * 4); A((void**)&s.splatL, Nc * 4);
   A((void**)&s.wave, (size_t)kWaveN * kWaveN * 16);
+  if (s.flags & DOB_PHYS_WAVE) {
+    A((void**)&s.wspec, (size_t)kWaveN * kWaveN * 8);
+    A((void**)&s.wfilm, (size_t)kWaveN * kWaveN * 4);
+  }
   A((void**)&s.parcels, (size_t)s.cap * 32);
   A((void**)&s.red, RED_COUNT * sizeof(double));
   A((void**)&s.redu, REDU_COUNT * sizeof(unsigned int));
@@ -899,6 +906,18 @@ dob_status dob_run_stage(dob_ctx* ctx, int stage) {
   return DOB_OK;
 }
 
+dob_status dob_wave_step(dob_ctx* ctx) {
+  if (!ctx) return DOB_EINVAL;
+  if (!(ctx->s.flags & DOB_PHYS_WAVE))
+    return fail(ctx, DOB_ESTATE, "dob_wave_step", "context created without DOB_PHYS_WAVE (reference mode)");
+  dob_status st = upload_params(ctx, 0u);
+  if (st != DOB_OK) return st;
+  launch_wave_step(ctx->s, ctx->stream);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  return DOB_OK;
+}
+
 dob_status dob_sync(dob_ctx* ctx) {
   if (!ctx) return DOB_EINVAL;
   CK(cudaStreamSynchronize(ctx->stream));
@@ -945,12 +964,26 @@ dob_status dob_time_steps(dob_ctx* ctx, int nsteps, uint32_t flags, float* ms) {
 }
 
 dob_status dob_bench_kernel(dob_ctx* ctx, int which, int reps, float* avg_ms, double* bytes_per_launch) {
-  if (!ctx || !avg_ms || reps < 1 || which != 0) return DOB_EINVAL;
+  if (!ctx || !avg_ms || reps < 1 || which < 0 || which > 1) return DOB_EINVAL;
+  if (which == 1) {
+    if (!(ctx->s.flags & DOB_PHYS_WAVE))
+      return fail(ctx, DOB_ESTATE, "dob_bench_kernel", "context created without DOB_PHYS_WAVE");
+    dob_status st = upload_params(ctx, 0u);
+    if (st != DOB_OK) return st;
+  }
   CK(cudaStreamSynchronize(ctx->stream));
   double total = 0.0, bytes = 0.0;
   for (int r = 0; r < reps; ++r) {
     CK(cudaEventRecord(ctx->ev0, ctx->stream));
-    bytes = smoother_pass(ctx->s, ctx->stream);
+    if (which == 0) {
+      bytes = smoother_pass(ctx->s, ctx->stream);
+    } else {
+      // the wave substep: wave 16 B in, film 4 + spectrum 8 B out (force +
+      // row FFT); spectrum 8 in + 8 out twice (columns, inverse rows);
+      // spectrum 8 + film 4 in, wave 16 out (finalize): 88 B per texel
+      launch_wave_step(ctx->s, ctx->stream);
+      bytes = 88.0 * kWaveN * kWaveN;
+    }
     CK(cudaEventRecord(ctx->ev1, ctx->stream));
     CK(cudaEventSynchronize(ctx->ev1));
     float ms = 0.0f;
@@ -968,9 +1001,11 @@ dob_status dob_save_state(dob_ctx* ctx, int slot) {
   const size_t N = s.g.n(), Nc = s.gc.n();
   const size_t vsb = vs_bytes(s.prec), dsb = ds_bytes(s.prec);
   const int nch = s.ref ? 4 : 1;
-  void* src[] = {s.u, s.v, s.w, s.cen, s.curl, s.p, s.conc, s.parcels, s.plo};
+  // the wave field is state only when the wave solver advances it
+  void* src[] = {s.u, s.v, s.w, s.cen, s.curl, s.p, s.conc, s.parcels, s.plo, s.wave};
   const size_t sz[] = {N * vsb, N * vsb, N * vsb, N * 4 * vsb, s.curl ? N * 4 * vsb : 0, N * 4, Nc * nch * dsb,
-                       (size_t)s.cap * 32, s.plo ? N * 4 : 0};
+                       (size_t)s.cap * 32, s.plo ? N * 4 : 0,
+                       (s.flags & DOB_PHYS_WAVE) ? (size_t)kWaveN * kWaveN * 16 : 0};
   Snapshot& sn = ctx->snaps[slot];
   if (!sn.valid) {
     for (size_t k = 0; k < sizeof(sz) / sizeof(sz[0]); ++k) {
@@ -1001,7 +1036,7 @@ dob_status dob_load_state(dob_ctx* ctx, int slot) {
   Snapshot& sn = ctx->snaps[slot];
   if (!sn.valid) return fail(ctx, DOB_ESTATE, "dob_load_state", "empty snapshot slot");
   DevState& s = ctx->s;
-  void* dst[] = {s.u, s.v, s.w, s.cen, s.curl, s.p, s.conc, s.parcels, s.plo};
+  void* dst[] = {s.u, s.v, s.w, s.cen, s.curl, s.p, s.conc, s.parcels, s.plo, s.wave};
   for (size_t k = 0; k < sn.bufs.size(); ++k)
     if (sn.sizes[k]) CK(cudaMemcpyAsync(dst[k], sn.bufs[k], sn.sizes[k], cudaMemcpyDeviceToDevice, ctx->stream));
   ctx->high_water = sn.high_water;

@@ -49,6 +49,8 @@ struct DevState {
   void* lim;                     // closed box: the predictor's tap minimum and maximum (2 x DS per cell)
   uint32_t *splatI, *splatL;
   float4* wave;
+  float2* wspec;                 // wave solver (DOB_PHYS_WAVE): 512x512 complex spectra
+  float* wfilm;                  // wave solver: the force pass's surfactant film
   float* parcels;
   uint32_t cap;
   double* red;                   // FP64 reduction slots
@@ -208,6 +210,8 @@ void launch_curl(const DevState& s, cudaStream_t st);
 void launch_casson(const DevState& s, cudaStream_t st);
 void launch_mac_rhs(const DevState& s, cudaStream_t st);
 void launch_project(const DevState& s, cudaStream_t st);
+// ---- the 512x512 wave solver (k_wave.cu) -------------------------------------------------
+void launch_wave_step(const DevState& s, cudaStream_t st);
 // ---- closed-box column kernels of the step graph (k_box.cu) ------------------------------
 // Same results as launch_casson / launch_mac_rhs / launch_project followed by
 // launch_mac_to_center.  Casson needs dye on the velocity grid.

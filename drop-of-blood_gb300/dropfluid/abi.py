@@ -37,6 +37,7 @@ DOB_PHYS_NECK = 8
 DOB_PHYS_SOLENOIDAL = 16
 DOB_PHYS_SURFACE = 32
 DOB_PHYS_REFERENCE_ALL = 63
+DOB_PHYS_WAVE = 64
 
 # dob_field
 FIELD_VEL_U = 0

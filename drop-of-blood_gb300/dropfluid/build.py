@@ -1,8 +1,9 @@
 """In-tree build of libdropfluid.so for sm_103a (nvcc only, no cmake).
 
 Each kernel family is one translation unit, compiled in parallel; the
-parcel/injection unit (k_exact.cu) is compiled without multiply-add
-contraction so its arithmetic can be reproduced bit for bit on the host.
+parcel/injection unit (k_exact.cu) and the wave solver (k_wave.cu) are
+compiled without multiply-add contraction so their arithmetic can be
+reproduced bit for bit on the host.
 """
 from __future__ import annotations
 
@@ -26,6 +27,7 @@ UNITS = {
     "k_box.cu": [],
     "k_mg.cu": [],
     "k_exact.cu": ["-fmad=false"],
+    "k_wave.cu": ["-fmad=false"],
     "dob_noalloc.cu": [],
     "dob_tape.cu": [],
     "k_adjoint.cu": [],

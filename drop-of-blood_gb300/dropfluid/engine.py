@@ -169,6 +169,10 @@ class DropFluid:
     def run_stage(self, stage):
         self._ck(self._L.dob_run_stage(self._h, int(stage)), f"dob_run_stage({stage})")
 
+    def wave_step(self):
+        """One substep of the 512x512 wave solver (contexts made with DOB_PHYS_WAVE)."""
+        self._ck(self._L.dob_wave_step(self._h), "dob_wave_step")
+
     def sync(self):
         self._ck(self._L.dob_sync(self._h), "dob_sync")
 

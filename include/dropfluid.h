@@ -71,7 +71,10 @@ enum {
   DOB_PHYS_NECK = 8,           /* drop-neck momentum blend (fluid.ts:198-285)         */
   DOB_PHYS_SOLENOIDAL = 16,    /* deep-column solenoidal forcing (fluid.ts:488-503)   */
   DOB_PHYS_SURFACE = 32,       /* Marangoni + kinematic top layers (fluid.ts:287-310) */
-  DOB_PHYS_REFERENCE_ALL = 63
+  DOB_PHYS_REFERENCE_ALL = 63,
+  DOB_PHYS_WAVE = 64           /* run the 512x512 wave solver (wave.ts:55-388) at the start
+                                  of every step, before the advection (BloodDropEngine.ts:
+                                  1886-1912); without it the wave field is an input      */
 };
 
 /* Step configuration (plain data, versioned by struct_size). */
@@ -285,6 +288,13 @@ dob_status dob_step_uniforms(dob_ctx* ctx, const float* blocks, int nsteps,
 
 /* Run exactly one stage of the step on the current state (parity tests). */
 dob_status dob_run_stage(dob_ctx* ctx, int stage);
+/* One substep of the 512x512 gravity-capillary wave solver on the wave field
+   (DOB_FIELD_WAVE), from the current uniforms and v faces: replaces the
+   seven wave passes of encodePhysicsStep (wave.ts:55-388,
+   BloodDropEngine.ts:1886-1912).  dob_step runs it at the start of every
+   step when the context was created with DOB_PHYS_WAVE in reference mode;
+   DOB_ESTATE otherwise. */
+dob_status dob_wave_step(dob_ctx* ctx);
 
 /* Device time of nsteps steps (dob_step with `flags`; with DOB_STEP_STATS
    the statistics kernels run but nothing is read back), measured with CUDA
@@ -293,7 +303,8 @@ dob_status dob_run_stage(dob_ctx* ctx, int stage);
 dob_status dob_time_steps(dob_ctx* ctx, int nsteps, uint32_t flags, float* ms);
 
 /* Kernel micro-benchmark on the current state: launches the step's dominant
-   kernel (which = 0: the level-0 pressure smoother pass) `reps` times with
+   kernel (which = 0: the level-0 pressure smoother pass; which = 1: one
+   wave substep, its four kernels, on a context made with DOB_PHYS_WAVE) `reps` times with
    CUDA events around each launch; returns the mean device ms per launch and
    the kernel's algorithmic bytes per launch (minimum HBM traffic of one
    pass).  No counterpart in the reference. */

@@ -1686,6 +1686,7 @@ template <class R> class Sim {
       const uint64_t hw = (uint64_t)highWater + spawn_count();
       highWater = (uint32_t)(hw < cap ? hw : cap);
     }
+    if (flag(DOB_PHYS_WAVE)) wave_step();  // BloodDropEngine.ts:1886-1912, before the advection
     advect_mac();
     mac_to_center();
     if (flag(DOB_PHYS_VORT_CONF)) curl_stage();
@@ -1708,6 +1709,7 @@ template <class R> class Sim {
   }
 
 #include "dob_oracle_adjoint.inc"
+#include "dob_oracle_wave.inc"
 };
 
 struct AnySim {
@@ -2017,6 +2019,23 @@ void orc_set_threads(int n) {
 }
 int orc_get_threads(void) { return omp_get_max_threads(); }
 
+// The wave substep on the simulation's wave field (wave.ts:55-388).
+int orc_wave_step(orc_sim* s) {
+  if (s->a.f64) s->a.sd->wave_step(); else s->a.sf->wave_step();
+  return DOB_OK;
+}
+// Unitary 2-D transform of a 512x512 complex field (interleaved re, im; x
+// fastest) by the wave passes: rows then columns forward, columns then rows
+// inverse.
+int orc_wave_fft2(float* data, int inverse) {
+  if (!data) return DOB_EINVAL;
+  const size_t n = (size_t)2 * kWaveN * kWaveN;
+  std::vector<float> a(data, data + n), b(n);
+  if (!inverse) { Sim<float>::wave_fft_lines(a, 2, b, true, false); Sim<float>::wave_fft_lines(b, 2, a, false, false); }
+  else { Sim<float>::wave_fft_lines(a, 2, b, false, true); Sim<float>::wave_fft_lines(b, 2, a, true, true); }
+  memcpy(data, a.data(), n * sizeof(float));
+  return DOB_OK;
+}
 int orc_adjoint_stage(orc_sim* s, int stage) { return DISPATCH(s, adjoint_stage(stage)); }
 int orc_tape_forward(orc_sim* s, int nsteps) { return DISPATCH(s, tape_forward(nsteps)); }
 int orc_tape_backward(orc_sim* s, const float* dye_grad, size_t bytes) {

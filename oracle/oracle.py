@@ -64,6 +64,8 @@ def lib():
         L.orc_set_threads.argtypes = [C.c_int]
         L.orc_get_threads.restype = C.c_int
         L.orc_adjoint_stage.argtypes = [P, C.c_int]
+        L.orc_wave_step.argtypes = [P]
+        L.orc_wave_fft2.argtypes = [C.POINTER(C.c_float), C.c_int]
         L.orc_tape_forward.argtypes = [P, C.c_int]
         L.orc_tape_backward.argtypes = [P, C.POINTER(C.c_float), C.c_size_t]
         L.orc_sphere_impulse.argtypes = [P, C.POINTER(C.c_float), C.c_float, C.POINTER(C.c_float),
@@ -93,6 +95,15 @@ def set_threads(n: int):
 
 def get_threads() -> int:
     return int(lib().orc_get_threads())
+
+
+def wave_fft2(z: np.ndarray, inverse: bool = False) -> np.ndarray:
+    """Unitary 2-D transform of a 512x512 complex64 array by the wave passes."""
+    a = np.ascontiguousarray(np.asarray(z, np.complex64)).copy()
+    assert a.shape == (512, 512)
+    f = a.view(np.float32)
+    _check(lib().orc_wave_fft2(_fptr(f), int(bool(inverse))), "wave_fft2")
+    return a
 
 
 def eval_math(fn: int, x, y=None) -> np.ndarray:
@@ -199,6 +210,10 @@ class OracleSim:
 
     def run_stage(self, stage):
         _check(lib().orc_run_stage(self._h, int(stage)), f"run_stage({stage})")
+
+    def wave_step(self):
+        """One substep of the 512x512 wave solver on the wave field."""
+        _check(lib().orc_wave_step(self._h), "wave_step")
 
     # -- discrete adjoint (closed box, dye_refine 1) ---------------------------------------
     def adjoint_stage(self, stage):
