@@ -26,7 +26,13 @@
 //   * the first call on each device does a one-time set-up with that device
 //     current: it looks up the array's device address with
 //     cudaGetSymbolAddress and raises the coarse-grid kernel's shared-memory
-//     limit.  Make that first call before any stream capture.
+//     limit.  Make that first call before any stream capture;
+//   * with an exact coarsest solve (mg_coarse_sweeps = -1), a call whose
+//     coarsest grid differs from the one the array's inverse was made for
+//     (its dims, the boundary mode, or its spacing, i.e. the number of
+//     coarsenings) recomputes that inverse on the host and uploads it,
+//     waiting for the caller's stream to drain; such a call blocks the host
+//     and must not be made during stream capture.
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string.h>
@@ -71,8 +77,12 @@ constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
 void* g_scratch_ptr[kMaxDevices] = {};
 int g_num_sms[kMaxDevices] = {};
-// which coarsest-grid inverse each device's array holds (nx, ny, nz, ref)
-int g_inv_key[kMaxDevices][4] = {};
+// Which coarsest-grid inverse each device's array holds: the grid's dims, the
+// boundary mode and the bits of the level's h^2 (the inverse is scaled by it,
+// and h^2 depends on how many coarsenings lead to the grid: 48x64x48 with 3
+// grids and 96x128x96 with 4 both end at 12x16x12, with h^2 16 and 64).
+constexpr int kInvKey = 5;
+int g_inv_key[kMaxDevices][kInvKey] = {};
 
 size_t round_up(size_t b) { return (b + kAlign - 1) / kAlign * kAlign; }
 
@@ -188,15 +198,19 @@ extern "C" dob_status dob_pressure_solve_noalloc(const dob_config* cfg, const fl
     L.b = take(L.d.n());
   }
   if (cfg->mg_coarse_sweeps < 0) {
-    // the coarsest grid's inverse sits at the end of the array; it is
-    // recomputed on the host only when the grid differs from the last call's
+    // The coarsest grid's inverse sits at the end of the array.  It is
+    // recomputed on the host and uploaded only when its key (dims, boundary
+    // mode, h^2) differs from the one the array holds; that upload waits for
+    // the caller's stream (see the header).
     const MgLevel& C = s.lv[s.nlev - 1];
     float* inv = reinterpret_cast<float*>(cur + kScratchBytes - kDenseBytes);
-    const int key[4] = {C.d.nx, C.d.ny, C.d.nz, s.ref};
+    int h2_bits = 0;
+    memcpy(&h2_bits, &C.h2, sizeof(h2_bits));
+    const int key[kInvKey] = {C.d.nx, C.d.ny, C.d.nz, s.ref, h2_bits};
     bool same = true;
     {
       std::lock_guard<std::mutex> lock(g_setup_mutex);
-      for (int k = 0; k < 4; ++k) same = same && g_inv_key[device][k] == key[k];
+      for (int k = 0; k < kInvKey; ++k) same = same && g_inv_key[device][k] == key[k];
     }
     if (!same) {
       const std::vector<float> h = coarse_inverse(C.d, C.h2, s.ref);
@@ -205,7 +219,7 @@ extern "C" dob_status dob_pressure_solve_noalloc(const dob_config* cfg, const fl
       if (e == cudaSuccess) e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
       if (e != cudaSuccess) return cuda_fail("coarse inverse upload", e);
       std::lock_guard<std::mutex> lock(g_setup_mutex);
-      for (int k = 0; k < 4; ++k) g_inv_key[device][k] = key[k];
+      for (int k = 0; k < kInvKey; ++k) g_inv_key[device][k] = key[k];
     }
     s.cinv = inv;
     s.cn = (int)C.d.n();

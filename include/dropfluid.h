@@ -418,7 +418,12 @@ dob_status dob_eval_math(int fn, const float* x, const float* y, float* out, uin
    race; order them on one stream.  The first call on each device performs a
    one-time set-up with that device current (cudaGetSymbolAddress of the
    array, the coarse-grid kernel's shared-memory limit); make it before any
-   stream capture.  Errors: dob_last_error(NULL). */
+   stream capture.  With an exact coarsest solve, a call whose coarsest grid
+   differs from the previous such call's on this device (dims, bc_mode, or
+   mg_levels relative to the fine grid, which sets the coarse spacing)
+   rebuilds the grid's dense inverse on the host and uploads it into the
+   array: that call waits for `stream` to drain before it returns and must
+   not be made during stream capture.  Errors: dob_last_error(NULL). */
 dob_status dob_pressure_solve_noalloc(const dob_config* cfg, const float* rhs, float* pressure, void* stream);
 
 #ifdef __cplusplus

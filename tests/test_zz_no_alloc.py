@@ -109,6 +109,27 @@ def test_noalloc_smaller_grid_after_larger(gpu_lib):
         assert rel_l2(_noalloc_solve(gpu_lib, torch, small, rhs, p0), _context_solve(small, rhs, p0)) < STAGE_TOL
 
 
+@pytest.mark.gpu
+@pytest.mark.parametrize("order", [((96, 128, 96), (48, 64, 48)), ((48, 64, 48), (96, 128, 96))])
+def test_noalloc_same_coarsest_grid_other_spacing(gpu_lib, order):
+    """48x64x48 with 3 grids and 96x128x96 with 4 both end at a 12x16x12
+    coarsest grid, solved exactly with a dense inverse scaled by the level's
+    h^2 (16 and 64).  Called one after the other, in either order, each call
+    must use the inverse of its own hierarchy, not the one the previous call
+    left in the shared array."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    for k, dims in enumerate(order * 2):
+        cfg = _config("box", dims)
+        assert cfg.mg_coarse_sweeps == -1
+        assert [d >> (cfg.mg_levels - 1) for d in dims] == [12, 16, 12]
+        rhs = _rhs(cfg, 31 + k)
+        p0 = np.zeros(rhs.shape, np.float32)
+        err = rel_l2(_noalloc_solve(gpu_lib, torch, cfg, rhs, p0), _context_solve(cfg, rhs, p0))
+        assert err < STAGE_TOL, (dims, err)
+
+
 def test_noalloc_rejects_bad_sizes_before_device_use(gpu_lib):
     """Grids beyond the fixed array's 2^21 cells and malformed requests are
     refused with DOB_EINVAL before any device call (no GPU needed)."""
