@@ -1,0 +1,231 @@
+"""Parity of the CUDA path with the oracle at the benchmark sizes.
+
+The stage-level tests run on reduced grids; these run the benchmark
+scenes themselves (through the C ABI) beside the oracle on the host cores:
+
+* box192 (192x256x192, three r=12 drops, 393216 parcels, FP32): the first
+  10 steps from the first release, against the FP32 oracle, with the FP64
+  oracle's error reported;
+* box96 (96x128x96, one r=8 drop, the adjoint scene): all 32 steps;
+* the reference's own setup (`dob_config_reference`: 96x128x96 velocity,
+  192x256x192 four-channel dye, 4 grids with the L0 1+1 / L1-L2 2+2 / L3 6
+  schedule, 393216 parcels, the wave solver each substep) driven by the
+  host drop-lifecycle sequence through the first drop's impact, in FP32
+  and with the reference's binary16 storage;
+* box192 in the mixed mode (relative residual 1e-8) against an FP64 run
+  whose pressure is converged to the FP64 floor.
+
+Fields must agree within relative L2 1e-4 (FP16-stored fields at the bound
+their rounding allows, stated per test), every projected step must hold
+max |div u| dt/dx <= 1e-5, and a full-size parcel step from the same state
+must give the same parcel bits and fixed-point splat sums.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from helpers import bits_equal, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+STEP_TOL = 1e-4
+
+
+def _abi():
+    from dropfluid import abi
+    return abi
+
+
+@pytest.fixture(scope="module")
+def oracle_all_cores(oracle_mod):
+    oracle_mod.set_threads(os.cpu_count() or 1)
+    return oracle_mod
+
+
+def _fields(abi, ref):
+    names = ["VEL_U", "VEL_V", "VEL_W", "PRESSURE", "CONC"]
+    return [(n, getattr(abi, "FIELD_" + n)) for n in names]
+
+
+def _compare(tag, g, o, o64=None, tol=STEP_TOL, tols=None):
+    abi = _abi()
+    errs = {}
+    for name, f in _fields(abi, False):
+        e = rel_l2(g.get_field(f), o.get_field(f))
+        msg = f"{tag} {name}: rel L2 vs oracle {e:.2e}"
+        if o64 is not None:
+            msg += f", vs FP64 oracle {rel_l2(g.get_field(f), o64.get_field64(f)):.2e}"
+        print(msg)
+        errs[name] = e
+    for name, e in errs.items():
+        bar = (tols or {}).get(name, tol)
+        assert e < bar, (tag, name, e, bar)
+
+
+def _parcel_step_bit_exact(g, o, n_live, stages):
+    """Load the device's velocity, dye, wave and parcels into the oracle and
+    run the parcel stages on both: same parcel bits and splat sums."""
+    abi = _abi()
+    ref = g.cfg.bc_mode == abi.DOB_BC_REFERENCE
+    move = [abi.FIELD_VEL_U, abi.FIELD_VEL_V, abi.FIELD_VEL_W, abi.FIELD_VEL_CENTER, abi.FIELD_CONC]
+    if ref:
+        move += [abi.FIELD_CURL, abi.FIELD_WAVE]
+    for f in move:
+        o.set_field(f, g.get_field(f))
+    p = g.get_parcels(n_live)
+    o.set_parcels(p, 0)
+    for e in (g, o):
+        e.set_high_water(n_live)
+        e.run_stage(abi.STAGE_CLEAR_SPLATS)
+        for s in stages:
+            e.run_stage(s)
+    gp, op = g.get_parcels(n_live), o.get_parcels(n_live)
+    assert bits_equal(gp, op), int((gp.view(np.uint32) != op.view(np.uint32)).any(axis=1).sum())
+    si = g.get_field(abi.FIELD_SPLAT_INTACT)
+    assert bits_equal(si, o.get_field(abi.FIELD_SPLAT_INTACT))
+    assert bits_equal(g.get_field(abi.FIELD_SPLAT_LYSED), o.get_field(abi.FIELD_SPLAT_LYSED))
+    assert int(si.astype(np.uint64).sum()) > 0
+    return gp
+
+
+def test_box192_fp32_first_steps(oracle_all_cores, gpu_lib):
+    """Configuration 1 at full size: steps 0-9 (drop 0 released at step 0,
+    8 V-cycles on the two steps after it, 4 afterwards)."""
+    abi = _abi()
+    from dropfluid import DropFluid, scenes
+    sc = scenes.box192()
+    g = DropFluid(sc.config)
+    o = oracle_all_cores.OracleSim(sc.config)
+    o64 = oracle_all_cores.OracleSim(sc.config, fp64=True)
+    for k in range(10):
+        for d in sc.releases_at(k):
+            for e in (g, o, o64):
+                sc.release(e, d)
+        st = g.step(1, stats=True)
+        assert st["max_div"] <= 1e-5, (k, st)
+        o.step(1)
+        o64.step(1)
+    _compare("box192 step 10", g, o, o64)
+    del o64
+    _parcel_step_bit_exact(g, o, sc.drops[0].n_parcels, [abi.STAGE_PARCEL_ADVECT])
+    g.close()
+
+
+def test_box96_all_steps(oracle_all_cores, gpu_lib):
+    """Configuration 3's scene (the adjoint case) over its 32 steps."""
+    from dropfluid import DropFluid, scenes
+    sc = scenes.box96()
+    g = DropFluid(sc.config)
+    o = oracle_all_cores.OracleSim(sc.config)
+    o64 = oracle_all_cores.OracleSim(sc.config, fp64=True)
+    for k in range(sc.steps):
+        for d in sc.releases_at(k):
+            for e in (g, o, o64):
+                sc.release(e, d)
+        st = g.step(1, stats=True)
+        assert st["max_div"] <= 1e-5, (k, st)
+        o.step(1)
+        o64.step(1)
+    _compare("box96 step 32", g, o, o64)
+    g.close()
+
+
+def _reference_run(oracle_mod, prec, warm_substeps=52, compared=8):
+    """The reference setup from a reset with seed 1: the device alone runs
+    the first `warm_substeps` substeps of the host drop-lifecycle sequence
+    (the first drop falls from the pipette height), its state is loaded into
+    the oracle, and both run the next `compared` substeps with the same
+    blocks, through the drop's impact on the meniscus (0.92 s, substep 56)
+    and its first drainage and parcel emission."""
+    abi = _abi()
+    from dropfluid import DropFluid
+    from dropfluid.sequencer import SubstepSequencer
+    cfg = abi.config_reference()
+    cfg.precision_mode = prec
+    cfg.physics_flags = abi.DOB_PHYS_REFERENCE_ALL | abi.DOB_PHYS_WAVE
+    assert (cfg.nx, cfg.ny, cfg.nz, cfg.dye_refine, cfg.mg_levels) == (96, 128, 96, 2, 4)
+    assert cfg.parcel_capacity == 393216 and cfg.reference_schedule == 1
+    seq = SubstepSequencer(seed=1.0)
+    g = DropFluid(cfg)
+    g.set_uniforms(seq.reset_simulation(1.0))
+    g.reset()
+    warm = np.stack([seq.advance_substep()[0] for _ in range(warm_substeps)])
+    g.step_uniforms(warm)
+    o = oracle_mod.OracleSim(cfg)
+    o.set_uniforms(warm[-1])
+    o.reset()
+    for f in (abi.FIELD_VEL_U, abi.FIELD_VEL_V, abi.FIELD_VEL_W, abi.FIELD_VEL_CENTER, abi.FIELD_CURL,
+              abi.FIELD_PRESSURE, abi.FIELD_CONC, abi.FIELD_WAVE):
+        o.set_field(f, g.get_field(f))
+    o.set_parcels(g.get_parcels(), 0)
+    o.set_high_water(seq.high_water)
+    g.set_high_water(seq.high_water)
+    spawned = 0
+    last = None
+    for _ in range(compared):
+        blk, spawn, _ = seq.advance_substep()
+        spawned += spawn
+        for e in (g, o):
+            e.set_uniforms(blk)
+            e.step(1)
+        last = blk
+    assert spawned > 0, "the compared window must include the drop's drainage"
+    return g, o, seq, last
+
+
+def test_reference_setup_fp32(oracle_all_cores, gpu_lib):
+    abi = _abi()
+    g, o, seq, last = _reference_run(oracle_all_cores, abi.DOB_PREC_FP32)
+    # the wave texture stores halves: a texel whose value flips one half ulp
+    # moves by 2^-11 relative once the faces it reads differ in their last bits
+    e = rel_l2(g.get_field(abi.FIELD_WAVE), o.get_field(abi.FIELD_WAVE))
+    print(f"reference fp32 WAVE: rel L2 {e:.2e}")
+    assert e < 1e-3
+    _compare("reference fp32 substep 60", g, o)
+    # one full-size parcel substep (emission + advection + splat) from the device's state
+    o.set_uniforms(last)
+    _parcel_step_bit_exact(g, o, seq.high_water, [abi.STAGE_PARCEL_EMIT, abi.STAGE_PARCEL_ADVECT])
+    g.close()
+
+
+def test_reference_setup_fp16_storage(oracle_all_cores, gpu_lib):
+    """Binary16 storage of velocity, curl and dye (rgba16float): the
+    oracle rounds every store the same way, but a store whose FP32 value
+    differs in its last bits (multiply-add contraction) can round to the
+    neighbouring half, a 2^-11 (4.9e-4) relative step; after 8 substeps the
+    binary16 fields are within 1e-3 of the oracle (measured 1.4e-4) and the
+    pressure (FP32) within 1e-4 (measured 1.3e-5)."""
+    abi = _abi()
+    g, o, seq, last = _reference_run(oracle_all_cores, abi.DOB_PREC_REFERENCE_FP16)
+    _compare("reference fp16 substep 60", g, o, tol=1e-3, tols={"PRESSURE": STEP_TOL})
+    g.close()
+
+
+def test_box192_mixed_against_fp64(oracle_all_cores, gpu_lib):
+    """Configuration 2 at full size: the mixed mode to a relative residual
+    of 1e-8 for the first 5 steps, against an FP64 run (the oracle in
+    double, 12 V-cycles per step, converged to the FP64 floor).  Velocity
+    and pressure within 1e-4; the FP16-stored dye within 1e-3 (its rounding
+    step is 2.4e-4 relative per store; measured 1.8e-4 after 5 steps)."""
+    from dropfluid import DropFluid, scenes
+    sc = scenes.box192_mixed_1e8()
+    ref = scenes.box192()
+    ref.config.mg_cycles = 12
+    ref.config.mg_cycles_injected = 12
+    g = DropFluid(sc.config)
+    o64 = oracle_all_cores.OracleSim(ref.config, fp64=True)
+    for k in range(5):
+        for d in sc.releases_at(k):
+            sc.release(g, d)
+            ref.release(o64, d)
+        st = g.step(1, stats=True)
+        assert st["max_div"] <= 1e-5, (k, st)
+        assert st["residual_l2"] <= 1.05e-8 * st["rhs_l2"], (k, st)
+        o64.step(1)
+    abi = _abi()
+    for name, f in _fields(abi, False):
+        e = rel_l2(g.get_field(f), o64.get_field64(f))
+        print(f"box192 mixed step 5 {name}: rel L2 vs FP64 {e:.2e}")
+        assert e < (1e-3 if name == "CONC" else STEP_TOL), (name, e)
+    g.close()
