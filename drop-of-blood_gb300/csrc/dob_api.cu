@@ -503,6 +503,11 @@ dob_status dob_create(const dob_config* cfg, dob_ctx** out) {
     A((void**)&s.wfilm, (size_t)kWaveN * kWaveN * 4);
   }
   A((void**)&s.parcels, (size_t)s.cap * 32);
+  if (s.ref && light_dims_ok(s.g)) {
+    A((void**)&s.light, N * sizeof(half4));
+    A((void**)&s.brick_raw, N / 64 * sizeof(float));
+    A((void**)&s.bricks, N / 64 * sizeof(float));
+  }
   A((void**)&s.red, RED_COUNT * sizeof(double));
   A((void**)&s.redu, REDU_COUNT * sizeof(unsigned int));
   s.nlev = cfg->mg_levels;
@@ -631,6 +636,8 @@ dob_status dob_reset(dob_ctx* ctx) {
   CK(cudaMemcpy(s.parcels, empty.data(), empty.size() * 4, cudaMemcpyHostToDevice));
   CK(cudaMemsetAsync(s.red, 0, RED_COUNT * sizeof(double), ctx->stream));
   CK(cudaMemsetAsync(s.redu, 0, REDU_COUNT * sizeof(unsigned int), ctx->stream));
+  // the reset's lighting passes (BloodDropEngine.ts:1760) on the cleared dye
+  if (s.light) launch_light_volume(s, ctx->stream);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(ctx->stream));
   return DOB_OK;
@@ -711,7 +718,7 @@ namespace {
 struct FieldDesc {
   void* dev;
   size_t count;     // host elements
-  int kind;         // 0: VS, 1: DS, 2: f32, 3: u32, 4: f32 red-black split
+  int kind;         // 0: VS, 1: DS, 2: f32, 3: u32, 4: f32 red-black split, 5: binary16
 };
 }  // namespace
 
@@ -731,6 +738,9 @@ static bool field_desc(dob_ctx* ctx, int field, FieldDesc* f) {
     case DOB_FIELD_SPLAT_INTACT: *f = {s.splatI, Nc, 3}; return true;
     case DOB_FIELD_SPLAT_LYSED: *f = {s.splatL, Nc, 3}; return true;
     case DOB_FIELD_WAVE: *f = {s.wave, (size_t)4 * kWaveN * kWaveN, 2}; return true;
+    case DOB_FIELD_LIGHT: *f = {s.light, 4 * N, 5}; return s.light != nullptr;
+    case DOB_FIELD_BRICKS: *f = {s.bricks, N / 64, 2}; return s.bricks != nullptr;
+    case DOB_FIELD_BRICKS_RAW: *f = {s.brick_raw, N / 64, 2}; return s.brick_raw != nullptr;
     default: break;
   }
   void* dev = nullptr;
@@ -744,7 +754,9 @@ static bool field_desc(dob_ctx* ctx, int field, FieldDesc* f) {
 dob_status dob_set_field(dob_ctx* ctx, int field, const void* host, size_t bytes) {
   if (!ctx || !host) return DOB_EINVAL;
   FieldDesc f;
-  if (!field_desc(ctx, field, &f)) return fail(ctx, DOB_EINVAL, "dob_set_field", "unknown or read-only field");
+  const bool read_only = field == DOB_FIELD_LIGHT || field == DOB_FIELD_BRICKS || field == DOB_FIELD_BRICKS_RAW;
+  if (read_only || !field_desc(ctx, field, &f))
+    return fail(ctx, DOB_EINVAL, "dob_set_field", "unknown or read-only field");
   if (bytes != f.count * 4) return fail(ctx, DOB_EINVAL, "dob_set_field", "byte count does not match the field");
   CK(cudaStreamSynchronize(ctx->stream));
   const size_t eb = f.kind == 0 ? vs_bytes(ctx->s.prec) : f.kind == 1 ? ds_bytes(ctx->s.prec) : 4;
@@ -789,7 +801,7 @@ dob_status dob_get_field(dob_ctx* ctx, int field, void* host, size_t bytes) {
   FieldDesc f;
   if (!field_desc(ctx, field, &f)) return fail(ctx, DOB_EINVAL, "dob_get_field", "unknown field");
   if (bytes != f.count * 4) return fail(ctx, DOB_EINVAL, "dob_get_field", "byte count does not match the field");
-  const size_t eb = f.kind == 0 ? vs_bytes(ctx->s.prec) : f.kind == 1 ? ds_bytes(ctx->s.prec) : 4;
+  const size_t eb = f.kind == 0 ? vs_bytes(ctx->s.prec) : f.kind == 1 ? ds_bytes(ctx->s.prec) : f.kind == 5 ? 2 : 4;
   if (f.kind == 4) {
     float* tmp = nullptr;
     CK(cudaMalloc(&tmp, bytes));
@@ -823,7 +835,9 @@ dob_status dob_get_field(dob_ctx* ctx, int field, void* host, size_t bytes) {
 }
 
 // ---- stepping ----------------------------------------------------------------------------
-dob_status dob_step(dob_ctx* ctx, int nsteps, uint32_t flags, dob_step_stats* stats) {
+// `light`: end with the lighting passes (DOB_PHYS_LIGHTING), which read the
+// last step's parameters.
+static dob_status step_impl(dob_ctx* ctx, int nsteps, uint32_t flags, dob_step_stats* stats, bool light) {
   if (!ctx || nsteps < 0) return DOB_EINVAL;
   if (ctx->cfg.bc_mode == DOB_BC_REFERENCE && !isfinite(ctx->U[38]))
     return fail(ctx, DOB_EINVAL, "dob_step", "non-finite dt");
@@ -832,6 +846,10 @@ dob_status dob_step(dob_ctx* ctx, int nsteps, uint32_t flags, dob_step_stats* st
   for (int k = 0; k < nsteps; ++k) {
     dob_status st = one_step(ctx, flags, timing ? stage_ms : nullptr);
     if (st != DOB_OK) return st;
+  }
+  if (light && nsteps > 0 && ctx->s.light && (ctx->s.flags & DOB_PHYS_LIGHTING)) {
+    launch_light_volume(ctx->s, ctx->stream);
+    CK(cudaGetLastError());
   }
   if (stats) {
     memset(stats, 0, sizeof(*stats));
@@ -846,6 +864,10 @@ dob_status dob_step(dob_ctx* ctx, int nsteps, uint32_t flags, dob_step_stats* st
     for (int k = 0; k < DOB_STAGE_COUNT; ++k) stats->stage_ms[k] = stage_ms[k];
   }
   return DOB_OK;
+}
+
+dob_status dob_step(dob_ctx* ctx, int nsteps, uint32_t flags, dob_step_stats* stats) {
+  return step_impl(ctx, nsteps, flags, stats, true);
 }
 
 dob_status dob_step_async(dob_ctx* ctx, int slot) {
@@ -887,7 +909,7 @@ dob_status dob_step_uniforms(dob_ctx* ctx, const float* blocks, int nsteps, uint
   for (int k = 0; k < nsteps; ++k) {
     dob_status st = dob_set_uniforms(ctx, blocks + (size_t)k * 128);
     if (st != DOB_OK) return st;
-    st = dob_step(ctx, 1, flags, k == nsteps - 1 ? stats : nullptr);
+    st = step_impl(ctx, 1, flags, k == nsteps - 1 ? stats : nullptr, k == nsteps - 1);
     if (st != DOB_OK) return st;
   }
   return DOB_OK;
@@ -915,6 +937,17 @@ dob_status dob_wave_step(dob_ctx* ctx) {
   launch_wave_step(ctx->s, ctx->stream);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(ctx->stream));
+  return DOB_OK;
+}
+
+dob_status dob_light_volume(dob_ctx* ctx) {
+  if (!ctx) return DOB_EINVAL;
+  if (!ctx->s.light)
+    return fail(ctx, DOB_ESTATE, "dob_light_volume", "reference mode with nx, ny, nz divisible by 4 only");
+  dob_status st = upload_params(ctx, 0u);
+  if (st != DOB_OK) return st;
+  launch_light_volume(ctx->s, ctx->stream);
+  CK(cudaGetLastError());
   return DOB_OK;
 }
 
@@ -964,10 +997,15 @@ dob_status dob_time_steps(dob_ctx* ctx, int nsteps, uint32_t flags, float* ms) {
 }
 
 dob_status dob_bench_kernel(dob_ctx* ctx, int which, int reps, float* avg_ms, double* bytes_per_launch) {
-  if (!ctx || !avg_ms || reps < 1 || which < 0 || which > 1) return DOB_EINVAL;
+  if (!ctx || !avg_ms || reps < 1 || which < 0 || which > 2) return DOB_EINVAL;
   if (which == 1) {
     if (!(ctx->s.flags & DOB_PHYS_WAVE))
       return fail(ctx, DOB_ESTATE, "dob_bench_kernel", "context created without DOB_PHYS_WAVE");
+    dob_status st = upload_params(ctx, 0u);
+    if (st != DOB_OK) return st;
+  }
+  if (which == 2) {
+    if (!ctx->s.light) return fail(ctx, DOB_ESTATE, "dob_bench_kernel", "no light volume in this mode");
     dob_status st = upload_params(ctx, 0u);
     if (st != DOB_OK) return st;
   }
@@ -977,6 +1015,14 @@ dob_status dob_bench_kernel(dob_ctx* ctx, int which, int reps, float* avg_ms, do
     CK(cudaEventRecord(ctx->ev0, ctx->stream));
     if (which == 0) {
       bytes = smoother_pass(ctx->s, ctx->stream);
+    } else if (which == 2) {
+      // light volume: the 4-channel dye read once (every dye voxel is a tap
+      // of some centre sample), the light volume written once (8 B per
+      // velocity cell), the two brick maps (4 B per 64 cells each) and the
+      // raw map read 125 times from L2, counted once
+      launch_light_volume(ctx->s, ctx->stream);
+      const size_t dsb = ctx->s.prec == DOB_PREC_FP32 ? 4 : 2;
+      bytes = (double)ctx->s.gc.n() * 4 * dsb + (double)ctx->s.g.n() * 8 + (double)ctx->s.g.n() / 64 * 12;
     } else {
       // the wave substep: wave 16 B in, film 4 + spectrum 8 B out (force +
       // row FFT); spectrum 8 in + 8 out twice (columns, inverse rows);

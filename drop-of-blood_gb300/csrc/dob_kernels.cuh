@@ -53,6 +53,10 @@ struct DevState {
   float* wfilm;                  // wave solver: the force pass's surfactant film
   float* parcels;
   uint32_t cap;
+  // light volume (reference mode, dims divisible by 4): 4 x binary16 per
+  // velocity cell, and the raw and dilated occupancy of its 4x4x4 bricks
+  half4* light;
+  float *brick_raw, *bricks;
   double* red;                   // FP64 reduction slots
   unsigned int* redu;            // u32 reduction slots / flags
   int nlev;
@@ -212,6 +216,9 @@ void launch_mac_rhs(const DevState& s, cudaStream_t st);
 void launch_project(const DevState& s, cudaStream_t st);
 // ---- the 512x512 wave solver (k_wave.cu) -------------------------------------------------
 void launch_wave_step(const DevState& s, cudaStream_t st);
+// ---- light volume and brick occupancy (k_light.cu) ------------------------------------------
+bool light_dims_ok(const Grid& g);
+void launch_light_volume(const DevState& s, cudaStream_t st);
 // ---- closed-box column kernels of the step graph (k_box.cu) ------------------------------
 // Same results as launch_casson / launch_mac_rhs / launch_project followed by
 // launch_mac_to_center.  Casson needs dye on the velocity grid.

@@ -36,6 +36,7 @@ SIGNATURES = {
     "dob_step_uniforms": (C.c_int, [P, FP, C.c_int, C.c_uint32, C.POINTER(abi.DobStepStats)]),
     "dob_run_stage": (C.c_int, [P, C.c_int]),
     "dob_wave_step": (C.c_int, [P]),
+    "dob_light_volume": (C.c_int, [P]),
     "dob_sync": (C.c_int, [P]),
     "dob_memory_bytes": (C.c_int, [P, C.POINTER(C.c_uint64)]),
     "dob_launches_per_step": (C.c_int, [P, C.POINTER(C.c_int)]),

@@ -38,6 +38,7 @@ DOB_PHYS_SOLENOIDAL = 16
 DOB_PHYS_SURFACE = 32
 DOB_PHYS_REFERENCE_ALL = 63
 DOB_PHYS_WAVE = 64
+DOB_PHYS_LIGHTING = 128
 
 # dob_field
 FIELD_VEL_U = 0
@@ -53,6 +54,9 @@ FIELD_SPLAT_INTACT = 9
 FIELD_SPLAT_LYSED = 10
 FIELD_WAVE = 11
 FIELD_DIVERGENCE = 12
+FIELD_LIGHT = 13
+FIELD_BRICKS = 14
+FIELD_BRICKS_RAW = 15
 # adjoint fields (closed box, FP32, dye_refine 1)
 FIELD_ADJ_VEL_U = 16
 FIELD_ADJ_VEL_V = 17
@@ -88,6 +92,9 @@ def field_shapes(vdims, cdims, ref):
         FIELD_SPLAT_LYSED: ((cz, cy, cx), np.uint32),
         FIELD_WAVE: ((WAVE_N, WAVE_N, 4), np.float32),
         FIELD_DIVERGENCE: v,
+        FIELD_LIGHT: ((nz, ny, nx, 4), np.float32),
+        FIELD_BRICKS: ((nz // 4, ny // 4, nx // 4), np.float32),
+        FIELD_BRICKS_RAW: ((nz // 4, ny // 4, nx // 4), np.float32),
         FIELD_ADJ_VEL_U: v, FIELD_ADJ_VEL_V: v, FIELD_ADJ_VEL_W: v,
         FIELD_ADJ_VEL_U2: v, FIELD_ADJ_VEL_V2: v, FIELD_ADJ_VEL_W2: v,
         FIELD_ADJ_CENTER: ((nz, ny, nx, 4), np.float32),

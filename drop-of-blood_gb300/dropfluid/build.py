@@ -1,8 +1,8 @@
 """In-tree build of libdropfluid.so for sm_103a (nvcc only, no cmake).
 
 Each kernel family is one translation unit, compiled in parallel; the
-parcel/injection unit (k_exact.cu) and the wave solver (k_wave.cu) are
-compiled without multiply-add contraction so their arithmetic can be
+parcel/injection unit (k_exact.cu), the wave solver (k_wave.cu) and the
+light volume (k_light.cu) are compiled without multiply-add contraction so their arithmetic can be
 reproduced bit for bit on the host.
 """
 from __future__ import annotations
@@ -28,6 +28,7 @@ UNITS = {
     "k_mg.cu": [],
     "k_exact.cu": ["-fmad=false"],
     "k_wave.cu": ["-fmad=false"],
+    "k_light.cu": ["-fmad=false"],
     "dob_noalloc.cu": [],
     "dob_tape.cu": [],
     "k_adjoint.cu": [],

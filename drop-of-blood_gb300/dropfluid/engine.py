@@ -173,6 +173,11 @@ class DropFluid:
         """One substep of the 512x512 wave solver (contexts made with DOB_PHYS_WAVE)."""
         self._ck(self._L.dob_wave_step(self._h), "dob_wave_step")
 
+    def light_volume(self):
+        """Light volume and brick occupancy from the current dye and wave
+        (reference mode); read them with FIELD_LIGHT / FIELD_BRICKS."""
+        self._ck(self._L.dob_light_volume(self._h), "dob_light_volume")
+
     def sync(self):
         self._ck(self._L.dob_sync(self._h), "dob_sync")
 

@@ -72,9 +72,13 @@ enum {
   DOB_PHYS_SOLENOIDAL = 16,    /* deep-column solenoidal forcing (fluid.ts:488-503)   */
   DOB_PHYS_SURFACE = 32,       /* Marangoni + kinematic top layers (fluid.ts:287-310) */
   DOB_PHYS_REFERENCE_ALL = 63,
-  DOB_PHYS_WAVE = 64           /* run the 512x512 wave solver (wave.ts:55-388) at the start
+  DOB_PHYS_WAVE = 64,          /* run the 512x512 wave solver (wave.ts:55-388) at the start
                                   of every step, before the advection (BloodDropEngine.ts:
                                   1886-1912); without it the wave field is an input      */
+  DOB_PHYS_LIGHTING = 128      /* end every dob_step / dob_step_uniforms call with the light
+                                  volume and brick passes (dob_light_volume), as the
+                                  reference's frame encodes them once after its substeps
+                                  (BloodDropEngine.ts:2601-2616, 2629-2664)              */
 };
 
 /* Step configuration (plain data, versioned by struct_size). */
@@ -130,6 +134,11 @@ typedef struct dob_config {
      CONC_PRED                            : Nc
      SPLAT_INTACT, SPLAT_LYSED            : Nc (uint32)
      WAVE                                 : 4*512*512 (eta, deta/dt, lap, film)
+     LIGHT   (reference mode, read-only)  : 4*nx*ny*nz (key light, back light,
+                                            multiple scattering, filtered total
+                                            haemoglobin), binary16 values
+     BRICKS, BRICKS_RAW (reference mode,
+             read-only)                   : (nx/4)*(ny/4)*(nz/4)
    with Nc = (dye_refine*nx)*(dye_refine*ny)*(dye_refine*nz). */
 typedef enum dob_field {
   DOB_FIELD_VEL_U = 0,
@@ -145,7 +154,11 @@ typedef enum dob_field {
   DOB_FIELD_SPLAT_LYSED = 10,
   DOB_FIELD_WAVE = 11,
   DOB_FIELD_DIVERGENCE = 12,   /* read-only: MAC divergence of the current velocity */
-  DOB_FIELD_COUNT = 13,
+  DOB_FIELD_LIGHT = 13,        /* read-only: light volume (lighting.ts:19-170)        */
+  DOB_FIELD_BRICKS = 14,       /* read-only: dilated brick occupancy 0/1/2 (lighting.ts:
+                                  205-240)                                             */
+  DOB_FIELD_BRICKS_RAW = 15,   /* read-only: raw brick occupancy 0/1 (lighting.ts:172-203) */
+  DOB_FIELD_COUNT = 16,
   /* Adjoint fields (closed box, FP32, dye_refine 1; see dob_adjoint_stage).
      Host FP32, natural layout.  ADJ_VEL_U/V/W: adjoint of the MAC faces a
      stage reads (after dob_tape_backward: d loss / d initial velocity);
@@ -296,6 +309,18 @@ dob_status dob_run_stage(dob_ctx* ctx, int stage);
    DOB_ESTATE otherwise. */
 dob_status dob_wave_step(dob_ctx* ctx);
 
+/* The light volume and the empty-space brick map from the current dye and
+   wave fields and uniform block: replaces encodeLightingPasses
+   (lighting.ts:19-240; BloodDropEngine.ts dispatches it after each frame's
+   physics and at the reset).  Per velocity-grid voxel: key-light
+   transmittance with wave caustics and drop shadows, back-light
+   transmittance, multiply scattered red light, filtered total haemoglobin,
+   stored as binary16 (rgba16float); then the 4x4x4 brick occupancy of the
+   filtered total and its two-shell dilation.  Reference mode with nx, ny,
+   nz divisible by 4 (DOB_ESTATE otherwise).  Queued on the context's
+   stream; dob_reset runs it too. */
+dob_status dob_light_volume(dob_ctx* ctx);
+
 /* Device time of nsteps steps (dob_step with `flags`; with DOB_STEP_STATS
    the statistics kernels run but nothing is read back), measured with CUDA
    events on the context's stream; replaces the reference's per-pass GPU
@@ -304,7 +329,8 @@ dob_status dob_time_steps(dob_ctx* ctx, int nsteps, uint32_t flags, float* ms);
 
 /* Kernel micro-benchmark on the current state: launches the step's dominant
    kernel (which = 0: the level-0 pressure smoother pass; which = 1: one
-   wave substep, its four kernels, on a context made with DOB_PHYS_WAVE) `reps` times with
+   wave substep, its four kernels, on a context made with DOB_PHYS_WAVE;
+   which = 2: the light volume and brick passes, reference mode) `reps` times with
    CUDA events around each launch; returns the mean device ms per launch and
    the kernel's algorithmic bytes per launch (minimum HBM traffic of one
    pass).  No counterpart in the reference. */

@@ -490,6 +490,8 @@ template <class R> class Sim {
       q[4] = R(0); q[5] = R(-0.003); q[6] = R(0); q[7] = R(0);
     }
     highWater = 0;
+    // the reset's lighting passes (BloodDropEngine.ts:1760)
+    if (ref && nconc == 4 && dv.nx % 4 == 0 && dv.ny % 4 == 0 && dv.nz % 4 == 0) light_volume();
   }
 
   // ---- FLUID_ADVECT_MAC (fluid.ts:144-329) ----------------------------------------
@@ -1710,6 +1712,7 @@ template <class R> class Sim {
 
 #include "dob_oracle_adjoint.inc"
 #include "dob_oracle_wave.inc"
+#include "dob_oracle_light.inc"
 };
 
 struct AnySim {
@@ -1834,6 +1837,15 @@ template <class R> int get_field(Sim<R>& s, int field, void* host, size_t bytes)
       if (bytes != s.wave.size() * 4) return DOB_EINVAL;
       memcpy(host, s.wave.data(), bytes);
       return DOB_OK;
+    case DOB_FIELD_LIGHT:
+      if (s.light.size() != 4 * N) return DOB_ESTATE;
+      return get(s.light, 4 * N);
+    case DOB_FIELD_BRICKS:
+    case DOB_FIELD_BRICKS_RAW: {
+      const auto& b = field == DOB_FIELD_BRICKS ? s.bricks : s.brickRaw;
+      if (b.empty()) return DOB_ESTATE;
+      return get(b, b.size());
+    }
     case DOB_FIELD_DIVERGENCE: {
       if (bytes != N * sizeof(float)) return DOB_EINVAL;
       float* f = (float*)host;
@@ -2002,6 +2014,9 @@ int orc_get_field(orc_sim* s, int field, void* host, size_t bytes) {
 int orc_step(orc_sim* s, int nsteps, double* stats) {
   if (nsteps < 0) return DOB_EINVAL;
   for (int k = 0; k < nsteps; ++k) DISPATCH(s, step(stats != nullptr));
+  // DOB_PHYS_LIGHTING: the lighting passes once after the frame's steps
+  const dob_config& cfg = s->a.f64 ? s->a.sd->cfg : s->a.sf->cfg;
+  if (nsteps > 0 && cfg.bc_mode == DOB_BC_REFERENCE && (cfg.physics_flags & DOB_PHYS_LIGHTING)) DISPATCH(s, light_volume());
   if (stats) {
     const double* ls = s->a.f64 ? s->a.sd->last_stats : s->a.sf->last_stats;
     for (int i = 0; i < 5; ++i) stats[i] = ls[i];
@@ -2018,6 +2033,9 @@ void orc_set_threads(int n) {
   if (n > 0) omp_set_num_threads(n);
 }
 int orc_get_threads(void) { return omp_get_max_threads(); }
+
+// The light volume and brick passes (lighting.ts:19-240).
+int orc_light_volume(orc_sim* s) { return DISPATCH(s, light_volume()); }
 
 // The wave substep on the simulation's wave field (wave.ts:55-388).
 int orc_wave_step(orc_sim* s) {

@@ -45,6 +45,7 @@ int orc_get_threads(void);
    dob_adjoint_stage / dob_tape_forward / dob_tape_backward; the oracle's
    tape keeps every step, no checkpoints). */
 int orc_wave_step(orc_sim* s);
+int orc_light_volume(orc_sim* s);
 int orc_wave_fft2(float* data, int inverse);
 int orc_adjoint_stage(orc_sim* s, int stage);
 int orc_tape_forward(orc_sim* s, int nsteps);

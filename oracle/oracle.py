@@ -65,6 +65,7 @@ def lib():
         L.orc_get_threads.restype = C.c_int
         L.orc_adjoint_stage.argtypes = [P, C.c_int]
         L.orc_wave_step.argtypes = [P]
+        L.orc_light_volume.argtypes = [P]
         L.orc_wave_fft2.argtypes = [C.POINTER(C.c_float), C.c_int]
         L.orc_tape_forward.argtypes = [P, C.c_int]
         L.orc_tape_backward.argtypes = [P, C.POINTER(C.c_float), C.c_size_t]
@@ -214,6 +215,10 @@ class OracleSim:
     def wave_step(self):
         """One substep of the 512x512 wave solver on the wave field."""
         _check(lib().orc_wave_step(self._h), "wave_step")
+
+    def light_volume(self):
+        """The light volume and brick passes (lighting.ts:19-240)."""
+        _check(lib().orc_light_volume(self._h), "light_volume")
 
     # -- discrete adjoint (closed box, dye_refine 1) ---------------------------------------
     def adjoint_stage(self, stage):

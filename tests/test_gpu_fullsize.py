@@ -183,6 +183,14 @@ def test_reference_setup_fp32(oracle_all_cores, gpu_lib):
     print(f"reference fp32 WAVE: rel L2 {e:.2e}")
     assert e < 1e-3
     _compare("reference fp32 substep 60", g, o)
+    # the frame's lighting passes on the device's state: bit for bit
+    o.set_field(abi.FIELD_CONC, g.get_field(abi.FIELD_CONC))
+    o.set_field(abi.FIELD_WAVE, g.get_field(abi.FIELD_WAVE))
+    for e in (g, o):
+        e.light_volume()
+    assert bits_equal(g.get_field(abi.FIELD_LIGHT), o.get_field(abi.FIELD_LIGHT))
+    assert bits_equal(g.get_field(abi.FIELD_BRICKS), o.get_field(abi.FIELD_BRICKS))
+    assert (g.get_field(abi.FIELD_BRICKS) > 0).any()
     # one full-size parcel substep (emission + advection + splat) from the device's state
     o.set_uniforms(last)
     _parcel_step_bit_exact(g, o, seq.high_water, [abi.STAGE_PARCEL_EMIT, abi.STAGE_PARCEL_ADVECT])

@@ -720,3 +720,68 @@ def test_pipelined_steps_match_synchronous(gpu_lib):
     b.step_result(0)
     a.close()
     b.close()
+
+
+# ---- light volume and brick occupancy (lighting.ts:19-240) -------------------------------------
+@pytest.mark.parametrize("prec,variant", [(0, "studio"), (0, "dark_camera"), (2, "studio")])
+def test_light_volume_bit_exact(both, prec, variant):
+    """The light volume (binary16 key light, back light, multiple scattering,
+    filtered total) and both brick maps equal the oracle bit for bit, from a
+    seeded dye and wave field with two drops above the surface; the dark
+    variant also moves the camera (the back light's heading)."""
+    abi = _abi()
+    cfg = ref_config(prec=prec)
+    g, o = both(cfg)
+    st = ref_state(cfg, seed=12)
+    # a sparser dye than the stage tests' (most voxels under the empty-water
+    # threshold, marches that run their 9 samples)
+    conc = st[abi.FIELD_CONC]
+    conc *= (conc[..., :1] > 0.35).astype(np.float32) * 0.05
+    if prec == abi.DOB_PREC_REFERENCE_FP16:
+        # the device stores the loaded dye as binary16; give the oracle the same values
+        st[abi.FIELD_CONC] = conc.astype(np.float16).astype(np.float32)
+    blk = ref_block()
+    if variant == "dark_camera":
+        blk[51] = 1.0
+        blk[8:16] = [0.3, 0.1, -0.5, 0.0, 0.1, 0.2, 0.7, 1.0]
+        blk[32:35] = [0.5, 0.4, 1.8]
+    for e in (g, o):
+        e.set_uniforms(blk)
+        load_state(e, st)
+        e.light_volume()
+    a, b = g.get_field(abi.FIELD_LIGHT), o.get_field(abi.FIELD_LIGHT)
+    assert bits_equal(a, b), (int((a != b).any(axis=-1).sum()), float(np.abs(a - b).max()))
+    assert (a[..., 0] < 1.0).any() and (a[..., 2] > 0.0).any()
+    for f in (abi.FIELD_BRICKS_RAW, abi.FIELD_BRICKS):
+        assert bits_equal(g.get_field(f), o.get_field(f)), f
+    assert (g.get_field(abi.FIELD_BRICKS) == 1.0).any() and (g.get_field(abi.FIELD_BRICKS) == 2.0).any()
+
+
+def test_lighting_flag_runs_once_per_call(gpu_lib):
+    """DOB_PHYS_LIGHTING ends dob_step / dob_step_uniforms with the lighting
+    passes on the last step's parameters: the same bits as an explicit
+    dob_light_volume after the same steps."""
+    abi = _abi()
+    from dropfluid import DropFluid
+    cfg = ref_config()
+    cfg_l = ref_config()
+    cfg_l.physics_flags = abi.DOB_PHYS_REFERENCE_ALL | abi.DOB_PHYS_LIGHTING
+    a, b = DropFluid(cfg), DropFluid(cfg_l)
+    st = ref_state(cfg, seed=13)
+    del st[abi.FIELD_CURL]
+    blocks = np.stack([ref_block(sim_time=0.5 + k / 60.0, spawn=256, cursor=256 * k) for k in range(3)])
+    for e in (a, b):
+        e.set_uniforms(blocks[0])
+        e.reset()
+        load_state(e, st)
+        e.step_uniforms(blocks)
+    a.light_volume()
+    assert bits_equal(a.get_field(abi.FIELD_LIGHT), b.get_field(abi.FIELD_LIGHT))
+    assert bits_equal(a.get_field(abi.FIELD_BRICKS), b.get_field(abi.FIELD_BRICKS))
+    r = DropFluid(box_config())
+    from dropfluid import DropFluidError
+    with pytest.raises(DropFluidError) as ei:
+        r.light_volume()
+    assert ei.value.status == abi.DOB_ESTATE
+    for e in (a, b, r):
+        e.close()
