@@ -42,6 +42,9 @@ for _p in (PKG, ORACLE_DIR):
         sys.path.insert(0, _p)
 
 METRIC = "steps/s @192x256x192: mixed vs FP32 at div<1e-5; adjoint/forward step ratio"
+WORKLOAD = ("box192: 192x256x192 closed-box MAC step, 3 drops r=12 released at steps 0/40/80, 393216 parcels, "
+            "FP32 storage, 4 V-cycles of 2+2 RBGS on 5 grids with an exact 12x16x12 coarsest solve (8 V-cycles "
+            "on the two steps after each release), Casson tau_y=0.005 mu_p=1e-3, dx=1 dt=0.02")
 
 
 def rank_info():
@@ -220,7 +223,76 @@ def wave_leg(peak):
         return {"error": f"{type(ex).__name__}: {ex}"}
 
 
-def adjoint_leg(fd_dirs: int = 16):
+def fd64_check(sc, grads, target, d_imp, ndirs, seed=12345, h=1e-5, eps=1e-3):
+    """The device gradient of the box96 loss against central differences of
+    the FP64 oracle's loss (the oracle in double arithmetic, the same scene,
+    V-cycles per step and target): the drop impulse (step h relative) and
+    the same seeded random directions of the initial MAC velocity as the
+    device check (step eps in world units, 1.3e-5 of the injected face
+    speed), small enough that the FP64 trajectory crosses no limiter or
+    clamp branch.  Each loss is 32 FP64 steps on the host cores."""
+    import numpy as np
+    import oracle
+    from dropfluid import abi, scenes
+    oracle.build()
+    oracle.set_threads(os.cpu_count() or 1)
+    t0 = time.perf_counter()
+    cfg = sc.config.copy()
+    cfg.mg_cycles_injected = 0  # the recorded trajectory runs mg_cycles on every step
+    o = oracle.OracleSim(cfg, fp64=True)
+    vel = (abi.FIELD_VEL_U, abi.FIELD_VEL_V, abi.FIELD_VEL_W)
+
+    def loss64(scene, pert=None):
+        o.reset()
+        for j in scene.releases_at(0):
+            scene.release(o, j)
+        if pert is not None:
+            for f, d in pert.items():
+                o.set_field64(f, o.get_field64(f) + d)
+        # the recorded trajectory's forward: centre velocity from the faces,
+        # then plain steps (dob_tape_forward gives the same bits)
+        o.run_stage(abi.STAGE_MAC_TO_CENTER)
+        o.step(scene.steps)
+        d = o.get_field64(abi.FIELD_CONC) - target
+        return float(np.sum(d * d))
+
+    fd_imp = (loss64(scenes.box96(impulse_scale=1.0 + h)) - loss64(scenes.box96(impulse_scale=1.0 - h))) / (2 * h)
+    # the FP64 oracle's own discrete adjoint of its own trajectory
+    o.reset()
+    for j in sc.releases_at(0):
+        sc.release(o, j)
+    o.tape_forward(sc.steps)
+    o.tape_backward((2.0 * (o.get_field64(abi.FIELD_CONC) - target)).astype(np.float32))
+    g64 = {k: np.asarray(v, np.float64) for k, v in o.gradients().items()}
+    d0 = sc.drops[0]
+    imp64 = o.sphere_impulse(d0.center, d0.radius, (0.0, d0.w_cells_per_step * cfg.dx / cfg.dt, 0.0))
+    rng = np.random.default_rng(seed)
+    shape = grads["u"].shape
+    errs, errs64, rows = [], [], []
+    for _ in range(ndirs):
+        d = {f: rng.standard_normal(shape).astype(np.float32).astype(np.float64) for f in vel}
+        ad = sum(float(np.sum(grads[k].astype(np.float64) * d[f])) for k, f in zip("uvw", vel))
+        ad64 = sum(float(np.sum(g64[k] * d[f])) for k, f in zip("uvw", vel))
+        fd = (loss64(sc, {f: eps * a for f, a in d.items()}) - loss64(sc, {f: -eps * a for f, a in d.items()})) / (2 * eps)
+        errs.append(abs(fd - ad) / max(abs(fd), 1e-30))
+        errs64.append(abs(fd - ad64) / max(abs(fd), 1e-30))
+        rows.append([ad, ad64, fd])
+    o.close()
+
+    def rel(a, b):
+        return float(np.linalg.norm((a - b).ravel()) / max(np.linalg.norm(b.ravel()), 1e-300))
+    return {"impulse_fd64": fd_imp, "impulse_rel_err": abs(d_imp - fd_imp) / abs(fd_imp),
+            "impulse_adjoint64": imp64, "impulse_adjoint64_rel_err": abs(imp64 - fd_imp) / abs(fd_imp),
+            "dirs": ndirs, "eps_world": eps, "h_impulse": h,
+            "rel_err_max": max(errs), "rel_err_median": float(np.median(errs)),
+            "adjoint64_rel_err_max": max(errs64), "adjoint64_rel_err_median": float(np.median(errs64)),
+            "device_vs_adjoint64_field_rel_l2": {k: rel(np.asarray(grads[k], np.float64), g64[k]) for k in "uvw"},
+            "directional": rows, "directional_columns": ["device", "FP64 adjoint", "FP64 differences"],
+            "host_s": time.perf_counter() - t0,
+            "reference": "FP64 oracle (double arithmetic on the host cores), same scene, target and V-cycles"}
+
+
+def adjoint_leg(fd_dirs: int = 16, fd64_dirs: int = 16):
     """Forward/backward pair of the discrete adjoint.
 
     box96 (96x128x96, one r=8 drop with N(0, 0.05) face noise, 32 steps,
@@ -289,7 +361,9 @@ def adjoint_leg(fd_dirs: int = 16):
         lm = l2_loss(fwd(sc, {f: -eps * a for f, a in d.items()}), target)[0]
         fd = (lp - lm) / (2 * eps)
         errs.append(abs(fd - ad) / max(abs(fd), 1e-30))
+    fd64 = fd64_check(sc, grads, target, d_imp, fd_dirs) if fd64_dirs else None
     out["box96"] = {
+        "fd64": fd64,
         "steps": sc.steps, "checkpoint_every": 8, "loss": loss,
         "forward_step_ms": fwd_ms, "tape_forward_ms_per_step": 1e3 * t_tape_fwd / sc.steps,
         "backward_ms_per_step": 1e3 * t_bwd / sc.steps,
@@ -411,18 +485,113 @@ def accuracy_run():
             "gpu_s": t_gpu, "fp64_cpu_s": t_cpu}
 
 
-def reference_block(sim_time=0.5, spawn=512, cursor=0):
-    """Uniform block of the reference-mode scene: two active drop slots
-    draining into the free surface (a fixed stand-in for the reference's
-    drop-lifecycle model, which is host input), dt = 1/60."""
-    from dropfluid import uniforms as U
-    snap = U.DropSnapshot(sim_time=sim_time, active_count=2)
-    snap.slots[0] = U.DropSlot(active=True, center=(0.03, 0.285, -0.02), radius=0.05, vel_y=-0.3,
-                               oscillation=0.01, vol_drain_rate=0.42, seed=1.5)
-    snap.slots[1] = U.DropSlot(active=True, center=(-0.12, 0.31, 0.09), radius=0.03, vel_y=-0.5,
-                               oscillation=0.0, vol_drain_rate=0.05, seed=2.7)
-    return U.SimUniformPacker().pack(drops=snap, dt=U.FIXED_SIM_DT, global_seed=1.5, spawn_cursor=cursor,
-                                     spawn_count=spawn).copy()
+def reference_sequence(warm_substeps=56):
+    """The reference setup's host input from the drop-lifecycle restatement
+    (dropfluid.sequencer, BloodDropEngine.ts:1682-1844): the reset block and
+    the blocks of the first `warm_substeps` fixed 1/60 s substeps, whose last
+    ones cover the first drop's impact on the meniscus (0.92 s, substep 56)
+    and the start of its drainage and parcel emission."""
+    from dropfluid.sequencer import SubstepSequencer
+    seq = SubstepSequencer(seed=1.0)
+    reset = seq.reset_simulation(1.0)
+    blocks = [seq.advance_substep()[0] for _ in range(warm_substeps)]
+    return seq, reset, blocks
+
+
+# Algorithmic bytes of one reference-mode substep, per stage: every array a
+# stage reads read once and every array it writes written once, at the
+# storage widths of the precision mode (vs: velocity / centre / curl
+# element, ds: dye element; V velocity cells, C = 8 V dye voxels).
+def reference_stage_bytes(cfg, high_water):
+    from dropfluid import abi
+    V = cfg.nx * cfg.ny * cfg.nz
+    C = V * cfg.dye_refine ** 3
+    vs = 2 if cfg.precision_mode == abi.DOB_PREC_REFERENCE_FP16 else 4
+    ds = 2 if cfg.precision_mode != abi.DOB_PREC_FP32 else 4
+    # V-cycle, reference schedule: level 0 one sweep before and after (12 B
+    # per cell and sweep), residual + restriction and prolongation 8.5 B
+    # each; levels 1-2 two and two sweeps; the 12x16x12 grid is negligible
+    mg = (2 * 12 + 17) * V + (4 * 12 + 17) * (V / 8 + V / 64)
+    return {
+        "wave": 88 * 512 * 512 if cfg.physics_flags & abi.DOB_PHYS_WAVE else 0,
+        "advect_mac": 10 * vs * V,                     # u,v,w + centre in, u,v,w out
+        "mac_to_center": 2 * 7 * vs * V,               # twice: faces in, centre out
+        "curl": 8 * vs * V,                            # centre in, curl out
+        "casson_forces": 10 * vs * V + 4 * ds * C,     # faces + curl in, dye sampled, faces out
+        "mac_rhs": (3 * vs + 4) * V,
+        "pressure_solve": mg,
+        "project": (6 * vs + 4) * V,
+        "clear_splats": 8 * C,
+        "parcel_advect": 64 * high_water,              # 32 B per parcel in and out
+        "conc_predict": 5 * ds * C + 4 * vs * V,       # dye in, predictor out, centre sampled
+        "conc_resolve": (9 * ds + 8) * C + 4 * vs * V,  # dye, predictor, two splats in, dye out
+    }
+
+
+def reference_mode_leg(peak, substeps=60):
+    """The reference's own setup (dob_config_reference: 96x128x96 velocity,
+    192x256x192 four-channel dye, reference V-cycle schedule, 393216
+    parcels, the wave solver each substep), driven by the host
+    drop-lifecycle sequence.  After 50 untimed substeps, `substeps` more
+    (the first drop's impact, drainage and parcel emission) run through
+    dob_step_uniforms with a block copy per substep (wall clock, host
+    included); the device time of 20 graph-replayed substeps on the last
+    block; per-stage device times (stage by stage, events) against the
+    stage byte model.  Errors are reported in the line, not raised."""
+    try:
+        import numpy as np
+        from dropfluid import DropFluid, abi
+        cfg = abi.config_reference()
+        cfg.physics_flags = abi.DOB_PHYS_REFERENCE_ALL | abi.DOB_PHYS_WAVE
+        out = {}
+        for name, prec in (("fp32", abi.DOB_PREC_FP32), ("fp16_storage", abi.DOB_PREC_REFERENCE_FP16)):
+            cfg.precision_mode = prec
+            seq, reset, warm = reference_sequence(50)
+            e = DropFluid(cfg)
+            e.set_uniforms(reset)
+            e.reset()
+            e.step_uniforms(np.stack(warm))
+            blocks = [seq.advance_substep() for _ in range(substeps)]
+            e.sync()
+            t0 = time.perf_counter()
+            e.step_uniforms(np.stack([b[0] for b in blocks]))
+            e.sync()
+            wall = time.perf_counter() - t0
+            ms = e.time_steps(20) / 20.0
+            tst = e.step(2, timing=True)
+            stage_ms = {k: v / 2.0 for k, v in tst["stage_ms"].items() if v > 0}
+            sb = reference_stage_bytes(cfg, seq.high_water)
+            total = sum(sb.values())
+            stages = {}
+            for key, v in stage_ms.items():  # stage names as in abi.STAGE_NAMES
+                b = sb.get(key)
+                stages[key] = {"ms": v, "bytes": b,
+                               "gbs": (b / (v * 1e-3) / 1e9) if b else None,
+                               "frac": (b / (v * 1e-3) / 1e9 / peak) if b else None}
+            dom = max(stages.items(), key=lambda kv: kv[1]["ms"])
+            e.bench_kernel(2, reps=3)
+            lk_ms, lk_bytes = e.bench_kernel(2, reps=20)
+            light = {"us_per_launch": lk_ms * 1e3, "bytes_per_launch": lk_bytes,
+                     "achieved_gbs": lk_bytes / (lk_ms * 1e-3) / 1e9,
+                     "frac_of_measured_hbm": lk_bytes / (lk_ms * 1e-3) / 1e9 / peak,
+                     "kernels": 2, "note": "light volume + brick dilation (lighting.ts:19-240), once per frame; "
+                                           "20 launches on the live state, CUDA events"}
+            out[name] = {
+                "steps_per_s_e2e": substeps / wall, "e2e_path": "dob_step_uniforms, one 512-byte block per substep",
+                "steps_per_s_device": 1e3 / ms, "ms_per_step_device": ms,
+                "bytes_per_step": total, "achieved_gbs": total / (ms * 1e-3) / 1e9,
+                "frac_of_measured_hbm": total / (ms * 1e-3) / 1e9 / peak,
+                "spawned_parcels": int(sum(b[1] for b in blocks)), "high_water": seq.high_water,
+                "stages": stages, "dominant_stage": dom[0], "light_volume": light,
+                "launches_per_step": e.launches_per_step(),
+            }
+            e.close()
+        out["workload"] = ("reference setup: 96x128x96 velocity, 192x256x192 dye, Dirichlet free-surface top, "
+                           "reference V-cycle (L0 1+1, L1-L2 2+2, L3 6 sweeps), 393216-parcel ring, wave solver "
+                           "each substep; uniforms from the drop-lifecycle sequence (seed 1), substeps 51-110")
+        return out
+    except Exception as ex:  # reported, never fatal
+        return {"error": f"{type(ex).__name__}: {ex}"}
 
 
 def configs_report():
@@ -437,11 +606,14 @@ def configs_report():
 
     def reference96():
         cfg = abi.config_reference()  # 96x128x96 velocity, 192x256x192 dye, 393216 parcels
-        blk = reference_block()
+        # the block of the drop-lifecycle sequence right after the first
+        # drop's impact (draining, parcels spawned every substep)
+        _, reset, blocks = reference_sequence(60)
 
         def setup(e):
-            e.set_uniforms(blk)
+            e.set_uniforms(reset)
             e.reset()
+            e.set_uniforms(blocks[-1])
         return cfg, setup
 
     def scene_setup(sc):
@@ -453,7 +625,8 @@ def configs_report():
     cases = [("cfg0 box48 (48x64x48, FP32)", scene_setup(scenes.box48()), 20, (20, 20, 20)),
              ("cfg1 box192 (192x256x192, FP32)", scene_setup(scenes.box192()), 20, (3, 1, 3)),
              ("cfg3 box96 (96x128x96, FP32)", scene_setup(scenes.box96()), 32, (8, 2, 8)),
-             ("reference mode (96x128x96 velocity, 192x256x192 dye, free-surface top, 2 drops)", reference96(), 20,
+             ("reference mode (96x128x96 velocity, 192x256x192 dye, free-surface top, first drop draining)",
+              reference96(), 20,
               (2, 1, 2))]
     out = []
     for name, (cfg, setup), gsteps, (n32, n1, n64) in cases:
@@ -486,26 +659,48 @@ def configs_report():
     return {"configs": out, "host_cores": ncores}
 
 
+def release_note(scene, start, n):
+    """Which drop releases (and their extra-cycle steps) a timed window holds."""
+    rel = [d.release_step for d in scene.drops if start <= d.release_step < start + n]
+    if not rel:
+        return f"steps {start}-{start + n - 1}: no drop release in the window"
+    return f"steps {start}-{start + n - 1}: drop releases at steps {rel} (8 V-cycles on the two steps after each)"
+
+
 def run_reference(args, rank, world):
+    """The reference arm: the oracle (the CPU restatement of the reference
+    step; the reference's own WGSL step needs a browser WebGPU stack) on all
+    host cores, over the same window of the same scene as the GPU arm: W
+    untimed steps from the first release, then K timed steps with the
+    releases that fall inside them."""
     if rank != 0:
         return 0
+    import oracle
     from dropfluid import scenes
     threads = os.cpu_count() or 1
-    steps = max(1, min(args.steps, 6))
+    warmup = max(3, args.warmup)
+    steps = max(1, min(args.steps, 200))
+    oracle.build()
+    oracle.set_threads(threads)
+    sc = scenes.box192()
+    sim = oracle.OracleSim(sc.config)
     t_start = time.perf_counter()
-    value, secs = cpu_baseline(scenes.box192, steps, threads)
+    run_scene_steps(sc, sim, 0, warmup, timed=False)
+    t0 = time.perf_counter()
+    run_scene_steps(sc, sim, warmup, steps, timed=False)
+    secs = time.perf_counter() - t0
+    value = steps / secs
+    window = release_note(sc, warmup, steps)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world,
-        "steps": steps, "warmup": 1, "ms_per_step": 1000.0 / value, "higher_is_better": True,
+        "steps": steps, "warmup": warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "box192: 192x256x192 closed-box MAC step, 3 drops r=12, 393216 parcels, FP32, "
-                               "4 V-cycles of 2+2 RBGS on 5 grids, exact 12x16x12 coarsest solve "
-                               "(dropfluid.scenes.box192)",
-                   "grid": [192, 256, 192], "parallelism": "replicas"},
+        "config": {"workload": WORKLOAD, "grid": [192, 256, 192], "parallelism": "replicas",
+                   "timed": f"host wall clock of K oracle steps; {window}"},
         "cpu_baseline": {"value": value, "unit": "steps/s", "cores": threads, "kind": "port",
-                         "sample": f"{steps} steps of box192 after drop 0 released and 1 warm-up step "
-                                   f"({secs:.1f} s); the reference's own WGSL step needs a browser WebGPU "
-                                   f"stack, unavailable on this box"},
+                         "sample": f"{steps} steps of box192 ({window}) after {warmup} warm-up steps, FP32 oracle "
+                                   f"with OpenMP on {threads} threads: {secs:.1f} s; the reference's own WGSL step "
+                                   f"needs a browser WebGPU stack, unavailable on this box"},
         "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "wall_s": time.perf_counter() - t_start,
     }
@@ -522,6 +717,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-reference-mode", action="store_true")
     ap.add_argument("--accuracy", action="store_true",
                     help="error of the FP32 and mixed runs against an FP64 run at steps 50/100/200, then exit")
     ap.add_argument("--configs", action="store_true",
@@ -667,27 +863,26 @@ def main():
                          f"and 1 warm-up step: {csecs:.1f} s"}
 
     wave = wave_leg(measured_peaks()[0]) if rank == 0 else None
+    refmode = reference_mode_leg(measured_peaks()[0]) if rank == 0 and not args.no_reference_mode else None
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "box192: 192x256x192 closed-box MAC step, 3 drops r=12 released at "
-                                   "steps 0/40/80, 393216 parcels, FP32 storage, 4 V-cycles of 2+2 RBGS on "
-                                   "5 grids with an exact 12x16x12 coarsest solve (8 V-cycles on the "
-                                   "two steps after each release), Casson tau_y=0.005 "
-                                   "mu_p=1e-3, dx=1 dt=0.02",
+            "config": {"workload": WORKLOAD,
                        "grid": [192, 256, 192], "parallelism": "replicas" if world > 1 else "single",
                        "l2": "inputs larger than L2 (>=12 fields x 37.7 MB per step), no flush",
                        "timed": "device time of K graph-replayed steps (CUDA events on the library stream); "
-                                "drop releases between segments untimed"},
+                                "drop releases between segments untimed; "
+                                + release_note(sc, args.warmup, args.steps)},
             "cell_updates_per_s": value * 192 * 256 * 192,
             "max_div": st["max_div"], "residual_l2": st["residual_l2"], "rhs_l2": st["rhs_l2"],
             "mixed": mixed,
             "adjoint_forward_ratio": adj["box96"]["ratio"] if adj else None,
             "adjoint": adj,
             "wave": wave,
+            "reference_mode": refmode,
             "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "path": "DropFluid.run_pipelined (dob_step_async + dob_step_result, 2 steps in flight): "
                             "params host->device from pinned memory, step graph with statistics, statistics "

@@ -237,3 +237,76 @@ def test_recorded_forward_matches_steps_and_repeats(gpu_lib):
         assert rel_l2(g2[c], g1[c]) < 1e-6, c
     a.close()
     b.close()
+
+
+def test_gradient_directions_against_fp64_differences(gpu_lib, oracle_mod):
+    """Directional derivatives of the trajectory loss along seeded random
+    directions of the initial MAC velocity: the device gradient (the adjoint
+    of the FP32 trajectory) and the FP64 oracle's adjoint against central
+    differences of the FP64 oracle's loss (step 1e-6, below every limiter
+    and clamp branch of the FP64 trajectory), each within 1e-3 per
+    direction, and the device's field gradients within 1e-3 (relative L2)
+    of the FP64 adjoint's.  The scene is the benchmark's drop (-1.5
+    cells/step with N(0, 0.05) face noise) on the 48x64x48 box, 8 steps."""
+    from dropfluid import DropFluid, scenes
+    sc = scenes.box48()
+    sc.drops[0].n_parcels = 0
+    sc.drops[0].w_cells_per_step = -1.5
+    sc.drops[0].noise_cells_per_step = 0.05
+    cfg = sc.config
+    cfg.mg_cycles_injected = 0  # recorded steps run mg_cycles
+    steps = 8
+    g = DropFluid(cfg)
+    o = oracle_mod.OracleSim(cfg, fp64=True)
+
+    def init(e, scale=1.0, pert=None):
+        e.reset()
+        w0 = sc.drops[0].w_cells_per_step
+        sc.drops[0].w_cells_per_step = w0 * scale
+        sc.release(e, 0)
+        sc.drops[0].w_cells_per_step = w0
+        for f, a in (pert or {}).items():
+            e.set_field64(f, e.get_field64(f) + a)
+
+    init(o, 1.1)
+    o.tape_forward(steps)
+    target = o.get_field64(abi.FIELD_CONC)
+    grads = {}
+    for name, e in (("gpu", g), ("orc", o)):
+        init(e)
+        if name == "gpu":
+            e.tape_forward(steps, 4)
+            dye = np.asarray(e.get_field(abi.FIELD_CONC), np.float64)
+        else:
+            e.tape_forward(steps)
+            dye = e.get_field64(abi.FIELD_CONC)
+        e.tape_backward((2 * (dye - target)).astype(np.float32))
+        grads[name] = {k: np.asarray(v, np.float64) for k, v in e.gradients().items()}
+    vel = (abi.FIELD_VEL_U, abi.FIELD_VEL_V, abi.FIELD_VEL_W)
+
+    def loss64(pert):
+        init(o, 1.0, pert)
+        o.tape_forward(steps)
+        dd = o.get_field64(abi.FIELD_CONC) - target
+        return float(np.sum(dd * dd))
+
+    rng = np.random.default_rng(2)
+    eps = 1e-6
+    shape = grads["gpu"]["u"].shape
+    dev_err, orc_err = [], []
+    for _ in range(6):
+        dirs = {f: rng.standard_normal(shape) for f in vel}
+        fd = (loss64({f: eps * a for f, a in dirs.items()}) - loss64({f: -eps * a for f, a in dirs.items()})) / (2 * eps)
+        for name, errs in (("gpu", dev_err), ("orc", orc_err)):
+            ad = sum(float(np.sum(grads[name][k] * dirs[f])) for k, f in zip("uvw", vel))
+            errs.append(abs(ad - fd) / abs(fd))
+    print("directional rel err, device:", ["%.1e" % x for x in dev_err])
+    print("directional rel err, FP64 adjoint:", ["%.1e" % x for x in orc_err])
+    for k in "uvw":
+        print(f"field gradient {k}: device vs FP64 adjoint rel L2 {rel_l2(grads['gpu'][k], grads['orc'][k]):.2e}")
+    # measured: FP64 adjoint 1.3e-4, device 2.1e-4 at worst; field gradients 1.5e-4
+    assert max(orc_err) < 1e-3, orc_err
+    assert max(dev_err) < 1e-3, dev_err
+    for k in "uvw":
+        assert rel_l2(grads["gpu"][k], grads["orc"][k]) < 1e-3, k
+    g.close()
