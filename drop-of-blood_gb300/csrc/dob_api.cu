@@ -79,6 +79,7 @@ static bool valid_config(const dob_config* c, std::string* why) {
       return no("mg_coarse_sweeps = -1 (exact coarsest solve) needs a coarsest grid of at most 4096 cells");
   }
   if (c->precision_mode == DOB_PREC_MIXED && (c->mg_max_outer < 1 || c->mg_max_outer > 32)) return no("mg_max_outer must be 1..32");
+  if (c->precision_mode == DOB_PREC_MIXED && c->mg_levels < 2) return no("the mixed mode needs at least 2 grids");
   if (!(c->mg_rel_tol >= 0.0) || !(c->mg_div_tol >= 0.0) || !isfinite(c->mg_rel_tol) || !isfinite(c->mg_div_tol))
     return no("mg_rel_tol and mg_div_tol must be finite and >= 0");
   if (c->parcel_capacity < 1 || c->parcel_capacity > (1u << 26)) return no("parcel_capacity out of range");
@@ -173,7 +174,9 @@ static void swap_vel(DevState& s) {
 }
 
 // Enqueue one stage on the context's stream, updating the ping-pong state.
-static void enqueue_stage(dob_ctx* ctx, DevState& s, int stage, cudaStream_t st) {
+// in_step: the stage runs inside a full step, after the projection and the
+// centre pass (the dye stages may then skip clear water, see k_fluid.cu).
+static void enqueue_stage(dob_ctx* ctx, DevState& s, int stage, cudaStream_t st, bool in_step = false) {
   const size_t nc = s.gc.n();
   switch (stage) {
     case DOB_STAGE_ADVECT_MAC: launch_advect_mac(s, st); swap_vel(s); break;
@@ -189,8 +192,8 @@ static void enqueue_stage(dob_ctx* ctx, DevState& s, int stage, cudaStream_t st)
       break;
     case DOB_STAGE_PARCEL_EMIT: launch_parcel_emit(s, st); break;
     case DOB_STAGE_PARCEL_ADVECT: launch_parcel_advect(s, st); break;
-    case DOB_STAGE_CONC_PREDICT: launch_conc_predict(s, st); break;
-    case DOB_STAGE_CONC_RESOLVE: launch_conc_resolve(s, st); std::swap(s.conc, s.conc2); break;
+    case DOB_STAGE_CONC_PREDICT: launch_conc_predict(s, st, false, in_step); break;
+    case DOB_STAGE_CONC_RESOLVE: launch_conc_resolve(s, st, in_step); std::swap(s.conc, s.conc2); break;
     default: break;
   }
   (void)ctx;
@@ -234,7 +237,7 @@ static void enqueue_step_body(dob_ctx* ctx, DevState& s, cudaStream_t st, float*
       launch_dye_resolve_lim(s, st);
       std::swap(s.conc, s.conc2);
     } else {
-      enqueue_stage(ctx, s, stage, st);
+      enqueue_stage(ctx, s, stage, st, true);
     }
     if (stage_ms) {
       cudaEventRecord(ctx->stage_ev[1], st);
@@ -364,7 +367,7 @@ static void fill_stats(dob_ctx* ctx, const double* red, const unsigned int* redu
   stats->steps_done = steps;
   if (ctx->cfg.precision_mode == DOB_PREC_MIXED) {
     stats->outer_iters = (int)redu[REDU_ITERS];
-    stats->vcycles = (int)redu[REDU_ITERS] * ctx->cfg.mg_cycles;
+    stats->vcycles = (int)redu[REDU_VCYCLES];
   } else {
     stats->outer_iters = 0;
     stats->vcycles = cycles;  // of the last step
@@ -495,6 +498,11 @@ dob_status dob_create(const dob_config* cfg, dob_ctx** out) {
   A((void**)&s.p, N * 4); A((void**)&s.rhs, N * 4);
   const int nch = s.ref ? 4 : 1;
   A(&s.conc, Nc * nch * dsb); A(&s.conc2, Nc * nch * dsb); A(&s.pred, Nc * dsb);
+  s.concA = s.conc;
+  if (s.ref) {
+    const size_t nb = dye_brick_count(s.gc) * sizeof(uint32_t);
+    A((void**)&s.cbrickA, nb); A((void**)&s.cbrickB, nb); A((void**)&s.pbrick, nb);
+  }
   if (!s.ref) A(&s.lim, Nc * 2 * dsb);
   A((void**)&s.splatI, Nc * 4); A((void**)&s.splatL, Nc * 4);
   A((void**)&s.wave, (size_t)kWaveN * kWaveN * 16);
@@ -548,6 +556,9 @@ dob_status dob_create(const dob_config* cfg, dob_ctx** out) {
   // max |b - A p| target: the projected divergence is b - A p, reported as
   // max |div| dt/dx in the closed box and unscaled in reference mode
   s.div_tol_r = (float)(s.ref ? cfg->mg_div_tol : cfg->mg_div_tol * cfg->dx / cfg->dt);
+  // the mixed solve stops at 0.9 of the divergence target: the projection
+  // that follows adds its own FP32 rounding to the divergence it leaves
+  if (s.prec == DOB_PREC_MIXED) s.div_tol_r *= 0.9f;
   if (st != DOB_OK) {
     *out = nullptr;
     std::string keep = ctx->err;
@@ -627,6 +638,12 @@ dob_status dob_reset(dob_ctx* ctx) {
     if (a) CK(cudaMemsetAsync(a, 0, N * 4, ctx->stream));
   CK(cudaMemsetAsync(s.conc, 0, Nc * nch * dsb, ctx->stream));
   CK(cudaMemsetAsync(s.conc2, 0, Nc * nch * dsb, ctx->stream));
+  if (s.cbrickA) {  // clear water everywhere
+    const size_t nb = dye_brick_count(s.gc) * sizeof(uint32_t);
+    CK(cudaMemsetAsync(s.cbrickA, 0, nb, ctx->stream));
+    CK(cudaMemsetAsync(s.cbrickB, 0, nb, ctx->stream));
+    CK(cudaMemsetAsync(s.pbrick, 0, nb, ctx->stream));
+  }
   CK(cudaMemsetAsync(s.pred, 0, Nc * dsb, ctx->stream));
   CK(cudaMemsetAsync(s.splatI, 0, Nc * 4, ctx->stream));
   CK(cudaMemsetAsync(s.splatL, 0, Nc * 4, ctx->stream));
@@ -707,6 +724,17 @@ dob_status dob_set_high_water(dob_ctx* ctx, uint32_t hw) {
   return DOB_OK;
 }
 
+// Dye written from outside the step (field I/O, snapshots): every dye brick
+// may hold dye until the next resolve rewrites the flags.
+static dob_status dye_bricks_unknown(dob_ctx* ctx) {
+  DevState& s = ctx->s;
+  if (!s.cbrickA) return DOB_OK;
+  const size_t nb = dye_brick_count(s.gc) * sizeof(uint32_t);
+  CK(cudaMemsetAsync(s.cbrickA, 1, nb, ctx->stream));
+  CK(cudaMemsetAsync(s.cbrickB, 1, nb, ctx->stream));
+  return DOB_OK;
+}
+
 // ---- field I/O -----------------------------------------------------------------------
 __global__ void k_add_arrays(const float* __restrict__ a, const float* __restrict__ b, float* __restrict__ out,
                              size_t n) {
@@ -758,6 +786,10 @@ dob_status dob_set_field(dob_ctx* ctx, int field, const void* host, size_t bytes
   if (read_only || !field_desc(ctx, field, &f))
     return fail(ctx, DOB_EINVAL, "dob_set_field", "unknown or read-only field");
   if (bytes != f.count * 4) return fail(ctx, DOB_EINVAL, "dob_set_field", "byte count does not match the field");
+  if (field == DOB_FIELD_CONC) {
+    dob_status bs = dye_bricks_unknown(ctx);
+    if (bs != DOB_OK) return bs;
+  }
   CK(cudaStreamSynchronize(ctx->stream));
   const size_t eb = f.kind == 0 ? vs_bytes(ctx->s.prec) : f.kind == 1 ? ds_bytes(ctx->s.prec) : 4;
   if (f.kind == 4) {
@@ -1088,6 +1120,8 @@ dob_status dob_load_state(dob_ctx* ctx, int slot) {
   ctx->high_water = sn.high_water;
   ctx->step_index = sn.step_index;
   ctx->inject_pending = sn.inject_pending;
+  dob_status bs = dye_bricks_unknown(ctx);
+  if (bs != DOB_OK) return bs;
   CK(cudaStreamSynchronize(ctx->stream));
   return DOB_OK;
 }

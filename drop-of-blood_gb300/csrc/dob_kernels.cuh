@@ -53,6 +53,12 @@ struct DevState {
   float* wfilm;                  // wave solver: the force pass's surfactant film
   float* parcels;
   uint32_t cap;
+  // sparse dye bricks (reference mode, k_fluid.cu): per 8x8x8 brick of the
+  // dye grid, whether the predictor / a dye buffer's lysed channel holds a
+  // nonzero value; concA is the buffer cbrickA belongs to (conc and conc2
+  // swap every step, the flags stay with their buffer)
+  const void* concA;
+  uint32_t *cbrickA, *cbrickB, *pbrick;
   // light volume (reference mode, dims divisible by 4): 4 x binary16 per
   // velocity cell, and the raw and dilated occupancy of its 4x4x4 bricks
   half4* light;
@@ -101,17 +107,24 @@ enum {
   RED_P_SUM = 1,
   RED_RHS_NORM2 = 2,
   RED_RES_NORM2 = 3,
-  RED_DEFECT_NORM2 = 4,   // base of per-outer-iteration defect norms
+  RED_DEFECT_NORM2 = 4,   // ||r||^2: [0] the mixed round's residual, [1] the cycle's
   RED_COUNT = 4 + 32
 };
 enum {
   REDU_MAXDIV = 0,
   REDU_ALIVE = 1,
   REDU_DONE = 2,          // defect loop converged (kernels of later iterations exit)
-  REDU_ITERS = 3,         // defect iterations executed
-  REDU_DEFECT_MAX = 8,    // base of per-outer-iteration max |r| (float bits)
+  REDU_ITERS = 3,         // mixed solve: rounds that corrected the pressure
+  REDU_INNER_DONE = 4,    // mixed solve: the round's V-cycles have converged (their kernels exit)
+  REDU_VCYCLES = 5,       // mixed solve: V-cycles completed in the step
+  REDU_INNER_ITERS = 6,   // mixed solve: V-cycles begun in the current round
+  REDU_DEFECT_MAX = 8,    // max |r| (float bits): [0] the round's residual, [1] the cycle's
   REDU_COUNT = 8 + 32
 };
+// the mixed solve: at most this many rounds (error-free residuals) per step,
+// and V-cycles per round
+constexpr int kMixedMaxRounds = 4;
+constexpr int kMixedMaxCycles = 16;
 
 // ---- block reductions ---------------------------------------------------------------
 __device__ __forceinline__ double warp_sum(double v) {
@@ -234,10 +247,15 @@ void launch_project_center_box(const DevState& s, cudaStream_t st, float scale =
                                unsigned int* maxbits = nullptr);
 void launch_divergence(const DevState& s, float* out, float scale, unsigned int* maxbits, cudaStream_t st);
 // bracket: also write the minimum and maximum of the predictor's 8 dye taps
-// (closed box) for launch_dye_resolve_lim
-void launch_conc_predict(const DevState& s, cudaStream_t st, bool bracket = false);
+// (closed box) for launch_dye_resolve_lim.  sparse (reference mode, inside a
+// step, where the centre velocity is bounded by the projection's clamp):
+// skip the blocks the dye-brick flags show to be clear water (same results).
+// Both kernels always maintain the flags of what they write.
+void launch_conc_predict(const DevState& s, cudaStream_t st, bool bracket = false, bool sparse = false);
 void launch_dye_resolve_lim(const DevState& s, cudaStream_t st);
-void launch_conc_resolve(const DevState& s, cudaStream_t st);
+void launch_conc_resolve(const DevState& s, cudaStream_t st, bool sparse = false);
+// number of 8x8x8 dye bricks (one uint32 flag each)
+size_t dye_brick_count(const Grid& gc);
 
 // Largest coarsest grid solved exactly by the dense inverse (64 MB of FP32),
 // and the size the closed-box configuration deepens its hierarchy to: one

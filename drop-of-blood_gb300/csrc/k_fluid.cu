@@ -468,19 +468,82 @@ __global__ void __launch_bounds__(256) k_divergence(Grid g, int ref, const VS* _
   if (maxbits) block_max_atomic(m, maxbits);
 }
 
+// ---- sparse dye bricks (reference mode) ------------------------------------------------------
+// Most of the 192x256x192 dye grid is clear water.  Per 8x8x8 brick of the
+// dye grid the predictor records whether any of its values is nonzero, and
+// the resolve whether any lysed value (.y, the only channel the predictor
+// reads) of its output is.  Inside a step the predictor skips a block whose
+// departure points can only reach bricks without lysed dye (its result
+// there is exactly +0), and the resolve skips the voxels of a block that
+// sees no predictor value within one voxel and no splat (its early-out
+// writes exactly zeros there).  Flags are plain stores of 1 (a race between
+// writers of the same value is harmless); the launchers clear them first.
+constexpr int kDyeBrick = 8;
+// |centre velocity| per axis inside a step: the projection clamps the faces
+// to +-2 (fluid.ts:908) and the centre is their mean (with a margin)
+constexpr float kDyeSpeedBound = 2.0f * 1.0001f;
+__host__ __device__ __forceinline__ Grid brick_grid(const Grid& gc) {
+  return Grid{(gc.nx + kDyeBrick - 1) / kDyeBrick, (gc.ny + kDyeBrick - 1) / kDyeBrick,
+              (gc.nz + kDyeBrick - 1) / kDyeBrick};
+}
+__device__ __forceinline__ void mark_brick(const Grid& gc, uint32_t* flags, int x, int y, int z) {
+  flags[brick_grid(gc).at(x / kDyeBrick, y / kDyeBrick, z / kDyeBrick)] = 1u;
+}
+// Whether any brick overlapping the block's voxels, widened by rx, ry, rz
+// voxels per axis, is flagged (block-uniform; every thread must call it).
+__device__ __forceinline__ bool block_any_brick(const Grid& gc, const uint32_t* flags, int rx, int ry, int rz) {
+  __shared__ int any;
+  const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+  if (tid == 0) any = 0;
+  __syncthreads();
+  const int x0 = max((int)(blockIdx.x * blockDim.x) - rx, 0);
+  const int x1 = min((int)(blockIdx.x * blockDim.x + blockDim.x) - 1 + rx, gc.nx - 1);
+  const int y0 = max((int)(blockIdx.y * blockDim.y) - ry, 0);
+  const int y1 = min((int)(blockIdx.y * blockDim.y + blockDim.y) - 1 + ry, gc.ny - 1);
+  const int z0 = max((int)blockIdx.z - rz, 0), z1 = min((int)blockIdx.z + rz, gc.nz - 1);
+  const Grid b = brick_grid(gc);
+  const int bx0 = x0 / kDyeBrick, by0 = y0 / kDyeBrick, bz0 = z0 / kDyeBrick;
+  const int nbx = x1 / kDyeBrick - bx0 + 1, nby = y1 / kDyeBrick - by0 + 1, nbz = z1 / kDyeBrick - bz0 + 1;
+  const int count = nbx * nby * nbz;
+  for (int k = tid; k < count; k += blockDim.x * blockDim.y) {
+    const int ix = k % nbx, iy = (k / nbx) % nby, iz = k / (nbx * nby);
+    if (__ldg(flags + b.at(bx0 + ix, by0 + iy, bz0 + iz))) any = 1;
+  }
+  __syncthreads();
+  return any != 0;
+}
+// The predictor's reach: RK2 departures move at most `speed` dt per axis in
+// world units, plus one voxel for the interpolation's taps.
+__device__ __forceinline__ bool block_reaches_dye(const Grid& gc, const StepParams& P, const uint32_t* cbrick,
+                                                  float speed) {
+  const float d = speed * P.dt;
+  const int rx = (int)ceilf(d * (float)gc.nx / P.dsize[0]) + 1;
+  const int ry = (int)ceilf(d * (float)gc.ny / P.dsize[1]) + 1;
+  const int rz = (int)ceilf(d * (float)gc.nz / P.dsize[2]) + 1;
+  return block_any_brick(gc, cbrick, rx, ry, rz);
+}
+
 // ---- CONC_PREDICT (advect.ts:28-72) -----------------------------------------------------------
 template <class VS, class DS>
 __global__ void __launch_bounds__(256, 8) k_conc_predict(Grid gc, Grid g, const StepParams* __restrict__ Pp, int ref,
                                                       const typename Vec4Of<VS>::type* __restrict__ cen,
                                                       const typename Vec4Of<DS>::type* __restrict__ conc4,
                                                       const DS* __restrict__ dye, DS* __restrict__ pred,
-                                                      DS* __restrict__ lim) {
+                                                      DS* __restrict__ lim, const uint32_t* __restrict__ cbrick,
+                                                      uint32_t* __restrict__ pbrick) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int z = blockIdx.z;
+  const StepParams& P = *Pp;
+  // reference mode inside a step (the centre velocity there comes from faces
+  // clamped to +-2 by the projection): a block whose departure points can
+  // only reach dye bricks with no lysed dye writes zeros without tracing
+  if (cbrick && !block_reaches_dye(gc, P, cbrick, kDyeSpeedBound)) {
+    if (x < gc.nx && y < gc.ny) stf(pred + gc.at(x, y, z), 0.0f);
+    return;
+  }
   if (x >= gc.nx || y >= gc.ny) return;
   const size_t i = gc.at(x, y, z);
-  const StepParams& P = *Pp;
   const Recip3 dims = recip3(v3((float)gc.nx, (float)gc.ny, (float)gc.nz));
   const float dtv = P.dt;
   const Recip3 dom = recip3(dsize_of(P));
@@ -489,7 +552,12 @@ __global__ void __launch_bounds__(256, 8) k_conc_predict(Grid gc, Grid g, const 
     if (x == 0 || x >= gc.nx - 1 || z == 0 || z >= gc.nz - 1 || y >= gc.ny - 1) { stf(pred + i, 0.0f); return; }
     const dob_v3 v0 = sample_center(g, cen, uvw);
     const float speed2 = dot3(v0, v0);
-    if (speed2 < 2.5e-5f) { stf(pred + i, ld4(conc4 + i).y); return; }
+    if (speed2 < 2.5e-5f) {
+      const float pv = ld4(conc4 + i).y;
+      stf(pred + i, pv);
+      if (pbrick && pv != 0.0f) mark_brick(gc, pbrick, x, y, z);
+      return;
+    }
     dob_v3 back;
     if (speed2 < 0.012f) {
       back = clamp3(uvw - (v0 * dtv) / dom, 0.001f, 0.999f);
@@ -499,7 +567,9 @@ __global__ void __launch_bounds__(256, 8) k_conc_predict(Grid gc, Grid g, const 
       back = clamp3(uvw - (vMid * dtv) / dom, 0.001f, 0.999f);
     }
     const Taps t = make_taps(gc, back.x, back.y, back.z);
-    stf(pred + i, lerp8x4(t, conc4).y);
+    const float pv = lerp8x4(t, conc4).y;
+    stf(pred + i, pv);
+    if (pbrick && pv != 0.0f) mark_brick(gc, pbrick, x, y, z);
   } else {
     const dob_v3 v0 = gc.nx == g.nx ? center_at_cell(g, cen, uvw, x, y, z, i) : sample_center(g, cen, uvw);
     const dob_v3 mid = clamp3(uvw - (0.5f * (v0 * dtv)) / dom, 0.001f, 0.999f);
@@ -532,16 +602,20 @@ __device__ __forceinline__ float intact_raw(const Grid& gc, const uint32_t* s, i
 }
 
 template <class VS, class DS>
-__global__ void __launch_bounds__(256) k_conc_resolve_ref(Grid gc, Grid g, const StepParams* __restrict__ Pp,
+__global__ void __launch_bounds__(256, 3) k_conc_resolve_ref(Grid gc, Grid g, const StepParams* __restrict__ Pp,
                                                           const typename Vec4Of<VS>::type* __restrict__ cen,
                                                           const typename Vec4Of<DS>::type* __restrict__ conc,
                                                           const DS* __restrict__ pred,
                                                           const uint32_t* __restrict__ splatI,
                                                           const uint32_t* __restrict__ splatL,
-                                                          typename Vec4Of<DS>::type* __restrict__ out) {
+                                                          typename Vec4Of<DS>::type* __restrict__ out,
+                                                          const uint32_t* __restrict__ pbrick,
+                                                          uint32_t* __restrict__ cbrick_out) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int z = blockIdx.z;
+  // inside a step: no predictor value within one voxel of the block
+  const bool clear = pbrick && !block_any_brick(gc, pbrick, 1, 1, 1);
   if (x >= gc.nx || y >= gc.ny) return;
   const size_t i = gc.at(x, y, z);
   if (x == 0 || x >= gc.nx - 1 || z == 0 || z >= gc.nz - 1 || y >= gc.ny - 1) {
@@ -552,6 +626,11 @@ __global__ void __launch_bounds__(256) k_conc_resolve_ref(Grid gc, Grid g, const
   const dob_v3 dims = v3((float)gc.nx, (float)gc.ny, (float)gc.nz);
   const uint32_t rawIntact = __ldg(splatI + i), rawLysed = __ldg(splatL + i);
   const bool inFloorZone = y <= 7;
+  // the early-out below with oct0 = oct1 = 0 (every predictor tap is +0)
+  if (clear && !inFloorZone && rawIntact == 0u && rawLysed == 0u) {
+    st4(out + i, make_float4(0.f, 0.f, 0.f, 0.f));
+    return;
+  }
   if (rawIntact == 0u && rawLysed == 0u) {
     const dob_v3 g0 = v3((float)x, (float)y, (float)z) / dims;
     const dob_v3 g1 = (v3((float)x, (float)y, (float)z) + v3(1.0f, 1.0f, 1.0f)) / dims;
@@ -655,6 +734,7 @@ __global__ void __launch_bounds__(256) k_conc_resolve_ref(Grid gc, Grid g, const
     vOx = rawOx * (1.0f - 0.82f * bedFrac);
   }
   st4(out + i, make_float4(cIntact, cLysed, vOx, cBed));
+  if (cLysed != 0.0f) mark_brick(gc, cbrick_out, x, y, z);
 }
 
 // Closed box: MacCormack correction of the single dye, 8-tap min/max limiter.
@@ -788,12 +868,21 @@ void launch_divergence(const DevState& s, float* out, float scale, unsigned int*
   });
 }
 
-void launch_conc_predict(const DevState& s, cudaStream_t st, bool bracket) {
+// the dye-brick flags of a dye buffer (reference mode)
+static uint32_t* brick_flags_of(const DevState& s, const void* conc) {
+  return conc == s.concA ? s.cbrickA : s.cbrickB;
+}
+size_t dye_brick_count(const Grid& gc) { return brick_grid(gc).n(); }
+
+void launch_conc_predict(const DevState& s, cudaStream_t st, bool bracket, bool sparse) {
+  uint32_t* pb = s.ref ? s.pbrick : nullptr;
+  if (pb) cudaMemsetAsync(pb, 0, brick_grid(s.gc).n() * sizeof(uint32_t), st);
+  const uint32_t* cb = s.ref && sparse ? brick_flags_of(s, s.conc) : nullptr;
   DOB_VEL_DISPATCH(s.prec, {
     k_conc_predict<VS, DS><<<cell_grid(s.gc), cell_block(), 0, st>>>(
         s.gc, s.g, s.params, s.ref, (const typename Vec4Of<VS>::type*)s.cen,
         (const typename Vec4Of<DS>::type*)s.conc, (const DS*)s.conc, (DS*)s.pred,
-        bracket && !s.ref ? (DS*)s.lim : nullptr);
+        bracket && !s.ref ? (DS*)s.lim : nullptr, cb, pb);
   });
 }
 
@@ -805,12 +894,15 @@ void launch_dye_resolve_lim(const DevState& s, cudaStream_t st) {
   });
 }
 
-void launch_conc_resolve(const DevState& s, cudaStream_t st) {
+void launch_conc_resolve(const DevState& s, cudaStream_t st, bool sparse) {
+  uint32_t* cb = s.ref ? brick_flags_of(s, s.conc2) : nullptr;
+  if (cb) cudaMemsetAsync(cb, 0, brick_grid(s.gc).n() * sizeof(uint32_t), st);
   DOB_VEL_DISPATCH(s.prec, {
     if (s.ref) {
       k_conc_resolve_ref<VS, DS><<<cell_grid(s.gc), cell_block(), 0, st>>>(
           s.gc, s.g, s.params, (const typename Vec4Of<VS>::type*)s.cen, (const typename Vec4Of<DS>::type*)s.conc,
-          (const DS*)s.pred, s.splatI, s.splatL, (typename Vec4Of<DS>::type*)s.conc2);
+          (const DS*)s.pred, s.splatI, s.splatL, (typename Vec4Of<DS>::type*)s.conc2, sparse ? s.pbrick : nullptr,
+          cb);
     } else {
       k_dye_resolve_box<VS, DS><<<cell_grid(s.gc), cell_block(), 0, st>>>(
           s.gc, s.g, s.params, (const typename Vec4Of<VS>::type*)s.cen, (const DS*)s.conc, (const DS*)s.pred,

@@ -275,17 +275,12 @@ __device__ __forceinline__ Row4 ld_row4(const T* a, uint32_t half, uint32_t r, u
 // the (dz, dy, dx) averaging order match k_residual_restrict.  1/h2 is a power
 // of two, so scaling by it equals the division.  Capped at 64 registers (4
 // blocks per SM): 17.2 -> 16.0 us at 192x256x192.
+// The body of k_residual_restrict2 for coarse cells X = 2q, 2q+1 of coarse
+// row (Y, Z); rr / ra (optional) accumulate r^2 and max |r| of the fine cells.
 template <class T, class TC>
-__global__ void __launch_bounds__(256, 4) k_residual_restrict2(Grid f, Grid c, float inv_h2, int ref,
-                                                            const T* __restrict__ a, const T* __restrict__ b,
-                                                            TC* __restrict__ bc, const unsigned int* __restrict__ skip) {
-  pdl_wait();
-  pdl_trigger();
-  if (skip_now(skip)) return;
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  const int Y = blockIdx.y * blockDim.y + threadIdx.y;
-  const int Z = blockIdx.z;
-  if (2 * q >= c.nx || Y >= c.ny) return;
+__device__ __forceinline__ void restrict_pair(Grid f, Grid c, float inv_h2, int ref, const T* __restrict__ a,
+                                              const T* __restrict__ b, TC* __restrict__ bc, int q, int Y, int Z,
+                                              float* rr, float* ra) {
   const uint32_t hx = (uint32_t)f.nx >> 1, half = (uint32_t)(f.n() >> 1), sz = (uint32_t)f.ny * hx;
   const uint32_t w = 2u * (uint32_t)q;
   const int y0 = 2 * Y, z0 = 2 * Z;
@@ -346,7 +341,12 @@ __global__ void __launch_bounds__(256, 4) k_residual_restrict2(Grid f, Grid c, f
         sumN = fmaf(wzp, Pzp.v[i], sumN);
         const float diag = dyz + (wxm + wxp);
         const float lap = (sumN - diag * P.v[i]) * inv_h2;
-        sum[i >> 1] = sum[i >> 1] + (Bb[dz][dy].v[i] - lap);
+        const float res = Bb[dz][dy].v[i] - lap;
+        sum[i >> 1] = sum[i >> 1] + res;
+        if (rr) {
+          *rr = fmaf(res, res, *rr);
+          *ra = fmaxf(*ra, fabsf(res));
+        }
       }
     }
   const uint32_t hc = (uint32_t)c.nx >> 1, halfc = (uint32_t)(c.n() >> 1);
@@ -354,6 +354,30 @@ __global__ void __launch_bounds__(256, 4) k_residual_restrict2(Grid f, Grid c, f
   const int pc = (Y + Z) & 1;  // colour of coarse X = 2q
   stf(bc + (pc ? halfc : 0u) + rc, sum[0] * 0.125f);
   stf(bc + (pc ? 0u : halfc) + rc, sum[1] * 0.125f);
+}
+
+// norm2 / maxbits (RED, the mixed solve's convergence test): also ||r||^2
+// and max |r| over the fine cells, one FP64 add and one max per block.
+template <class T, class TC, bool RED>
+__global__ void __launch_bounds__(256, 4) k_residual_restrict2(Grid f, Grid c, float inv_h2, int ref,
+                                                            const T* __restrict__ a, const T* __restrict__ b,
+                                                            TC* __restrict__ bc, const unsigned int* __restrict__ skip,
+                                                            double* __restrict__ norm2, unsigned int* __restrict__ maxbits) {
+  pdl_wait();
+  pdl_trigger();
+  if (skip_now(skip)) return;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int Y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int Z = blockIdx.z;
+  if (RED) {  // the reduction needs every thread of the block at its barrier
+    float rr = 0.0f, ra = 0.0f;
+    if (2 * q < c.nx && Y < c.ny) restrict_pair<T, TC>(f, c, inv_h2, ref, a, b, bc, q, Y, Z, &rr, &ra);
+    block_sum_atomic_f(rr, norm2);
+    block_max_atomic(ra, maxbits);
+    return;
+  }
+  if (2 * q >= c.nx || Y >= c.ny) return;
+  restrict_pair<T, TC>(f, c, inv_h2, ref, a, b, bc, q, Y, Z, nullptr, nullptr);
 }
 
 // MG_PROLONG_ADD, two coarse cells per thread (and ZC coarse planes per
@@ -829,33 +853,70 @@ __global__ void __launch_bounds__(256) k_defect_df4(Grid d, int ref, const float
   if (maxbits) block_max_atomic(ra, maxbits);
 }
 
-// One check of the defect loop: converged when max |r| <= div_tol_r and
-// ||r|| <= rel_tol ||b|| (a zero tolerance switches its test off).  On
-// convergence it sets the skip flag the rest of the iteration reads; it
-// counts corrections and stops the loop after max_outer of them.  Inside a
-// captured graph the loop is a conditional while-node and `cond` ends it;
-// the reduction slots are cleared for the next iteration.
-__global__ void k_defect_check(unsigned int* __restrict__ maxbits, double* __restrict__ rnorm2,
-                               const double* __restrict__ bnorm2, float div_tol_r, double rel_tol, int max_outer,
-                               unsigned int* __restrict__ done, unsigned int* __restrict__ iters,
-                               cudaGraphConditionalHandle cond, int use_cond) {
-  if (*done) {
-    if (use_cond) cudaGraphSetConditional(cond, 0u);
-    return;
-  }
+// Convergence test of the mixed solve: max |r| <= div_tol_r and ||r|| <=
+// rel_tol ||b|| (a zero tolerance switches its test off).  The tested slots
+// are cleared for the next accumulation.
+__device__ __forceinline__ bool mixed_converged(unsigned int* maxbits, double* rnorm2, const double* bnorm2,
+                                                float div_tol_r, double rel_tol) {
   const bool div_ok = div_tol_r <= 0.0f || __uint_as_float(*maxbits) <= div_tol_r;
   const double rn = sqrt(*rnorm2), bn = sqrt(*bnorm2);
   const bool rel_ok = rel_tol <= 0.0 || bn == 0.0 || rn <= rel_tol * bn;
   *maxbits = 0u;
   *rnorm2 = 0.0;
-  if (div_ok && rel_ok) {
+  return div_ok && rel_ok;
+}
+
+// Test of a round's error-free residual r0 = b - A (p + plo).  Converged (or
+// an earlier round was): `done` and `inner_done` make every later kernel of
+// the solve return at once (the round's first cycle test then leaves its
+// loop off).  Otherwise the round counts, its cycle counter starts at the
+// `untested` cycles that open it, which count as completed V-cycles.
+__global__ void k_mixed_round_check(unsigned int* __restrict__ maxbits, double* __restrict__ rnorm2,
+                                    const double* __restrict__ bnorm2, float div_tol_r, double rel_tol,
+                                    unsigned int* __restrict__ done, unsigned int* __restrict__ inner_done,
+                                    unsigned int* __restrict__ rounds, unsigned int* __restrict__ inner_iters,
+                                    unsigned int* __restrict__ vcycles, int untested) {
+  if (*done) {
+    *inner_done = 1u;
+    return;
+  }
+  if (mixed_converged(maxbits, rnorm2, bnorm2, div_tol_r, rel_tol)) {
     *done = 1u;
+    *inner_done = 1u;
+    return;
+  }
+  *rounds = *rounds + 1u;
+  *inner_done = 0u;
+  *inner_iters = (unsigned int)untested;
+  *vcycles = *vcycles + (unsigned int)untested;
+}
+
+// Test of the correction after a V-cycle's level-0 pre-smoothing, on the
+// residual r0 - A e that the restriction formed: converged -> `inner_done`
+// (the round's remaining kernels return at once where they read it) and the
+// loop ends.  Otherwise the cycle goes on; the loop ends once max_cycles
+// cycles have begun.  The first test of a round comes before its loop;
+// `completes`: the test closes a loop iteration, which completed a cycle.
+__global__ void k_mixed_cycle_check(unsigned int* __restrict__ maxbits, double* __restrict__ rnorm2,
+                                    const double* __restrict__ bnorm2, float div_tol_r, double rel_tol,
+                                    int max_cycles, int completes, unsigned int* __restrict__ inner_done,
+                                    unsigned int* __restrict__ inner_iters, unsigned int* __restrict__ vcycles,
+                                    cudaGraphConditionalHandle cond, int use_cond) {
+  if (*inner_done) {
+    *maxbits = 0u;
+    *rnorm2 = 0.0;
     if (use_cond) cudaGraphSetConditional(cond, 0u);
     return;
   }
-  const unsigned int n = *iters + 1u;
-  *iters = n;
-  if (use_cond && n >= (unsigned int)max_outer) cudaGraphSetConditional(cond, 0u);  // this correction is the last
+  const unsigned int n = *inner_iters + 1u;  // the cycle this pre-smoothing began
+  *inner_iters = n;
+  if (completes) *vcycles = *vcycles + 1u;   // the loop body completed the previous cycle
+  if (mixed_converged(maxbits, rnorm2, bnorm2, div_tol_r, rel_tol) || n > (unsigned int)max_cycles) {
+    *inner_done = 1u;
+    if (use_cond) cudaGraphSetConditional(cond, 0u);
+    return;
+  }
+  if (use_cond) cudaGraphSetConditional(cond, 1u);
 }
 
 // (p, plo) += e, error-free (same split layout)
@@ -958,12 +1019,19 @@ static inline dim3 pair_grid(const Grid& c, const dim3& b) {
   const int q = c.nx / 2;
   return dim3((q + b.x - 1) / b.x, (c.ny + b.y - 1) / b.y, c.nz);
 }
+// norm2 / maxbits: also reduce ||r||^2 and max |r| of level l's residual
+// (the mixed solve's convergence test)
 template <class T, class TC = T>
 static void restrict_level(const DevState& s, int l, const T* x, const T* b, TC* bc, const unsigned int* skip,
-                           cudaStream_t st) {
+                           cudaStream_t st, double* norm2 = nullptr, unsigned int* maxbits = nullptr) {
   const Grid f = s.lv[l].d, c = s.lv[l + 1].d;  // nx % 4 == 0 on every transfer level
   const dim3 bp = pair_block(c);
-  launch_pdl(k_residual_restrict2<T, TC>, pair_grid(c, bp), bp, 0, st, f, c, 1.0f / s.lv[l].h2, s.ref, x, b, bc, skip);
+  if (norm2)
+    launch_pdl(k_residual_restrict2<T, TC, true>, pair_grid(c, bp), bp, 0, st, f, c, 1.0f / s.lv[l].h2, s.ref, x, b,
+               bc, skip, norm2, maxbits);
+  else
+    launch_pdl(k_residual_restrict2<T, TC, false>, pair_grid(c, bp), bp, 0, st, f, c, 1.0f / s.lv[l].h2, s.ref, x, b,
+               bc, skip, norm2, maxbits);
 }
 static inline dim3 quad_grid(const Grid& d, const dim3& b) {
   const int q = d.nx / 8;
@@ -1145,24 +1213,6 @@ static void mix_restrict(const DevState& s, int l, const MixLv* M, const unsigne
   else if (M[l + 1].h) restrict_level<float, __nv_bfloat16>(s, l, M[l].ef, M[l].bf, M[l + 1].bh, skip, st);
   else restrict_level<float, float>(s, l, M[l].ef, M[l].bf, M[l + 1].bf, skip, st);
 }
-static void mix_vcycle(const DevState& s, const MixLv* M, bool zero0, const unsigned int* skip, cudaStream_t st) {
-  const int L = s.nlev;
-  if (L == 1) {
-    mix_smooth(s, 0, M, s.pre + s.post, zero0, false, skip, st);
-    return;
-  }
-  mix_smooth(s, 0, M, s.pre0, zero0, false, skip, st);
-  mix_restrict(s, 0, M, skip, st);
-  for (int l = 1; l < L - 1; ++l) {
-    mix_smooth(s, l, M, s.pre, true, false, skip, st);
-    mix_restrict(s, l, M, skip, st);
-  }
-  if (M[L - 1].h) coarse_solve<__nv_bfloat16>(s, L - 1, M[L - 1].eh, M[L - 1].bh, skip, st);
-  else coarse_solve<float>(s, L - 1, M[L - 1].ef, M[L - 1].bf, skip, st);
-  for (int l = L - 2; l >= 1; --l) mix_smooth(s, l, M, s.post, false, true, skip, st);
-  mix_smooth(s, 0, M, s.post0, false, true, skip, st);
-}
-
 double smoother_pass(const DevState& s, cudaStream_t st) {
   smooth<float, float>(s, 0, s.p, s.rhs, 1, false, nullptr, nullptr, st);
   // a red and a black half-sweep each read the other colour's half and their
@@ -1193,12 +1243,26 @@ void launch_residual_norm(const DevState& s, double* out, cudaStream_t st) {
   defect(s, nullptr, out, nullptr, nullptr, st);
 }
 
-// Mixed precision: defect correction.  Each outer iteration forms the
-// residual of the double-float pressure, stops the loop (device flag: the
-// kernels of the remaining iterations return at once, so the step stays one
-// captured graph) once max |r| and/or ||r|| / ||b|| meet their targets, else
-// solves A e = r with `cycles` V-cycles from zero (FP32 levels 0-1, BF16
-// coarser) and adds e to the pressure without rounding loss.
+// Mixed precision: rounds of defect correction.  Each round forms the
+// residual r0 = b - A (p + plo) of the double-float pressure without
+// rounding loss and tests it (k_mixed_round_check): converged -> this and
+// every later round return at once (device flags, so the step stays one
+// captured graph).  Otherwise the round solves A e = r0 by V-cycles on e
+// from zero (FP32 levels 0-1, BF16 coarser) and tests, after each cycle's
+// level-0 pre-smoothing, the residual r0 - A e that the restriction forms
+// anyway (k_residual_restrict2 with its reductions, k_mixed_cycle_check),
+// stopping there once it meets the targets; then (p, plo) += e without
+// rounding loss.  The correction is small against p, so its FP32 residual
+// has no rounding floor at the targets: the error-free residual is formed
+// once per round (usually one round per step), not once per V-cycle, and no
+// separate check pass runs.  The first round may open with `mg_cycles`
+// untested cycles that read no flag.  Inside a stream capture each round's
+// loop is a conditional while-node rotated so that each iteration ends at a
+// test (body: the rest of a cycle, then the next cycle's pre-smoothing,
+// restriction and test), so its kernels read no skip flag; the round's
+// first test, before the loop, switches it on.  Outside a capture,
+// kMixedMaxCycles iterations per round are enqueued and the kernels after
+// convergence return at once.
 static void mixed_solve(const DevState& s, cudaStream_t st) {
   const size_t n = s.g.n();
   MixLv M[kMaxLevels];
@@ -1208,47 +1272,87 @@ static void mixed_solve(const DevState& s, cudaStream_t st) {
     M[l] = {h ? nullptr : s.lv[l].e, h ? nullptr : s.lv[l].b, h ? s.lv[l].eh : nullptr, h ? s.lv[l].bh : nullptr, h};
   }
   unsigned int* done = s.redu + REDU_DONE;
-  double* rn2 = s.red + RED_DEFECT_NORM2;
-  unsigned int* rmax = s.redu + REDU_DEFECT_MAX;
-  cudaMemsetAsync(s.redu + REDU_DONE, 0, 2 * sizeof(unsigned int), st);  // done, iters
-  cudaMemsetAsync(rmax, 0, sizeof(unsigned int), st);
+  unsigned int* inner_done = s.redu + REDU_INNER_DONE;
+  double* bn2 = s.red + RED_RHS_NORM2;
+  double* rn2 = s.red + RED_DEFECT_NORM2;        // [0] round, [1] cycle
+  unsigned int* rmax = s.redu + REDU_DEFECT_MAX;  // [0] round, [1] cycle
+  cudaMemsetAsync(s.redu + REDU_DONE, 0, 5 * sizeof(unsigned int), st);  // done .. inner_iters
+  cudaMemsetAsync(rmax, 0, 2 * sizeof(unsigned int), st);
   cudaMemsetAsync(s.red + RED_RHS_NORM2, 0, sizeof(double) * (RED_COUNT - RED_RHS_NORM2), st);
-  k_sumsq64<<<s.num_sms * 4, 256, 0, st>>>(s.rhs, n, s.red + RED_RHS_NORM2);
-  auto iteration = [&](cudaStream_t q, cudaGraphConditionalHandle cond, int use_cond) {
-    defect(s, s.r0, rn2, rmax, done, q);
-    k_defect_check<<<1, 1, 0, q>>>(rmax, rn2, s.red + RED_RHS_NORM2, s.div_tol_r, s.rel_tol, s.max_outer, done,
-                                   s.redu + REDU_ITERS, cond, use_cond);
-    for (int c = 0; c < s.cycles; ++c) mix_vcycle(s, M, c == 0, done, q);
-    k_add_df<<<s.num_sms * 4, 256, 0, q>>>(s.p, s.plo, s.e0, n, done);
+  k_sumsq64<<<s.num_sms * 4, 256, 0, st>>>(s.rhs, n, bn2);
+  const int rounds = s.max_outer < 1 ? 1 : (s.max_outer > kMixedMaxRounds ? kMixedMaxRounds : s.max_outer);
+  const int L = s.nlev;  // >= 2 in the mixed mode
+  const int untested = s.cycles < 0 ? 0 : (s.cycles > kMixedMaxCycles ? kMixedMaxCycles : s.cycles);
+  // a cycle's level-0 pre-smoothing, restriction and test
+  auto head = [&](cudaStream_t q, const unsigned int* skip, cudaGraphConditionalHandle cond, int use_cond,
+                  int completes) {
+    mix_smooth(s, 0, M, s.pre0, false, false, skip, q);
+    restrict_level<float, float>(s, 0, M[0].ef, M[0].bf, M[1].bf, skip, q, rn2 + 1, rmax + 1);
+    k_mixed_cycle_check<<<1, 1, 0, q>>>(rmax + 1, rn2 + 1, bn2, s.div_tol_r, s.rel_tol, kMixedMaxCycles, completes,
+                                        inner_done, s.redu + REDU_INNER_ITERS, s.redu + REDU_VCYCLES, cond,
+                                        use_cond);
   };
-  // Inside a stream capture the loop becomes a conditional while-node, so a
-  // step runs only the iterations it needs; otherwise all max_outer
-  // iterations are enqueued and the converged ones return at once.
-  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-  cudaGraph_t graph = nullptr;
-  const cudaGraphNode_t* deps = nullptr;
-  size_t ndeps = 0;
-  if (s.aux && cudaStreamGetCaptureInfo(st, &cs, nullptr, &graph, &deps, nullptr, &ndeps) != cudaSuccess) {
-    cudaGetLastError();
-    cs = cudaStreamCaptureStatusNone;
-  }
-  if (cs == cudaStreamCaptureStatusActive) {
-    cudaGraphConditionalHandle cond;
-    cudaGraphConditionalHandleCreate(&cond, graph, 1u, cudaGraphCondAssignDefault);
-    cudaGraphNodeParams np = {};
-    np.type = cudaGraphNodeTypeConditional;
-    np.conditional.handle = cond;
-    np.conditional.type = cudaGraphCondTypeWhile;
-    np.conditional.size = 1;
-    cudaGraphNode_t node;
-    cudaGraphAddNode(&node, graph, deps, nullptr, ndeps, &np);
-    cudaGraph_t body = np.conditional.phGraph_out[0];
-    cudaStreamBeginCaptureToGraph(s.aux, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
-    iteration(s.aux, cond, 1);
-    cudaStreamEndCapture(s.aux, &body);
-    cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
-  } else {
-    for (int it = 0; it < s.max_outer; ++it) iteration(st, 0, 0);
+  // the rest of the cycle: coarser levels and the level-0 post-smoothing
+  auto tail = [&](cudaStream_t q, const unsigned int* skip) {
+    for (int l = 1; l < L - 1; ++l) {
+      mix_smooth(s, l, M, s.pre, true, false, skip, q);
+      mix_restrict(s, l, M, skip, q);
+    }
+    if (M[L - 1].h) coarse_solve<__nv_bfloat16>(s, L - 1, M[L - 1].eh, M[L - 1].bh, skip, q);
+    else coarse_solve<float>(s, L - 1, M[L - 1].ef, M[L - 1].bf, skip, q);
+    for (int l = L - 2; l >= 1; --l) mix_smooth(s, l, M, s.post, false, true, skip, q);
+    mix_smooth(s, 0, M, s.post0, false, true, skip, q);
+  };
+  for (int r = 0; r < rounds; ++r) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaGraph_t graph = nullptr;
+    if (s.aux && cudaStreamGetCaptureInfo(st, &cs, nullptr, &graph, nullptr, nullptr, nullptr) != cudaSuccess) {
+      cudaGetLastError();
+      cs = cudaStreamCaptureStatusNone;
+    }
+    const bool captured = cs == cudaStreamCaptureStatusActive;
+    cudaGraphConditionalHandle cond = 0;
+    // the loop runs only if the round's first test switches it on
+    if (captured) cudaGraphConditionalHandleCreate(&cond, graph, 0u, cudaGraphCondAssignDefault);
+    const int plain = r == 0 ? untested : 0;
+    defect(s, s.r0, rn2, rmax, done, st);
+    k_mixed_round_check<<<1, 1, 0, st>>>(rmax, rn2, bn2, s.div_tol_r, s.rel_tol, done, inner_done,
+                                         s.redu + REDU_ITERS, s.redu + REDU_INNER_ITERS, s.redu + REDU_VCYCLES,
+                                         plain);
+    // the first round's untested cycles (the first from e = 0) read no flag:
+    // a step whose pressure already meets the targets still runs them
+    for (int c = 0; c < plain; ++c) {
+      mix_smooth(s, 0, M, s.pre0, c == 0, false, nullptr, st);
+      restrict_level<float, float>(s, 0, M[0].ef, M[0].bf, M[1].bf, nullptr, st);
+      tail(st, nullptr);
+    }
+    if (plain == 0)
+      launch_pdl(k_fill_zero<float>, dim3(s.num_sms * 2), dim3(256), 0, st, s.e0, n, (const unsigned int*)done);
+    head(st, done, cond, captured ? 1 : 0, 0);
+    if (captured) {
+      const cudaGraphNode_t* deps = nullptr;
+      size_t ndeps = 0;
+      cudaStreamGetCaptureInfo(st, &cs, nullptr, &graph, &deps, nullptr, &ndeps);
+      cudaGraphNodeParams np = {};
+      np.type = cudaGraphNodeTypeConditional;
+      np.conditional.handle = cond;
+      np.conditional.type = cudaGraphCondTypeWhile;
+      np.conditional.size = 1;
+      cudaGraphNode_t node;
+      cudaGraphAddNode(&node, graph, deps, nullptr, ndeps, &np);
+      cudaGraph_t body = np.conditional.phGraph_out[0];
+      cudaStreamBeginCaptureToGraph(s.aux, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+      tail(s.aux, nullptr);
+      head(s.aux, nullptr, cond, 1, 1);
+      cudaStreamEndCapture(s.aux, &body);
+      cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+    } else {
+      for (int it = 0; it < kMixedMaxCycles; ++it) {
+        tail(st, inner_done);
+        head(st, inner_done, 0, 0, 1);
+      }
+    }
+    k_add_df<<<s.num_sms * 4, 256, 0, st>>>(s.p, s.plo, s.e0, n, done);
   }
   if (!s.ref) {
     cudaMemsetAsync(s.red + RED_P_SUM, 0, sizeof(double), st);

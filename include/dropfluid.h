@@ -57,8 +57,9 @@ enum {
 enum {
   DOB_PREC_FP32 = 0,           /* all fields FP32                                   */
   DOB_PREC_MIXED = 1,          /* FP16 dye; pressure as an FP32 pair (double-float)
-                                  corrected by an error-free residual loop whose
-                                  V-cycles store levels >= 2 as BF16                */
+                                  corrected by rounds of an error-free residual and
+                                  V-cycles on the correction that store levels >= 2
+                                  as BF16; needs mg_levels >= 2                      */
   DOB_PREC_REFERENCE_FP16 = 2  /* velocity/curl/dye stored as binary16 like the
                                   reference's rgba16float textures; pressure FP32  */
 };
@@ -101,8 +102,15 @@ typedef struct dob_config {
   int32_t mg_coarse_sweeps;    /* RBGS sweeps on the coarsest grid (reference: 6);
                                   -1: exact solve with a dense (pseudo-)inverse,
                                   coarsest grid of at most 4096 cells              */
-  int32_t mg_cycles;           /* V-cycles per step (reference: 1)                   */
-  int32_t mg_max_outer;        /* mixed mode: max defect-correction iterations       */
+  int32_t mg_cycles;           /* V-cycles per step (reference: 1); mixed mode: the
+                                  V-cycles the first round of a step runs before
+                                  its first convergence test (0: test from the
+                                  first cycle on)                                    */
+  int32_t mg_max_outer;        /* mixed mode: rounds of defect correction per step
+                                  (one error-free residual of the pressure each, then
+                                  up to 16 V-cycles on the correction, tested after
+                                  each finest-level pre-smoothing); at most 4 are
+                                  run, 1..32 accepted                                */
   double mg_rel_tol;           /* mixed mode: stop at ||b-Ap||/||b|| <= this (0: off)  */
   double mg_div_tol;           /* mixed mode: stop at max |b-Ap| (= the projected max
                                   |div u|) scaled like dob_step_stats.max_div <= this
