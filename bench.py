@@ -223,14 +223,25 @@ def wave_leg(peak):
         return {"error": f"{type(ex).__name__}: {ex}"}
 
 
-def fd64_check(sc, grads, target, d_imp, ndirs, seed=12345, h=1e-5, eps=1e-3):
+def impulse_step(w_cells, h, dx, dt):
+    """The injected face velocity is a float32: the scales 1 +- h reach the
+    fields as float32(v (1 +- h)) / v.  Returns the realised difference of
+    the two scales, the denominator of the central difference."""
+    import numpy as np
+    v = w_cells * dx / dt
+    return (float(np.float32(v * (1.0 + h))) - float(np.float32(v * (1.0 - h)))) / v
+
+
+def fd64_check(sc, grads, target, d_imp, ndirs, seed=12345, h=1e-5, eps=1e-6):
     """The device gradient of the box96 loss against central differences of
     the FP64 oracle's loss (the oracle in double arithmetic, the same scene,
-    V-cycles per step and target): the drop impulse (step h relative) and
-    the same seeded random directions of the initial MAC velocity as the
-    device check (step eps in world units, 1.3e-5 of the injected face
-    speed), small enough that the FP64 trajectory crosses no limiter or
-    clamp branch.  Each loss is 32 FP64 steps on the host cores."""
+    V-cycles per step and target), and the FP64 oracle's own adjoint against
+    the same differences: the drop impulse (scale 1 +- h, divided by the
+    realised float32 difference of the injected velocities) and the same
+    seeded random directions of the initial MAC velocity as the device check
+    (step eps in world units against face speeds of 75: small enough that
+    the FP64 trajectory crosses next to no limiter or clamp branch).  Each
+    loss is 32 FP64 steps on the host cores."""
     import numpy as np
     import oracle
     from dropfluid import abi, scenes
@@ -256,7 +267,8 @@ def fd64_check(sc, grads, target, d_imp, ndirs, seed=12345, h=1e-5, eps=1e-3):
         d = o.get_field64(abi.FIELD_CONC) - target
         return float(np.sum(d * d))
 
-    fd_imp = (loss64(scenes.box96(impulse_scale=1.0 + h)) - loss64(scenes.box96(impulse_scale=1.0 - h))) / (2 * h)
+    fd_imp = ((loss64(scenes.box96(impulse_scale=1.0 + h)) - loss64(scenes.box96(impulse_scale=1.0 - h))) /
+              impulse_step(sc.drops[0].w_cells_per_step, h, cfg.dx, cfg.dt))
     # the FP64 oracle's own discrete adjoint of its own trajectory
     o.reset()
     for j in sc.releases_at(0):
@@ -347,7 +359,7 @@ def adjoint_leg(fd_dirs: int = 16, fd64_dirs: int = 16):
     h = 1e-3
     lp = l2_loss(fwd(scenes.box96(impulse_scale=1.0 + h)), target)[0]
     lm = l2_loss(fwd(scenes.box96(impulse_scale=1.0 - h)), target)[0]
-    fd_imp = (lp - lm) / (2 * h)
+    fd_imp = (lp - lm) / impulse_step(sc.drops[0].w_cells_per_step, h, sc.config.dx, sc.config.dt)
     rng = np.random.default_rng(12345)
     eps = 1e-3 * 75.0  # 0.1 % of the injected face speed (1.5 cells/step = 75 world units)
     errs = []
@@ -659,6 +671,41 @@ def configs_report():
     return {"configs": out, "host_cores": ncores}
 
 
+# Algorithmic bytes of one closed-box step per velocity cell (every array a
+# stage reads read once, every array it writes written once): the stages
+# outside the pressure solve, and one V-cycle of 2+2 red-black sweeps (12 B
+# per cell and sweep) with its transfers (8.5 B each) on every level, levels
+# summed as L0 (1 + 1/8 + 1/64 + ...).  FP32 storage: advection 24, Casson 28,
+# divergence 16, projection 28, dye advection 20, parcels 2.7 (393216 x 64 B
+# over 192x256x192).  Mixed: FP16 dye (Casson 26, dye 16), BF16 levels >= 2
+# (half the bytes there), and per round the error-free residual (p, plo, b in,
+# r out: 16 B) and the update (e, p, plo in, p, plo out: 20 B); the tested
+# cycle cut short after its pre-smoothing and restriction adds 32.5 B.
+def step_bytes_per_cell(cycles, mixed=False, rounds=0, cut_short=0.0):
+    lev = [1.0, 1 / 8, 1 / 64, 1 / 512, 1 / 4096]
+    per_level = 4 * 12 + 8.5 + 8.5
+    if not mixed:
+        return 118.4 + cycles * per_level * sum(lev)
+    cyc = per_level * (lev[0] + lev[1]) + 0.5 * per_level * sum(lev[2:])
+    return 112.7 + cycles * cyc + rounds * (16 + 20) + cut_short * 32.5
+
+
+def headline_step_roofline(scene, start, n, steps_per_s):
+    """Step-level roofline of the FP32 window: V-cycles per step from the
+    release rule (mg_cycles_injected on the two steps after a release)."""
+    c = scene.config
+    cyc = []
+    for k in range(start, start + n):
+        after = any(0 <= k - d.release_step < 2 for d in scene.drops)
+        cyc.append(c.mg_cycles_injected if after else c.mg_cycles)
+    mean_c = sum(cyc) / len(cyc)
+    b = step_bytes_per_cell(mean_c) * c.nx * c.ny * c.nz
+    peak, src = measured_peaks()
+    gbs = b * steps_per_s / 1e9
+    return {"bytes_per_step": b, "vcycles_per_step": mean_c, "achieved_gbs": gbs, "frac": gbs / peak,
+            "peak_source": src, "model": "stage byte model per velocity cell (bench.step_bytes_per_cell)"}
+
+
 def release_note(scene, start, n):
     """Which drop releases (and their extra-cycle steps) a timed window holds."""
     rel = [d.release_step for d in scene.drops if start <= d.release_step < start + n]
@@ -722,6 +769,10 @@ def main():
                     help="error of the FP32 and mixed runs against an FP64 run at steps 50/100/200, then exit")
     ap.add_argument("--configs", action="store_true",
                     help="per-configuration GPU and host-core throughput (FP32, FP32 1 thread, FP64), then exit")
+    ap.add_argument("--profile-reference", action="store_true",
+                    help="run only the reference setup on the drop-lifecycle sequence (50 substeps, then --steps "
+                         "substeps, the light volume after each, untimed) and exit: the command the "
+                         "reference-mode ncu captures are taken with")
     ap.add_argument("--profile-run", action="store_true",
                     help="run only the FP32 scene (warm-up + steps, untimed) and exit: the command "
                          "the ncu launch lists and kernel captures are taken with")
@@ -742,6 +793,19 @@ def main():
     if args.configs:
         if rank == 0:
             print(json.dumps(configs_report()), flush=True)
+        return 0
+    if args.profile_reference:
+        import numpy as np
+        cfg = abi.config_reference()
+        cfg.physics_flags = abi.DOB_PHYS_REFERENCE_ALL | abi.DOB_PHYS_WAVE | abi.DOB_PHYS_LIGHTING
+        seq, reset, warm = reference_sequence(50)
+        with DropFluid(cfg) as e:
+            e.set_uniforms(reset)
+            e.reset()
+            e.step_uniforms(np.stack(warm))
+            for _ in range(args.steps):
+                e.step_uniforms(seq.advance_substep()[0][None])
+            e.sync()
         return 0
     dist = Dist(world)
 
@@ -809,19 +873,20 @@ def main():
             dist.barrier()
             ms_w = dist.max(run_scene_steps(scene, e, args.warmup, args.steps, timed=True))
             e.load_state(0)
-            divs, iters = [], []
+            divs, iters, cycs = [], [], []
             for k in range(args.warmup, args.warmup + args.steps):
                 for d in scene.releases_at(k):
                     scene.release(e, d)
                 stw = e.step(1, stats=True)
                 divs.append(stw["max_div"])
                 iters.append(stw["outer_iters"])
+                cycs.append(stw["vcycles"])
             e.close()
             v = world * args.steps / (ms_w / 1000.0)
             return {"value": v, "unit": "steps/s", "ms_per_step": ms_w / args.steps,
                     "max_div_max": max(divs), "max_div_median": statistics.median(divs),
                     "steps_div_le_1e-5": sum(1 for dv in divs if dv <= 1e-5), "steps": len(divs),
-                    "outer_iters_mean": statistics.mean(iters)}
+                    "outer_iters_mean": statistics.mean(iters), "vcycles_mean": statistics.mean(cycs)}
         # FP32 with a fixed number of V-cycles per step: the fewest cycles
         # that keep max |div| dt/dx <= 1e-5 on every step of the run (the
         # steps right after a drop release need more than the others) is the
@@ -834,16 +899,40 @@ def main():
         fp32_w, fp32_8 = fp32[4], fp32[8]
         ok = [c for c in sorted(fp32) if fp32[c]["steps_div_le_1e-5"] == fp32[c]["steps"]]
         at_div = ok[0] if ok else None
-        mx = window(scenes.box192(abi.DOB_PREC_MIXED))
+        # V-cycles run in the first round before its first convergence test
+        mixes = {}
+        for cyc in (0, 2, 3):
+            scm = scenes.box192(abi.DOB_PREC_MIXED)
+            scm.config.mg_cycles = cyc
+            mixes[cyc] = window(scm)
+        ok_m = [c for c in sorted(mixes) if mixes[c]["steps_div_le_1e-5"] == mixes[c]["steps"]]
+        best = max(ok_m, key=lambda c: mixes[c]["value"]) if ok_m else 0
+        mx = mixes[best]
         m8 = window(scenes.box192_mixed_1e8())
         mixed = dict(mx)
+        peak_w = measured_peaks()[0]
+        cells = 192 * 256 * 192
+
+        def step_roof(w, mixed_mode, cycles):
+            b = step_bytes_per_cell(cycles, mixed_mode, w.get("outer_iters_mean", 0),
+                                    1.0 if mixed_mode else 0.0) * cells
+            gbs = b * w["value"] / 1e9
+            return {"bytes_per_step": b, "achieved_gbs": gbs, "frac_of_measured_hbm": gbs / peak_w,
+                    "vcycles_per_step": cycles}
         mixed.update({
+            "step_roofline": step_roof(mx, True, mx["vcycles_mean"]),
+            "fp32_step_roofline": step_roof(fp32_w, False, 4),
+            "untested_cycles": best,
+            "by_untested_cycles": {str(c): {k: mixes[c][k] for k in ("value", "vcycles_mean", "max_div_max",
+                                                                     "steps_div_le_1e-5")} for c in mixes},
             "fp32_cycles_at_div_1e-5": at_div,
             "speedup_vs_fp32_at_div_1e-5": mx["value"] / fp32[at_div]["value"] if at_div else None,
             "speedup_vs_fp32": mx["value"] / fp32_w["value"],
             "speedup_vs_fp32_8cycles": mx["value"] / fp32_8["value"],
-            "precision": "FP16 dye; pressure as an FP32 pair (double-float) corrected by an error-free residual "
-                         "loop, 1 V-cycle per iteration with BF16 levels >= 2; stop at max |div| dt/dx <= 1e-5",
+            "precision": "FP16 dye; pressure as an FP32 pair (double-float); per round one error-free residual, "
+                         "then V-cycles on the correction (BF16 levels >= 2), untested_cycles of them untested, "
+                         "then tested on the restriction's residual until max |div| dt/dx <= 1e-5; "
+                         "outer_iters = rounds, vcycles = V-cycles",
             "fp32_4cycles": fp32_w, "fp32_5cycles": fp32[5], "fp32_6cycles": fp32[6], "fp32_8cycles": fp32_8,
             "mixed_rel_1e-8": m8,
         })
@@ -877,6 +966,7 @@ def main():
                                 "drop releases between segments untimed; "
                                 + release_note(sc, args.warmup, args.steps)},
             "cell_updates_per_s": value * 192 * 256 * 192,
+            "step_roofline": headline_step_roofline(sc, args.warmup, args.steps, value),
             "max_div": st["max_div"], "residual_l2": st["residual_l2"], "rhs_l2": st["rhs_l2"],
             "mixed": mixed,
             "adjoint_forward_ratio": adj["box96"]["ratio"] if adj else None,
