@@ -15,8 +15,9 @@ w * dx / dt):
            face, 393216 parcels split evenly, 200 steps.
   box192_mixed   box192 with FP16 dye and the mixed pressure solve: an
            error-free residual of the double-float pressure, then V-cycles on
-           the correction (BF16 levels 2-3), tested after each cycle's
-           finest-level pre-smoothing, until max |div| dt/dx <= 1e-5
+           the correction (BF16 levels 2-3; three untested, then tested after
+           each further cycle's finest-level pre-smoothing) until max |div|
+           dt/dx <= 1e-5
            (box192_mixed_1e8: also ||b - A p|| / ||b|| <= 1e-8).
   box96    96x128x96, one sphere r=8 with a seeded centre, w=-1.5 plus
            N(0, 0.05) per face like box192, 32 steps (the adjoint scene:
@@ -151,7 +152,7 @@ def box192(precision: int = abi.DOB_PREC_FP32, seed: int = 2024) -> Scene:
     cfg.precision_mode = precision
     cfg.parcel_capacity = 393216
     if precision == abi.DOB_PREC_MIXED:
-        cfg.mg_cycles = 0  # V-cycles of the first round before its first convergence test
+        cfg.mg_cycles = 3  # V-cycles of the first round before its first convergence test
     rng = SplitMix64(seed)
     r = 12.0
     drops = []
