@@ -386,18 +386,42 @@ def adjoint_leg(fd_dirs: int = 16, fd64_dirs: int = 16):
     eng.close()
     # ---- box192, three soft-edged drops at step 0, 64 steps, checkpoints every 16 --------------
     # gradient in the three impulses and the three release positions, each
-    # checked against central differences of the device loss
-    sc = scenes.box192_adjoint()
+    # checked against central differences of the device loss; in FP32 and in
+    # the mixed mode (whose gradients are also set against the FP32 ones)
+    out["box192"] = box192_adjoint(abi.DOB_PREC_FP32)
+    out["box192_mixed"] = box192_adjoint(abi.DOB_PREC_MIXED)
+    fp32, mx = out["box192"], out["box192_mixed"]
+    gi32, gim = np.asarray(fp32.pop("_impulse")), np.asarray(mx.pop("_impulse"))
+    gp32, gpm = np.asarray(fp32.pop("_position")), np.asarray(mx.pop("_position"))
+    mx["impulse_rel_diff_vs_fp32"] = float(np.max(np.abs(gim - gi32) / np.abs(gi32)))
+    mx["position_rel_diff_vs_fp32"] = float(max(np.linalg.norm(gpm[k] - gp32[k]) / np.linalg.norm(gp32[k])
+                                                 for k in range(len(gp32))))
+    return out
+
+
+def box192_adjoint(precision):
+    """Cost and drop gradients of the 64-step box192 trajectory (three
+    soft-edged drops at step 0, checkpoints every 16) in one precision mode:
+    backward / forward ratio, the recording forward per step, the impulse
+    and release-position gradients against central differences of the
+    device loss."""
+    import numpy as np
+    from dropfluid import DropFluid, abi, scenes
+    from dropfluid.adjoint import DropTrajectory, l2_loss
+
+    def scene(**kw):
+        return scenes.box192_adjoint(precision=precision, **kw)
+    sc = scene()
     eng = DropFluid(sc.config)
     traj = DropTrajectory(eng, 16)
 
-    def fwd192(scene):
+    def fwd192(sn):
         eng.reset()
-        for j in range(len(scene.drops)):
-            scene.release(eng, j)
-        return traj.forward(scene.steps)
+        for j in range(len(sn.drops)):
+            sn.release(eng, j)
+        return traj.forward(sn.steps)
     shifts = ((0.5, -0.3, 0.2), (-0.4, 0.2, 0.3), (0.3, 0.4, -0.5))
-    target = fwd192(scenes.box192_adjoint(impulse_scale=(1.1, 0.9, 1.05), shift=shifts)).astype(np.float64)
+    target = fwd192(scene(impulse_scale=(1.1, 0.9, 1.05), shift=shifts)).astype(np.float64)
     loss, g = l2_loss(fwd192(sc), target)
     traj.backward(g)  # first call captures the segment graphs
     eng.sync()
@@ -418,33 +442,39 @@ def adjoint_leg(fd_dirs: int = 16, fd64_dirs: int = 16):
         sp = [1.0] * 3
         sm = [1.0] * 3
         sp[k], sm[k] = 1.0 + h, 1.0 - h
-        fd = (l2_loss(fwd192(scenes.box192_adjoint(impulse_scale=sp)), target)[0] -
-              l2_loss(fwd192(scenes.box192_adjoint(impulse_scale=sm)), target)[0]) / (2 * h)
+        fd = (l2_loss(fwd192(scene(impulse_scale=sp)), target)[0] -
+              l2_loss(fwd192(scene(impulse_scale=sm)), target)[0]) / (2 * h)
         imp_err.append(abs(fd - drop_g[k]["impulse"]) / abs(fd))
         fdk = []
         for j in range(3):
             shp = [[0.0] * 3 for _ in range(3)]
             shm = [[0.0] * 3 for _ in range(3)]
             shp[k][j], shm[k][j] = eps, -eps
-            fd = (l2_loss(fwd192(scenes.box192_adjoint(shift=shp)), target)[0] -
-                  l2_loss(fwd192(scenes.box192_adjoint(shift=shm)), target)[0]) / (2 * eps)
+            fd = (l2_loss(fwd192(scene(shift=shp)), target)[0] -
+                  l2_loss(fwd192(scene(shift=shm)), target)[0]) / (2 * eps)
             fdk.append(fd)
         gp = drop_g[k]["position"]
         fd_pos.append(fdk)
         pos_err.append(float(np.linalg.norm(np.asarray(fdk) - gp) / np.linalg.norm(gp)))
-    out["box192"] = {"steps": sc.steps, "checkpoint_every": 16, "forward_step_ms": fwd_ms,
-                     "tape_forward_ms_per_step": 1e3 * t_tape_fwd192 / sc.steps,
-                     "backward_ms_per_step": 1e3 * t_bwd / sc.steps, "ratio": 1e3 * t_bwd / sc.steps / fwd_ms,
-                     "loss": loss, "drops": "three soft-edged drops (edge 2 cells) injected at step 0, 393216 parcels",
-                     "target": "same drops with impulses x(1.1, 0.9, 1.05) and centres shifted by up to 0.5 cells",
-                     "impulse_grad": [d["impulse"] for d in drop_g],
-                     "position_grad": [d["position"].tolist() for d in drop_g],
-                     "position_fd": fd_pos,
-                     "impulse_fd_rel_err_max": max(imp_err),
-                     "position_fd_rel_err_max": max(pos_err),
-                     "fd_steps": {"impulse": h, "position_world": eps}}
+    res = {"steps": sc.steps, "checkpoint_every": 16, "forward_step_ms": fwd_ms,
+           "tape_forward_ms_per_step": 1e3 * t_tape_fwd192 / sc.steps,
+           "backward_ms_per_step": 1e3 * t_bwd / sc.steps, "ratio": 1e3 * t_bwd / sc.steps / fwd_ms,
+           "gradient_cost_ratio": 1e3 * (t_tape_fwd192 + t_bwd) / sc.steps / fwd_ms,
+           "loss": loss, "drops": "three soft-edged drops (edge 2 cells) injected at step 0, 393216 parcels",
+           "target": "same drops with impulses x(1.1, 0.9, 1.05) and centres shifted by up to 0.5 cells",
+           "impulse_grad": [d["impulse"] for d in drop_g],
+           "position_grad": [d["position"].tolist() for d in drop_g],
+           "position_fd": fd_pos,
+           "impulse_fd_rel_err_max": max(imp_err),
+           "position_fd_rel_err_max": max(pos_err),
+           "fd_steps": {"impulse": h, "position_world": eps},
+           "_impulse": [d["impulse"] for d in drop_g], "_position": [d["position"] for d in drop_g]}
+    if precision == abi.DOB_PREC_MIXED:
+        res["precision"] = ("mixed: binary16 dye, pressure pair to max |div| dt/dx <= 1e-5; the adjoint reads the "
+                            "binary16 linearisation points and solves the pressure adjoint with the mixed solver "
+                            "to a relative residual of 1e-6")
     eng.close()
-    return out
+    return res
 
 
 ACC_STEPS = (50, 100, 200)

@@ -517,6 +517,7 @@ dob_status dob_create(const dob_config* cfg, dob_ctx** out) {
     A((void**)&s.bricks, N / 64 * sizeof(float));
   }
   A((void**)&s.red, RED_COUNT * sizeof(double));
+  A((void**)&s.part, PART_SLOTS * kSumBlocks * sizeof(double));
   A((void**)&s.redu, REDU_COUNT * sizeof(unsigned int));
   s.nlev = cfg->mg_levels;
   for (int l = 0; l < s.nlev; ++l) {

@@ -64,6 +64,7 @@ struct DevState {
   half4* light;
   float *brick_raw, *bricks;
   double* red;                   // FP64 reduction slots
+  double* part;                  // per-block partials of the mean removals: PART_SLOTS x kSumBlocks
   unsigned int* redu;            // u32 reduction slots / flags
   int nlev;
   MgLevel lv[kMaxLevels];
@@ -98,8 +99,12 @@ struct AdjState {
   float* le[kMaxLevels];   // coarse corrections (split, levels >= 1)
   float* lb[kMaxLevels];   // coarse right-hand sides (split, levels >= 1)
   float *alpha, *gq;       // Casson adjoint scratch: per-cell alpha, 2 dL/dQ
+  double* part;            // partial sums of the mean removals: 2 x kSumBlocks
+  float *lam, *lamlo;      // mixed mode: adjoint pressure solve's solution pair (split)
   double* red;             // FP64 reduction slots (mean removal)
 };
+// relative residual of the mixed mode's adjoint pressure solve
+constexpr double kAdjRelTol = 1e-6;
 
 // reduction slot indices in DevState::red / redu
 enum {
@@ -164,6 +169,33 @@ inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, s
   return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
 }
 
+// Deterministic FP64 sums (the mean removals, whose result enters the
+// state): each block stores its partial in its own slot of `part`
+// (block_sum_store) and the consumer adds the slots in a fixed order
+// (sum_partials), so the bits do not depend on the order in which blocks
+// finish, as one FP64 atomic per block would.
+constexpr int kSumBlocks = 1024;  // most blocks of a partial-sum launch (slots per array)
+enum { PART_RHS = 0, PART_P = 1, PART_SLOTS = 2 };
+__device__ __forceinline__ void block_sum_store(double v, double* part) {
+  __shared__ double wpart[32];
+  const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  const int nthreads = blockDim.x * blockDim.y * blockDim.z;
+  v = warp_sum(v);
+  if ((tid & 31) == 0) wpart[tid >> 5] = v;
+  __syncthreads();
+  if (tid < 32) {
+    double s = tid < (nthreads + 31) / 32 ? wpart[tid] : 0.0;
+    s = warp_sum(s);
+    if (tid == 0) part[blockIdx.x] = s;
+  }
+}
+// Sum of part[0, nb) in a fixed order; call from a whole warp (every lane
+// gets the same value: strided per-lane sums, then a butterfly).
+__device__ __forceinline__ double sum_partials(const double* part, int nb) {
+  double s = 0.0;
+  for (int i = threadIdx.x & 31; i < nb; i += 32) s += part[i];
+  return warp_sum(s);
+}
 // Sum `v` over the block and add it to *out with one FP64 atomic per block.
 __device__ __forceinline__ void block_sum_atomic(double v, double* out) {
   __shared__ double part[32];
@@ -275,9 +307,11 @@ std::vector<float> coarse_inverse(const Grid& c, float h2, int ref);
 cudaError_t mg_prepare();
 void launch_pressure_solve(const DevState& s, cudaStream_t st);
 void launch_residual_norm(const DevState& s, double* out, cudaStream_t st);
-void launch_sum(const float* a, size_t n, double* out, int num_sms, cudaStream_t st);
+// mean removal: launch_sum leaves per-block partials in part (kSumBlocks
+// doubles), launch_sub_mean adds them in a fixed order and subtracts the mean
+void launch_sum(const float* a, size_t n, double* part, int num_sms, cudaStream_t st);
 // sumsq (statistics): also accumulate the sum of squares of the result there
-void launch_sub_mean(float* a, size_t n, const double* sum, int num_sms, cudaStream_t st, double* sumsq = nullptr);
+void launch_sub_mean(float* a, size_t n, const double* part, int num_sms, cudaStream_t st, double* sumsq = nullptr);
 void launch_sumsq(const float* a, size_t n, double* out, int num_sms, cudaStream_t st);
 // Natural <-> red-black split copy of a level-0 array (field I/O).
 void launch_split(const float* src, float* dst, const Grid& d, bool to_split, cudaStream_t st);

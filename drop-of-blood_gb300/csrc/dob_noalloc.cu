@@ -55,7 +55,8 @@ namespace {
 constexpr size_t kNoAllocMaxCells = size_t(1) << 21;
 constexpr size_t kAlign = 256;
 constexpr size_t kSlotBytes = 1024;  // FP64 + u32 reduction slots at the front
-// Layout for n cells: slots, split p (4n), split rhs (4n), then correction and
+constexpr size_t kPartBytes = PART_SLOTS * kSumBlocks * sizeof(double);  // mean-removal partials
+// Layout for n cells: slots, partials, split p (4n), split rhs (4n), then correction and
 // right-hand side of every coarser grid, each rounded up to 256 bytes.  The
 // coarser grids hold fewer than n/7 cells together, so 10 bytes per cell
 // bounds the whole layout for every accepted grid.
@@ -64,7 +65,7 @@ constexpr size_t kSlotBytes = 1024;  // FP64 + u32 reduction slots at the front
 // multigrid arrays.
 constexpr int kNoAllocDenseMax = kDenseCoarseTarget;
 constexpr size_t kDenseBytes = (size_t)kNoAllocDenseMax * kNoAllocDenseMax * sizeof(float);
-constexpr size_t kScratchBytes = kSlotBytes + 10 * kNoAllocMaxCells + kDenseBytes;
+constexpr size_t kScratchBytes = kSlotBytes + kPartBytes + 10 * kNoAllocMaxCells + kDenseBytes;
 
 static_assert(RED_COUNT * sizeof(double) <= 512, "reduction slots exceed their area");
 static_assert(REDU_COUNT * sizeof(unsigned int) <= kSlotBytes - 512, "flag slots exceed their area");
@@ -175,7 +176,8 @@ extern "C" dob_status dob_pressure_solve_noalloc(const dob_config* cfg, const fl
   unsigned char* cur = static_cast<unsigned char*>(base);
   s.red = reinterpret_cast<double*>(cur);
   s.redu = reinterpret_cast<unsigned int*>(cur + 512);
-  size_t used = kSlotBytes;
+  s.part = reinterpret_cast<double*>(cur + kSlotBytes);
+  size_t used = kSlotBytes + kPartBytes;
   auto take = [&](size_t cells) {
     float* p = reinterpret_cast<float*>(cur + used);
     used += round_up(cells * sizeof(float));

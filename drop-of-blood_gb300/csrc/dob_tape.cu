@@ -1,6 +1,7 @@
 // dob_tape.cu — the forward/backward pair of the discrete adjoint
 // (dob_adjoint_stage, dob_tape_forward, dob_tape_backward,
-// dob_adjoint_sphere_impulse) for the closed-box FP32 step.
+// dob_adjoint_sphere_impulse) for the closed-box step in FP32 and in the
+// mixed mode.
 //
 // Memory is bounded by checkpointing: the forward keeps (velocity, dye,
 // pressure) every k steps; the backward recomputes one segment of at most k
@@ -12,6 +13,11 @@
 // own values (up to the order of the FP64 atomic sums in the mean removal).
 // Parcels are passive tracers in the closed box (nothing reads their splat)
 // and are not recomputed.
+//
+// Mixed mode: the tape and the checkpoints hold the dye and the predictor
+// at their binary16 storage width and the pressure as its FP32 pair (p,
+// plo), so a recomputed segment is the forward's own; the backward reads
+// the binary16 linearisation points and keeps its adjoint arrays in FP32.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <string.h>
@@ -21,6 +27,12 @@
 #include "dob_ctx.h"
 
 using namespace dob;
+
+#define TCK(call)                                                                         \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess) return record_error(ctx, DOB_ECUDA, #call, cudaGetErrorString(e_)); \
+  } while (0)
 
 namespace dob {
 
@@ -34,12 +46,13 @@ struct AdjCtx {
   // the tape slots hold the last segment's linearisation points, recorded by
   // dob_tape_forward (no recomputation of that segment needed)
   bool last_in_slots = false;
-  std::vector<float*> ck;   // per checkpoint: u, v, w, dye, p (5 arrays)
+  std::vector<float*> ck;   // per checkpoint: u, v, w, dye, p, plo (kCk arrays; plo in the mixed mode only)
   std::vector<void*> tbufs; // segment buffers
   std::vector<float*> Tu, Tv, Tw, Tc;  // k + 1 entries
   std::vector<float4*> Tcen;           // k + 1 entries
   std::vector<float*> Tua, Tva, Twa, Tpred;  // k entries
   float* Tp = nullptr;
+  float* Tplo = nullptr;    // mixed mode: the pressure's low part
   float* Trhs = nullptr;
   float* Tsc[3] = {nullptr, nullptr, nullptr};  // Casson's output during recomputation (no adjoint reads it)
   double* dred = nullptr;   // reduction slots of the drop gradients (4 doubles)
@@ -47,10 +60,16 @@ struct AdjCtx {
   // the dye adjoint ping-pong at its start, recomputation or the recorded
   // last segment)
   std::vector<cudaGraphExec_t> seg_graphs;
+  // captured recording step j of the forward's last segment (tape slots j
+  // and j + 1; the step's parameters are uploaded before each launch)
+  std::vector<cudaGraphExec_t> rec_graphs;
   void drop_graphs() {
     for (cudaGraphExec_t& g : seg_graphs)
       if (g) cudaGraphExecDestroy(g);
     seg_graphs.clear();
+    for (cudaGraphExec_t& g : rec_graphs)
+      if (g) cudaGraphExecDestroy(g);
+    rec_graphs.clear();
   }
 };
 
@@ -69,11 +88,19 @@ void adjoint_free(dob_ctx* ctx) {
 
 namespace {
 
+constexpr size_t kCk = 6;  // arrays per checkpoint
+
 dob_status need_box_fp32(dob_ctx* ctx, const char* what) {
-  if (ctx->cfg.bc_mode != DOB_BC_CLOSED_BOX || ctx->cfg.precision_mode != DOB_PREC_FP32 || ctx->cfg.dye_refine != 1)
-    return record_error(ctx, DOB_ESTATE, what, "the adjoint covers the closed-box FP32 step with dye_refine 1");
+  const int prec = ctx->cfg.precision_mode;
+  if (ctx->cfg.bc_mode != DOB_BC_CLOSED_BOX || (prec != DOB_PREC_FP32 && prec != DOB_PREC_MIXED) ||
+      ctx->cfg.dye_refine != 1)
+    return record_error(ctx, DOB_ESTATE, what,
+                        "the adjoint covers the closed-box step (FP32 or mixed precision) with dye_refine 1");
   return DOB_OK;
 }
+bool mixed(const dob_ctx* ctx) { return ctx->s.prec == DOB_PREC_MIXED; }
+// bytes of one dye (or predictor) value as stored
+size_t dye_bytes(const dob_ctx* ctx) { return mixed(ctx) ? 2 : 4; }
 
 dob_status alloc(dob_ctx* ctx, std::vector<void*>& list, void** p, size_t bytes) {
   cudaError_t e = cudaMalloc(p, bytes);
@@ -107,11 +134,13 @@ dob_status ensure_adj(dob_ctx* ctx) {
   if (st == DOB_OK) st = alloc(ctx, A->bufs, (void**)&a.acen, N * sizeof(float4));
   F(&a.ac, Nc); F(&a.ac2, Nc); F(&a.apred, Nc);
   F(&a.ap, N); F(&a.arhs, N); F(&a.alpha, N); F(&a.gq, N);
+  if (s.prec == DOB_PREC_MIXED) { F(&a.lam, N); F(&a.lamlo, N); }
   for (int l = 1; l < s.nlev; ++l) {
     F(&a.le[l], s.lv[l].d.n());
     F(&a.lb[l], s.lv[l].d.n());
   }
   if (st == DOB_OK) st = alloc(ctx, A->bufs, (void**)&a.red, 8 * sizeof(double));
+  if (st == DOB_OK) st = alloc(ctx, A->bufs, (void**)&a.part, 2 * kSumBlocks * sizeof(double));
   if (st == DOB_OK) st = alloc(ctx, A->bufs, (void**)&A->dred, 4 * sizeof(double));
   if (st != DOB_OK) adjoint_free(ctx);
   return st;
@@ -122,6 +151,10 @@ void zero_adj(const DevState& s, const AdjState& a, cudaStream_t st) {
   for (float* p : {a.au, a.av, a.aw, a.au2, a.av2, a.aw2, a.ap, a.arhs}) cudaMemsetAsync(p, 0, N * 4, st);
   for (float* p : {a.ac, a.ac2, a.apred}) cudaMemsetAsync(p, 0, Nc * 4, st);
   cudaMemsetAsync(a.acen, 0, N * sizeof(float4), st);
+  if (a.lam) {  // mixed mode: the adjoint pressure solve's warm start
+    cudaMemsetAsync(a.lam, 0, N * 4, st);
+    cudaMemsetAsync(a.lamlo, 0, N * 4, st);
+  }
   for (int l = 1; l < s.nlev; ++l) {
     cudaMemsetAsync(a.le[l], 0, s.lv[l].d.n() * 4, st);
     cudaMemsetAsync(a.lb[l], 0, s.lv[l].d.n() * 4, st);
@@ -132,7 +165,7 @@ void zero_adj(const DevState& s, const AdjState& a, cudaStream_t st) {
 dob_status ensure_tape(dob_ctx* ctx, int k, int nseg) {
   AdjCtx* A = ctx->adj;
   const DevState& s = ctx->s;
-  const size_t N = s.g.n(), Nc = s.gc.n();
+  const size_t N = s.g.n(), Nc = s.gc.n(), db = dye_bytes(ctx);
   if (A->k != k) {
     A->drop_graphs();
     for (void* p : A->tbufs) cudaFree(p);
@@ -147,23 +180,28 @@ dob_status ensure_tape(dob_ctx* ctx, int k, int nseg) {
     };
     for (int j = 0; j <= k; ++j) {
       F((void**)&A->Tu[j], N * 4); F((void**)&A->Tv[j], N * 4); F((void**)&A->Tw[j], N * 4);
-      F((void**)&A->Tc[j], Nc * 4); F((void**)&A->Tcen[j], N * sizeof(float4));
+      F((void**)&A->Tc[j], Nc * db); F((void**)&A->Tcen[j], N * sizeof(float4));
       if (j < k) {
         F((void**)&A->Tua[j], N * 4); F((void**)&A->Tva[j], N * 4); F((void**)&A->Twa[j], N * 4);
-        F((void**)&A->Tpred[j], Nc * 4);
+        F((void**)&A->Tpred[j], Nc * db);
       }
     }
     F((void**)&A->Tp, N * 4);
+    if (mixed(ctx)) F((void**)&A->Tplo, N * 4);
     F((void**)&A->Trhs, N * 4);
     for (int c = 0; c < 3; ++c) F((void**)&A->Tsc[c], N * 4);
     if (st != DOB_OK) return st;
     A->k = k;
   }
-  const size_t want = (size_t)nseg * 5;
+  const size_t want = (size_t)nseg * kCk;
   while (A->ck.size() < want) {
     float* p = nullptr;
-    const size_t j = A->ck.size() % 5;
-    const size_t b = (j == 3 ? Nc : N) * 4;
+    const size_t j = A->ck.size() % kCk;
+    if (j == 5 && !mixed(ctx)) {
+      A->ck.push_back(nullptr);
+      continue;
+    }
+    const size_t b = j == 3 ? Nc * db : N * 4;
     cudaError_t e = cudaMalloc(&p, b);
     if (e != cudaSuccess) {
       cudaGetLastError();
@@ -178,13 +216,14 @@ void save_checkpoint(dob_ctx* ctx, int seg) {
   AdjCtx* A = ctx->adj;
   const DevState& s = ctx->s;
   const size_t N = s.g.n(), Nc = s.gc.n();
-  float** c = &A->ck[(size_t)seg * 5];
+  float** c = &A->ck[(size_t)seg * kCk];
   cudaStream_t st = ctx->stream;
   cudaMemcpyAsync(c[0], s.u, N * 4, cudaMemcpyDeviceToDevice, st);
   cudaMemcpyAsync(c[1], s.v, N * 4, cudaMemcpyDeviceToDevice, st);
   cudaMemcpyAsync(c[2], s.w, N * 4, cudaMemcpyDeviceToDevice, st);
-  cudaMemcpyAsync(c[3], s.conc, Nc * 4, cudaMemcpyDeviceToDevice, st);
+  cudaMemcpyAsync(c[3], s.conc, Nc * dye_bytes(ctx), cudaMemcpyDeviceToDevice, st);
   cudaMemcpyAsync(c[4], s.p, N * 4, cudaMemcpyDeviceToDevice, st);
+  if (mixed(ctx)) cudaMemcpyAsync(c[5], s.plo, N * 4, cudaMemcpyDeviceToDevice, st);
 }
 
 // Recompute steps [0, len) of segment `seg` from its checkpoint, recording
@@ -194,12 +233,13 @@ void restore_checkpoint(dob_ctx* ctx, int seg) {
   const DevState& s = ctx->s;
   const size_t N = s.g.n(), Nc = s.gc.n();
   cudaStream_t st = ctx->stream;
-  float** c = &A->ck[(size_t)seg * 5];
+  float** c = &A->ck[(size_t)seg * kCk];
   cudaMemcpyAsync(A->Tu[0], c[0], N * 4, cudaMemcpyDeviceToDevice, st);
   cudaMemcpyAsync(A->Tv[0], c[1], N * 4, cudaMemcpyDeviceToDevice, st);
   cudaMemcpyAsync(A->Tw[0], c[2], N * 4, cudaMemcpyDeviceToDevice, st);
-  cudaMemcpyAsync(A->Tc[0], c[3], Nc * 4, cudaMemcpyDeviceToDevice, st);
+  cudaMemcpyAsync(A->Tc[0], c[3], Nc * dye_bytes(ctx), cudaMemcpyDeviceToDevice, st);
   cudaMemcpyAsync(A->Tp, c[4], N * 4, cudaMemcpyDeviceToDevice, st);
+  if (mixed(ctx)) cudaMemcpyAsync(A->Tplo, c[5], N * 4, cudaMemcpyDeviceToDevice, st);
 }
 // Step j of a segment from tape slot j: the step's fluid and dye stages
 // writing their linearisation points into the tape (slot j + 1 receives the
@@ -213,7 +253,7 @@ void tape_step(dob_ctx* ctx, int j, bool parcels) {
   const DevState& s = ctx->s;
   cudaStream_t st = ctx->stream;
   DevState t = s;
-  t.p = A->Tp; t.rhs = A->Trhs;
+  t.p = A->Tp; t.plo = A->Tplo; t.rhs = A->Trhs;
   t.u = A->Tu[j]; t.v = A->Tv[j]; t.w = A->Tw[j]; t.cen = A->Tcen[j];
   t.u2 = A->Tua[j]; t.v2 = A->Tva[j]; t.w2 = A->Twa[j];
   launch_advect_mac(t, st);
@@ -257,19 +297,40 @@ dob_status record_last_segment(dob_ctx* ctx, int seg, int len) {
   DevState t = s;
   t.u = A->Tu[0]; t.v = A->Tv[0]; t.w = A->Tw[0]; t.cen = A->Tcen[0];
   launch_mac_to_center(t, st);
+  if (A->rec_graphs.size() != (size_t)A->k) {
+    for (cudaGraphExec_t& g : A->rec_graphs)
+      if (g) cudaGraphExecDestroy(g);
+    A->rec_graphs.assign(A->k, nullptr);
+  }
   for (int j = 0; j < len; ++j) {
     dob_status e = step_host_begin(ctx);
     if (e != DOB_OK) return e;
-    tape_step(ctx, j, true);
+    // one captured graph per slot: the mixed solve's loops become while-nodes
+    // (uncaptured, every possible cycle would be enqueued behind flags)
+    cudaGraphExec_t& ge = A->rec_graphs[j];
+    if (!ge) {
+      TCK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+      tape_step(ctx, j, true);
+      cudaGraph_t g = nullptr;
+      TCK(cudaStreamEndCapture(st, &g));
+      cudaError_t ce = cudaGraphInstantiate(&ge, g, 0);
+      cudaGraphDestroy(g);
+      if (ce != cudaSuccess) {
+        ge = nullptr;
+        return record_error(ctx, DOB_ECUDA, "cudaGraphInstantiate", cudaGetErrorString(ce));
+      }
+    }
+    TCK(cudaGraphLaunch(ge, st));
     step_host_end(ctx);
   }
   cudaMemcpyAsync(s.u, A->Tu[len], N * 4, cudaMemcpyDeviceToDevice, st);
   cudaMemcpyAsync(s.v, A->Tv[len], N * 4, cudaMemcpyDeviceToDevice, st);
   cudaMemcpyAsync(s.w, A->Tw[len], N * 4, cudaMemcpyDeviceToDevice, st);
   cudaMemcpyAsync(s.cen, A->Tcen[len], N * sizeof(float4), cudaMemcpyDeviceToDevice, st);
-  cudaMemcpyAsync(s.conc, A->Tc[len], Nc * 4, cudaMemcpyDeviceToDevice, st);
-  cudaMemcpyAsync(s.pred, A->Tpred[len - 1], Nc * 4, cudaMemcpyDeviceToDevice, st);
+  cudaMemcpyAsync(s.conc, A->Tc[len], Nc * dye_bytes(ctx), cudaMemcpyDeviceToDevice, st);
+  cudaMemcpyAsync(s.pred, A->Tpred[len - 1], Nc * dye_bytes(ctx), cudaMemcpyDeviceToDevice, st);
   cudaMemcpyAsync(s.p, A->Tp, N * 4, cudaMemcpyDeviceToDevice, st);
+  if (mixed(ctx)) cudaMemcpyAsync(s.plo, A->Tplo, N * 4, cudaMemcpyDeviceToDevice, st);
   cudaMemcpyAsync(s.rhs, A->Trhs, N * 4, cudaMemcpyDeviceToDevice, st);
   return DOB_OK;
 }
@@ -344,11 +405,6 @@ bool adjoint_field(dob_ctx* ctx, int field, void** dev, size_t* count, int* kind
 }
 }  // namespace dob
 
-#define TCK(call)                                                                         \
-  do {                                                                                    \
-    cudaError_t e_ = (call);                                                              \
-    if (e_ != cudaSuccess) return record_error(ctx, DOB_ECUDA, #call, cudaGetErrorString(e_)); \
-  } while (0)
 
 extern "C" {
 

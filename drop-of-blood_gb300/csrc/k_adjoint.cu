@@ -1,5 +1,5 @@
 // k_adjoint.cu — discrete adjoint (transpose of the Jacobian) of every stage
-// of the closed-box FP32 step.
+// of the closed-box step, FP32 and mixed precision.
 //
 // Each kernel is the exact transpose of the linearisation of one forward
 // kernel at the forward state it is given (the "tape"):
@@ -13,8 +13,11 @@
 //                    transpose of the stencil plus the alpha chain (two
 //                    passes: per-cell coefficients, then a gather)
 //   divergence / projection  D^T and G^T with the wall masks
-//   pressure solve   every V-cycle run backwards with the transposed
-//                    smoother half-sweeps, restriction and prolongation
+//   pressure solve   FP32 (a fixed number of V-cycles): every V-cycle run
+//                    backwards with the transposed smoother half-sweeps,
+//                    restriction and prolongation; mixed (solved to a
+//                    tolerance): the adjoint of an exact solve, the same
+//                    solver on the adjoint right-hand side
 //   dye predict / MacCormack resolve  transposed samples; the limiter passes
 //                    the adjoint through, or to the neighbourhood tap that
 //                    supplied the clamped value
@@ -115,8 +118,9 @@ __device__ __forceinline__ dob_v3 dfrac_core(const Taps& t, const NodeLo& n, F v
   }
   return v3(dfx, dfy, dfz);
 }
-__device__ __forceinline__ dob_v3 lerp8_dfrac(const Taps& t, const NodeLo& n, const float* a) {
-  return dfrac_core(t, n, [&](uint32_t k) { return a[k]; });
+template <class S>
+__device__ __forceinline__ dob_v3 lerp8_dfrac(const Taps& t, const NodeLo& n, const S* a) {
+  return dfrac_core(t, n, [&](uint32_t k) { return ldv(a + k); });
 }
 // sum over the xyz channels of a float4 field: sum_ch g_ch * d lerp8_ch / d(fx, fy, fz)
 // (the derivative is linear in the values, so the channels are contracted first)
@@ -245,9 +249,10 @@ __device__ __forceinline__ dob_v3 out_adj(const Grid& g, const float* au2, const
 }
 // Pass 1: per cell, alpha and G = 2 dL/dQ (Q = |grad u|^2 of the Casson
 // shear rate); the dye adjoint of the cell.
+template <class DS>
 __global__ void __launch_bounds__(256, 5) k_adj_casson1(Grid g, const StepParams* __restrict__ Pp,
                                                      const float* __restrict__ u, const float* __restrict__ v,
-                                                     const float* __restrict__ w, const float* __restrict__ dye,
+                                                     const float* __restrict__ w, const DS* __restrict__ dye,
                                                      const float* __restrict__ au2, const float* __restrict__ av2,
                                                      const float* __restrict__ aw2, float* __restrict__ alpha_out,
                                                      float* __restrict__ gq_out, float* ac) {
@@ -260,7 +265,7 @@ __global__ void __launch_bounds__(256, 5) k_adj_casson1(Grid g, const StepParams
   const dob_v3 mZp = ldm(g, u, v, w, x, y, z + 1), mZn = ldm(g, u, v, w, x, y, z - 1);
   const dob_v3 du = mXp - mXn, dv = mYp - mYn, dw = mZp - mZn;
   const dob_v3 lap = (mXp + mXn + mYp + mYn + mZp + mZn) - 6.0f * mac;
-  const float cval = dye[i];
+  const float cval = ldv(dye + i);
   const float c = dob_clampf(cval, 0.0f, 1.5f);
   const float dxv = P.dx;
   const float Q = dot3(du, du) + dot3(dv, dv) + dot3(dw, dw);
@@ -767,8 +772,9 @@ __global__ void __launch_bounds__(256) k_adj_prolong2(Grid f, Grid c, int ref, c
 // coefficients) and the transposed smoother are capped at 4-5 blocks of 256
 // per SM (a few spilled bytes): latency-bound, they gain more from the
 // resident warps (192x256x192 backward 4.81 -> 4.67 ms per step).
+template <class DS>
 __global__ void __launch_bounds__(256, 4) k_adj_conc_predict(Grid gc, Grid g, const StepParams* __restrict__ Pp,
-                                                          const float4* __restrict__ cen, const float* __restrict__ dye,
+                                                          const float4* __restrict__ cen, const DS* __restrict__ dye,
                                                           const float* __restrict__ apred, float* ac, float4* acen) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
@@ -803,9 +809,10 @@ __global__ void __launch_bounds__(256, 4) k_adj_conc_predict(Grid gc, Grid g, co
 }
 
 // ---- CONC_RESOLVE (closed box: MacCormack with the 8-tap limiter) -----------------------------
+template <class DS>
 __global__ void __launch_bounds__(256, 5) k_adj_dye_resolve(Grid gc, Grid g, const StepParams* __restrict__ Pp,
-                                                         const float4* __restrict__ cen, const float* __restrict__ dye,
-                                                         const float* __restrict__ pred, const float* __restrict__ ac2,
+                                                         const float4* __restrict__ cen, const DS* __restrict__ dye,
+                                                         const DS* __restrict__ pred, const float* __restrict__ ac2,
                                                          float* ac, float* apred, float4* acen) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
@@ -830,7 +837,7 @@ __global__ void __launch_bounds__(256, 5) k_adj_dye_resolve(Grid gc, Grid g, con
   const Taps tF = make_taps(gc, uvwFwd.x, uvwFwd.y, uvwFwd.z);
   const float gBackEst = lerp8(tF, pred);
   const float kap = 0.45f * P.sharp;
-  const float gCorr = __fmaf_rn(kap, dye[i] - gBackEst, pred[i]);  // as the forward rounds it
+  const float gCorr = __fmaf_rn(kap, ldv(dye + i) - gBackEst, ldv(pred + i));  // as the forward rounds it
   // the limiter's taps: the forward predictor's (make_taps at the departure point)
   const int bx = (int)floorf(texel(uvwBack.x, gc.nx)), by = (int)floorf(texel(uvwBack.y, gc.ny));
   const int bz = (int)floorf(texel(uvwBack.z, gc.nz));
@@ -840,7 +847,7 @@ __global__ void __launch_bounds__(256, 5) k_adj_dye_resolve(Grid gc, Grid g, con
   for (int k = 0; k < 8; ++k) {
     id[k] = gc.at(dob_clampi(bx + (k & 1), 0, gc.nx - 1), dob_clampi(by + ((k >> 1) & 1), 0, gc.ny - 1),
                   dob_clampi(bz + ((k >> 2) & 1), 0, gc.nz - 1));
-    s[k] = dye[id[k]];
+    s[k] = ldv(dye + id[k]);
   }
   // the forward's min/max trees (dob_minf/dob_maxf keep the second operand on ties)
   auto pick_min = [&](int a, int b) { return s[a] < s[b] ? a : b; };
@@ -878,17 +885,28 @@ void launch_adj_advect_mac(const DevState& s, const AdjState& a, cudaStream_t st
 void launch_adj_mac_to_center(const DevState& s, const AdjState& a, cudaStream_t st) {
   k_adj_mac_to_center<<<cgrid(s.g), cblock(), 0, st>>>(s.g, a.acen, a.au, a.av, a.aw);
 }
+// The dye and the predictor are read at their storage width: binary16 in
+// the mixed mode (the adjoint of the rounding store is the identity, so the
+// adjoint arrays stay FP32).
+#define ADJ_DYE_DISPATCH(prec, ...)                                \
+  do {                                                             \
+    if ((prec) == DOB_PREC_MIXED) { using DS = __half; __VA_ARGS__; } \
+    else { using DS = float; __VA_ARGS__; }                        \
+  } while (0)
+
 void launch_adj_casson(const DevState& s, const AdjState& a, cudaStream_t st) {
-  k_adj_casson1<<<cgrid(s.g), cblock(), 0, st>>>(s.g, s.params, (const float*)s.u, (const float*)s.v,
-                                                 (const float*)s.w, (const float*)s.conc, a.au2, a.av2, a.aw2,
-                                                 a.alpha, a.gq, a.ac);
+  ADJ_DYE_DISPATCH(s.prec, {
+    k_adj_casson1<DS><<<cgrid(s.g), cblock(), 0, st>>>(s.g, s.params, (const float*)s.u, (const float*)s.v,
+                                                       (const float*)s.w, (const DS*)s.conc, a.au2, a.av2, a.aw2,
+                                                       a.alpha, a.gq, a.ac);
+  });
   k_adj_casson2<<<cgrid(s.g), cblock(), 0, st>>>(s.g, (const float*)s.u, (const float*)s.v, (const float*)s.w, a.au2,
                                                  a.av2, a.aw2, a.alpha, a.gq, a.au, a.av, a.aw);
 }
 void launch_adj_mac_rhs(const DevState& s, const AdjState& a, cudaStream_t st) {
   // transpose of the mean removal (a symmetric projection), then D^T
-  launch_sum(a.arhs, s.g.n(), a.red + 0, s.num_sms, st);
-  launch_sub_mean(a.arhs, s.g.n(), a.red + 0, s.num_sms, st);
+  launch_sum(a.arhs, s.g.n(), a.part, s.num_sms, st);
+  launch_sub_mean(a.arhs, s.g.n(), a.part, s.num_sms, st);
   k_adj_mac_rhs<<<cgrid(s.g), cblock(), 0, st>>>(s.g, a.arhs, a.au, a.av, a.aw);
 }
 void launch_adj_project(const DevState& s, const AdjState& a, cudaStream_t st) {
@@ -1046,22 +1064,57 @@ static void adj_vcycle(const DevState& s, const AdjState& a, cudaStream_t st) {
   adj_restrict(s, a, 0, a.ap, a.arhs, st);
   adj_smooth(L0.d, L0.h2, s.ref, s.pre0, a.ap, a.arhs, st);
 }
+// rhs += lam + lamlo (the adjoint of the right-hand side through an exact
+// solve); the solution's adjoint is consumed
+__global__ void __launch_bounds__(256) k_adj_take_solution(const float* __restrict__ lam,
+                                                           const float* __restrict__ lamlo, float* arhs, float* ap,
+                                                           size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    arhs[i] += lam[i] + lamlo[i];
+    ap[i] = 0.0f;
+  }
+}
 void launch_adj_pressure_solve(const DevState& s, const AdjState& a, cudaStream_t st) {
   const size_t n = s.g.n();
   if (!s.ref) {
-    launch_sum(a.ap, n, a.red + 1, s.num_sms, st);
-    launch_sub_mean(a.ap, n, a.red + 1, s.num_sms, st);
+    launch_sum(a.ap, n, a.part + kSumBlocks, s.num_sms, st);
+    launch_sub_mean(a.ap, n, a.part + kSumBlocks, s.num_sms, st);
+  }
+  if (s.prec == DOB_PREC_MIXED) {
+    // The mixed forward solves to a tolerance, not a fixed number of cycles:
+    // its pressure is A^+ b up to that tolerance, whatever the warm start, so
+    // its adjoint is the same solve: A lam = ap (A symmetric, ap zero-mean),
+    // by the mixed solver itself to ||ap - A lam|| <= kAdjRelTol ||ap||, then
+    // rhs adjoint += lam and no adjoint reaches the warm start.  The solve
+    // starts from the previous (later) step's lam, which the reverse sweep
+    // leaves in place: the adjoint pressures of neighbouring steps are close,
+    // so fewer V-cycles reach the tolerance.
+    DevState t = s;
+    t.p = a.lam;
+    t.plo = a.lamlo;
+    t.rhs = a.ap;
+    t.rel_tol = kAdjRelTol;
+    t.div_tol_r = 0.0f;
+    t.max_outer = kMixedMaxRounds;
+    t.cycles = 0;
+    launch_pressure_solve(t, st);
+    k_adj_take_solution<<<s.num_sms * 4, 256, 0, st>>>(a.lam, a.lamlo, a.arhs, a.ap, n);
+    return;
   }
   for (int c = 0; c < s.cycles; ++c) adj_vcycle(s, a, st);
 }
 void launch_adj_conc_predict(const DevState& s, const AdjState& a, cudaStream_t st) {
-  k_adj_conc_predict<<<cgrid(s.gc), cblock(), 0, st>>>(s.gc, s.g, s.params, (const float4*)s.cen,
-                                                       (const float*)s.conc, a.apred, a.ac, a.acen);
+  ADJ_DYE_DISPATCH(s.prec, {
+    k_adj_conc_predict<DS><<<cgrid(s.gc), cblock(), 0, st>>>(s.gc, s.g, s.params, (const float4*)s.cen,
+                                                             (const DS*)s.conc, a.apred, a.ac, a.acen);
+  });
 }
 void launch_adj_conc_resolve(const DevState& s, const AdjState& a, cudaStream_t st) {
-  k_adj_dye_resolve<<<cgrid(s.gc), cblock(), 0, st>>>(s.gc, s.g, s.params, (const float4*)s.cen,
-                                                      (const float*)s.conc, (const float*)s.pred, a.ac2, a.ac,
-                                                      a.apred, a.acen);
+  ADJ_DYE_DISPATCH(s.prec, {
+    k_adj_dye_resolve<DS><<<cgrid(s.gc), cblock(), 0, st>>>(s.gc, s.g, s.params, (const float4*)s.cen,
+                                                            (const DS*)s.conc, (const DS*)s.pred, a.ac2, a.ac,
+                                                            a.apred, a.acen);
+  });
 }
 
 }  // namespace dob

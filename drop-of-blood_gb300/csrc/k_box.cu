@@ -194,8 +194,8 @@ void launch_mac_rhs_box(const DevState& s, cudaStream_t st, double* sumsq) {
     k_rhs_box<VS, kRhsZ><<<col_grid<kRhsZ>(s.g), dim3(32, 8), 0, st>>>(s.g, (const VS*)s.u, (const VS*)s.v, (const VS*)s.w,
                                                          s.rhs);
   });
-  launch_sum(s.rhs, s.g.n(), s.red + RED_RHS_SUM, s.num_sms, st);
-  launch_sub_mean(s.rhs, s.g.n(), s.red + RED_RHS_SUM, s.num_sms, st, sumsq);
+  launch_sum(s.rhs, s.g.n(), s.part + PART_RHS * kSumBlocks, s.num_sms, st);
+  launch_sub_mean(s.rhs, s.g.n(), s.part + PART_RHS * kSumBlocks, s.num_sms, st, sumsq);
 }
 
 void launch_project_center_box(const DevState& s, cudaStream_t st, float scale, unsigned int* maxbits) {

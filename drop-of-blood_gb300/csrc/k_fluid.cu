@@ -482,6 +482,7 @@ constexpr int kDyeBrick = 8;
 // |centre velocity| per axis inside a step: the projection clamps the faces
 // to +-2 (fluid.ts:908) and the centre is their mean (with a margin)
 constexpr float kDyeSpeedBound = 2.0f * 1.0001f;
+constexpr int kDyeResolveZ = 4;  // voxels per thread along z in the reference-mode resolve
 __host__ __device__ __forceinline__ Grid brick_grid(const Grid& gc) {
   return Grid{(gc.nx + kDyeBrick - 1) / kDyeBrick, (gc.ny + kDyeBrick - 1) / kDyeBrick,
               (gc.nz + kDyeBrick - 1) / kDyeBrick};
@@ -489,9 +490,11 @@ __host__ __device__ __forceinline__ Grid brick_grid(const Grid& gc) {
 __device__ __forceinline__ void mark_brick(const Grid& gc, uint32_t* flags, int x, int y, int z) {
   flags[brick_grid(gc).at(x / kDyeBrick, y / kDyeBrick, z / kDyeBrick)] = 1u;
 }
-// Whether any brick overlapping the block's voxels, widened by rx, ry, rz
-// voxels per axis, is flagged (block-uniform; every thread must call it).
-__device__ __forceinline__ bool block_any_brick(const Grid& gc, const uint32_t* flags, int rx, int ry, int rz) {
+// Whether any brick overlapping the block's voxels (x and y from the block
+// index, planes zlo..zhi), widened by rx, ry, rz voxels per axis, is flagged
+// (block-uniform; every thread must call it).
+__device__ __forceinline__ bool block_any_brick(const Grid& gc, const uint32_t* flags, int rx, int ry, int rz,
+                                                int zlo, int zhi) {
   __shared__ int any;
   const int tid = threadIdx.x + blockDim.x * threadIdx.y;
   if (tid == 0) any = 0;
@@ -500,7 +503,7 @@ __device__ __forceinline__ bool block_any_brick(const Grid& gc, const uint32_t* 
   const int x1 = min((int)(blockIdx.x * blockDim.x + blockDim.x) - 1 + rx, gc.nx - 1);
   const int y0 = max((int)(blockIdx.y * blockDim.y) - ry, 0);
   const int y1 = min((int)(blockIdx.y * blockDim.y + blockDim.y) - 1 + ry, gc.ny - 1);
-  const int z0 = max((int)blockIdx.z - rz, 0), z1 = min((int)blockIdx.z + rz, gc.nz - 1);
+  const int z0 = max(zlo - rz, 0), z1 = min(zhi + rz, gc.nz - 1);
   const Grid b = brick_grid(gc);
   const int bx0 = x0 / kDyeBrick, by0 = y0 / kDyeBrick, bz0 = z0 / kDyeBrick;
   const int nbx = x1 / kDyeBrick - bx0 + 1, nby = y1 / kDyeBrick - by0 + 1, nbz = z1 / kDyeBrick - bz0 + 1;
@@ -515,34 +518,21 @@ __device__ __forceinline__ bool block_any_brick(const Grid& gc, const uint32_t* 
 // The predictor's reach: RK2 departures move at most `speed` dt per axis in
 // world units, plus one voxel for the interpolation's taps.
 __device__ __forceinline__ bool block_reaches_dye(const Grid& gc, const StepParams& P, const uint32_t* cbrick,
-                                                  float speed) {
+                                                  float speed, int zlo, int zhi) {
   const float d = speed * P.dt;
   const int rx = (int)ceilf(d * (float)gc.nx / P.dsize[0]) + 1;
   const int ry = (int)ceilf(d * (float)gc.ny / P.dsize[1]) + 1;
   const int rz = (int)ceilf(d * (float)gc.nz / P.dsize[2]) + 1;
-  return block_any_brick(gc, cbrick, rx, ry, rz);
+  return block_any_brick(gc, cbrick, rx, ry, rz, zlo, zhi);
 }
 
 // ---- CONC_PREDICT (advect.ts:28-72) -----------------------------------------------------------
 template <class VS, class DS>
-__global__ void __launch_bounds__(256, 8) k_conc_predict(Grid gc, Grid g, const StepParams* __restrict__ Pp, int ref,
-                                                      const typename Vec4Of<VS>::type* __restrict__ cen,
-                                                      const typename Vec4Of<DS>::type* __restrict__ conc4,
-                                                      const DS* __restrict__ dye, DS* __restrict__ pred,
-                                                      DS* __restrict__ lim, const uint32_t* __restrict__ cbrick,
-                                                      uint32_t* __restrict__ pbrick) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = blockIdx.y * blockDim.y + threadIdx.y;
-  const int z = blockIdx.z;
-  const StepParams& P = *Pp;
-  // reference mode inside a step (the centre velocity there comes from faces
-  // clamped to +-2 by the projection): a block whose departure points can
-  // only reach dye bricks with no lysed dye writes zeros without tracing
-  if (cbrick && !block_reaches_dye(gc, P, cbrick, kDyeSpeedBound)) {
-    if (x < gc.nx && y < gc.ny) stf(pred + gc.at(x, y, z), 0.0f);
-    return;
-  }
-  if (x >= gc.nx || y >= gc.ny) return;
+__device__ __forceinline__ void predict_cell(const Grid& gc, const Grid& g, const StepParams& P, int ref,
+                                             const typename Vec4Of<VS>::type* __restrict__ cen,
+                                             const typename Vec4Of<DS>::type* __restrict__ conc4,
+                                             const DS* __restrict__ dye, DS* __restrict__ pred, DS* __restrict__ lim,
+                                             uint32_t* __restrict__ pbrick, int x, int y, int z) {
   const size_t i = gc.at(x, y, z);
   const Recip3 dims = recip3(v3((float)gc.nx, (float)gc.ny, (float)gc.nz));
   const float dtv = P.dt;
@@ -588,6 +578,34 @@ __global__ void __launch_bounds__(256, 8) k_conc_predict(Grid gc, Grid g, const 
   }
 }
 
+// ZP voxels per thread along z (grid z = nz / ZP): with the brick flags
+// (reference mode inside a step, ZP = kDyeResolveZ) one reach test serves
+// ZP planes; the closed box runs one voxel per thread.
+template <class VS, class DS, int ZP>
+__global__ void __launch_bounds__(256, ZP == 1 ? 8 : 4) k_conc_predict(Grid gc, Grid g, const StepParams* __restrict__ Pp, int ref,
+                                                      const typename Vec4Of<VS>::type* __restrict__ cen,
+                                                      const typename Vec4Of<DS>::type* __restrict__ conc4,
+                                                      const DS* __restrict__ dye, DS* __restrict__ pred,
+                                                      DS* __restrict__ lim, const uint32_t* __restrict__ cbrick,
+                                                      uint32_t* __restrict__ pbrick) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z0 = blockIdx.z * ZP;
+  const int z1 = min(z0 + ZP, gc.nz);
+  const StepParams& P = *Pp;
+  // reference mode inside a step (the centre velocity there comes from faces
+  // clamped to +-2 by the projection): a block whose departure points can
+  // only reach dye bricks with no lysed dye writes zeros without tracing
+  if (cbrick && !block_reaches_dye(gc, P, cbrick, kDyeSpeedBound, z0, z1 - 1)) {
+    if (x < gc.nx && y < gc.ny)
+      for (int z = z0; z < z1; ++z) stf(pred + gc.at(x, y, z), 0.0f);
+    return;
+  }
+  if (x >= gc.nx || y >= gc.ny) return;
+#pragma unroll 1
+  for (int z = z0; z < z1; ++z) predict_cell<VS, DS>(gc, g, P, ref, cen, conc4, dye, pred, lim, pbrick, x, y, z);
+}
+
 // ---- CONC_RESOLVE (advect.ts:81-298) ------------------------------------------------------------
 template <class S>
 __device__ __forceinline__ float ldcs(const Grid& gc, const S* a, int x, int y, int z) {
@@ -601,36 +619,20 @@ __device__ __forceinline__ float intact_raw(const Grid& gc, const uint32_t* s, i
   return (float)__ldg(s + gc.at(dob_clampi(x, 0, gc.nx - 1), dob_clampi(y, 0, gc.ny - 1), dob_clampi(z, 0, gc.nz - 1))) * kSplatInv;
 }
 
+// One interior voxel of the resolve (the boundary shell and the clear-water
+// early-out are the kernel's).
 template <class VS, class DS>
-__global__ void __launch_bounds__(256, 3) k_conc_resolve_ref(Grid gc, Grid g, const StepParams* __restrict__ Pp,
-                                                          const typename Vec4Of<VS>::type* __restrict__ cen,
-                                                          const typename Vec4Of<DS>::type* __restrict__ conc,
-                                                          const DS* __restrict__ pred,
-                                                          const uint32_t* __restrict__ splatI,
-                                                          const uint32_t* __restrict__ splatL,
-                                                          typename Vec4Of<DS>::type* __restrict__ out,
-                                                          const uint32_t* __restrict__ pbrick,
-                                                          uint32_t* __restrict__ cbrick_out) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = blockIdx.y * blockDim.y + threadIdx.y;
-  const int z = blockIdx.z;
-  // inside a step: no predictor value within one voxel of the block
-  const bool clear = pbrick && !block_any_brick(gc, pbrick, 1, 1, 1);
-  if (x >= gc.nx || y >= gc.ny) return;
+__device__ __forceinline__ void resolve_ref_cell(const Grid& gc, const Grid& g, const StepParams& P,
+                                                 const typename Vec4Of<VS>::type* __restrict__ cen,
+                                                 const typename Vec4Of<DS>::type* __restrict__ conc,
+                                                 const DS* __restrict__ pred, const uint32_t* __restrict__ splatI,
+                                                 const uint32_t* __restrict__ splatL,
+                                                 typename Vec4Of<DS>::type* __restrict__ out,
+                                                 uint32_t* __restrict__ cbrick_out, int x, int y, int z) {
   const size_t i = gc.at(x, y, z);
-  if (x == 0 || x >= gc.nx - 1 || z == 0 || z >= gc.nz - 1 || y >= gc.ny - 1) {
-    st4(out + i, make_float4(0.f, 0.f, 0.f, 0.f));
-    return;
-  }
-  const StepParams& P = *Pp;
   const dob_v3 dims = v3((float)gc.nx, (float)gc.ny, (float)gc.nz);
-  const uint32_t rawIntact = __ldg(splatI + i), rawLysed = __ldg(splatL + i);
   const bool inFloorZone = y <= 7;
-  // the early-out below with oct0 = oct1 = 0 (every predictor tap is +0)
-  if (clear && !inFloorZone && rawIntact == 0u && rawLysed == 0u) {
-    st4(out + i, make_float4(0.f, 0.f, 0.f, 0.f));
-    return;
-  }
+  const uint32_t rawIntact = __ldg(splatI + i), rawLysed = __ldg(splatL + i);
   if (rawIntact == 0u && rawLysed == 0u) {
     const dob_v3 g0 = v3((float)x, (float)y, (float)z) / dims;
     const dob_v3 g1 = (v3((float)x, (float)y, (float)z) + v3(1.0f, 1.0f, 1.0f)) / dims;
@@ -735,6 +737,58 @@ __global__ void __launch_bounds__(256, 3) k_conc_resolve_ref(Grid gc, Grid g, co
   }
   st4(out + i, make_float4(cIntact, cLysed, vOx, cBed));
   if (cLysed != 0.0f) mark_brick(gc, cbrick_out, x, y, z);
+}
+
+// Each thread resolves kDyeResolveZ voxels along z: their splat sums are
+// loaded before the block's brick test, so in clear water (most of the dye
+// grid) the flag loads, the barrier and the splat loads overlap and one
+// test serves kDyeResolveZ planes; the voxels that need the full resolve
+// then run it one after another.
+template <class VS, class DS>
+__global__ void __launch_bounds__(256, 3) k_conc_resolve_ref(Grid gc, Grid g, const StepParams* __restrict__ Pp,
+                                                          const typename Vec4Of<VS>::type* __restrict__ cen,
+                                                          const typename Vec4Of<DS>::type* __restrict__ conc,
+                                                          const DS* __restrict__ pred,
+                                                          const uint32_t* __restrict__ splatI,
+                                                          const uint32_t* __restrict__ splatL,
+                                                          typename Vec4Of<DS>::type* __restrict__ out,
+                                                          const uint32_t* __restrict__ pbrick,
+                                                          uint32_t* __restrict__ cbrick_out) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z0 = blockIdx.z * kDyeResolveZ;
+  const bool inside = x < gc.nx && y < gc.ny;
+  uint32_t rI[kDyeResolveZ], rL[kDyeResolveZ];
+#pragma unroll
+  for (int k = 0; k < kDyeResolveZ; ++k) {
+    const bool ok = inside && z0 + k < gc.nz;
+    const size_t i = ok ? gc.at(x, y, z0 + k) : 0;
+    rI[k] = ok ? __ldg(splatI + i) : 0u;
+    rL[k] = ok ? __ldg(splatL + i) : 0u;
+  }
+  // inside a step: no predictor value within one voxel of the block
+  const bool clear = pbrick && !block_any_brick(gc, pbrick, 1, 1, 1, z0, z0 + kDyeResolveZ - 1);
+  if (!inside) return;
+  const bool shellXY = x == 0 || x >= gc.nx - 1 || y >= gc.ny - 1;
+  const bool inFloorZone = y <= 7;
+  unsigned need = 0u;
+#pragma unroll
+  for (int k = 0; k < kDyeResolveZ; ++k) {
+    const int z = z0 + k;
+    if (z >= gc.nz) break;
+    // the boundary shell, and clear water's early-out (every predictor tap
+    // +0, so oct0 = oct1 = 0 below) outside the floor zone
+    if (shellXY || z == 0 || z >= gc.nz - 1 || (clear && !inFloorZone && rI[k] == 0u && rL[k] == 0u))
+      st4(out + gc.at(x, y, z), make_float4(0.f, 0.f, 0.f, 0.f));
+    else
+      need |= 1u << k;
+  }
+  const StepParams& P = *Pp;
+  while (need) {
+    const int k = __ffs(need) - 1;
+    need &= need - 1u;
+    resolve_ref_cell<VS, DS>(gc, g, P, cen, conc, pred, splatI, splatL, out, cbrick_out, x, y, z0 + k);
+  }
 }
 
 // Closed box: MacCormack correction of the single dye, 8-tap min/max limiter.
@@ -849,8 +903,8 @@ void launch_mac_rhs(const DevState& s, cudaStream_t st) {
                                                            (const VS*)s.w, s.wave, s.rhs, nullptr);
   });
   if (!s.ref) {  // compatibility of the pure-Neumann problem: zero-mean right-hand side
-    launch_sum(s.rhs, s.g.n(), s.red + RED_RHS_SUM, s.num_sms, st);
-    launch_sub_mean(s.rhs, s.g.n(), s.red + RED_RHS_SUM, s.num_sms, st);
+    launch_sum(s.rhs, s.g.n(), s.part + PART_RHS * kSumBlocks, s.num_sms, st);
+    launch_sub_mean(s.rhs, s.g.n(), s.part + PART_RHS * kSumBlocks, s.num_sms, st);
   }
 }
 
@@ -879,10 +933,18 @@ void launch_conc_predict(const DevState& s, cudaStream_t st, bool bracket, bool 
   if (pb) cudaMemsetAsync(pb, 0, brick_grid(s.gc).n() * sizeof(uint32_t), st);
   const uint32_t* cb = s.ref && sparse ? brick_flags_of(s, s.conc) : nullptr;
   DOB_VEL_DISPATCH(s.prec, {
-    k_conc_predict<VS, DS><<<cell_grid(s.gc), cell_block(), 0, st>>>(
-        s.gc, s.g, s.params, s.ref, (const typename Vec4Of<VS>::type*)s.cen,
-        (const typename Vec4Of<DS>::type*)s.conc, (const DS*)s.conc, (DS*)s.pred,
-        bracket && !s.ref ? (DS*)s.lim : nullptr, cb, pb);
+    if (cb) {
+      dim3 gr = cell_grid(s.gc);
+      gr.z = (s.gc.nz + kDyeResolveZ - 1) / kDyeResolveZ;
+      k_conc_predict<VS, DS, kDyeResolveZ><<<gr, cell_block(), 0, st>>>(
+          s.gc, s.g, s.params, s.ref, (const typename Vec4Of<VS>::type*)s.cen,
+          (const typename Vec4Of<DS>::type*)s.conc, (const DS*)s.conc, (DS*)s.pred, nullptr, cb, pb);
+    } else {
+      k_conc_predict<VS, DS, 1><<<cell_grid(s.gc), cell_block(), 0, st>>>(
+          s.gc, s.g, s.params, s.ref, (const typename Vec4Of<VS>::type*)s.cen,
+          (const typename Vec4Of<DS>::type*)s.conc, (const DS*)s.conc, (DS*)s.pred,
+          bracket && !s.ref ? (DS*)s.lim : nullptr, nullptr, pb);
+    }
   });
 }
 
@@ -899,7 +961,9 @@ void launch_conc_resolve(const DevState& s, cudaStream_t st, bool sparse) {
   if (cb) cudaMemsetAsync(cb, 0, brick_grid(s.gc).n() * sizeof(uint32_t), st);
   DOB_VEL_DISPATCH(s.prec, {
     if (s.ref) {
-      k_conc_resolve_ref<VS, DS><<<cell_grid(s.gc), cell_block(), 0, st>>>(
+      dim3 gr = cell_grid(s.gc);
+      gr.z = (s.gc.nz + kDyeResolveZ - 1) / kDyeResolveZ;
+      k_conc_resolve_ref<VS, DS><<<gr, cell_block(), 0, st>>>(
           s.gc, s.g, s.params, (const typename Vec4Of<VS>::type*)s.cen, (const typename Vec4Of<DS>::type*)s.conc,
           (const DS*)s.pred, s.splatI, s.splatL, (typename Vec4Of<DS>::type*)s.conc2, sparse ? s.pbrick : nullptr,
           cb);

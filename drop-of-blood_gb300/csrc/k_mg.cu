@@ -625,7 +625,7 @@ __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
   hi = s;
   lo = lo + err;
 }
-__global__ void k_sum64(const float* __restrict__ a, size_t n, double* __restrict__ out) {
+__global__ void k_sum64(const float* __restrict__ a, size_t n, double* __restrict__ part) {
   float hi = 0.0f, lo = 0.0f;
   const size_t n4 = n >> 2;
   const float4* a4 = reinterpret_cast<const float4*>(a);
@@ -638,7 +638,7 @@ __global__ void k_sum64(const float* __restrict__ a, size_t n, double* __restric
   }
   for (size_t i = 4 * n4 + blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     two_sum_acc(hi, lo, a[i]);
-  block_sum_atomic((double)hi + (double)lo, out);
+  block_sum_store((double)hi + (double)lo, part);
 }
 // sum of squares: per-thread error-free FP32 accumulation, FP64 across threads
 __global__ void k_sumsq64(const float* __restrict__ a, size_t n, double* __restrict__ out) {
@@ -651,13 +651,17 @@ __global__ void k_sumsq64(const float* __restrict__ a, size_t n, double* __restr
   }
   block_sum_atomic((double)hi + (double)lo, out);
 }
-// a[i] -= mean, with the mean summed in FP64 and applied in FP32; sumsq
-// (statistics): also the sum of squares of the result, accumulated as
-// k_sumsq64 does (no separate pass over the array).
-__global__ void k_sub_mean(float* __restrict__ a, size_t n, const double* __restrict__ sum,
+// a[i] -= mean, with the mean summed in FP64 (k_sum64's nb partials, added
+// in a fixed order) and applied in FP32; sumsq (statistics): also the sum
+// of squares of the result, accumulated as k_sumsq64 does (no separate
+// pass over the array).
+__global__ void k_sub_mean(float* __restrict__ a, size_t n, const double* __restrict__ part, int nb,
                            double* __restrict__ sumsq) {
   __shared__ float s_mean;
-  if (threadIdx.x == 0) s_mean = (float)(*sum / (double)n);
+  if (threadIdx.x < 32) {
+    const double sum = sum_partials(part, nb);
+    if (threadIdx.x == 0) s_mean = (float)(sum / (double)n);
+  }
   __syncthreads();
   const float mean = s_mean;
   const size_t n4 = n >> 2;
@@ -948,23 +952,26 @@ __global__ void k_add_df(float* __restrict__ p, float* __restrict__ plo, const f
 }
 // sum of p + plo (per-thread double-float, FP64 across threads)
 __global__ void k_sum_df(const float* __restrict__ p, const float* __restrict__ plo, size_t n,
-                         double* __restrict__ out) {
+                         double* __restrict__ part) {
   float hi = 0.0f, lo = 0.0f;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     float e;
     two_sum(hi, p[i], hi, e);
     lo += e + plo[i];
   }
-  block_sum_atomic((double)hi + (double)lo, out);
+  block_sum_store((double)hi + (double)lo, part);
 }
-// (p, plo) -= mean, with the mean as a double-float pair
+// (p, plo) -= mean, with the mean (k_sum_df's nb partials, added in a fixed
+// order) as a double-float pair
 __global__ void k_sub_mean_df(float* __restrict__ p, float* __restrict__ plo, size_t n,
-                              const double* __restrict__ sum) {
+                              const double* __restrict__ part, int nb) {
   __shared__ float s_mh, s_ml;
-  if (threadIdx.x == 0) {
-    const double m = *sum / (double)n;
-    s_mh = (float)m;
-    s_ml = (float)(m - (double)s_mh);
+  if (threadIdx.x < 32) {
+    const double m = sum_partials(part, nb) / (double)n;
+    if (threadIdx.x == 0) {
+      s_mh = (float)m;
+      s_ml = (float)(m - (double)s_mh);
+    }
   }
   __syncthreads();
   const float mh = s_mh, ml = s_ml;
@@ -1060,12 +1067,13 @@ cudaError_t mg_prepare() {
   return e;
 }
 
-void launch_sum(const float* a, size_t n, double* out, int num_sms, cudaStream_t st) {
-  cudaMemsetAsync(out, 0, sizeof(double), st);
-  k_sum64<<<num_sms * 4, 256, 0, st>>>(a, n, out);
+// blocks of the partial-sum launches (one slot each in a kSumBlocks array)
+static int sum_blocks(int num_sms) { return num_sms * 4 < kSumBlocks ? num_sms * 4 : kSumBlocks; }
+void launch_sum(const float* a, size_t n, double* part, int num_sms, cudaStream_t st) {
+  k_sum64<<<sum_blocks(num_sms), 256, 0, st>>>(a, n, part);
 }
-void launch_sub_mean(float* a, size_t n, const double* sum, int num_sms, cudaStream_t st, double* sumsq) {
-  k_sub_mean<<<num_sms * 4, 256, 0, st>>>(a, n, sum, sumsq);
+void launch_sub_mean(float* a, size_t n, const double* part, int num_sms, cudaStream_t st, double* sumsq) {
+  k_sub_mean<<<num_sms * 4, 256, 0, st>>>(a, n, part, sum_blocks(num_sms), sumsq);
 }
 void launch_sumsq(const float* a, size_t n, double* out, int num_sms, cudaStream_t st) {
   k_sumsq64<<<num_sms * 4, 256, 0, st>>>(a, n, out);
@@ -1355,9 +1363,9 @@ static void mixed_solve(const DevState& s, cudaStream_t st) {
     k_add_df<<<s.num_sms * 4, 256, 0, st>>>(s.p, s.plo, s.e0, n, done);
   }
   if (!s.ref) {
-    cudaMemsetAsync(s.red + RED_P_SUM, 0, sizeof(double), st);
-    k_sum_df<<<s.num_sms * 4, 256, 0, st>>>(s.p, s.plo, n, s.red + RED_P_SUM);
-    k_sub_mean_df<<<s.num_sms * 4, 256, 0, st>>>(s.p, s.plo, n, s.red + RED_P_SUM);
+    double* part = s.part + PART_P * kSumBlocks;
+    k_sum_df<<<sum_blocks(s.num_sms), 256, 0, st>>>(s.p, s.plo, n, part);
+    k_sub_mean_df<<<s.num_sms * 4, 256, 0, st>>>(s.p, s.plo, n, part, sum_blocks(s.num_sms));
   }
 }
 
@@ -1450,8 +1458,8 @@ void launch_pressure_solve(const DevState& s, cudaStream_t st) {
   for (int l = 0; l < s.nlev; ++l) { E[l] = s.lv[l].e; B[l] = s.lv[l].b; }
   for (int c = 0; c < s.cycles; ++c) vcycle<float>(s, s.p, s.rhs, E, B, false, nullptr, st);
   if (!s.ref) {
-    launch_sum(s.p, n, s.red + RED_P_SUM, s.num_sms, st);
-    launch_sub_mean(s.p, n, s.red + RED_P_SUM, s.num_sms, st);
+    launch_sum(s.p, n, s.part + PART_P * kSumBlocks, s.num_sms, st);
+    launch_sub_mean(s.p, n, s.part + PART_P * kSumBlocks, s.num_sms, st);
   }
 }
 

@@ -1,4 +1,5 @@
-"""Autograd-Function-style wrapper of the discrete adjoint (closed box, FP32).
+"""Autograd-Function-style wrapper of the discrete adjoint (closed box, FP32 or
+mixed precision).
 
     traj = DropTrajectory(sim, checkpoint_every=8)
     dye = traj.forward(32)                 # dob_tape_forward

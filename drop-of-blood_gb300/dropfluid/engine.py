@@ -210,7 +210,7 @@ class DropFluid:
                  "dob_bench_kernel")
         return float(ms.value), float(by.value)
 
-    # -- discrete adjoint (closed box, FP32, dye_refine 1) ------------------------------------
+    # -- discrete adjoint (closed box, FP32 or mixed, dye_refine 1) ---------------------------
     def adjoint_stage(self, stage):
         """Transpose of the Jacobian of one stage at the current forward state
         (field conventions of dob_adjoint_stage)."""

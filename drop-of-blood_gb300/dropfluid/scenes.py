@@ -178,13 +178,15 @@ def box96(seed: int = 7, impulse_scale: float = 1.0) -> Scene:
                                          16384, seed + 2)])
 
 
-def box192_adjoint(impulse_scale=(1.0, 1.0, 1.0), shift=((0.0, 0.0, 0.0),) * 3, edge_cells: float = 2.0) -> Scene:
+def box192_adjoint(impulse_scale=(1.0, 1.0, 1.0), shift=((0.0, 0.0, 0.0),) * 3, edge_cells: float = 2.0,
+                   precision: int = abi.DOB_PREC_FP32) -> Scene:
     """The box192 drops, all released at step 0 as soft-edged drops (edge
     `edge_cells` wide, so the loss is differentiable in their centres), 64
     steps: the full-size forward + adjoint case.  impulse_scale / shift
-    perturb each drop's velocity and centre (for targets and differences)."""
-    sc = box192()
-    sc.name = "box192_adjoint"
+    perturb each drop's velocity and centre (for targets and differences);
+    precision DOB_PREC_MIXED gives the box192_mixed solve and storage."""
+    sc = box192(precision)
+    sc.name = "box192_adjoint" if precision == abi.DOB_PREC_FP32 else "box192_adjoint_mixed"
     sc.steps = 64
     for k, d in enumerate(sc.drops):
         d.release_step = 0

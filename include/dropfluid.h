@@ -167,7 +167,8 @@ typedef enum dob_field {
                                   205-240)                                             */
   DOB_FIELD_BRICKS_RAW = 15,   /* read-only: raw brick occupancy 0/1 (lighting.ts:172-203) */
   DOB_FIELD_COUNT = 16,
-  /* Adjoint fields (closed box, FP32, dye_refine 1; see dob_adjoint_stage).
+  /* Adjoint fields (closed box, FP32 or mixed, dye_refine 1; see
+     dob_adjoint_stage).
      Host FP32, natural layout.  ADJ_VEL_U/V/W: adjoint of the MAC faces a
      stage reads (after dob_tape_backward: d loss / d initial velocity);
      ADJ_VEL_U2/V2/W2: adjoint of the faces advection / Casson write to
@@ -363,8 +364,8 @@ dob_status dob_memory_bytes(const dob_ctx* ctx, uint64_t* bytes);
 dob_status dob_save_state(dob_ctx* ctx, int slot);
 dob_status dob_load_state(dob_ctx* ctx, int slot);
 
-/* ---- discrete adjoint (no counterpart in the reference; closed box, FP32,
-        dye_refine 1) ------------------------------------------------------
+/* ---- discrete adjoint (no counterpart in the reference; closed box, FP32
+        or DOB_PREC_MIXED, dye_refine 1) -----------------------------------
 
    dob_adjoint_stage runs the transpose of the Jacobian of one stage at the
    current forward state (the state the forward stage would read), on the
@@ -374,18 +375,27 @@ dob_status dob_load_state(dob_ctx* ctx, int slot);
      CASSON_FORCES   ADJ_VEL_*2 -> ADJ_VEL_*, ADJ_CONC
      MAC_RHS         ADJ_RHS -> ADJ_VEL_* (ADJ_RHS is made mean-free in place)
      PRESSURE_SOLVE  ADJ_PRESSURE -> ADJ_PRESSURE (replaced), ADJ_RHS
+                     FP32: the transpose of the mg_cycles V-cycles (the
+                     replaced ADJ_PRESSURE is the adjoint of the warm start);
+                     mixed: the forward is solved to a tolerance, so its
+                     adjoint is that of an exact solve: ADJ_RHS += lam with
+                     A lam = ADJ_PRESSURE solved by the mixed solver to a
+                     relative residual of 1e-6, ADJ_PRESSURE set to 0
      PROJECT         ADJ_VEL_* -> ADJ_VEL_* (replaced), ADJ_PRESSURE
      CONC_PREDICT    ADJ_PRED -> ADJ_CONC, ADJ_CENTER
      CONC_RESOLVE    ADJ_CONC2 -> ADJ_CONC, ADJ_PRED, ADJ_CENTER
    Other stages return DOB_EINVAL.  Where the forward is not differentiable
    (clamps at their bounds, the dye limiter, |grad u| = 0) the adjoint takes
-   the branch the forward executed. */
+   the branch the forward executed.  In the mixed mode the dye and the
+   predictor are read at their binary16 values (the adjoint of a rounding
+   store is the identity); the adjoint fields stay FP32. */
 dob_status dob_adjoint_stage(dob_ctx* ctx, int stage);
 
 /* Forward half of the forward/backward pair: sets the centre velocity from
    the MAC faces (so the trajectory's state is velocity, dye and pressure),
    then runs nsteps steps, keeping a checkpoint of (velocity, dye, pressure)
-   every `checkpoint_every` steps in device memory.  The steps of the last
+   every `checkpoint_every` steps in device memory (mixed mode: the dye at
+   its binary16 width and the pressure as its FP32 pair).  The steps of the last
    segment also record the linearisation points the backward needs, so the
    next dob_tape_backward does not recompute that segment.  The context ends
    in the final state, as after dob_step (same bits). */
@@ -410,7 +420,7 @@ dob_status dob_adjoint_sphere_impulse(dob_ctx* ctx, const float center[3], float
    DOB_FIELD_ADJ_CONC of the state right after the drop (after
    dob_tape_backward: the trajectory's initial state).  out[0] = d loss / d s
    for injected velocity s * vel at s = 1 (the noise is not scaled); out[1..3]
-   = d loss / d center (world units).  Closed box, FP32, dye_refine 1. */
+   = d loss / d center (world units).  Closed box, FP32 or mixed, dye_refine 1. */
 dob_status dob_adjoint_sphere_soft(dob_ctx* ctx, const float center[3], float radius, float edge, float dye,
                                    const float vel[3], float noise_sigma, uint64_t seed, double out[4]);
 

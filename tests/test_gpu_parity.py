@@ -785,3 +785,60 @@ def test_lighting_flag_runs_once_per_call(gpu_lib):
     assert ei.value.status == abi.DOB_ESTATE
     for e in (a, b, r):
         e.close()
+
+
+@pytest.mark.parametrize("prec", [0, 2])
+def test_reference_step_sparse_dye_equals_stage_launches(gpu_lib, prec):
+    """Inside a step the reference-mode predictor and resolve skip clear
+    water by 8x8x8 brick flags, four planes per thread; launched as single
+    stages they trace every voxel.  With the dye in one corner of the grid,
+    three steps (graph replays) give the same bits as the same stages
+    launched one by one, in FP32 and with binary16 storage."""
+    abi = _abi()
+    from dropfluid import DropFluid
+    cfg = ref_config(prec=prec)
+    cfg.physics_flags = abi.DOB_PHYS_REFERENCE_ALL
+    st = ref_state(cfg, seed=5)
+    conc = st[abi.FIELD_CONC]
+    keep = np.zeros(conc.shape[:3], bool)
+    keep[4:28, 40:84, 6:30] = True  # (z, y, x) of the 64x96x64 dye grid
+    conc[~keep] = 0.0
+    blk = ref_block(spawn=0)
+    a, b = DropFluid(cfg), DropFluid(cfg)
+    for e in (a, b):
+        e.set_uniforms(blk)
+        load_state(e, st)
+    order = [abi.STAGE_ADVECT_MAC, abi.STAGE_MAC_TO_CENTER, abi.STAGE_CURL, abi.STAGE_CASSON_FORCES,
+             abi.STAGE_MAC_RHS, abi.STAGE_PRESSURE_SOLVE, abi.STAGE_PROJECT, abi.STAGE_MAC_TO_CENTER,
+             abi.STAGE_CLEAR_SPLATS, abi.STAGE_PARCEL_EMIT, abi.STAGE_PARCEL_ADVECT, abi.STAGE_CONC_PREDICT,
+             abi.STAGE_CONC_RESOLVE]
+    for _ in range(3):
+        a.step(1)
+        for s in order:
+            b.run_stage(s)
+    for f in (abi.FIELD_VEL_U, abi.FIELD_VEL_V, abi.FIELD_VEL_W, abi.FIELD_PRESSURE, abi.FIELD_CONC,
+              abi.FIELD_CONC_PRED):
+        assert bits_equal(a.get_field(f), b.get_field(f)), f
+    c = a.get_field(abi.FIELD_CONC)
+    assert (c[..., 1] > 0).any() and (c[..., 1] == 0).mean() > 0.5
+    a.close()
+    b.close()
+
+
+def test_mixed_steps_are_reproducible(gpu_lib):
+    """The mixed mode's mean removal sums per-block partials in a fixed order
+    (not FP64 atomics in completion order), so two runs of the same steps
+    give the same bits; the double-float pressure's low part would
+    otherwise carry the last bits of whichever order the blocks finished in."""
+    abi = _abi()
+    from dropfluid import DropFluid, scenes
+    out = []
+    for _ in range(2):
+        sc = scenes.box192(abi.DOB_PREC_MIXED)
+        e = DropFluid(sc.config)
+        sc.release(e, 0)
+        e.step(3)
+        out.append({f: e.get_field(f) for f in (abi.FIELD_VEL_U, abi.FIELD_PRESSURE, abi.FIELD_CONC)})
+        e.close()
+    for f in out[0]:
+        assert bits_equal(out[0][f], out[1][f]), f
