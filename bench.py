@@ -570,6 +570,38 @@ def reference_stage_bytes(cfg, high_water):
     }
 
 
+RENDER_W, RENDER_H = 960, 540  # the reference renders its volume pass at half of a 1920x1080 canvas
+
+
+def render_frame(e, block):
+    """The plume render (dob_render_plume) of the live state: a submerged
+    camera 0.6 m in front of the impact point, just below the meniscus,
+    looking up at the drained plume, the last substep's drops, a synthetic
+    stand-in for the spectral table; one render for the image (light volume
+    + march, copied to the host), then 10 timed launches of the march alone
+    (dob_bench_kernel 3)."""
+    import numpy as np
+    from dropfluid import uniforms as U
+    eye, target = (0.0, 0.10, 0.60), (0.0, 0.20, 0.0)
+    vp, ivp = U.camera_matrices(eye, target, 40.0, RENDER_W / RENDER_H)
+    blk = np.array(block, np.float32).copy()
+    blk[0:16], blk[16:32], blk[32:35] = ivp, vp, eye
+    blk[36], blk[37] = RENDER_W, RENDER_H
+    blk[56] = max(0.20, float(np.linalg.norm(np.subtract(target, eye))))
+    e.set_uniforms(blk)
+    e.set_spectral_lut(U.synthetic_spectral_lut())
+    img = e.render_plume(RENDER_W, RENDER_H)
+    f = img.view(np.float16).astype(np.float32)
+    e.bench_kernel(3, reps=2)
+    ms, _ = e.bench_kernel(3, reps=10)
+    px = RENDER_W * RENDER_H
+    return {"width": RENDER_W, "height": RENDER_H, "ms_per_frame": ms, "rays_per_s": px / (ms * 1e-3),
+            "frames_per_s": 1e3 / ms, "pixels_through_dye": float((f[..., 3] > 0).mean()),
+            "tau_total_max": float(f[..., 3].max()),
+            "note": "marchPlume (render.ts:1593-2109) from fsMain's camera ray as the submerged primary march, "
+                    "one thread per pixel; synthetic spectral table; light volume not included in the time"}
+
+
 def reference_mode_leg(peak, substeps=60):
     """The reference's own setup (dob_config_reference: 96x128x96 velocity,
     192x256x192 four-channel dye, reference V-cycle schedule, 393216
@@ -618,13 +650,14 @@ def reference_mode_leg(peak, substeps=60):
                      "frac_of_measured_hbm": lk_bytes / (lk_ms * 1e-3) / 1e9 / peak,
                      "kernels": 2, "note": "light volume + brick dilation (lighting.ts:19-240), once per frame; "
                                            "20 launches on the live state, CUDA events"}
+            render = render_frame(e, blocks[-1][0])
             out[name] = {
                 "steps_per_s_e2e": substeps / wall, "e2e_path": "dob_step_uniforms, one 512-byte block per substep",
                 "steps_per_s_device": 1e3 / ms, "ms_per_step_device": ms,
                 "bytes_per_step": total, "achieved_gbs": total / (ms * 1e-3) / 1e9,
                 "frac_of_measured_hbm": total / (ms * 1e-3) / 1e9 / peak,
                 "spawned_parcels": int(sum(b[1] for b in blocks)), "high_water": seq.high_water,
-                "stages": stages, "dominant_stage": dom[0], "light_volume": light,
+                "stages": stages, "dominant_stage": dom[0], "light_volume": light, "plume_render": render,
                 "launches_per_step": e.launches_per_step(),
             }
             e.close()

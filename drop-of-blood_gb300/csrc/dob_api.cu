@@ -594,6 +594,8 @@ void dob_destroy(dob_ctx* ctx) {
   for (auto& sn : ctx->snaps)
     for (void* p : sn.bufs) cudaFree(p);
   for (void* p : ctx->allocs) cudaFree(p);
+  if (ctx->lut) cudaFree(ctx->lut);
+  if (ctx->image) cudaFree(ctx->image);
   if (ctx->host_params) cudaFreeHost(ctx->host_params);
   for (int k = 0; k < kParamRing; ++k)
     if (ctx->param_ev[k]) cudaEventDestroy(ctx->param_ev[k]);
@@ -984,6 +986,48 @@ dob_status dob_light_volume(dob_ctx* ctx) {
   return DOB_OK;
 }
 
+dob_status dob_set_spectral_lut(dob_ctx* ctx, const float* rgba, size_t bytes) {
+  if (!ctx || !rgba) return DOB_EINVAL;
+  const size_t want = (size_t)DOB_SPECTRAL_LUT_W * DOB_SPECTRAL_LUT_H * 4 * sizeof(float);
+  if (bytes != want) return fail(ctx, DOB_EINVAL, "dob_set_spectral_lut", "need 256 x 64 x 4 floats");
+  if (!ctx->lut) CK(cudaMalloc((void**)&ctx->lut, want));
+  CK(cudaMemcpyAsync(ctx->lut, rgba, want, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return DOB_OK;
+}
+
+// the image buffer for a W x H render (8 halves per pixel)
+static dob_status render_prepare(dob_ctx* ctx, uint32_t w, uint32_t h, const char* what) {
+  if (!ctx->s.light) return fail(ctx, DOB_ESTATE, what, "reference mode with nx, ny, nz divisible by 4 only");
+  if (!ctx->lut) return fail(ctx, DOB_ESTATE, what, "no spectral table (dob_set_spectral_lut)");
+  if (w < 1 || h < 1 || w > 8192 || h > 8192) return fail(ctx, DOB_EINVAL, what, "image size out of 1..8192");
+  const size_t need = (size_t)w * h * 8 * sizeof(__half);
+  if (need > ctx->image_cap) {
+    if (ctx->image) cudaFree(ctx->image);
+    ctx->image = nullptr;
+    ctx->image_cap = 0;
+    CK(cudaMalloc((void**)&ctx->image, need));
+    ctx->image_cap = need;
+  }
+  ctx->render_w = (int)w;
+  ctx->render_h = (int)h;
+  return upload_params(ctx, 0u);
+}
+
+dob_status dob_render_plume(dob_ctx* ctx, uint32_t width, uint32_t height, uint16_t* out, size_t bytes) {
+  if (!ctx || !out) return DOB_EINVAL;
+  if (bytes != (size_t)width * height * 8 * sizeof(uint16_t))
+    return fail(ctx, DOB_EINVAL, "dob_render_plume", "byte count != width x height x 8 halves");
+  dob_status st = render_prepare(ctx, width, height, "dob_render_plume");
+  if (st != DOB_OK) return st;
+  launch_light_volume(ctx->s, ctx->stream);
+  launch_render_plume(ctx->s, ctx->lut, (int)width, (int)height, ctx->image, ctx->stream);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(out, ctx->image, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return DOB_OK;
+}
+
 dob_status dob_sync(dob_ctx* ctx) {
   if (!ctx) return DOB_EINVAL;
   CK(cudaStreamSynchronize(ctx->stream));
@@ -1030,7 +1074,7 @@ dob_status dob_time_steps(dob_ctx* ctx, int nsteps, uint32_t flags, float* ms) {
 }
 
 dob_status dob_bench_kernel(dob_ctx* ctx, int which, int reps, float* avg_ms, double* bytes_per_launch) {
-  if (!ctx || !avg_ms || reps < 1 || which < 0 || which > 2) return DOB_EINVAL;
+  if (!ctx || !avg_ms || reps < 1 || which < 0 || which > 3) return DOB_EINVAL;
   if (which == 1) {
     if (!(ctx->s.flags & DOB_PHYS_WAVE))
       return fail(ctx, DOB_ESTATE, "dob_bench_kernel", "context created without DOB_PHYS_WAVE");
@@ -1042,12 +1086,22 @@ dob_status dob_bench_kernel(dob_ctx* ctx, int which, int reps, float* avg_ms, do
     dob_status st = upload_params(ctx, 0u);
     if (st != DOB_OK) return st;
   }
+  if (which == 3) {
+    if (!ctx->render_w) return fail(ctx, DOB_ESTATE, "dob_bench_kernel", "no render yet (dob_render_plume)");
+    dob_status st = render_prepare(ctx, (uint32_t)ctx->render_w, (uint32_t)ctx->render_h, "dob_bench_kernel");
+    if (st != DOB_OK) return st;
+  }
   CK(cudaStreamSynchronize(ctx->stream));
   double total = 0.0, bytes = 0.0;
   for (int r = 0; r < reps; ++r) {
     CK(cudaEventRecord(ctx->ev0, ctx->stream));
     if (which == 0) {
       bytes = smoother_pass(ctx->s, ctx->stream);
+    } else if (which == 3) {
+      // plume march: the image written once (16 B per pixel); the volumes it
+      // samples stay in L2 across rays and are not counted
+      launch_render_plume(ctx->s, ctx->lut, ctx->render_w, ctx->render_h, ctx->image, ctx->stream);
+      bytes = 16.0 * ctx->render_w * ctx->render_h;
     } else if (which == 2) {
       // light volume: the 4-channel dye read once (every dye voxel is a tap
       // of some centre sample), the light volume written once (8 B per

@@ -76,6 +76,12 @@ struct dob_ctx {
     bool pending = false;
     int cycles = 0;               // V-cycles of the step (FP32 pressure)
   } async_slots[8];
+  // plume render (dob_render_plume): the caller's spectral table (256 x 64
+  // float4) and the image buffer (8 halves per pixel), grown on demand
+  float4* lut = nullptr;
+  __half* image = nullptr;
+  size_t image_cap = 0;
+  int render_w = 0, render_h = 0;  // the last render's size (dob_bench_kernel 3)
 };
 
 namespace dob {

@@ -263,6 +263,9 @@ void launch_project(const DevState& s, cudaStream_t st);
 void launch_wave_step(const DevState& s, cudaStream_t st);
 // ---- light volume and brick occupancy (k_light.cu) ------------------------------------------
 bool light_dims_ok(const Grid& g);
+// ---- the plume render (k_render.cu) --------------------------------------------------------
+// lut: 256 x 64 float4 (spectral transmittance); out: W x H x 8 halves
+void launch_render_plume(const DevState& s, const float4* lut, int W, int H, __half* out, cudaStream_t st);
 void launch_light_volume(const DevState& s, cudaStream_t st);
 // ---- closed-box column kernels of the step graph (k_box.cu) ------------------------------
 // Same results as launch_casson / launch_mac_rhs / launch_project followed by

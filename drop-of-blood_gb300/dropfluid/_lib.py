@@ -37,6 +37,8 @@ SIGNATURES = {
     "dob_run_stage": (C.c_int, [P, C.c_int]),
     "dob_wave_step": (C.c_int, [P]),
     "dob_light_volume": (C.c_int, [P]),
+    "dob_set_spectral_lut": (C.c_int, [P, C.c_void_p, C.c_size_t]),
+    "dob_render_plume": (C.c_int, [P, C.c_uint32, C.c_uint32, C.c_void_p, C.c_size_t]),
     "dob_sync": (C.c_int, [P]),
     "dob_memory_bytes": (C.c_int, [P, C.POINTER(C.c_uint64)]),
     "dob_launches_per_step": (C.c_int, [P, C.POINTER(C.c_int)]),

@@ -29,6 +29,7 @@ UNITS = {
     "k_exact.cu": ["-fmad=false"],
     "k_wave.cu": ["-fmad=false"],
     "k_light.cu": ["-fmad=false"],
+    "k_render.cu": ["-fmad=false"],
     "dob_noalloc.cu": [],
     "dob_tape.cu": [],
     "k_adjoint.cu": [],

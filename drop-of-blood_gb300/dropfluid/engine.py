@@ -178,6 +178,23 @@ class DropFluid:
         (reference mode); read them with FIELD_LIGHT / FIELD_BRICKS."""
         self._ck(self._L.dob_light_volume(self._h), "dob_light_volume")
 
+    def set_spectral_lut(self, lut):
+        """The renderer's 256 x 64 spectral transmittance table, (64, 256, 4)
+        float32 (u fastest)."""
+        a = np.ascontiguousarray(lut, np.float32)
+        if a.shape != (64, 256, 4):
+            raise ValueError("spectral table must be (64, 256, 4)")
+        self._ck(self._L.dob_set_spectral_lut(self._h, a.ctypes.data, a.nbytes), "dob_set_spectral_lut")
+
+    def render_plume(self, width, height):
+        """The plume render of the current state (dob_render_plume): (height,
+        width, 8) binary16 as uint16 -- radiance rgb, total optical depth,
+        transmittance rgb, intact-cell optical depth."""
+        out = np.zeros((int(height), int(width), 8), np.uint16)
+        self._ck(self._L.dob_render_plume(self._h, int(width), int(height), out.ctypes.data, out.nbytes),
+                 "dob_render_plume")
+        return out
+
     def sync(self):
         self._ck(self._L.dob_sync(self._h), "dob_sync")
 

@@ -149,3 +149,49 @@ def default_block(dt: float = FIXED_SIM_DT, sim_time: float = 0.0, global_seed: 
     """A block with the default config, no drops, and the given dt/time/seed."""
     p = SimUniformPacker()
     return p.pack(drops=DropSnapshot(sim_time=sim_time), dt=dt, global_seed=global_seed).copy()
+
+
+def camera_matrices(eye, target, fovy_deg: float = 40.0, aspect: float = 16.0 / 9.0, near: float = 0.01,
+                    far: float = 20.0):
+    """(view_proj, inv_view_proj) of a right-handed look-at camera with a
+    WebGPU clip range (z in [0, 1]), each 16 float32 in column-major order as
+    the uniform block stores them (the block's matrices are gl-matrix mat4s);
+    y is up."""
+    eye = np.asarray(eye, np.float64)
+    f = np.asarray(target, np.float64) - eye
+    f /= np.linalg.norm(f)
+    up = np.array([0.0, 1.0, 0.0]) if abs(f[1]) < 0.99 else np.array([1.0, 0.0, 0.0])
+    s = np.cross(f, up)
+    s /= np.linalg.norm(s)
+    u = np.cross(s, f)
+    view = np.eye(4)
+    view[0, :3], view[1, :3], view[2, :3] = s, u, -f
+    view[:3, 3] = -view[:3, :3] @ eye
+    t = 1.0 / math.tan(math.radians(fovy_deg) / 2.0)
+    proj = np.zeros((4, 4))
+    proj[0, 0] = t / aspect
+    proj[1, 1] = t
+    proj[2, 2] = far / (near - far)
+    proj[2, 3] = near * far / (near - far)
+    proj[3, 2] = -1.0
+    vp = proj @ view
+    return (vp.T.ravel().astype(np.float32), np.linalg.inv(vp).T.ravel().astype(np.float32))
+
+
+def synthetic_spectral_lut(seed: int = 0) -> np.ndarray:
+    """A stand-in for the renderer's 256 x 64 spectral transmittance table
+    (its shape and axes: u = tau / (0.012 + 0.996 tau), v = oxygenated
+    fraction; rgb transmittance falling with tau, blue and green faster than
+    red), (64, 256, 4) float32.  The reference builds its table from
+    tabulated absorption spectra on the host; a caller of the renderer
+    passes that table instead."""
+    rng = np.random.default_rng(seed)
+    u = (np.arange(256) + 0.5) / 256.0
+    tau = 0.012 * u / np.maximum(1.0 - 0.996 * u, 1e-6)
+    v = (np.arange(64) + 0.5) / 64.0
+    k = np.array([0.9, 5.5, 7.0]) * (1.0 + 0.05 * rng.standard_normal(3))
+    ox = np.array([0.4, -1.2, 0.6])
+    out = np.ones((64, 256, 4), np.float32)
+    for c in range(3):
+        out[:, :, c] = np.exp(-tau[None, :] * k[c] * (1.0 + 0.3 * ox[c] * v[:, None]))
+    return out

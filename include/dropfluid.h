@@ -339,7 +339,8 @@ dob_status dob_time_steps(dob_ctx* ctx, int nsteps, uint32_t flags, float* ms);
 /* Kernel micro-benchmark on the current state: launches the step's dominant
    kernel (which = 0: the level-0 pressure smoother pass; which = 1: one
    wave substep, its four kernels, on a context made with DOB_PHYS_WAVE;
-   which = 2: the light volume and brick passes, reference mode) `reps` times with
+   which = 2: the light volume and brick passes, reference mode; which = 3:
+   the plume march at the last dob_render_plume's size) `reps` times with
    CUDA events around each launch; returns the mean device ms per launch and
    the kernel's algorithmic bytes per launch (minimum HBM traffic of one
    pass).  No counterpart in the reference. */
@@ -363,6 +364,35 @@ dob_status dob_memory_bytes(const dob_ctx* ctx, uint64_t* bytes);
    and back.  Slots are allocated on first use. */
 dob_status dob_save_state(dob_ctx* ctx, int slot);
 dob_status dob_load_state(dob_ctx* ctx, int slot);
+
+/* ---- plume render (render.ts:1593-2109, 2411-2434, 2659-2688) -----------
+
+   The volumetric plume march of the reference renderer (marchPlume) as a
+   headless image: per pixel fsMain's camera ray and thin lens from the
+   uniform block (invViewProj, camera position, focal distance, aperture,
+   frame index for the jitter), driven as the submerged camera's primary
+   march from 0.02 to the flat meniscus plane (the reference refines rays
+   steeper than 0.052 upward against the waves; not restated), with the
+   reference's constants, fine quality and the inspect mode off.  Reference
+   mode with nx, ny, nz divisible by 4.
+
+   dob_set_spectral_lut stores the renderer's 256 x 64 spectral
+   transmittance table (the reference builds it on the host and uploads it
+   as an rgba texture: u = tau / (0.012 + 0.996 tau), v = oxygenated
+   fraction); host FP32, 4 floats (r, g, b, a) per texel, row-major, u
+   fastest.
+
+   dob_render_plume computes the light volume of the current state (the
+   frame's lighting pass, as dob_light_volume) and then, per pixel of a
+   width x height image (y down, pixel centres), 8 binary16 values: the
+   plume's radiance r, g, b, its total optical depth, its transmittance r,
+   g, b and its intact-cell optical depth; the composite is behind *
+   transmittance + radiance (render.ts:2632).  out: host, bytes = width x
+   height x 16.  Blocks until the image is on the host. */
+#define DOB_SPECTRAL_LUT_W 256
+#define DOB_SPECTRAL_LUT_H 64
+dob_status dob_set_spectral_lut(dob_ctx* ctx, const float* rgba, size_t bytes);
+dob_status dob_render_plume(dob_ctx* ctx, uint32_t width, uint32_t height, uint16_t* out, size_t bytes);
 
 /* ---- discrete adjoint (no counterpart in the reference; closed box, FP32
         or DOB_PREC_MIXED, dye_refine 1) -----------------------------------

@@ -1713,6 +1713,7 @@ template <class R> class Sim {
 #include "dob_oracle_adjoint.inc"
 #include "dob_oracle_wave.inc"
 #include "dob_oracle_light.inc"
+#include "dob_oracle_render.inc"
 };
 
 struct AnySim {
@@ -2036,6 +2037,10 @@ int orc_get_threads(void) { return omp_get_max_threads(); }
 
 // The light volume and brick passes (lighting.ts:19-240).
 int orc_light_volume(orc_sim* s) { return DISPATCH(s, light_volume()); }
+int orc_render_plume(orc_sim* s, const float* lut, int width, int height, uint16_t* out) {
+  if (!s || !lut || !out || width < 1 || height < 1) return DOB_EINVAL;
+  return DISPATCH(s, render_plume(lut, width, height, out));
+}
 
 // The wave substep on the simulation's wave field (wave.ts:55-388).
 int orc_wave_step(orc_sim* s) {

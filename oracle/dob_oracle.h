@@ -46,6 +46,9 @@ int orc_get_threads(void);
    tape keeps every step, no checkpoints). */
 int orc_wave_step(orc_sim* s);
 int orc_light_volume(orc_sim* s);
+/* the plume render (dob_render_plume): light volume, then 8 binary16 values
+   per pixel; lut: 256 x 64 x 4 floats */
+int orc_render_plume(orc_sim* s, const float* lut, int width, int height, uint16_t* out);
 int orc_wave_fft2(float* data, int inverse);
 int orc_adjoint_stage(orc_sim* s, int stage);
 int orc_tape_forward(orc_sim* s, int nsteps);

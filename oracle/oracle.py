@@ -66,6 +66,7 @@ def lib():
         L.orc_adjoint_stage.argtypes = [P, C.c_int]
         L.orc_wave_step.argtypes = [P]
         L.orc_light_volume.argtypes = [P]
+        L.orc_render_plume.argtypes = [P, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
         L.orc_wave_fft2.argtypes = [C.POINTER(C.c_float), C.c_int]
         L.orc_tape_forward.argtypes = [P, C.c_int]
         L.orc_tape_backward.argtypes = [P, C.POINTER(C.c_float), C.c_size_t]
@@ -219,6 +220,17 @@ class OracleSim:
     def light_volume(self):
         """The light volume and brick passes (lighting.ts:19-240)."""
         _check(lib().orc_light_volume(self._h), "light_volume")
+
+    def render_plume(self, width, height, lut):
+        """The plume render (render.ts:1593-2109 from fsMain's camera ray):
+        (height, width, 8) binary16 as uint16 (radiance rgb, tauTotal,
+        transmittance rgb, tauIntact); lut (64, 256, 4) float32."""
+        lut = np.ascontiguousarray(lut, np.float32)
+        assert lut.shape == (64, 256, 4)
+        out = np.zeros((height, width, 8), np.uint16)
+        _check(lib().orc_render_plume(self._h, lut.ctypes.data, int(width), int(height), out.ctypes.data),
+               "render_plume")
+        return out
 
     # -- discrete adjoint (closed box, dye_refine 1) ---------------------------------------
     def adjoint_stage(self, stage):
