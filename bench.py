@@ -573,7 +573,7 @@ def reference_stage_bytes(cfg, high_water):
 RENDER_W, RENDER_H = 960, 540  # the reference renders its volume pass at half of a 1920x1080 canvas
 
 
-def render_frame(e, block):
+def render_frame(e, block, cfg):
     """The plume render (dob_render_plume) of the live state: a submerged
     camera 0.6 m in front of the impact point, just below the meniscus,
     looking up at the drained plume, the last substep's drops, a synthetic
@@ -595,11 +595,37 @@ def render_frame(e, block):
     e.bench_kernel(3, reps=2)
     ms, _ = e.bench_kernel(3, reps=10)
     px = RENDER_W * RENDER_H
-    return {"width": RENDER_W, "height": RENDER_H, "ms_per_frame": ms, "rays_per_s": px / (ms * 1e-3),
-            "frames_per_s": 1e3 / ms, "pixels_through_dye": float((f[..., 3] > 0).mean()),
-            "tau_total_max": float(f[..., 3].max()),
-            "note": "marchPlume (render.ts:1593-2109) from fsMain's camera ray as the submerged primary march, "
-                    "one thread per pixel; synthetic spectral table; light volume not included in the time"}
+    out = {"width": RENDER_W, "height": RENDER_H, "ms_per_frame": ms, "rays_per_s": px / (ms * 1e-3),
+           "frames_per_s": 1e3 / ms, "pixels_through_dye": float((f[..., 3] > 0).mean()),
+           "tau_total_max": float(f[..., 3].max()),
+           "note": "marchPlume (render.ts:1593-2109) from fsMain's camera ray as the submerged primary march, "
+                   "one thread per pixel; synthetic spectral table; light volume not included in the time"}
+    # the same frame at a quarter of the pixels by the oracle on the host
+    # cores (its restatement of the march), bits compared with the device's
+    try:
+        import oracle
+        from dropfluid import abi
+        oracle.build()
+        oracle.set_threads(os.cpu_count() or 1)
+        w, h = RENDER_W // 2, RENDER_H // 2
+        vp2, ivp2 = U.camera_matrices(eye, target, 40.0, w / h)
+        blk[0:16], blk[16:32], blk[36], blk[37] = ivp2, vp2, w, h
+        e.set_uniforms(blk)
+        dev = e.render_plume(w, h)
+        o = oracle.OracleSim(cfg)
+        o.set_uniforms(blk)
+        for fld in (abi.FIELD_CONC, abi.FIELD_WAVE):
+            o.set_field(fld, e.get_field(fld))
+        t0 = time.perf_counter()
+        host = o.render_plume(w, h, U.synthetic_spectral_lut())
+        t = time.perf_counter() - t0
+        o.close()
+        out["cpu_reference"] = {"width": w, "height": h, "seconds": t, "rays_per_s": w * h / t,
+                                "cores": os.cpu_count(), "bits_equal_device": bool(np.array_equal(dev, host)),
+                                "kind": "port (oracle restatement, light volume included)"}
+    except Exception as ex:  # reported in the line, not raised
+        out["cpu_reference"] = {"error": str(ex)[:200]}
+    return out
 
 
 def reference_mode_leg(peak, substeps=60):
@@ -650,7 +676,7 @@ def reference_mode_leg(peak, substeps=60):
                      "frac_of_measured_hbm": lk_bytes / (lk_ms * 1e-3) / 1e9 / peak,
                      "kernels": 2, "note": "light volume + brick dilation (lighting.ts:19-240), once per frame; "
                                            "20 launches on the live state, CUDA events"}
-            render = render_frame(e, blocks[-1][0])
+            render = render_frame(e, blocks[-1][0], cfg)
             out[name] = {
                 "steps_per_s_e2e": substeps / wall, "e2e_path": "dob_step_uniforms, one 512-byte block per substep",
                 "steps_per_s_device": 1e3 / ms, "ms_per_step_device": ms,

@@ -20,9 +20,11 @@
 // with the library's own exp / pow / sqrt (dob_math.h), so the host oracle
 // reproduces every pixel's bits.
 //
-// GB300 layout: one thread per pixel in 16x8 tiles, so a warp's rays are
+// GB300 layout: one thread per pixel in 16x16 tiles, so a warp's rays are
 // neighbours and march through neighbouring texels; rays in clear water
-// leave through the brick skip after a few brick reads.
+// leave through the brick skip after a few brick reads.  Capped at 128
+// registers (two 256-thread blocks per SM): 2.44 -> 2.24 ms for a dense
+// 960x540 frame against 168 registers in 16x8 tiles (same bits).
 #define DOB_UNFUSED 1
 #include "dob_kernels.cuh"
 
@@ -30,7 +32,7 @@ namespace dob {
 namespace {
 
 constexpr int kLutW = 256, kLutH = 64;  // common.ts:22-23
-constexpr int kRenderBX = 16, kRenderBY = 8;
+constexpr int kRenderBX = 16, kRenderBY = 16;
 
 struct PlumeOut {
   dob_v3 radiance, transmittance, bentDir;
@@ -587,7 +589,7 @@ __device__ PlumeOut march_plume(const RenderTex<V4>& T, const StepParams& P, dob
 // at the flat meniscus plane.  Output per pixel, 8 halves: radiance rgb,
 // tauTotal, transmittance rgb, tauIntact.
 template <class V4>
-__global__ void __launch_bounds__(kRenderBX * kRenderBY)
+__global__ void __launch_bounds__(kRenderBX * kRenderBY, 2)
     k_render_plume(RenderTex<V4> T, const StepParams* __restrict__ Pp, int W, int H, __half* __restrict__ out) {
   const int px = blockIdx.x * kRenderBX + threadIdx.x;
   const int py = blockIdx.y * kRenderBY + threadIdx.y;
