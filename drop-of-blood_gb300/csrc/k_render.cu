@@ -12,9 +12,8 @@
 // linear clamp-to-edge sampler interpolates (in FP32): the light volume
 // (k_light.cu, binary16, velocity grid), the four-channel dye (dye grid),
 // the dilated 4x4x4 brick occupancy, the 512x512 wave field and a caller's
-// 256x64 spectral transmittance table.  The submerged ray ends at the flat
-// meniscus plane; the reference refines rays steeper than 0.052 upward with
-// intersectWaterSurface against the waves, which is not restated here.
+// 256x64 spectral transmittance table.  The submerged ray ends where it
+// crosses the wave surface (intersectWaterSurface, render.ts:1004-1128).
 //
 // Compiled without multiply-add contraction (DOB_UNFUSED, -fmad=false) and
 // with the library's own exp / pow / sqrt (dob_math.h), so the host oracle
@@ -158,6 +157,98 @@ __device__ float surface_height_smooth(const StepParams& P, const float4* wave, 
     h = dob_mix(s1, s0, g0y) * window;
   }
   return P.U[40] + h;
+}
+
+// marchSurfaceSegment (render.ts:1004-1067): the first crossing of the wave
+// surface on [segLo, segHi] in `steps` uniform steps, bisected 4 times
+// (on the cubic B-spline height where it brackets the crossing too), then
+// the secant point
+__device__ float march_surface_segment(const StepParams& P, const float4* wave, dob_v3 ro, dob_v3 rd, float segLo,
+                                       float segHi, int steps, bool fromAir) {
+  if (segHi <= segLo + 1e-5f) return -1.0f;
+  const float dt = (segHi - segLo) / (float)steps;
+  float prevT = segLo;
+  const dob_v3 p0 = ro + rd * prevT;
+  float prevF = p0.y - surface_height(P, wave, p0.x, p0.z);
+  for (int i = 1; i <= steps; ++i) {
+    const float currT = segLo + (float)i * dt;
+    const dob_v3 pC = ro + rd * currT;
+    const float currF = pC.y - surface_height(P, wave, pC.x, pC.z);
+    const bool crossed = fromAir ? (prevF >= 0.0f && currF <= 0.0f) : (prevF <= 0.0f && currF >= 0.0f);
+    if (crossed) {
+      float a = prevT, b = currT;
+      const dob_v3 pa0 = ro + rd * a, pb0 = ro + rd * b;
+      const float faSmooth = pa0.y - surface_height_smooth(P, wave, pa0.x, pa0.z);
+      const float fbSmooth = pb0.y - surface_height_smooth(P, wave, pb0.x, pb0.z);
+      const bool useSmooth = fromAir ? (faSmooth >= 0.0f && fbSmooth <= 0.0f) : (faSmooth <= 0.0f && fbSmooth >= 0.0f);
+      float fa = useSmooth ? faSmooth : prevF;
+      float fb = useSmooth ? fbSmooth : currF;
+      for (int j = 0; j < 4; ++j) {
+        const float mid = 0.5f * (a + b);
+        const dob_v3 pM = ro + rd * mid;
+        const float hM = useSmooth ? surface_height_smooth(P, wave, pM.x, pM.z) : surface_height(P, wave, pM.x, pM.z);
+        const float fm = pM.y - hM;
+        const bool midCross = fromAir ? (fa >= 0.0f && fm <= 0.0f) : (fa <= 0.0f && fm >= 0.0f);
+        if (midCross) {
+          b = mid;
+          fb = fm;
+        } else {
+          a = mid;
+          fa = fm;
+        }
+      }
+      const float denom = fb - fa;
+      const float frac = fabsf(denom) > 1e-6f ? dob_clampf(-fa / denom, 0.0f, 1.0f) : 0.5f;
+      return a + (b - a) * frac;
+    }
+    prevT = currT;
+    prevF = currF;
+  }
+  return -1.0f;
+}
+// intersectWaterSurface (render.ts:1069-1128)
+__device__ float intersect_water_surface(const StepParams& P, const float4* wave, dob_v3 ro, dob_v3 rd, float tMin,
+                                         float tMax, bool fromAir) {
+  const float baseY = P.U[40];
+  const float minH = baseY - 0.145f, maxH = baseY + 0.145f;
+  float tLo = tMin, tHi = tMax;
+  if (fabsf(rd.y) < 1e-4f) {
+    if (ro.y < minH || ro.y > maxH) return -1.0f;
+    tHi = dob_minf(tMax, tMin + 2.8f);
+  } else {
+    const float tA = (minH - ro.y) / rd.y, tB = (maxH - ro.y) / rd.y;
+    tLo = dob_maxf(tMin, dob_minf(tA, tB));
+    tHi = dob_minf(tMax, dob_maxf(tA, tB));
+    if (tHi < tLo) return -1.0f;
+  }
+  const float rdXZ2 = rd.x * rd.x + rd.z * rd.z;
+  float wLo = tLo, wHi = dob_minf(tHi, tLo + 2.8f);
+  bool checkWaves = true;
+  if (rdXZ2 > 1e-6f) {
+    const float bXZ = (ro.x * rd.x + ro.z * rd.z) / rdXZ2;
+    const float cXZ = ((ro.x * ro.x + ro.z * ro.z) - 2.2080f * 2.2080f) / rdXZ2;
+    const float discXZ = bXZ * bXZ - cXZ;
+    if (discXZ <= 0.0f) {
+      checkWaves = false;
+    } else {
+      const float sXZ = dob_sqrt(discXZ);
+      wLo = dob_maxf(tLo, -bXZ - sXZ);
+      wHi = dob_minf(tHi, -bXZ + sXZ);
+      if (wHi <= wLo) checkWaves = false;
+    }
+  }
+  if (checkWaves) {
+    const float horizSpan = dob_sqrt(dob_maxf(rdXZ2, 0.0f)) * (wHi - wLo);
+    const int adaptiveSteps = dob_clampi((int)ceilf(horizSpan / 0.0052f), 14, 56);
+    const float hHit = march_surface_segment(P, wave, ro, rd, wLo, wHi, adaptiveSteps, fromAir);
+    if (hHit > 0.0f) return hHit;
+  }
+  const bool validFlatDir = fromAir ? (ro.y >= baseY && rd.y < -1e-4f) : (ro.y <= baseY && rd.y > 1e-4f);
+  if (validFlatDir) {
+    const float tFlat = (baseY - ro.y) / rd.y;
+    if (tFlat >= tMin && tFlat <= tMax) return tFlat;
+  }
+  return -1.0f;
 }
 
 // henyeyGreenstein (render.ts:208-212)
@@ -585,8 +676,9 @@ __device__ PlumeOut march_plume(const RenderTex<V4>& T, const StepParams& P, dob
 }
 
 // One pixel: fsMain's camera ray and lens (render.ts:2659-2684), then the
-// submerged branch's primary march (render.ts:2420-2434) with the ray's end
-// at the flat meniscus plane.  Output per pixel, 8 halves: radiance rgb,
+// submerged branch's primary march (render.ts:2420-2434), ending at the
+// ray's crossing of the wave surface (the flat plane for rays within 0.052
+// of horizontal, as the reference takes it).  Output per pixel, 8 halves: radiance rgb,
 // tauTotal, transmittance rgb, tauIntact.
 template <class V4>
 __global__ void __launch_bounds__(kRenderBX * kRenderBY, 2)
@@ -610,7 +702,13 @@ __global__ void __launch_bounds__(kRenderBX * kRenderBY, 2)
   const float tFocus = focalDist / cosAxis;
   const float apRadius = dob_maxf(0.0f, U[57]);
   float tUnderSurf = -1.0f;
-  if (camRelY < -0.0005f && rd.y > 0.001f) tUnderSurf = dob_minf(12.0f, (U[40] - ro.y) / rd.y);
+  if (camRelY < -0.0005f && rd.y > 0.001f) {
+    const float tFlatApprox = (U[40] - ro.y) / rd.y;
+    if (rd.y > 0.052f && tFlatApprox < 4.5f)
+      tUnderSurf = intersect_water_surface(P, T.wave, ro, rd, 0.004f, dob_minf(12.0f, tFlatApprox + 0.8f), false);
+    else
+      tUnderSurf = dob_minf(12.0f, tFlatApprox);
+  }
   const float tPlumeEnd = tUnderSurf > 0.0f ? tUnderSurf + 0.004f : 5.5f;
   const PlumeOut o = march_plume(T, P, ro, rd, 0.02f, tPlumeEnd, tFocus, apRadius, jitter);
   __half* q = out + 8 * ((size_t)py * W + px);

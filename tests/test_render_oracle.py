@@ -82,3 +82,43 @@ def test_camera_matrices_round_trip():
     t = -np.array([0.1, 0.2, 1.5]) / np.linalg.norm([0.1, 0.2, 1.5])
     assert np.dot(d, t) > 0.9999
     assert np.allclose(vp.reshape(4, 4).T @ M, np.eye(4), atol=1e-4)
+
+
+def test_render_upward_rays_end_at_the_waves(oracle_mod):
+    """A camera below the meniscus looking up: rays steeper than 0.052 end
+    where they cross the wave surface (intersectWaterSurface), so a raised
+    wave field changes the depth the rays gather through a plume that
+    reaches the surface; a flat field gives the flat-plane image."""
+    cfg = abi.config_reference()
+    cfg.nx, cfg.ny, cfg.nz = 32, 48, 32
+    cfg.mg_levels = 3
+    cfg.parcel_capacity = 1024
+    eye, target = (0.02, -0.12, 0.95), (0.0, 0.05, 0.0)
+    vp, ivp = U.camera_matrices(eye, target, 40.0, W / H)
+    blk = U.SimUniformPacker().pack(drops=U.DropSnapshot(sim_time=0.5, active_count=0), dt=1.0 / 60.0,
+                                    frame_index=7, config=U.FluidOpticalConfig(), inv_view_proj=ivp, view_proj=vp,
+                                    camera_pos=eye, camera_target=target, viewport_width=W,
+                                    viewport_height=H).copy()
+    nz, ny, nx = 64, 96, 64
+    z, y, x = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    blob = np.exp(-(((x - 32) / 10.0) ** 2 + ((y - 80) / 30.0) ** 2 + ((z - 31) / 10.0) ** 2) * 1.5)
+    conc = np.zeros((nz, ny, nx, 4), np.float32)
+    conc[..., 0] = 0.6 * blob
+    conc[..., 1] = 0.2 * blob
+    conc[..., 2] = 0.5 * blob
+    lut = U.synthetic_spectral_lut()
+    wave = np.zeros((512, 512, 4), np.float32)
+    i = np.linspace(0, 6 * np.pi, 512)
+    wave[..., 0] = 0.03 * np.sin(i[None, :]) * np.cos(0.7 * i[:, None])
+    out = []
+    for w in (np.zeros_like(wave), wave):
+        o = oracle_mod.OracleSim(cfg)
+        o.set_uniforms(blk)
+        o.set_field(abi.FIELD_CONC, conc)
+        o.set_field(abi.FIELD_WAVE, w)
+        out.append(halves(o.render_plume(W, H, lut)))
+    flat, wavy = out
+    assert np.isfinite(wavy).all()
+    assert (flat[..., 3] > 0).mean() > 0.05
+    changed = (flat[..., 3] != wavy[..., 3])
+    assert changed.mean() > 0.05
