@@ -371,9 +371,10 @@ dob_status dob_load_state(dob_ctx* ctx, int slot);
    headless image: per pixel fsMain's camera ray and thin lens from the
    uniform block (invViewProj, camera position, focal distance, aperture,
    frame index for the jitter), driven as the submerged camera's primary
-   march from 0.02 to the flat meniscus plane (the reference refines rays
-   steeper than 0.052 upward against the waves; not restated), with the
-   reference's constants, fine quality and the inspect mode off.  Reference
+   march from 0.02 to the meniscus (rays steeper than 0.052 upward end
+   where they cross the wave surface, intersectWaterSurface, render.ts:
+   1004-1128; the others at the flat plane), with the reference's
+   constants, fine quality and the inspect mode off.  Reference
    mode with nx, ny, nz divisible by 4.
 
    dob_set_spectral_lut stores the renderer's 256 x 64 spectral
