@@ -135,7 +135,10 @@ static void fill_params(dob_ctx* ctx, StepParams* P, uint32_t spawn) {
     P->damp = c.vel_damping;
     P->sharp = c.dye_sharpness;
   }
-  for (int k = 0; k < 3; ++k) P->dsize[k] = P->dmax[k] - P->dmin[k];
+  for (int k = 0; k < 3; ++k) {
+    P->dsize[k] = P->dmax[k] - P->dmin[k];
+    P->rdsize[k] = 1.0f / P->dsize[k];
+  }
   P->tau_y = c.casson_tau_y;
   P->mu_p = c.casson_mu_p;
   P->dx = c.dx;
@@ -480,8 +483,8 @@ dob_status dob_create(const dob_config* cfg, dob_ctx** out) {
   CK(cudaStreamCreateWithFlags(&ctx->aux_stream, cudaStreamNonBlocking));
   CK(mg_prepare());
   s.aux = ctx->aux_stream;
-  s.g = Grid{(int)cfg->nx, (int)cfg->ny, (int)cfg->nz};
-  s.gc = Grid{(int)(cfg->nx * cfg->dye_refine), (int)(cfg->ny * cfg->dye_refine), (int)(cfg->nz * cfg->dye_refine)};
+  s.g = make_grid((int)cfg->nx, (int)cfg->ny, (int)cfg->nz);
+  s.gc = make_grid((int)(cfg->nx * cfg->dye_refine), (int)(cfg->ny * cfg->dye_refine), (int)(cfg->nz * cfg->dye_refine));
   s.prec = cfg->precision_mode;
   s.ref = cfg->bc_mode == DOB_BC_REFERENCE;
   s.flags = s.ref ? cfg->physics_flags : 0;
@@ -522,7 +525,7 @@ dob_status dob_create(const dob_config* cfg, dob_ctx** out) {
   s.nlev = cfg->mg_levels;
   for (int l = 0; l < s.nlev; ++l) {
     MgLevel& L = s.lv[l];
-    L.d = Grid{s.g.nx >> l, s.g.ny >> l, s.g.nz >> l};
+    L.d = make_grid(s.g.nx >> l, s.g.ny >> l, s.g.nz >> l);
     const float sc = (float)s.g.nx / (float)L.d.nx;
     L.h2 = sc * sc;
     if (l == 0) { L.e = s.p; L.b = s.rhs; continue; }

@@ -36,6 +36,7 @@ struct StepParams {
   float dmin[3];
   float dmax[3];
   float dsize[3];
+  float rdsize[3];     // 1 / dsize (IEEE quotients, formed on the host)
   float damp;          // advection damping
   float sharp;         // MacCormack sharpness
   float tau_y, mu_p, dx;
@@ -48,9 +49,16 @@ struct StepParams {
 
 struct Grid {
   int nx, ny, nz;
+  // 1/nx, 1/ny, 1/nz as IEEE quotients (make_grid): the kernels divide by the
+  // grid's dimensions through them (div_by) instead of forming the
+  // reciprocals per thread.  Grids built only for indexing leave them 0.
+  float rx, ry, rz;
   __host__ __device__ size_t n() const { return (size_t)nx * ny * nz; }
   __host__ __device__ size_t at(int x, int y, int z) const { return ((size_t)z * ny + y) * nx + x; }
 };
+inline Grid make_grid(int nx, int ny, int nz) {
+  return Grid{nx, ny, nz, 1.0f / (float)nx, 1.0f / (float)ny, 1.0f / (float)nz};
+}
 
 // ---- storage types -------------------------------------------------------------
 struct alignas(8) half4 {
@@ -277,6 +285,13 @@ struct Recip3 {
   dob_v3 d, r;
 };
 __device__ __forceinline__ Recip3 recip3(dob_v3 d) { return {d, v3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z)}; }
+// the grid's dimensions and the domain size with their host-formed reciprocals
+__device__ __forceinline__ Recip3 grid_recip(const Grid& g) {
+  return {v3((float)g.nx, (float)g.ny, (float)g.nz), v3(g.rx, g.ry, g.rz)};
+}
+__device__ __forceinline__ Recip3 dom_recip(const StepParams& P) {
+  return {v3(P.dsize[0], P.dsize[1], P.dsize[2]), v3(P.rdsize[0], P.rdsize[1], P.rdsize[2])};
+}
 __device__ __forceinline__ float div_by(float a, float d, float rd) {
   const float q = __fmul_rn(a, rd);
   return __fmaf_rn(__fmaf_rn(-q, d, a), rd, q);

@@ -169,7 +169,7 @@ extern "C" dob_status dob_pressure_solve_noalloc(const dob_config* cfg, const fl
   // Carve the scratch array: the same hierarchy dob_create allocates.
   DevState s;
   memset(&s, 0, sizeof(s));
-  s.g = Grid{(int)nx, (int)ny, (int)nz};
+  s.g = make_grid((int)nx, (int)ny, (int)nz);
   s.prec = DOB_PREC_FP32;
   s.ref = cfg->bc_mode == DOB_BC_REFERENCE;
   s.num_sms = num_sms;
@@ -188,7 +188,7 @@ extern "C" dob_status dob_pressure_solve_noalloc(const dob_config* cfg, const fl
   s.nlev = cfg->mg_levels;
   for (int l = 0; l < s.nlev; ++l) {
     MgLevel& L = s.lv[l];
-    L.d = Grid{s.g.nx >> l, s.g.ny >> l, s.g.nz >> l};
+    L.d = make_grid(s.g.nx >> l, s.g.ny >> l, s.g.nz >> l);
     const float sc = (float)s.g.nx / (float)L.d.nx;
     L.h2 = sc * sc;
     if (l == 0) {

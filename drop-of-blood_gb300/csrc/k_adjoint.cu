@@ -180,9 +180,9 @@ __device__ __forceinline__ void adj_face(const Grid& g, const float* uk, const f
   const dob_v3 B = F - (vMid * dtv) / dom;
   const dob_v3 Bc = clamp3(B, 0.002f, 0.998f);
   dob_v3 S = Bc;
-  if (comp == 0) S.x = S.x - 0.5f / (float)g.nx;
-  if (comp == 1) S.y = S.y - 0.5f / (float)g.ny;
-  if (comp == 2) S.z = S.z - 0.5f / (float)g.nz;
+  if (comp == 0) S.x = S.x - 0.5f * g.rx;
+  if (comp == 1) S.y = S.y - 0.5f * g.ry;
+  if (comp == 2) S.z = S.z - 0.5f * g.rz;
   const dob_v3 Sc = clamp3(S, 0.001f, 0.999f);
   const Taps tS = make_taps(g, Sc.x, Sc.y, Sc.z);
   // backward
@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(256, 4) k_adj_advect_mac(Grid g, const StepPar
   const size_t i = g.at(x, y, z);
   const StepParams& P = *Pp;
   const dob_v3 dims = v3((float)g.nx, (float)g.ny, (float)g.nz);
-  const Recip3 dimr = recip3(dims), dom = recip3(dsize_of(P));
+  const Recip3 dimr = grid_recip(g), dom = dom_recip(P);
   const float dtv = P.dt;
   const float damp = P.damp;
   const bool wall = comp == 0 ? x >= g.nx - 1 : comp == 1 ? y >= g.ny - 1 : z >= g.nz - 1;
@@ -787,8 +787,8 @@ __global__ void __launch_bounds__(256, 4) k_adj_conc_predict(Grid gc, Grid g, co
   const dob_v3 dimsc = v3((float)gc.nx, (float)gc.ny, (float)gc.nz);
   const dob_v3 dimsg = v3((float)g.nx, (float)g.ny, (float)g.nz);
   const float dtv = P.dt;
-  const Recip3 dom = recip3(dsize_of(P));
-  const dob_v3 uvw = (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / recip3(dimsc);
+  const Recip3 dom = dom_recip(P);
+  const dob_v3 uvw = (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / grid_recip(gc);
   const Taps t0 = make_taps_exact(g, uvw.x, uvw.y, uvw.z);  // the forward's cell-centre sample (dye on the velocity grid)
   const dob_v3 v0 = lerp8x3_fixed(t0, cen);
   const dob_v3 M = uvw - (0.5f * (v0 * dtv)) / dom;
@@ -824,8 +824,8 @@ __global__ void __launch_bounds__(256, 5) k_adj_dye_resolve(Grid gc, Grid g, con
   const StepParams& P = *Pp;
   const dob_v3 dims = v3((float)gc.nx, (float)gc.ny, (float)gc.nz);
   const float dtv = P.dt;
-  const Recip3 dom = recip3(dsize_of(P));
-  const dob_v3 uvw = (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / recip3(dims);
+  const Recip3 dom = dom_recip(P);
+  const dob_v3 uvw = (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / grid_recip(gc);
   const Taps t0 = make_taps_exact(g, uvw.x, uvw.y, uvw.z);  // the forward's cell-centre sample (dye on the velocity grid)
   const dob_v3 v0 = lerp8x3_fixed(t0, cen);
   const dob_v3 uvwMid = clamp3(uvw - (0.5f * (v0 * dtv)) / dom, 0.001f, 0.999f);

@@ -83,9 +83,11 @@ __global__ void k_init_vel(Grid g, const StepParams* __restrict__ Pp, VS* u, VS*
 // at 192x256x192: 336 -> 327, 150 -> 131 and 94 -> 86 us.
 template <class VS>
 __device__ __forceinline__ float sample_mac(const Grid& g, const VS* a, dob_v3 uvw, int comp) {
-  if (comp == 0) uvw.x = uvw.x - 0.5f / (float)g.nx;
-  if (comp == 1) uvw.y = uvw.y - 0.5f / (float)g.ny;
-  if (comp == 2) uvw.z = uvw.z - 0.5f / (float)g.nz;
+  // 0.5 / n is half the host-formed 1 / n (the same quotient: scaling by a
+  // power of two commutes with rounding)
+  if (comp == 0) uvw.x = uvw.x - 0.5f * g.rx;
+  if (comp == 1) uvw.y = uvw.y - 0.5f * g.ry;
+  if (comp == 2) uvw.z = uvw.z - 0.5f * g.rz;
   uvw = clamp3(uvw, 0.001f, 0.999f);
   const Taps t = make_taps(g, uvw.x, uvw.y, uvw.z);
   return lerp8(t, a);
@@ -112,8 +114,7 @@ __global__ void __launch_bounds__(256, 5) k_advect_mac(Grid g, const StepParams*
                                                     VS* __restrict__ vo, VS* __restrict__ wo) {
   CELL_INDEX
   const StepParams& P = *Pp;
-  const dob_v3 dims = v3((float)g.nx, (float)g.ny, (float)g.nz);
-  const Recip3 dimr = recip3(dims), dom = recip3(dsize_of(P));
+  const Recip3 dimr = grid_recip(g), dom = dom_recip(P);
   const float dtv = P.dt;
   const float damp = P.damp;
   // a: the cell centre, b: the upper faces; face X is (b.x, a.y, a.z) etc.
@@ -135,7 +136,7 @@ __global__ void __launch_bounds__(256, 5) k_advect_mac(Grid g, const StepParams*
   float vz = sample_mac(g, w, trace_back(g, cen, uvwZ, v0Z, dtv, dom), 2) * damp;
   if (ref) {
     const float surfY = P.U[40];
-    const dob_v3 pCell = to_world(P, (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / dims);
+    const dob_v3 pCell = to_world(P, (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / dimr);
     const dob_v3 pFaceY = to_world(P, uvwY);
     float activeNeckMask = 0.0f;
     if (flags & DOB_PHYS_NECK) {
@@ -145,30 +146,38 @@ __global__ void __launch_bounds__(256, 5) k_advect_mac(Grid g, const StepParams*
         const float dX = drop(P, d, 0), dZ = drop(P, d, 2);
         const float relx = pFaceY.x - dX, relz = pFaceY.z - dZ;
         const float r = length2f(relx, relz);
-        const float theta = dob_atan2(relz, relx);
         const float seed = signedSeed;
-        const float azim = azim_neck(theta, seed);
         const float sp = dob_smoothstep(0.14f, 0.76f, drain);
         const float rNeckBase =
             dob_clampf(drop(P, d, 3) * dob_mix(0.80f, 1.08f, sp) + dob_mix(0.012f, 0.030f, sp), 0.018f, 0.088f);
-        const float rNeck = rNeckBase * azim;
-        const float rRatio = r / dob_maxf(rNeck, 1e-4f);
-        const float slugRadial = (0.14f + 1.00f * dob_minf(rRatio * rRatio, 1.20f)) * (1.0f - dob_smoothstep(0.78f, 1.15f, rRatio));
-        const float stemRadial = (0.68f + 0.32f * dob_minf(rRatio * rRatio, 1.0f)) * (1.0f - dob_smoothstep(0.74f, 1.10f, rRatio));
-        const float radialProfile = dob_mix(stemRadial, slugRadial, sp);
-        const float vertMask = dob_smoothstep(surfY - 0.058f, surfY - 0.014f, pFaceY.y);
-        const float meniscusShear = dob_mix(1.0f, 0.36f, dob_smoothstep(surfY - 0.024f, surfY - 0.002f, pFaceY.y));
-        const float mask = radialProfile * vertMask;
-        activeNeckMask = dob_maxf(activeNeckMask, radialProfile);
-        if (mask > 0.001f) {
-          const float lobeMod = 1.0f + 0.036f * dob_cos(4.0f * theta + seed * 1.73f) + 0.026f * dob_cos(6.0f * theta - seed * 2.31f);
-          const float impactSpeed = dob_clampf(-drop(P, d, 4), 0.10f, 0.65f);
-          const float slugDrive = dob_clampf(dob_pow(dob_maxf(drain, 0.0f), 0.66f) * 0.84f, 0.0f, 1.24f);
-          const float stemDrive = dob_clampf(0.045f + drain * 0.22f, 0.0f, 0.20f) * dob_smoothstep(0.0f, 0.05f, drain);
-          const float fluxDrive = dob_mix(stemDrive, slugDrive, sp);
-          const float targetVy = -dob_clampf(0.14f + 0.64f * impactSpeed, 0.15f, 0.39f) * fluxDrive * lobeMod * meniscusShear;
-          const float blend = dob_clampf(dtv * dob_mix(14.0f, 22.0f, sp) * mask, 0.0f, 1.0f);
-          vy = dob_mix(vy, targetVy, blend);
+        // The azimuthal factor lies in [0.92, 1.08] and both radial profiles
+        // vanish exactly from rRatio = 1.15 on, so at r >= 1.25 rNeckBase the
+        // profile, the mask and this drop's share of activeNeckMask are
+        // exactly 0; at or below surfY - 0.058 the vertical mask is exactly 0,
+        // and activeNeckMask is read only in the top two layers.  The angle
+        // and its harmonics are formed only where they can change a result.
+        if (r < rNeckBase * 1.25f && (y >= g.ny - 2 || pFaceY.y > surfY - 0.058f)) {
+          const float theta = dob_atan2(relz, relx);
+          const float azim = azim_neck(theta, seed);
+          const float rNeck = rNeckBase * azim;
+          const float rRatio = r / dob_maxf(rNeck, 1e-4f);
+          const float slugRadial = (0.14f + 1.00f * dob_minf(rRatio * rRatio, 1.20f)) * (1.0f - dob_smoothstep(0.78f, 1.15f, rRatio));
+          const float stemRadial = (0.68f + 0.32f * dob_minf(rRatio * rRatio, 1.0f)) * (1.0f - dob_smoothstep(0.74f, 1.10f, rRatio));
+          const float radialProfile = dob_mix(stemRadial, slugRadial, sp);
+          const float vertMask = dob_smoothstep(surfY - 0.058f, surfY - 0.014f, pFaceY.y);
+          const float meniscusShear = dob_mix(1.0f, 0.36f, dob_smoothstep(surfY - 0.024f, surfY - 0.002f, pFaceY.y));
+          const float mask = radialProfile * vertMask;
+          activeNeckMask = dob_maxf(activeNeckMask, radialProfile);
+          if (mask > 0.001f) {
+            const float lobeMod = 1.0f + 0.036f * dob_cos(4.0f * theta + seed * 1.73f) + 0.026f * dob_cos(6.0f * theta - seed * 2.31f);
+            const float impactSpeed = dob_clampf(-drop(P, d, 4), 0.10f, 0.65f);
+            const float slugDrive = dob_clampf(dob_pow(dob_maxf(drain, 0.0f), 0.66f) * 0.84f, 0.0f, 1.24f);
+            const float stemDrive = dob_clampf(0.045f + drain * 0.22f, 0.0f, 0.20f) * dob_smoothstep(0.0f, 0.05f, drain);
+            const float fluxDrive = dob_mix(stemDrive, slugDrive, sp);
+            const float targetVy = -dob_clampf(0.14f + 0.64f * impactSpeed, 0.15f, 0.39f) * fluxDrive * lobeMod * meniscusShear;
+            const float blend = dob_clampf(dtv * dob_mix(14.0f, 22.0f, sp) * mask, 0.0f, 1.0f);
+            vy = dob_mix(vy, targetVy, blend);
+          }
         }
         const float vertMaskXZ = dob_smoothstep(surfY - 0.058f, surfY - 0.014f, pCell.y);
         if (vertMaskXZ > 0.001f) {
@@ -218,10 +227,14 @@ __global__ void __launch_bounds__(256, 5) k_advect_mac(Grid g, const StepParams*
     if (flags & DOB_PHYS_SPONGE) {
       const float halfXZ = P.U[52], yMin = P.U[53];
       const float rCellXZ = length2f(pCell.x, pCell.z);
-      const float wallFade = (1.0f - dob_smoothstep(halfXZ * 0.68f, halfXZ * 0.94f, rCellXZ)) *
-                             dob_smoothstep(yMin + 0.004f, yMin + 0.052f, pCell.y);
-      const float spongeMul = dob_mix(0.84f, 1.0f, wallFade);
-      vx = vx * spongeMul; vy = vy * spongeMul; vz = vz * spongeMul;
+      // inside the inner radius and above the floor band the fade is exactly
+      // 1 and the factor exactly 1: the smoothsteps are formed only outside
+      if (!(rCellXZ <= halfXZ * 0.68f && pCell.y >= yMin + 0.052f)) {
+        const float wallFade = (1.0f - dob_smoothstep(halfXZ * 0.68f, halfXZ * 0.94f, rCellXZ)) *
+                               dob_smoothstep(yMin + 0.004f, yMin + 0.052f, pCell.y);
+        const float spongeMul = dob_mix(0.84f, 1.0f, wallFade);
+        vx = vx * spongeMul; vy = vy * spongeMul; vz = vz * spongeMul;
+      }
     }
   }
   if (x >= g.nx - 1) vx = 0.0f;
@@ -247,7 +260,7 @@ __global__ void __launch_bounds__(256) k_mac_to_center(Grid g, const StepParams*
   float cy = 0.5f * (vD + vU);
   if (ref && (flags & DOB_PHYS_SURFACE) && y >= g.ny - 2 && cy < 0.0f) {
     const StepParams& P = *Pp;
-    const dob_v3 dims = v3((float)g.nx, (float)g.ny, (float)g.nz);
+    const Recip3 dims = grid_recip(g);
     const dob_v3 pCell = to_world(P, (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / dims);
     float activeNeck = 0.0f;
     for (int d = 0; d < kMaxDrops; ++d) {
@@ -319,7 +332,7 @@ __global__ void __launch_bounds__(256) k_casson(Grid g, Grid gc, const StepParam
                                                 VS* __restrict__ wo) {
   CELL_INDEX
   const StepParams& P = *Pp;
-  const dob_v3 dims = v3((float)g.nx, (float)g.ny, (float)g.nz);
+  const Recip3 dims = grid_recip(g);
   const float dtv = P.dt;
   dob_v3 mac = v3(ldf(u + i), ldf(v + i), ldf(w + i));
   const dob_v3 mXp = ldmac(g, u, v, w, x + 1, y, z), mXn = ldmac(g, u, v, w, x - 1, y, z);
@@ -534,9 +547,9 @@ __device__ __forceinline__ void predict_cell(const Grid& gc, const Grid& g, cons
                                              const DS* __restrict__ dye, DS* __restrict__ pred, DS* __restrict__ lim,
                                              uint32_t* __restrict__ pbrick, int x, int y, int z) {
   const size_t i = gc.at(x, y, z);
-  const Recip3 dims = recip3(v3((float)gc.nx, (float)gc.ny, (float)gc.nz));
+  const Recip3 dims = grid_recip(gc);
   const float dtv = P.dt;
-  const Recip3 dom = recip3(dsize_of(P));
+  const Recip3 dom = dom_recip(P);
   const dob_v3 uvw = (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / dims;
   if (ref) {
     if (x == 0 || x >= gc.nx - 1 || z == 0 || z >= gc.nz - 1 || y >= gc.ny - 1) { stf(pred + i, 0.0f); return; }
@@ -631,16 +644,17 @@ __device__ __forceinline__ void resolve_ref_cell(const Grid& gc, const Grid& g, 
                                                  uint32_t* __restrict__ cbrick_out, int x, int y, int z) {
   const size_t i = gc.at(x, y, z);
   const dob_v3 dims = v3((float)gc.nx, (float)gc.ny, (float)gc.nz);
+  const Recip3 dimr = grid_recip(gc);
   const bool inFloorZone = y <= 7;
   const uint32_t rawIntact = __ldg(splatI + i), rawLysed = __ldg(splatL + i);
   if (rawIntact == 0u && rawLysed == 0u) {
-    const dob_v3 g0 = v3((float)x, (float)y, (float)z) / dims;
-    const dob_v3 g1 = (v3((float)x, (float)y, (float)z) + v3(1.0f, 1.0f, 1.0f)) / dims;
+    const dob_v3 g0 = v3((float)x, (float)y, (float)z) / dimr;
+    const dob_v3 g1 = (v3((float)x, (float)y, (float)z) + v3(1.0f, 1.0f, 1.0f)) / dimr;
     const float oct0 = lerp8(make_taps(gc, g0.x, g0.y, g0.z), pred);
     const float oct1 = lerp8(make_taps(gc, g1.x, g1.y, g1.z), pred);
     float bedActive = 0.0f;
     if (inFloorZone) {
-      const dob_v3 gh = (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / dims;
+      const dob_v3 gh = (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / dimr;
       bedActive = lerp8x4(make_taps(gc, gh.x, gh.y, gh.z), conc).w;
     }
     if (oct0 + oct1 <= 1.0e-7f && bedActive <= 1.0e-6f) {
@@ -661,7 +675,7 @@ __device__ __forceinline__ void resolve_ref_cell(const Grid& gc, const Grid& g, 
     lapIntact = (intact_raw(gc, splatI, x + 1, y, z) + intact_raw(gc, splatI, x - 1, y, z) + intact_raw(gc, splatI, x, y + 1, z) +
                  intact_raw(gc, splatI, x, y - 1, z) + intact_raw(gc, splatI, x, y, z + 1) + intact_raw(gc, splatI, x, y, z - 1)) *
                 (1.0f / 6.0f);
-  const dob_v3 uvw = (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / dims;
+  const dob_v3 uvw = (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / dimr;
   const float dtv = P.dt;
   const dob_v3 dom = dsize_of(P);
   const dob_v3 pw = to_world(P, uvw);
@@ -803,10 +817,9 @@ __global__ void __launch_bounds__(256) k_dye_resolve_box(Grid gc, Grid g, const 
   if (x >= gc.nx || y >= gc.ny) return;
   const size_t i = gc.at(x, y, z);
   const StepParams& P = *Pp;
-  const dob_v3 dims = v3((float)gc.nx, (float)gc.ny, (float)gc.nz);
   const float dtv = P.dt;
-  const Recip3 dom = recip3(dsize_of(P));
-  const dob_v3 uvw = (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / recip3(dims);
+  const Recip3 dom = dom_recip(P);
+  const dob_v3 uvw = (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / grid_recip(gc);
   const dob_v3 v0 = gc.nx == g.nx ? center_at_cell(g, cen, uvw, x, y, z, i) : sample_center(g, cen, uvw);
   const dob_v3 uvwMid = clamp3(uvw - (0.5f * (v0 * dtv)) / dom, 0.001f, 0.999f);
   const dob_v3 vMid = sample_center(g, cen, uvwMid);
@@ -838,9 +851,9 @@ __global__ void __launch_bounds__(256, 8) k_dye_resolve_lim(Grid gc, Grid g, con
   const size_t i = gc.at(x, y, z);
   const StepParams& P = *Pp;
   const float dtv = P.dt;
-  const Recip3 dom = recip3(dsize_of(P));
+  const Recip3 dom = dom_recip(P);
   const dob_v3 uvw = (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) /
-                     recip3(v3((float)gc.nx, (float)gc.ny, (float)gc.nz));
+                     grid_recip(gc);
   const dob_v3 v0 = gc.nx == g.nx ? center_at_cell(g, cen, uvw, x, y, z, i) : sample_center(g, cen, uvw);
   const dob_v3 uvwFwd = clamp3(uvw + (v0 * dtv) / dom, 0.001f, 0.999f);
   const float gBackEst = lerp8(make_taps(gc, uvwFwd.x, uvwFwd.y, uvwFwd.z), pred);

@@ -64,7 +64,7 @@ __global__ void __launch_bounds__(kLightBX * kLightBY * kLightBZ)
   float4 out = make_float4(1.0f, 1.0f, 0.0f, 0.0f);
   const bool inside = x < g.nx;
   if (inside) {
-    const dob_v3 dims = v3((float)g.nx, (float)g.ny, (float)g.nz);
+    const Recip3 dims = grid_recip(g);
     const dob_v3 uvw = (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / dims;
     const dob_v3 p = to_world(P, uvw);
     const dob_v3 dom = dsize_of(P);

@@ -427,12 +427,12 @@ __global__ void __launch_bounds__(256) k_prolong_add2(Grid f, Grid c, int ref, T
   float fxv[4], fyv[2];
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
-    const float cx = __fmaf_rn(((float)(4 * q + i) + 0.5f) / (float)f.nx, (float)c.nx, -0.5f);  // one rounding
+    const float cx = __fmaf_rn(div_by((float)(4 * q + i) + 0.5f, (float)f.nx, f.rx), (float)c.nx, -0.5f);  // one rounding
     fxv[i] = cx - floorf(cx);
   }
 #pragma unroll
   for (int d = 0; d < 2; ++d) {
-    const float cy = __fmaf_rn(((float)(2 * Y + d) + 0.5f) / (float)f.ny, (float)c.ny, -0.5f);
+    const float cy = __fmaf_rn(div_by((float)(2 * Y + d) + 0.5f, (float)f.ny, f.ry), (float)c.ny, -0.5f);
     fyv[d] = cy - floorf(cy);
   }
 #pragma unroll
@@ -442,7 +442,7 @@ __global__ void __launch_bounds__(256) k_prolong_add2(Grid f, Grid c, int ref, T
     float fzv[2];
 #pragma unroll
     for (int d = 0; d < 2; ++d) {
-      const float cz = __fmaf_rn(((float)(2 * Z + d) + 0.5f) / (float)f.nz, (float)c.nz, -0.5f);
+      const float cz = __fmaf_rn(div_by((float)(2 * Z + d) + 0.5f, (float)f.nz, f.rz), (float)c.nz, -0.5f);
       fzv[d] = cz - floorf(cz);
     }
     // the fine rows of this coarse plane, all loaded before any store (the
