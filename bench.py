@@ -865,6 +865,9 @@ def main():
     ap.add_argument("--profile-run", action="store_true",
                     help="run only the FP32 scene (warm-up + steps, untimed) and exit: the command "
                          "the ncu launch lists and kernel captures are taken with")
+    ap.add_argument("--profile-scene", choices=["box192", "box96"], default="box192",
+                    help="scene of --profile-run: box192 (the headline workload) or box96 (96x128x96, "
+                         "the small case for full-metric kernel captures)")
     args = ap.parse_args()
     rank, world, local = rank_info()
     if args.impl == "reference":
@@ -899,7 +902,7 @@ def main():
     dist = Dist(world)
 
     # ---- FP32 drop-in step (the headline) ----------------------------------------------------
-    sc = scenes.box192()
+    sc = scenes.box96() if (args.profile_run and args.profile_scene == "box96") else scenes.box192()
     eng = DropFluid(sc.config)
     run_scene_steps(sc, eng, 0, args.warmup, timed=False)
     eng.sync()
