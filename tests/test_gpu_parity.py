@@ -421,9 +421,10 @@ def test_reference_mode_steps_parity(oracle_mod, gpu_lib):
 
 def test_wave_solver_bit_exact(oracle_mod, gpu_lib):
     """The wave substep (force, row/column FFTs, spectral propagation,
-    finalize; wave.ts:55-388) equals the oracle bit for bit over three
+    finalize; wave.ts:55-388) equals the oracle bit for bit over five
     substeps, from a seeded half-valued wave field with two drops at the
-    surface and the v faces feeding the subsurface term."""
+    surface and the v faces feeding the subsurface term; the dt changes at
+    the fourth substep."""
     abi = _abi()
     from dropfluid import DropFluid
     cfg = ref_config()
@@ -437,8 +438,8 @@ def test_wave_solver_bit_exact(oracle_mod, gpu_lib):
         e.set_uniforms(ref_block(sim_time=0.5, spawn=0))
         e.reset()
         load_state(e, st)
-    for k in range(3):
-        blk = ref_block(sim_time=0.5 + k / 60.0, spawn=0)
+    for k, dt in enumerate((1.0 / 60.0, 1.0 / 60.0, 1.0 / 60.0, 1.0 / 120.0, 1.0 / 120.0)):
+        blk = ref_block(sim_time=0.5 + k / 60.0, spawn=0, dt=dt)
         for e in (g, o):
             e.set_uniforms(blk)
             e.wave_step()
