@@ -253,7 +253,7 @@ static void enqueue_step_body(dob_ctx* ctx, DevState& s, cudaStream_t st, float*
       cudaMemsetAsync(s.red + RED_RHS_NORM2, 0, sizeof(double), st);
       launch_sumsq(s.rhs, s.g.n(), s.red + RED_RHS_NORM2, s.num_sms, st);
     }
-    if (stats_div && stage == DOB_STAGE_PRESSURE_SOLVE) {
+    if (stats_div && stage == DOB_STAGE_PRESSURE_SOLVE && (ctx->stats_mask & DOB_STATS_RESIDUAL)) {
       launch_residual_norm(s, s.red + RED_RES_NORM2, st);
     }
     if (stats_div && stage == DOB_STAGE_PROJECT && s.ref) {
@@ -375,12 +375,12 @@ static void fill_stats(dob_ctx* ctx, const double* red, const unsigned int* redu
     stats->outer_iters = 0;
     stats->vcycles = cycles;  // of the last step
   }
-  stats->residual_l2 = sqrt(red[RED_RES_NORM2]);
+  stats->residual_l2 = (ctx->stats_mask & DOB_STATS_RESIDUAL) ? sqrt(red[RED_RES_NORM2]) : -1.0;
   stats->rhs_l2 = sqrt(red[RED_RHS_NORM2]);
   float md;
   memcpy(&md, &redu[REDU_MAXDIV], 4);
   stats->max_div = (double)md;
-  stats->parcels_alive = redu[REDU_ALIVE];
+  stats->parcels_alive = (ctx->stats_mask & DOB_STATS_PARCELS) ? redu[REDU_ALIVE] : 0u;
 }
 
 static dob_status finish_stats(dob_ctx* ctx, dob_step_stats* stats, int steps) {
@@ -388,7 +388,7 @@ static dob_status finish_stats(dob_ctx* ctx, dob_step_stats* stats, int steps) {
   DevState& s = ctx->s;
   double red[RED_COUNT];
   unsigned int redu[REDU_COUNT];
-  launch_count_alive(s, s.redu + REDU_ALIVE, ctx->stream);
+  if (ctx->stats_mask & DOB_STATS_PARCELS) launch_count_alive(s, s.redu + REDU_ALIVE, ctx->stream);
   CK(cudaMemcpyAsync(red, s.red, sizeof(red), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaMemcpyAsync(redu, s.redu, sizeof(redu), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
@@ -922,12 +922,24 @@ dob_status dob_step_async(dob_ctx* ctx, int slot) {
   dob_status st = one_step(ctx, DOB_STEP_STATS, nullptr);
   if (st != DOB_OK) return st;
   DevState& s = ctx->s;
-  launch_count_alive(s, s.redu + REDU_ALIVE, ctx->stream);
+  if (ctx->stats_mask & DOB_STATS_PARCELS) launch_count_alive(s, s.redu + REDU_ALIVE, ctx->stream);
   CK(cudaMemcpyAsync(a.red, s.red, RED_COUNT * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaMemcpyAsync(a.redu, s.redu, REDU_COUNT * sizeof(unsigned int), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaEventRecord(a.done, ctx->stream));
   a.cycles = ctx->last_cycles;
   a.pending = true;
+  return DOB_OK;
+}
+
+dob_status dob_set_step_stats(dob_ctx* ctx, uint32_t mask) {
+  if (!ctx || (mask & ~DOB_STATS_ALL)) return DOB_EINVAL;
+  for (auto& a : ctx->async_slots)
+    if (a.pending) return fail(ctx, DOB_ESTATE, "dob_set_step_stats", "a pipelined step is pending");
+  if (mask != ctx->stats_mask) {
+    CK(cudaStreamSynchronize(ctx->stream));
+    drop_graphs(ctx);  // the statistics graph holds the residual pass or not
+    ctx->stats_mask = mask;
+  }
   return DOB_OK;
 }
 

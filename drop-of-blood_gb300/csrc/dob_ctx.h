@@ -63,6 +63,7 @@ struct dob_ctx {
   // pressure is FP32): an injection sets kInjectedSteps
   int inject_pending = 0;
   int last_cycles = 0;  // V-cycles of the last step (FP32 pressure)
+  uint32_t stats_mask = DOB_STATS_ALL;  // statistics a DOB_STEP_STATS step forms
   int kernels_per_step = 0;
   dob::Snapshot snaps[dob::kSnapshots];
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;

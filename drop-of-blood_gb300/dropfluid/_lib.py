@@ -51,6 +51,7 @@ SIGNATURES = {
     "dob_pressure_solve_noalloc": (C.c_int, [C.POINTER(abi.DobConfig), P, P, P]),
     "dob_step_async": (C.c_int, [P, C.c_int]),
     "dob_step_result": (C.c_int, [P, C.c_int, C.POINTER(abi.DobStepStats)]),
+    "dob_set_step_stats": (C.c_int, [P, C.c_uint32]),
     "dob_adjoint_stage": (C.c_int, [P, C.c_int]),
     "dob_tape_forward": (C.c_int, [P, C.c_int, C.c_int]),
     "dob_tape_backward": (C.c_int, [P, FP, C.c_size_t]),

@@ -124,6 +124,10 @@ STAGE_NAMES = [
 
 STEP_STATS = 1
 STEP_TIMING = 2
+# statistics a DOB_STEP_STATS step forms (dob_set_step_stats)
+STATS_RESIDUAL = 1
+STATS_PARCELS = 2
+STATS_ALL = 3
 STEP_NO_GRAPH = 4
 
 WAVE_N = 512

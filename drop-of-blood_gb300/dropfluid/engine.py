@@ -148,6 +148,12 @@ class DropFluid:
         self._ck(self._L.dob_step_result(self._h, int(slot), C.byref(st)), "dob_step_result")
         return self._stats_dict(st)
 
+    def set_step_stats(self, mask):
+        """Statistics a step with statistics forms (dob_set_step_stats):
+        abi.STATS_ALL, or a mask of STATS_RESIDUAL / STATS_PARCELS over the
+        always-formed max |div| and ||b||."""
+        self._ck(self._L.dob_set_step_stats(self._h, int(mask)), "dob_set_step_stats")
+
     def run_pipelined(self, n, depth=2):
         """n steps, each step's statistics read back while the next runs."""
         out = []

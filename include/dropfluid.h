@@ -220,9 +220,10 @@ typedef struct dob_step_stats {
   int32_t vcycles;              /* V-cycles in the last step                      */
   int32_t outer_iters;          /* defect-correction iterations in the last step  */
   double rhs_l2;                /* ||b|| of the last pressure solve (FP64)        */
-  double residual_l2;           /* ||b - A p|| after the last solve (FP64)        */
+  double residual_l2;           /* ||b - A p|| after the last solve (FP64); -1
+                                   when not formed (dob_set_step_stats)         */
   double max_div;               /* max |div u| * dt / dx after projection         */
-  uint32_t parcels_alive;
+  uint32_t parcels_alive;       /* 0 when not formed (dob_set_step_stats)         */
   uint32_t pad;
   float stage_ms[DOB_STAGE_COUNT];
 } dob_step_stats;
@@ -302,6 +303,21 @@ dob_status dob_step(dob_ctx* ctx, int nsteps, uint32_t flags, dob_step_stats* st
    A slot must be read back before it is reused. */
 dob_status dob_step_async(dob_ctx* ctx, int slot);
 dob_status dob_step_result(dob_ctx* ctx, int slot, dob_step_stats* stats);
+
+/* Which statistics a step with DOB_STEP_STATS (and dob_step_async) forms.
+   max |div| and ||b|| always (in the closed box they come out of the
+   projection and the mean removal at no extra pass; in reference mode they
+   are a divergence pass and a sum of squares).  DOB_STATS_RESIDUAL adds
+   ||b - A p|| (one
+   error-free residual pass over the pressure, about 60 us at 192x256x192),
+   DOB_STATS_PARCELS the live-parcel count (one reduction over the ring).
+   Default DOB_STATS_ALL; the fields of a step are the same bits whatever
+   the mask.  (The reference reads back only GPU timestamps per frame,
+   BloodDropEngine.ts:2400-2456.) */
+#define DOB_STATS_RESIDUAL 1u
+#define DOB_STATS_PARCELS 2u
+#define DOB_STATS_ALL 3u
+dob_status dob_set_step_stats(dob_ctx* ctx, uint32_t mask);
 
 /* Reference mode: nsteps substeps, each with its own 128-float block
    (the reference's multi-substep staging path, BloodDropEngine.ts:2634-2651). */

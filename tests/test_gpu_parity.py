@@ -393,6 +393,36 @@ def test_step_statistics_match_fields(gpu_lib):
     g.close()
 
 
+def test_step_statistics_selection(gpu_lib):
+    """dob_set_step_stats: without DOB_STATS_RESIDUAL / DOB_STATS_PARCELS a
+    step with statistics skips the residual pass and the parcel count
+    (reported as -1 and 0), keeps max |div| and ||b||, and leaves the same
+    field bits; pipelined and synchronous; a bad mask is refused."""
+    abi = _abi()
+    from dropfluid import DropFluid, scenes
+    from dropfluid._lib import DropFluidError
+    sc = scenes.box48()
+    a, b = DropFluid(sc.config), DropFluid(sc.config)
+    b.set_step_stats(0)
+    for e in (a, b):
+        sc.release(e, 0)
+    sa = [a.step(1, stats=True) for _ in range(2)] + a.run_pipelined(4)
+    sb = [b.step(1, stats=True) for _ in range(2)] + b.run_pipelined(4)
+    for x, y in zip(sa, sb):
+        assert x["residual_l2"] > 0 and x["parcels_alive"] > 0
+        assert y["residual_l2"] == -1.0 and y["parcels_alive"] == 0
+        # ||b|| sums FP64 block partials with atomics: equal to summation order
+        assert x["max_div"] == y["max_div"] and abs(x["rhs_l2"] - y["rhs_l2"]) <= 1e-12 * x["rhs_l2"]
+    for f in (abi.FIELD_VEL_U, abi.FIELD_VEL_V, abi.FIELD_VEL_W, abi.FIELD_PRESSURE, abi.FIELD_CONC):
+        assert bits_equal(a.get_field(f), b.get_field(f)), f
+    b.set_step_stats(abi.STATS_ALL)
+    assert b.step(1, stats=True)["residual_l2"] > 0
+    with pytest.raises(DropFluidError):
+        b.set_step_stats(8)
+    a.close()
+    b.close()
+
+
 def test_reference_mode_steps_parity(oracle_mod, gpu_lib):
     """Reference setup (Dirichlet free-surface top, drops, parcels, 2x dye),
     8 substeps at a reduced grid: relative L2 <= 1e-4 against the oracle."""
