@@ -131,6 +131,27 @@ __device__ __forceinline__ float texel(float u, int n) {
 __device__ __forceinline__ Taps make_taps(const Grid& g, float u, float v, float w) {
   return taps_at(g, texel(u, g.nx), texel(v, g.ny), texel(w, g.nz));
 }
+// make_taps for coordinates in [0.001, 0.999], where the semi-Lagrangian
+// kernels clamp every sample point first: the floor of u n - 1/2 is then in
+// [-1, n-1], so only the lower tap can leave the grid (below) and only the
+// upper one (above), and each is clamped at that one end: the same taps
+// with two integer operations per axis fewer.
+__device__ __forceinline__ Taps make_taps_in(const Grid& g, float u, float v, float w) {
+  const float cx = texel(u, g.nx), cy = texel(v, g.ny), cz = texel(w, g.nz);
+  Taps t;
+  const float bx = floorf(cx), by = floorf(cy), bz = floorf(cz);
+  t.fx = cx - bx; t.fy = cy - by; t.fz = cz - bz;
+  const int ix = (int)bx, iy = (int)by, iz = (int)bz;
+  const int x0 = max(ix, 0), x1 = min(ix + 1, g.nx - 1);
+  const int y0 = max(iy, 0), y1 = min(iy + 1, g.ny - 1);
+  const int z0 = max(iz, 0), z1 = min(iz + 1, g.nz - 1);
+  const uint32_t sy = (uint32_t)g.nx, sz = (uint32_t)g.nx * (uint32_t)g.ny;
+  t.base = (uint32_t)z0 * sz + (uint32_t)y0 * sy + (uint32_t)x0;
+  t.ox = (uint32_t)(x1 - x0);
+  t.oy = (uint32_t)(y1 - y0) * sy;
+  t.oz = (uint32_t)(z1 - z0) * sz;
+  return t;
+}
 // make_taps with the texel coordinate formed without FMA contraction (the
 // rounded product, then the subtraction), as the host oracle forms it.  At
 // a fixed cell-centre or face-centre point uvw * dims rounds back to the
@@ -187,6 +208,12 @@ template <int NC, class V4> __device__ __forceinline__ float4 lerp8xn(const Taps
 template <class V4> __device__ __forceinline__ float4 lerp8x4(const Taps& t, const V4* a) { return lerp8xn<4>(t, a); }
 template <class V4> __device__ __forceinline__ dob_v3 sample_center(const Grid& g, const V4* cen, dob_v3 uvw) {
   const Taps t = make_taps(g, uvw.x, uvw.y, uvw.z);
+  const float4 r = lerp8xn<3>(t, cen);
+  return v3(r.x, r.y, r.z);
+}
+// sample_center at a point clamped to [0.001, 0.999] (make_taps_in)
+template <class V4> __device__ __forceinline__ dob_v3 sample_center_in(const Grid& g, const V4* cen, dob_v3 uvw) {
+  const Taps t = make_taps_in(g, uvw.x, uvw.y, uvw.z);
   const float4 r = lerp8xn<3>(t, cen);
   return v3(r.x, r.y, r.z);
 }

@@ -89,7 +89,7 @@ __device__ __forceinline__ float sample_mac(const Grid& g, const VS* a, dob_v3 u
   if (comp == 1) uvw.y = uvw.y - 0.5f * g.ry;
   if (comp == 2) uvw.z = uvw.z - 0.5f * g.rz;
   uvw = clamp3(uvw, 0.001f, 0.999f);
-  const Taps t = make_taps(g, uvw.x, uvw.y, uvw.z);
+  const Taps t = make_taps_in(g, uvw.x, uvw.y, uvw.z);
   return lerp8(t, a);
 }
 // midpoint trace from the face centre uvwF, whose centre velocity is v0
@@ -97,7 +97,7 @@ template <class V4>
 __device__ __forceinline__ dob_v3 trace_back(const Grid& g, const V4* cen, dob_v3 uvwF, dob_v3 v0, float dtv,
                                              const Recip3& dom) {
   const dob_v3 uvwMid = clamp3(uvwF - (0.5f * (v0 * dtv)) / dom, 0.002f, 0.998f);
-  const dob_v3 vMid = sample_center(g, cen, uvwMid);
+  const dob_v3 vMid = sample_center_in(g, cen, uvwMid);
   return clamp3(uvwF - (vMid * dtv) / dom, 0.002f, 0.998f);
 }
 __device__ __forceinline__ float azim_neck(float theta, float seed) {
@@ -566,19 +566,19 @@ __device__ __forceinline__ void predict_cell(const Grid& gc, const Grid& g, cons
       back = clamp3(uvw - (v0 * dtv) / dom, 0.001f, 0.999f);
     } else {
       const dob_v3 mid = clamp3(uvw - (0.5f * (v0 * dtv)) / dom, 0.001f, 0.999f);
-      const dob_v3 vMid = sample_center(g, cen, mid);
+      const dob_v3 vMid = sample_center_in(g, cen, mid);
       back = clamp3(uvw - (vMid * dtv) / dom, 0.001f, 0.999f);
     }
-    const Taps t = make_taps(gc, back.x, back.y, back.z);
+    const Taps t = make_taps_in(gc, back.x, back.y, back.z);
     const float pv = lerp8x4(t, conc4).y;
     stf(pred + i, pv);
     if (pbrick && pv != 0.0f) mark_brick(gc, pbrick, x, y, z);
   } else {
     const dob_v3 v0 = gc.nx == g.nx ? center_at_cell(g, cen, uvw, x, y, z, i) : sample_center(g, cen, uvw);
     const dob_v3 mid = clamp3(uvw - (0.5f * (v0 * dtv)) / dom, 0.001f, 0.999f);
-    const dob_v3 vMid = sample_center(g, cen, mid);
+    const dob_v3 vMid = sample_center_in(g, cen, mid);
     const dob_v3 back = clamp3(uvw - (vMid * dtv) / dom, 0.001f, 0.999f);
-    const Taps tb = make_taps(gc, back.x, back.y, back.z);
+    const Taps tb = make_taps_in(gc, back.x, back.y, back.z);
     if (lim) {  // also the limiter's bracket for k_dye_resolve_lim
       float c[8];
       load8(tb, dye, c);
@@ -677,15 +677,15 @@ __device__ __forceinline__ void resolve_ref_cell(const Grid& gc, const Grid& g, 
                 (1.0f / 6.0f);
   const dob_v3 uvw = (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / dimr;
   const float dtv = P.dt;
-  const dob_v3 dom = dsize_of(P);
+  const Recip3 dom = dom_recip(P);
   const dob_v3 pw = to_world(P, uvw);
   const float halfXZ = P.U[52], yMin = P.U[53];
   const dob_v3 v0 = sample_center(g, cen, uvw);
   const dob_v3 uvwMid = clamp3(uvw - (0.5f * (v0 * dtv)) / dom, 0.001f, 0.999f);
-  const dob_v3 vMid = sample_center(g, cen, uvwMid);
+  const dob_v3 vMid = sample_center_in(g, cen, uvwMid);
   const dob_v3 uvwBack = clamp3(uvw - (vMid * dtv) / dom, 0.001f, 0.999f);
   const dob_v3 uvwFwd = clamp3(uvw + (v0 * dtv) / dom, 0.001f, 0.999f);
-  const float gBackEst = lerp8(make_taps(gc, uvwFwd.x, uvwFwd.y, uvwFwd.z), pred);
+  const float gBackEst = lerp8(make_taps_in(gc, uvwFwd.x, uvwFwd.y, uvwFwd.z), pred);
   const float4 orig = ld4(conc + i);
   const float gOrig = orig.y;
   const float gCorr = gPred + (0.45f * P.U[47]) * (gOrig - gBackEst);
@@ -822,10 +822,10 @@ __global__ void __launch_bounds__(256) k_dye_resolve_box(Grid gc, Grid g, const 
   const dob_v3 uvw = (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / grid_recip(gc);
   const dob_v3 v0 = gc.nx == g.nx ? center_at_cell(g, cen, uvw, x, y, z, i) : sample_center(g, cen, uvw);
   const dob_v3 uvwMid = clamp3(uvw - (0.5f * (v0 * dtv)) / dom, 0.001f, 0.999f);
-  const dob_v3 vMid = sample_center(g, cen, uvwMid);
+  const dob_v3 vMid = sample_center_in(g, cen, uvwMid);
   const dob_v3 uvwBack = clamp3(uvw - (vMid * dtv) / dom, 0.001f, 0.999f);
   const dob_v3 uvwFwd = clamp3(uvw + (v0 * dtv) / dom, 0.001f, 0.999f);
-  const float gBackEst = lerp8(make_taps(gc, uvwFwd.x, uvwFwd.y, uvwFwd.z), pred);
+  const float gBackEst = lerp8(make_taps_in(gc, uvwFwd.x, uvwFwd.y, uvwFwd.z), pred);
   const float gOrig = ldf(dye + i);
   // one explicit FMA, so the step's and the stage's resolve (and the
   // adjoint's replay of it) round the correction alike
@@ -833,7 +833,7 @@ __global__ void __launch_bounds__(256) k_dye_resolve_box(Grid gc, Grid g, const 
   // the limiter's bracket: the 8 dye taps around the departure point (the
   // predictor's taps)
   float c[8];
-  load8(make_taps(gc, uvwBack.x, uvwBack.y, uvwBack.z), dye, c);
+  load8(make_taps_in(gc, uvwBack.x, uvwBack.y, uvwBack.z), dye, c);
   stf(out + i, dob_clampf(gCorr, min8(c), max8(c)));
 }
 
@@ -856,7 +856,7 @@ __global__ void __launch_bounds__(256, 8) k_dye_resolve_lim(Grid gc, Grid g, con
                      grid_recip(gc);
   const dob_v3 v0 = gc.nx == g.nx ? center_at_cell(g, cen, uvw, x, y, z, i) : sample_center(g, cen, uvw);
   const dob_v3 uvwFwd = clamp3(uvw + (v0 * dtv) / dom, 0.001f, 0.999f);
-  const float gBackEst = lerp8(make_taps(gc, uvwFwd.x, uvwFwd.y, uvwFwd.z), pred);
+  const float gBackEst = lerp8(make_taps_in(gc, uvwFwd.x, uvwFwd.y, uvwFwd.z), pred);
   const float gOrig = ldf(dye + i);
   // one explicit FMA, so the step's and the stage's resolve (and the
   // adjoint's replay of it) round the correction alike
