@@ -174,7 +174,7 @@ __device__ __forceinline__ void adj_face(const Grid& g, const float* uk, const f
   const dob_v3 v0 = lerp8x3_fixed(t0, cen);
   const dob_v3 M = F - (0.5f * (v0 * dtv)) / dom;
   const dob_v3 Mc = clamp3(M, 0.002f, 0.998f);
-  const Taps tM = make_taps(g, Mc.x, Mc.y, Mc.z);
+  const Taps tM = make_taps_in(g, Mc.x, Mc.y, Mc.z);
   const float4 vmr = lerp8xn<3>(tM, cen);
   const dob_v3 vMid = v3(vmr.x, vmr.y, vmr.z);
   const dob_v3 B = F - (vMid * dtv) / dom;
@@ -184,7 +184,7 @@ __device__ __forceinline__ void adj_face(const Grid& g, const float* uk, const f
   if (comp == 1) S.y = S.y - 0.5f * g.ry;
   if (comp == 2) S.z = S.z - 0.5f * g.rz;
   const dob_v3 Sc = clamp3(S, 0.001f, 0.999f);
-  const Taps tS = make_taps(g, Sc.x, Sc.y, Sc.z);
+  const Taps tS = make_taps_in(g, Sc.x, Sc.y, Sc.z);
   // backward
   scatter8(auk, tS, gout);
   const dob_v3 gS = (gout * lerp8_dfrac(tS, node_lo(g, Sc.x, Sc.y, Sc.z), uk)) * dims * pass3(S, 0.001f, 0.999f);
@@ -793,12 +793,12 @@ __global__ void __launch_bounds__(256, 4) k_adj_conc_predict(Grid gc, Grid g, co
   const dob_v3 v0 = lerp8x3_fixed(t0, cen);
   const dob_v3 M = uvw - (0.5f * (v0 * dtv)) / dom;
   const dob_v3 Mc = clamp3(M, 0.001f, 0.999f);
-  const Taps tM = make_taps(g, Mc.x, Mc.y, Mc.z);
+  const Taps tM = make_taps_in(g, Mc.x, Mc.y, Mc.z);
   const float4 vmr = lerp8xn<3>(tM, cen);
   const dob_v3 vMid = v3(vmr.x, vmr.y, vmr.z);
   const dob_v3 B = uvw - (vMid * dtv) / dom;
   const dob_v3 Bc = clamp3(B, 0.001f, 0.999f);
-  const Taps tB = make_taps(gc, Bc.x, Bc.y, Bc.z);
+  const Taps tB = make_taps_in(gc, Bc.x, Bc.y, Bc.z);
   scatter8(ac, tB, gout);
   const dob_v3 gB = (gout * lerp8_dfrac(tB, node_lo(gc, Bc.x, Bc.y, Bc.z), dye)) * dimsc * pass3(B, 0.001f, 0.999f);
   const dob_v3 gvMid = -(gB * dtv) / dom;
@@ -829,12 +829,12 @@ __global__ void __launch_bounds__(256, 5) k_adj_dye_resolve(Grid gc, Grid g, con
   const Taps t0 = make_taps_exact(g, uvw.x, uvw.y, uvw.z);  // the forward's cell-centre sample (dye on the velocity grid)
   const dob_v3 v0 = lerp8x3_fixed(t0, cen);
   const dob_v3 uvwMid = clamp3(uvw - (0.5f * (v0 * dtv)) / dom, 0.001f, 0.999f);
-  const float4 vmr = lerp8xn<3>(make_taps(g, uvwMid.x, uvwMid.y, uvwMid.z), cen);
+  const float4 vmr = lerp8xn<3>(make_taps_in(g, uvwMid.x, uvwMid.y, uvwMid.z), cen);
   const dob_v3 vMid = v3(vmr.x, vmr.y, vmr.z);
   const dob_v3 uvwBack = clamp3(uvw - (vMid * dtv) / dom, 0.001f, 0.999f);
   const dob_v3 Fw = uvw + (v0 * dtv) / dom;
   const dob_v3 uvwFwd = clamp3(Fw, 0.001f, 0.999f);
-  const Taps tF = make_taps(gc, uvwFwd.x, uvwFwd.y, uvwFwd.z);
+  const Taps tF = make_taps_in(gc, uvwFwd.x, uvwFwd.y, uvwFwd.z);
   const float gBackEst = lerp8(tF, pred);
   const float kap = 0.45f * P.sharp;
   const float gCorr = __fmaf_rn(kap, ldv(dye + i) - gBackEst, ldv(pred + i));  // as the forward rounds it
