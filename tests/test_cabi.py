@@ -100,5 +100,6 @@ def test_null_arguments(lib):
     assert lib.dob_create(None, None) == abi.DOB_EINVAL
     assert lib.dob_reset(None) == abi.DOB_EINVAL
     assert lib.dob_step(None, 1, 0, None) == abi.DOB_EINVAL
+    assert lib.dob_set_step_stats(None, abi.STATS_ALL) == abi.DOB_EINVAL
     lib.dob_destroy(None)
     assert lib.dob_abi_version() == abi.DOB_ABI_VERSION
