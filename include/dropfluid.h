@@ -444,8 +444,11 @@ dob_status dob_adjoint_stage(dob_ctx* ctx, int stage);
    every `checkpoint_every` steps in device memory (mixed mode: the dye at
    its binary16 width and the pressure as its FP32 pair).  The steps of the last
    segment also record the linearisation points the backward needs, so the
-   next dob_tape_backward does not recompute that segment.  The context ends
-   in the final state, as after dob_step (same bits). */
+   next dob_tape_backward does not recompute that segment; with
+   checkpoint_every = nsteps that is the whole trajectory (the tape then
+   holds nsteps steps' points, about 0.45 GB per step at 192x256x192 in
+   FP32).  The context ends in the final state, as after dob_step (same
+   bits). */
 dob_status dob_tape_forward(dob_ctx* ctx, int nsteps, int checkpoint_every);
 
 /* Backward half: given d loss / d final dye (Nc floats, host), recomputes
