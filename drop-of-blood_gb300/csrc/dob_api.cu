@@ -221,9 +221,13 @@ static void enqueue_step_body(dob_ctx* ctx, DevState& s, cudaStream_t st, float*
     if (!s.ref && stage == DOB_STAGE_MAC_TO_CENTER) continue;
     if (stage_ms) cudaEventRecord(ctx->stage_ev[0], st);
     if (!s.ref && stage == DOB_STAGE_PROJECT) {
-      // with statistics the projection also forms max |div| (no separate pass)
+      // with statistics the projection also forms max |div| (no separate
+      // pass), and always the bound on the centre velocity that lets the
+      // predictor skip blocks that cannot reach dye
       if (stats_div) cudaMemsetAsync(s.redu + REDU_MAXDIV, 0, sizeof(unsigned int), st);
-      launch_project_center_box(s, st, ctx->cfg.dt / ctx->cfg.dx, stats_div ? s.redu + REDU_MAXDIV : nullptr);
+      cudaMemsetAsync(s.redu + REDU_SPEED, 0, sizeof(unsigned int), st);
+      launch_project_center_box(s, st, ctx->cfg.dt / ctx->cfg.dx, stats_div ? s.redu + REDU_MAXDIV : nullptr,
+                                s.redu + REDU_SPEED);
       swap_vel(s);
     } else if (!s.ref && stage == DOB_STAGE_MAC_RHS) {
       // with statistics the mean removal also forms ||rhs||^2
@@ -234,8 +238,8 @@ static void enqueue_step_body(dob_ctx* ctx, DevState& s, cudaStream_t st, float*
       swap_vel(s);
     } else if (!s.ref && stage == DOB_STAGE_CONC_PREDICT) {
       // closed box: the predictor brackets its taps for the resolve, which
-      // then traces only the forward sample
-      launch_conc_predict(s, st, true);
+      // then traces only the forward sample; both skip clear water
+      launch_conc_predict(s, st, true, true);
     } else if (!s.ref && stage == DOB_STAGE_CONC_RESOLVE) {
       launch_dye_resolve_lim(s, st);
       std::swap(s.conc, s.conc2);
@@ -502,9 +506,11 @@ dob_status dob_create(const dob_config* cfg, dob_ctx** out) {
   const int nch = s.ref ? 4 : 1;
   A(&s.conc, Nc * nch * dsb); A(&s.conc2, Nc * nch * dsb); A(&s.pred, Nc * dsb);
   s.concA = s.conc;
-  if (s.ref) {
+  s.concB = s.conc2;
+  {
     const size_t nb = dye_brick_count(s.gc) * sizeof(uint32_t);
-    A((void**)&s.cbrickA, nb); A((void**)&s.cbrickB, nb); A((void**)&s.pbrick, nb);
+    A((void**)&s.cbrickA, nb); A((void**)&s.cbrickB, nb);
+    if (s.ref) A((void**)&s.pbrick, nb);
   }
   if (!s.ref) A(&s.lim, Nc * 2 * dsb);
   A((void**)&s.splatI, Nc * 4); A((void**)&s.splatL, Nc * 4);
@@ -648,7 +654,7 @@ dob_status dob_reset(dob_ctx* ctx) {
     const size_t nb = dye_brick_count(s.gc) * sizeof(uint32_t);
     CK(cudaMemsetAsync(s.cbrickA, 0, nb, ctx->stream));
     CK(cudaMemsetAsync(s.cbrickB, 0, nb, ctx->stream));
-    CK(cudaMemsetAsync(s.pbrick, 0, nb, ctx->stream));
+    if (s.pbrick) CK(cudaMemsetAsync(s.pbrick, 0, nb, ctx->stream));
   }
   CK(cudaMemsetAsync(s.pred, 0, Nc * dsb, ctx->stream));
   CK(cudaMemsetAsync(s.splatI, 0, Nc * 4, ctx->stream));
@@ -684,6 +690,7 @@ dob_status dob_inject_sphere(dob_ctx* ctx, const float c[3], float r, float dye,
   dob_status st = upload_params(ctx, 0);
   if (st != DOB_OK) return st;
   launch_inject_sphere(ctx->s, c, r, dye, vel, sigma, seed, ctx->stream);
+  launch_dye_bricks_unknown(ctx->s, ctx->stream);
   ctx->inject_pending = kInjectedSteps;
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(ctx->stream));
@@ -701,6 +708,7 @@ dob_status dob_inject_sphere_soft(dob_ctx* ctx, const float c[3], float r, float
   dob_status st = upload_params(ctx, 0);
   if (st != DOB_OK) return st;
   launch_inject_sphere_soft(ctx->s, c, r, edge, dye, vel, sigma, seed, ctx->stream);
+  launch_dye_bricks_unknown(ctx->s, ctx->stream);
   ctx->inject_pending = kInjectedSteps;
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(ctx->stream));
@@ -733,11 +741,8 @@ dob_status dob_set_high_water(dob_ctx* ctx, uint32_t hw) {
 // Dye written from outside the step (field I/O, snapshots): every dye brick
 // may hold dye until the next resolve rewrites the flags.
 static dob_status dye_bricks_unknown(dob_ctx* ctx) {
-  DevState& s = ctx->s;
-  if (!s.cbrickA) return DOB_OK;
-  const size_t nb = dye_brick_count(s.gc) * sizeof(uint32_t);
-  CK(cudaMemsetAsync(s.cbrickA, 1, nb, ctx->stream));
-  CK(cudaMemsetAsync(s.cbrickB, 1, nb, ctx->stream));
+  launch_dye_bricks_unknown(ctx->s, ctx->stream);
+  CK(cudaGetLastError());
   return DOB_OK;
 }
 

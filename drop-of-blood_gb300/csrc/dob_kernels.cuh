@@ -53,11 +53,12 @@ struct DevState {
   float* wfilm;                  // wave solver: the force pass's surfactant film
   float* parcels;
   uint32_t cap;
-  // sparse dye bricks (reference mode, k_fluid.cu): per 8x8x8 brick of the
-  // dye grid, whether the predictor / a dye buffer's lysed channel holds a
-  // nonzero value; concA is the buffer cbrickA belongs to (conc and conc2
-  // swap every step, the flags stay with their buffer)
-  const void* concA;
+  // sparse dye bricks (k_fluid.cu): per 8x8x8 brick of the dye grid,
+  // whether the predictor (reference mode) / a dye buffer (its lysed
+  // channel in reference mode) holds a nonzero value; concA and concB are
+  // the buffers cbrickA and cbrickB belong to (conc and conc2 swap every
+  // step, the flags stay with their buffer; other dye arrays have none)
+  const void *concA, *concB;
   uint32_t *cbrickA, *cbrickB, *pbrick;
   // light volume (reference mode, dims divisible by 4): 4 x binary16 per
   // velocity cell, and the raw and dilated occupancy of its 4x4x4 bricks
@@ -123,6 +124,7 @@ enum {
   REDU_INNER_DONE = 4,    // mixed solve: the round's V-cycles have converged (their kernels exit)
   REDU_VCYCLES = 5,       // mixed solve: V-cycles completed in the step
   REDU_INNER_ITERS = 6,   // mixed solve: V-cycles begun in the current round
+  REDU_SPEED = 7,         // closed-box step: max |centre velocity| per axis after the projection (float bits)
   REDU_DEFECT_MAX = 8,    // max |r| (float bits): [0] the round's residual, [1] the cycle's
   REDU_COUNT = 8 + 32
 };
@@ -228,6 +230,21 @@ __device__ __forceinline__ void block_sum_atomic_f(float v, double* out) {
   }
 }
 // Max of non-negative floats via their bit patterns.
+// Block maximum of unsigned values, one atomicMax per block (the bits of
+// |x| order non-negative floats, +inf above them and NaN above +inf).
+__device__ __forceinline__ void block_max_u32(unsigned int v, unsigned int* out) {
+  __shared__ unsigned int upart[32];
+  const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  const int nthreads = blockDim.x * blockDim.y * blockDim.z;
+  v = __reduce_max_sync(0xffffffffu, v);
+  if ((tid & 31) == 0) upart[tid >> 5] = v;
+  __syncthreads();
+  if (tid < 32) {
+    unsigned int s = tid < (nthreads + 31) / 32 ? upart[tid] : 0u;
+    s = __reduce_max_sync(0xffffffffu, s);
+    if (tid == 0 && s != 0u) atomicMax(out, s);
+  }
+}
 __device__ __forceinline__ void block_max_atomic(float v, unsigned int* out) {
   __shared__ float part[32];
   const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
@@ -277,17 +294,22 @@ void launch_mac_rhs_box(const DevState& s, cudaStream_t st, double* sumsq = null
 // projection of (u, v, w) into (u2, v2, w2) and the centre velocity of the
 // projected faces, one pass (the caller swaps the buffers)
 // maxbits: also max |div| * scale of the projected faces (statistics), as
-// launch_divergence forms it
+// launch_divergence forms it; speedbits: also the largest |component| of the
+// stored centre velocity (the sparse dye predictor's reach)
 void launch_project_center_box(const DevState& s, cudaStream_t st, float scale = 0.0f,
-                               unsigned int* maxbits = nullptr);
+                               unsigned int* maxbits = nullptr, unsigned int* speedbits = nullptr);
 void launch_divergence(const DevState& s, float* out, float scale, unsigned int* maxbits, cudaStream_t st);
 // bracket: also write the minimum and maximum of the predictor's 8 dye taps
-// (closed box) for launch_dye_resolve_lim.  sparse (reference mode, inside a
-// step, where the centre velocity is bounded by the projection's clamp):
-// skip the blocks the dye-brick flags show to be clear water (same results).
-// Both kernels always maintain the flags of what they write.
+// (closed box) for launch_dye_resolve_lim.  sparse (inside a step, where the
+// centre velocity is bounded: by the projection's clamp in reference mode,
+// by the projection's s.redu[REDU_SPEED] in the closed box): skip the
+// blocks the dye-brick flags show to be clear water (same results).  The
+// resolves always maintain the flags of the dye buffer they write.
 void launch_conc_predict(const DevState& s, cudaStream_t st, bool bracket = false, bool sparse = false);
 void launch_dye_resolve_lim(const DevState& s, cudaStream_t st);
+// dye written from outside the step (injection, field I/O, snapshots, the
+// tape): every brick of both dye buffers may hold dye until the next resolve
+void launch_dye_bricks_unknown(const DevState& s, cudaStream_t st);
 void launch_conc_resolve(const DevState& s, cudaStream_t st, bool sparse = false);
 // number of 8x8x8 dye bricks (one uint32 flag each)
 size_t dye_brick_count(const Grid& gc);

@@ -328,6 +328,7 @@ dob_status record_last_segment(dob_ctx* ctx, int seg, int len) {
   cudaMemcpyAsync(s.w, A->Tw[len], N * 4, cudaMemcpyDeviceToDevice, st);
   cudaMemcpyAsync(s.cen, A->Tcen[len], N * sizeof(float4), cudaMemcpyDeviceToDevice, st);
   cudaMemcpyAsync(s.conc, A->Tc[len], Nc * dye_bytes(ctx), cudaMemcpyDeviceToDevice, st);
+  launch_dye_bricks_unknown(s, st);  // the dye came from the tape
   cudaMemcpyAsync(s.pred, A->Tpred[len - 1], Nc * dye_bytes(ctx), cudaMemcpyDeviceToDevice, st);
   cudaMemcpyAsync(s.p, A->Tp, N * 4, cudaMemcpyDeviceToDevice, st);
   if (mixed(ctx)) cudaMemcpyAsync(s.plo, A->Tplo, N * 4, cudaMemcpyDeviceToDevice, st);

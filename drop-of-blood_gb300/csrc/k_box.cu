@@ -42,6 +42,8 @@ __global__ void __launch_bounds__(256) k_casson_box(Grid g, const StepParams* __
   uint32_t i = c.i;
   dob_v3 mZn = ld3(u, v, w, c.z0 > 0 ? i - c.sz : i);
   dob_v3 mac = ld3(u, v, w, i);
+  // a rolled loop: unrolled over its 8 planes it takes 58 registers and
+  // runs slower (93 -> 107 us at 192x256x192)
   for (int z = c.z0; z < c.zend; ++z) {
     const dob_v3 mZp = ld3(u, v, w, z < g.nz - 1 ? i + c.sz : i);
     const dob_v3 mXn = v3(x_minus(c, mac.x, u, i), x_minus(c, mac.y, v, i), x_minus(c, mac.z, w, i));
@@ -67,7 +69,7 @@ __global__ void __launch_bounds__(256) k_casson_box(Grid g, const StepParams* __
 }
 
 // ---- divergence into the split right-hand side (k_mac_rhs, closed box) ------------------
-template <class VS, int ZC>
+template <class VS, int ZC, bool FULL>
 __global__ void __launch_bounds__(256) k_rhs_box(Grid g, const VS* __restrict__ u, const VS* __restrict__ v,
                                                  const VS* __restrict__ w, float* __restrict__ rhs) {
   const Col c = column<ZC>(g);
@@ -75,7 +77,10 @@ __global__ void __launch_bounds__(256) k_rhs_box(Grid g, const VS* __restrict__ 
   const uint32_t half = (uint32_t)(g.n() >> 1), hx = (uint32_t)g.nx >> 1;
   uint32_t i = c.i;
   float wBack = c.z0 > 0 ? ldf(w + i - c.sz) : 0.0f;
-  for (int z = c.z0; z < c.zend; ++z) {
+#pragma unroll
+  for (int k = 0; k < ZC; ++k) {
+    const int z = c.z0 + k;
+    if (!FULL && z >= c.zend) break;
     const float uo_ = ldf(u + i), vo_ = ldf(v + i), wo_ = ldf(w + i);
     const float uL = x_minus(c, uo_, u, i);
     const float uRight = c.x >= g.nx - 1 ? 0.0f : uo_;
@@ -101,19 +106,28 @@ __global__ void __launch_bounds__(256) k_rhs_box(Grid g, const VS* __restrict__ 
 // Bound by the latency of the split-layout pressure loads: capped at 32
 // registers (8 blocks per SM, a 24-byte spill), 114.8 -> 102.5 us at
 // 192x256x192.
-template <class VS, int ZC>
-__global__ void __launch_bounds__(256, 8) k_project_center_box(Grid g, const VS* __restrict__ u,
+// FULL (nz % ZC == 0): the plane loop has a fixed trip count and is
+// unrolled, so the loads of the next planes issue ahead of this plane's
+// stores (102 -> 86 us at 192x256x192).  Blocks per SM of the register cap
+// (8: 32 registers) as measured against 6 and 4 (97 and 108 us).
+#ifndef DOB_PROJECT_MIN_BLOCKS
+#define DOB_PROJECT_MIN_BLOCKS 8
+#endif
+template <class VS, int ZC, bool FULL>
+__global__ void __launch_bounds__(256, DOB_PROJECT_MIN_BLOCKS) k_project_center_box(Grid g, const VS* __restrict__ u,
                                                             const VS* __restrict__ v, const VS* __restrict__ w,
                                                             const float* __restrict__ p,
                                                             const float* __restrict__ plo, VS* __restrict__ uo,
                                                             VS* __restrict__ vo, VS* __restrict__ wo,
                                                             typename Vec4Of<VS>::type* __restrict__ cen,
-                                                            float scale, unsigned int* __restrict__ maxbits) {
+                                                            float scale, unsigned int* __restrict__ maxbits,
+                                                            unsigned int* __restrict__ speedbits) {
   const Col c = column<ZC>(g);
   if (c.z0 >= g.nz) return;  // uniform over the block
   const uint32_t half = (uint32_t)(g.n() >> 1), hx = (uint32_t)g.nx >> 1;
   const bool df = plo != nullptr;
   float mdiv = 0.0f;  // max |div| dt/dx of the projected faces (maxbits: statistics)
+  unsigned int smax = 0u;  // bits of max |component| of the stored centre velocity (speedbits)
   auto pidx = [&](int x, int y, int z) {  // rb_index in 32 bits
     return ((uint32_t)(x + y + z) & 1u) * half + ((uint32_t)z * (uint32_t)g.ny + (uint32_t)y) * hx + ((uint32_t)x >> 1);
   };
@@ -130,7 +144,10 @@ __global__ void __launch_bounds__(256, 8) k_project_center_box(Grid g, const VS*
   }
   float pC, lC;
   ldp(pidx(c.x, c.y, c.z0), pC, lC);
-  for (int z = c.z0; z < c.zend; ++z) {
+#pragma unroll
+  for (int k = 0; k < ZC; ++k) {
+    const int z = c.z0 + k;
+    if (!FULL && z >= c.zend) break;
     const bool has_zp = z < g.nz - 1;
     float pZp = 0.0f, lZp = 0.0f;
     if (has_zp) ldp(pidx(c.x, c.y, z + 1), pZp, lZp);
@@ -159,7 +176,11 @@ __global__ void __launch_bounds__(256, 8) k_project_center_box(Grid g, const VS*
     if (c.valid) {
       stf(uo + i, mx); stf(vo + i, my); stf(wo + i, mz);
       const float uR = vs_round<VS>(mx), vU = vs_round<VS>(my), wF = vs_round<VS>(mz);
-      st4(cen + i, make_float4(0.5f * (uL + uR), 0.5f * (vD + vU), 0.5f * (wB + wF), 0.0f));
+      const float cx = 0.5f * (uL + uR), cy = 0.5f * (vD + vU), cz = 0.5f * (wB + wF);
+      st4(cen + i, make_float4(cx, cy, cz, 0.0f));
+      if (speedbits)  // of the values as stored (binary16 rounds them); NaN orders above every float
+        smax = max(smax, max(__float_as_uint(fabsf(vs_round<VS>(cx))),
+                             max(__float_as_uint(fabsf(vs_round<VS>(cy))), __float_as_uint(fabsf(vs_round<VS>(cz))))));
       // k_divergence's expression on the stored faces (walls are 0)
       if (maxbits) mdiv = dob_maxf(mdiv, fabsf((uR - uL) + (vU - vD) + (wF - wB)) * scale);
     }
@@ -169,6 +190,7 @@ __global__ void __launch_bounds__(256, 8) k_project_center_box(Grid g, const VS*
     i += c.sz;
   }
   if (maxbits) block_max_atomic(mdiv, maxbits);
+  if (speedbits) block_max_u32(smax, speedbits);
 }
 
 template <int ZC>
@@ -183,26 +205,36 @@ bool box_casson_applies(const DevState& s) {
 
 void launch_casson_box(const DevState& s, cudaStream_t st) {
   DOB_VEL_DISPATCH(s.prec, {
-    k_casson_box<VS, DS, kCassonZ><<<col_grid<kCassonZ>(s.g), dim3(32, 8), 0, st>>>(s.g, s.params, (const VS*)s.u, (const VS*)s.v,
-                                                                (const VS*)s.w, (const DS*)s.conc, (VS*)s.u2,
-                                                                (VS*)s.v2, (VS*)s.w2);
+    k_casson_box<VS, DS, kCassonZ><<<col_grid<kCassonZ>(s.g), dim3(32, 8), 0, st>>>(
+        s.g, s.params, (const VS*)s.u, (const VS*)s.v, (const VS*)s.w, (const DS*)s.conc, (VS*)s.u2, (VS*)s.v2,
+        (VS*)s.w2);
   });
 }
 
 void launch_mac_rhs_box(const DevState& s, cudaStream_t st, double* sumsq) {
   DOB_VEL_DISPATCH(s.prec, {
-    k_rhs_box<VS, kRhsZ><<<col_grid<kRhsZ>(s.g), dim3(32, 8), 0, st>>>(s.g, (const VS*)s.u, (const VS*)s.v, (const VS*)s.w,
-                                                         s.rhs);
+    if (s.g.nz % kRhsZ == 0)
+      k_rhs_box<VS, kRhsZ, true><<<col_grid<kRhsZ>(s.g), dim3(32, 8), 0, st>>>(s.g, (const VS*)s.u, (const VS*)s.v,
+                                                                             (const VS*)s.w, s.rhs);
+    else
+      k_rhs_box<VS, kRhsZ, false><<<col_grid<kRhsZ>(s.g), dim3(32, 8), 0, st>>>(s.g, (const VS*)s.u, (const VS*)s.v,
+                                                                              (const VS*)s.w, s.rhs);
   });
   launch_sum(s.rhs, s.g.n(), s.part + PART_RHS * kSumBlocks, s.num_sms, st);
   launch_sub_mean(s.rhs, s.g.n(), s.part + PART_RHS * kSumBlocks, s.num_sms, st, sumsq);
 }
 
-void launch_project_center_box(const DevState& s, cudaStream_t st, float scale, unsigned int* maxbits) {
+void launch_project_center_box(const DevState& s, cudaStream_t st, float scale, unsigned int* maxbits,
+                               unsigned int* speedbits) {
   DOB_VEL_DISPATCH(s.prec, {
-    k_project_center_box<VS, kProjectZ><<<col_grid<kProjectZ>(s.g), dim3(32, 8), 0, st>>>(
-        s.g, (const VS*)s.u, (const VS*)s.v, (const VS*)s.w, s.p, s.plo, (VS*)s.u2, (VS*)s.v2, (VS*)s.w2,
-        (typename Vec4Of<VS>::type*)s.cen, scale, maxbits);
+    if (s.g.nz % kProjectZ == 0)
+      k_project_center_box<VS, kProjectZ, true><<<col_grid<kProjectZ>(s.g), dim3(32, 8), 0, st>>>(
+          s.g, (const VS*)s.u, (const VS*)s.v, (const VS*)s.w, s.p, s.plo, (VS*)s.u2, (VS*)s.v2, (VS*)s.w2,
+          (typename Vec4Of<VS>::type*)s.cen, scale, maxbits, speedbits);
+    else
+      k_project_center_box<VS, kProjectZ, false><<<col_grid<kProjectZ>(s.g), dim3(32, 8), 0, st>>>(
+          s.g, (const VS*)s.u, (const VS*)s.v, (const VS*)s.w, s.p, s.plo, (VS*)s.u2, (VS*)s.v2, (VS*)s.w2,
+          (typename Vec4Of<VS>::type*)s.cen, scale, maxbits, speedbits);
   });
 }
 

@@ -529,13 +529,18 @@ __device__ __forceinline__ bool block_any_brick(const Grid& gc, const uint32_t* 
   return any != 0;
 }
 // The predictor's reach: RK2 departures move at most `speed` dt per axis in
-// world units, plus one voxel for the interpolation's taps.
+// world units, plus one voxel for the interpolation's taps (a reach of the
+// whole grid or more, or a non-finite speed, covers the whole grid).
+__device__ __forceinline__ int reach_voxels(float d, int n, float size) {
+  const float r = ceilf(d * (float)n / size);
+  return (r < (float)n ? (int)r : n) + 1;
+}
 __device__ __forceinline__ bool block_reaches_dye(const Grid& gc, const StepParams& P, const uint32_t* cbrick,
                                                   float speed, int zlo, int zhi) {
   const float d = speed * P.dt;
-  const int rx = (int)ceilf(d * (float)gc.nx / P.dsize[0]) + 1;
-  const int ry = (int)ceilf(d * (float)gc.ny / P.dsize[1]) + 1;
-  const int rz = (int)ceilf(d * (float)gc.nz / P.dsize[2]) + 1;
+  const int rx = reach_voxels(d, gc.nx, P.dsize[0]);
+  const int ry = reach_voxels(d, gc.ny, P.dsize[1]);
+  const int rz = reach_voxels(d, gc.nz, P.dsize[2]);
   return block_any_brick(gc, cbrick, rx, ry, rz, zlo, zhi);
 }
 
@@ -600,19 +605,30 @@ __global__ void __launch_bounds__(256, ZP == 1 ? 8 : 4) k_conc_predict(Grid gc, 
                                                       const typename Vec4Of<DS>::type* __restrict__ conc4,
                                                       const DS* __restrict__ dye, DS* __restrict__ pred,
                                                       DS* __restrict__ lim, const uint32_t* __restrict__ cbrick,
-                                                      uint32_t* __restrict__ pbrick) {
+                                                      uint32_t* __restrict__ pbrick,
+                                                      const unsigned int* __restrict__ speedbits) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int z0 = blockIdx.z * ZP;
   const int z1 = min(z0 + ZP, gc.nz);
   const StepParams& P = *Pp;
-  // reference mode inside a step (the centre velocity there comes from faces
-  // clamped to +-2 by the projection): a block whose departure points can
-  // only reach dye bricks with no lysed dye writes zeros without tracing
-  if (cbrick && !block_reaches_dye(gc, P, cbrick, kDyeSpeedBound, z0, z1 - 1)) {
-    if (x < gc.nx && y < gc.ny)
-      for (int z = z0; z < z1; ++z) stf(pred + gc.at(x, y, z), 0.0f);
-    return;
+  // inside a step: a block whose departure points can only reach dye bricks
+  // holding nothing but +0 (reference mode: no lysed dye) writes the zeros
+  // the trace would give without tracing.  The centre velocity is bounded
+  // per axis by the projection's clamp to +-2 in reference mode, by the
+  // projection's own maximum (speedbits, a margin of 1e-4 for the
+  // departure's rounding) in the closed box.
+  if (cbrick) {
+    const float speed = speedbits ? __uint_as_float(*speedbits) * 1.0001f : kDyeSpeedBound;
+    if (!block_reaches_dye(gc, P, cbrick, speed, z0, z1 - 1)) {
+      if (x < gc.nx && y < gc.ny)
+        for (int z = z0; z < z1; ++z) {
+          const size_t i = gc.at(x, y, z);
+          stf(pred + i, 0.0f);
+          if (lim) { stf(lim + 2 * i, 0.0f); stf(lim + 2 * i + 1, 0.0f); }
+        }
+      return;
+    }
   }
   if (x >= gc.nx || y >= gc.ny) return;
 #pragma unroll 1
@@ -839,16 +855,28 @@ __global__ void __launch_bounds__(256) k_dye_resolve_box(Grid gc, Grid g, const 
 
 // The same resolve in the step: the predictor (k_conc_predict with `lim`)
 // has already bracketed its 8 taps, so only the forward sample is traced.
+// cbrick_out (the flags of `out`): a brick is marked when it receives a
+// value whose bits are not those of +0.
 template <class VS, class DS>
 __global__ void __launch_bounds__(256, 8) k_dye_resolve_lim(Grid gc, Grid g, const StepParams* __restrict__ Pp,
                                                          const typename Vec4Of<VS>::type* __restrict__ cen,
                                                          const DS* __restrict__ dye, const DS* __restrict__ pred,
-                                                         const DS* __restrict__ lim, DS* __restrict__ out) {
+                                                         const DS* __restrict__ lim, DS* __restrict__ out,
+                                                         uint32_t* __restrict__ cbrick_out) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int z = blockIdx.z;
   if (x >= gc.nx || y >= gc.ny) return;
   const size_t i = gc.at(x, y, z);
+  // A bracket of two zeros clamps every correction to its upper end: min(max(g,
+  // lo), hi) is hi whenever lo and hi are zeros of either sign (max gives g > 0
+  // or lo, min of either with hi is hi), so the trace is not needed.
+  const float lo = ldf(lim + 2 * i), hi = ldf(lim + 2 * i + 1);
+  if (lo == 0.0f && hi == 0.0f) {
+    stf(out + i, hi);
+    if (cbrick_out && __float_as_uint(hi) != 0u) mark_brick(gc, cbrick_out, x, y, z);
+    return;
+  }
   const StepParams& P = *Pp;
   const float dtv = P.dt;
   const Recip3 dom = dom_recip(P);
@@ -861,7 +889,9 @@ __global__ void __launch_bounds__(256, 8) k_dye_resolve_lim(Grid gc, Grid g, con
   // one explicit FMA, so the step's and the stage's resolve (and the
   // adjoint's replay of it) round the correction alike
   const float gCorr = __fmaf_rn(0.45f * P.sharp, gOrig - gBackEst, ldf(pred + i));
-  stf(out + i, dob_clampf(gCorr, ldf(lim + 2 * i), ldf(lim + 2 * i + 1)));
+  const float r = dob_clampf(gCorr, lo, hi);
+  stf(out + i, r);
+  if (cbrick_out && __float_as_uint(r) != 0u) mark_brick(gc, cbrick_out, x, y, z);
 }
 
 // ---- host launchers ------------------------------------------------------------------------------
@@ -935,43 +965,54 @@ void launch_divergence(const DevState& s, float* out, float scale, unsigned int*
   });
 }
 
-// the dye-brick flags of a dye buffer (reference mode)
+// the dye-brick flags of one of the context's two dye buffers (none for
+// other dye arrays, such as the adjoint's tape)
 static uint32_t* brick_flags_of(const DevState& s, const void* conc) {
-  return conc == s.concA ? s.cbrickA : s.cbrickB;
+  return conc == s.concA ? s.cbrickA : conc == s.concB ? s.cbrickB : nullptr;
+}
+void launch_dye_bricks_unknown(const DevState& s, cudaStream_t st) {
+  const size_t nb = brick_grid(s.gc).n() * sizeof(uint32_t);
+  if (s.cbrickA) cudaMemsetAsync(s.cbrickA, 1, nb, st);
+  if (s.cbrickB) cudaMemsetAsync(s.cbrickB, 1, nb, st);
 }
 size_t dye_brick_count(const Grid& gc) { return brick_grid(gc).n(); }
 
 void launch_conc_predict(const DevState& s, cudaStream_t st, bool bracket, bool sparse) {
   uint32_t* pb = s.ref ? s.pbrick : nullptr;
   if (pb) cudaMemsetAsync(pb, 0, brick_grid(s.gc).n() * sizeof(uint32_t), st);
-  const uint32_t* cb = s.ref && sparse ? brick_flags_of(s, s.conc) : nullptr;
+  const uint32_t* cb = sparse ? brick_flags_of(s, s.conc) : nullptr;
   DOB_VEL_DISPATCH(s.prec, {
-    if (cb) {
+    if (cb && s.ref) {
       dim3 gr = cell_grid(s.gc);
       gr.z = (s.gc.nz + kDyeResolveZ - 1) / kDyeResolveZ;
       k_conc_predict<VS, DS, kDyeResolveZ><<<gr, cell_block(), 0, st>>>(
           s.gc, s.g, s.params, s.ref, (const typename Vec4Of<VS>::type*)s.cen,
-          (const typename Vec4Of<DS>::type*)s.conc, (const DS*)s.conc, (DS*)s.pred, nullptr, cb, pb);
+          (const typename Vec4Of<DS>::type*)s.conc, (const DS*)s.conc, (DS*)s.pred, nullptr, cb, pb, nullptr);
     } else {
+      // the closed box's bound on the centre velocity comes from the projection
       k_conc_predict<VS, DS, 1><<<cell_grid(s.gc), cell_block(), 0, st>>>(
           s.gc, s.g, s.params, s.ref, (const typename Vec4Of<VS>::type*)s.cen,
           (const typename Vec4Of<DS>::type*)s.conc, (const DS*)s.conc, (DS*)s.pred,
-          bracket && !s.ref ? (DS*)s.lim : nullptr, nullptr, pb);
+          bracket && !s.ref ? (DS*)s.lim : nullptr, cb, pb, cb ? s.redu + REDU_SPEED : nullptr);
     }
   });
 }
 
 void launch_dye_resolve_lim(const DevState& s, cudaStream_t st) {
+  uint32_t* cb = brick_flags_of(s, s.conc2);
+  if (cb) cudaMemsetAsync(cb, 0, brick_grid(s.gc).n() * sizeof(uint32_t), st);
   DOB_VEL_DISPATCH(s.prec, {
     k_dye_resolve_lim<VS, DS><<<cell_grid(s.gc), cell_block(), 0, st>>>(
         s.gc, s.g, s.params, (const typename Vec4Of<VS>::type*)s.cen, (const DS*)s.conc, (const DS*)s.pred,
-        (const DS*)s.lim, (DS*)s.conc2);
+        (const DS*)s.lim, (DS*)s.conc2, cb);
   });
 }
 
 void launch_conc_resolve(const DevState& s, cudaStream_t st, bool sparse) {
-  uint32_t* cb = s.ref ? brick_flags_of(s, s.conc2) : nullptr;
-  if (cb) cudaMemsetAsync(cb, 0, brick_grid(s.gc).n() * sizeof(uint32_t), st);
+  uint32_t* cb = brick_flags_of(s, s.conc2);
+  // reference mode: the resolve rewrites its output's flags; the closed box's
+  // tracing resolve does not, so its output's flags say "may hold dye"
+  if (cb) cudaMemsetAsync(cb, s.ref ? 0 : 1, brick_grid(s.gc).n() * sizeof(uint32_t), st);
   DOB_VEL_DISPATCH(s.prec, {
     if (s.ref) {
       dim3 gr = cell_grid(s.gc);

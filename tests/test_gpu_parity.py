@@ -557,6 +557,38 @@ def test_fused_projection_equals_separate_stages(gpu_lib):
     assert bits_equal(a.get_parcels(), b.get_parcels())
 
 
+def test_closed_box_sparse_dye_equals_stage_launches(gpu_lib):
+    """The closed-box step skips clear water in the dye predictor (blocks
+    whose departure points, bounded by the projection's largest centre
+    velocity, reach no dye brick) and in the resolve (voxels whose tap
+    bracket is two zeros): the same bits as the stages launched one by one
+    (dense), over 10 steps of box96 with a second injection (flags reset to
+    "may hold dye") halfway."""
+    abi = _abi()
+    from dropfluid import DropFluid, scenes
+    sc = scenes.box96()
+    sc.config.mg_cycles_injected = 0  # the stages run the plain V-cycle schedule
+    a, b = DropFluid(sc.config), DropFluid(sc.config)
+    sc.release(a, 0)
+    sc.release(b, 0)
+    order = [abi.STAGE_ADVECT_MAC, abi.STAGE_MAC_TO_CENTER, abi.STAGE_CASSON_FORCES, abi.STAGE_MAC_RHS,
+             abi.STAGE_PRESSURE_SOLVE, abi.STAGE_PROJECT, abi.STAGE_MAC_TO_CENTER, abi.STAGE_CLEAR_SPLATS,
+             abi.STAGE_PARCEL_EMIT, abi.STAGE_PARCEL_ADVECT, abi.STAGE_CONC_PREDICT, abi.STAGE_CONC_RESOLVE]
+    for k in range(10):
+        if k == 5:
+            for e in (a, b):
+                e.inject_sphere((40.0, 70.0, 50.0), 6.0, 1.0, (0.0, -0.5, 0.0), 0.0, 99)
+        a.step(1)
+        for stage in order:
+            b.run_stage(stage)
+        for f in (abi.FIELD_VEL_U, abi.FIELD_VEL_V, abi.FIELD_VEL_W, abi.FIELD_PRESSURE, abi.FIELD_CONC):
+            assert bits_equal(a.get_field(f), b.get_field(f)), (k, f)
+    conc = a.get_field(abi.FIELD_CONC)
+    assert (conc > 0).mean() < 0.5  # most of the box is clear water: the skips ran
+    a.close()
+    b.close()
+
+
 def test_injection_step_runs_more_cycles(gpu_lib, oracle_mod):
     """The two steps after a drop's injection run mg_cycles_injected V-cycles
     (closed-box default 8): their projections hold max |div| dt/dx <= 1e-5,
