@@ -823,7 +823,10 @@ def headline_step_roofline(scene, start, n, steps_per_s):
     peak, src = measured_peaks()
     gbs = b * steps_per_s / 1e9
     return {"bytes_per_step": b, "vcycles_per_step": mean_c, "achieved_gbs": gbs, "frac": gbs / peak,
-            "peak_source": src, "model": "stage byte model per velocity cell (bench.step_bytes_per_cell)"}
+            "peak_source": src, "model": "stage byte model per velocity cell (bench.step_bytes_per_cell); it "
+                                         "counts the dye predictor and resolve over every voxel, while the step "
+                                         "skips clear water there, so the fraction is the step's rate against "
+                                         "the dense algorithm's bytes"}
 
 
 def release_note(scene, start, n):
