@@ -53,8 +53,15 @@ __global__ void __launch_bounds__(256) k_casson_box(Grid g, const StepParams* __
     const dob_v3 lapMac = (mXp + mXn + mYp + mYn + mZp + mZn) - 6.0f * mac;
     const float cval = ldf(dye + i);
     const float cc = dob_clampf(cval, 0.0f, 1.5f);
-    const float gdot = div_by(dob_sqrt(dot3(du, du) + dot3(dv, dv) + dot3(dw, dw)), twoDx, rTwoDx);
-    const float sqrtYield = dob_sqrt(P.tau_y * cc * cc / (gdot + 0.4f));
+    const float ssq = dot3(du, du) + dot3(dv, dv) + dot3(dw, dw);
+    // clear water (cc = +0) with a finite shear and yield stress: the yield
+    // term is sqrt(+-0 / (gdot + 0.4)), a zero that leaves sqrtMu + it
+    // unchanged, so its square roots and division are not formed
+    float sqrtYield = 0.0f;
+    if (!(cc == 0.0f && ssq <= 3.4e38f && fabsf(P.tau_y) <= 3.4e38f)) {
+      const float gdot = div_by(dob_sqrt(ssq), twoDx, rTwoDx);
+      sqrtYield = dob_sqrt(P.tau_y * cc * cc / (gdot + 0.4f));
+    }
     const float nu = (sqrtMu + sqrtYield) * (sqrtMu + sqrtYield);
     const float alpha = dob_minf(div_by(nu * dtv, dx2, rDx2), 0.125f);
     dob_v3 out = mac + alpha * lapMac;

@@ -344,11 +344,18 @@ __global__ void __launch_bounds__(256) k_casson(Grid g, Grid gc, const StepParam
   if (ref) {
     const dob_v3 concCell = sample_conc_rg<DS>(gc, conc4, uvwCell);
     const float cRbc = dob_clampf(concCell.x, 0.0f, 1.5f);
-    const float shearRate = 50.0f * dob_sqrt(dot3(du, du) + dot3(dv, dv) + dot3(dw, dw) + 1e-6f);
     const float cassonScale = P.U[58];
     const float sqrtMuInf = dob_sqrt(0.00010f * (1.0f + 1.35f * cRbc));
-    const float tauYield = 0.0036f * cassonScale * cRbc * cRbc;
-    const float sqrtYieldTerm = dob_sqrt(tauYield / dob_maxf(shearRate + 0.40f, 0.40f));
+    // without red cells (cRbc = +0) and with a finite scale the yield term
+    // is sqrt(+-0 / max(shearRate + 0.4, 0.4)), a zero that leaves
+    // sqrtMuInf + it unchanged: the shear rate's root and the division are
+    // not formed
+    float sqrtYieldTerm = 0.0f;
+    if (!(cRbc == 0.0f && fabsf(cassonScale) <= 3.4e38f)) {
+      const float shearRate = 50.0f * dob_sqrt(dot3(du, du) + dot3(dv, dv) + dot3(dw, dw) + 1e-6f);
+      const float tauYield = 0.0036f * cassonScale * cRbc * cRbc;
+      sqrtYieldTerm = dob_sqrt(tauYield / dob_maxf(shearRate + 0.40f, 0.40f));
+    }
     const float alpha = dob_clampf((sqrtMuInf + sqrtYieldTerm) * (sqrtMuInf + sqrtYieldTerm), 0.00010f, 0.0044f);
     mac = mac + alpha * lapMac;
     if (flags & DOB_PHYS_VORT_CONF) {
