@@ -189,10 +189,7 @@ static void enqueue_stage(dob_ctx* ctx, DevState& s, int stage, cudaStream_t st,
     case DOB_STAGE_MAC_RHS: launch_mac_rhs(s, st); break;
     case DOB_STAGE_PRESSURE_SOLVE: launch_pressure_solve(s, st); break;
     case DOB_STAGE_PROJECT: launch_project(s, st); break;
-    case DOB_STAGE_CLEAR_SPLATS:
-      cudaMemsetAsync(s.splatI, 0, nc * 4, st);
-      cudaMemsetAsync(s.splatL, 0, nc * 4, st);
-      break;
+    case DOB_STAGE_CLEAR_SPLATS: launch_clear_splats(s, st); break;
     case DOB_STAGE_PARCEL_EMIT: launch_parcel_emit(s, st); break;
     case DOB_STAGE_PARCEL_ADVECT: launch_parcel_advect(s, st); break;
     case DOB_STAGE_CONC_PREDICT: launch_conc_predict(s, st, false, in_step); break;
@@ -509,7 +506,7 @@ dob_status dob_create(const dob_config* cfg, dob_ctx** out) {
   s.concB = s.conc2;
   {
     const size_t nb = dye_brick_count(s.gc) * sizeof(uint32_t);
-    A((void**)&s.cbrickA, nb); A((void**)&s.cbrickB, nb);
+    A((void**)&s.cbrickA, nb); A((void**)&s.cbrickB, nb); A((void**)&s.sbrick, nb);
     if (s.ref) A((void**)&s.pbrick, nb);
   }
   if (!s.ref) A(&s.lim, Nc * 2 * dsb);
@@ -654,6 +651,7 @@ dob_status dob_reset(dob_ctx* ctx) {
     const size_t nb = dye_brick_count(s.gc) * sizeof(uint32_t);
     CK(cudaMemsetAsync(s.cbrickA, 0, nb, ctx->stream));
     CK(cudaMemsetAsync(s.cbrickB, 0, nb, ctx->stream));
+    CK(cudaMemsetAsync(s.sbrick, 0, nb, ctx->stream));  // the splat accumulators are zeroed below
     if (s.pbrick) CK(cudaMemsetAsync(s.pbrick, 0, nb, ctx->stream));
   }
   CK(cudaMemsetAsync(s.pred, 0, Nc * dsb, ctx->stream));
@@ -801,6 +799,8 @@ dob_status dob_set_field(dob_ctx* ctx, int field, const void* host, size_t bytes
     dob_status bs = dye_bricks_unknown(ctx);
     if (bs != DOB_OK) return bs;
   }
+  if ((field == DOB_FIELD_SPLAT_INTACT || field == DOB_FIELD_SPLAT_LYSED) && ctx->s.sbrick)
+    CK(cudaMemsetAsync(ctx->s.sbrick, 1, dye_brick_count(ctx->s.gc) * sizeof(uint32_t), ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   const size_t eb = f.kind == 0 ? vs_bytes(ctx->s.prec) : f.kind == 1 ? ds_bytes(ctx->s.prec) : 4;
   if (f.kind == 4) {

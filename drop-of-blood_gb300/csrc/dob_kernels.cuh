@@ -60,6 +60,9 @@ struct DevState {
   // step, the flags stay with their buffer; other dye arrays have none)
   const void *concA, *concB;
   uint32_t *cbrickA, *cbrickB, *pbrick;
+  // per 8x8x8 brick of the dye grid, whether the splat accumulators may
+  // hold a nonzero sum there (set by every splat, cleared with the bricks)
+  uint32_t* sbrick;
   // light volume (reference mode, dims divisible by 4): 4 x binary16 per
   // velocity cell, and the raw and dilated occupancy of its 4x4x4 bricks
   half4* light;
@@ -310,6 +313,9 @@ void launch_dye_resolve_lim(const DevState& s, cudaStream_t st);
 // dye written from outside the step (injection, field I/O, snapshots, the
 // tape): every brick of both dye buffers may hold dye until the next resolve
 void launch_dye_bricks_unknown(const DevState& s, cudaStream_t st);
+// zero the splat accumulators: only the bricks a splat has marked (the
+// others hold zeros already), then clear their marks
+void launch_clear_splats(const DevState& s, cudaStream_t st);
 void launch_conc_resolve(const DevState& s, cudaStream_t st, bool sparse = false);
 // number of 8x8x8 dye bricks (one uint32 flag each)
 size_t dye_brick_count(const Grid& gc);

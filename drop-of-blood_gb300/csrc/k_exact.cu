@@ -15,7 +15,18 @@
 
 namespace dob {
 
-__device__ __forceinline__ void splat_trilinear(const Grid& gc, uint32_t* dst, dob_v3 uvw, float mass, float minMass) {
+// Mark the 8x8x8 brick of dye voxel (x, y, z) as holding a splat: a plain
+// store of 1 (writers of the same value may race harmlessly), left out when
+// the flag already reads 1 (most splats land in bricks already marked, and
+// a stale 0 only costs a redundant store).
+__device__ __forceinline__ void mark_splat(const Grid& gc, uint32_t* sbrick, int x, int y, int z) {
+  if (!sbrick) return;
+  const int bnx = (gc.nx + 7) >> 3, bny = (gc.ny + 7) >> 3;
+  uint32_t* f = sbrick + ((z >> 3) * bny + (y >> 3)) * bnx + (x >> 3);
+  if (*f == 0u) *f = 1u;
+}
+__device__ __forceinline__ void splat_trilinear(const Grid& gc, uint32_t* dst, dob_v3 uvw, float mass, float minMass,
+                                                uint32_t* sbrick) {
   if (mass <= minMass) return;
   const dob_v3 dims = v3((float)gc.nx, (float)gc.ny, (float)gc.nz);
   const dob_v3 coord = uvw * dims - v3(0.5f, 0.5f, 0.5f);
@@ -41,6 +52,21 @@ __device__ __forceinline__ void splat_trilinear(const Grid& gc, uint32_t* dst, d
   if (w101 > 0u) atomicAdd(dst + gc.at(x1, y0, z1), w101);
   if (w011 > 0u) atomicAdd(dst + gc.at(x0, y1, z1), w011);
   if (w111 > 0u) atomicAdd(dst + gc.at(x1, y1, z1), w111);
+  // the eight taps are the corners x0|x1 x y0|y1 x z0|z1: mark each distinct
+  // brick among them once (usually all eight share one)
+  if (sbrick && (w000 | w100 | w010 | w110 | w001 | w101 | w011 | w111)) {
+    const bool dx = (x0 >> 3) != (x1 >> 3), dy = (y0 >> 3) != (y1 >> 3), dz = (z0 >> 3) != (z1 >> 3);
+    mark_splat(gc, sbrick, x0, y0, z0);
+    if (dx) mark_splat(gc, sbrick, x1, y0, z0);
+    if (dy) mark_splat(gc, sbrick, x0, y1, z0);
+    if (dx && dy) mark_splat(gc, sbrick, x1, y1, z0);
+    if (dz) {
+      mark_splat(gc, sbrick, x0, y0, z1);
+      if (dx) mark_splat(gc, sbrick, x1, y0, z1);
+      if (dy) mark_splat(gc, sbrick, x0, y1, z1);
+      if (dx && dy) mark_splat(gc, sbrick, x1, y1, z1);
+    }
+  }
 }
 
 __device__ __forceinline__ float azim_modes(float theta, float seed) {
@@ -62,7 +88,7 @@ __device__ __forceinline__ dob_v3 hash33(dob_v3 p3in) {
 // ---- PARTICLE_EMIT (particles.ts:53-181) ---------------------------------------------
 __global__ void __launch_bounds__(256) k_parcel_emit(Grid gc, const StepParams* __restrict__ Pp, float4* parcels,
                                                      uint32_t cap, const float4* __restrict__ wave,
-                                                     uint32_t* __restrict__ splatL) {
+                                                     uint32_t* __restrict__ splatL, uint32_t* __restrict__ sbrick) {
   const StepParams& P = *Pp;
   const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t spawnCount = P.spawn_count;
@@ -96,7 +122,10 @@ __global__ void __launch_bounds__(256) k_parcel_emit(Grid gc, const StepParams* 
       const int cx = dob_clampi((int)floorf(cd.x), 0, gc.nx - 1), cy = dob_clampi((int)floorf(cd.y), 0, gc.ny - 1),
                 cz = dob_clampi((int)floorf(cd.z), 0, gc.nz - 1);
       const uint32_t fpOld = (uint32_t)rintf(o0.w * kSplatScale);
-      if (fpOld > 0u) atomicAdd(splatL + gc.at(cx, cy, cz), fpOld);
+      if (fpOld > 0u) {
+        atomicAdd(splatL + gc.at(cx, cy, cz), fpOld);
+        mark_splat(gc, sbrick, cx, cy, cz);
+      }
     }
   }
   const float seqIdx = (float)ringIdx + seed * 137.0f;
@@ -176,7 +205,8 @@ __global__ void __launch_bounds__(256) k_parcel_advect_ref(Grid g, Grid gc, cons
                                                            const typename Vec4Of<VS>::type* __restrict__ cen,
                                                            const typename Vec4Of<DS>::type* __restrict__ conc,
                                                            float4* __restrict__ parcels,
-                                                           uint32_t* __restrict__ splatI, uint32_t* __restrict__ splatL) {
+                                                           uint32_t* __restrict__ splatI, uint32_t* __restrict__ splatL,
+                                                           uint32_t* __restrict__ sbrick) {
   const StepParams& P = *Pp;
   const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= P.advect_count) return;
@@ -250,7 +280,7 @@ __global__ void __launch_bounds__(256) k_parcel_advect_ref(Grid g, Grid gc, cons
     const float dmBed = mass * dob_clampf(settleWeight * dtv * 1.65f, 0.0f, 0.095f);
     if (dmBed > 1e-7f) {
       mass = dob_maxf(0.0f, mass - dmBed);
-      splat_trilinear(gc, splatL, clamp3(uvw, 0.002f, 0.998f), dmBed * 0.68f, 1e-7f);
+      splat_trilinear(gc, splatL, clamp3(uvw, 0.002f, 0.998f), dmBed * 0.68f, 1e-7f, sbrick);
     }
     if (mass <= 1e-5f) {
       parcels[2 * (size_t)gid] = make_float4(q0.x, q0.y, q0.z, 0.0f);
@@ -279,14 +309,14 @@ __global__ void __launch_bounds__(256) k_parcel_advect_ref(Grid g, Grid gc, cons
     const float dmLysed = dob_minf(lysableHeadroom, mass * dob_clampf(fragility * kLysis * 1.95f * dtv, 0.0f, 0.16f));
     if (dmLysed > 1e-7f) {
       mass = dob_maxf(0.0f, mass - dmLysed);
-      splat_trilinear(gc, splatL, clamp3(uvw, 0.002f, 0.998f), dmLysed, 1e-7f);
+      splat_trilinear(gc, splatL, clamp3(uvw, 0.002f, 0.998f), dmLysed, 1e-7f, sbrick);
     }
   }
   parcels[2 * (size_t)gid] = make_float4(pos.x, pos.y, pos.z, mass);
   parcels[2 * (size_t)gid + 1] = make_float4(stretch.x, stretch.y, stretch.z, ageTicks + dob_clampf(lysis, 0.0f, 0.98f));
   const float sLenNow = length3(stretch);
   if (sLenNow < 0.0038f) {
-    splat_trilinear(gc, splatI, clamp3(uvw, 0.002f, 0.998f), mass, 1e-6f);
+    splat_trilinear(gc, splatI, clamp3(uvw, 0.002f, 0.998f), mass, 1e-6f, sbrick);
   } else {
     const float sxz = length2f(stretch.x, stretch.z);
     const dob_v3 horiz = sxz > 1e-4f ? v3(-stretch.z, 0.0f, stretch.x) / dob_maxf(sxz, 1e-5f) : v3(1.0f, 0.0f, 0.0f);
@@ -301,10 +331,10 @@ __global__ void __launch_bounds__(256) k_parcel_advect_ref(Grid g, Grid gc, cons
     const dob_v3 uvw1 = clamp3(to_uvw(P, pos - 0.14f * stretch + sheetVec), 0.002f, 0.998f);
     const dob_v3 uvw2 = clamp3(to_uvw(P, pos + 0.14f * stretch - sheetVec), 0.002f, 0.998f);
     const dob_v3 uvw3 = clamp3(to_uvw(P, pos + 0.42f * stretch), 0.002f, 0.998f);
-    splat_trilinear(gc, splatI, uvw0, 0.21f * mass, 1e-6f);
-    splat_trilinear(gc, splatI, uvw1, 0.29f * mass, 1e-6f);
-    splat_trilinear(gc, splatI, uvw2, 0.29f * mass, 1e-6f);
-    splat_trilinear(gc, splatI, uvw3, 0.21f * mass, 1e-6f);
+    splat_trilinear(gc, splatI, uvw0, 0.21f * mass, 1e-6f, sbrick);
+    splat_trilinear(gc, splatI, uvw1, 0.29f * mass, 1e-6f, sbrick);
+    splat_trilinear(gc, splatI, uvw2, 0.29f * mass, 1e-6f, sbrick);
+    splat_trilinear(gc, splatI, uvw3, 0.21f * mass, 1e-6f, sbrick);
   }
 }
 
@@ -313,7 +343,8 @@ __global__ void __launch_bounds__(256) k_parcel_advect_ref(Grid g, Grid gc, cons
 template <class VS>
 __global__ void __launch_bounds__(256) k_parcel_advect_box(Grid g, Grid gc, const StepParams* __restrict__ Pp,
                                                            const typename Vec4Of<VS>::type* __restrict__ cen,
-                                                           float4* __restrict__ parcels, uint32_t* __restrict__ splatI) {
+                                                           float4* __restrict__ parcels, uint32_t* __restrict__ splatI,
+                                                           uint32_t* __restrict__ sbrick) {
   const StepParams& P = *Pp;
   const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= P.advect_count) return;
@@ -331,7 +362,7 @@ __global__ void __launch_bounds__(256) k_parcel_advect_box(Grid g, Grid gc, cons
   const dob_v3 hi = v3(P.dmax[0], P.dmax[1], P.dmax[2]) - dsize_of(P) * 0.002f;
   pos = v3(dob_clampf(pos.x, lo.x, hi.x), dob_clampf(pos.y, lo.y, hi.y), dob_clampf(pos.z, lo.z, hi.z));
   parcels[2 * (size_t)gid] = make_float4(pos.x, pos.y, pos.z, mass);
-  splat_trilinear(gc, splatI, clamp3(to_uvw(P, pos), 0.002f, 0.998f), mass, 1e-6f);
+  splat_trilinear(gc, splatI, clamp3(to_uvw(P, pos), 0.002f, 0.998f), mass, 1e-6f, sbrick);
 }
 
 __global__ void k_count_alive(const float4* __restrict__ parcels, uint32_t cap, unsigned int* __restrict__ out) {
@@ -513,7 +544,7 @@ __global__ void k_eval_math(int fn, const float* __restrict__ x, const float* __
 
 void launch_parcel_emit(const DevState& s, cudaStream_t st) {
   if (!s.ref) return;
-  k_parcel_emit<<<8192 / 256, 256, 0, st>>>(s.gc, s.params, (float4*)s.parcels, s.cap, s.wave, s.splatL);
+  k_parcel_emit<<<8192 / 256, 256, 0, st>>>(s.gc, s.params, (float4*)s.parcels, s.cap, s.wave, s.splatL, s.sbrick);
 }
 
 void launch_parcel_advect(const DevState& s, cudaStream_t st) {
@@ -522,11 +553,52 @@ void launch_parcel_advect(const DevState& s, cudaStream_t st) {
     if (s.ref)
       k_parcel_advect_ref<VS, DS><<<blocks, 256, 0, st>>>(s.g, s.gc, s.params, (const typename Vec4Of<VS>::type*)s.cen,
                                                           (const typename Vec4Of<DS>::type*)s.conc, (float4*)s.parcels,
-                                                          s.splatI, s.splatL);
+                                                          s.splatI, s.splatL, s.sbrick);
     else
       k_parcel_advect_box<VS><<<blocks, 256, 0, st>>>(s.g, s.gc, s.params, (const typename Vec4Of<VS>::type*)s.cen,
-                                                      (float4*)s.parcels, s.splatI);
+                                                      (float4*)s.parcels, s.splatI, s.sbrick);
   });
+}
+
+// One warp per brick of the dye grid: a marked brick's accumulators in both
+// arrays are zeroed (8-voxel rows, 16-byte stores where the rows allow) and
+// its mark cleared; unmarked bricks hold zeros already.
+__global__ void __launch_bounds__(256) k_clear_splat_bricks(Grid gc, uint32_t* __restrict__ splatI,
+                                                            uint32_t* __restrict__ splatL,
+                                                            uint32_t* __restrict__ sbrick) {
+  const int bnx = (gc.nx + 7) >> 3, bny = (gc.ny + 7) >> 3, bnz = (gc.nz + 7) >> 3;
+  const int nb = bnx * bny * bnz, lane = threadIdx.x & 31;
+  const bool vec = (gc.nx & 3) == 0;
+  const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
+  for (int b = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); b < nb; b += (int)((gridDim.x * blockDim.x) >> 5)) {
+    if (sbrick[b] == 0u) continue;  // the same b in every lane
+    const int bx = b % bnx, by = (b / bnx) % bny, bz = b / (bnx * bny);
+    const int x0 = bx << 3, nxr = min(8, gc.nx - x0);
+    for (int r = lane; r < 64; r += 32) {  // 8 rows in y by 8 planes
+      const int y = (by << 3) + (r & 7), z = (bz << 3) + (r >> 3);
+      if (y >= gc.ny || z >= gc.nz) continue;
+      const size_t base = gc.at(x0, y, z);
+      if (vec && nxr == 8) {
+        reinterpret_cast<uint4*>(splatI + base)[0] = zero;
+        reinterpret_cast<uint4*>(splatI + base)[1] = zero;
+        reinterpret_cast<uint4*>(splatL + base)[0] = zero;
+        reinterpret_cast<uint4*>(splatL + base)[1] = zero;
+      } else {
+        for (int k = 0; k < nxr; ++k) { splatI[base + k] = 0u; splatL[base + k] = 0u; }
+      }
+    }
+    __syncwarp();
+    if (lane == 0) sbrick[b] = 0u;
+  }
+}
+
+void launch_clear_splats(const DevState& s, cudaStream_t st) {
+  if (!s.sbrick) {
+    cudaMemsetAsync(s.splatI, 0, s.gc.n() * 4, st);
+    cudaMemsetAsync(s.splatL, 0, s.gc.n() * 4, st);
+    return;
+  }
+  k_clear_splat_bricks<<<s.num_sms * 8, 256, 0, st>>>(s.gc, s.splatI, s.splatL, s.sbrick);
 }
 
 void launch_count_alive(const DevState& s, unsigned int* out, cudaStream_t st) {

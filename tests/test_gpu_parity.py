@@ -331,6 +331,20 @@ def test_reference_parcels_bit_exact(both):
     assert bits_equal(g.get_field(abi.FIELD_SPLAT_INTACT), o.get_field(abi.FIELD_SPLAT_INTACT))
     assert bits_equal(g.get_field(abi.FIELD_SPLAT_LYSED), o.get_field(abi.FIELD_SPLAT_LYSED))
     assert g.get_field(abi.FIELD_SPLAT_INTACT).sum() > 0
+    # the device clears only the bricks its splats marked: everything is zero
+    # again, and a second round matches the host's
+    g.run_stage(abi.STAGE_CLEAR_SPLATS)
+    assert not g.get_field(abi.FIELD_SPLAT_INTACT).any() and not g.get_field(abi.FIELD_SPLAT_LYSED).any()
+    for e in (g, o):
+        e.run_stage(abi.STAGE_CLEAR_SPLATS)
+        e.run_stage(abi.STAGE_PARCEL_EMIT)
+        e.run_stage(abi.STAGE_PARCEL_ADVECT)
+    assert bits_equal(g.get_field(abi.FIELD_SPLAT_INTACT), o.get_field(abi.FIELD_SPLAT_INTACT))
+    assert bits_equal(g.get_field(abi.FIELD_SPLAT_LYSED), o.get_field(abi.FIELD_SPLAT_LYSED))
+    # splats written from outside: every brick may hold them until the next clear
+    g.set_field(abi.FIELD_SPLAT_INTACT, np.full(g.get_field(abi.FIELD_SPLAT_INTACT).shape, 7.0, np.float32))
+    g.run_stage(abi.STAGE_CLEAR_SPLATS)
+    assert not g.get_field(abi.FIELD_SPLAT_INTACT).any() and not g.get_field(abi.FIELD_SPLAT_LYSED).any()
 
 
 # ---- full steps ------------------------------------------------------------------------------
