@@ -392,7 +392,7 @@ __global__ void __launch_bounds__(256, 4) k_residual_restrict2(Grid f, Grid c, f
 // half-sweep to follow).  Weights use the same per-cell formula as
 // k_prolong_add.
 template <class T, class TC, bool BLACK, int ZC>
-__global__ void __launch_bounds__(256) k_prolong_add2(Grid f, Grid c, int ref, T* __restrict__ a,
+__global__ void __launch_bounds__(256, ZC == 4 ? 3 : 4) k_prolong_add2(Grid f, Grid c, int ref, T* __restrict__ a,
                                                       const TC* __restrict__ e, const unsigned int* __restrict__ skip) {
   pdl_wait();
   pdl_trigger();
@@ -435,19 +435,8 @@ __global__ void __launch_bounds__(256) k_prolong_add2(Grid f, Grid c, int ref, T
     const float cy = __fmaf_rn(div_by((float)(2 * Y + d) + 0.5f, (float)f.ny, f.ry), (float)c.ny, -0.5f);
     fyv[d] = cy - floorf(cy);
   }
-#pragma unroll
-  for (int zi = 0; zi < ZC; ++zi) {
-    const int Z = Z0 + zi;
-    load_plane(Z + 1, t[2]);
-    float fzv[2];
-#pragma unroll
-    for (int d = 0; d < 2; ++d) {
-      const float cz = __fmaf_rn(div_by((float)(2 * Z + d) + 0.5f, (float)f.nz, f.rz), (float)c.nz, -0.5f);
-      fzv[d] = cz - floorf(cz);
-    }
-    // the fine rows of this coarse plane, all loaded before any store (the
-    // compiler cannot move a load of `a` above a store through it)
-    float2 ve[2][2], vo[2][2];
+  // the fine rows of coarse plane Z (BLACK: the colour-1 pair of each row)
+  auto load_rows = [&](int Z, float2 (&ve)[2][2], float2 (&vo)[2][2]) {
 #pragma unroll
     for (int dz = 0; dz < 2; ++dz)
 #pragma unroll
@@ -461,6 +450,26 @@ __global__ void __launch_bounds__(256) k_prolong_add2(Grid f, Grid c, int ref, T
           vo[dz][dy] = Pair<T>::ld(a + (par ? 0u : half) + r);
         }
       }
+  };
+  // The fine rows of each coarse plane are loaded before any of its stores,
+  // and those of the next plane before this plane's stores (the compiler
+  // cannot move a load of `a` above a store through it; the rows of
+  // different planes are different words), so a thread's planes overlap
+  // their load latencies.
+  float2 ve[2][2], vo[2][2];
+  load_rows(Z0, ve, vo);
+#pragma unroll
+  for (int zi = 0; zi < ZC; ++zi) {
+    const int Z = Z0 + zi;
+    load_plane(Z + 1, t[2]);
+    float2 ne[2][2], no[2][2];
+    if (zi + 1 < ZC) load_rows(Z + 1, ne, no);
+    float fzv[2];
+#pragma unroll
+    for (int d = 0; d < 2; ++d) {
+      const float cz = __fmaf_rn(div_by((float)(2 * Z + d) + 0.5f, (float)f.nz, f.rz), (float)c.nz, -0.5f);
+      fzv[d] = cz - floorf(cz);
+    }
 #pragma unroll
     for (int dz = 0; dz < 2; ++dz)
 #pragma unroll
@@ -489,6 +498,15 @@ __global__ void __launch_bounds__(256) k_prolong_add2(Grid f, Grid c, int ref, T
           Pair<T>::st(a + (par ? 0u : half) + r, make_float2(o2.x + corr[1], o2.y + corr[3]));
         }
       }
+    if (zi + 1 < ZC) {
+#pragma unroll
+      for (int dz = 0; dz < 2; ++dz)
+#pragma unroll
+        for (int dy = 0; dy < 2; ++dy) {
+          ve[dz][dy] = ne[dz][dy];
+          vo[dz][dy] = no[dz][dy];
+        }
+    }
 #pragma unroll
     for (int j = 0; j < 3; ++j)
 #pragma unroll
