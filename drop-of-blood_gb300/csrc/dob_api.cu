@@ -210,8 +210,10 @@ static void enqueue_step_body(dob_ctx* ctx, DevState& s, cudaStream_t st, float*
   // the wave substep comes first and the advection reads its result
   // (BloodDropEngine.ts:1886-1912)
   if (s.flags & DOB_PHYS_WAVE) launch_wave_step(s, st);
+  bool centre_fused = false;  // reference mode: the projection has formed the centre velocity
   for (int k = 0; k < n; ++k) {
     const int stage = kStepOrder[k];
+    if (centre_fused && stage == DOB_STAGE_MAC_TO_CENTER) continue;
     if (stage == DOB_STAGE_CURL && !(s.ref && (s.flags & DOB_PHYS_VORT_CONF))) continue;
     // closed box: the centre after advection has no reader, and the centre
     // after the projection comes out of the fused projection kernel
@@ -226,6 +228,11 @@ static void enqueue_step_body(dob_ctx* ctx, DevState& s, cudaStream_t st, float*
       launch_project_center_box(s, st, ctx->cfg.dt / ctx->cfg.dx, stats_div ? s.redu + REDU_MAXDIV : nullptr,
                                 s.redu + REDU_SPEED);
       swap_vel(s);
+    } else if (s.ref && stage == DOB_STAGE_PROJECT) {
+      // the projection and the centre velocity after it in one pass
+      launch_project_center_ref(s, st);
+      swap_vel(s);
+      centre_fused = true;
     } else if (!s.ref && stage == DOB_STAGE_MAC_RHS) {
       // with statistics the mean removal also forms ||rhs||^2
       if (stats_div) cudaMemsetAsync(s.red + RED_RHS_NORM2, 0, sizeof(double), st);

@@ -302,6 +302,10 @@ void launch_mac_rhs_box(const DevState& s, cudaStream_t st, double* sumsq = null
 void launch_project_center_box(const DevState& s, cudaStream_t st, float scale = 0.0f,
                                unsigned int* maxbits = nullptr, unsigned int* speedbits = nullptr);
 void launch_divergence(const DevState& s, float* out, float scale, unsigned int* maxbits, cudaStream_t st);
+// reference mode: the projection of (u, v, w) into (u2, v2, w2) and the
+// centre velocity of the projected faces (the MAC_TO_CENTER after it), one
+// pass (the caller swaps the buffers)
+void launch_project_center_ref(const DevState& s, cudaStream_t st);
 // bracket: also write the minimum and maximum of the predictor's 8 dye taps
 // (closed box) for launch_dye_resolve_lim.  sparse (inside a step, where the
 // centre velocity is bounded: by the projection's clamp in reference mode,

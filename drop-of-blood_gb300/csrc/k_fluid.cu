@@ -244,6 +244,25 @@ __global__ void __launch_bounds__(256, 5) k_advect_mac(Grid g, const StepParams*
 }
 
 // ---- FLUID_MAC_TO_CENTER (fluid.ts:917-962) -----------------------------------------------
+// Reference mode: a downward centre velocity in the top two layers is
+// damped near the surface except inside an active drop's neck.
+__device__ __forceinline__ float surface_stagnation(const Grid& g, const StepParams& P, int flags, int x, int y, int z,
+                                                    float cy) {
+  if (!((flags & DOB_PHYS_SURFACE) && y >= g.ny - 2 && cy < 0.0f)) return cy;
+  const Recip3 dims = grid_recip(g);
+  const dob_v3 pCell = to_world(P, (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / dims);
+  float activeNeck = 0.0f;
+  for (int d = 0; d < kMaxDrops; ++d) {
+    if (drop(P, d, 7) > 0.0f && drop(P, d, 6) > 0.008f) {
+      const float rActive = dob_clampf(drop(P, d, 3) * 1.15f + 0.032f, 0.046f, 0.092f);
+      const float rDist = length2f(pCell.x - drop(P, d, 0), pCell.z - drop(P, d, 2));
+      const float drainGate = dob_smoothstep(0.008f, 0.065f, drop(P, d, 6));
+      activeNeck = dob_maxf(activeNeck, (1.0f - dob_smoothstep(rActive * 0.78f, rActive * 1.20f, rDist)) * drainGate);
+    }
+  }
+  const float stagGate = dob_mix(0.45f, 1.0f, dob_smoothstep(0.002f, 0.018f, dob_maxf(0.0f, P.U[40] - pCell.y)));
+  return cy * dob_mix(stagGate, 1.0f, activeNeck);
+}
 template <class VS>
 __global__ void __launch_bounds__(256) k_mac_to_center(Grid g, const StepParams* __restrict__ Pp, int ref, int flags,
                                                        const VS* __restrict__ u, const VS* __restrict__ v,
@@ -258,22 +277,7 @@ __global__ void __launch_bounds__(256) k_mac_to_center(Grid g, const StepParams*
   const float wB = z == 0 ? 0.0f : ldf(w + i - (size_t)g.nx * g.ny);
   const float cx = 0.5f * (uL + uR), cz = 0.5f * (wB + wF);
   float cy = 0.5f * (vD + vU);
-  if (ref && (flags & DOB_PHYS_SURFACE) && y >= g.ny - 2 && cy < 0.0f) {
-    const StepParams& P = *Pp;
-    const Recip3 dims = grid_recip(g);
-    const dob_v3 pCell = to_world(P, (v3((float)x, (float)y, (float)z) + v3(0.5f, 0.5f, 0.5f)) / dims);
-    float activeNeck = 0.0f;
-    for (int d = 0; d < kMaxDrops; ++d) {
-      if (drop(P, d, 7) > 0.0f && drop(P, d, 6) > 0.008f) {
-        const float rActive = dob_clampf(drop(P, d, 3) * 1.15f + 0.032f, 0.046f, 0.092f);
-        const float rDist = length2f(pCell.x - drop(P, d, 0), pCell.z - drop(P, d, 2));
-        const float drainGate = dob_smoothstep(0.008f, 0.065f, drop(P, d, 6));
-        activeNeck = dob_maxf(activeNeck, (1.0f - dob_smoothstep(rActive * 0.78f, rActive * 1.20f, rDist)) * drainGate);
-      }
-    }
-    const float stagGate = dob_mix(0.45f, 1.0f, dob_smoothstep(0.002f, 0.018f, dob_maxf(0.0f, P.U[40] - pCell.y)));
-    cy = cy * dob_mix(stagGate, 1.0f, activeNeck);
-  }
+  if (ref) cy = surface_stagnation(g, *Pp, flags, x, y, z, cy);
   st4(cen + i, make_float4(cx, cy, cz, 0.0f));
 }
 
@@ -462,6 +466,50 @@ __global__ void __launch_bounds__(256) k_project(Grid g, const StepParams* __res
     mx = dob_clampf(mx, -2.0f, 2.0f); my = dob_clampf(my, -2.0f, 2.0f); mz = dob_clampf(mz, -2.0f, 2.0f);
   }
   stf(u + i, mx); stf(v + i, my); stf(w + i, mz);
+}
+
+// FLUID_MAC_PROJECT and the MAC_TO_CENTER that follows it (reference mode)
+// in one pass, out of place: the projected faces go to uo/vo/wo (the caller
+// swaps the buffers); each cell forms its lower faces' projected values with
+// k_project's arithmetic for the cell below, then the centre velocity from
+// the faces as stored (binary16 rounds them) with k_mac_to_center's.
+template <class VS> __device__ __forceinline__ float as_stored_vs(float v);
+template <> __device__ __forceinline__ float as_stored_vs<float>(float v) { return v; }
+template <> __device__ __forceinline__ float as_stored_vs<__half>(float v) { return __half2float(__float2half_rn(v)); }
+template <class VS>
+__global__ void __launch_bounds__(256) k_project_center_ref(Grid g, const StepParams* __restrict__ Pp, int flags,
+                                                            const VS* __restrict__ u, const VS* __restrict__ v,
+                                                            const VS* __restrict__ w, const float* __restrict__ p,
+                                                            const float* __restrict__ plo,
+                                                            const float4* __restrict__ wave, VS* __restrict__ uo,
+                                                            VS* __restrict__ vo, VS* __restrict__ wo,
+                                                            typename Vec4Of<VS>::type* __restrict__ cen) {
+  CELL_INDEX
+  const size_t ic = rb_index(g, x, y, z);
+  const float pC = __ldg(p + ic);
+  const float lC = plo ? __ldg(plo + ic) : 0.0f;
+  // the face between a lower cell (pl, ll) and an upper one (ph, lh)
+  auto dpf = [&](size_t jl, size_t jh) {
+    return plo ? (__ldg(p + jh) - __ldg(p + jl)) + (__ldg(plo + jh) - __ldg(plo + jl)) : (__ldg(p + jh) - __ldg(p + jl));
+  };
+  float mx = ldf(u + i), my = ldf(v + i), mz = ldf(w + i);
+  if (x < g.nx - 1) mx = mx - dpf(ic, rb_index(g, x + 1, y, z)); else mx = 0.0f;
+  if (y < g.ny - 1) my = my - dpf(ic, rb_index(g, x, y + 1, z));
+  else my = my - (top_pressure(g, *Pp, wave, x, z) - pC);
+  if (z < g.nz - 1) mz = mz - dpf(ic, rb_index(g, x, y, z + 1)); else mz = 0.0f;
+  mx = dob_clampf(mx, -2.0f, 2.0f); my = dob_clampf(my, -2.0f, 2.0f); mz = dob_clampf(mz, -2.0f, 2.0f);
+  stf(uo + i, mx); stf(vo + i, my); stf(wo + i, mz);
+  float uL = 0.0f, vD = 0.0f, wB = 0.0f;
+  if (x > 0) uL = as_stored_vs<VS>(dob_clampf(ldf(u + i - 1) - dpf(rb_index(g, x - 1, y, z), ic), -2.0f, 2.0f));
+  if (y > 0) vD = as_stored_vs<VS>(dob_clampf(ldf(v + i - g.nx) - dpf(rb_index(g, x, y - 1, z), ic), -2.0f, 2.0f));
+  if (z > 0)
+    wB = as_stored_vs<VS>(dob_clampf(ldf(w + i - (size_t)g.nx * g.ny) - dpf(rb_index(g, x, y, z - 1), ic), -2.0f, 2.0f));
+  const float uR = x >= g.nx - 1 ? 0.0f : as_stored_vs<VS>(mx);
+  const float vU = as_stored_vs<VS>(my);
+  const float wF = z >= g.nz - 1 ? 0.0f : as_stored_vs<VS>(mz);
+  const float cx = 0.5f * (uL + uR), cz = 0.5f * (wB + wF);
+  const float cy = surface_stagnation(g, *Pp, flags, x, y, z, 0.5f * (vD + vU));
+  st4(cen + i, make_float4(cx, cy, cz, 0.0f));
 }
 
 // ---- divergence field and its max (statistics) -----------------------------------------
@@ -962,6 +1010,14 @@ void launch_project(const DevState& s, cudaStream_t st) {
   DOB_VEL_DISPATCH(s.prec, {
     k_project<VS><<<cell_grid(s.g), cell_block(), 0, st>>>(s.g, s.params, s.ref, (VS*)s.u, (VS*)s.v, (VS*)s.w, s.p,
                                                            s.plo, s.wave);
+  });
+}
+
+void launch_project_center_ref(const DevState& s, cudaStream_t st) {
+  DOB_VEL_DISPATCH(s.prec, {
+    k_project_center_ref<VS><<<cell_grid(s.g), cell_block(), 0, st>>>(
+        s.g, s.params, s.flags, (const VS*)s.u, (const VS*)s.v, (const VS*)s.w, s.p, s.plo, s.wave, (VS*)s.u2,
+        (VS*)s.v2, (VS*)s.w2, (typename Vec4Of<VS>::type*)s.cen);
   });
 }
 
