@@ -529,9 +529,11 @@ dob_status dob_create(const dob_config* cfg, dob_ctx** out) {
     A((void**)&s.brick_raw, N / 64 * sizeof(float));
     A((void**)&s.bricks, N / 64 * sizeof(float));
   }
-  A((void**)&s.red, RED_COUNT * sizeof(double));
+  // the FP64 and u32 reduction slots in one block, so the statistics a
+  // pipelined step reads back are one copy
+  A((void**)&s.red, kStatsBytes);
+  if (st == DOB_OK) s.redu = reinterpret_cast<unsigned int*>(s.red + RED_COUNT);
   A((void**)&s.part, PART_SLOTS * kSumBlocks * sizeof(double));
-  A((void**)&s.redu, REDU_COUNT * sizeof(unsigned int));
   s.nlev = cfg->mg_levels;
   for (int l = 0; l < s.nlev; ++l) {
     MgLevel& L = s.lv[l];
@@ -617,8 +619,7 @@ void dob_destroy(dob_ctx* ctx) {
   for (int k = 0; k <= DOB_STAGE_COUNT; ++k)
     if (ctx->stage_ev[k]) cudaEventDestroy(ctx->stage_ev[k]);
   for (auto& a : ctx->async_slots) {
-    if (a.red) cudaFreeHost(a.red);
-    if (a.redu) cudaFreeHost(a.redu);
+    if (a.red) cudaFreeHost(a.red);  // a.redu lies in the same block
     if (a.done) cudaEventDestroy(a.done);
   }
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -927,16 +928,15 @@ dob_status dob_step_async(dob_ctx* ctx, int slot) {
   dob_ctx::AsyncSlot& a = ctx->async_slots[slot];
   if (a.pending) return fail(ctx, DOB_ESTATE, "dob_step_async", "result slot still pending");
   if (!a.red) {
-    CK(cudaMallocHost((void**)&a.red, RED_COUNT * sizeof(double)));
-    CK(cudaMallocHost((void**)&a.redu, REDU_COUNT * sizeof(unsigned int)));
+    CK(cudaMallocHost((void**)&a.red, kStatsBytes));
+    a.redu = reinterpret_cast<unsigned int*>(a.red + RED_COUNT);
     CK(cudaEventCreateWithFlags(&a.done, cudaEventDisableTiming));
   }
   dob_status st = one_step(ctx, DOB_STEP_STATS, nullptr);
   if (st != DOB_OK) return st;
   DevState& s = ctx->s;
   if (ctx->stats_mask & DOB_STATS_PARCELS) launch_count_alive(s, s.redu + REDU_ALIVE, ctx->stream);
-  CK(cudaMemcpyAsync(a.red, s.red, RED_COUNT * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-  CK(cudaMemcpyAsync(a.redu, s.redu, REDU_COUNT * sizeof(unsigned int), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(a.red, s.red, kStatsBytes, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaEventRecord(a.done, ctx->stream));
   a.cycles = ctx->last_cycles;
   a.pending = true;

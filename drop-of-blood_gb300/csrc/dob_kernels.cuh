@@ -131,6 +131,8 @@ enum {
   REDU_DEFECT_MAX = 8,    // max |r| (float bits): [0] the round's residual, [1] the cycle's
   REDU_COUNT = 8 + 32
 };
+// the reduction slots as one block: RED_COUNT doubles, then REDU_COUNT u32
+constexpr size_t kStatsBytes = RED_COUNT * sizeof(double) + REDU_COUNT * sizeof(unsigned int);
 // the mixed solve: at most this many rounds (error-free residuals) per step,
 // and V-cycles per round
 constexpr int kMixedMaxRounds = 4;
