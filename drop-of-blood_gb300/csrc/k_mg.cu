@@ -278,9 +278,13 @@ __device__ __forceinline__ Row4 ld_row4(const T* a, uint32_t half, uint32_t r, u
 // The body of k_residual_restrict2 for coarse cells X = 2q, 2q+1 of coarse
 // row (Y, Z); rr / ra (optional) accumulate r^2 and max |r| of the fine cells.
 template <class T, class TC>
+// ered (optional): also the coarse level's first red half-sweep from a zero
+// guess at the pair's red cell (k_rbgs_v4's ZOTH arithmetic: the neighbours
+// are zeros, so the value is -h2c b / diag of the right-hand side as stored).
 __device__ __forceinline__ void restrict_pair(Grid f, Grid c, float inv_h2, int ref, const T* __restrict__ a,
                                               const T* __restrict__ b, TC* __restrict__ bc, int q, int Y, int Z,
-                                              float* rr, float* ra) {
+                                              float* rr, float* ra, TC* __restrict__ ered = nullptr,
+                                              float h2c = 0.0f) {
   const uint32_t hx = (uint32_t)f.nx >> 1, half = (uint32_t)(f.n() >> 1), sz = (uint32_t)f.ny * hx;
   const uint32_t w = 2u * (uint32_t)q;
   const int y0 = 2 * Y, z0 = 2 * Z;
@@ -354,6 +358,17 @@ __device__ __forceinline__ void restrict_pair(Grid f, Grid c, float inv_h2, int 
   const int pc = (Y + Z) & 1;  // colour of coarse X = 2q
   stf(bc + (pc ? halfc : 0u) + rc, sum[0] * 0.125f);
   stf(bc + (pc ? 0u : halfc) + rc, sum[1] * 0.125f);
+  if (ered) {
+    const int X = pc ? 2 * q + 1 : 2 * q;  // the red cell of the pair
+    const float bv = as_stored<TC>((pc ? sum[1] : sum[0]) * 0.125f);
+    const float wxm = X > 0 ? 1.0f : 0.0f, wxp = X < c.nx - 1 ? 1.0f : 0.0f;
+    const float wym = Y > 0 ? 1.0f : 0.0f, wyp = Y < c.ny - 1 ? 1.0f : 0.0f;
+    const float wzm = Z > 0 ? 1.0f : 0.0f, wzp = Z < c.nz - 1 ? 1.0f : 0.0f;
+    const float dyz = (wym + (ref ? 1.0f : wyp)) + (wzm + wzp);
+    const float diag = dyz + (wxm + wxp);
+    const float t = 0.0f - h2c * bv;
+    stf(ered + rc, diag == 6.0f ? t * (1.0f / 6.0f) : t / diag);
+  }
 }
 
 // norm2 / maxbits (RED, the mixed solve's convergence test): also ||r||^2
@@ -362,7 +377,8 @@ template <class T, class TC, bool RED>
 __global__ void __launch_bounds__(256, 4) k_residual_restrict2(Grid f, Grid c, float inv_h2, int ref,
                                                             const T* __restrict__ a, const T* __restrict__ b,
                                                             TC* __restrict__ bc, const unsigned int* __restrict__ skip,
-                                                            double* __restrict__ norm2, unsigned int* __restrict__ maxbits) {
+                                                            double* __restrict__ norm2, unsigned int* __restrict__ maxbits,
+                                                            TC* __restrict__ ered, float h2c) {
   pdl_wait();
   pdl_trigger();
   if (skip_now(skip)) return;
@@ -377,7 +393,7 @@ __global__ void __launch_bounds__(256, 4) k_residual_restrict2(Grid f, Grid c, f
     return;
   }
   if (2 * q >= c.nx || Y >= c.ny) return;
-  restrict_pair<T, TC>(f, c, inv_h2, ref, a, b, bc, q, Y, Z, nullptr, nullptr);
+  restrict_pair<T, TC>(f, c, inv_h2, ref, a, b, bc, q, Y, Z, nullptr, nullptr, ered, h2c);
 }
 
 // MG_PROLONG_ADD, two coarse cells per thread (and ZC coarse planes per
@@ -1047,16 +1063,20 @@ static inline dim3 pair_grid(const Grid& c, const dim3& b) {
 // norm2 / maxbits: also reduce ||r||^2 and max |r| of level l's residual
 // (the mixed solve's convergence test)
 template <class T, class TC = T>
+// ered: also the first red half-sweep from zero of level l + 1 (its
+// smoothing then starts with the black half-sweep)
 static void restrict_level(const DevState& s, int l, const T* x, const T* b, TC* bc, const unsigned int* skip,
-                           cudaStream_t st, double* norm2 = nullptr, unsigned int* maxbits = nullptr) {
+                           cudaStream_t st, double* norm2 = nullptr, unsigned int* maxbits = nullptr,
+                           TC* ered = nullptr) {
   const Grid f = s.lv[l].d, c = s.lv[l + 1].d;  // nx % 4 == 0 on every transfer level
   const dim3 bp = pair_block(c);
+  const float h2c = s.lv[l + 1].h2;
   if (norm2)
     launch_pdl(k_residual_restrict2<T, TC, true>, pair_grid(c, bp), bp, 0, st, f, c, 1.0f / s.lv[l].h2, s.ref, x, b,
-               bc, skip, norm2, maxbits);
+               bc, skip, norm2, maxbits, (TC*)nullptr, h2c);
   else
     launch_pdl(k_residual_restrict2<T, TC, false>, pair_grid(c, bp), bp, 0, st, f, c, 1.0f / s.lv[l].h2, s.ref, x, b,
-               bc, skip, norm2, maxbits);
+               bc, skip, norm2, maxbits, ered, h2c);
 }
 static inline dim3 quad_grid(const Grid& d, const dim3& b) {
   const int q = d.nx / 8;
@@ -1139,9 +1159,11 @@ static void half_sweep(const DevState& s, int l, int c, bool zoth, T* a, const T
 // zero (the first red half-sweep then reads no neighbours, and the black
 // half-sweep never reads its own old values, so nothing is filled unless
 // there are no sweeps); ec: coarse correction to add first.
+// red_done: the first red half-sweep from zero was formed by the restriction
+// into this level (restrict_level's ered)
 template <class T, class TC = T>
 static void smooth(const DevState& s, int l, T* a, const T* b, int sweeps, bool zero_first, const TC* ec,
-                   const unsigned int* skip, cudaStream_t st) {
+                   const unsigned int* skip, cudaStream_t st, bool red_done = false) {
   const MgLevel& L = s.lv[l];
   if (zero_first && sweeps == 0) launch_pdl(k_fill_zero<T>, dim3(s.num_sms * 2), dim3(256), 0, st, a, L.d.n(), skip);
   if (ec) {
@@ -1163,7 +1185,10 @@ static void smooth(const DevState& s, int l, T* a, const T* b, int sweeps, bool 
     }
   }
   for (int k = 0; k < sweeps; ++k)
-    for (int c = 0; c < 2; ++c) half_sweep<T>(s, l, c, zero_first && k == 0 && c == 0, a, b, skip, st);
+    for (int c = 0; c < 2; ++c) {
+      if (red_done && k == 0 && c == 0) continue;
+      half_sweep<T>(s, l, c, zero_first && k == 0 && c == 0, a, b, skip, st);
+    }
 }
 
 template <class T, int CS>
@@ -1204,10 +1229,15 @@ static void vcycle(const DevState& s, T* x0, const T* b0, T* const* E, T* const*
     return;
   }
   smooth<T, T>(s, 0, x0, b0, s.pre0, zero0, nullptr, skip, st);
-  restrict_level<T>(s, 0, x0, b0, B[1], skip, st);
+  // each level in between starts its smoothing from zero: its first red
+  // half-sweep reads only its right-hand side, so the restriction forming
+  // that right-hand side also forms it (one launch fewer per level)
+  const bool fuse = s.pre > 0;
+  restrict_level<T>(s, 0, x0, b0, B[1], skip, st, nullptr, nullptr, fuse && L > 2 ? E[1] : nullptr);
   for (int l = 1; l < L - 1; ++l) {
-    smooth<T, T>(s, l, E[l], B[l], s.pre, true, nullptr, skip, st);
-    restrict_level<T>(s, l, E[l], B[l], B[l + 1], skip, st);
+    smooth<T, T>(s, l, E[l], B[l], s.pre, true, nullptr, skip, st, fuse);
+    restrict_level<T>(s, l, E[l], B[l], B[l + 1], skip, st, nullptr, nullptr,
+                      fuse && l + 1 < L - 1 ? E[l + 1] : nullptr);
   }
   coarse_solve<T>(s, L - 1, E[L - 1], B[L - 1], skip, st);
   for (int l = L - 2; l >= 1; --l) smooth<T, T>(s, l, E[l], B[l], s.post, false, E[l + 1], skip, st);
