@@ -489,8 +489,10 @@ dob_status dob_create(const dob_config* cfg, dob_ctx** out) {
   CK(cudaDeviceGetAttribute(&s.num_sms, cudaDevAttrMultiProcessorCount, ctx->device));
   CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
   CK(cudaStreamCreateWithFlags(&ctx->aux_stream, cudaStreamNonBlocking));
+  CK(cudaStreamCreateWithFlags(&ctx->aux_stream2, cudaStreamNonBlocking));
   CK(mg_prepare());
   s.aux = ctx->aux_stream;
+  s.aux2 = ctx->aux_stream2;
   s.g = make_grid((int)cfg->nx, (int)cfg->ny, (int)cfg->nz);
   s.gc = make_grid((int)(cfg->nx * cfg->dye_refine), (int)(cfg->ny * cfg->dye_refine), (int)(cfg->nz * cfg->dye_refine));
   s.prec = cfg->precision_mode;
@@ -624,6 +626,7 @@ void dob_destroy(dob_ctx* ctx) {
   }
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   if (ctx->aux_stream) cudaStreamDestroy(ctx->aux_stream);
+  if (ctx->aux_stream2) cudaStreamDestroy(ctx->aux_stream2);
   delete ctx;
 }
 

@@ -38,7 +38,8 @@ struct dob_ctx {
   dob::DevState s;
   int device = 0;
   cudaStream_t stream = nullptr;
-  cudaStream_t aux_stream = nullptr;  // body capture of conditional graph nodes
+  cudaStream_t aux_stream = nullptr;   // body capture of conditional graph nodes
+  cudaStream_t aux_stream2 = nullptr;  // the same, one nesting level up
   std::string err;
   float U[128];
   dob::StepParams* host_params = nullptr;  // pinned ring

@@ -85,9 +85,10 @@ struct DevState {
   int max_outer;
   double rel_tol;   // stop when ||b - A p|| <= rel_tol ||b|| (0: off)
   float div_tol_r;  // stop when max |b - A p| <= div_tol_r (0: off)
-  // second stream of the context: captures the body of the defect loop's
-  // conditional while-node when the step is captured into a graph
-  cudaStream_t aux;
+  // second and third streams of the context: capture the bodies of the
+  // defect loop's conditional nodes (a round's while-node of V-cycles, the
+  // if-node of a round after the first) when the step is captured
+  cudaStream_t aux, aux2;
 };
 constexpr int kMixedBF16Level = 2;
 

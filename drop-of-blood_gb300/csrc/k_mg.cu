@@ -908,21 +908,27 @@ __device__ __forceinline__ bool mixed_converged(unsigned int* maxbits, double* r
 // an earlier round was): `done` and `inner_done` make every later kernel of
 // the solve return at once (the round's first cycle test then leaves its
 // loop off).  Otherwise the round counts, its cycle counter starts at the
-// `untested` cycles that open it, which count as completed V-cycles.
+// `untested` cycles that open it, which count as completed V-cycles.  With
+// `use_cond` the test also sets `cond` (the if-node of a captured round) to
+// whether the round runs.
 __global__ void k_mixed_round_check(unsigned int* __restrict__ maxbits, double* __restrict__ rnorm2,
                                     const double* __restrict__ bnorm2, float div_tol_r, double rel_tol,
                                     unsigned int* __restrict__ done, unsigned int* __restrict__ inner_done,
                                     unsigned int* __restrict__ rounds, unsigned int* __restrict__ inner_iters,
-                                    unsigned int* __restrict__ vcycles, int untested) {
+                                    unsigned int* __restrict__ vcycles, int untested,
+                                    cudaGraphConditionalHandle cond, int use_cond) {
   if (*done) {
     *inner_done = 1u;
+    if (use_cond) cudaGraphSetConditional(cond, 0u);
     return;
   }
   if (mixed_converged(maxbits, rnorm2, bnorm2, div_tol_r, rel_tol)) {
     *done = 1u;
     *inner_done = 1u;
+    if (use_cond) cudaGraphSetConditional(cond, 0u);
     return;
   }
+  if (use_cond) cudaGraphSetConditional(cond, 1u);
   *rounds = *rounds + 1u;
   *inner_done = 0u;
   *inner_iters = (unsigned int)untested;
@@ -1316,9 +1322,11 @@ void launch_residual_norm(const DevState& s, double* out, cudaStream_t st) {
 // loop is a conditional while-node rotated so that each iteration ends at a
 // test (body: the rest of a cycle, then the next cycle's pre-smoothing,
 // restriction and test), so its kernels read no skip flag; the round's
-// first test, before the loop, switches it on.  Outside a capture,
-// kMixedMaxCycles iterations per round are enqueued and the kernels after
-// convergence return at once.
+// first test, before the loop, switches it on.  Each round after the first
+// is captured as an if-node that the round's residual test switches on, so
+// rounds that are not needed (usually all after the first) launch nothing.
+// Outside a capture, kMixedMaxCycles iterations per round are enqueued and
+// the kernels after convergence return at once.
 static void mixed_solve(const DevState& s, cudaStream_t st) {
   const size_t n = s.g.n();
   MixLv M[kMaxLevels];
@@ -1359,56 +1367,120 @@ static void mixed_solve(const DevState& s, cudaStream_t st) {
     for (int l = L - 2; l >= 1; --l) mix_smooth(s, l, M, s.post, false, true, skip, q);
     mix_smooth(s, 0, M, s.post0, false, true, skip, q);
   };
-  for (int r = 0; r < rounds; ++r) {
-    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-    cudaGraph_t graph = nullptr;
-    if (s.aux && cudaStreamGetCaptureInfo(st, &cs, nullptr, &graph, nullptr, nullptr, nullptr) != cudaSuccess) {
-      cudaGetLastError();
-      cs = cudaStreamCaptureStatusNone;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaGraph_t top = nullptr;
+  if (s.aux && s.aux2 && cudaStreamGetCaptureInfo(st, &cs, nullptr, &top, nullptr, nullptr, nullptr) != cudaSuccess) {
+    cudaGetLastError();
+    cs = cudaStreamCaptureStatusNone;
+  }
+  const bool captured = cs == cudaStreamCaptureStatusActive;
+  auto new_handle = [&]() {
+    cudaGraphConditionalHandle h = 0;
+    cudaGraphConditionalHandleCreate(&h, top, 0u, cudaGraphCondAssignDefault);
+    return h;
+  };
+  // a conditional node after the work captured so far on q; its body is
+  // captured on `body` between open_cond and close_cond
+  auto open_cond = [&](cudaStream_t q, cudaGraphConditionalHandle h, cudaGraphConditionalNodeType type,
+                       cudaStream_t body) {
+    cudaStreamCaptureStatus qs;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t ndeps = 0;
+    cudaStreamGetCaptureInfo(q, &qs, nullptr, &g, &deps, nullptr, &ndeps);
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = type;
+    np.conditional.size = 1;
+    cudaGraphNode_t node = nullptr;
+    cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &np);
+    cudaStreamBeginCaptureToGraph(body, np.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                  cudaStreamCaptureModeRelaxed);
+    return node;
+  };
+  auto close_cond = [&](cudaStream_t q, cudaGraphNode_t node, cudaStream_t body) {
+    cudaGraph_t g = nullptr;
+    cudaStreamEndCapture(body, &g);
+    cudaStreamUpdateCaptureDependencies(q, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+  };
+  // a round's cycles after its first test: the while-node that the test
+  // switched on, or kMixedMaxCycles flag-guarded iterations
+  auto cycles = [&](cudaStream_t q, cudaGraphConditionalHandle cond) {
+    if (captured) {
+      cudaGraphNode_t node = open_cond(q, cond, cudaGraphCondTypeWhile, s.aux);
+      tail(s.aux, nullptr);
+      head(s.aux, nullptr, cond, 1, 1);
+      close_cond(q, node, s.aux);
+    } else {
+      for (int it = 0; it < kMixedMaxCycles; ++it) {
+        tail(q, inner_done);
+        head(q, inner_done, 0, 0, 1);
+      }
     }
-    const bool captured = cs == cudaStreamCaptureStatusActive;
-    cudaGraphConditionalHandle cond = 0;
-    // the loop runs only if the round's first test switches it on
-    if (captured) cudaGraphConditionalHandleCreate(&cond, graph, 0u, cudaGraphCondAssignDefault);
-    const int plain = r == 0 ? untested : 0;
+  };
+  // round 0: its first `untested` cycles (the first from e = 0) read no
+  // flag, so a step whose pressure already meets the targets still runs them
+  {
+    const cudaGraphConditionalHandle cond = captured ? new_handle() : 0;
     defect(s, s.r0, rn2, rmax, done, st);
     k_mixed_round_check<<<1, 1, 0, st>>>(rmax, rn2, bn2, s.div_tol_r, s.rel_tol, done, inner_done,
                                          s.redu + REDU_ITERS, s.redu + REDU_INNER_ITERS, s.redu + REDU_VCYCLES,
-                                         plain);
-    // the first round's untested cycles (the first from e = 0) read no flag:
-    // a step whose pressure already meets the targets still runs them
-    for (int c = 0; c < plain; ++c) {
+                                         untested, 0, 0);
+    for (int c = 0; c < untested; ++c) {
       mix_smooth(s, 0, M, s.pre0, c == 0, false, nullptr, st);
       restrict_level<float, float>(s, 0, M[0].ef, M[0].bf, M[1].bf, nullptr, st);
       tail(st, nullptr);
     }
-    if (plain == 0)
+    if (untested == 0)
       launch_pdl(k_fill_zero<float>, dim3(s.num_sms * 2), dim3(256), 0, st, s.e0, n, (const unsigned int*)done);
     head(st, done, cond, captured ? 1 : 0, 0);
-    if (captured) {
-      const cudaGraphNode_t* deps = nullptr;
-      size_t ndeps = 0;
-      cudaStreamGetCaptureInfo(st, &cs, nullptr, &graph, &deps, nullptr, &ndeps);
-      cudaGraphNodeParams np = {};
-      np.type = cudaGraphNodeTypeConditional;
-      np.conditional.handle = cond;
-      np.conditional.type = cudaGraphCondTypeWhile;
-      np.conditional.size = 1;
-      cudaGraphNode_t node;
-      cudaGraphAddNode(&node, graph, deps, nullptr, ndeps, &np);
-      cudaGraph_t body = np.conditional.phGraph_out[0];
-      cudaStreamBeginCaptureToGraph(s.aux, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
-      tail(s.aux, nullptr);
-      head(s.aux, nullptr, cond, 1, 1);
-      cudaStreamEndCapture(s.aux, &body);
-      cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
-    } else {
-      for (int it = 0; it < kMixedMaxCycles; ++it) {
-        tail(st, inner_done);
-        head(st, inner_done, 0, 0, 1);
+    cycles(st, cond);
+    k_add_df<<<s.num_sms * 4, 256, 0, st>>>(s.p, s.plo, s.e0, n, done);
+  }
+  // the later rounds.  Captured: round r's test (after round r - 1) sets the
+  // handle of an if-node that holds the whole round, so a round that is not
+  // needed launches nothing; inside it `done` is clear, and its kernels read
+  // no flag.  Otherwise every round is enqueued and returns at once once
+  // `done` is set.
+  if (rounds > 1) {
+    cudaGraphConditionalHandle h = captured ? new_handle() : 0;
+    defect(s, s.r0, rn2, rmax, done, st);
+    k_mixed_round_check<<<1, 1, 0, st>>>(rmax, rn2, bn2, s.div_tol_r, s.rel_tol, done, inner_done,
+                                         s.redu + REDU_ITERS, s.redu + REDU_INNER_ITERS, s.redu + REDU_VCYCLES, 0,
+                                         h, captured ? 1 : 0);
+    for (int r = 1; r < rounds; ++r) {
+      const bool last = r + 1 == rounds;
+      if (captured) {
+        const cudaGraphConditionalHandle cond = new_handle();
+        const cudaGraphConditionalHandle next = last ? 0 : new_handle();
+        const cudaGraphNode_t node = open_cond(st, h, cudaGraphCondTypeIf, s.aux2);
+        launch_pdl(k_fill_zero<float>, dim3(s.num_sms * 2), dim3(256), 0, s.aux2, s.e0, n,
+                   (const unsigned int*)nullptr);
+        head(s.aux2, nullptr, cond, 1, 0);
+        cycles(s.aux2, cond);
+        k_add_df<<<s.num_sms * 4, 256, 0, s.aux2>>>(s.p, s.plo, s.e0, n, nullptr);
+        if (!last) {
+          defect(s, s.r0, rn2, rmax, nullptr, s.aux2);
+          k_mixed_round_check<<<1, 1, 0, s.aux2>>>(rmax, rn2, bn2, s.div_tol_r, s.rel_tol, done, inner_done,
+                                                   s.redu + REDU_ITERS, s.redu + REDU_INNER_ITERS,
+                                                   s.redu + REDU_VCYCLES, 0, next, 1);
+        }
+        close_cond(st, node, s.aux2);
+        h = next;
+      } else {
+        launch_pdl(k_fill_zero<float>, dim3(s.num_sms * 2), dim3(256), 0, st, s.e0, n, (const unsigned int*)done);
+        head(st, done, 0, 0, 0);
+        cycles(st, 0);
+        k_add_df<<<s.num_sms * 4, 256, 0, st>>>(s.p, s.plo, s.e0, n, done);
+        if (!last) {
+          defect(s, s.r0, rn2, rmax, done, st);
+          k_mixed_round_check<<<1, 1, 0, st>>>(rmax, rn2, bn2, s.div_tol_r, s.rel_tol, done, inner_done,
+                                               s.redu + REDU_ITERS, s.redu + REDU_INNER_ITERS,
+                                               s.redu + REDU_VCYCLES, 0, 0, 0);
+        }
       }
     }
-    k_add_df<<<s.num_sms * 4, 256, 0, st>>>(s.p, s.plo, s.e0, n, done);
   }
   if (!s.ref) {
     double* part = s.part + PART_P * kSumBlocks;

@@ -543,6 +543,40 @@ def test_graph_replay_equals_stage_launches(gpu_lib):
     assert bits_equal(a.get_parcels(), b.get_parcels())
 
 
+@pytest.mark.parametrize("rel_tol", [0.0, 1e-8])
+def test_mixed_graph_replay_equals_stage_launches(gpu_lib, rel_tol):
+    """The mixed solve captured into the step graph (a while-node of V-cycles
+    per round, an if-node for each round after the first) gives the bits and
+    the round / V-cycle counts of the same steps enqueued without a graph
+    (every round launched, returning at once after convergence): with the
+    divergence target alone (one round) and with the relative target 1e-8
+    (several rounds)."""
+    abi = _abi()
+    from dropfluid import DropFluid, scenes
+    sc = scenes.box48()
+    cfg = sc.config
+    cfg.precision_mode = abi.DOB_PREC_MIXED
+    cfg.mg_cycles = 1
+    cfg.mg_rel_tol = rel_tol
+    cfg.mg_div_tol = 1e-5
+    cfg.mg_max_outer = 4
+    a, b = DropFluid(cfg), DropFluid(cfg)
+    sc.release(a, 0)
+    sc.release(b, 0)
+    rounds = []
+    for _ in range(4):
+        sa = a.step(1, stats=True, graph=True)
+        sb = b.step(1, stats=True, graph=False)
+        assert (sa["outer_iters"], sa["vcycles"]) == (sb["outer_iters"], sb["vcycles"])
+        rounds.append(sa["outer_iters"])
+    if rel_tol > 0:
+        assert max(rounds) >= 2, rounds
+    for f in (abi.FIELD_VEL_U, abi.FIELD_VEL_V, abi.FIELD_PRESSURE, abi.FIELD_CONC):
+        assert bits_equal(a.get_field(f), b.get_field(f)), f
+    a.close()
+    b.close()
+
+
 def test_fused_projection_equals_separate_stages(gpu_lib):
     """The closed-box step leaves out the centre pass after advection (no
     reader) and runs projection + centre as one out-of-place kernel; a step
