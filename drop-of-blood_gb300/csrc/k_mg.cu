@@ -789,102 +789,109 @@ __global__ void __launch_bounds__(256) k_defect_df(Grid d, int ref, const float*
 // k_defect_df on the red-black split layout with the smoother's thread
 // shape: four consecutive same-colour cells of a row per thread (16-byte
 // loads), ZC planes per thread (with ZC > 1 the other colour's row vectors
-// serve three planes each), blockIdx.z = 2 * z-chunk + colour.  Absent neighbours enter
-// with weight 0 (an exact zero added to the double-float sum changes
-// nothing), so every cell's r has the bits of k_defect_df.  One FP64 add and
-// one max per block.  Rows with nx % 8 == 0.
+// serve three planes each), blockIdx.z = 2 * (group of `zs` z-chunks) +
+// colour.  Absent neighbours enter with weight 0 (an exact zero added to the
+// double-float sum changes nothing), so every cell's r has the bits of
+// k_defect_df.  One FP64 add and one max per block: a block walks `zs`
+// chunks so that the reductions' same-address atomics stay few (one per
+// plane and colour cost 12 of 57 us at 192x256x192; four planes per block:
+// 51 us, 78 registers; capped at 64 it spills and runs no faster).  Rows
+// with nx % 8 == 0.
 template <int ZC>
 __global__ void __launch_bounds__(256) k_defect_df4(Grid d, int ref, const float* __restrict__ p,
                                                     const float* __restrict__ plo, const float* __restrict__ b,
                                                     float* __restrict__ r_out, double* __restrict__ norm2,
                                                     unsigned int* __restrict__ maxbits,
-                                                    const unsigned int* __restrict__ skip) {
+                                                    const unsigned int* __restrict__ skip, int zs) {
   pdl_wait();
   pdl_trigger();
   if (skip_now(skip)) return;
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int color = blockIdx.z & 1;
-  const int z0 = (blockIdx.z >> 1) * ZC;
   const uint32_t hx = (uint32_t)d.nx >> 1;
   const uint32_t k0 = 4u * (uint32_t)q;
   float rr = 0.0f, ra = 0.0f;
-  if (k0 < hx && y < d.ny) {
-    const uint32_t half = (uint32_t)(d.n() >> 1);
-    const uint32_t sz = (uint32_t)d.ny * hx;
-    const uint32_t own = color ? half : 0u, oth = color ? 0u : half;
-    const uint32_t r0 = (uint32_t)z0 * sz + (uint32_t)y * hx + k0;
-    const bool has_ym = y > 0, has_yp = y < d.ny - 1;
-    const bool has_zlo = z0 > 0, has_zhi = z0 + ZC < d.nz;
-    const uint32_t oym = has_ym ? hx : 0u, oyp = has_yp ? hx : 0u;
-    const bool has_e0 = k0 > 0, has_e1 = k0 + 4 < hx;
-    const uint32_t ke0 = has_e0 ? k0 - 1 : k0, ke1 = has_e1 ? k0 + 4 : k0 + 3;
-    const float wym = has_ym ? 1.0f : 0.0f, wyp = has_yp ? 1.0f : 0.0f;
-    const int p0 = (y + z0 + color) & 1;
-    const bool df = plo != nullptr;
-    const float4 zero4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    auto ld4f = [](const float* a) { return *reinterpret_cast<const float4*>(a); };
-    const uint32_t rzlo = has_zlo ? r0 - sz : r0, rzhi = has_zhi ? r0 + ZC * sz : r0 + (ZC - 1) * sz;
-    float4 C[ZC + 2], L[ZC + 2];  // other colour's p and plo, planes z0 - 1 .. z0 + ZC
-    C[0] = ld4f(p + oth + rzlo);
-    L[0] = df ? ld4f(plo + oth + rzlo) : zero4;
+  for (int zc = 0; zc < zs; ++zc) {
+    const int z0 = ((blockIdx.z >> 1) * zs + zc) * ZC;
+    if (z0 >= d.nz) break;
+    if (k0 < hx && y < d.ny) {
+      const uint32_t half = (uint32_t)(d.n() >> 1);
+      const uint32_t sz = (uint32_t)d.ny * hx;
+      const uint32_t own = color ? half : 0u, oth = color ? 0u : half;
+      const uint32_t r0 = (uint32_t)z0 * sz + (uint32_t)y * hx + k0;
+      const bool has_ym = y > 0, has_yp = y < d.ny - 1;
+      const bool has_zlo = z0 > 0, has_zhi = z0 + ZC < d.nz;
+      const uint32_t oym = has_ym ? hx : 0u, oyp = has_yp ? hx : 0u;
+      const bool has_e0 = k0 > 0, has_e1 = k0 + 4 < hx;
+      const uint32_t ke0 = has_e0 ? k0 - 1 : k0, ke1 = has_e1 ? k0 + 4 : k0 + 3;
+      const float wym = has_ym ? 1.0f : 0.0f, wyp = has_yp ? 1.0f : 0.0f;
+      const int p0 = (y + z0 + color) & 1;
+      const bool df = plo != nullptr;
+      const float4 zero4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      auto ld4f = [](const float* a) { return *reinterpret_cast<const float4*>(a); };
+      const uint32_t rzlo = has_zlo ? r0 - sz : r0, rzhi = has_zhi ? r0 + ZC * sz : r0 + (ZC - 1) * sz;
+      float4 C[ZC + 2], L[ZC + 2];  // other colour's p and plo, planes z0 - 1 .. z0 + ZC
+      C[0] = ld4f(p + oth + rzlo);
+      L[0] = df ? ld4f(plo + oth + rzlo) : zero4;
 #pragma unroll
-    for (int i = 0; i < ZC; ++i) {
-      C[i + 1] = ld4f(p + oth + r0 + i * sz);
-      L[i + 1] = df ? ld4f(plo + oth + r0 + i * sz) : zero4;
-    }
-    C[ZC + 1] = ld4f(p + oth + rzhi);
-    L[ZC + 1] = df ? ld4f(plo + oth + rzhi) : zero4;
-#pragma unroll
-    for (int i = 0; i < ZC; ++i) {
-      const uint32_t r = r0 + i * sz;
-      const int par = p0 ^ (i & 1);
-      const float4 pc = ld4f(p + own + r), bv = ld4f(b + own + r);
-      const float4 lc = df ? ld4f(plo + own + r) : zero4;
-      const float4 ym = ld4f(p + oth + r - oym), yp = ld4f(p + oth + r + oyp);
-      const float4 lym = df ? ld4f(plo + oth + r - oym) : zero4, lyp = df ? ld4f(plo + oth + r + oyp) : zero4;
-      const uint32_t kex = r - k0 + (par == 0 ? ke0 : ke1);
-      const float ex = p[oth + kex], lex = df ? plo[oth + kex] : 0.0f;
-      const float wex = (par == 0 ? has_e0 : has_e1) ? 1.0f : 0.0f;
-      const float wzm = (i > 0 || has_zlo) ? 1.0f : 0.0f;
-      const float wzp = (i < ZC - 1 || has_zhi) ? 1.0f : 0.0f;
-      const float4 cm = C[i + 1], zm = C[i], zp = C[i + 2];
-      const float4 lcm = L[i + 1], lzm = L[i], lzp = L[i + 2];
-      float res[4];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const float xm = par == 0 ? (j == 0 ? ex : f4get(cm, j - 1)) : f4get(cm, j);
-        const float xp = par == 0 ? f4get(cm, j) : (j == 3 ? ex : f4get(cm, j + 1));
-        const float lxm = par == 0 ? (j == 0 ? lex : f4get(lcm, j - 1)) : f4get(lcm, j);
-        const float lxp = par == 0 ? f4get(lcm, j) : (j == 3 ? lex : f4get(lcm, j + 1));
-        const float wxm = (par == 0 && j == 0) ? wex : 1.0f;
-        const float wxp = (par == 1 && j == 3) ? wex : 1.0f;
-        // neighbour order x-, x+, y-, y+, z-, z+ as k_defect_df
-        const float nv[6] = {wxm * xm, wxp * xp, wym * f4get(ym, j), wyp * f4get(yp, j), wzm * f4get(zm, j),
-                             wzp * f4get(zp, j)};
-        const float nl[6] = {wxm * lxm, wxp * lxp, wym * f4get(lym, j), wyp * f4get(lyp, j), wzm * f4get(lzm, j),
-                             wzp * f4get(lzp, j)};
-        float sh = 0.0f, sl = 0.0f, low = 0.0f;
-#pragma unroll
-        for (int k = 0; k < 6; ++k) {
-          float e;
-          two_sum(sh, nv[k], sh, e);
-          sl += e;
-          low += nl[k];
-        }
-        const float diag = (ref ? 1.0f : 0.0f) + wxm + wxp + wym + (ref ? 0.0f : wyp) + wzm + wzp;
-        const float pcj = f4get(pc, j);
-        const float prod = diag * pcj;
-        const float perr = fmaf(diag, pcj, -prod);
-        float th, te;
-        two_sum(sh, -prod, th, te);
-        const float tl = ((te + sl) - perr) + (df ? fmaf(-diag, f4get(lc, j), low) : low);
-        const float rv = (f4get(bv, j) - th) - tl;
-        res[j] = rv;
-        rr = fmaf(rv, rv, rr);
-        ra = fmaxf(ra, fabsf(rv));
+      for (int i = 0; i < ZC; ++i) {
+        C[i + 1] = ld4f(p + oth + r0 + i * sz);
+        L[i + 1] = df ? ld4f(plo + oth + r0 + i * sz) : zero4;
       }
-      if (r_out) *reinterpret_cast<float4*>(r_out + own + r) = make_float4(res[0], res[1], res[2], res[3]);
+      C[ZC + 1] = ld4f(p + oth + rzhi);
+      L[ZC + 1] = df ? ld4f(plo + oth + rzhi) : zero4;
+#pragma unroll
+      for (int i = 0; i < ZC; ++i) {
+        const uint32_t r = r0 + i * sz;
+        const int par = p0 ^ (i & 1);
+        const float4 pc = ld4f(p + own + r), bv = ld4f(b + own + r);
+        const float4 lc = df ? ld4f(plo + own + r) : zero4;
+        const float4 ym = ld4f(p + oth + r - oym), yp = ld4f(p + oth + r + oyp);
+        const float4 lym = df ? ld4f(plo + oth + r - oym) : zero4, lyp = df ? ld4f(plo + oth + r + oyp) : zero4;
+        const uint32_t kex = r - k0 + (par == 0 ? ke0 : ke1);
+        const float ex = p[oth + kex], lex = df ? plo[oth + kex] : 0.0f;
+        const float wex = (par == 0 ? has_e0 : has_e1) ? 1.0f : 0.0f;
+        const float wzm = (i > 0 || has_zlo) ? 1.0f : 0.0f;
+        const float wzp = (i < ZC - 1 || has_zhi) ? 1.0f : 0.0f;
+        const float4 cm = C[i + 1], zm = C[i], zp = C[i + 2];
+        const float4 lcm = L[i + 1], lzm = L[i], lzp = L[i + 2];
+        float res[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const float xm = par == 0 ? (j == 0 ? ex : f4get(cm, j - 1)) : f4get(cm, j);
+          const float xp = par == 0 ? f4get(cm, j) : (j == 3 ? ex : f4get(cm, j + 1));
+          const float lxm = par == 0 ? (j == 0 ? lex : f4get(lcm, j - 1)) : f4get(lcm, j);
+          const float lxp = par == 0 ? f4get(lcm, j) : (j == 3 ? lex : f4get(lcm, j + 1));
+          const float wxm = (par == 0 && j == 0) ? wex : 1.0f;
+          const float wxp = (par == 1 && j == 3) ? wex : 1.0f;
+          // neighbour order x-, x+, y-, y+, z-, z+ as k_defect_df
+          const float nv[6] = {wxm * xm, wxp * xp, wym * f4get(ym, j), wyp * f4get(yp, j), wzm * f4get(zm, j),
+                               wzp * f4get(zp, j)};
+          const float nl[6] = {wxm * lxm, wxp * lxp, wym * f4get(lym, j), wyp * f4get(lyp, j), wzm * f4get(lzm, j),
+                               wzp * f4get(lzp, j)};
+          float sh = 0.0f, sl = 0.0f, low = 0.0f;
+#pragma unroll
+          for (int k = 0; k < 6; ++k) {
+            float e;
+            two_sum(sh, nv[k], sh, e);
+            sl += e;
+            low += nl[k];
+          }
+          const float diag = (ref ? 1.0f : 0.0f) + wxm + wxp + wym + (ref ? 0.0f : wyp) + wzm + wzp;
+          const float pcj = f4get(pc, j);
+          const float prod = diag * pcj;
+          const float perr = fmaf(diag, pcj, -prod);
+          float th, te;
+          two_sum(sh, -prod, th, te);
+          const float tl = ((te + sl) - perr) + (df ? fmaf(-diag, f4get(lc, j), low) : low);
+          const float rv = (f4get(bv, j) - th) - tl;
+          res[j] = rv;
+          rr = fmaf(rv, rv, rr);
+          ra = fmaxf(ra, fabsf(rv));
+        }
+        if (r_out) *reinterpret_cast<float4*>(r_out + own + r) = make_float4(res[0], res[1], res[2], res[3]);
+      }
     }
   }
   if (norm2) block_sum_atomic_f(rr, norm2);
@@ -1284,6 +1291,7 @@ double smoother_pass(const DevState& s, cudaStream_t st) {
 
 // r = b - A (p + plo) on the finest grid, ||r||^2 and max |r|: the vector
 // kernel on rows with nx % 8 == 0, else one thread per cell.
+constexpr int kDefectPlanes = 4;
 static void defect(const DevState& s, float* r_out, double* norm2, unsigned int* maxbits, const unsigned int* skip,
                    cudaStream_t st) {
   const Grid& d = s.g;
@@ -1291,12 +1299,14 @@ static void defect(const DevState& s, float* r_out, double* norm2, unsigned int*
     k_defect_df<<<g_cells(d), b_cells(), 0, st>>>(d, s.ref, s.p, s.plo, s.rhs, r_out, norm2, maxbits, skip);
     return;
   }
-  // one plane per thread: 61 us at 192x256x192 against 69 us with two
-  // (100 registers) and 144 us for one thread per cell
+  // one plane per thread: 57 us at 192x256x192 against 69 us with two
+  // (100 registers) and 144 us for one thread per cell; a block walking
+  // kDefectPlanes planes (one reduction per block): 51 us
   const dim3 bq = quad_block(d);
   dim3 gq = quad_grid(d, bq);
-  gq.z = 2 * d.nz;
-  launch_pdl(k_defect_df4<1>, gq, bq, 0, st, d, s.ref, s.p, s.plo, s.rhs, r_out, norm2, maxbits, skip);
+  gq.z = 2 * ((d.nz + kDefectPlanes - 1) / kDefectPlanes);
+  launch_pdl(k_defect_df4<1>, gq, bq, 0, st, d, s.ref, s.p, s.plo, s.rhs, r_out, norm2, maxbits, skip,
+             (int)kDefectPlanes);
 }
 
 void launch_residual_norm(const DevState& s, double* out, cudaStream_t st) {
