@@ -899,9 +899,10 @@ def main():
     ap.add_argument("--profile-run", action="store_true",
                     help="run only the FP32 scene (warm-up + steps, untimed) and exit: the command "
                          "the ncu launch lists and kernel captures are taken with")
-    ap.add_argument("--profile-scene", choices=["box192", "box96"], default="box192",
-                    help="scene of --profile-run: box192 (the headline workload) or box96 (96x128x96, "
-                         "the small case for full-metric kernel captures)")
+    ap.add_argument("--profile-scene", choices=["box192", "box96", "box192_mixed"], default="box192",
+                    help="scene of --profile-run: box192 (the headline workload), box96 (96x128x96, "
+                         "the small case for full-metric kernel captures) or box192_mixed (box192 with "
+                         "FP16 dye and the mixed pressure solve)")
     args = ap.parse_args()
     rank, world, local = rank_info()
     if args.impl == "reference":
@@ -936,7 +937,12 @@ def main():
     dist = Dist(world)
 
     # ---- FP32 drop-in step (the headline) ----------------------------------------------------
-    sc = scenes.box96() if (args.profile_run and args.profile_scene == "box96") else scenes.box192()
+    if args.profile_run and args.profile_scene == "box96":
+        sc = scenes.box96()
+    elif args.profile_run and args.profile_scene == "box192_mixed":
+        sc = scenes.box192(abi.DOB_PREC_MIXED)
+    else:
+        sc = scenes.box192()
     eng = DropFluid(sc.config)
     run_scene_steps(sc, eng, 0, args.warmup, timed=False)
     eng.sync()
