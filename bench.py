@@ -156,10 +156,11 @@ def ncu_traffic():
         return None
 
 
-def run_scene_steps(scene, eng, start, n, timed):
+def run_scene_steps(scene, eng, start, n, timed, graph=True):
     """Advance n steps from `start`, releasing drops on schedule.  Returns
     the device milliseconds of the step segments when `timed` (releases are
-    host calls between segments and are not timed)."""
+    host calls between segments and are not timed).  graph=False (untimed
+    only) launches the steps kernel by kernel instead of replaying a graph."""
     total = 0.0
     k = start
     end = start + n
@@ -174,7 +175,7 @@ def run_scene_steps(scene, eng, start, n, timed):
         if timed:
             total += eng.time_steps(seg)
         else:
-            eng.step(seg)
+            eng.step(seg, graph=graph)
         k = nxt
     return total
 
@@ -903,6 +904,9 @@ def main():
                     help="scene of --profile-run: box192 (the headline workload), box96 (96x128x96, "
                          "the small case for full-metric kernel captures) or box192_mixed (box192 with "
                          "FP16 dye and the mixed pressure solve)")
+    ap.add_argument("--profile-no-graph", action="store_true",
+                    help="with --profile-run: launch the steps kernel by kernel, not as graph replays (ncu "
+                         "profiles no kernel of a graph that holds conditional nodes, as the mixed step's does)")
     args = ap.parse_args()
     rank, world, local = rank_info()
     if args.impl == "reference":
@@ -944,10 +948,11 @@ def main():
     else:
         sc = scenes.box192()
     eng = DropFluid(sc.config)
-    run_scene_steps(sc, eng, 0, args.warmup, timed=False)
+    graph = not (args.profile_run and args.profile_no_graph)
+    run_scene_steps(sc, eng, 0, args.warmup, timed=False, graph=graph)
     eng.sync()
     if args.profile_run:
-        run_scene_steps(sc, eng, args.warmup, args.steps, timed=False)
+        run_scene_steps(sc, eng, args.warmup, args.steps, timed=False, graph=graph)
         eng.sync()
         return 0
     clocks = ClockSampler()
